@@ -1,0 +1,104 @@
+"""ctypes binding of libffs.so (the C ABI declared in include/ffs.h)."""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_void_p
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libffs.so"
+
+FFS_OK = 0
+ERRORS = {-1: "FFS_EINVAL", -2: "FFS_ENOMEM", -3: "FFS_ECUDA", -4: "FFS_ENAN", -5: "FFS_ETIMEDOUT",
+          -6: "FFS_EUNSUPPORTED", -7: "FFS_ESTATE"}
+FFS_ETD3, FFS_AB3 = 0, 1
+FFS_FP64, FFS_FP32 = 0, 1
+
+# Every symbol include/ffs.h declares (checked by the CPU test suite).
+EXPORTS = [
+    "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_get_fields",
+    "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
+    "ffs_stats_records", "ffs_spectrum_lengths", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
+    "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_stream",
+    "ffs_last_error", "ffs_destroy",
+]
+
+
+class FFSParams(ctypes.Structure):
+    """Mirror of ``ffs_params`` (include/ffs.h)."""
+
+    _fields_ = [
+        ("nx", c_int32), ("ny", c_int32), ("nz", c_int32),
+        ("lx", c_double), ("ly", c_double), ("lz", c_double),
+        ("nu", c_double), ("cutoff", c_double),
+        ("integrator", c_int32), ("variable_dt", c_int32),
+        ("cfl", c_double), ("dt", c_double),
+        ("hyperviscosity", c_int32), ("hv_nu", c_double), ("hv_m", c_int32),
+        ("les", c_int32), ("smag_c", c_double), ("filter_width", c_double),
+        ("density", c_int32), ("density_pr", c_double), ("density_gradient", c_double), ("gravity", c_double),
+        ("gravity_dir", c_int32),
+        ("forcing", c_int32), ("forcing_power", c_double), ("forcing_kf", c_double),
+        ("precision", c_int32), ("dt_stat", c_int32), ("dt_spec", c_int32), ("write_time", c_int32),
+        ("start", c_int64), ("start_time", c_double),
+        ("device", c_int32), ("reference_cfl_slot", c_int32),
+        ("stats_capacity", c_int32), ("spec_capacity", c_int32),
+    ]
+
+
+_lib = None
+
+
+def lib_available() -> bool:
+    return LIB_PATH.exists()
+
+
+def load() -> ctypes.CDLL:
+    """Load libffs.so; raise loudly if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA engine first (python {HERE / 'build.py'})")
+    L = ctypes.CDLL(str(LIB_PATH), mode=os.RTLD_LOCAL if hasattr(os, "RTLD_LOCAL") else 0)
+    P = POINTER(FFSParams)
+    H = c_void_p
+    D = POINTER(c_double)
+    sig = {
+        "ffs_params_default": (c_int32, [P]),
+        "ffs_create": (c_int32, [P, POINTER(c_void_p)]),
+        "ffs_set_fields": (c_int32, [H, D, D, D, D, c_int32]),
+        "ffs_initialize": (c_int32, [H]),
+        "ffs_step": (c_int32, [H, c_int64]),
+        "ffs_get_fields": (c_int32, [H, D, D, D, D, c_int32]),
+        "ffs_get_spectral": (c_int32, [H, c_int32, D]),
+        "ffs_set_spectral": (c_int32, [H, c_int32, D]),
+        "ffs_stats_header": (c_int32, [H, c_char_p, c_int64]),
+        "ffs_stats_ncols": (c_int32, [H]),
+        "ffs_record_ncols": (c_int32, [H]),
+        "ffs_stats_records": (c_int64, [H, D, c_int64]),
+        "ffs_spectrum_lengths": (c_int32, [H, POINTER(c_int32), POINTER(c_int32)]),
+        "ffs_spectrum_records": (c_int64, [H, D, c_int64]),
+        "ffs_iteration": (c_int64, [H]),
+        "ffs_time": (c_double, [H]),
+        "ffs_dt": (c_double, [H]),
+        "ffs_time_steps": (c_int32, [H, c_int64, D]),
+        "ffs_profile_kernels": (c_int32, [H, c_int64, c_char_p, c_int64, D, c_int32, POINTER(c_int32)]),
+        "ffs_launches_per_step": (c_int32, [H]),
+        "ffs_device_bytes": (c_int64, [H]),
+        "ffs_stream": (c_void_p, [H]),
+        "ffs_last_error": (c_char_p, [H]),
+        "ffs_destroy": (None, [H]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+class FFSError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code

@@ -1,0 +1,647 @@
+// Host side of the engine for one arithmetic type: buffers, launch geometry, the
+// CUDA-graph step, set/get of fields and records.
+#pragma once
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "ffs_engine.h"
+#include "ffs_kernels.cuh"
+
+namespace ffsgpu {
+
+#define FFS_CK(call)                                                                     \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess) {                                                             \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);                          \
+      return FFS_ECUDA;                                                                  \
+    }                                                                                    \
+  } while (0)
+
+// Radix plans (product == n), largest radix first; radix-3 last.
+inline bool make_plan(int n, FftPlan& P) {
+  int r[4] = {0, 0, 0, 0}, np = 0;
+  switch (n) {
+    case 8: r[0] = 8; np = 1; break;
+    case 16: r[0] = 16; np = 1; break;
+    case 32: r[0] = 8; r[1] = 4; np = 2; break;
+    case 48: r[0] = 4; r[1] = 4; r[2] = 3; np = 3; break;
+    case 64: r[0] = 8; r[1] = 8; np = 2; break;
+    case 96: r[0] = 8; r[1] = 4; r[2] = 3; np = 3; break;
+    case 128: r[0] = 16; r[1] = 8; np = 2; break;
+    case 192: r[0] = 8; r[1] = 8; r[2] = 3; np = 3; break;
+    case 256: r[0] = 16; r[1] = 16; np = 2; break;
+    case 384: r[0] = 16; r[1] = 8; r[2] = 3; np = 3; break;
+    case 512: r[0] = 8; r[1] = 8; r[2] = 8; np = 3; break;
+    case 768: r[0] = 16; r[1] = 16; r[2] = 3; np = 3; break;
+    case 1024: r[0] = 16; r[1] = 8; r[2] = 8; np = 3; break;
+    default: return false;
+  }
+  P.n = n; P.np = np;
+  int mx = 0;
+  for (int i = 0; i < 4; ++i) { P.r[i] = r[i]; mx = std::max(mx, r[i]); }
+  P.tpl = n / mx;
+  return true;
+}
+
+inline int round32(int x) { return ((x + 31) / 32) * 32; }
+
+template <typename T>
+class Engine : public EngineBase {
+ public:
+  static constexpr int TX = sizeof(T) == 4 ? 8 : 4;   // kx lines per CTA in the y/z passes
+  Inst<T> I;
+  ffs_params P;
+  cudaStream_t s = nullptr;
+  std::vector<void*> allocs;
+  int64_t bytes = 0;
+  FieldList inv_list{}, fwd_list{};
+  int nin = 0, nout = 0;
+  int lyz = 4;
+  int txz = TX;               // kx lines per CTA in the forward z pass
+  int nparts = 0;
+  size_t smem_z = 0, smem_y = 0, smem_x = 0, smem_zu = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int n_launch = 0;
+
+  ~Engine() override {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (void* p : allocs) cudaFree(p);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  template <typename U> int alloc(U** p, size_t count, std::string& err) {
+    void* q = nullptr;
+    size_t b = count * sizeof(U);
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&q, b);
+    if (e != cudaSuccess) {
+      err = std::string("cudaMalloc of ") + std::to_string(b) + " bytes: " + cudaGetErrorString(e);
+      return e == cudaErrorMemoryAllocation ? FFS_ENOMEM : FFS_ECUDA;
+    }
+    allocs.push_back(q);
+    bytes += (int64_t)b;
+    *p = reinterpret_cast<U*>(q);
+    FFS_CK(cudaMemsetAsync(q, 0, b, s));
+    return 0;
+  }
+
+  // retained-range counts for one axis (Globals.jl:132-142, 163-169)
+  static void retained(int n, double L, double cutoffr, bool half, int& pos, int& cnt) {
+    // k values exactly as rfftfreq / fftfreq compute them
+    std::vector<double> k;
+    if (half) { for (int i = 0; i <= n / 2; ++i) k.push_back(((double)n / 2 - ((double)n / 2 - i)) / L); }
+    else {
+      for (int i = 0; i < n / 2; ++i) k.push_back(((double)n / 2 - ((double)n / 2 - i)) / L);
+      for (int i = n / 2; i >= 1; --i) k.push_back(-(double)i / L);
+    }
+    double kmax = 0.0;
+    if (half) kmax = k.back();
+    else for (double v : k) kmax = std::max(kmax, fabs(v));
+    const double c = (cutoffr * kmax) * (cutoffr * kmax);
+    pos = 0;
+    while (pos < (int)k.size() && !(k[pos] * k[pos] > c) && (half || pos < n / 2)) ++pos;
+    if (half) { cnt = pos; return; }
+    int neg = 0;
+    while (neg < n / 2 && !(k[n - 1 - neg] * k[n - 1 - neg] > c)) ++neg;
+    cnt = pos + neg;
+  }
+
+  int create(const ffs_params& p, std::string& err) override {
+    P = p;
+    memset(&I, 0, sizeof(I));
+    if (p.nx <= 0 || p.ny <= 0 || p.nz <= 0) { err = "grid sizes must be positive"; return FFS_EINVAL; }
+    if (!make_plan(p.nx, I.px) || !make_plan(p.ny, I.py) || !make_plan(p.nz, I.pz)) {
+      err = "unsupported grid size: each of nx, ny, nz must be one of 8,16,32,48,64,96,128,192,256,384,512,768,1024";
+      return FFS_EUNSUPPORTED;
+    }
+    if (!(p.lx > 0 && p.ly > 0 && p.lz > 0)) { err = "domain sizes must be positive"; return FFS_EINVAL; }
+    if (!(p.cutoff > 0 && p.cutoff <= 1.0)) { err = "cutoff must be in (0, 1]"; return FFS_EINVAL; }
+    if (p.dt_stat <= 0 || p.dt_spec <= 0) { err = "dtStat and dtSpec must be positive"; return FFS_EINVAL; }
+    if (p.integrator != FFS_ETD3 && p.integrator != FFS_AB3) { err = "unknown integrator"; return FFS_EINVAL; }
+    if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
+    if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
+    if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
+    FFS_CK(cudaSetDevice(p.device));
+    FFS_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+
+    I.nx = p.nx; I.ny = p.ny; I.nz = p.nz; I.nxh = p.nx / 2 + 1;
+    I.lx = p.lx; I.ly = p.ly; I.lz = p.lz;
+    I.inv_n = 1.0 / ((double)p.nx * (double)p.ny * (double)p.nz);
+    int xp, xc, yp, yc, zp, zc;
+    retained(p.nx, p.lx, p.cutoff, true, xp, xc);
+    retained(p.ny, p.ly, p.cutoff, false, yp, yc);
+    retained(p.nz, p.lz, p.cutoff, false, zp, zc);
+    I.Mx = xc; I.KXP = ((xc + 7) / 8) * 8;
+    I.ypos = yp; I.NYR = yc; I.zpos = zp; I.NZR = zc;
+    I.uniformL = (p.lx == p.ly && p.ly == p.lz);
+    lyz = p.nx <= 256 ? 4 : 1;
+    if (((long long)p.ny * p.nz) % lyz != 0 || ((long long)p.ny * p.nz) % LYZ_IO != 0) {
+      err = "ny*nz must be a multiple of 4"; return FFS_EUNSUPPORTED;
+    }
+    txz = TX;
+    if (p.nz > 512) txz = TX / 2;
+
+    // physics
+    I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
+    I.ab3 = p.integrator == FFS_AB3; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
+    I.hv = p.hyperviscosity != 0; I.hv_m = p.hv_m; I.hv_nu = p.hv_nu;
+    I.les = p.les != 0;
+    const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
+    I.les_alpha = p.smag_c * p.smag_c * fw * fw;
+    I.density = p.density != 0; I.gdir = p.gravity_dir;
+    I.alpha = p.density ? p.nu / p.density_pr : 0.0;
+    I.dgrad = p.density_gradient; I.gval = p.gravity;
+    I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
+    I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
+
+    // field lists
+    nin = 0;
+    for (int c = F_UX; c <= F_WZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
+    if (I.les) for (int c = F_SXX; c <= F_SYZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
+    if (I.density) { inv_list.code[nin] = F_RHO; inv_list.slot[nin] = nin; ++nin; }
+    inv_list.n = nin;
+    nout = 0;
+    auto addo = [&](int role, int slot) { fwd_list.code[nout] = role; fwd_list.slot[nout] = slot; ++nout; };
+    addo(R_NX, 0); addo(R_NY, 1); addo(R_NZ, 2); addo(R_KE, 3);
+    if (I.les) { addo(R_TXX, 6); addo(R_TXY, 7); addo(R_TXZ, 8); addo(R_TYY, 9); addo(R_TYZ, 10); }
+    if (I.density) { addo(R_FX, 4); addo(R_FY, 5); addo(R_FZ, nin - 1); }
+    fwd_list.n = nout;
+    I.nin = nin; I.nout = nout;
+    for (int i = 0; i < nout; ++i) { I.out_role[i] = fwd_list.code[i]; I.out_slot[i] = fwd_list.slot[i]; }
+    for (int i = 0; i < nin; ++i) I.in_code[i] = inv_list.code[i];
+    const int nslots = std::max(nin, 4);
+
+    // buffers
+    int rc;
+    I.ncomp = I.density ? 4 : 3;
+    I.cstride = (long long)I.NZR * I.NYR * I.KXP;
+    I.wzs = (long long)p.nz * I.NYR * I.KXP;
+    I.wys = (long long)p.nz * p.ny * I.KXP;
+    cplx<T>* tw[3];
+    int ns[3] = {p.nx, p.ny, p.nz};
+    for (int a = 0; a < 3; ++a) {
+      if ((rc = alloc(&tw[a], ns[a], err))) return rc;
+      std::vector<cplx<T>> h(ns[a]);
+      for (int t = 0; t < ns[a]; ++t) {
+        // exp(-2 pi i t / n) from the FP64 angle, exact at multiples of pi/4
+        const double ang = -2.0 * M_PI * (double)t / ns[a];
+        double c = cos(ang), sn = sin(ang);
+        if ((8 * t) % ns[a] == 0) {
+          const int o = (8 * t) / ns[a];
+          const double r = sqrt(0.5);
+          const double cs8[8] = {1, r, 0, -r, -1, -r, 0, r};
+          c = cs8[o]; sn = -cs8[(o + 6) % 8];
+        }
+        h[t].x = (T)c; h[t].y = (T)sn;
+      }
+      FFS_CK(cudaMemcpyAsync(tw[a], h.data(), ns[a] * sizeof(cplx<T>), cudaMemcpyHostToDevice, s));
+      FFS_CK(cudaStreamSynchronize(s));
+    }
+    I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
+    if ((rc = alloc(&I.uh, (size_t)I.ncomp * I.cstride, err))) return rc;
+    if ((rc = alloc(&I.hist, (size_t)2 * I.ncomp * I.cstride, err))) return rc;
+    if ((rc = alloc(&I.wz, (size_t)nslots * I.wzs, err))) return rc;
+    if ((rc = alloc(&I.wy, (size_t)nslots * I.wys, err))) return rc;
+    if ((rc = alloc(&I.st, 1, err))) return rc;
+    nparts = (I.KXP / txz) * I.NYR;
+    if ((rc = alloc(&I.partials, (size_t)nparts * QPAD, err))) return rc;
+    // record layout
+    ncols_stats = 22 + (I.density ? 8 : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
+    ncols_rec = ncols_stats + 13;
+    I.ncols = ncols_rec;
+    I.rec_cap = p.stats_capacity > 0 ? p.stats_capacity : 256;
+    if ((rc = alloc(&I.records, (size_t)I.rec_cap * I.ncols, err))) return rc;
+    // spectrum bins (Globals.jl:144-152)
+    const double kx1 = 1.0 / p.lx, ky1 = 1.0 / p.ly;
+    lenH = kx1 >= ky1 ? p.nx / 2 + 1 : p.ny / 2 + 1;
+    I.maxdkh = kx1 >= ky1 ? kx1 : ky1;
+    lenV = p.nz / 2 + 1;
+    I.dkz = 1.0 / p.lz;
+    I.nbinH = lenH; I.nbinV = lenV;
+    I.spec_cap = p.spec_capacity > 0 ? p.spec_capacity : 16;
+    if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 4 * std::max(lenH, lenV), err))) return rc;
+    // ETD tables
+    if (!I.ab3 && I.uniformL) {
+      const long long a = I.Mx - 1, b = std::max(I.ypos - 1, I.NYR - I.ypos), c = std::max(I.zpos - 1, I.NZR - I.zpos);
+      I.qmax = (int)(a * a + b * b + c * c);
+      if ((rc = alloc(&I.etab, (size_t)4 * (I.qmax + 1), err))) return rc;
+      if (I.density && (rc = alloc(&I.etab_rho, (size_t)4 * (I.qmax + 1), err))) return rc;
+    }
+    // staging for two physical FP64 fields
+    if ((rc = alloc(&I.phys, (size_t)2 * p.nx * p.ny * p.nz, err))) return rc;
+
+    // launch geometry / shared memory
+    const size_t cb = sizeof(cplx<T>);
+    smem_z = (size_t)TX * p.nz * cb * (I.pz.np >= 3 ? 2 : 1);
+    smem_y = (size_t)TX * p.ny * cb * (I.py.np >= 3 ? 2 : 1);
+    {
+      const int PIN = (nin + 1) / 2;
+      const int LIN = PIN * lyz;
+      const int MXP = I.Mx | 1;
+      smem_x = cb * ((size_t)nin * lyz * MXP + (size_t)p.nx * (LIN + 1) + (size_t)p.nx * LIN * (I.px.np >= 3 ? 2 : 1));
+    }
+    smem_zu = cb * ((size_t)txz * p.nz * (I.pz.np >= 3 ? 2 : 1) + (size_t)(4 + ((I.les || I.density) ? 4 : 0)) * I.NZR * txz);
+    if ((rc = set_smem(err))) return rc;
+
+    // state and header
+    if ((rc = reset_state(err))) return rc;
+    header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
+    if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
+    if (I.les) header += ",prh,prv,praniso,pr";
+    if (I.forcing) header += ",hp,vp,tp";
+    if (I.hv) header += ",hdissh,hdissv,hdiss";
+    FFS_CK(cudaStreamSynchronize(s));
+    return 0;
+  }
+
+  template <typename K> int smem_attr(K kern, size_t bytes_, std::string& err) {
+    if (bytes_ > 48 * 1024) FFS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes_));
+    return 0;
+  }
+
+  int set_smem(std::string& err) {
+    int dev = P.device, maxs = 0;
+    FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    size_t need[4] = {smem_z, smem_y, smem_x, smem_zu};
+    for (size_t v : need)
+      if (v > (size_t)maxs) {
+        err = "shared memory per CTA (" + std::to_string(v) + " bytes) exceeds the device limit " + std::to_string(maxs);
+        return FFS_EUNSUPPORTED;
+      }
+    int rc;
+    if ((rc = smem_attr(k_inv_z<T, TX>, smem_z, err))) return rc;
+    if ((rc = smem_attr(k_inv_y<T, TX>, smem_y, err))) return rc;
+    if ((rc = smem_attr(k_fwd_y<T, TX>, smem_y, err))) return rc;
+    if ((rc = smem_attr(k_fwd_z_store<T, TX>, smem_z, err))) return rc;
+    if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
+    if (txz == TX) { if ((rc = smem_attr(k_fwd_z_update<T, TX>, smem_zu, err))) return rc; }
+    else { if ((rc = smem_attr(k_fwd_z_update<T, TX / 2>, smem_zu, err))) return rc; }
+    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    if ((rc = smem_attr(k_phys_fwd_x<T>, io, err))) return rc;
+    if ((rc = smem_attr(k_inv_x_phys<T>, io, err))) return rc;
+    return 0;
+  }
+
+  using XK = void (*)(Inst<T>);
+  XK xpass_ptr() const {
+    const bool L = I.les, D = I.density;
+    if (lyz == 4) {
+      if (L && D) return k_x_pass<T, true, true, 4>;
+      if (L) return k_x_pass<T, true, false, 4>;
+      if (D) return k_x_pass<T, false, true, 4>;
+      return k_x_pass<T, false, false, 4>;
+    }
+    if (L && D) return k_x_pass<T, true, true, 1>;
+    if (L) return k_x_pass<T, true, false, 1>;
+    if (D) return k_x_pass<T, false, true, 1>;
+    return k_x_pass<T, false, false, 1>;
+  }
+
+  int reset_state(std::string& err) {
+    DevState h;
+    memset(&h, 0, sizeof(h));
+    h.iteration = P.start;
+    h.time = P.start_time;
+    h.dt = h.dt2 = h.dt3 = P.dt;
+    h.nl_h = h.nl_v = h.press_h = h.press_v = 1.0;   // simulationtypes.jl:94-95
+    FFS_CK(cudaMemcpyAsync(I.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    iteration = h.iteration; time = h.time; dt = h.dt;
+    return 0;
+  }
+
+  // ---------------------------------------------------------------- launches
+  dim3 blk(int lines, const FftPlan& pl) const { return dim3(round32(lines * pl.tpl)); }
+
+  void launch_inv_z(const FieldList& F) {
+    k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+  }
+  void launch_inv_y(const FieldList& F) {
+    k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+  }
+  void launch_fwd_y(const FieldList& F) {
+    k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+  }
+  void launch_x() {
+    const int PIN = (nin + 1) / 2;
+    xpass_ptr()<<<dim3(I.ny * I.nz / lyz), blk(PIN * lyz, I.px), smem_x, s>>>(I);
+  }
+  void launch_scalar(int mode) { k_scalar<T><<<1, 256, 0, s>>>(I, mode); }
+  bool use_table() const { return !I.ab3 && I.uniformL; }
+  void launch_table(int mode) {
+    if (!use_table()) return;
+    const int nb = std::min(1024, (I.qmax + 1 + 255) / 256);
+    k_etd_table<T><<<nb, 256, 0, s>>>(I, mode);
+  }
+  void launch_zu(int mode) {
+    if (txz == TX)
+      k_fwd_z_update<T, TX><<<dim3(I.KXP / TX, I.NYR), blk(TX, I.pz), smem_zu, s>>>(I, fwd_list, mode);
+    else
+      k_fwd_z_update<T, TX / 2><<<dim3(I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_zu, s>>>(I, fwd_list, mode);
+  }
+  void launch_fin(int mode) { k_finalize<T><<<1, 1024, 0, s>>>(I, mode, nparts); }
+
+  void enqueue_step(int mode) {
+    launch_inv_z(inv_list);
+    launch_inv_y(inv_list);
+    launch_x();
+    launch_fwd_y(fwd_list);
+    launch_scalar(mode);
+    launch_table(mode);
+    launch_zu(mode);
+    launch_fin(mode);
+  }
+  int launches_per_step() const override { return 7 + (use_table() ? 1 : 0); }
+
+  // ---------------------------------------------------------------- fields
+  void repack_in(const double* src, double* dst, int layout) const {
+    const long long nx = P.nx, ny = P.ny, nz = P.nz;
+    if (layout == 0) { memcpy(dst, src, sizeof(double) * nx * ny * nz); return; }
+    const long long rx = 2 * (nx / 2 + 1);
+    for (long long r = 0; r < ny * nz; ++r) memcpy(dst + r * nx, src + r * rx, sizeof(double) * nx);
+  }
+  void repack_out(const double* src, double* dst, int layout) const {
+    const long long nx = P.nx, ny = P.ny, nz = P.nz;
+    if (layout == 0) { memcpy(dst, src, sizeof(double) * nx * ny * nz); return; }
+    const long long rx = 2 * (nx / 2 + 1);
+    for (long long r = 0; r < ny * nz; ++r) {
+      memcpy(dst + r * rx, src + r * nx, sizeof(double) * nx);
+      for (long long i = nx; i < rx; ++i) dst[r * rx + i] = 0.0;
+    }
+  }
+
+  int set_fields(const double* u1, const double* u2, const double* u3, const double* rho, int layout,
+                 std::string& err) override {
+    if (!u1 || !u2 || !u3) { err = "velocity pointers must not be NULL"; return FFS_EINVAL; }
+    if (layout != 0 && layout != 1) { err = "layout must be 0 or 1"; return FFS_EINVAL; }
+    const size_t N = (size_t)P.nx * P.ny * P.nz;
+    std::vector<double> tmp(2 * N, 0.0);
+    const double* src[4] = {u1, u2, u3, rho};
+    const int nf = I.density ? 4 : 3;
+    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    for (int pair = 0; pair < 2; ++pair) {
+      const int f0 = 2 * pair;
+      const int cnt = std::min(2, nf - f0);
+      if (cnt <= 0) break;
+      for (int k = 0; k < cnt; ++k) {
+        if (src[f0 + k]) repack_in(src[f0 + k], tmp.data() + k * N, layout);
+        else std::fill(tmp.begin() + k * N, tmp.begin() + (k + 1) * N, 0.0);
+      }
+      FFS_CK(cudaMemcpyAsync(I.phys, tmp.data(), sizeof(double) * cnt * N, cudaMemcpyHostToDevice, s));
+      k_phys_fwd_x<T><<<P.ny * P.nz / LYZ_IO, blk(2 * LYZ_IO, I.px), io, s>>>(I, cnt, f0);
+      FFS_CK(cudaGetLastError());
+      FFS_CK(cudaStreamSynchronize(s));
+    }
+    FieldList F{};
+    F.n = nf;
+    for (int i = 0; i < nf; ++i) { F.code[i] = i; F.slot[i] = i; }
+    launch_fwd_y(F);
+    k_fwd_z_store<T, TX><<<dim3(nf, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    FFS_CK(cudaGetLastError());
+    int rc;
+    if ((rc = reset_state(err))) return rc;
+    FFS_CK(cudaMemsetAsync(I.hist, 0, sizeof(cplx<T>) * 2 * I.ncomp * I.cstride, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    initialized = false;
+    rec_host.clear(); spec_host.clear();
+    return 0;
+  }
+
+  int get_fields(double* u1, double* u2, double* u3, double* rho, int layout, std::string& err) override {
+    if (layout != 0 && layout != 1) { err = "layout must be 0 or 1"; return FFS_EINVAL; }
+    const size_t N = (size_t)P.nx * P.ny * P.nz;
+    double* dst[4] = {u1, u2, u3, rho};
+    const int nf = I.density ? 4 : 3;
+    FieldList F{};
+    F.n = nf;
+    const int codes[4] = {F_UX, F_UY, F_UZ, F_RHO};
+    for (int i = 0; i < nf; ++i) { F.code[i] = codes[i]; F.slot[i] = i; }
+    launch_inv_z(F);
+    launch_inv_y(F);
+    std::vector<double> tmp(2 * N);
+    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    for (int pair = 0; pair < 2; ++pair) {
+      const int f0 = 2 * pair;
+      const int cnt = std::min(2, nf - f0);
+      if (cnt <= 0) break;
+      // shift the wanted slots to 0/1 by offsetting the wy base
+      Inst<T> J = I;
+      J.wy = I.wy + (long long)f0 * I.wys;
+      k_inv_x_phys<T><<<P.ny * P.nz / LYZ_IO, blk(2 * LYZ_IO, I.px), io, s>>>(J, cnt);
+      FFS_CK(cudaGetLastError());
+      FFS_CK(cudaMemcpyAsync(tmp.data(), I.phys, sizeof(double) * cnt * N, cudaMemcpyDeviceToHost, s));
+      FFS_CK(cudaStreamSynchronize(s));
+      for (int k = 0; k < cnt; ++k)
+        if (dst[f0 + k]) repack_out(tmp.data() + k * N, dst[f0 + k], layout);
+    }
+    if (!I.density && rho) {
+      const long long rx = layout ? 2 * (P.nx / 2 + 1) : P.nx;
+      memset(rho, 0, sizeof(double) * rx * P.ny * P.nz);
+    }
+    return 0;
+  }
+
+  int get_spectral(int comp, double* out, std::string& err) override {
+    if (comp < 0 || comp >= I.ncomp) { err = "component out of range"; return FFS_EINVAL; }
+    std::vector<cplx<T>> h((size_t)I.cstride);
+    FFS_CK(cudaMemcpyAsync(h.data(), I.uh + comp * I.cstride, sizeof(cplx<T>) * I.cstride, cudaMemcpyDeviceToHost, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    const long long nxh = I.nxh;
+    memset(out, 0, sizeof(double) * 2 * nxh * P.ny * P.nz);
+    for (int kc = 0; kc < I.NZR; ++kc) {
+      const int z = kc < I.zpos ? kc : P.nz - I.NZR + kc;
+      for (int jc = 0; jc < I.NYR; ++jc) {
+        const int y = jc < I.ypos ? jc : P.ny - I.NYR + jc;
+        for (int ix = 0; ix < I.Mx; ++ix) {
+          const cplx<T> v = h[((long long)kc * I.NYR + jc) * I.KXP + ix];
+          const long long o = ((long long)z * P.ny + y) * nxh + ix;
+          out[2 * o] = (double)v.x; out[2 * o + 1] = (double)v.y;
+        }
+      }
+    }
+    return 0;
+  }
+
+  int set_spectral(int comp, const double* in, std::string& err) override {
+    if (comp < 0 || comp >= I.ncomp) { err = "component out of range"; return FFS_EINVAL; }
+    std::vector<cplx<T>> h((size_t)I.cstride);
+    memset(h.data(), 0, sizeof(cplx<T>) * h.size());
+    const long long nxh = I.nxh;
+    for (int kc = 0; kc < I.NZR; ++kc) {
+      const int z = kc < I.zpos ? kc : P.nz - I.NZR + kc;
+      for (int jc = 0; jc < I.NYR; ++jc) {
+        const int y = jc < I.ypos ? jc : P.ny - I.NYR + jc;
+        for (int ix = 0; ix < I.Mx; ++ix) {
+          const long long o = ((long long)z * P.ny + y) * nxh + ix;
+          cplx<T>& v = h[((long long)kc * I.NYR + jc) * I.KXP + ix];
+          v.x = (T)in[2 * o]; v.y = (T)in[2 * o + 1];
+        }
+      }
+    }
+    FFS_CK(cudaMemcpyAsync(I.uh + comp * I.cstride, h.data(), sizeof(cplx<T>) * I.cstride, cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    initialized = false;
+    return 0;
+  }
+
+  // ---------------------------------------------------------------- stepping
+  int initialize(std::string& err) override {
+    int rc;
+    if ((rc = reset_state(err))) return rc;
+    enqueue_step(1);
+    FFS_CK(cudaGetLastError());
+    FFS_CK(cudaStreamSynchronize(s));
+    if ((rc = pull_state(err))) return rc;
+    initialized = true;
+    return 0;
+  }
+
+  int build_graph(std::string& err) {
+    if (gexec) return 0;
+    FFS_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(0);
+    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return FFS_ECUDA; }
+    FFS_CK(cudaGraphInstantiate(&gexec, graph, 0));
+    n_launch = launches_per_step();
+    return 0;
+  }
+
+  DevState hs{};
+  int pull_state(std::string& err) {
+    FFS_CK(cudaMemcpyAsync(&hs, I.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    iteration = hs.iteration; time = hs.time; dt = hs.dt;
+    return 0;
+  }
+
+  // move device records to the host vectors
+  int drain(int64_t it_first, int64_t it_last, std::string& err) {
+    int rc;
+    if ((rc = pull_state(err))) return rc;
+    const long long nrec = std::min<long long>(hs.nrec, I.rec_cap);
+    if (hs.nrec > I.rec_cap) { err = "stats record buffer overflow"; return FFS_ESTATE; }
+    if (nrec > 0) {
+      const size_t off = rec_host.size();
+      rec_host.resize(off + (size_t)nrec * I.ncols);
+      FFS_CK(cudaMemcpyAsync(rec_host.data() + off, I.records, sizeof(double) * nrec * I.ncols, cudaMemcpyDeviceToHost, s));
+    }
+    const long long nsp = std::min<long long>(hs.nspec, I.spec_cap);
+    const int stride = std::max(lenH, lenV);
+    if (nsp > 0) {
+      std::vector<double> tmp((size_t)nsp * 4 * stride);
+      FFS_CK(cudaMemcpyAsync(tmp.data(), I.spec, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, s));
+      FFS_CK(cudaStreamSynchronize(s));
+      // iterations of the spectrum records in this chunk
+      std::vector<int64_t> its;
+      for (int64_t it = it_first; it <= it_last; ++it)
+        if (it % P.dt_spec == 0) its.push_back(it);
+      for (long long r = 0; r < nsp; ++r) {
+        spec_host.push_back(r < (long long)its.size() ? (double)its[r] : -1.0);
+        const double* rec = tmp.data() + r * 4 * stride;
+        for (int q = 0; q < 4; ++q) {
+          const int len = (q % 2 == 0) ? lenH : lenV;
+          spec_host.insert(spec_host.end(), rec + q * stride, rec + q * stride + len);
+        }
+      }
+      FFS_CK(cudaMemsetAsync(I.spec, 0, sizeof(double) * tmp.size(), s));
+    }
+    // reset the device counters
+    const long long zero = 0;
+    FFS_CK(cudaMemcpyAsync(&I.st->nrec, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaMemcpyAsync(&I.st->nspec, &zero, sizeof(zero), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    if (hs.err & 1u) { err = "non-finite value in the spectral state (simulation diverged)"; return FFS_ENAN; }
+    return 0;
+  }
+
+  int step(int64_t n, std::string& err) override {
+    if (!initialized) { err = "ffs_initialize must be called before ffs_step"; return FFS_ESTATE; }
+    if (n < 0) { err = "nsteps must be >= 0"; return FFS_EINVAL; }
+    int rc;
+    if ((rc = build_graph(err))) return rc;
+    int64_t done = 0;
+    while (done < n) {
+      // chunk so that the device record buffers cannot overflow
+      int64_t chunk = 0, ns = 0, nsp = 0;
+      const int64_t it0 = iteration + done;
+      while (done + chunk < n) {
+        const int64_t it = it0 + chunk;
+        const int64_t a = (it % P.dt_stat == 0) ? 1 : 0, b = (it % P.dt_spec == 0) ? 1 : 0;
+        if (ns + a > I.rec_cap || nsp + b > I.spec_cap) break;
+        ns += a; nsp += b; ++chunk;
+        if (chunk >= 4096) break;
+      }
+      for (int64_t i = 0; i < chunk; ++i) FFS_CK(cudaGraphLaunch(gexec, s));
+      FFS_CK(cudaStreamSynchronize(s));
+      if ((rc = drain(it0, it0 + chunk - 1, err))) return rc;
+      done += chunk;
+    }
+    return 0;
+  }
+
+  int time_steps(int64_t n, double* ms, std::string& err) override {
+    if (!initialized) { err = "ffs_initialize must be called first"; return FFS_ESTATE; }
+    int rc;
+    if ((rc = build_graph(err))) return rc;
+    cudaEvent_t a, b;
+    FFS_CK(cudaEventCreate(&a));
+    FFS_CK(cudaEventCreate(&b));
+    FFS_CK(cudaEventRecord(a, s));
+    for (int64_t i = 0; i < n; ++i) FFS_CK(cudaGraphLaunch(gexec, s));
+    FFS_CK(cudaEventRecord(b, s));
+    FFS_CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    FFS_CK(cudaEventElapsedTime(&f, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    return drain(iteration, iteration + n - 1, err);
+  }
+
+  int profile(int64_t n, std::vector<KernelTiming>& out, std::string& err) override {
+    if (!initialized) { err = "ffs_initialize must be called first"; return FFS_ESTATE; }
+    const char* names[8] = {"inv_z", "inv_y", "x_pass", "fwd_y", "scalar", "etd_table", "fwd_z_update", "finalize"};
+    double acc[8] = {0};
+    cudaEvent_t ev[9];
+    for (auto& e : ev) FFS_CK(cudaEventCreate(&e));
+    const int64_t it0 = iteration;
+    for (int64_t i = 0; i < n; ++i) {
+      FFS_CK(cudaEventRecord(ev[0], s));
+      launch_inv_z(inv_list); FFS_CK(cudaEventRecord(ev[1], s));
+      launch_inv_y(inv_list); FFS_CK(cudaEventRecord(ev[2], s));
+      launch_x(); FFS_CK(cudaEventRecord(ev[3], s));
+      launch_fwd_y(fwd_list); FFS_CK(cudaEventRecord(ev[4], s));
+      launch_scalar(0); FFS_CK(cudaEventRecord(ev[5], s));
+      launch_table(0); FFS_CK(cudaEventRecord(ev[6], s));
+      launch_zu(0); FFS_CK(cudaEventRecord(ev[7], s));
+      launch_fin(0); FFS_CK(cudaEventRecord(ev[8], s));
+      FFS_CK(cudaEventSynchronize(ev[8]));
+      for (int k = 0; k < 8; ++k) {
+        float f = 0.f;
+        FFS_CK(cudaEventElapsedTime(&f, ev[k], ev[k + 1]));
+        acc[k] += f;
+      }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    out.clear();
+    for (int k = 0; k < 8; ++k) {
+      if (k == 5 && !use_table()) continue;
+      out.push_back({names[k], acc[k]});
+    }
+    return drain(it0, it0 + n - 1, err);
+  }
+
+  int64_t device_bytes() const override { return bytes; }
+  void* stream() const override { return (void*)s; }
+};
+
+}  // namespace ffsgpu

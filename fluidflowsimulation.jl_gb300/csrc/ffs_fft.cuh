@@ -1,0 +1,201 @@
+// Shared-memory Stockham FFT core for line batches (sm_103a).
+//
+// A CTA transforms L lines of length n.  Line l, element j lives in shared memory
+// at buf[j * LS + l] (lines fastest), so a warp touches consecutive addresses.
+// Pass 0 reads its inputs through a loader functor (usually straight from global
+// memory, with any spectral prologue fused in) and the last pass hands its outputs
+// to a storer functor (global store, pruning, or epilogue math), so a two-pass
+// transform (n = R0 * R1) makes a single round trip through shared memory.
+//
+// Formulation (radix R, sub-transform length p, T = n / R butterflies per line):
+//   k = i mod p;  x_m = in[i + m T] * w^(k m n/(p R));  X = DFT_R(x);
+//   out[(i - k) R + k + m p] = X_m
+// with w = exp(-2 pi i / n) for the forward transform and its conjugate for the
+// inverse.  Output comes out in natural order after the last pass.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ffsgpu {
+
+template <typename T> struct cplx { T x, y; };
+
+template <typename T> __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x = a; r.y = b; return r; }
+template <typename T> __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cplx<T> b) {
+  return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ cplx<T> scl(cplx<T> a, T s) { return mk(a.x * s, a.y * s); }
+template <typename T> __device__ __forceinline__ cplx<T> cjg(cplx<T> a) { return mk(a.x, -a.y); }
+// multiply by +i (DIR=+1) or -i (DIR=-1)
+template <int DIR, typename T> __device__ __forceinline__ cplx<T> mul_i(cplx<T> a) {
+  return DIR > 0 ? mk(-a.y, a.x) : mk(a.y, -a.x);
+}
+
+struct FftPlan {
+  int n;      // transform length
+  int np;     // number of passes
+  int r[4];   // radices, product == n
+  int tpl;    // threads per line = n / max radix
+};
+
+// ---------------------------------------------------------------------------------
+// Small DFTs in registers. DIR = -1 forward (exp(-i..)), +1 inverse.
+// Constants are exact mathematical values (cos/sin of multiples of pi/8, sqrt(3)/2).
+// ---------------------------------------------------------------------------------
+#define FFS_C8 0.92387953251128675612818318939678829   /* cos(pi/8) */
+#define FFS_S8 0.38268343236508977172845998403039887   /* sin(pi/8) */
+#define FFS_R2 0.70710678118654752440084436210484904   /* sqrt(1/2) */
+#define FFS_R3 0.86602540378443864676372317075293618   /* sqrt(3)/2 */
+
+template <int DIR, typename T> __device__ __forceinline__ void dft2(cplx<T>& a, cplx<T>& b) {
+  cplx<T> t = a; a = t + b; b = t - b;
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft4(cplx<T>& x0, cplx<T>& x1, cplx<T>& x2, cplx<T>& x3) {
+  cplx<T> a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = mul_i<DIR>(x1 - x3);
+  x0 = a0 + a2; x2 = a0 - a2; x1 = a1 + a3; x3 = a1 - a3;
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft3(cplx<T>& x0, cplx<T>& x1, cplx<T>& x2) {
+  const T h = T(0.5), s = T(FFS_R3);
+  cplx<T> t1 = x1 + x2, t2 = x1 - x2;
+  cplx<T> c = mk(x0.x - h * t1.x, x0.y - h * t1.y);
+  cplx<T> d = scl(mul_i<DIR>(t2), s);
+  x0 = x0 + t1; x1 = c + d; x2 = c - d;
+}
+
+// multiply by exp(DIR * 2 pi i t / 8), t = 1,2,3
+template <int DIR, int t, typename T> __device__ __forceinline__ cplx<T> w8(cplx<T> a) {
+  const T r = T(FFS_R2);
+  if (t == 1) return DIR > 0 ? mk(r * (a.x - a.y), r * (a.x + a.y)) : mk(r * (a.x + a.y), r * (a.y - a.x));
+  if (t == 2) return mul_i<DIR>(a);
+  // t == 3: exp(DIR 3 pi i/4) = (-r, DIR r)
+  return DIR > 0 ? mk(-r * (a.x + a.y), r * (a.x - a.y)) : mk(r * (a.y - a.x), -r * (a.x + a.y));
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T>* x) {
+  dft4<DIR>(x[0], x[2], x[4], x[6]);
+  dft4<DIR>(x[1], x[3], x[5], x[7]);
+  cplx<T> o1 = w8<DIR, 1>(x[3]), o2 = w8<DIR, 2>(x[5]), o3 = w8<DIR, 3>(x[7]);
+  cplx<T> e0 = x[0], e1 = x[2], e2 = x[4], e3 = x[6], o0 = x[1];
+  x[0] = e0 + o0; x[4] = e0 - o0;
+  x[1] = e1 + o1; x[5] = e1 - o1;
+  x[2] = e2 + o2; x[6] = e2 - o2;
+  x[3] = e3 + o3; x[7] = e3 - o3;
+}
+
+// multiply by exp(DIR * 2 pi i t / 16) for t in {1,2,3,4,6,9}
+template <int DIR, int t, typename T> __device__ __forceinline__ cplx<T> w16(cplx<T> a) {
+  const T c = T(FFS_C8), s = T(FFS_S8);
+  if (t == 0) return a;
+  if (t == 2) return w8<DIR, 1>(a);
+  if (t == 4) return mul_i<DIR>(a);
+  if (t == 6) return w8<DIR, 3>(a);
+  // general: (cos th, DIR sin th) * a
+  T cr, si;
+  if (t == 1) { cr = c; si = s; }
+  else if (t == 3) { cr = s; si = c; }
+  else { cr = -c; si = -s; }  // t == 9: cos(9pi/8) = -cos(pi/8), sin(9pi/8) = -sin(pi/8)
+  si = DIR > 0 ? si : -si;
+  return mk(a.x * cr - a.y * si, a.x * si + a.y * cr);
+}
+
+template <int DIR, typename T> __device__ __forceinline__ void dft16(cplx<T>* x) {
+  // x index m = 4 m1 + m2, output k = k1 + 4 k2
+  dft4<DIR>(x[0], x[4], x[8], x[12]);
+  dft4<DIR>(x[1], x[5], x[9], x[13]);
+  dft4<DIR>(x[2], x[6], x[10], x[14]);
+  dft4<DIR>(x[3], x[7], x[11], x[15]);
+  // now x[4 k1 + m2] holds Y[m2][k1]; twiddle by W16^(m2 k1)
+  x[5] = w16<DIR, 1>(x[5]); x[9] = w16<DIR, 2>(x[9]); x[13] = w16<DIR, 3>(x[13]);
+  x[6] = w16<DIR, 2>(x[6]); x[10] = w16<DIR, 4>(x[10]); x[14] = w16<DIR, 6>(x[14]);
+  x[7] = w16<DIR, 3>(x[7]); x[11] = w16<DIR, 6>(x[11]); x[15] = w16<DIR, 9>(x[15]);
+  // Y[m2][k1] at x[m2 + 4 k1]; DFT4 over m2 for each k1
+  dft4<DIR>(x[0], x[1], x[2], x[3]);
+  dft4<DIR>(x[4], x[5], x[6], x[7]);
+  dft4<DIR>(x[8], x[9], x[10], x[11]);
+  dft4<DIR>(x[12], x[13], x[14], x[15]);
+  // result X[k1 + 4 k2] sits at x[4 k1 + k2]: transpose the 4x4
+  cplx<T> t;
+#define FFS_SW(a, b) t = x[a]; x[a] = x[b]; x[b] = t;
+  FFS_SW(1, 4) FFS_SW(2, 8) FFS_SW(3, 12) FFS_SW(6, 9) FFS_SW(7, 13) FFS_SW(11, 14)
+#undef FFS_SW
+}
+
+template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T>* x) {
+  if (R == 2) dft2<DIR>(x[0], x[1]);
+  else if (R == 3) dft3<DIR>(x[0], x[1], x[2]);
+  else if (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
+  else if (R == 8) dft8<DIR>(x);
+  else if (R == 16) dft16<DIR>(x);
+}
+
+// ---------------------------------------------------------------------------------
+// One Stockham pass over L lines.
+//   FIRST: read through ld(l, j) instead of shared memory.
+//   LAST:  write through st(l, j, v) instead of shared memory.
+// tw: table exp(-2 pi i t / n), t in [0, n) (global memory, read through L1).
+// ---------------------------------------------------------------------------------
+template <int R, int DIR, int L, typename T, class LD, class ST>
+__device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, const cplx<T>* __restrict__ in,
+                                         cplx<T>* __restrict__ out, int LS, const cplx<T>* __restrict__ tw,
+                                         LD& ld, ST& st) {
+  const int T_ = n / R;
+  const int nb = L * T_;
+  const int tws = n / (p * R);
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+    const int l = b % L, i = b / L;
+    const int k = i % p;
+    cplx<T> x[R];
+    if (first) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) x[m] = ld(l, i + m * T_);
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m) x[m] = in[(i + m * T_) * LS + l];
+      if (k != 0) {
+#pragma unroll
+        for (int m = 1; m < R; ++m) {
+          cplx<T> w = tw[k * m * tws];
+          if (DIR > 0) w.y = -w.y;
+          x[m] = x[m] * w;
+        }
+      }
+    }
+    dftR<R, DIR>(x);
+    const int j = (i - k) * R + k;
+    if (last) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) st(l, j + m * p, x[m]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m) out[(j + m * p) * LS + l] = x[m];
+    }
+  }
+}
+
+// Runs the whole plan. s0/s1: shared buffers of n*LS elements (s1 unused for np <= 2).
+// Ends with a __syncthreads() so callers may reuse the buffers immediately.
+template <int DIR, int L, typename T, class LD, class ST>
+__device__ void fft_lines(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS, const cplx<T>* __restrict__ tw, LD ld,
+                          ST st) {
+  int p = 1;
+  for (int pass = 0; pass < P.np; ++pass) {
+    const bool first = pass == 0, last = pass == P.np - 1;
+    cplx<T>* in = (pass & 1) ? s0 : s1;   // output buffer of the previous pass
+    cplx<T>* out = (pass & 1) ? s1 : s0;
+    switch (P.r[pass]) {
+      case 16: fft_pass<16, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+      case 8: fft_pass<8, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+      case 4: fft_pass<4, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+      case 3: fft_pass<3, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+      default: fft_pass<2, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+    }
+    p *= P.r[pass];
+    __syncthreads();
+  }
+}
+
+}  // namespace ffsgpu

@@ -1,0 +1,108 @@
+// Internal definitions shared by the CUDA passes and the C-ABI host runtime.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ffs_fft.cuh"
+
+namespace ffsgpu {
+
+// Field codes produced by the spectral prologue of the inverse z pass.
+enum FieldCode : int {
+  F_UX = 0, F_UY, F_UZ,          // velocity
+  F_WX, F_WY, F_WZ,              // vorticity  i k x u
+  F_SXX, F_SXY, F_SXZ, F_SYY, F_SYZ,   // strain sym(i k (x) u), traceless, 5 comps
+  F_RHO                          // density perturbation
+};
+
+// Forward-field roles consumed by the forward z pass.
+enum FwdRole : int { R_NX = 0, R_NY, R_NZ, R_KE, R_TXX, R_TXY, R_TXZ, R_TYY, R_TYZ, R_FX, R_FY, R_FZ };
+
+// Stats partial-sum quantities (per CTA of the forward z pass).
+enum StatQ : int {
+  Q_U1 = 0, Q_U2, Q_U3, Q_U12, Q_U22, Q_U32, Q_EH, Q_EV, Q_NLH, Q_NLV, Q_PH, Q_PV,
+  Q_D1DY, Q_D1DX, Q_D2DY, Q_D2DX, Q_LESH, Q_LESV, Q_HVH, Q_HVV,
+  Q_RHO, Q_RHO2, Q_DR1, Q_DR2, Q_DR3, Q_BF, Q_HP, Q_VP,
+  Q_IL0,  // 9 integral-length plane sums: [component][plane x,y,z]
+  Q_COUNT = Q_IL0 + 9
+};
+constexpr int QPAD = 40;
+
+// Device-resident scalar state (one per simulation).
+struct DevState {
+  long long iteration;     // reference s.iteration
+  double time;             // reference s.time
+  double dt, dt2, dt3;     // integrator dt history (dt = current)
+  long long ts_iter;       // integrator's own call counter
+  double At, Bt, Ct;       // AB3 scalars of the current step
+  int stage;               // 1, 2, 3: integrator stage of the current step
+  int hist_parity;         // which history slot holds fm1
+  double slot_u;           // the reference's reductionh[1] (single Julia thread)
+  double slot_rho;         // density reduction[1]
+  unsigned long long umax_bits;    // running max |u_i| of this step (atomicMax on double bits)
+  unsigned long long rhomax_bits;  // running max |rho|
+  double force_coef;       // isotropic band forcing: eps / (2 E_f)
+  double Ef;
+  double nl_h, nl_v, press_h, press_v;  // last non-linear / pressure stats
+  long long nrec;          // stats records written
+  long long nspec;         // spectrum records written
+  unsigned int err;        // bit 0: non-finite value in the update
+  int pad0;
+};
+
+template <typename T> struct Inst {
+  // grid
+  int nx, ny, nz, nxh;
+  int Mx, KXP;             // retained kx count, padded row length
+  int NYR, ypos;           // retained ky count, count of retained ky >= 0
+  int NZR, zpos;
+  int uniformL;            // lx == ly == lz: ETD coefficients tabulated by i^2+j^2+l^2
+  double lx, ly, lz;
+  double inv_n;            // 1 / (nx ny nz)
+  FftPlan px, py, pz;
+  const cplx<T>* twx;
+  const cplx<T>* twy;
+  const cplx<T>* twz;
+  // resident spectral state, compact [comp][kz'][ky'][KXP]
+  cplx<T>* uh;             // 3 velocity comps (+ rho)
+  cplx<T>* hist;           // [2][ncomp][...]
+  long long cstride;       // elements per compact component = NZR*NYR*KXP
+  int ncomp;               // 3 or 4
+  // work arrays
+  cplx<T>* wz;             // [slot][nz][NYR][KXP]
+  cplx<T>* wy;             // [slot][nz][ny][KXP]
+  long long wzs, wys;      // slot strides
+  double* phys;            // FP64 physical staging [field][nz][ny][nx]
+  // scalar state and outputs
+  DevState* st;
+  double* partials;        // [nblocks_z][QPAD]
+  double* records;         // stats records [cap][ncols]
+  int rec_cap, ncols;
+  double* spec;            // spectrum records [cap][4][nbin]
+  int spec_cap, nbinH, nbinV;
+  double maxdkh, dkz;
+  // ETD coefficient tables [q][4] (E, A, B, C), velocity then density
+  T* etab;
+  T* etab_rho;
+  int qmax;
+  // physics
+  double nu, cfl, dt0;
+  int ab3, adaptive, ref_slot;
+  int hv, hv_m;
+  double hv_nu;
+  int les;
+  double les_alpha;        // c^2 Delta^2
+  int density, gdir;
+  double alpha, dgrad, gval;
+  int forcing;
+  double f_eps, f_kf;
+  int dt_stat, dt_spec;
+  // field lists for the passes
+  int nin;                 // inverse fields
+  int in_code[12];
+  int nout;                // forward fields (incl. kinetic-energy field)
+  int out_role[12];
+  int out_slot[12];
+};
+
+}  // namespace ffsgpu

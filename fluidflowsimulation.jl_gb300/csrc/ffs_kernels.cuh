@@ -1,0 +1,968 @@
+// The GPU passes of one pseudo-spectral step (templated on the arithmetic type T).
+//
+// Step = inverse z (spectral prologue) -> inverse y -> fused x pass (c2r, physical
+// products, r2c) -> forward y -> scalar kernel (dt, integrator coefficients, forcing)
+// -> forward z + update (projection, integrator, forcing, stats) -> finalize.
+//
+// Memory layout in HBM (complex T, kx fastest, kx padded to KXP):
+//   uh   [comp][kz'][ky'][kx]     retained (dealiased) modes only
+//   wz   [slot][z][ky'][kx]       after the z pass (inverse) / before it (forward)
+//   wy   [slot][z][y][kx]         after the y pass (inverse) / before it (forward)
+// Physical space exists only in shared memory inside the x pass.
+#pragma once
+#include "ffs_internal.h"
+
+namespace ffsgpu {
+
+constexpr int LYZ_IO = 4;  // (y,z) lines per CTA in the transform-only x kernels
+
+struct FieldList {
+  int n;
+  int code[12];   // FieldCode (inverse z) or role (forward passes)
+  int slot[12];   // work-array slot
+};
+
+// ------------------------------------------------------------------ index helpers
+template <typename T> __device__ __forceinline__ int ycomp(const Inst<T>& I, int y) {
+  if (y < I.ypos) return y;
+  int neg = I.NYR - I.ypos;
+  if (y >= I.ny - neg) return y - (I.ny - I.NYR);
+  return -1;
+}
+template <typename T> __device__ __forceinline__ int zcomp(const Inst<T>& I, int z) {
+  if (z < I.zpos) return z;
+  int neg = I.NZR - I.zpos;
+  if (z >= I.nz - neg) return z - (I.nz - I.NZR);
+  return -1;
+}
+// signed integer wavenumber index of compact y / z index
+template <typename T> __device__ __forceinline__ int ysig(const Inst<T>& I, int jc) {
+  int y = jc < I.ypos ? jc : I.ny - I.NYR + jc;
+  return y < I.ny / 2 ? y : y - I.ny;
+}
+template <typename T> __device__ __forceinline__ int zsig(const Inst<T>& I, int kc) {
+  int z = kc < I.zpos ? kc : I.nz - I.NZR + kc;
+  return z < I.nz / 2 ? z : z - I.nz;
+}
+
+__device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
+  // non-negative doubles order like their bit patterns
+  atomicMax(a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T> __device__ __forceinline__ double proj(cplx<T> a, cplx<T> b) {
+  return (double)a.x * (double)b.x + (double)a.y * (double)b.y;
+}
+
+// ====================================================================================
+// Inverse z pass with the spectral prologue (fourierspacep1!, models.jl:63-119):
+//   velocity, vorticity i k x u, strain sym(i k (x) u), density, each to its own slot.
+// grid (nfields, KXP/TX, NYR); block TX * tpl_z
+// ====================================================================================
+template <typename T, int TX>
+__global__ void __launch_bounds__(512) k_inv_z(Inst<T> I, FieldList F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + I.nz * TX;
+  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
+  const int code = F.code[fi];
+  const long long cs = I.cstride;
+  const int rowstride = I.NYR * I.KXP;
+  const cplx<T>* uh = I.uh + (long long)jc * I.KXP + kx0;
+  const T kyv = T(ysig(I, jc)) / T(I.ly);
+  auto ld = [&](int l, int z) -> cplx<T> {
+    const int kc = zcomp(I, z);
+    const int ix = kx0 + l;
+    if (kc < 0 || ix >= I.Mx) return mk(T(0), T(0));
+    const cplx<T>* p = uh + (long long)kc * rowstride + l;
+    const T kx = T(ix) / T(I.lx), ky = kyv, kz = T(zsig(I, kc)) / T(I.lz);
+    switch (code) {
+      case F_UX: return p[0];
+      case F_UY: return p[cs];
+      case F_UZ: return p[2 * cs];
+      case F_RHO: return p[3 * cs];
+      case F_WX: { cplx<T> uy = p[cs], uz = p[2 * cs];   // i (ky uz - kz uy)
+        return mk(-(ky * uz.y - kz * uy.y), ky * uz.x - kz * uy.x); }
+      case F_WY: { cplx<T> ux = p[0], uz = p[2 * cs];    // i (kz ux - kx uz)
+        return mk(-(kz * ux.y - kx * uz.y), kz * ux.x - kx * uz.x); }
+      case F_WZ: { cplx<T> ux = p[0], uy = p[cs];        // i (kx uy - ky ux)
+        return mk(-(kx * uy.y - ky * ux.y), kx * uy.x - ky * ux.x); }
+      case F_SXX: { cplx<T> ux = p[0]; return mk(-kx * ux.y, kx * ux.x); }
+      case F_SYY: { cplx<T> uy = p[cs]; return mk(-ky * uy.y, ky * uy.x); }
+      case F_SXY: { cplx<T> ux = p[0], uy = p[cs];
+        cplx<T> a = mk(kx * uy.x + ky * ux.x, kx * uy.y + ky * ux.y);
+        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
+      case F_SXZ: { cplx<T> ux = p[0], uz = p[2 * cs];
+        cplx<T> a = mk(kx * uz.x + kz * ux.x, kx * uz.y + kz * ux.y);
+        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
+      default: { cplx<T> uy = p[cs], uz = p[2 * cs];     // F_SYZ
+        cplx<T> a = mk(ky * uz.x + kz * uy.x, ky * uz.y + kz * uy.y);
+        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
+    }
+  };
+  cplx<T>* out = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
+  auto st = [&](int l, int z, cplx<T> v) { out[(long long)z * rowstride + l] = v; };
+  fft_lines<+1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
+}
+
+// ====================================================================================
+// Inverse y pass: grid (nfields, KXP/TX, nz); block TX * tpl_y
+// ====================================================================================
+template <typename T, int TX>
+__global__ void __launch_bounds__(512) k_inv_y(Inst<T> I, FieldList F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + I.ny * TX;
+  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
+  const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)z * I.NYR * I.KXP + kx0;
+  cplx<T>* out = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
+  auto ld = [&](int l, int y) -> cplx<T> {
+    const int jc = ycomp(I, y);
+    if (jc < 0) return mk(T(0), T(0));
+    return in[(long long)jc * I.KXP + l];
+  };
+  auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
+  fft_lines<+1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
+}
+
+// ====================================================================================
+// Forward y pass (keeps retained ky only): grid (nfields, KXP/TX, nz)
+// The kinetic-energy field is transformed only at stats/spectrum iterations.
+// ====================================================================================
+template <typename T, int TX>
+__global__ void __launch_bounds__(512) k_fwd_y(Inst<T> I, FieldList F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + I.ny * TX;
+  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
+  if (F.code[fi] == R_KE) {
+    const long long it = I.st->iteration;
+    if ((it % I.dt_stat) != 0 && (it % I.dt_spec) != 0) return;
+  }
+  const cplx<T>* in = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
+  cplx<T>* out = I.wz + (long long)F.slot[fi] * I.wzs + (long long)z * I.NYR * I.KXP + kx0;
+  auto ld = [&](int l, int y) -> cplx<T> { return in[(long long)y * I.KXP + l]; };
+  auto st = [&](int l, int y, cplx<T> v) {
+    const int jc = ycomp(I, y);
+    if (jc >= 0) out[(long long)jc * I.KXP + l] = v;
+  };
+  fft_lines<-1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
+}
+
+// ====================================================================================
+// Fused x pass (realspace! + realspacecalculation! + calc_les! + find_max, models.jl
+// 121-214 / 228-280, les_real_calc.jl:13-139, utils.jl:247-258):
+//   stage half spectra -> c2r (two real fields per complex line) -> physical products
+//   -> r2c (two real fields per complex line) -> Hermitian unpack -> store kx < KXP.
+// grid (ny*nz/LYZ); block >= LYZ*PIN*tpl_x
+// Real fields in:  u(3) w(3) [S(5) if LES] [rho if DEN]
+// Real fields out: N(3) ke [tau(5) if LES] [flux(3) if DEN]
+// ====================================================================================
+template <bool LES, bool DEN> struct XFields {
+  static constexpr int nin = 6 + (LES ? 5 : 0) + (DEN ? 1 : 0);
+  static constexpr int nout = 4 + (LES ? 5 : 0) + (DEN ? 3 : 0);
+  static constexpr int PIN = (nin + 1) / 2;
+  static constexpr int POUT = (nout + 1) / 2;
+};
+
+template <typename T, bool LES, bool DEN, int LYZ>
+__global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
+  using XF = XFields<LES, DEN>;
+  constexpr int PIN = XF::PIN, POUT = XF::POUT;
+  constexpr int LIN = PIN * LYZ, LOUT = POUT * LYZ;
+  constexpr int LSX = LIN + 1;   // odd stride for the exchange buffer
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = I.nx, Mx = I.Mx;
+  const int MXP = Mx | 1;
+  cplx<T>* stage = reinterpret_cast<cplx<T>*>(smem_raw);                  // [nin][LYZ][MXP]
+  cplx<T>* sx = stage + (size_t)XF::nin * LYZ * MXP;                         // [n][LSX]
+  cplx<T>* s0 = sx + (size_t)n * LSX;                                      // [n][LIN]
+  cplx<T>* s1 = s0 + (size_t)n * LIN;                                      // [n][LIN] (np >= 3)
+  __shared__ double red[32];
+
+  const int g0 = blockIdx.x * LYZ;
+  const long long it = I.st->iteration;
+  const bool want_ke = ((it % I.dt_stat) == 0) || ((it % I.dt_spec) == 0);
+
+  // 1. stage the half spectra (coalesced along kx)
+  {
+    const int per = XF::nin * LYZ * Mx;
+    for (int e = threadIdx.x; e < per; e += blockDim.x) {
+      const int kx = e % Mx, r = e / Mx, q = r % LYZ, f = r / LYZ;
+      const int g = g0 + q;
+      stage[(f * LYZ + q) * MXP + kx] = I.wy[(long long)f * I.wys + (long long)g * I.KXP + kx];
+    }
+  }
+  __syncthreads();
+
+  // 2. c2r: complex line l = p*LYZ + q carries fields (2p, 2p+1) of line q
+  auto ldi = [&](int l, int j) -> cplx<T> {
+    const int p = l / LYZ, q = l % LYZ;
+    const bool cj = 2 * j > n;
+    const int k = cj ? n - j : j;
+    if (k >= Mx) return mk(T(0), T(0));
+    const int fa = 2 * p, fb = 2 * p + 1;
+    cplx<T> A = stage[(fa * LYZ + q) * MXP + k];
+    cplx<T> B = fb < XF::nin ? stage[(fb * LYZ + q) * MXP + k] : mk(T(0), T(0));
+    if (k == 0 || 2 * k == n) { A.y = T(0); B.y = T(0); }
+    if (cj) { A.y = -A.y; B.y = -B.y; }
+    return mk(A.x - B.y, A.y + B.x);
+  };
+  auto sti = [&](int l, int j, cplx<T> v) { sx[j * LSX + l] = v; };
+  fft_lines<+1, LIN, T>(I.px, s0, s1, LIN, I.twx, ldi, sti);
+
+  // 3. physical space products, in place in sx (outputs in the first POUT pairs)
+  double umax = 0.0, rmax = 0.0;
+  for (int e = threadIdx.x; e < n * LYZ; e += blockDim.x) {
+    const int q = e % LYZ, j = e / LYZ;
+    cplx<T>* row = sx + j * LSX + q;
+    T f[2 * PIN];
+#pragma unroll
+    for (int p = 0; p < PIN; ++p) { cplx<T> v = row[p * LYZ]; f[2 * p] = v.x; f[2 * p + 1] = v.y; }
+    const T ux = f[0], uy = f[1], uz = f[2], wx = f[3], wy = f[4], wz = f[5];
+    T o[2 * POUT];
+#pragma unroll
+    for (int r = 0; r < 2 * POUT; ++r) o[r] = T(0);
+    o[0] = uy * wz - uz * wy;             // (u x w), models.jl:260
+    o[1] = uz * wx - ux * wz;
+    o[2] = ux * wy - uy * wx;
+    o[3] = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);   // models.jl:224
+    umax = fmax(umax, fmax(fabs((double)ux), fmax(fabs((double)uy), fabs((double)uz))));
+    if (LES) {
+      const T xx = f[6], xy = f[7], xz = f[8], yy = f[9], yz = f[10];
+      const T zz = -xx - yy;
+      const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
+      const T two_nut = T(2) * T(I.les_alpha) * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
+      o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
+    }
+    if (DEN) {
+      constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
+      const T rho = f[fr];
+      rmax = fmax(rmax, fabs((double)rho));
+      o[of] = -rho * ux; o[of + 1] = -rho * uy; o[of + 2] = -rho * uz;   // models.jl:266
+    }
+#pragma unroll
+    for (int r = 0; r < POUT; ++r) row[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
+  }
+  // block max -> one atomic per CTA
+  if (I.adaptive) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+      rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+    if (lane == 0) { red[w] = umax; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = 0.0;
+      for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
+      atomic_max_pos(&I.st->umax_bits, m);
+    }
+    __syncthreads();
+    if (DEN) {
+      if (lane == 0) red[w] = rmax;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
+        atomic_max_pos(&I.st->rhomax_bits, m);
+      }
+    }
+  }
+  __syncthreads();
+
+  // 4. r2c of the output pairs, result back into sx
+  auto ldf = [&](int l, int j) -> cplx<T> { return sx[j * LSX + l]; };
+  auto stf = [&](int l, int j, cplx<T> v) { sx[j * LSX + l] = v; };
+  fft_lines<-1, LOUT, T>(I.px, s0, s1, LIN, I.twx, ldf, stf);
+
+  // 5. unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 and store
+  const int KXP = I.KXP;
+  const int per = LOUT * KXP;
+  for (int e = threadIdx.x; e < per; e += blockDim.x) {
+    const int k = e % KXP, l = e / KXP, r = l / LYZ, q = l % LYZ;
+    const int g = g0 + q;
+    cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
+    if (k < Mx) {
+      const cplx<T> zk = sx[k * LSX + l];
+      const cplx<T> zm = sx[((n - k) % n) * LSX + l];
+      A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
+      B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+    }
+    const int oa = 2 * r, ob = 2 * r + 1;
+    if (oa < XF::nout) I.wy[(long long)I.out_slot[oa] * I.wys + (long long)g * KXP + k] = A;
+    if (ob < XF::nout) I.wy[(long long)I.out_slot[ob] * I.wys + (long long)g * KXP + k] = B;
+  }
+}
+
+// ====================================================================================
+// ETD phi-function coefficients (ETD.jl:142-227, ETD1stand2ndO.jl:12-66), FP64.
+// Returns E = exp(c dt) and A, B, C so that u' = E u + A N + B fm1 + C fm2.
+// ====================================================================================
+__device__ inline void etd_coeffs(double c, double dt, double dt2, double dt3, int stage, double& E, double& A,
+                                  double& B, double& C) {
+  const double cdt = c * dt;
+  E = exp(cdt);
+  const bool test = -cdt <= 1e-4;
+  const bool inf = (c == -INFINITY);
+  if (stage == 1) {
+    const double cdt2 = cdt * dt, c2dt3 = cdt2 * cdt, c3dt4 = c2dt3 * cdt;
+    A = inf ? 0.0 : (test ? dt + 0.5 * cdt2 + c2dt3 / 6 + c3dt4 / 24 : expm1(cdt) / c);
+    B = 0.0; C = 0.0;
+  } else if (stage == 2) {
+    const double cp2 = c * c, cdtp2 = cdt * dt, c2dtp3 = cdtp2 * cdt, c3dtp4 = c2dtp3 * cdt;
+    const double em = expm1(cdt), c2dt2 = c * c * dt2;
+    const double dtp2 = dt * dt, dtp3 = dtp2 * dt, dtp4 = dtp3 * dt;
+    A = inf ? 0.0 : (test ? dt + cdtp2 / 2 + c2dtp3 / 6 + c3dtp4 / 24 + dtp2 / (2 * dt2) + (c * dtp3) / (6 * dt2) +
+                                (cp2 * dtp4) / (24 * dt2)
+                          : (em - c * (dt - dt2 * em)) / c2dt2);
+    B = inf ? 0.0 : (test ? (-(dtp2 / (2 * dt2)) - (c * dtp3) / (6 * dt2) - (cp2 * dtp4) / (24 * dt2))
+                          : (cdt - em) / c2dt2);
+    C = 0.0;
+  } else {
+    const double a0 = (dt * (2 * dt * dt + 6 * dt2 * (dt2 + dt3) + 3 * dt * (2 * dt2 + dt3))) / (6 * dt2 * (dt2 + dt3));
+    const double a1 = (dt * dt * (dt * dt + 6 * dt2 * (dt2 + dt3) + 2 * dt * (2 * dt2 + dt3))) / (12 * dt2 * (dt2 + dt3));
+    const double a2 = (dt * dt * dt * (4 * dt2 * (dt2 + dt3) + dt * (2 * dt2 + dt3))) / (24 * dt2 * (dt2 + dt3));
+    const double a3 = dt * dt * dt * dt / 24;
+    const double b0 = -((dt * dt * (2 * dt + 3 * (dt2 + dt3))) / (6 * (dt2 * dt3)));
+    const double b1 = -(((dt * dt * dt * (dt + 2 * (dt2 + dt3)))) / (12 * (dt2 * dt3)));
+    const double b2 = -((dt * dt * dt * dt * (dt2 + dt3)) / (24 * (dt2 * dt3)));
+    const double c0 = (dt * dt * (2 * dt + 3 * dt2)) / (6 * dt3 * (dt2 + dt3));
+    const double c1 = (dt * dt * dt * (dt + 2 * dt2)) / (12 * dt3 * (dt2 + dt3));
+    const double c2 = (dt * dt * dt * dt * dt2) / (24 * dt3 * (dt2 + dt3));
+    const double e1 = dt * dt + dt * (2 * dt2 + dt3), e2 = dt2 * (dt2 + dt3), e3 = 2 * dt, e4 = 2 * dt2 + dt3;
+    const double e5 = dt * (dt + dt2 + dt3), e6 = dt2 + dt3, e7 = dt2 * dt3, e8 = dt * (dt + dt2), e9 = dt3 * (dt2 + dt3);
+    const double l1 = c, l2 = l1 * l1, l3 = l2 * l1;
+    if (inf) { A = B = C = 0.0; return; }
+    if (test) {
+      A = fma(a1, l1, fma(a2, l2, fma(a3, l3, a0)));
+      B = fma(b1, l1, fma(b2, l2, b0));
+      C = fma(c1, l1, fma(c2, l2, c0));
+    } else {
+      const double em = expm1(cdt);
+      A = (2 * em - l2 * (e1 - e2 * em) - l1 * (e3 - e4 * em)) / (l3 * e2);
+      B = (e5 * l2 - 2 * em + l1 * (e3 - e6 * em)) / (l3 * e7);
+      C = (2 * em - e8 * l2 - l1 * (e3 - dt2 * em)) / (l3 * e9);
+    }
+  }
+}
+
+// velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95)
+template <typename T> __device__ __forceinline__ double c_vel(const Inst<T>& I, double k2) {
+  double c = k2 * (-I.nu);
+  if (I.hv) {
+    double km = 1.0;
+    for (int m = 0; m < I.hv_m; ++m) km *= k2;
+    c = fma(k2, -I.nu, km * (-I.hv_nu));
+  }
+  return c;
+}
+
+// ====================================================================================
+// Scalar kernel: set_dt! (time_step_functions.jl:86-129), integrator dt history
+// (Adams_Bashforth.jl:37-47, ETD.jl:110-114), AB3 coefficients (Adams_Bashforth.jl
+// 49-89), forcing energy of the band. mode 0: a step; mode 1: initialize!.
+// One CTA.
+// ====================================================================================
+template <typename T>
+__global__ void k_scalar(Inst<T> I, int mode) {
+  DevState* S = I.st;
+  __shared__ double sh_ef[256];
+  if (threadIdx.x == 0) {
+    const long long it = S->iteration;
+    if (I.adaptive) {
+      const double m = __longlong_as_double((long long)S->umax_bits);
+      S->slot_u = I.ref_slot ? fmax(m, S->slot_u) : m;
+      if (I.density) {
+        const double mr = __longlong_as_double((long long)S->rhomax_bits);
+        S->slot_rho = I.ref_slot ? fmax(mr, S->slot_rho) : mr;
+      }
+      const double umax = S->slot_u;
+      const double dx = 2.0 * M_PI * I.ly / I.ny;
+      double cfl = I.cfl;
+      if (it == 0) cfl *= 0.1;
+      else if (it == 1) cfl *= 0.2;
+      else if (it == 2) cfl *= 0.4;
+      else if (it == 3) cfl *= 0.8;
+      double newdt = cfl * dx / umax;
+      if (I.density) {
+        const double den = S->slot_rho * fabs(I.gval);
+        newdt = fmin(newdt, cfl * sqrt(dx / den));
+      }
+      if (it > 3) {
+        const double dt = S->dt;
+        newdt = newdt < dt ? fmax(dt / 1.25, newdt) : fmin(1.25 * dt, newdt);
+      }
+      if (I.ab3) {
+        if (S->ts_iter == 0) { S->dt3 = S->dt2 = S->dt = newdt / 2; }
+        else { S->dt3 = S->dt2; S->dt2 = S->dt; S->dt = newdt; }
+      } else {
+        S->dt3 = S->dt2; S->dt2 = S->dt; S->dt = newdt;
+      }
+    }
+    if (mode == 1) {
+      // initialize! of the integrator: dt history := current dt (Adams_Bashforth.jl:28-35, ETD.jl:99-108)
+      S->dt2 = S->dt; S->dt3 = S->dt;
+      S->stage = 0;
+    } else {
+      S->ts_iter += 1;
+      const long long i = S->ts_iter;
+      S->stage = i >= 3 ? 3 : (int)i;
+      if (I.ab3) {
+        const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
+        if (I.adaptive) {
+          S->At = (1. + (dt * (2 * dt + 6 * dt2 + 3 * dt3)) / (6 * dt2 * (dt2 + dt3))) * dt;
+          S->Bt = (-dt * dt * (2 * dt + 3 * dt2 + 3 * dt3) / (6 * dt2 * dt3 * (dt + dt2))) * (dt + dt2);
+          S->Ct = (dt * dt * (2 * dt + 3 * dt2) / (6 * dt3 * (dt + dt2 + dt3) * (dt2 + dt3))) * (dt + dt2 + dt3);
+        } else {
+          S->At = 23 * dt / 12; S->Bt = -16 * dt / 12; S->Ct = 5 * dt / 12;
+        }
+      }
+    }
+  }
+  // isotropic band forcing: E_f = sum_{0<|k|<=kf} 1/2 w |u|^2 from the current u
+  if (I.forcing && mode == 0) {
+    const int bx = (int)floor(I.f_kf * I.lx) + 1, by = (int)floor(I.f_kf * I.ly) + 1, bz = (int)floor(I.f_kf * I.lz) + 1;
+    const int cnt = bx * (2 * by + 1) * (2 * bz + 1);
+    double e = 0.0;
+    for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+      const int ix = t % bx, r = t / bx, iy = r % (2 * by + 1) - by, iz = r / (2 * by + 1) - bz;
+      if (ix >= I.Mx) continue;
+      const double kx = ix / I.lx, ky = iy / I.ly, kz = iz / I.lz;
+      const double k2 = kx * kx + ky * ky + kz * kz;
+      if (k2 == 0.0 || k2 > I.f_kf * I.f_kf) continue;
+      const int y = iy >= 0 ? iy : I.ny + iy, z = iz >= 0 ? iz : I.nz + iz;
+      const int jc = ycomp(I, y), kc = zcomp(I, z);
+      if (jc < 0 || kc < 0) continue;
+      const long long idx = ((long long)kc * I.NYR + jc) * I.KXP + ix;
+      double a = 0.0;
+      for (int c = 0; c < 3; ++c) { cplx<T> v = I.uh[c * I.cstride + idx]; a += (double)v.x * v.x + (double)v.y * v.y; }
+      e += 0.5 * (ix > 0 ? 2.0 : 1.0) * a;
+    }
+    sh_ef[threadIdx.x] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int i = 0; i < blockDim.x; ++i) s += sh_ef[i];
+      S->Ef = s;
+      S->force_coef = s > 0.0 ? I.f_eps / (2.0 * s) : 0.0;
+    }
+  }
+}
+
+// ETD coefficient tables by q = i^2 + j^2 + l^2 (uniform domain), for the current
+// stage and dt history. Multi-CTA; runs after k_scalar.
+template <typename T>
+__global__ void k_etd_table(Inst<T> I, int mode) {
+  const DevState* S = I.st;
+  const int stage = S->stage;
+  if (mode == 1 || stage == 0) return;
+  const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
+  const double L2 = I.lx * I.lx;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= I.qmax; q += gridDim.x * blockDim.x) {
+    const double k2 = (double)q / L2;
+    double E, A, B, C;
+    etd_coeffs(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
+    T* e = I.etab + 4 * (size_t)q;
+    e[0] = T(E); e[1] = T(A); e[2] = T(B); e[3] = T(C);
+    if (I.density && I.etab_rho) {
+      etd_coeffs(k2 * (-I.alpha), dt, dt2, dt3, stage, E, A, B, C);
+      T* r = I.etab_rho + 4 * (size_t)q;
+      r[0] = T(E); r[1] = T(A); r[2] = T(B); r[3] = T(C);
+    }
+  }
+}
+
+// ====================================================================================
+// Forward z pass + update (myfourier! z-part + dealias + 1/N + rhs[1]=0, models.jl
+// 171-175; fourierspacep2!, models.jl:282-364; time_step!, models.jl:468-472 and
+// time_step_functions.jl:72-80; stats reductions, stats.jl; spectrum, spec.jl).
+// grid (KXP/TX, NYR); block TX * tpl_z.  mode 0: step, 1: initialize! (no update).
+// ====================================================================================
+template <typename T, int TX>
+__global__ void __launch_bounds__(512) k_fwd_z_update(Inst<T> I, FieldList F, int mode) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nz = I.nz, NZR = I.NZR;
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + nz * TX;
+  cplx<T>* accN = s1 + (I.pz.np >= 3 ? nz * TX : 0);  // [3][NZR][TX]
+  cplx<T>* accK = accN + 3 * NZR * TX;                 // [NZR][TX]
+  cplx<T>* accT = accK + NZR * TX;                     // [3][NZR][TX] (LES)
+  cplx<T>* accF = accT + 3 * NZR * TX;                 // [NZR][TX]    (density)
+  __shared__ double red[QPAD][17];
+
+  const DevState* S = I.st;
+  const long long it = S->iteration;
+  const bool stats_t = (it % I.dt_stat) == 0;
+  const bool spec_t = mode == 0 && (it % I.dt_spec) == 0;
+  const int kx0 = blockIdx.x * TX, jc = blockIdx.y;
+  const int rowstride = I.NYR * I.KXP;
+  const T kyv = T(ysig(I, jc)) / T(I.ly);
+
+  // zero the LES / density accumulators
+  if (I.les || I.density) {
+    for (int e = threadIdx.x; e < 4 * NZR * TX; e += blockDim.x) accT[e] = mk(T(0), T(0));
+  }
+  __syncthreads();
+
+  // 1. forward z transforms of the forward fields
+  for (int fi = 0; fi < F.n; ++fi) {
+    const int role = F.code[fi];
+    if (role == R_KE && !(stats_t || spec_t)) continue;
+    const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
+    auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
+    auto st = [&](int l, int z, cplx<T> v) {
+      const int kc = zcomp(I, z);
+      if (kc < 0) return;
+      const int m = kc * TX + l;
+      if (role <= R_NZ) { accN[role * NZR * TX + m] = v; return; }
+      if (role == R_KE) { accK[m] = v; return; }
+      const T kx = T(kx0 + l) / T(I.lx), ky = kyv, kz = T(zsig(I, kc)) / T(I.lz);
+      // i k . tau for the traceless symmetric tau (models.jl:330); zz = -xx - yy
+      auto addT = [&](int c, T kk, cplx<T> a) { cplx<T>& d = accT[c * NZR * TX + m]; d.x -= kk * a.y; d.y += kk * a.x; };
+      switch (role) {
+        case R_TXX: addT(0, kx, v); addT(2, -kz, v); break;
+        case R_TXY: addT(0, ky, v); addT(1, kx, v); break;
+        case R_TXZ: addT(0, kz, v); addT(2, kx, v); break;
+        case R_TYY: addT(1, ky, v); addT(2, -kz, v); break;
+        case R_TYZ: addT(1, kz, v); addT(2, ky, v); break;
+        case R_FX: { cplx<T>& d = accF[m]; d.x -= kx * v.y; d.y += kx * v.x; } break;
+        case R_FY: { cplx<T>& d = accF[m]; d.x -= ky * v.y; d.y += ky * v.x; } break;
+        default: { cplx<T>& d = accF[m]; d.x -= kz * v.y; d.y += kz * v.x; } break;
+      }
+    };
+    fft_lines<-1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
+  }
+
+  // 2. per-mode update
+  const T sc = T(I.inv_n);
+  const int par = S->hist_parity;
+  const long long cs = I.cstride;
+  cplx<T>* hA = I.hist + (long long)par * I.ncomp * cs;         // fm1
+  cplx<T>* hB = I.hist + (long long)(1 - par) * I.ncomp * cs;   // fm2 -> receives the new rhs
+  const int stage = S->stage;
+  const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
+  const T At = T(S->At), Bt = T(S->Bt), Ct = T(S->Ct);
+  const T fdt = T(dt * S->force_coef);
+  const double kf2 = I.f_kf * I.f_kf;
+  double q[Q_COUNT];
+  const bool do_stats = stats_t;
+  if (do_stats) {
+#pragma unroll
+    for (int i = 0; i < Q_COUNT; ++i) q[i] = 0.0;
+  }
+  bool bad = false;
+  const int ky_i = ysig(I, jc);
+  for (int m = threadIdx.x; m < NZR * TX; m += blockDim.x) {
+    const int l = m % TX, kc = m / TX, ix = kx0 + l;
+    const long long gi = (long long)kc * rowstride + (long long)jc * I.KXP + ix;
+    if (ix >= I.Mx) {   // padding columns stay zero
+      if (mode == 0) for (int c = 0; c < I.ncomp; ++c) I.uh[c * cs + gi] = mk(T(0), T(0));
+      continue;
+    }
+    const int kz_i = zsig(I, kc);
+    const T kx = T(ix) / T(I.lx), ky = kyv, kz = T(kz_i) / T(I.lz);
+    const T k2 = kx * kx + (ky * ky + kz * kz);
+    const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
+    cplx<T> N[3], u[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      N[c] = k0 ? mk(T(0), T(0)) : scl(accN[c * NZR * TX + m], sc);   // models.jl:174
+      u[c] = I.uh[c * cs + gi];
+    }
+    cplx<T> rhs[3] = {N[0], N[1], N[2]};
+    cplx<T> rho = mk(T(0), T(0));
+    if (I.density) rho = I.uh[3 * cs + gi];
+    cplx<T> divT[3] = {mk(T(0), T(0)), mk(T(0), T(0)), mk(T(0), T(0))};
+    if (I.les) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) divT[c] = scl(accT[c * NZR * TX + m], sc);
+    }
+    if (I.ab3) {   // explicit (hyper)viscosity, models.jl:320-326
+      const T cv = T(c_vel(I, (double)k2));
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + scl(u[c], cv);
+    }
+    if (I.les) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + divT[c];
+    }
+    if (I.density) rhs[I.gdir] = rhs[I.gdir] + scl(rho, T(I.gval));   // models.jl:334-336
+    // projection (models.jl:338-339)
+    {
+      const cplx<T> kd = mk(kx * rhs[0].x + ky * rhs[1].x + kz * rhs[2].x, kx * rhs[0].y + ky * rhs[1].y + kz * rhs[2].y);
+      const T inv = k0 ? T(0) : T(1) / k2;
+      const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
+      rhs[0] = rhs[0] + scl(p1, kx); rhs[1] = rhs[1] + scl(p1, ky); rhs[2] = rhs[2] + scl(p1, kz);
+    }
+    // density rhs: i k . flux - drho/dz * u_g  (vectorfunctions.jl:93-103)
+    cplx<T> rrhs = mk(T(0), T(0));
+    if (I.density) {
+      rrhs = scl(accF[m], sc) + scl(u[I.gdir], T(-I.dgrad));
+      if (I.ab3) rrhs = rrhs + scl(rho, T(k2 * T(-I.alpha)));
+    }
+
+    if (do_stats) {
+      const double w = ix > 0 ? 2.0 : 1.0;
+      const double kxd = kx, kyd = ky, kzd = kz, k2d = k2;
+      double a2[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) a2[c] = proj(u[c], u[c]);
+      if (k0) { q[Q_U1] += u[0].x; q[Q_U2] += u[1].x; q[Q_U3] += u[2].x; }
+      q[Q_U12] += w * a2[0]; q[Q_U22] += w * a2[1]; q[Q_U32] += w * a2[2];
+      q[Q_EH] += w * k2d * (a2[0] + a2[1]); q[Q_EV] += w * k2d * a2[2];
+      q[Q_D1DY] += w * kyd * kyd * a2[0]; q[Q_D1DX] += w * kxd * kxd * a2[0];
+      q[Q_D2DY] += w * kyd * kyd * a2[1]; q[Q_D2DX] += w * kxd * kxd * a2[1];
+      // non-linear transfer: (N - i k ke) . u (stats.jl:897-917)
+      cplx<T> ke = scl(accK[m], sc);
+      const T kk[3] = {kx, ky, kz};
+      cplx<T> r[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) r[c] = mk(N[c].x + kk[c] * ke.y, N[c].y - kk[c] * ke.x);
+      q[Q_NLH] += w * (proj(r[0], u[0]) + proj(r[1], u[1]));
+      q[Q_NLV] += w * proj(r[2], u[2]);
+      // pressure transfer (stats.jl:764-814)
+      if (I.les) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) r[c] = r[c] + divT[c];
+      }
+      if (I.density) r[I.gdir] = r[I.gdir] + scl(rho, T(I.gval));
+      const double kdx = (double)kx * r[0].x + (double)ky * r[1].x + (double)kz * r[2].x;
+      const double kdy = (double)kx * r[0].y + (double)ky * r[1].y + (double)kz * r[2].y;
+      const double inv = k0 ? 0.0 : 1.0 / k2d;
+      const double p1x = -kdx * inv, p1y = -kdy * inv;
+      q[Q_PH] += w * (u[0].x * p1x * kxd + u[0].y * p1y * kxd + u[1].x * p1x * kyd + u[1].y * p1y * kyd);
+      q[Q_PV] += w * (u[2].x * p1x * kzd + u[2].y * p1y * kzd);
+      if (I.les) {
+        q[Q_LESH] += w * (proj(divT[0], u[0]) + proj(divT[1], u[1]));
+        q[Q_LESV] += w * proj(divT[2], u[2]);
+      }
+      if (I.hv) {
+        double km = 1.0;
+        for (int i = 0; i < I.hv_m; ++i) km *= k2d;
+        q[Q_HVH] += w * km * (a2[0] + a2[1]);
+        q[Q_HVV] += w * km * a2[2];
+      }
+      if (I.density) {
+        const double r2 = proj(rho, rho);
+        if (k0) q[Q_RHO] += rho.x;
+        q[Q_RHO2] += w * r2;
+        q[Q_DR1] += w * kxd * kxd * r2; q[Q_DR2] += w * kyd * kyd * r2; q[Q_DR3] += w * kzd * kzd * r2;
+        q[Q_BF] += w * proj(u[I.gdir], rho);
+      }
+      if (I.forcing && mode == 0 && k2d > 0.0 && k2d <= kf2) {
+        const double f = (double)fdt;
+        q[Q_HP] += w * (f * (a2[0] + a2[1]) + 0.5 * f * f * (a2[0] + a2[1]));
+        q[Q_VP] += w * (f * a2[2] + 0.5 * f * f * a2[2]);
+      }
+      // integral-length plane sums (stats.jl:952-980)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (ix == 0) q[Q_IL0 + 3 * c + 0] += a2[c];
+        if (ky_i == 0) q[Q_IL0 + 3 * c + 1] += w * a2[c];
+        if (kz_i == 0) q[Q_IL0 + 3 * c + 2] += w * a2[c];
+      }
+    }
+    if (spec_t) {
+      // spectrum_u + calculate_specHV (spec.jl:316-327, 424-450)
+      const double hh = 0.5 * (proj(u[0], u[0]) + proj(u[1], u[1]));
+      const double vv = 0.5 * proj(u[2], u[2]);
+      const long long rec = S->nspec;
+      if (rec < I.spec_cap) {
+        double* sp = I.spec + rec * 4LL * (I.nbinH > I.nbinV ? I.nbinH : I.nbinV);
+        const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
+        const int nk = (int)rint(fabs((double)kz) / I.dkz);
+        const int nj = (int)rint(fabs((double)ky) / I.maxdkh);
+        const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
+        double vals[2] = {hh, vv};
+        for (int s = 0; s < 2; ++s) {
+          double* H = sp + (2 * s) * stride;
+          double* V = sp + (2 * s + 1) * stride;
+          const double ee = vals[s];
+          if (ix == 0) {
+            if (nj < I.nbinH) { atomicAdd(&H[0], 0.5 * ee); atomicAdd(&H[nj], 0.5 * ee); }
+            if (nk < I.nbinV) atomicAdd(&V[nk], ee);
+          } else {
+            const double e2 = 2.0 * ee;
+            if (nx < I.nbinH) atomicAdd(&H[nx], 0.5 * e2 * I.maxdkh);
+            if (nj < I.nbinH) atomicAdd(&H[nj], 0.5 * e2 * I.maxdkh);
+            if (nk < I.nbinV) atomicAdd(&V[nk], e2 * I.dkz);
+          }
+        }
+      }
+    }
+
+    if (mode == 1) {   // initialize!: fm1 = fm2 = rhs (Adams_Bashforth.jl:28-35, ETD.jl:99-108)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { hA[c * cs + gi] = rhs[c]; hB[c * cs + gi] = rhs[c]; }
+      if (I.density) { hA[3 * cs + gi] = rrhs; hB[3 * cs + gi] = rrhs; }
+      continue;
+    }
+    // time step
+    cplx<T> f1[3], f2[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { f1[c] = hA[c * cs + gi]; f2[c] = hB[c * cs + gi]; }
+    T E, A, B, C;
+    if (I.ab3) {
+      if (stage == 2) {   // fix_fm2! (ETD.jl:130-140)
+        const T f = T(-(dt3 + dt2) / dt2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f2[c] = scl(rhs[c] - f1[c], f) + rhs[c];
+      }
+      E = T(1); A = At; B = Bt; C = Ct;
+    } else if (I.uniformL) {
+      const int qq = ix * ix + ky_i * ky_i + kz_i * kz_i;
+      const T* e = I.etab + 4 * (size_t)qq;
+      E = e[0]; A = e[1]; B = e[2]; C = e[3];
+    } else {
+      double e, a, b, cc;
+      etd_coeffs(c_vel(I, (double)k2), dt, dt2, dt3, stage, e, a, b, cc);
+      E = T(e); A = T(a); B = T(b); C = T(cc);
+    }
+    cplx<T> un[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
+      un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
+    }
+    if (I.forcing && (double)k2 > 0.0 && (double)k2 <= kf2) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) un[c] = un[c] + scl(u[c], fdt);
+    }
+    {  // projection after the update (time_step_functions.jl:78)
+      const cplx<T> kd = mk(kx * un[0].x + ky * un[1].x + kz * un[2].x, kx * un[0].y + ky * un[1].y + kz * un[2].y);
+      const T inv = k0 ? T(0) : T(1) / k2;
+      const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
+      un[0] = un[0] + scl(p1, kx); un[1] = un[1] + scl(p1, ky); un[2] = un[2] + scl(p1, kz);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      bad |= !(isfinite((double)un[c].x) && isfinite((double)un[c].y));
+      I.uh[c * cs + gi] = un[c];
+      hB[c * cs + gi] = rhs[c];
+    }
+    if (I.density) {
+      cplx<T> r1 = hA[3 * cs + gi], r2 = hB[3 * cs + gi];
+      if (I.ab3) {
+        if (stage == 2) r2 = scl(rrhs - r1, T(-(dt3 + dt2) / dt2)) + rrhs;
+        E = T(1); A = At; B = Bt; C = Ct;
+      } else if (I.uniformL) {
+        const int qq = ix * ix + ky_i * ky_i + kz_i * kz_i;
+        const T* e = I.etab_rho + 4 * (size_t)qq;
+        E = e[0]; A = e[1]; B = e[2]; C = e[3];
+      } else {
+        double e, a, b, cc;
+        etd_coeffs((double)k2 * (-I.alpha), dt, dt2, dt3, stage, e, a, b, cc);
+        E = T(e); A = T(a); B = T(b); C = T(cc);
+      }
+      cplx<T> rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + scl(rho, E)));
+      bad |= !(isfinite((double)rn.x) && isfinite((double)rn.y));
+      I.uh[3 * cs + gi] = rn;
+      hB[3 * cs + gi] = rrhs;
+    }
+  }
+  if (mode == 0 && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&I.st->err, 1u);
+
+  // 3. stats partials of this CTA (fixed-order reduction: warp shuffle tree, then warps)
+  if (do_stats) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const long long cta = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+    for (int i = 0; i < Q_COUNT; ++i) {
+      double v = q[i];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[i][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < Q_COUNT) {
+      double s = 0.0;
+      for (int i = 0; i < nw; ++i) s += red[threadIdx.x][i];
+      I.partials[cta * QPAD + threadIdx.x] = s;
+    }
+  }
+}
+
+// ====================================================================================
+// Finalize: stats record (stats.jl:64-219), reference reductionh reuse for the next
+// CFL (time_step_functions.jl:87 with utils.jl:247-258), iteration/time advance
+// (models.jl:14-15). One CTA of 1024 threads. mode 0: step, 1: initialize!.
+// ====================================================================================
+template <typename T>
+__global__ void k_finalize(Inst<T> I, int mode, int nparts) {
+  DevState* S = I.st;
+  __shared__ double tot[QPAD];
+  const long long it = S->iteration;
+  const bool stats_t = (it % I.dt_stat) == 0;
+  if (stats_t) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int qi = w; qi < Q_COUNT; qi += nw) {
+      double s = 0.0;
+      for (int c = lane; c < nparts; c += 32) s += I.partials[(long long)c * QPAD + qi];
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) tot[qi] = s;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  if (stats_t) {
+    S->nl_h = tot[Q_NLH]; S->nl_v = tot[Q_NLV];
+    S->press_h = tot[Q_PH]; S->press_v = tot[Q_PV];
+  }
+  if (mode == 1) {
+    // calculate_rhs! at initialize!: pressure_stats leaves its sum in reductionh[1]
+    if (stats_t && I.adaptive && I.ref_slot) S->slot_u = tot[Q_PH];
+    S->umax_bits = 0ull; S->rhomax_bits = 0ull;
+    return;
+  }
+  if (stats_t) {
+    const long long r = S->nrec;
+    if (r < I.rec_cap) {
+      double* row = I.records + r * I.ncols;
+      const double u12 = tot[Q_U12], u22 = tot[Q_U22], u32 = tot[Q_U32];
+      const double kh = (u12 + u22) / 2, kv = u32 / 2;
+      const double eh = I.nu * tot[Q_EH], ev = I.nu * tot[Q_EV];
+      const double nlh = tot[Q_NLH], nlv = tot[Q_NLV], ph = tot[Q_PH], pv = tot[Q_PV];
+      int c = 0;
+      row[c++] = (double)it; row[c++] = S->time;
+      row[c++] = tot[Q_U1]; row[c++] = tot[Q_U2]; row[c++] = tot[Q_U3];
+      row[c++] = u12; row[c++] = u22; row[c++] = u32;
+      row[c++] = kh; row[c++] = kv; row[c++] = 2 * kv / kh; row[c++] = kh + kv;
+      row[c++] = eh; row[c++] = ev; row[c++] = eh + ev;
+      row[c++] = nlh; row[c++] = nlv; row[c++] = ph; row[c++] = pv;
+      row[c++] = -(nlh + ph); row[c++] = nlv + pv;
+      double tdiss = eh + ev;
+      if (I.les) tdiss += -tot[Q_LESH] - tot[Q_LESV];
+      if (I.hv) tdiss += I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);
+      row[c++] = tdiss;
+      if (I.density) {
+        const double rd = I.alpha * (tot[Q_DR1] + tot[Q_DR2] + tot[Q_DR3]);
+        row[c++] = tot[Q_RHO]; row[c++] = tot[Q_RHO2]; row[c++] = tot[Q_DR1]; row[c++] = tot[Q_DR2];
+        row[c++] = tot[Q_DR3]; row[c++] = rd; row[c++] = rd; row[c++] = -I.gval * tot[Q_BF];
+      }
+      if (I.les) {
+        const double prh = -tot[Q_LESH], prv = -tot[Q_LESV];
+        row[c++] = prh; row[c++] = prv; row[c++] = (2 * prv) / prh; row[c++] = prh + prv;
+      }
+      if (I.forcing) {
+        const double dt = S->dt;
+        row[c++] = tot[Q_HP] / dt; row[c++] = tot[Q_VP] / dt; row[c++] = (tot[Q_HP] + tot[Q_VP]) / dt;
+      }
+      if (I.hv) {
+        row[c++] = I.hv_nu * tot[Q_HVH]; row[c++] = I.hv_nu * tot[Q_HVV]; row[c++] = I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);
+      }
+      // 9 integral-length plane sums and 4 derivative variances (Scales.txt inputs)
+      for (int i = 0; i < 9; ++i) row[c++] = tot[Q_IL0 + i];
+      row[c++] = tot[Q_D1DY]; row[c++] = tot[Q_D1DX]; row[c++] = tot[Q_D2DY]; row[c++] = tot[Q_D2DX];
+    }
+    S->nrec = r + 1;
+    if (I.adaptive && I.ref_slot) {
+      // the last reduction of writestats that reuses reductionh / density reduction
+      double slot = tot[Q_D2DX];
+      if (I.les) slot = tot[Q_LESH];
+      if (I.hv) slot = tot[Q_HVH];
+      S->slot_u = slot;
+      if (I.density) S->slot_rho = tot[Q_BF];
+    }
+  }
+  if (mode == 0 && (it % I.dt_spec) == 0) S->nspec += 1;
+  S->iteration = it + 1;
+  S->time += S->dt;
+  S->hist_parity ^= 1;
+  S->umax_bits = 0ull; S->rhomax_bits = 0ull;
+}
+
+// ====================================================================================
+// Transform-only helpers for set/get of physical fields (FP64 host layout
+// [z][y][x], unpadded).
+// ====================================================================================
+
+// physical -> wy slots (r2c along x), nf fields paired two per complex line
+template <typename T>
+__global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
+  constexpr int L = 2 * LYZ_IO;   // up to 4 fields -> 2 complex lines per (y,z)
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = I.nx;
+  cplx<T>* sx = reinterpret_cast<cplx<T>*>(smem_raw);   // [n][L+1]
+  cplx<T>* s0 = sx + n * (L + 1);
+  cplx<T>* s1 = s0 + n * L;
+  const int g0 = blockIdx.x * LYZ_IO;
+  const long long plane = (long long)I.ny * I.nz * n;
+  auto ld = [&](int l, int j) -> cplx<T> {
+    const int p = l / LYZ_IO, q = l % LYZ_IO;
+    const int fa = 2 * p, fb = 2 * p + 1;
+    const long long base = (long long)(g0 + q) * n + j;
+    const T a = fa < nf ? T(I.phys[fa * plane + base]) : T(0);
+    const T b = fb < nf ? T(I.phys[fb * plane + base]) : T(0);
+    return mk(a, b);
+  };
+  auto st = [&](int l, int j, cplx<T> v) { sx[j * (L + 1) + l] = v; };
+  fft_lines<-1, L, T>(I.px, s0, s1, L, I.twx, ld, st);
+  const int KXP = I.KXP;
+  for (int e = threadIdx.x; e < L * KXP; e += blockDim.x) {
+    const int k = e % KXP, l = e / KXP, p = l / LYZ_IO, q = l % LYZ_IO;
+    cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
+    if (k < I.Mx) {
+      const cplx<T> zk = sx[k * (L + 1) + l];
+      const cplx<T> zm = sx[((n - k) % n) * (L + 1) + l];
+      A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
+      B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+    }
+    const long long off = (long long)(g0 + q) * KXP + k;
+    if (2 * p < nf) I.wy[(long long)(slot0 + 2 * p) * I.wys + off] = A;
+    if (2 * p + 1 < nf) I.wy[(long long)(slot0 + 2 * p + 1) * I.wys + off] = B;
+  }
+}
+
+// wz slots -> compact spectral state: forward z, 1/N scaling, dealias (myfourier!)
+template <typename T, int TX>
+__global__ void __launch_bounds__(512) k_fwd_z_store(Inst<T> I, FieldList F) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + I.nz * TX;
+  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
+  const int rowstride = I.NYR * I.KXP;
+  const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
+  cplx<T>* out = I.uh + (long long)F.code[fi] * I.cstride + (long long)jc * I.KXP + kx0;
+  const T sc = T(I.inv_n);
+  auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
+  auto st = [&](int l, int z, cplx<T> v) {
+    const int kc = zcomp(I, z);
+    if (kc < 0) return;
+    out[(long long)kc * rowstride + l] = (kx0 + l < I.Mx) ? scl(v, sc) : mk(T(0), T(0));
+  };
+  fft_lines<-1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
+}
+
+// wy slots -> physical (c2r along x) into the FP64 staging buffer
+template <typename T>
+__global__ void k_inv_x_phys(Inst<T> I, int nf) {
+  constexpr int L = 2 * LYZ_IO;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = I.nx, Mx = I.Mx;
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + n * L;
+  const int g0 = blockIdx.x * LYZ_IO;
+  const long long plane = (long long)I.ny * I.nz * n;
+  auto ld = [&](int l, int j) -> cplx<T> {
+    const int p = l / LYZ_IO, q = l % LYZ_IO;
+    const bool cj = 2 * j > n;
+    const int k = cj ? n - j : j;
+    if (k >= Mx) return mk(T(0), T(0));
+    const int fa = 2 * p, fb = 2 * p + 1;
+    const long long off = (long long)(g0 + q) * I.KXP + k;
+    cplx<T> A = fa < nf ? I.wy[(long long)fa * I.wys + off] : mk(T(0), T(0));
+    cplx<T> B = fb < nf ? I.wy[(long long)fb * I.wys + off] : mk(T(0), T(0));
+    if (k == 0 || 2 * k == n) { A.y = T(0); B.y = T(0); }
+    if (cj) { A.y = -A.y; B.y = -B.y; }
+    return mk(A.x - B.y, A.y + B.x);
+  };
+  auto st = [&](int l, int j, cplx<T> v) {
+    const int p = l / LYZ_IO, q = l % LYZ_IO;
+    const long long base = (long long)(g0 + q) * n + j;
+    if (2 * p < nf) I.phys[(2 * p) * plane + base] = (double)v.x;
+    if (2 * p + 1 < nf) I.phys[(2 * p + 1) * plane + base] = (double)v.y;
+  };
+  fft_lines<+1, L, T>(I.px, s0, s1, L, I.twx, ld, st);
+}
+
+}  // namespace ffsgpu

@@ -1,0 +1,264 @@
+"""Host-side mirror of the reference's simulation API over libffs.
+
+``Simulation`` owns one engine handle (one GPU simulation). ``run_simulation`` mirrors
+``run_simulation()`` (src/FluidFlowSimulation.jl:23-65): it reads ``global`` and the
+``u1.$start``/``u2``/``u3`` (+``rho``) files, runs ``initialize!`` and the time loop on
+the GPU, and writes Stats.txt, the u spectra and the field files in the reference
+formats.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_double, c_int32, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from . import fields as _fields
+from ._lib import FFS_FP32, FFSError, FFSParams, load
+from .globalfile import parameters, readglobal
+
+_D = ctypes.POINTER(c_double)
+
+
+def _ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_D)
+
+
+def julia_float(x: float) -> str:
+    """Print a Float64 the way Julia's ``print`` does (shortest round-trip digits)."""
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "Inf" if x > 0 else "-Inf"
+    r = repr(float(x))
+    if "e" in r:
+        m, e = r.split("e")
+        if "." not in m:
+            m += ".0"
+        return f"{m}e{int(e)}"
+    if "." not in r:
+        r += ".0"
+    return r
+
+
+class Simulation:
+    """One GPU simulation (the reference's ``Simulation`` object, src/simulationtypes.jl:45-100)."""
+
+    def __init__(self, params: FFSParams):
+        self._L = load()
+        self.params = params
+        h = c_void_p()
+        rc = self._L.ffs_create(byref(params), byref(h))
+        if rc != 0:
+            raise FFSError(rc, self._L.ffs_last_error(None).decode())
+        self._h = h
+        self.nx, self.ny, self.nz = params.nx, params.ny, params.nz
+        self.ncols = self._L.ffs_stats_ncols(h)
+        self.rec_ncols = self._L.ffs_record_ncols(h)
+        buf = ctypes.create_string_buffer(4096)
+        self._check(self._L.ffs_stats_header(h, buf, 4096))
+        self.header = buf.value.decode()
+        lh, lv = c_int32(), c_int32()
+        self._check(self._L.ffs_spectrum_lengths(h, byref(lh), byref(lv)))
+        self.lenH, self.lenV = lh.value, lv.value
+        self.has_density = bool(params.density)
+
+    @classmethod
+    def from_global(cls, d: dict, precision: str | None = None, device: int = 0) -> "Simulation":
+        return cls(parameters(d, precision=precision, device=device))
+
+    # ---------------------------------------------------------------- plumbing
+    def _check(self, rc: int):
+        if rc != 0:
+            raise FFSError(rc, self._L.ffs_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.ffs_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------------- reference API
+    def set_fields(self, u1, u2, u3, rho=None, layout: int = 0):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (u1, u2, u3)]
+        r = None if rho is None else np.ascontiguousarray(rho, dtype=np.float64)
+        self._check(self._L.ffs_set_fields(self._h, _ptr(a[0]), _ptr(a[1]), _ptr(a[2]), _ptr(r), layout))
+
+    def initialize(self):
+        """``initialize!(s)`` (src/FluidFlowSimulation.jl:67-91)."""
+        self._check(self._L.ffs_initialize(self._h))
+
+    def advance_in_time(self, nsteps: int = 1):
+        """``advance_in_time!(s)`` repeated ``nsteps`` times (src/models.jl:3-17)."""
+        self._check(self._L.ffs_step(self._h, int(nsteps)))
+
+    def fields(self, layout: int = 0):
+        shape = (self.nz, self.ny, self.nx if layout == 0 else 2 * (self.nx // 2 + 1))
+        out = [np.empty(shape) for _ in range(4 if self.has_density else 3)]
+        rho = out[3] if self.has_density else None
+        self._check(self._L.ffs_get_fields(self._h, _ptr(out[0]), _ptr(out[1]), _ptr(out[2]), _ptr(rho), layout))
+        return tuple(out)
+
+    def spectral(self, comp: int) -> np.ndarray:
+        out = np.empty((self.nz, self.ny, self.nx // 2 + 1), dtype=np.complex128)
+        self._check(self._L.ffs_get_spectral(self._h, comp, out.ctypes.data_as(_D)))
+        return out
+
+    def set_spectral(self, comp: int, a: np.ndarray):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        self._check(self._L.ffs_set_spectral(self._h, comp, a.ctypes.data_as(_D)))
+
+    def records(self) -> np.ndarray:
+        """Pending stats records: Stats.txt columns then 13 Scales.txt inputs."""
+        n = self._L.ffs_stats_records(self._h, None, 0)
+        out = np.empty((max(n, 0), self.rec_ncols))
+        if n > 0:
+            self._L.ffs_stats_records(self._h, out.ctypes.data_as(_D), n)
+        return out
+
+    def stats_rows(self) -> np.ndarray:
+        return self.records()[:, : self.ncols]
+
+    def spectra(self) -> list[dict]:
+        rl = 1 + 2 * self.lenH + 2 * self.lenV
+        n = self._L.ffs_spectrum_records(self._h, None, 0)
+        out = np.empty((max(n, 0), rl))
+        if n > 0:
+            self._L.ffs_spectrum_records(self._h, out.ctypes.data_as(_D), n)
+        res = []
+        H, V = self.lenH, self.lenV
+        for r in out:
+            hH, hV = r[1:1 + H], r[1 + H:1 + H + V]
+            vH, vV = r[1 + H + V:1 + 2 * H + V], r[1 + 2 * H + V:]
+            res.append({"iteration": int(r[0]), "u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH,
+                        "u_v.specH": vH, "u_v.specV": vV})
+        return res
+
+    @property
+    def iteration(self) -> int:
+        return int(self._L.ffs_iteration(self._h))
+
+    @property
+    def time(self) -> float:
+        return float(self._L.ffs_time(self._h))
+
+    @property
+    def dt(self) -> float:
+        return float(self._L.ffs_dt(self._h))
+
+    # ---------------------------------------------------------------- timing
+    def time_steps(self, nsteps: int) -> float:
+        ms = c_double()
+        self._check(self._L.ffs_time_steps(self._h, int(nsteps), byref(ms)))
+        return ms.value
+
+    def profile_kernels(self, nsteps: int) -> dict[str, float]:
+        names = ctypes.create_string_buffer(1024)
+        ms = (c_double * 16)()
+        nk = c_int32()
+        self._check(self._L.ffs_profile_kernels(self._h, int(nsteps), names, 1024, ms, 16, byref(nk)))
+        keys = names.value.decode().split(",")
+        return {k: ms[i] for i, k in enumerate(keys[: nk.value])}
+
+    @property
+    def launches_per_step(self) -> int:
+        return int(self._L.ffs_launches_per_step(self._h))
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self._L.ffs_device_bytes(self._h))
+
+    @property
+    def stream(self) -> int:
+        return int(self._L.ffs_stream(self._h) or 0)
+
+
+# ----------------------------------------------------------------------------------
+# Reference output formats
+# ----------------------------------------------------------------------------------
+
+def stats_line(row) -> str:
+    """One Stats.txt row (``join(file,(init,time,results...,"\\n"),",","")``, stats.jl:44-46)."""
+    return ",".join([str(int(row[0]))] + [julia_float(v) for v in row[1:]]) + "\n"
+
+
+def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarray) -> None:
+    """``writespectrum("u", ...)`` (spec.jl:173-194): tab-separated (k, E) pairs."""
+    i = rec["iteration"]
+    for name, k in (("u_h.specH", KH), ("u_h.specV", KRZ), ("u.specH", KH), ("u_v.specH", KH), ("u_v.specV", KRZ)):
+        with open(folder / f"{name}.{i}", "w") as f:
+            for a, b in zip(k, rec[name]):
+                f.write(f"{julia_float(float(a))}\t{julia_float(float(b))}\n")
+
+
+def run_simulation(folder: str | Path = ".", precision: str | None = None, device: int = 0) -> Simulation:
+    """Mirror of ``run_simulation()`` (src/FluidFlowSimulation.jl:23-65) on the GPU engine."""
+    folder = Path(folder)
+    d = readglobal(folder / "global")
+    sim = Simulation.from_global(d, precision=precision, device=device)
+    p = sim.params
+    start = int(p.start)
+    u = [_fields.read_field(folder / f"u{i}.{start}", p.nx, p.ny, p.nz) for i in (1, 2, 3)]
+    rho = None
+    if p.density and (folder / f"rho.{start}").exists():
+        rho = _fields.read_field(folder / f"rho.{start}", p.nx, p.ny, p.nz)
+    sim.set_fields(*u, rho)
+    total = int(d["nt"]) if "nt" in d else (1 << 62) - start
+    lengthtime = float(d["timeDuration"]) if "timeDuration" in d else float("inf")
+    if start == 0:
+        (folder / "Stats.txt").write_text(sim.header + "\n")
+    sim.initialize()
+    final_step = start + total
+    final_time = p.start_time + lengthtime
+    kx1, ky1 = 1.0 / p.lx, 1.0 / p.ly
+    KH = (np.arange(p.nx // 2 + 1) / p.lx) if kx1 >= ky1 else (np.arange(p.ny // 2 + 1) / p.ly)
+    KRZ = np.arange(p.nz // 2 + 1) / p.lz
+    wt = int(p.write_time)
+
+    def flush():
+        rows = sim.stats_rows()
+        with open(folder / "Stats.txt", "a") as f:
+            for r in rows:
+                f.write(stats_line(r))
+        for rec in sim.spectra():
+            write_spectrum_files(folder, rec, KH, KRZ)
+
+    while sim.iteration < final_step and sim.time < final_time:
+        it = sim.iteration
+        nxt = min(final_step, (it // wt + 1) * wt)
+        if lengthtime != float("inf"):
+            nxt = it + 1       # time-limited runs check the clock every step
+        sim.advance_in_time(nxt - it)
+        flush()
+        if sim.iteration % wt == 0 and sim.iteration < final_step:
+            _write_output(folder, sim)
+    # tail of run_simulation (FluidFlowSimulation.jl:46-58): the final fields are written
+    # only when the last iteration is not a multiple of writeTime
+    flush()
+    if sim.iteration % wt != 0:
+        _write_output(folder, sim)
+    return sim
+
+
+def _write_output(folder: Path, sim: Simulation) -> None:
+    """``writeoutput`` (src/output.jl:1-8): u1.N u2.N u3.N (+ rho.N)."""
+    f = sim.fields()
+    i = sim.iteration
+    for k in range(3):
+        _fields.write_field(folder / f"u{k + 1}.{i}", f[k])
+    if sim.has_density:
+        _fields.write_field(folder / f"rho.{i}", f[3])

@@ -1,0 +1,150 @@
+/*
+ * ffs.h — C ABI of the GB300 pseudo-spectral solver-step engine (libffs.so).
+ *
+ * The engine replaces the body of FluidFlowSimulation.jl's time loop: the reference's
+ * `initialize!(s)` (src/FluidFlowSimulation.jl:67-91) and `advance_in_time!(s)`
+ * (src/models.jl:3-17) with everything they call. The reference has no FFI of its own
+ * (it extends through Julia multiple dispatch on the Simulation type parameters,
+ * src/simulationtypes.jl:45-100); these entry points are what a `ccall` shim mirroring
+ * `run_simulation()` (src/FluidFlowSimulation.jl:23-65) binds.
+ *
+ * Conventions: plain C types only; every function returns 0 on success or a negative
+ * FFS_E* code, with a message in ffs_last_error(). No exceptions or aborts cross the
+ * ABI. A handle is used by one host thread at a time; handles are independent and
+ * each owns a CUDA stream and all of its device memory. The library keeps no pointer
+ * to caller memory after a call returns.
+ *
+ * Field layout (same as the reference's PaddedArray, src/output.jl:6-8): Float64,
+ * x fastest, either unpadded nx*ny*nz (layout 0) or padded 2*(nx/2+1)*ny*nz (layout 1).
+ */
+#ifndef FFS_H
+#define FFS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFS_OK 0
+#define FFS_EINVAL (-1)
+#define FFS_ENOMEM (-2)
+#define FFS_ECUDA (-3)
+#define FFS_ENAN (-4)
+#define FFS_ETIMEDOUT (-5)
+#define FFS_EUNSUPPORTED (-6)
+#define FFS_ESTATE (-7)
+
+#define FFS_ETD3 0 /* ETD3rdO (src/time_step_functions/ETD.jl) */
+#define FFS_AB3 1  /* Adams_Bashforth3rdO (src/time_step_functions/Adams_Bashforth.jl) */
+
+#define FFS_FP64 0
+#define FFS_FP32 1
+
+typedef struct ffs_handle ffs_handle;
+
+/* Mirrors the in-scope keys of the `global` file read by parameters()
+ * (src/simulationtypes.jl:242-365, src/Globals.jl:106-183). */
+typedef struct ffs_params {
+  int32_t nx, ny, nz;          /* nx ny nz */
+  double lx, ly, lz;           /* xDomainSize.. in units of 2 pi: k = i / L */
+  double nu;                   /* kinematicViscosity */
+  double cutoff;               /* cutoff (dealias ratio), default 2/3 */
+  int32_t integrator;          /* velocityTimeStep: FFS_ETD3 | FFS_AB3 */
+  int32_t variable_dt;         /* variableTimestepFlag (default 1) */
+  double cfl;                  /* cfl, default 0.18 */
+  double dt;                   /* dt (fixed dt, or the initial value) */
+  int32_t hyperviscosity;      /* hyperViscosity present */
+  double hv_nu;                /* hyperViscosityCoefficient */
+  int32_t hv_m;                /* hyperViscosityM, default 2 */
+  int32_t les;                 /* lesModel Smagorinsky */
+  double smag_c;               /* smagorinskyConstant, default 0.17 */
+  double filter_width;         /* filterWidth (<= 0: reference default (lx 2pi/nx)/cutoff) */
+  int32_t density;             /* densityStratification */
+  double density_pr;           /* Pr */
+  double density_gradient;     /* densityGradient */
+  double gravity;              /* zAcceleration / referenceDensity */
+  int32_t gravity_dir;         /* gravityDirection: 0 x, 1 y, 2 z */
+  int32_t forcing;             /* forcing isotropicBand (no reference counterpart) */
+  double forcing_power;        /* forcingPower (epsilon) */
+  double forcing_kf;           /* forcingKf */
+  int32_t precision;           /* FFS_FP64 | FFS_FP32 */
+  int32_t dt_stat;             /* dtStat */
+  int32_t dt_spec;             /* dtSpec */
+  int32_t write_time;          /* writeTime */
+  int64_t start;               /* start */
+  double start_time;           /* startTime */
+  int32_t device;              /* CUDA device ordinal */
+  int32_t reference_cfl_slot;  /* 1: CFL uses the reference's reused reduction slot */
+  int32_t stats_capacity;      /* stats records kept on the device between reads */
+  int32_t spec_capacity;       /* spectrum records kept on the device between reads */
+} ffs_params;
+
+/* Fill defaults: reference defaults for every key that has one. */
+int ffs_params_default(ffs_params* p);
+
+/* Build a simulation (parameters(), src/simulationtypes.jl:242-365). */
+int ffs_create(const ffs_params* p, ffs_handle** h);
+
+/* Load physical fields (the reference reads u1.N u2.N u3.N [rho.N],
+ * src/simulationtypes.jl:276, src/density_stratification_types.jl:166).
+ * rho may be NULL (zero density). layout 0: nx*ny*nz, 1: padded 2*(nx/2+1)*ny*nz. */
+int ffs_set_fields(ffs_handle* h, const double* u1, const double* u2, const double* u3, const double* rho,
+                   int32_t layout);
+
+/* initialize!(s) (src/FluidFlowSimulation.jl:67-91): forward transform, first
+ * right-hand side, integrator history. */
+int ffs_initialize(ffs_handle* h);
+
+/* advance_in_time!(s) nsteps times (src/models.jl:3-17). Records Stats rows at
+ * iterations multiple of dtStat and u spectra at multiples of dtSpec on the device. */
+int ffs_step(ffs_handle* h, int64_t nsteps);
+
+/* Physical fields at the current iteration (real!(s.u), src/output.jl:1-8). */
+int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout);
+
+/* Spectral state as the reference's s.u.c: complex128 half spectrum [nz][ny][nx/2+1]
+ * (interleaved re,im; zero outside the retained box). comp: 0..2 velocity, 3 density. */
+int ffs_get_spectral(ffs_handle* h, int32_t comp, double* out);
+int ffs_set_spectral(ffs_handle* h, int32_t comp, const double* in);
+
+/* Stats.txt header (statsheader, src/stats.jl:1-7) and number of columns per row. */
+int ffs_stats_header(const ffs_handle* h, char* buf, int64_t len);
+int32_t ffs_stats_ncols(const ffs_handle* h);
+/* Columns kept per record: the Stats.txt columns, then 9 integral-length plane sums
+ * and 4 derivative variances (inputs of Scales.txt, src/stats.jl:74-109). */
+int32_t ffs_record_ncols(const ffs_handle* h);
+/* Move up to max_rows pending stats records to the host (oldest first). */
+int64_t ffs_stats_records(ffs_handle* h, double* out, int64_t max_rows);
+
+/* u spectra (spectrum_u + calculate_specHV, src/spec.jl:316-327,424-450):
+ * lengths of the H and V spectra, then pending records of
+ * [iteration, u_h.specH(lenH), u_h.specV(lenV), u_v.specH(lenH), u_v.specV(lenV)]. */
+int ffs_spectrum_lengths(const ffs_handle* h, int32_t* lenH, int32_t* lenV);
+int64_t ffs_spectrum_records(ffs_handle* h, double* out, int64_t max_rows);
+
+int64_t ffs_iteration(const ffs_handle* h);
+double ffs_time(const ffs_handle* h);
+double ffs_dt(const ffs_handle* h);
+
+/* Timing: run nsteps steps and return the elapsed device time (CUDA events on the
+ * handle's stream, steps captured in a CUDA graph). */
+int ffs_time_steps(ffs_handle* h, int64_t nsteps, double* ms);
+/* Per-kernel timing of nsteps steps launched one kernel at a time with CUDA events
+ * around each launch. names: comma-separated kernel names; ms: per kernel total. */
+int ffs_profile_kernels(ffs_handle* h, int64_t nsteps, char* names, int64_t names_len, double* ms, int32_t max_k,
+                        int32_t* nk);
+/* Kernel launches per step (for launch counting). */
+int32_t ffs_launches_per_step(const ffs_handle* h);
+/* Device bytes held by the handle. */
+int64_t ffs_device_bytes(const ffs_handle* h);
+/* The handle's cudaStream_t. */
+void* ffs_stream(const ffs_handle* h);
+
+const char* ffs_last_error(const ffs_handle* h);
+void ffs_destroy(ffs_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFS_H */

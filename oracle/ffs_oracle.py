@@ -1,0 +1,815 @@
+"""FP64 CPU restatement of FluidFlowSimulation.jl's solver step.
+
+TEST INFRASTRUCTURE ONLY. This module is the checker that the GPU engine is compared
+against; it is never part of the product path. It restates, operation for operation,
+the reference's Julia code for one time step (``advance_in_time!``) and everything it
+calls. Citations are ``file:line`` inside the reference project (``src/...``).
+
+Parity status: the reference is pure Julia and needs Julia + FFTW, neither of which
+exists in this environment, and its only test is a placeholder (``test/runtests.jl:5``).
+This restatement is therefore pinned by analytic known-answer tests (Taylor-Green
+invariants, exact linear decay under ETD, divergence-free projection, energy budget,
+forcing power) rather than by reference outputs. FFTW is replaced by pocketfft
+(``scipy.fft``); both are FP64 FFTs accurate to ~1e-16 relative.
+
+Conventions (same memory order as the reference's column-major Julia arrays):
+  physical arrays:  real  [z, y, x]           (x fastest)
+  spectral arrays:  complex [z, y, kx], kx in 0..nx/2 (half spectrum), x fastest
+"""
+from __future__ import annotations
+
+import math
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+import scipy.fft as sfft
+
+_WORKERS = int(os.environ.get("FFS_ORACLE_WORKERS", os.cpu_count() or 1))
+
+
+# ----------------------------------------------------------------------------------
+# Grid tables — src/Globals.jl
+# ----------------------------------------------------------------------------------
+
+def rfftfreq(n: int, s: float) -> np.ndarray:
+    """``rfftfreq`` of ``src/Globals.jl:95-97``: ``[(n/2 - i)/s for i = n/2:-1:0]``."""
+    i = np.arange(n / 2, -1.0, -1.0)
+    return (n / 2 - i) / s
+
+
+def fftfreq(n: int, s: float) -> np.ndarray:
+    """``fftfreq`` of ``src/Globals.jl:99-104`` (Nyquist negative for even n)."""
+    if n % 2 == 0:
+        a = (n / 2 - np.arange(n / 2, 0.0, -1.0)) / s
+        b = -np.arange(n / 2, 0.0, -1.0) / s
+        return np.concatenate([a, b])
+    a = (n / 2 - np.arange(n / 2, -0.5, -1.0)) / s
+    b = -np.arange((n - 1) / 2, 0.0, -1.0) / s
+    return np.concatenate([a, b])
+
+
+@dataclass
+class Grid:
+    """Wavenumber tables, dealias mask and retained ranges (``src/Globals.jl:106-171``)."""
+
+    nx: int
+    ny: int
+    nz: int
+    lx: float = 1.0
+    ly: float = 1.0
+    lz: float = 1.0
+    cutoff: float = 2.0 / 3.0
+
+    def __post_init__(self):
+        self.nxh = self.nx // 2 + 1
+        self.kx = rfftfreq(self.nx, self.lx)            # Globals.jl:119
+        self.ky = fftfreq(self.ny, self.ly)             # Globals.jl:120
+        self.kz = fftfreq(self.nz, self.lz)             # Globals.jl:121
+        c = self.cutoff
+        cx = (c * self.kx[-1]) ** 2                     # Globals.jl:136
+        cy = (c * np.max(np.abs(self.ky))) ** 2         # Globals.jl:137
+        cz = (c * np.max(np.abs(self.kz))) ** 2         # Globals.jl:138
+        KX = self.kx[None, None, :]
+        KY = self.ky[None, :, None]
+        KZ = self.kz[:, None, None]
+        # DEALIAS[i,j,k] = kx^2 > cx | ky^2 > cy | kz^2 > cz   (Globals.jl:142)
+        self.dealias = (KX ** 2 > cx) | (KY ** 2 > cy) | (KZ ** 2 > cz)
+        self.keep = ~self.dealias
+        self.KX, self.KY, self.KZ = KX, KY, KZ
+        # K2 = muladd(KX,KX, muladd(KY,KY,KZ*KZ))   (ETD.jl:66)
+        self.K2 = KX * KX + (KY * KY + KZ * KZ)
+        self.N = self.nx * self.ny * self.nz
+        # 1D spectrum bins (Globals.jl:144-152, spec.jl:424-450)
+        self.KH = self.kx if self.kx[1] >= self.ky[1] else rfftfreq(self.ny, self.ly)
+        self.MAXDKH = self.KH[1]
+        self.KRZ = rfftfreq(self.nz, self.lz)
+        self.DKZ = self.KRZ[1]
+        # weight for the Hermitian half spectrum: 1 + (i > 1) (stats.jl:301)
+        self.w = np.where(np.arange(self.nxh) > 0, 2.0, 1.0)[None, None, :]
+
+    # --- transforms (utils.jl:101-106; FluidFields real!) ---------------------------------
+    def myfourier(self, phys: np.ndarray) -> np.ndarray:
+        """Forward: unnormalised r2c, zero the DEALIAS modes, times 1/(nx ny nz)."""
+        c = sfft.rfftn(phys, axes=(-3, -2, -1), workers=_WORKERS)
+        c[..., self.dealias] = 0.0
+        c *= 1.0 / self.N
+        return c
+
+    def real(self, spec: np.ndarray) -> np.ndarray:
+        """Inverse: unnormalised c2r (FFTW brfft semantics)."""
+        return sfft.irfftn(spec, s=(self.nz, self.ny, self.nx), axes=(-3, -2, -1),
+                           norm="forward", workers=_WORKERS)
+
+    def project(self, v: np.ndarray) -> np.ndarray:
+        """``pressure_projection!`` (models.jl:443-456): v - k (k.v)/k^2, k=0 untouched."""
+        kd = self.KX * v[0] + self.KY * v[1] + self.KZ * v[2]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            p1 = -kd / self.K2
+        p1[0, 0, 0] = 0.0
+        return np.stack([p1 * self.KX + v[0], p1 * self.KY + v[1], p1 * self.KZ + v[2]])
+
+
+# ----------------------------------------------------------------------------------
+# Parameters — src/simulationtypes.jl:242-365 (in-scope keys only)
+# ----------------------------------------------------------------------------------
+
+def _num(s: str) -> float:
+    """Parse a `global` numeric value (the reference runs ``eval(Meta.parse(...))``).
+
+    Supports plain numbers, ``Inf`` and products/quotients with ``π``/``pi`` such as
+    ``2π`` or ``2pi/128``.
+    """
+    import re
+    t = s.strip().replace("π", "pi")
+    t = re.sub(r"(\d)\s*pi", r"\1*pi", t)
+    return float(eval(t, {"__builtins__": {}}, {"pi": math.pi, "Inf": math.inf}))
+
+
+@dataclass
+class Params:
+    nx: int = 32
+    ny: int = 32
+    nz: int = 32
+    lx: float = 1.0
+    ly: float = 1.0
+    lz: float = 1.0
+    nu: float = 0.0
+    cutoff: float = 2.0 / 3.0
+    integrator: str = "ETD3rdO"          # or "Adams_Bashforth3rdO"
+    variable_dt: bool = True
+    cfl: float = 0.18
+    dt: float = 0.0
+    hv: bool = False
+    hv_nu: float = 0.0
+    hv_m: int = 2
+    les: bool = False
+    smag_c: float = 0.17
+    filter_width: float | None = None
+    density: bool = False
+    density_pr: float = 1.0
+    density_gradient: float = 0.0
+    gravity: float = 0.0                 # zAcceleration / referenceDensity
+    gravity_dir: int = 2                 # 0 x, 1 y, 2 z
+    forcing: bool = False
+    forcing_power: float = 0.1
+    forcing_kf: float = 2.5
+    dt_stat: int = 1
+    dt_spec: int = 1
+    write_time: int = 1 << 30
+    start: int = 0
+    start_time: float = 0.0
+    reference_cfl_slot: bool = True
+
+    @classmethod
+    def from_global(cls, d: dict) -> "Params":
+        """Mirror ``parameters(d)`` (simulationtypes.jl:242-365) for the in-scope keys."""
+        p = cls()
+        p.nx, p.ny, p.nz = int(d["nx"]), int(d["ny"]), int(d["nz"])
+        p.lx, p.ly, p.lz = _num(d["xDomainSize"]), _num(d["yDomainSize"]), _num(d["zDomainSize"])
+        p.nu = _num(d["kinematicViscosity"])
+        if "cutoff" in d:
+            p.cutoff = _num(d["cutoff"])
+        p.start = int(d.get("start", 0))
+        p.start_time = float(d.get("startTime", 0.0))
+        p.dt_stat = int(d["dtStat"])
+        p.dt_spec = int(d["dtSpec"])                       # KeyError like :262
+        p.write_time = int(d["writeTime"])
+        p.integrator = d.get("velocityTimeStep", "ETD3rdO")
+        p.variable_dt = d.get("variableTimestepFlag", "true").strip().lower() == "true"
+        p.cfl = float(d.get("cfl", 0.18))
+        p.dt = _num(d["dt"]) if "dt" in d else 0.0
+        if "hyperViscosity" in d:
+            p.hv = True
+            p.hv_nu = float(d["hyperViscosityCoefficient"])
+            p.hv_m = int(d.get("hyperViscosityM", 2))
+        if d.get("lesModel") == "Smagorinsky":
+            p.les = True
+            p.smag_c = _num(d.get("smagorinskyConstant", "0.17"))
+            p.filter_width = (_num(d["filterWidth"]) if "filterWidth" in d
+                              else (p.lx * 2 * math.pi / p.nx) / p.cutoff)   # les_types.jl:366
+        if "densityStratification" in d:
+            p.density = True
+            p.density_pr = _num(d["Pr"])
+            p.density_gradient = _num(d["densityGradient"])
+            p.gravity = _num(d["zAcceleration"]) / _num(d["referenceDensity"])
+            p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
+        if d.get("forcing") == "isotropicBand":
+            p.forcing = True
+            p.forcing_power = _num(d.get("forcingPower", "0.1"))
+            p.forcing_kf = _num(d.get("forcingKf", "2.5"))
+        if "referenceCflSlot" in d:
+            p.reference_cfl_slot = d["referenceCflSlot"].strip().lower() == "true"
+        return p
+
+    @property
+    def ab3(self) -> bool:
+        return self.integrator == "Adams_Bashforth3rdO"
+
+
+# ----------------------------------------------------------------------------------
+# Time integrators — src/time_step_functions/*.jl
+# ----------------------------------------------------------------------------------
+
+class AB3:
+    """Adams-Bashforth 3 (Adams_Bashforth.jl:1-128) with the Euler/AB2 start-up."""
+
+    def __init__(self, adaptive: bool, idt: float):
+        self.adaptive = adaptive
+        self.dt = self.dt2 = self.dt3 = idt            # Adams_Bashforth.jl:13-23
+        self.iteration = 0
+        self.fm1 = None
+        self.fm2 = None
+
+    def initialize(self, rhs, dt_now):
+        """Adams_Bashforth.jl:28-35: fm1 = fm2 = rhs, dt history = current dt."""
+        self.fm1 = rhs.copy()
+        self.fm2 = rhs.copy()
+        self.dt = dt_now
+        self.dt2 = self.dt
+        self.dt3 = self.dt
+
+    def set_dt(self, dt):
+        """Adams_Bashforth.jl:37-47 (adaptive only)."""
+        if not self.adaptive:
+            return
+        if self.iteration == 0:
+            self.dt3 = self.dt2 = self.dt = dt / 2
+        else:
+            self.dt3 = self.dt2
+            self.dt2 = self.dt
+            self.dt = dt
+
+    def coefficients(self):
+        """Adaptive formulas (Adams_Bashforth.jl:49-89); fixed dt: 23/12, -16/12, 5/12 dt."""
+        dt, dt2, dt3 = self.dt, self.dt2, self.dt3
+        if not self.adaptive:
+            return 23 * dt / 12, -16 * dt / 12, 5 * dt / 12
+        At = (1.0 + (dt * (2 * dt + 6 * dt2 + 3 * dt3)) / (6 * dt2 * (dt2 + dt3))) * dt
+        Bt = (-dt * dt * (2 * dt + 3 * dt2 + 3 * dt3) / (6 * dt2 * dt3 * (dt + dt2))) * (dt + dt2)
+        Ct = (dt * dt * (2 * dt + 3 * dt2) / (6 * dt3 * (dt + dt2 + dt3) * (dt2 + dt3))) * (dt + dt2 + dt3)
+        return At, Bt, Ct
+
+    def step(self, u, rhs, explicit=None):
+        """Adams_Bashforth.jl:102-128 (+ fix_fm2! at the second call, ETD.jl:130-140)."""
+        self.iteration += 1
+        if self.iteration == 2:
+            self.fm2 = -(self.dt3 + self.dt2) * (rhs - self.fm1) / self.dt2 + rhs
+        At, Bt, Ct = self.coefficients()
+        unew = At * rhs + (Bt * self.fm1 + (Ct * self.fm2 + u))
+        self.fm2 = self.fm1
+        self.fm1 = rhs.copy()
+        return unew
+
+
+class ETD3:
+    """Exponential time differencing, 3rd order (ETD.jl:3-261, ETD1stand2ndO.jl:1-66)."""
+
+    def __init__(self, adaptive: bool, idt: float, c: np.ndarray):
+        self.adaptive = adaptive
+        self.dt = self.dt2 = self.dt3 = idt            # ETD.jl:33-36
+        self.iteration = 0
+        self.c = c                                      # c = -nu k^2 (- nuh k^2M)
+        self.fm1 = None
+        self.fm2 = None
+        self.At = self.Bt = self.Ct = None
+
+    def set_dt(self, dt):
+        """ETD.jl:110-114 — rotates on every call when adaptive."""
+        if not self.adaptive:
+            return
+        self.dt3 = self.dt2
+        self.dt2 = self.dt
+        self.dt = dt
+
+    def initialize(self, rhs, dt_now):
+        """ETD.jl:99-108."""
+        self.fm1 = rhs.copy()
+        self.fm2 = rhs.copy()
+        self.dt = dt_now
+        self.dt2 = self.dt
+        self.dt3 = self.dt
+        self.set_dt(self.dt)
+        if not self.adaptive:
+            self.set_ABCt()
+
+    def set_ABCt(self):
+        """ETD.jl:142-227 (Taylor branch when -c dt <= 1e-4, zero when c == -Inf)."""
+        l1 = self.c
+        dt, dt2, dt3 = self.dt, self.dt2, self.dt3
+        a0 = (dt * (2 * dt * dt + 6 * dt2 * (dt2 + dt3) + 3 * dt * (2 * dt2 + dt3))) / (6 * dt2 * (dt2 + dt3))
+        a1 = (dt * dt * (dt ** 2 + 6 * dt2 * (dt2 + dt3) + 2 * dt * (2 * dt2 + dt3))) / (12 * dt2 * (dt2 + dt3))
+        a2 = (dt * dt * dt * (4 * dt2 * (dt2 + dt3) + dt * (2 * dt2 + dt3))) / (24 * dt2 * (dt2 + dt3))
+        a3 = dt * dt * dt * dt / 24
+        b0 = -((dt ** 2 * (2 * dt + 3 * (dt2 + dt3))) / (6 * (dt2 * dt3)))
+        b1 = -(((dt * dt * dt * (dt + 2 * (dt2 + dt3)))) / (12 * (dt2 * dt3)))
+        b2 = -((dt * dt * dt * dt * (dt2 + dt3)) / (24 * (dt2 * dt3)))
+        c0 = (dt * dt * (2 * dt + 3 * dt2)) / (6 * dt3 * (dt2 + dt3))
+        c1 = (dt * dt * dt * (dt + 2 * dt2)) / (12 * dt3 * (dt2 + dt3))
+        c2 = (dt * dt * dt * dt * dt2) / (24 * dt3 * (dt2 + dt3))
+        e1 = dt ** 2 + dt * (2 * dt2 + dt3)
+        e2 = dt2 * (dt2 + dt3)
+        e3 = 2 * dt
+        e4 = 2 * dt2 + dt3
+        e5 = dt * (dt + dt2 + dt3)
+        e6 = dt2 + dt3
+        e7 = dt2 * dt3
+        e8 = dt * (dt + dt2)
+        e9 = dt3 * (dt2 + dt3)
+        l2 = l1 * l1
+        l3 = l2 * l1
+        test = -l1 * dt <= 1e-4
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            em = np.expm1(l1 * dt)
+            At = np.where(test, a1 * l1 + (a2 * l2 + (a3 * l3 + a0)),
+                          (2 * em - l2 * (e1 - e2 * em) - l1 * (e3 - e4 * em)) / (l3 * e2))
+            Bt = np.where(test, b1 * l1 + (b2 * l2 + b0),
+                          (e5 * l2 - 2 * em + l1 * (e3 - e6 * em)) / (l3 * e7))
+            Ct = np.where(test, c1 * l1 + (c2 * l2 + c0),
+                          (2 * em - e8 * l2 - l1 * (e3 - dt2 * em)) / (l3 * e9))
+        inf = l1 == -np.inf
+        self.At = np.where(inf, 0.0, At)
+        self.Bt = np.where(inf, 0.0, Bt)
+        self.Ct = np.where(inf, 0.0, Ct)
+
+    def step(self, u, rhs):
+        """ETD.jl:229-247: ETD1 at call 1, ETD2 at call 2, ETD3 afterwards."""
+        self.iteration += 1
+        c = self.c
+        dt = self.dt
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            if self.iteration == 1:                   # ETD1stand2ndO.jl:12-26
+                cdt = c * dt
+                cdt2 = cdt * dt
+                c2dt3 = cdt2 * cdt
+                c3dt4 = c2dt3 * cdt
+                test = -cdt <= 1e-4
+                phi = np.where(test, dt + 0.5 * cdt2 + c2dt3 / 6 + c3dt4 / 24, np.expm1(cdt) / c)
+                phi = np.where(c == -np.inf, 0.0, phi)
+                unew = np.exp(cdt) * u + phi * rhs
+            elif self.iteration == 2:                 # ETD1stand2ndO.jl:37-66
+                dt2 = self.dt2
+                cp2 = c * c
+                cdt = c * dt
+                cdtp2 = cdt * dt
+                c2dtp3 = cdtp2 * cdt
+                c3dtp4 = c2dtp3 * cdt
+                em = np.expm1(cdt)
+                c2dt2 = c * c * dt2
+                dtp2 = dt * dt
+                dtp3 = dtp2 * dt
+                dtp4 = dtp3 * dt
+                test = -cdt <= 1e-4
+                At = np.where(test,
+                              dt + cdtp2 / 2 + c2dtp3 / 6 + c3dtp4 / 24 + dtp2 / (2 * dt2)
+                              + (c * dtp3) / (6 * dt2) + (cp2 * dtp4) / (24 * dt2),
+                              (em - c * (dt - dt2 * em)) / c2dt2)
+                Bt = np.where(test, (-(dtp2 / (2 * dt2)) - (c * dtp3) / (6 * dt2) - (cp2 * dtp4) / (24 * dt2)),
+                              (cdt - em) / c2dt2)
+                inf = c == -np.inf
+                At = np.where(inf, 0.0, At)
+                Bt = np.where(inf, 0.0, Bt)
+                unew = np.exp(cdt) * u + (At * rhs + Bt * self.fm1)
+            else:
+                if self.adaptive:                     # set_coefficients!, ETD.jl:116-123
+                    self.set_ABCt()
+                unew = self.At * rhs + (self.Bt * self.fm1 + (self.Ct * self.fm2 + np.exp(c * dt) * u))
+        self.fm2 = self.fm1
+        self.fm1 = rhs.copy()
+        return unew
+
+
+# ----------------------------------------------------------------------------------
+# The simulation — src/models.jl, src/FluidFlowSimulation.jl
+# ----------------------------------------------------------------------------------
+
+STATS_HEADER = ("iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,"
+                "nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss")
+
+
+def stats_header(p: Params) -> str:
+    """``statsheader`` (stats.jl:1-7); plug-in order = sim_fields (macros.jl:48)."""
+    cols = [STATS_HEADER]
+    if p.density:
+        cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux")
+    if p.les:
+        cols.append("prh,prv,praniso,pr")
+    if p.forcing:
+        cols.append("hp,vp,tp")
+    if p.hv:
+        cols.append("hdissh,hdissv,hdiss")
+    return ",".join(cols)
+
+
+def _proj(a, b):
+    """``proj(a,b)`` (forcing.jl:4): Re(a) Re(b) + Im(a) Im(b)."""
+    return a.real * b.real + a.imag * b.imag
+
+
+class OracleSimulation:
+    """FP64 restatement of the reference Simulation for the in-scope plug-ins."""
+
+    def __init__(self, p: Params, u_phys, rho_phys=None):
+        self.p = p
+        g = self.g = Grid(p.nx, p.ny, p.nz, p.lx, p.ly, p.lz, p.cutoff)
+        self.iteration = p.start
+        self.time = p.start_time
+        self.u = np.stack([np.asarray(x, dtype=np.float64) for x in u_phys])   # physical at first
+        self.rho = None
+        if p.density:
+            self.rho = (np.zeros((p.nz, p.ny, p.nx)) if rho_phys is None
+                        else np.asarray(rho_phys, dtype=np.float64))
+        c = -p.nu * g.K2                                     # init_c!, ETD.jl:60-69
+        if p.hv:
+            c = g.K2 * (-p.nu) + (g.K2 ** p.hv_m) * (-p.hv_nu)  # init_c_hv!, ETD.jl:84-95
+        if p.ab3:
+            self.ts = AB3(p.variable_dt, p.dt)
+        else:
+            self.ts = ETD3(p.variable_dt, p.dt, c)
+        if p.density:
+            alpha = p.nu / p.density_pr
+            if p.ab3:
+                self.rts = AB3(p.variable_dt, p.dt)
+            else:
+                self.rts = ETD3(p.variable_dt, p.dt, -alpha * g.K2)
+            self.alpha = alpha
+        self.gvec = np.zeros(3)
+        if p.density:
+            self.gvec[p.gravity_dir] = p.gravity
+        # reference reductionh[1] / density reduction[1] with Julia threads = 1
+        self.slot_u = 0.0
+        self.slot_rho = 0.0
+        self.nlstats = (1.0, 1.0)
+        self.pressstats = (1.0, 1.0)
+        self.stats_rows = []
+        self.spectra = {}
+        self.force = None
+        self.hp = self.vp = 0.0
+        self.umax_hist = []
+
+    # ---------------------------------------------------------------- time helpers
+    def get_dt(self):
+        return self.ts.dt
+
+    def is_stats_time(self):
+        return self.iteration % self.p.dt_stat == 0
+
+    def is_spec_time(self):
+        return self.iteration % self.p.dt_spec == 0
+
+    # ---------------------------------------------------------------- initialize!
+    def initialize(self):
+        """``initialize!(s)`` (FluidFlowSimulation.jl:67-91)."""
+        g = self.g
+        self.u = g.myfourier(self.u)
+        if self.p.density:
+            self.rho = g.myfourier(self.rho)
+        self.calculate_rhs()
+        dt_now = self.get_dt()
+        self.ts.initialize(self.rhs, dt_now)
+        if self.p.density:
+            self.rts.initialize(self.rhorhs, dt_now)
+
+    # ---------------------------------------------------------------- calculate_rhs!
+    def calculate_rhs(self):
+        """``calculate_rhs!`` (models.jl:19-51)."""
+        p, g = self.p, self.g
+        u = self.u
+        KX, KY, KZ = g.KX, g.KY, g.KZ
+        stats_t = self.is_stats_time()
+        spec_t = self.is_spec_time()
+        # fourierspacep1! (models.jl:63-119): w = (i k) x u ; S = symouter(i k, u)
+        ikx, iky, ikz = 1j * KX, 1j * KY, 1j * KZ
+        w = np.stack([iky * u[2] - ikz * u[1], ikz * u[0] - ikx * u[2], ikx * u[1] - iky * u[0]])
+        if p.les:
+            S = np.stack([ikx * u[0], 0.5 * (ikx * u[1] + iky * u[0]), 0.5 * (ikx * u[2] + ikz * u[0]),
+                          iky * u[1], 0.5 * (iky * u[2] + ikz * u[1])])
+        # realspace! (models.jl:121-214)
+        ur = g.real(u)
+        wr = g.real(w)
+        kspec = None
+        if spec_t or stats_t:                                     # :130-134
+            kspec = g.myfourier(0.5 * (ur[0] * ur[0] + ur[1] * ur[1] + ur[2] * ur[2]))
+        if p.density:
+            rhor = g.real(self.rho)
+        if p.les:
+            Sr = g.real(S)
+            # calc_les! Smagorinsky (les_real_calc.jl:77-79): nu_t = c^2 D^2 |S|, tau = 2 nu_t S
+            xx, xy, xz, yy, yz = Sr
+            zz = -xx - yy
+            nrm = np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
+            alpha_les = p.smag_c * p.smag_c * p.filter_width ** 2
+            nut = alpha_les * nrm
+            taur = 2.0 * nut[None] * Sr
+        # realspacecalculation! (models.jl:236-280): rhs = u x w ; flux = -rho u
+        nl = np.stack([ur[1] * wr[2] - ur[2] * wr[1], ur[2] * wr[0] - ur[0] * wr[2],
+                       ur[0] * wr[1] - ur[1] * wr[0]])
+        if p.density:
+            flux = -rhor[None] * ur
+        if p.variable_dt:                                         # find_max, utils.jl:247-258
+            m = float(np.max(np.abs(ur)))
+            self.slot_u = max(m, self.slot_u) if p.reference_cfl_slot else m
+            self.umax_hist.append(m)
+            if p.density:
+                mr = float(np.max(np.abs(rhor)))
+                self.slot_rho = max(mr, self.slot_rho) if p.reference_cfl_slot else mr
+        nlh = g.myfourier(nl)
+        nlh[:, 0, 0, 0] = 0.0                                     # models.jl:174
+        # u round trip + projection (models.jl:192-193)
+        self.u = u = g.project(g.myfourier(ur))
+        if p.density:
+            fluxh = g.myfourier(flux)
+            self.rho = g.myfourier(rhor)
+        tauh = g.myfourier(taur) if p.les else None
+        # set_dt! (time_step_functions.jl:86-129)
+        if p.variable_dt:
+            self.set_dt()
+        if spec_t:
+            self.spectra[self.iteration] = self.spectrum_u()
+        if stats_t:                                               # models.jl:38-46
+            self.nlstats = self.non_linear_stats(nlh, kspec)
+            self.pressstats = self.pressure_stats(nlh, kspec, tauh)
+        # fourierspacep2! (models.jl:282-364)
+        rhs = nlh.copy()
+        if p.ab3:                                                 # explicit viscosity :320-326
+            if p.hv:
+                rhs = rhs + (g.K2 * (-p.nu) + (g.K2 ** p.hv_m) * (-p.hv_nu))[None] * u
+            else:
+                rhs = rhs + (g.K2 * (-p.nu))[None] * u
+        if p.les:                                                 # :328-332
+            rhs = rhs + self.div_tau(tauh)
+        if p.density:                                             # :334-336
+            for d in range(3):
+                if self.gvec[d] != 0.0:
+                    rhs[d] = rhs[d] + self.rho * self.gvec[d]
+        rhs = g.project(rhs)                                      # :338-339
+        rhs[:, g.dealias] = 0.0
+        self.rhs = rhs
+        self.kspec = kspec
+        self.tauh = tauh
+        if p.density:                                             # div!, vectorfunctions.jl:93-103
+            wdir = u[p.gravity_dir]
+            rr = 1j * (KX * fluxh[0] + (KY * fluxh[1] + KZ * fluxh[2])) + (-p.density_gradient) * wdir
+            if p.ab3:
+                rr = rr + (-self.alpha * g.K2) * self.rho
+            rr[g.dealias] = 0.0
+            self.rhorhs = rr
+
+    def div_tau(self, tauh):
+        """(i k) . tau for a symmetric traceless tau (models.jl:330)."""
+        g = self.g
+        xx, xy, xz, yy, yz = tauh
+        zz = -xx - yy
+        ikx, iky, ikz = 1j * g.KX, 1j * g.KY, 1j * g.KZ
+        return np.stack([ikx * xx + iky * xy + ikz * xz,
+                         ikx * xy + iky * yy + ikz * yz,
+                         ikx * xz + iky * yz + ikz * zz])
+
+    # ---------------------------------------------------------------- set_dt!
+    def set_dt(self):
+        """``set_dt!(s)`` (time_step_functions.jl:86-129)."""
+        p, g = self.p, self.g
+        umax = self.slot_u
+        dx = 2 * math.pi * p.ly / p.ny
+        cfl = p.cfl
+        it = self.iteration
+        if it == 0:
+            cfl *= 0.1
+        elif it == 1:
+            cfl *= 0.2
+        elif it == 2:
+            cfl *= 0.4
+        elif it == 3:
+            cfl *= 0.8
+        with np.errstate(divide="ignore"):
+            newdt = cfl * dx / umax if umax != 0 else math.inf
+        if p.density:
+            rmax = self.slot_rho
+            gn = abs(p.gravity)
+            den = rmax * gn
+            cap = cfl * math.sqrt(dx / den) if den > 0 else math.inf
+            newdt = min(newdt, cap)
+        if it > 3:
+            dt = self.get_dt()
+            if newdt < dt:
+                newdt = max(dt / 1.25, newdt)
+            else:
+                newdt = min(1.25 * dt, newdt)
+        self.ts.set_dt(newdt)
+        if p.density:
+            self.rts.set_dt(newdt)
+
+    # ---------------------------------------------------------------- forcing (new)
+    def compute_forcing(self):
+        """Isotropic band forcing at constant power (no reference counterpart).
+
+        E_f = sum_{0<|k|<=kf} 1/2 w |u|^2 ; f = dt * eps/(2 E_f) * u on that band,
+        applied after the integrator like the reference's add_forcing! hook
+        (forcing_types.jl:49-64, time_step_functions.jl:72-80).
+        """
+        p, g = self.p, self.g
+        u = self.u
+        band = (g.K2 <= p.forcing_kf ** 2) & (g.K2 > 0) & g.keep
+        w = g.w
+        e = 0.5 * w * (np.abs(u[0]) ** 2 + np.abs(u[1]) ** 2 + np.abs(u[2]) ** 2)
+        Ef = float(np.sum(e[band]))
+        coef = p.forcing_power / (2.0 * Ef) if Ef > 0 else 0.0
+        dt = self.get_dt()
+        f = np.where(band[None], (dt * coef) * u, 0.0)
+        self.force = f
+        wb = np.broadcast_to(w, band.shape)
+        sh = _proj(u[0], f[0]) + _proj(u[1], f[1]) + 0.5 * (np.abs(f[0]) ** 2 + np.abs(f[1]) ** 2)
+        sv = _proj(u[2], f[2]) + 0.5 * np.abs(f[2]) ** 2
+        self.hp = float(np.sum((wb * sh)[band])) / dt
+        self.vp = float(np.sum((wb * sv)[band])) / dt
+
+    # ---------------------------------------------------------------- advance_in_time!
+    def advance(self):
+        """``advance_in_time!`` (models.jl:3-17)."""
+        p, g = self.p, self.g
+        self.calculate_rhs()
+        if p.forcing:
+            self.compute_forcing()
+        if self.is_stats_time():
+            self.write_stats()
+        # time_step! (models.jl:468-472) -> VectorTimeStep (time_step_functions.jl:72-80)
+        if p.ab3:
+            u = self.ts.step(self.u, self.rhs)
+        else:
+            u = self.ts.step(self.u, self.rhs)
+        if p.forcing:
+            u = u + self.force
+        self.u = g.project(u)
+        self.u[:, g.dealias] = 0.0
+        if p.density:
+            self.rho = self.rts.step(self.rho, self.rhorhs)
+            self.rho[g.dealias] = 0.0
+        self.iteration += 1
+        self.time += self.get_dt()
+
+    def run(self, nsteps):
+        for _ in range(nsteps):
+            self.advance()
+
+    def finalize(self):
+        """Tail of ``run_simulation`` (FluidFlowSimulation.jl:46-49)."""
+        self.calculate_rhs()
+        if self.p.forcing:
+            self.compute_forcing()
+        self.write_stats()
+
+    # ---------------------------------------------------------------- stats
+    def _wsum(self, a):
+        return float(np.sum(self.g.w * a))
+
+    def non_linear_stats(self, nl, ke):
+        """stats.jl:897-917."""
+        g = self.g
+        u = self.u
+        r = [nl[0] - 1j * g.KX * ke, nl[1] - 1j * g.KY * ke, nl[2] - 1j * g.KZ * ke]
+        h = self._wsum(_proj(r[0], u[0]) + _proj(r[1], u[1]))
+        v = self._wsum(_proj(r[2], u[2]))
+        if self.p.variable_dt and self.p.reference_cfl_slot:
+            self.slot_u = h
+        return h, v
+
+    def pressure_stats(self, nl, ke, tauh):
+        """stats.jl:750-814."""
+        p, g = self.p, self.g
+        u = self.u
+        r = np.stack([nl[0] - 1j * ke * g.KX, nl[1] - 1j * ke * g.KY, nl[2] - 1j * ke * g.KZ])
+        if p.les:
+            r = r + self.div_tau(tauh)
+        if p.density:
+            for d in range(3):
+                if self.gvec[d] != 0.0:
+                    r[d] = r[d] + self.rho * self.gvec[d]
+        kd = g.KX * r[0] + g.KY * r[1] + g.KZ * r[2]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            p1 = -kd / g.K2
+        p1[0, 0, 0] = 0.0
+        h = self._wsum(_proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY))
+        v = self._wsum(_proj(u[2], p1 * g.KZ))
+        if self.p.variable_dt and self.p.reference_cfl_slot:
+            self.slot_u = h
+        return h, v
+
+    def velocity_row(self):
+        """``velocity_stats`` + ``stats`` (stats.jl:64-219), Stats.txt column order."""
+        p, g = self.p, self.g
+        u = self.u
+        a2 = [np.abs(u[i]) ** 2 for i in range(3)]
+        u12, u22, u32 = (self._wsum(a) for a in a2)
+        kh = (u12 + u22) / 2
+        kv = u32 / 2
+        k = kh + kv
+        kaniso = 2 * kv / kh
+        eh_raw = self._wsum(g.K2 * (a2[0] + a2[1]))
+        ev_raw = self._wsum(g.K2 * a2[2])
+        eh, ev = p.nu * eh_raw, p.nu * ev_raw
+        nlh, nlv = self.nlstats
+        ph, pv = self.pressstats
+        row = [u[0][0, 0, 0].real, u[1][0, 0, 0].real, u[2][0, 0, 0].real, u12, u22, u32,
+               kh, kv, kaniso, k, eh, ev, eh + ev, nlh, nlv, ph, pv, -(nlh + ph), (nlv + pv)]
+        tdiss = eh + ev
+        extra = []
+        slot = None
+        # derivative variances used for the Taylor scales (stats.jl:79-94); the last one
+        # (dx_squared_mean of u2) is what stays in reductionh[1]
+        slot = self._wsum(g.KX ** 2 * a2[1])
+        if p.density:
+            rho = self.rho
+            r2 = np.abs(rho) ** 2
+            rho2 = self._wsum(r2)
+            d1 = self._wsum(g.KX ** 2 * r2)
+            d2 = self._wsum(g.KY ** 2 * r2)
+            d3 = self._wsum(g.KZ ** 2 * r2)
+            rhodiss = self.alpha * (d1 + d2 + d3)
+            bf_raw = self._wsum(_proj(u[p.gravity_dir], rho))
+            bflux = -self.gvec[p.gravity_dir] * bf_raw
+            extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss, bflux]
+            if p.variable_dt and p.reference_cfl_slot:
+                self.slot_rho = bf_raw
+        if p.les:
+            t = self.div_tau(self.tauh)
+            hraw = self._wsum(_proj(t[0], u[0]) + _proj(t[1], u[1]))
+            vraw = self._wsum(_proj(t[2], u[2]))
+            prh, prv = -hraw, -vraw
+            extra += [prh, prv, (2 * prv) / prh, prh + prv]
+            tdiss += prh + prv
+            slot = hraw
+        if p.forcing:
+            extra += [self.hp, self.vp, self.hp + self.vp]
+        if p.hv:
+            hraw = self._wsum((g.K2 ** p.hv_m) * (a2[0] + a2[1]))
+            vraw = self._wsum((g.K2 ** p.hv_m) * a2[2])
+            extra += [p.hv_nu * hraw, p.hv_nu * vraw, p.hv_nu * (hraw + vraw)]
+            tdiss += p.hv_nu * (hraw + vraw)
+            slot = hraw
+        if p.variable_dt and p.reference_cfl_slot:
+            self.slot_u = slot
+        return row + [tdiss] + extra
+
+    def write_stats(self):
+        """``writestats`` (stats.jl:39-62): one Stats.txt row."""
+        self.stats_rows.append([float(self.iteration), float(self.time)] + self.velocity_row())
+
+    # ---------------------------------------------------------------- spectra
+    def spectrum_u(self):
+        """``spectrum_u`` + ``calculate_specHV`` (spec.jl:316-327, 424-450).
+
+        Returns dict with the horizontal/vertical parts binned into H and V spectra:
+        keys 'u_h.specH', 'u_h.specV', 'u.specH', 'u_v.specH', 'u_v.specV'.
+        """
+        u = self.u
+        hout = 0.5 * (_proj(u[0], u[0]) + _proj(u[1], u[1]))
+        vout = 0.5 * _proj(u[2], u[2])
+        hH, hV = self.calculate_specHV(hout)
+        vH, vV = self.calculate_specHV(vout)
+        return {"u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH,
+                "u_v.specH": vH, "u_v.specV": vV}
+
+    def calculate_specHV(self, out):
+        """spec.jl:424-450 (kx = 0 plane without the dk factors, as in the reference)."""
+        g = self.g
+        h = np.zeros(len(g.KH))
+        v = np.zeros(len(g.KRZ))
+        nk = np.rint(np.abs(g.kz) / g.DKZ).astype(np.int64)
+        nj = np.rint(np.abs(g.ky) / g.MAXDKH).astype(np.int64)
+        nx = np.rint(np.abs(g.kx) / g.MAXDKH).astype(np.int64)
+        keep = g.keep
+        o = np.where(keep, out, 0.0)
+        # i = 1 (kx = 0) terms
+        e0 = o[:, :, 0]
+        h[0] += 0.5 * float(np.sum(e0))
+        np.add.at(h, nj, 0.5 * np.sum(e0, axis=0))
+        np.add.at(v, nk, np.sum(e0, axis=1))
+        # i >= 2 terms
+        e = 2.0 * o[:, :, 1:]
+        np.add.at(h, nx[1:], 0.5 * g.MAXDKH * np.sum(e, axis=(0, 1)))
+        np.add.at(h, nj, 0.5 * g.MAXDKH * np.sum(e, axis=(0, 2)))
+        np.add.at(v, nk, g.DKZ * np.sum(e, axis=(1, 2)))
+        return h, v
+
+    # ---------------------------------------------------------------- accessors
+    def u_physical(self):
+        return self.g.real(self.u)
+
+    def rho_physical(self):
+        return self.g.real(self.rho)
+
+
+# ----------------------------------------------------------------------------------
+# Small helpers used by the known-answer tests
+# ----------------------------------------------------------------------------------
+
+def taylor_green(n: int):
+    """README.md:12-20: u1 = cos x sin y sin z, u2 = -sin x cos y sin z, u3 = 0."""
+    x = 2 * np.pi * np.arange(n) / n
+    X = x[None, None, :]
+    Y = x[None, :, None]
+    Z = x[:, None, None]
+    u1 = np.cos(X) * np.sin(Y) * np.sin(Z)
+    u2 = -np.sin(X) * np.cos(Y) * np.sin(Z)
+    u3 = np.zeros((n, n, n))
+    return u1, u2, u3

@@ -1,0 +1,155 @@
+"""Host logic on CPU: the C ABI library loads and exports what include/ffs.h declares,
+the `global` parser and parameter mapping, file formats and initial conditions."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def header_functions():
+    src = (ROOT / "include" / "ffs.h").read_text()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(ffs_[a-z_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    import __graft_entry__ as ge
+    if not pkg.lib_available():
+        ge.build()
+    L = pkg.load()
+    names = header_functions()
+    assert set(names) == set(pkg.EXPORTS)
+    for n in names:
+        assert hasattr(L, n), n
+
+
+def test_params_default_matches_reference_defaults(pkg):
+    p = pkg.FFSParams()
+    assert pkg.load().ffs_params_default(ctypes.byref(p)) == 0
+    assert p.cutoff == pytest.approx(2 / 3)          # Globals.jl:132
+    assert p.cfl == pytest.approx(0.18)              # simulationtypes.jl:310
+    assert p.integrator == pkg.FFS_ETD3              # simulationtypes.jl:308
+    assert p.variable_dt == 1                        # simulationtypes.jl:309
+    assert p.hv_m == 2 and p.smag_c == pytest.approx(0.17)
+
+
+def test_create_without_gpu_fails_cleanly(pkg):
+    """No GPU here: ffs_create must return an error code and a message, not crash."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = pkg.FFSParams()
+    L = pkg.load()
+    L.ffs_params_default(ctypes.byref(p))
+    h = ctypes.c_void_p()
+    rc = L.ffs_create(ctypes.byref(p), ctypes.byref(h))
+    assert rc < 0
+    assert L.ffs_last_error(None)
+
+
+def test_readglobal_and_parameters(pkg, tmp_path):
+    (tmp_path / "global").write_text("""// comment
+kinematicViscosity 0.03333333
+xDomainSize 1.0
+yDomainSize 1.0
+zDomainSize 2π
+
+nx 64
+ny 64
+nz 64
+nt 500
+dt 0.05
+dtStat 20
+dtSpec 20
+writeTime 100
+velocityTimeStep Adams_Bashforth3rdO
+variableTimestepFlag false
+hyperViscosity true
+hyperViscosityCoefficient 1e-12
+forcing isotropicBand
+forcingPower 0.1
+forcingKf 2.5
+precision FP32
+""")
+    d = pkg.readglobal(tmp_path / "global")
+    assert d["zDomainSize"] == "2π" and d["nt"] == "500"
+    p = pkg.parameters(d)
+    assert (p.nx, p.ny, p.nz) == (64, 64, 64)
+    assert p.lz == pytest.approx(2 * np.pi)
+    assert p.integrator == pkg.FFS_AB3 and p.variable_dt == 0 and p.dt == pytest.approx(0.05)
+    assert p.hyperviscosity == 1 and p.hv_nu == pytest.approx(1e-12) and p.hv_m == 2
+    assert p.forcing == 1 and p.precision == pkg.FFS_FP32
+    assert p.dt_stat == 20 and p.dt_spec == 20 and p.write_time == 100
+
+
+def test_parameters_requires_dtspec(pkg):
+    """The reference raises KeyError without dtSpec (simulationtypes.jl:262)."""
+    d = {"nx": "8", "ny": "8", "nz": "8", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+         "kinematicViscosity": "0.1", "dtStat": "1", "writeTime": "1"}
+    with pytest.raises(KeyError):
+        pkg.parameters(d)
+
+
+def test_parameters_rejects_out_of_scope_models(pkg):
+    d = {"nx": "8", "ny": "8", "nz": "8", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+         "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1", "lesModel": "Vreman"}
+    with pytest.raises(ValueError):
+        pkg.parameters(d)
+
+
+def test_parse_number(pkg):
+    assert pkg.parse_number("2π") == pytest.approx(2 * np.pi)
+    assert pkg.parse_number("2pi/128") == pytest.approx(2 * np.pi / 128)
+    assert pkg.parse_number("1e-3") == 1e-3
+    with pytest.raises(ValueError):
+        pkg.parse_number("__import__('os')")
+
+
+def test_julia_float_formatting(pkg):
+    assert pkg.julia_float(0.125) == "0.125"
+    assert pkg.julia_float(1.0) == "1.0"
+    assert pkg.julia_float(1e-5) == "1.0e-5"
+    assert pkg.julia_float(2.5e-20) == "2.5e-20"
+    assert pkg.stats_line([20.0, 1.0, 0.5]) == "20,1.0,0.5\n"
+
+
+def test_field_file_roundtrip(pkg, tmp_path):
+    a = np.random.default_rng(0).standard_normal((4, 6, 8))
+    pkg.write_field(tmp_path / "u1.0", a)
+    assert (tmp_path / "u1.0").stat().st_size == 8 * a.size
+    b = pkg.read_field(tmp_path / "u1.0", 8, 6, 4)
+    assert np.array_equal(a, b)
+    pad = np.zeros((4, 6, 10))
+    pad[:, :, :8] = a
+    pad.astype("<f8").tofile(str(tmp_path / "u2.0"))
+    assert np.array_equal(pkg.read_field(tmp_path / "u2.0", 8, 6, 4), a)
+
+
+def test_random_spectrum_properties(pkg):
+    u = pkg.random_spectrum(32, k0=4.0, seed=3)
+    urms = np.sqrt(np.mean(u[0] ** 2 + u[1] ** 2 + u[2] ** 2) / 3)
+    assert urms == pytest.approx(1.0, rel=1e-12)
+    uh = [np.fft.rfftn(x) for x in u]
+    k = np.fft.fftfreq(32, 1 / 32)
+    kx = np.arange(17)
+    div = kx[None, None, :] * uh[0] + k[None, :, None] * uh[1] + k[:, None, None] * uh[2]
+    assert np.abs(div).max() < 1e-10 * np.abs(uh[0]).max()
+    # reproducible for a seed, different for another
+    assert np.array_equal(u[0], pkg.random_spectrum(32, k0=4.0, seed=3)[0])
+    assert not np.array_equal(u[0], pkg.random_spectrum(32, k0=4.0, seed=4)[0])
+    # dealiased: nothing beyond |k| = n/3 on each axis
+    assert np.abs(uh[0][:, :, 11:]).max() < 1e-10
+
+
+def test_taylor_green_matches_readme(pkg):
+    u1, u2, u3 = pkg.taylor_green(16)
+    x = 2 * np.pi * 3 / 16
+    y = 2 * np.pi * 5 / 16
+    z = 2 * np.pi * 7 / 16
+    assert u1[7, 5, 3] == pytest.approx(np.cos(x) * np.sin(y) * np.sin(z))
+    assert u2[7, 5, 3] == pytest.approx(-np.sin(x) * np.cos(y) * np.sin(z))
+    assert not u3.any()
