@@ -1,0 +1,349 @@
+"""Benchmark: steps/s of the pseudo-spectral solver step, forced isotropic DNS 256^3.
+
+Workload (the FP32 chosen form of the forced-DNS configuration): seeded random-phase,
+divergence-free field with E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 4, u_rms = 1; isotropic band
+forcing |k| <= 2.5 at constant power eps = 0.1; nu = 1e-3; AB3 with adaptive dt (CFL 0.5);
+2/3 dealiasing; stats every 100 steps. A step is one advance_in_time! (one CUDA-graph
+launch of the whole step). The FP64 plain form is timed beside it and the FP32 error
+against FP64 after 10 steps is stated.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--grid n]
+
+N > 1 runs under torchrun as independent replicas (one per GPU, no collective on the data
+path); value = steps of all ranks / max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "steps/s at 256^3 FP32 (forced isotropic DNS), FP64 plain form and FP32 L2 error stated"
+NU, K0, EPS, KF, CFL, DTSTAT = 1e-3, 4.0, 0.1, 2.5, 0.5, 100
+
+
+def global_dict(n: int) -> dict:
+    return {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+            "zDomainSize": "1.0", "kinematicViscosity": str(NU), "dtStat": str(DTSTAT), "dtSpec": "1000000000",
+            "writeTime": "1000000000", "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true",
+            "cfl": str(CFL), "dt": "0.001", "forcing": "isotropicBand", "forcingPower": str(EPS),
+            "forcingKf": str(KF)}
+
+
+def workload_name(n: int) -> str:
+    return (f"forced isotropic DNS {n}^3: random-phase E(k)~k^4 exp(-2(k/4)^2) u_rms=1, band forcing "
+            f"|k|<=2.5 eps=0.1, nu=1e-3, AB3 CFL 0.5, 2/3 dealias, stats every {DTSTAT} steps")
+
+
+# ---------------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (clocks and throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------------- helpers
+def measured_peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel: str, n: int, prec: str) -> float | None:
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary (profiles/traffic.txt)."""
+    p = ROOT / "profiles" / "traffic.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        f = ln.split()
+        if len(f) >= 4 and not ln.startswith("#") and f[0] == kernel and f[1] == str(n) and f[2] == prec:
+            return float(f[3])
+    return None
+
+
+def algorithmic_bytes(n: int, elem: int) -> dict[str, float]:
+    """Minimal bytes each pass must move for the velocity-only step (retained modes only).
+
+    C = Mx*NYR*NZR (compact spectral component), V = Mx*NYR*n (after the z pass),
+    U = Mx*n*n (after the y pass), complex elements of `elem` bytes.
+    """
+    mx = int(math.floor((2.0 / 3.0) * (n // 2) + 1e-12)) + 1
+    nr = 2 * mx - 1
+    C, V, U = mx * nr * nr * elem, mx * nr * n * elem, mx * n * n * elem
+    return {"inv_z": 3 * C + 6 * V, "inv_y": 6 * V + 6 * U, "x_pass": 6 * U + 3 * U, "fwd_y": 3 * U + 3 * V,
+            "fwd_z_update": 3 * V + 9 * C + 6 * C, "step": 3 * C + 6 * V + 6 * V + 6 * U + 6 * U + 3 * U + 3 * U
+            + 3 * V + 3 * V + 15 * C}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cuda_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except ImportError:
+        pass
+
+
+# ---------------------------------------------------------------------------------- arms
+def cpu_reference_rate(n: int, budget_s: float, max_steps: int, warmup: int) -> tuple[float, int, int]:
+    """The FP64 CPU oracle (a port of the reference step) on this host's cores."""
+    import numpy as np
+    import __graft_entry__ as ge
+    from oracle.ffs_oracle import OracleSimulation, Params
+    pkg = ge.load_package()
+    u = pkg.random_spectrum(n, k0=K0, seed=2001)
+    s = OracleSimulation(Params.from_global(global_dict(n)), u)
+    s.initialize()
+    for _ in range(warmup):
+        s.advance()
+    t0 = time.perf_counter()
+    k = 0
+    while k < max_steps:
+        s.advance()
+        k += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("FFS_ORACLE_WORKERS", os.cpu_count() or 1))
+    del np
+    return k / dt, k, cores
+
+
+def run_reference_arm(args):
+    world, rank, local, dist = dist_setup(args)
+    if rank != 0:
+        return 0
+    n = args.grid
+    rate, k, cores = cpu_reference_rate(n, budget_s=args.ref_budget, max_steps=args.steps,
+                                        warmup=min(args.warmup, 1))
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
+            "steps": k, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 / rate, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": workload_name(n), "grid": n, "implementation": "FP64 CPU port of the reference "
+                       "step (numpy + scipy.fft pocketfft); the Julia/FFTW reference cannot run on this box"},
+            "cpu_baseline": {"value": rate, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": f"{k} timed steps of the {n}^3 workload after 1 warm-up step "
+                                       f"(budget {args.ref_budget:.0f} s)"},
+            "e2e": {"value": rate, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_engine_arm(args):
+    import numpy as np
+    import __graft_entry__ as ge
+    world, rank, local, dist = dist_setup(args)
+    pkg = ge.load_package()
+    pkg.load()
+    n = args.grid
+    d = global_dict(n)
+    u = pkg.random_spectrum(n, k0=K0, seed=2001)
+
+    def make(prec):
+        p = pkg.parameters(d, precision=prec, device=local)
+        sim = pkg.Simulation(p)
+        sim.set_fields(*u)
+        sim.initialize()
+        return sim
+
+    # --- device-resident throughput, FP32 chosen form
+    sim = make("FP32")
+    sim.advance_in_time(max(args.warmup, 3))
+    cuda_sync()
+    barrier(dist)
+    with ClockSampler(local) as clk:
+        ms = sim.time_steps(args.steps)
+    cuda_sync()
+    barrier(dist)
+    ms = max_over_ranks(dist, ms)
+    steps_s = args.steps * world / (ms / 1e3)
+    launches = sim.launches_per_step * args.steps
+    prof = sim.profile_kernels(max(5, min(20, args.steps)))
+    nprof = max(5, min(20, args.steps))
+    dev_bytes = sim.device_bytes
+    sim.close()
+
+    # --- FP64 plain form
+    sim64 = make("FP64")
+    sim64.advance_in_time(3)
+    k64 = max(5, args.steps // 10)
+    ms64 = sim64.time_steps(k64)
+    sim64.close()
+
+    # --- FP32 vs FP64 error after 10 steps (same initial fields)
+    a, b = make("FP32"), make("FP64")
+    a.advance_in_time(10)
+    b.advance_in_time(10)
+    err = max(float(np.linalg.norm(a.spectral(c) - b.spectral(c)) / np.linalg.norm(b.spectral(c)))
+              for c in range(3))
+    a.close()
+    b.close()
+
+    # --- end to end through the public API with host buffers
+    nb = 3 * u[0].nbytes
+    host = [np.ascontiguousarray(x) for x in u]
+    cuda_sync()
+    t0 = time.perf_counter()
+    e = pkg.Simulation(pkg.parameters(d, precision="FP32", device=local))
+    e.set_fields(*host)
+    e.initialize()
+    e.advance_in_time(args.steps)
+    rows = e.stats_rows()
+    out = e.fields()
+    t1 = time.perf_counter()
+    e.close()
+    e2e_s = max_over_ranks(dist, t1 - t0)
+    e2e_rate = args.steps * world / e2e_s
+
+    if rank != 0:
+        return 0
+    # --- roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    alg = algorithmic_bytes(n, 8)
+    top = max(prof, key=prof.get)
+    top_ms = prof[top] / nprof
+    achieved = alg.get(top, 0.0) / (top_ms / 1e3) / 1e9
+    traffic = ncu_traffic(top, n, "fp32")
+    cpu_rate, cpu_k, cores = (None, 0, 0)
+    if not args.no_cpu:
+        cpu_rate, cpu_k, cores = cpu_reference_rate(n, budget_s=args.cpu_budget, max_steps=50, warmup=1)
+    clocks = clk.summary()
+    line = {
+        "metric": METRIC, "value": steps_s, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(n), "grid": n, "precision": "FP32 transforms/products/updates, "
+                   "FP64 twiddles, phi-coefficients and reductions", "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2: {dev_bytes / 1e9:.2f} GB resident per GPU"},
+        "grid_point_updates_per_s": steps_s * n ** 3,
+        "fp64": {"value": k64 / (ms64 / 1e3), "unit": "steps/s", "ms_per_step": ms64 / k64, "steps": k64},
+        "fp32_speedup_vs_fp64": (steps_s / world) / (k64 / (ms64 / 1e3)),
+        "fp32_vs_fp64_rel_l2_10_steps": err,
+        "kernels_ms_per_step": {k: v / nprof for k, v in prof.items()},
+        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg.get(top), "step_algorithmic_bytes": alg["step"],
+                     "step_frac": alg["step"] / (ms / args.steps / 1e3) / 1e9 / peak},
+        "cpu_baseline": ({"value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": "port",
+                          "sample": f"{cpu_k} steps of the same {n}^3 workload, FP64 numpy/pocketfft oracle"}
+                         if cpu_rate else None),
+        "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": nb / args.steps,
+                "d2h_bytes_per_step": (sum(x.nbytes for x in out) + rows.nbytes) / args.steps,
+                "includes": "Simulation(), set_fields (host), initialize, advance_in_time(K), stats rows, "
+                            "get_fields (host)"},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=120.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+    return run_engine_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

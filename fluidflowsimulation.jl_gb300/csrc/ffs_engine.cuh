@@ -45,7 +45,7 @@ inline bool make_plan(int n, FftPlan& P) {
   P.n = n; P.np = np;
   int mx = 0;
   for (int i = 0; i < 4; ++i) { P.r[i] = r[i]; mx = std::max(mx, r[i]); }
-  P.tpl = n / mx;
+  P.tpl = n / mx;   // threads per line: one butterfly each in the largest-radix pass
   return true;
 }
 
@@ -55,6 +55,7 @@ template <typename T>
 class Engine : public EngineBase {
  public:
   static constexpr int TX = sizeof(T) == 4 ? 8 : 4;   // kx lines per CTA in the y/z passes
+  static constexpr int MAXT = 512;   // threads per CTA (launch bounds)
   Inst<T> I;
   ffs_params P;
   cudaStream_t s = nullptr;
@@ -64,7 +65,9 @@ class Engine : public EngineBase {
   int nin = 0, nout = 0;
   int lyz = 4;
   int txz = TX;               // kx lines per CTA in the forward z pass
+  int txy = TX;               // kx lines per CTA in the single-field y/z passes
   int nparts = 0;
+  int upd_blocks = 1;
   size_t smem_z = 0, smem_y = 0, smem_x = 0, smem_zu = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -141,13 +144,28 @@ class Engine : public EngineBase {
     retained(p.nz, p.lz, p.cutoff, false, zp, zc);
     I.Mx = xc; I.KXP = ((xc + 7) / 8) * 8;
     I.ypos = yp; I.NYR = yc; I.zpos = zp; I.NZR = zc;
-    I.uniformL = (p.lx == p.ly && p.ly == p.lz);
-    lyz = p.nx <= 256 ? 4 : 1;
-    if (((long long)p.ny * p.nz) % lyz != 0 || ((long long)p.ny * p.nz) % LYZ_IO != 0) {
-      err = "ny*nz must be a multiple of 4"; return FFS_EUNSUPPORTED;
+    {
+      // tabulate ETD coefficients by q = i^2 + j^2 + l^2 when k^2 = q / L^2 is exact
+      int ex = 0;
+      const double mant = frexp(p.lx, &ex);
+      I.uniformL = (p.lx == p.ly && p.ly == p.lz && mant == 0.5);
     }
+    // tile sizes: threads per CTA = lines * tpl must stay within the launch bounds
+    txy = TX;
+    while (txy > TX / 2 && txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) txy /= 2;
+    if (txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) { err = "grid size too large for this precision"; return FFS_EUNSUPPORTED; }
+    {
+      const int pin = ((6 + (p.les ? 5 : 0) + (p.density ? 1 : 0)) + 1) / 2;
+      lyz = 4;
+      while (lyz > 1 && pin * lyz * I.px.tpl > MAXT) lyz /= 2;
+      if (pin * lyz * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
+    }
+    if (((long long)p.ny * p.nz) % 4 != 0) { err = "ny*nz must be a multiple of 4"; return FFS_EUNSUPPORTED; }
+    if (2 * LYZ_IO * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
     txz = TX;
-    if (p.nz > 512) txz = TX / 2;
+    while (txz > 1 && 3 * txz * I.pz.tpl > MAXT) txz /= 2;
+    if (3 * txz * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
+    if (txz < TX / 4) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
 
     // physics
     I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
@@ -161,6 +179,10 @@ class Engine : public EngineBase {
     I.dgrad = p.density_gradient; I.gval = p.gravity;
     I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
     I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
+    I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
+    I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
+    I.inv_n_t = (T)I.inv_n; I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
+    I.gval_t = (T)p.gravity; I.dgrad_t = (T)p.density_gradient; I.kf2_t = (T)(p.forcing_kf * p.forcing_kf);
 
     // field lists
     nin = 0;
@@ -211,8 +233,18 @@ class Engine : public EngineBase {
     if ((rc = alloc(&I.wz, (size_t)nslots * I.wzs, err))) return rc;
     if ((rc = alloc(&I.wy, (size_t)nslots * I.wys, err))) return rc;
     if ((rc = alloc(&I.st, 1, err))) return rc;
-    nparts = (I.KXP / txz) * I.NYR;
+    {
+      int sms = 0;
+      FFS_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device));
+      nparts = 2 * std::max(sms, 1);   // CTAs of the stats kernel
+    }
     if ((rc = alloc(&I.partials, (size_t)nparts * QPAD, err))) return rc;
+    if ((rc = alloc(&I.sbuf, (size_t)((I.les || I.density) ? 8 : 4) * I.cstride, err))) return rc;
+    {
+      int sms = 0;
+      FFS_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device));
+      upd_blocks = (int)std::min<long long>((I.cstride + 255) / 256, (long long)sms * 16);
+    }
     // record layout
     ncols_stats = 22 + (I.density ? 8 : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
     ncols_rec = ncols_stats + 13;
@@ -229,26 +261,28 @@ class Engine : public EngineBase {
     I.spec_cap = p.spec_capacity > 0 ? p.spec_capacity : 16;
     if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 4 * std::max(lenH, lenV), err))) return rc;
     // ETD tables
-    if (!I.ab3 && I.uniformL) {
+    if (!I.ab3) {
       const long long a = I.Mx - 1, b = std::max(I.ypos - 1, I.NYR - I.ypos), c = std::max(I.zpos - 1, I.NZR - I.zpos);
       I.qmax = (int)(a * a + b * b + c * c);
-      if ((rc = alloc(&I.etab, (size_t)4 * (I.qmax + 1), err))) return rc;
-      if (I.density && (rc = alloc(&I.etab_rho, (size_t)4 * (I.qmax + 1), err))) return rc;
+      const size_t entries = I.uniformL ? (size_t)I.qmax + 1 : (size_t)I.cstride;
+      if ((rc = alloc(&I.etab, 4 * entries, err))) return rc;
+      if (I.density && (rc = alloc(&I.etab_rho, 4 * entries, err))) return rc;
     }
     // staging for two physical FP64 fields
     if ((rc = alloc(&I.phys, (size_t)2 * p.nx * p.ny * p.nz, err))) return rc;
 
     // launch geometry / shared memory
     const size_t cb = sizeof(cplx<T>);
-    smem_z = (size_t)TX * p.nz * cb * (I.pz.np >= 3 ? 2 : 1);
-    smem_y = (size_t)TX * p.ny * cb * (I.py.np >= 3 ? 2 : 1);
+    smem_z = (size_t)txy * p.nz * cb * (I.pz.np >= 3 ? 2 : 1);
+    smem_y = (size_t)txy * p.ny * cb * (I.py.np >= 3 ? 2 : 1);
     {
       const int PIN = (nin + 1) / 2;
       const int LIN = PIN * lyz;
       const int MXP = I.Mx | 1;
-      smem_x = cb * ((size_t)nin * lyz * MXP + (size_t)p.nx * (LIN + 1) + (size_t)p.nx * LIN * (I.px.np >= 3 ? 2 : 1));
+      smem_x = cb * ((size_t)p.nx * (LIN + 1) + std::max((size_t)nin * lyz * MXP, (size_t)p.nx * (LIN + 1)));
     }
-    smem_zu = cb * ((size_t)txz * p.nz * (I.pz.np >= 3 ? 2 : 1) + (size_t)(4 + ((I.les || I.density) ? 4 : 0)) * I.NZR * txz);
+    smem_zu = cb * ((size_t)3 * txz * p.nz * (I.pz.np >= 3 ? 2 : 1) +
+                    (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
     if ((rc = set_smem(err))) return rc;
 
     // state and header
@@ -263,7 +297,16 @@ class Engine : public EngineBase {
   }
 
   template <typename K> int smem_attr(K kern, size_t bytes_, std::string& err) {
-    if (bytes_ > 48 * 1024) FFS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes_));
+    cudaFuncAttributes fa;
+    FFS_CK(cudaFuncGetAttributes(&fa, kern));
+    int maxs = 0;
+    FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, P.device));
+    if (fa.sharedSizeBytes + bytes_ > (size_t)maxs) {
+      err = "shared memory per CTA (" + std::to_string(fa.sharedSizeBytes + bytes_) + " bytes) exceeds the device limit";
+      return FFS_EUNSUPPORTED;
+    }
+    // raise the dynamic limit whenever static + dynamic passes the 48 KB default
+    FFS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes_));
     return 0;
   }
 
@@ -281,28 +324,37 @@ class Engine : public EngineBase {
     if ((rc = smem_attr(k_inv_y<T, TX>, smem_y, err))) return rc;
     if ((rc = smem_attr(k_fwd_y<T, TX>, smem_y, err))) return rc;
     if ((rc = smem_attr(k_fwd_z_store<T, TX>, smem_z, err))) return rc;
+    if ((rc = smem_attr(k_inv_z<T, TX / 2>, smem_z, err))) return rc;
+    if ((rc = smem_attr(k_inv_y<T, TX / 2>, smem_y, err))) return rc;
+    if ((rc = smem_attr(k_fwd_y<T, TX / 2>, smem_y, err))) return rc;
+    if ((rc = smem_attr(k_fwd_z_store<T, TX / 2>, smem_z, err))) return rc;
     if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
-    if (txz == TX) { if ((rc = smem_attr(k_fwd_z_update<T, TX>, smem_zu, err))) return rc; }
-    else { if ((rc = smem_attr(k_fwd_z_update<T, TX / 2>, smem_zu, err))) return rc; }
-    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    if ((rc = smem_attr(zu_ptr(), smem_zu, err))) return rc;
+    const size_t io = io_smem();
     if ((rc = smem_attr(k_phys_fwd_x<T>, io, err))) return rc;
     if ((rc = smem_attr(k_inv_x_phys<T>, io, err))) return rc;
     return 0;
   }
 
+  size_t io_smem() const { return sizeof(cplx<T>) * (size_t)P.nx * 2 * (2 * LYZ_IO + 1); }
+
   using XK = void (*)(Inst<T>);
+  template <int LY> static XK xsel(bool L, bool D) {
+    if (L && D) return k_x_pass<T, true, true, LY>;
+    if (L) return k_x_pass<T, true, false, LY>;
+    if (D) return k_x_pass<T, false, true, LY>;
+    return k_x_pass<T, false, false, LY>;
+  }
   XK xpass_ptr() const {
-    const bool L = I.les, D = I.density;
-    if (lyz == 4) {
-      if (L && D) return k_x_pass<T, true, true, 4>;
-      if (L) return k_x_pass<T, true, false, 4>;
-      if (D) return k_x_pass<T, false, true, 4>;
-      return k_x_pass<T, false, false, 4>;
-    }
-    if (L && D) return k_x_pass<T, true, true, 1>;
-    if (L) return k_x_pass<T, true, false, 1>;
-    if (D) return k_x_pass<T, false, true, 1>;
-    return k_x_pass<T, false, false, 1>;
+    if (lyz == 4) return xsel<4>(I.les, I.density);
+    if (lyz == 2) return xsel<2>(I.les, I.density);
+    return xsel<1>(I.les, I.density);
+  }
+  using ZK = void (*)(Inst<T>, FieldList, int);
+  ZK zu_ptr() const {
+    if (txz == TX) return k_fwd_z<T, TX>;
+    if (txz == TX / 2) return k_fwd_z<T, TX / 2>;
+    return k_fwd_z<T, (TX / 4 > 0 ? TX / 4 : 1)>;
   }
 
   int reset_state(std::string& err) {
@@ -322,31 +374,38 @@ class Engine : public EngineBase {
   dim3 blk(int lines, const FftPlan& pl) const { return dim3(round32(lines * pl.tpl)); }
 
   void launch_inv_z(const FieldList& F) {
-    k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    if (txy == TX) k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    else k_inv_z<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   void launch_inv_y(const FieldList& F) {
-    k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    if (txy == TX) k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    else k_inv_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
   void launch_fwd_y(const FieldList& F) {
-    k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    if (txy == TX) k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    else k_fwd_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
+  }
+  void launch_fwd_z_store(const FieldList& F) {
+    if (txy == TX) k_fwd_z_store<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    else k_fwd_z_store<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   void launch_x() {
     const int PIN = (nin + 1) / 2;
     xpass_ptr()<<<dim3(I.ny * I.nz / lyz), blk(PIN * lyz, I.px), smem_x, s>>>(I);
   }
   void launch_scalar(int mode) { k_scalar<T><<<1, 256, 0, s>>>(I, mode); }
-  bool use_table() const { return !I.ab3 && I.uniformL; }
+  bool use_table() const { return !I.ab3; }
   void launch_table(int mode) {
     if (!use_table()) return;
-    const int nb = std::min(1024, (I.qmax + 1 + 255) / 256);
+    const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
+    const int nb = (int)std::min<long long>(1024, (count + 255) / 256);
     k_etd_table<T><<<nb, 256, 0, s>>>(I, mode);
   }
   void launch_zu(int mode) {
-    if (txz == TX)
-      k_fwd_z_update<T, TX><<<dim3(I.KXP / TX, I.NYR), blk(TX, I.pz), smem_zu, s>>>(I, fwd_list, mode);
-    else
-      k_fwd_z_update<T, TX / 2><<<dim3(I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_zu, s>>>(I, fwd_list, mode);
+    zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(3 * txz, I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
+  void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
+  void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
   void launch_fin(int mode) { k_finalize<T><<<1, 1024, 0, s>>>(I, mode, nparts); }
 
   void enqueue_step(int mode) {
@@ -357,9 +416,11 @@ class Engine : public EngineBase {
     launch_scalar(mode);
     launch_table(mode);
     launch_zu(mode);
+    launch_stats(mode);
+    launch_update(mode);
     launch_fin(mode);
   }
-  int launches_per_step() const override { return 7 + (use_table() ? 1 : 0); }
+  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0); }
 
   // ---------------------------------------------------------------- fields
   void repack_in(const double* src, double* dst, int layout) const {
@@ -386,7 +447,7 @@ class Engine : public EngineBase {
     std::vector<double> tmp(2 * N, 0.0);
     const double* src[4] = {u1, u2, u3, rho};
     const int nf = I.density ? 4 : 3;
-    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    const size_t io = io_smem();
     for (int pair = 0; pair < 2; ++pair) {
       const int f0 = 2 * pair;
       const int cnt = std::min(2, nf - f0);
@@ -404,7 +465,7 @@ class Engine : public EngineBase {
     F.n = nf;
     for (int i = 0; i < nf; ++i) { F.code[i] = i; F.slot[i] = i; }
     launch_fwd_y(F);
-    k_fwd_z_store<T, TX><<<dim3(nf, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    launch_fwd_z_store(F);
     FFS_CK(cudaGetLastError());
     int rc;
     if ((rc = reset_state(err))) return rc;
@@ -427,7 +488,7 @@ class Engine : public EngineBase {
     launch_inv_z(F);
     launch_inv_y(F);
     std::vector<double> tmp(2 * N);
-    const size_t io = sizeof(cplx<T>) * (size_t)P.nx * (2 * LYZ_IO + 1 + 2 * 2 * LYZ_IO);
+    const size_t io = io_smem();
     for (int pair = 0; pair < 2; ++pair) {
       const int f0 = 2 * pair;
       const int cnt = std::min(2, nf - f0);
@@ -609,9 +670,10 @@ class Engine : public EngineBase {
 
   int profile(int64_t n, std::vector<KernelTiming>& out, std::string& err) override {
     if (!initialized) { err = "ffs_initialize must be called first"; return FFS_ESTATE; }
-    const char* names[8] = {"inv_z", "inv_y", "x_pass", "fwd_y", "scalar", "etd_table", "fwd_z_update", "finalize"};
-    double acc[8] = {0};
-    cudaEvent_t ev[9];
+    const char* names[10] = {"inv_z", "inv_y", "x_pass", "fwd_y", "scalar", "etd_table", "fwd_z", "stats",
+                             "update", "finalize"};
+    double acc[10] = {0};
+    cudaEvent_t ev[11];
     for (auto& e : ev) FFS_CK(cudaEventCreate(&e));
     const int64_t it0 = iteration;
     for (int64_t i = 0; i < n; ++i) {
@@ -623,9 +685,11 @@ class Engine : public EngineBase {
       launch_scalar(0); FFS_CK(cudaEventRecord(ev[5], s));
       launch_table(0); FFS_CK(cudaEventRecord(ev[6], s));
       launch_zu(0); FFS_CK(cudaEventRecord(ev[7], s));
-      launch_fin(0); FFS_CK(cudaEventRecord(ev[8], s));
-      FFS_CK(cudaEventSynchronize(ev[8]));
-      for (int k = 0; k < 8; ++k) {
+      launch_stats(0); FFS_CK(cudaEventRecord(ev[8], s));
+      launch_update(0); FFS_CK(cudaEventRecord(ev[9], s));
+      launch_fin(0); FFS_CK(cudaEventRecord(ev[10], s));
+      FFS_CK(cudaEventSynchronize(ev[10]));
+      for (int k = 0; k < 10; ++k) {
         float f = 0.f;
         FFS_CK(cudaEventElapsedTime(&f, ev[k], ev[k + 1]));
         acc[k] += f;
@@ -633,7 +697,7 @@ class Engine : public EngineBase {
     }
     for (auto& e : ev) cudaEventDestroy(e);
     out.clear();
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < 10; ++k) {
       if (k == 5 && !use_table()) continue;
       out.push_back({names[k], acc[k]});
     }

@@ -1,11 +1,11 @@
 // Shared-memory Stockham FFT core for line batches (sm_103a).
 //
-// A CTA transforms L lines of length n.  Line l, element j lives in shared memory
-// at buf[j * LS + l] (lines fastest), so a warp touches consecutive addresses.
-// Pass 0 reads its inputs through a loader functor (usually straight from global
-// memory, with any spectral prologue fused in) and the last pass hands its outputs
-// to a storer functor (global store, pruning, or epilogue math), so a two-pass
-// transform (n = R0 * R1) makes a single round trip through shared memory.
+// A CTA transforms L lines of length n.  Line l, element j lives in shared memory at
+// buf[j * LS + l] (lines fastest), so a warp touches consecutive addresses.
+// Pass 0 reads its inputs through a loader functor (straight from global memory, with
+// any spectral prologue fused in) and the last pass hands its outputs to a storer
+// functor (global store, pruning, or epilogue math), so a two-pass transform
+// (n = R0 * R1) makes a single round trip through shared memory.
 //
 // Formulation (radix R, sub-transform length p, T = n / R butterflies per line):
 //   k = i mod p;  x_m = in[i + m T] * w^(k m n/(p R));  X = DFT_R(x);
@@ -37,7 +37,7 @@ struct FftPlan {
   int n;      // transform length
   int np;     // number of passes
   int r[4];   // radices, product == n
-  int tpl;    // threads per line = n / max radix
+  int tpl;    // threads per line = n / largest radix
 };
 
 // ---------------------------------------------------------------------------------
@@ -134,14 +134,15 @@ template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<
 
 // ---------------------------------------------------------------------------------
 // One Stockham pass over L lines.
-//   FIRST: read through ld(l, j) instead of shared memory.
-//   LAST:  write through st(l, j, v) instead of shared memory.
-// tw: table exp(-2 pi i t / n), t in [0, n) (global memory, read through L1).
+//   first: inputs come from the loader ld(l, j) instead of shared memory.
+//   last:  outputs go to the storer st(l, j, v) instead of shared memory.
+// In the last pass p * R = n, so every butterfly writes exactly the positions it read
+// (j = i); a storer may therefore write back into the buffer the last pass reads.
+// tw: table exp(-2 pi i t / n), t in [0, n).
 // ---------------------------------------------------------------------------------
 template <int R, int DIR, int L, typename T, class LD, class ST>
-__device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, const cplx<T>* __restrict__ in,
-                                         cplx<T>* __restrict__ out, int LS, const cplx<T>* __restrict__ tw,
-                                         LD& ld, ST& st) {
+__device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, const cplx<T>* in, cplx<T>* out,
+                                         int LS, const cplx<T>* __restrict__ tw, LD& ld, ST& st) {
   const int T_ = n / R;
   const int nb = L * T_;
   const int tws = n / (p * R);
@@ -176,15 +177,21 @@ __device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, co
   }
 }
 
-// Runs the whole plan. s0/s1: shared buffers of n*LS elements (s1 unused for np <= 2).
-// Ends with a __syncthreads() so callers may reuse the buffers immediately.
+// The shared buffer the last pass reads (and an in-place storer may write): s0 for one-
+// and two-pass plans, alternating s0/s1 for longer plans.
+template <typename T> __device__ __forceinline__ cplx<T>* fft_result_buffer(const FftPlan& P, cplx<T>* s0, cplx<T>* s1) {
+  return P.np >= 2 && ((P.np - 2) & 1) ? s1 : s0;
+}
+
+// Runs the whole plan. Pass 0 writes s0, later passes alternate s0/s1 (s1 is touched
+// only for plans of three or more passes). Ends with a __syncthreads().
 template <int DIR, int L, typename T, class LD, class ST>
 __device__ void fft_lines(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS, const cplx<T>* __restrict__ tw, LD ld,
                           ST st) {
   int p = 1;
   for (int pass = 0; pass < P.np; ++pass) {
     const bool first = pass == 0, last = pass == P.np - 1;
-    cplx<T>* in = (pass & 1) ? s0 : s1;   // output buffer of the previous pass
+    const cplx<T>* in = ((pass - 1) & 1) ? s1 : s0;
     cplx<T>* out = (pass & 1) ? s1 : s0;
     switch (P.r[pass]) {
       case 16: fft_pass<16, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;

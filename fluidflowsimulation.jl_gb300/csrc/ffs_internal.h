@@ -75,7 +75,8 @@ template <typename T> struct Inst {
   double* phys;            // FP64 physical staging [field][nz][ny][nx]
   // scalar state and outputs
   DevState* st;
-  double* partials;        // [nblocks_z][QPAD]
+  double* partials;        // [stats CTAs][QPAD]
+  cplx<T>* sbuf;           // scratch: N(3), ke, i k.tau(3), i k.flux (compact layout)
   double* records;         // stats records [cap][ncols]
   int rec_cap, ncols;
   double* spec;            // spectrum records [cap][4][nbin]
@@ -97,6 +98,9 @@ template <typename T> struct Inst {
   int forcing;
   double f_eps, f_kf;
   int dt_stat, dt_spec;
+  // the same constants in the arithmetic type (no per-element conversions)
+  T Lx_t, Ly_t, Lz_t, iLx_t, iLy_t, iLz_t;
+  T inv_n_t, nu_t, hvnu_t, alpha_t, gval_t, dgrad_t, kf2_t;
   // field lists for the passes
   int nin;                 // inverse fields
   int in_code[12];

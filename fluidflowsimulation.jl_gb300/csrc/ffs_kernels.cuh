@@ -10,9 +10,13 @@
 //   wy   [slot][z][y][kx]         after the y pass (inverse) / before it (forward)
 // Physical space exists only in shared memory inside the x pass.
 #pragma once
+#include "ffs_ddmath.cuh"
 #include "ffs_internal.h"
 
 namespace ffsgpu {
+
+// CTAs of at most 512 threads (<= 128 registers per thread); tiles shrink for large n.
+#define FFS_MAXT 512
 
 constexpr int LYZ_IO = 4;  // (y,z) lines per CTA in the transform-only x kernels
 
@@ -45,6 +49,22 @@ template <typename T> __device__ __forceinline__ int zsig(const Inst<T>& I, int 
   return z < I.nz / 2 ? z : z - I.nz;
 }
 
+// asynchronous global -> shared copy of one complex element (8 or 16 bytes)
+template <typename T> __device__ __forceinline__ void cp_async_elem(cplx<T>* dst, const cplx<T>* src) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+  if (sizeof(cplx<T>) == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// wavenumber i / L: FP64 divides exactly like the reference (KX[i] = i/LX); FP32
+// multiplies by the reciprocal.
+template <typename T> __device__ __forceinline__ T kval(int i, T L, T iL) {
+  return sizeof(T) == 8 ? T(i) / L : T(i) * iL;
+}
+
 __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
   // non-negative doubles order like their bit patterns
   atomicMax(a, (unsigned long long)__double_as_longlong(v));
@@ -60,22 +80,23 @@ template <typename T> __device__ __forceinline__ double proj(cplx<T> a, cplx<T> 
 // grid (nfields, KXP/TX, NYR); block TX * tpl_z
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(512) k_inv_z(Inst<T> I, FieldList F) {
+__global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + I.nz * TX;
+  cplx<T>* s1 = s0 + I.nz * TX;   // used by plans of three or more passes
   const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
   const int code = F.code[fi];
   const long long cs = I.cstride;
   const int rowstride = I.NYR * I.KXP;
   const cplx<T>* uh = I.uh + (long long)jc * I.KXP + kx0;
-  const T kyv = T(ysig(I, jc)) / T(I.ly);
+  const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
   auto ld = [&](int l, int z) -> cplx<T> {
     const int kc = zcomp(I, z);
     const int ix = kx0 + l;
     if (kc < 0 || ix >= I.Mx) return mk(T(0), T(0));
     const cplx<T>* p = uh + (long long)kc * rowstride + l;
-    const T kx = T(ix) / T(I.lx), ky = kyv, kz = T(zsig(I, kc)) / T(I.lz);
+    const T kx = kval(ix, Lx, iLx), ky = kyv, kz = kval(zsig(I, kc), Lz, iLz);
     switch (code) {
       case F_UX: return p[0];
       case F_UY: return p[cs];
@@ -109,7 +130,7 @@ __global__ void __launch_bounds__(512) k_inv_z(Inst<T> I, FieldList F) {
 // Inverse y pass: grid (nfields, KXP/TX, nz); block TX * tpl_y
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(512) k_inv_y(Inst<T> I, FieldList F) {
+__global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + I.ny * TX;
@@ -130,7 +151,7 @@ __global__ void __launch_bounds__(512) k_inv_y(Inst<T> I, FieldList F) {
 // The kinetic-energy field is transformed only at stats/spectrum iterations.
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(512) k_fwd_y(Inst<T> I, FieldList F) {
+__global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + I.ny * TX;
@@ -166,18 +187,19 @@ template <bool LES, bool DEN> struct XFields {
 };
 
 template <typename T, bool LES, bool DEN, int LYZ>
-__global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
+__global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   using XF = XFields<LES, DEN>;
   constexpr int PIN = XF::PIN, POUT = XF::POUT;
   constexpr int LIN = PIN * LYZ, LOUT = POUT * LYZ;
-  constexpr int LSX = LIN + 1;   // odd stride for the exchange buffer
+  constexpr int LSX = LIN + 1;   // odd line stride: conflict-free column reads in the unpack
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = I.nx, Mx = I.Mx;
   const int MXP = Mx | 1;
-  cplx<T>* stage = reinterpret_cast<cplx<T>*>(smem_raw);                  // [nin][LYZ][MXP]
-  cplx<T>* sx = stage + (size_t)XF::nin * LYZ * MXP;                         // [n][LSX]
-  cplx<T>* s0 = sx + (size_t)n * LSX;                                      // [n][LIN]
-  cplx<T>* s1 = s0 + (size_t)n * LIN;                                      // [n][LIN] (np >= 3)
+  // two buffers of [n][LSX] (the second at least as large as the staged half spectra,
+  // which live in it: the first c2r pass reads them and writes the first buffer)
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
+  cplx<T>* s1 = s0 + (size_t)n * LSX;
+  cplx<T>* stage = s1;                                                       // [nin][LYZ][MXP]
   __shared__ double red[32];
 
   const int g0 = blockIdx.x * LYZ;
@@ -190,8 +212,9 @@ __global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
     for (int e = threadIdx.x; e < per; e += blockDim.x) {
       const int kx = e % Mx, r = e / Mx, q = r % LYZ, f = r / LYZ;
       const int g = g0 + q;
-      stage[(f * LYZ + q) * MXP + kx] = I.wy[(long long)f * I.wys + (long long)g * I.KXP + kx];
+      cp_async_elem(stage + (f * LYZ + q) * MXP + kx, I.wy + (long long)f * I.wys + (long long)g * I.KXP + kx);
     }
+    cp_async_wait_all();
   }
   __syncthreads();
 
@@ -208,14 +231,17 @@ __global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
     if (cj) { A.y = -A.y; B.y = -B.y; }
     return mk(A.x - B.y, A.y + B.x);
   };
-  auto sti = [&](int l, int j, cplx<T> v) { sx[j * LSX + l] = v; };
-  fft_lines<+1, LIN, T>(I.px, s0, s1, LIN, I.twx, ldi, sti);
+  cplx<T>* ri = fft_result_buffer(I.px, s0, s1);   // physical values end up here
+  auto sti = [&](int l, int j, cplx<T> v) { ri[j * LSX + l] = v; };
+  fft_lines<+1, LIN, T>(I.px, s0, s1, LSX, I.twx, ldi, sti);
 
-  // 3. physical space products, in place in sx (outputs in the first POUT pairs)
-  double umax = 0.0, rmax = 0.0;
+  // 3. physical space products: inputs from ri, outputs (first POUT pairs) into s1
+  T umaxt = T(0), rmaxt = T(0);
+  const T les2 = T(2) * T(I.les_alpha);
   for (int e = threadIdx.x; e < n * LYZ; e += blockDim.x) {
     const int q = e % LYZ, j = e / LYZ;
-    cplx<T>* row = sx + j * LSX + q;
+    const cplx<T>* row = ri + j * LSX + q;
+    cplx<T>* orow = s1 + j * LSX + q;
     T f[2 * PIN];
 #pragma unroll
     for (int p = 0; p < PIN; ++p) { cplx<T> v = row[p * LYZ]; f[2 * p] = v.x; f[2 * p + 1] = v.y; }
@@ -227,24 +253,25 @@ __global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
     o[1] = uz * wx - ux * wz;
     o[2] = ux * wy - uy * wx;
     o[3] = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);   // models.jl:224
-    umax = fmax(umax, fmax(fabs((double)ux), fmax(fabs((double)uy), fabs((double)uz))));
+    umaxt = fmax(umaxt, fmax(fabs(ux), fmax(fabs(uy), fabs(uz))));
     if (LES) {
       const T xx = f[6], xy = f[7], xz = f[8], yy = f[9], yz = f[10];
       const T zz = -xx - yy;
       const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
-      const T two_nut = T(2) * T(I.les_alpha) * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
+      const T two_nut = les2 * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
       o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
     }
     if (DEN) {
       constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
       const T rho = f[fr];
-      rmax = fmax(rmax, fabs((double)rho));
+      rmaxt = fmax(rmaxt, fabs(rho));
       o[of] = -rho * ux; o[of + 1] = -rho * uy; o[of + 2] = -rho * uz;   // models.jl:266
     }
 #pragma unroll
-    for (int r = 0; r < POUT; ++r) row[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
+    for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
   }
   // block max -> one atomic per CTA
+  double umax = (double)umaxt, rmax = (double)rmaxt;
   if (I.adaptive) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -273,9 +300,10 @@ __global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
   __syncthreads();
 
   // 4. r2c of the output pairs, result back into sx
-  auto ldf = [&](int l, int j) -> cplx<T> { return sx[j * LSX + l]; };
-  auto stf = [&](int l, int j, cplx<T> v) { sx[j * LSX + l] = v; };
-  fft_lines<-1, LOUT, T>(I.px, s0, s1, LIN, I.twx, ldf, stf);
+  cplx<T>* rf = fft_result_buffer(I.px, s0, s1);
+  auto ldf = [&](int l, int j) -> cplx<T> { return s1[j * LSX + l]; };
+  auto stf = [&](int l, int j, cplx<T> v) { rf[j * LSX + l] = v; };
+  fft_lines<-1, LOUT, T>(I.px, s0, s1, LSX, I.twx, ldf, stf);
 
   // 5. unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 and store
   const int KXP = I.KXP;
@@ -285,78 +313,31 @@ __global__ void __launch_bounds__(512) k_x_pass(Inst<T> I) {
     const int g = g0 + q;
     cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
     if (k < Mx) {
-      const cplx<T> zk = sx[k * LSX + l];
-      const cplx<T> zm = sx[((n - k) % n) * LSX + l];
+      const cplx<T> zk = rf[k * LSX + l];
+      const cplx<T> zm = rf[((n - k) % n) * LSX + l];
       A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
       B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
     }
     const int oa = 2 * r, ob = 2 * r + 1;
-    if (oa < XF::nout) I.wy[(long long)I.out_slot[oa] * I.wys + (long long)g * KXP + k] = A;
-    if (ob < XF::nout) I.wy[(long long)I.out_slot[ob] * I.wys + (long long)g * KXP + k] = B;
+    // output 3 is the kinetic-energy field, needed only at stats/spectrum iterations
+    if (oa < XF::nout && (oa != 3 || want_ke)) I.wy[(long long)I.out_slot[oa] * I.wys + (long long)g * KXP + k] = A;
+    if (ob < XF::nout && (ob != 3 || want_ke)) I.wy[(long long)I.out_slot[ob] * I.wys + (long long)g * KXP + k] = B;
   }
 }
 
-// ====================================================================================
-// ETD phi-function coefficients (ETD.jl:142-227, ETD1stand2ndO.jl:12-66), FP64.
-// Returns E = exp(c dt) and A, B, C so that u' = E u + A N + B fm1 + C fm2.
-// ====================================================================================
-__device__ inline void etd_coeffs(double c, double dt, double dt2, double dt3, int stage, double& E, double& A,
-                                  double& B, double& C) {
-  const double cdt = c * dt;
-  E = exp(cdt);
-  const bool test = -cdt <= 1e-4;
-  const bool inf = (c == -INFINITY);
-  if (stage == 1) {
-    const double cdt2 = cdt * dt, c2dt3 = cdt2 * cdt, c3dt4 = c2dt3 * cdt;
-    A = inf ? 0.0 : (test ? dt + 0.5 * cdt2 + c2dt3 / 6 + c3dt4 / 24 : expm1(cdt) / c);
-    B = 0.0; C = 0.0;
-  } else if (stage == 2) {
-    const double cp2 = c * c, cdtp2 = cdt * dt, c2dtp3 = cdtp2 * cdt, c3dtp4 = c2dtp3 * cdt;
-    const double em = expm1(cdt), c2dt2 = c * c * dt2;
-    const double dtp2 = dt * dt, dtp3 = dtp2 * dt, dtp4 = dtp3 * dt;
-    A = inf ? 0.0 : (test ? dt + cdtp2 / 2 + c2dtp3 / 6 + c3dtp4 / 24 + dtp2 / (2 * dt2) + (c * dtp3) / (6 * dt2) +
-                                (cp2 * dtp4) / (24 * dt2)
-                          : (em - c * (dt - dt2 * em)) / c2dt2);
-    B = inf ? 0.0 : (test ? (-(dtp2 / (2 * dt2)) - (c * dtp3) / (6 * dt2) - (cp2 * dtp4) / (24 * dt2))
-                          : (cdt - em) / c2dt2);
-    C = 0.0;
-  } else {
-    const double a0 = (dt * (2 * dt * dt + 6 * dt2 * (dt2 + dt3) + 3 * dt * (2 * dt2 + dt3))) / (6 * dt2 * (dt2 + dt3));
-    const double a1 = (dt * dt * (dt * dt + 6 * dt2 * (dt2 + dt3) + 2 * dt * (2 * dt2 + dt3))) / (12 * dt2 * (dt2 + dt3));
-    const double a2 = (dt * dt * dt * (4 * dt2 * (dt2 + dt3) + dt * (2 * dt2 + dt3))) / (24 * dt2 * (dt2 + dt3));
-    const double a3 = dt * dt * dt * dt / 24;
-    const double b0 = -((dt * dt * (2 * dt + 3 * (dt2 + dt3))) / (6 * (dt2 * dt3)));
-    const double b1 = -(((dt * dt * dt * (dt + 2 * (dt2 + dt3)))) / (12 * (dt2 * dt3)));
-    const double b2 = -((dt * dt * dt * dt * (dt2 + dt3)) / (24 * (dt2 * dt3)));
-    const double c0 = (dt * dt * (2 * dt + 3 * dt2)) / (6 * dt3 * (dt2 + dt3));
-    const double c1 = (dt * dt * dt * (dt + 2 * dt2)) / (12 * dt3 * (dt2 + dt3));
-    const double c2 = (dt * dt * dt * dt * dt2) / (24 * dt3 * (dt2 + dt3));
-    const double e1 = dt * dt + dt * (2 * dt2 + dt3), e2 = dt2 * (dt2 + dt3), e3 = 2 * dt, e4 = 2 * dt2 + dt3;
-    const double e5 = dt * (dt + dt2 + dt3), e6 = dt2 + dt3, e7 = dt2 * dt3, e8 = dt * (dt + dt2), e9 = dt3 * (dt2 + dt3);
-    const double l1 = c, l2 = l1 * l1, l3 = l2 * l1;
-    if (inf) { A = B = C = 0.0; return; }
-    if (test) {
-      A = fma(a1, l1, fma(a2, l2, fma(a3, l3, a0)));
-      B = fma(b1, l1, fma(b2, l2, b0));
-      C = fma(c1, l1, fma(c2, l2, c0));
-    } else {
-      const double em = expm1(cdt);
-      A = (2 * em - l2 * (e1 - e2 * em) - l1 * (e3 - e4 * em)) / (l3 * e2);
-      B = (e5 * l2 - 2 * em + l1 * (e3 - e6 * em)) / (l3 * e7);
-      C = (2 * em - e8 * l2 - l1 * (e3 - dt2 * em)) / (l3 * e9);
-    }
-  }
-}
-
-// velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95)
+// velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95);
+// muladd(modk, m_nu, modk^M * m_nuh) is a single-rounding fma in the reference.
 template <typename T> __device__ __forceinline__ double c_vel(const Inst<T>& I, double k2) {
-  double c = k2 * (-I.nu);
-  if (I.hv) {
-    double km = 1.0;
-    for (int m = 0; m < I.hv_m; ++m) km *= k2;
-    c = fma(k2, -I.nu, km * (-I.hv_nu));
-  }
-  return c;
+  if (!I.hv) return dd::M(k2, -I.nu);
+  double km = k2;
+  for (int m = 1; m < I.hv_m; ++m) km = dd::M(km, k2);
+  return dd::fma_e(k2, -I.nu, dd::M(km, -I.hv_nu));
+}
+
+// k^2 as the reference forms it: muladd(KX,KX, muladd(KY,KY, KZ*KZ)) with K = i / L
+template <typename T> __device__ __forceinline__ double ref_k2(const Inst<T>& I, int ix, int iy, int iz) {
+  const double kx = dd::D((double)ix, I.lx), ky = dd::D((double)iy, I.ly), kz = dd::D((double)iz, I.lz);
+  return dd::fma_e(kx, kx, dd::fma_e(ky, ky, dd::M(kz, kz)));
 }
 
 // ====================================================================================
@@ -367,59 +348,63 @@ template <typename T> __device__ __forceinline__ double c_vel(const Inst<T>& I, 
 // ====================================================================================
 template <typename T>
 __global__ void k_scalar(Inst<T> I, int mode) {
-  DevState* S = I.st;
+  DevState* Sg = I.st;
   __shared__ double sh_ef[256];
+  __shared__ double sh_dt;
   if (threadIdx.x == 0) {
-    const long long it = S->iteration;
+    DevState S = *Sg;   // one load; all logic on the local copy
+    const long long it = S.iteration;
     if (I.adaptive) {
-      const double m = __longlong_as_double((long long)S->umax_bits);
-      S->slot_u = I.ref_slot ? fmax(m, S->slot_u) : m;
+      const double m = __longlong_as_double((long long)S.umax_bits);
+      S.slot_u = I.ref_slot ? fmax(m, S.slot_u) : m;
       if (I.density) {
-        const double mr = __longlong_as_double((long long)S->rhomax_bits);
-        S->slot_rho = I.ref_slot ? fmax(mr, S->slot_rho) : mr;
+        const double mr = __longlong_as_double((long long)S.rhomax_bits);
+        S.slot_rho = I.ref_slot ? fmax(mr, S.slot_rho) : mr;
       }
-      const double umax = S->slot_u;
+      const double umax = S.slot_u;
       const double dx = 2.0 * M_PI * I.ly / I.ny;
       double cfl = I.cfl;
       if (it == 0) cfl *= 0.1;
       else if (it == 1) cfl *= 0.2;
       else if (it == 2) cfl *= 0.4;
       else if (it == 3) cfl *= 0.8;
-      double newdt = cfl * dx / umax;
+      double newdt = dd::D(dd::M(cfl, dx), umax);
       if (I.density) {
-        const double den = S->slot_rho * fabs(I.gval);
-        newdt = fmin(newdt, cfl * sqrt(dx / den));
+        const double den = dd::M(S.slot_rho, fabs(I.gval));
+        newdt = fmin(newdt, dd::M(cfl, sqrt(dd::D(dx, den))));
       }
       if (it > 3) {
-        const double dt = S->dt;
-        newdt = newdt < dt ? fmax(dt / 1.25, newdt) : fmin(1.25 * dt, newdt);
+        const double dt = S.dt;
+        newdt = newdt < dt ? fmax(dd::D(dt, 1.25), newdt) : fmin(dd::M(1.25, dt), newdt);
       }
       if (I.ab3) {
-        if (S->ts_iter == 0) { S->dt3 = S->dt2 = S->dt = newdt / 2; }
-        else { S->dt3 = S->dt2; S->dt2 = S->dt; S->dt = newdt; }
+        if (S.ts_iter == 0) { S.dt3 = S.dt2 = S.dt = dd::D(newdt, 2.0); }
+        else { S.dt3 = S.dt2; S.dt2 = S.dt; S.dt = newdt; }
       } else {
-        S->dt3 = S->dt2; S->dt2 = S->dt; S->dt = newdt;
+        S.dt3 = S.dt2; S.dt2 = S.dt; S.dt = newdt;
       }
     }
     if (mode == 1) {
       // initialize! of the integrator: dt history := current dt (Adams_Bashforth.jl:28-35, ETD.jl:99-108)
-      S->dt2 = S->dt; S->dt3 = S->dt;
-      S->stage = 0;
+      S.dt2 = S.dt; S.dt3 = S.dt;
+      S.stage = 0;
     } else {
-      S->ts_iter += 1;
-      const long long i = S->ts_iter;
-      S->stage = i >= 3 ? 3 : (int)i;
+      S.ts_iter += 1;
+      const long long i = S.ts_iter;
+      S.stage = i >= 3 ? 3 : (int)i;
       if (I.ab3) {
-        const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
+        const double dt = S.dt, dt2 = S.dt2, dt3 = S.dt3;
         if (I.adaptive) {
-          S->At = (1. + (dt * (2 * dt + 6 * dt2 + 3 * dt3)) / (6 * dt2 * (dt2 + dt3))) * dt;
-          S->Bt = (-dt * dt * (2 * dt + 3 * dt2 + 3 * dt3) / (6 * dt2 * dt3 * (dt + dt2))) * (dt + dt2);
-          S->Ct = (dt * dt * (2 * dt + 3 * dt2) / (6 * dt3 * (dt + dt2 + dt3) * (dt2 + dt3))) * (dt + dt2 + dt3);
+          S.At = (1. + (dt * (2 * dt + 6 * dt2 + 3 * dt3)) / (6 * dt2 * (dt2 + dt3))) * dt;
+          S.Bt = (-dt * dt * (2 * dt + 3 * dt2 + 3 * dt3) / (6 * dt2 * dt3 * (dt + dt2))) * (dt + dt2);
+          S.Ct = (dt * dt * (2 * dt + 3 * dt2) / (6 * dt3 * (dt + dt2 + dt3) * (dt2 + dt3))) * (dt + dt2 + dt3);
         } else {
-          S->At = 23 * dt / 12; S->Bt = -16 * dt / 12; S->Ct = 5 * dt / 12;
+          S.At = 23 * dt / 12; S.Bt = -16 * dt / 12; S.Ct = 5 * dt / 12;
         }
       }
     }
+    *Sg = S;
+    sh_dt = S.dt;
   }
   // isotropic band forcing: E_f = sum_{0<|k|<=kf} 1/2 w |u|^2 from the current u
   if (I.forcing && mode == 0) {
@@ -440,85 +425,98 @@ __global__ void k_scalar(Inst<T> I, int mode) {
       for (int c = 0; c < 3; ++c) { cplx<T> v = I.uh[c * I.cstride + idx]; a += (double)v.x * v.x + (double)v.y * v.y; }
       e += 0.5 * (ix > 0 ? 2.0 : 1.0) * a;
     }
-    sh_ef[threadIdx.x] = e;
+    // fixed-order reduction
+    for (int o = 16; o > 0; o >>= 1) e += __shfl_xor_sync(0xffffffffu, e, o);
+    if ((threadIdx.x & 31) == 0) sh_ef[threadIdx.x >> 5] = e;
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0.0;
-      for (int i = 0; i < blockDim.x; ++i) s += sh_ef[i];
-      S->Ef = s;
-      S->force_coef = s > 0.0 ? I.f_eps / (2.0 * s) : 0.0;
+      for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh_ef[i];
+      Sg->Ef = s;
+      Sg->force_coef = s > 0.0 ? I.f_eps / (2.0 * s) : 0.0;
     }
   }
 }
 
-// ETD coefficient tables by q = i^2 + j^2 + l^2 (uniform domain), for the current
-// stage and dt history. Multi-CTA; runs after k_scalar.
+// ETD coefficient tables for the current stage and dt history: by q = i^2 + j^2 + l^2
+// when k^2 = q / L^2 is exact (uniform domain with L a power of two), else one entry per
+// retained mode (compact index). Multi-CTA; runs after k_scalar.
 template <typename T>
 __global__ void k_etd_table(Inst<T> I, int mode) {
   const DevState* S = I.st;
   const int stage = S->stage;
   if (mode == 1 || stage == 0) return;
   const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
-  const double L2 = I.lx * I.lx;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q <= I.qmax; q += gridDim.x * blockDim.x) {
-    const double k2 = (double)q / L2;
+  const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (long long)gridDim.x * blockDim.x) {
+    double k2;
+    if (I.uniformL) {
+      k2 = dd::D((double)q, I.lx * I.lx);
+    } else {
+      const int ix = (int)(q % I.KXP);
+      if (ix >= I.Mx) continue;
+      const long long r = q / I.KXP;
+      k2 = ref_k2(I, ix, ysig(I, (int)(r % I.NYR)), zsig(I, (int)(r / I.NYR)));
+    }
     double E, A, B, C;
-    etd_coeffs(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
-    T* e = I.etab + 4 * (size_t)q;
+    etd_coeffs_exact(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
+    T* e = I.etab + 4 * q;
     e[0] = T(E); e[1] = T(A); e[2] = T(B); e[3] = T(C);
     if (I.density && I.etab_rho) {
-      etd_coeffs(k2 * (-I.alpha), dt, dt2, dt3, stage, E, A, B, C);
-      T* r = I.etab_rho + 4 * (size_t)q;
+      etd_coeffs_exact(dd::M(k2, -I.alpha), dt, dt2, dt3, stage, E, A, B, C);
+      T* r = I.etab_rho + 4 * q;
       r[0] = T(E); r[1] = T(A); r[2] = T(B); r[3] = T(C);
     }
   }
 }
 
 // ====================================================================================
-// Forward z pass + update (myfourier! z-part + dealias + 1/N + rhs[1]=0, models.jl
-// 171-175; fourierspacep2!, models.jl:282-364; time_step!, models.jl:468-472 and
-// time_step_functions.jl:72-80; stats reductions, stats.jl; spectrum, spec.jl).
-// grid (KXP/TX, NYR); block TX * tpl_z.  mode 0: step, 1: initialize! (no update).
+// Forward z pass (myfourier! z-part + dealias + 1/N + rhs[1]=0, models.jl:171-175):
+// the three components of N = FFT(u x w) together, plus the auxiliary fields (kinetic
+// energy at stats/spectrum iterations; i k . tau for LES, models.jl:328-332; i k . flux
+// for density, vectorfunctions.jl:93-103). Retained modes only, written compactly to
+// the scratch buffer: [N(3)][ke][i k.tau(3)][i k.flux].
+// grid (KXP/TX, NYR); block 3 TX tpl_z.
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(512) k_fwd_z_update(Inst<T> I, FieldList F, int mode) {
+__global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int L3 = 3 * TX;
   const int nz = I.nz, NZR = I.NZR;
-  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + nz * TX;
-  cplx<T>* accN = s1 + (I.pz.np >= 3 ? nz * TX : 0);  // [3][NZR][TX]
-  cplx<T>* accK = accN + 3 * NZR * TX;                 // [NZR][TX]
-  cplx<T>* accT = accK + NZR * TX;                     // [3][NZR][TX] (LES)
-  cplx<T>* accF = accT + 3 * NZR * TX;                 // [NZR][TX]    (density)
-  __shared__ double red[QPAD][17];
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);   // [nz][3 TX]
+  cplx<T>* bufB = buf + nz * L3;                         // second buffer (plans of >= 3 passes)
+  cplx<T>* accT = bufB + (I.pz.np >= 3 ? nz * L3 : 0);   // [3][NZR][TX] i k . tau (LES)
+  cplx<T>* accF = accT + 3 * NZR * TX;                   // [NZR][TX]    i k . flux (density)
 
-  const DevState* S = I.st;
-  const long long it = S->iteration;
-  const bool stats_t = (it % I.dt_stat) == 0;
-  const bool spec_t = mode == 0 && (it % I.dt_spec) == 0;
+  const long long it = I.st->iteration;
+  const bool want_ke = ((it % I.dt_stat) == 0) || (mode == 0 && (it % I.dt_spec) == 0);
   const int kx0 = blockIdx.x * TX, jc = blockIdx.y;
   const int rowstride = I.NYR * I.KXP;
-  const T kyv = T(ysig(I, jc)) / T(I.ly);
+  const long long cs = I.cstride;
+  const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
+  const T sc = I.inv_n_t;
+  cplx<T>* out = I.sbuf + (long long)jc * I.KXP + kx0;   // + kc * rowstride + l (+ slot * cs)
+  const bool aux = I.les || I.density;
 
-  // zero the LES / density accumulators
-  if (I.les || I.density) {
+  if (aux) {
     for (int e = threadIdx.x; e < 4 * NZR * TX; e += blockDim.x) accT[e] = mk(T(0), T(0));
+    __syncthreads();
   }
-  __syncthreads();
-
-  // 1. forward z transforms of the forward fields
+  // auxiliary fields one at a time (TX lines each)
+  int nslot[3] = {0, 1, 2};
   for (int fi = 0; fi < F.n; ++fi) {
     const int role = F.code[fi];
-    if (role == R_KE && !(stats_t || spec_t)) continue;
+    if (role <= R_NZ) { nslot[role] = F.slot[fi]; continue; }
+    if (role == R_KE && !want_ke) continue;
     const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
     auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
     auto st = [&](int l, int z, cplx<T> v) {
       const int kc = zcomp(I, z);
       if (kc < 0) return;
+      if (role == R_KE) { out[3 * cs + (long long)kc * rowstride + l] = scl(v, sc); return; }
       const int m = kc * TX + l;
-      if (role <= R_NZ) { accN[role * NZR * TX + m] = v; return; }
-      if (role == R_KE) { accK[m] = v; return; }
-      const T kx = T(kx0 + l) / T(I.lx), ky = kyv, kz = T(zsig(I, kc)) / T(I.lz);
+      const T kx = kval(kx0 + l, Lx, iLx), ky = kyv, kz = kval(zsig(I, kc), Lz, iLz);
       // i k . tau for the traceless symmetric tau (models.jl:330); zz = -xx - yy
       auto addT = [&](int c, T kk, cplx<T> a) { cplx<T>& d = accT[c * NZR * TX + m]; d.x -= kk * a.y; d.y += kk * a.x; };
       switch (role) {
@@ -532,65 +530,100 @@ __global__ void __launch_bounds__(512) k_fwd_z_update(Inst<T> I, FieldList F, in
         default: { cplx<T>& d = accF[m]; d.x -= kz * v.y; d.y += kz * v.x; } break;
       }
     };
-    fft_lines<-1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
+    fft_lines<-1, TX, T>(I.pz, buf, bufB, TX, I.twz, ld, st);
   }
+  // the three components of N together (3 TX lines), straight to the scratch buffer
+  {
+    const cplx<T>* in0 = I.wz + (long long)nslot[0] * I.wzs + (long long)jc * I.KXP + kx0;
+    const cplx<T>* in1 = I.wz + (long long)nslot[1] * I.wzs + (long long)jc * I.KXP + kx0;
+    const cplx<T>* in2 = I.wz + (long long)nslot[2] * I.wzs + (long long)jc * I.KXP + kx0;
+    const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
+    auto ld = [&](int l, int z) -> cplx<T> {
+      const int c = l / TX, x = l % TX;
+      const cplx<T>* in = c == 0 ? in0 : (c == 1 ? in1 : in2);
+      return in[(long long)z * rowstride + x];
+    };
+    auto st = [&](int l, int z, cplx<T> v) {
+      const int kc = zcomp(I, z);
+      if (kc < 0) return;
+      const int c = l / TX, x = l % TX;
+      const bool k0 = kzero_col && x == 0 && z == 0;   // rhs.c[1] = 0 (models.jl:174)
+      out[c * cs + (long long)kc * rowstride + x] = k0 ? mk(T(0), T(0)) : scl(v, sc);
+    };
+    fft_lines<-1, L3, T>(I.pz, buf, bufB, L3, I.twz, ld, st);
+  }
+  if (aux) {
+    for (int m = threadIdx.x; m < NZR * TX; m += blockDim.x) {
+      const int l = m % TX, kc = m / TX;
+      const long long o = (long long)kc * rowstride + l;
+      if (I.les) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[(4 + c) * cs + o] = scl(accT[c * NZR * TX + m], sc);
+      }
+      if (I.density) out[7 * cs + o] = scl(accF[m], sc);
+    }
+  }
+}
 
-  // 2. per-mode update
-  const T sc = T(I.inv_n);
-  const int par = S->hist_parity;
+// ====================================================================================
+// Update (fourierspacep2!, models.jl:282-364; time_step!, models.jl:468-472 and
+// time_step_functions.jl:72-80): rhs = N (+ explicit (hyper)viscosity for AB3) + i k.tau
+// + rho g, projected; integrator (AB3 / ETD1-2-3); forcing increment; projection.
+// Density: rho rhs = i k.flux - drho/dz u_g, own integrator. Flat over the retained modes.
+// mode 1 (initialize!): fm1 = fm2 = rhs, no update.
+// ====================================================================================
+template <typename T>
+__global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
+  const DevState* S = I.st;
   const long long cs = I.cstride;
-  cplx<T>* hA = I.hist + (long long)par * I.ncomp * cs;         // fm1
-  cplx<T>* hB = I.hist + (long long)(1 - par) * I.ncomp * cs;   // fm2 -> receives the new rhs
+  const int par = S->hist_parity;
+  cplx<T>* __restrict__ hA = I.hist + (long long)par * I.ncomp * cs;         // fm1
+  cplx<T>* __restrict__ hB = I.hist + (long long)(1 - par) * I.ncomp * cs;   // fm2 -> receives the new rhs
+  cplx<T>* __restrict__ uh = I.uh;
+  const cplx<T>* __restrict__ sb = I.sbuf;
   const int stage = S->stage;
   const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
   const T At = T(S->At), Bt = T(S->Bt), Ct = T(S->Ct);
   const T fdt = T(dt * S->force_coef);
-  const double kf2 = I.f_kf * I.f_kf;
-  double q[Q_COUNT];
-  const bool do_stats = stats_t;
-  if (do_stats) {
-#pragma unroll
-    for (int i = 0; i < Q_COUNT; ++i) q[i] = 0.0;
-  }
+  const T fix2 = T(-(dt3 + dt2) / dt2);
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   bool bad = false;
-  const int ky_i = ysig(I, jc);
-  for (int m = threadIdx.x; m < NZR * TX; m += blockDim.x) {
-    const int l = m % TX, kc = m / TX, ix = kx0 + l;
-    const long long gi = (long long)kc * rowstride + (long long)jc * I.KXP + ix;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < cs; g += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(g % I.KXP);
     if (ix >= I.Mx) {   // padding columns stay zero
-      if (mode == 0) for (int c = 0; c < I.ncomp; ++c) I.uh[c * cs + gi] = mk(T(0), T(0));
+      if (mode == 0) for (int c = 0; c < I.ncomp; ++c) uh[c * cs + g] = mk(T(0), T(0));
       continue;
     }
-    const int kz_i = zsig(I, kc);
-    const T kx = T(ix) / T(I.lx), ky = kyv, kz = T(kz_i) / T(I.lz);
+    const long long r = g / I.KXP;
+    const int ky_i = ysig(I, (int)(r % I.NYR)), kz_i = zsig(I, (int)(r / I.NYR));
+    const T kx = kval(ix, Lx, iLx), ky = kval(ky_i, Ly, iLy), kz = kval(kz_i, Lz, iLz);
     const T k2 = kx * kx + (ky * ky + kz * kz);
     const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
-    cplx<T> N[3], u[3];
+    cplx<T> rhs[3], u[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      N[c] = k0 ? mk(T(0), T(0)) : scl(accN[c * NZR * TX + m], sc);   // models.jl:174
-      u[c] = I.uh[c * cs + gi];
-    }
-    cplx<T> rhs[3] = {N[0], N[1], N[2]};
+    for (int c = 0; c < 3; ++c) { rhs[c] = sb[c * cs + g]; u[c] = uh[c * cs + g]; }
     cplx<T> rho = mk(T(0), T(0));
-    if (I.density) rho = I.uh[3 * cs + gi];
-    cplx<T> divT[3] = {mk(T(0), T(0)), mk(T(0), T(0)), mk(T(0), T(0))};
-    if (I.les) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) divT[c] = scl(accT[c * NZR * TX + m], sc);
-    }
+    if (I.density) rho = uh[3 * cs + g];
     if (I.ab3) {   // explicit (hyper)viscosity, models.jl:320-326
-      const T cv = T(c_vel(I, (double)k2));
+      T cv;
+      if (sizeof(T) == 8) {   // K2*m_nu + (K2^M)*m_nuh as written in models.jl:322
+        const double kd = (double)k2;
+        double km = kd;
+        for (int i = 1; i < I.hv_m; ++i) km = dd::M(km, kd);
+        cv = T(I.hv ? dd::A(dd::M(kd, -I.nu), dd::M(km, -I.hv_nu)) : dd::M(kd, -I.nu));
+      } else {
+        cv = k2 * (-I.nu_t);
+        if (I.hv) { T km = k2; for (int i = 1; i < I.hv_m; ++i) km *= k2; cv += km * (-I.hvnu_t); }
+      }
 #pragma unroll
       for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + scl(u[c], cv);
     }
-    if (I.les) {
+    if (I.les) {   // + i k . tau (models.jl:328-332)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + divT[c];
+      for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + sb[(4 + c) * cs + g];
     }
-    if (I.density) rhs[I.gdir] = rhs[I.gdir] + scl(rho, T(I.gval));   // models.jl:334-336
-    // projection (models.jl:338-339)
-    {
+    if (I.density) rhs[I.gdir] = rhs[I.gdir] + scl(rho, I.gval_t);   // models.jl:334-336
+    {  // projection (models.jl:338-339)
       const cplx<T> kd = mk(kx * rhs[0].x + ky * rhs[1].x + kz * rhs[2].x, kx * rhs[0].y + ky * rhs[1].y + kz * rhs[2].y);
       const T inv = k0 ? T(0) : T(1) / k2;
       const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
@@ -599,136 +632,33 @@ __global__ void __launch_bounds__(512) k_fwd_z_update(Inst<T> I, FieldList F, in
     // density rhs: i k . flux - drho/dz * u_g  (vectorfunctions.jl:93-103)
     cplx<T> rrhs = mk(T(0), T(0));
     if (I.density) {
-      rrhs = scl(accF[m], sc) + scl(u[I.gdir], T(-I.dgrad));
-      if (I.ab3) rrhs = rrhs + scl(rho, T(k2 * T(-I.alpha)));
+      rrhs = sb[7 * cs + g] + scl(u[I.gdir], -I.dgrad_t);
+      if (I.ab3) rrhs = rrhs + scl(rho, k2 * (-I.alpha_t));
     }
-
-    if (do_stats) {
-      const double w = ix > 0 ? 2.0 : 1.0;
-      const double kxd = kx, kyd = ky, kzd = kz, k2d = k2;
-      double a2[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) a2[c] = proj(u[c], u[c]);
-      if (k0) { q[Q_U1] += u[0].x; q[Q_U2] += u[1].x; q[Q_U3] += u[2].x; }
-      q[Q_U12] += w * a2[0]; q[Q_U22] += w * a2[1]; q[Q_U32] += w * a2[2];
-      q[Q_EH] += w * k2d * (a2[0] + a2[1]); q[Q_EV] += w * k2d * a2[2];
-      q[Q_D1DY] += w * kyd * kyd * a2[0]; q[Q_D1DX] += w * kxd * kxd * a2[0];
-      q[Q_D2DY] += w * kyd * kyd * a2[1]; q[Q_D2DX] += w * kxd * kxd * a2[1];
-      // non-linear transfer: (N - i k ke) . u (stats.jl:897-917)
-      cplx<T> ke = scl(accK[m], sc);
-      const T kk[3] = {kx, ky, kz};
-      cplx<T> r[3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c) r[c] = mk(N[c].x + kk[c] * ke.y, N[c].y - kk[c] * ke.x);
-      q[Q_NLH] += w * (proj(r[0], u[0]) + proj(r[1], u[1]));
-      q[Q_NLV] += w * proj(r[2], u[2]);
-      // pressure transfer (stats.jl:764-814)
-      if (I.les) {
-#pragma unroll
-        for (int c = 0; c < 3; ++c) r[c] = r[c] + divT[c];
-      }
-      if (I.density) r[I.gdir] = r[I.gdir] + scl(rho, T(I.gval));
-      const double kdx = (double)kx * r[0].x + (double)ky * r[1].x + (double)kz * r[2].x;
-      const double kdy = (double)kx * r[0].y + (double)ky * r[1].y + (double)kz * r[2].y;
-      const double inv = k0 ? 0.0 : 1.0 / k2d;
-      const double p1x = -kdx * inv, p1y = -kdy * inv;
-      q[Q_PH] += w * (u[0].x * p1x * kxd + u[0].y * p1y * kxd + u[1].x * p1x * kyd + u[1].y * p1y * kyd);
-      q[Q_PV] += w * (u[2].x * p1x * kzd + u[2].y * p1y * kzd);
-      if (I.les) {
-        q[Q_LESH] += w * (proj(divT[0], u[0]) + proj(divT[1], u[1]));
-        q[Q_LESV] += w * proj(divT[2], u[2]);
-      }
-      if (I.hv) {
-        double km = 1.0;
-        for (int i = 0; i < I.hv_m; ++i) km *= k2d;
-        q[Q_HVH] += w * km * (a2[0] + a2[1]);
-        q[Q_HVV] += w * km * a2[2];
-      }
-      if (I.density) {
-        const double r2 = proj(rho, rho);
-        if (k0) q[Q_RHO] += rho.x;
-        q[Q_RHO2] += w * r2;
-        q[Q_DR1] += w * kxd * kxd * r2; q[Q_DR2] += w * kyd * kyd * r2; q[Q_DR3] += w * kzd * kzd * r2;
-        q[Q_BF] += w * proj(u[I.gdir], rho);
-      }
-      if (I.forcing && mode == 0 && k2d > 0.0 && k2d <= kf2) {
-        const double f = (double)fdt;
-        q[Q_HP] += w * (f * (a2[0] + a2[1]) + 0.5 * f * f * (a2[0] + a2[1]));
-        q[Q_VP] += w * (f * a2[2] + 0.5 * f * f * a2[2]);
-      }
-      // integral-length plane sums (stats.jl:952-980)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        if (ix == 0) q[Q_IL0 + 3 * c + 0] += a2[c];
-        if (ky_i == 0) q[Q_IL0 + 3 * c + 1] += w * a2[c];
-        if (kz_i == 0) q[Q_IL0 + 3 * c + 2] += w * a2[c];
-      }
-    }
-    if (spec_t) {
-      // spectrum_u + calculate_specHV (spec.jl:316-327, 424-450)
-      const double hh = 0.5 * (proj(u[0], u[0]) + proj(u[1], u[1]));
-      const double vv = 0.5 * proj(u[2], u[2]);
-      const long long rec = S->nspec;
-      if (rec < I.spec_cap) {
-        double* sp = I.spec + rec * 4LL * (I.nbinH > I.nbinV ? I.nbinH : I.nbinV);
-        const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
-        const int nk = (int)rint(fabs((double)kz) / I.dkz);
-        const int nj = (int)rint(fabs((double)ky) / I.maxdkh);
-        const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
-        double vals[2] = {hh, vv};
-        for (int s = 0; s < 2; ++s) {
-          double* H = sp + (2 * s) * stride;
-          double* V = sp + (2 * s + 1) * stride;
-          const double ee = vals[s];
-          if (ix == 0) {
-            if (nj < I.nbinH) { atomicAdd(&H[0], 0.5 * ee); atomicAdd(&H[nj], 0.5 * ee); }
-            if (nk < I.nbinV) atomicAdd(&V[nk], ee);
-          } else {
-            const double e2 = 2.0 * ee;
-            if (nx < I.nbinH) atomicAdd(&H[nx], 0.5 * e2 * I.maxdkh);
-            if (nj < I.nbinH) atomicAdd(&H[nj], 0.5 * e2 * I.maxdkh);
-            if (nk < I.nbinV) atomicAdd(&V[nk], e2 * I.dkz);
-          }
-        }
-      }
-    }
-
     if (mode == 1) {   // initialize!: fm1 = fm2 = rhs (Adams_Bashforth.jl:28-35, ETD.jl:99-108)
 #pragma unroll
-      for (int c = 0; c < 3; ++c) { hA[c * cs + gi] = rhs[c]; hB[c * cs + gi] = rhs[c]; }
-      if (I.density) { hA[3 * cs + gi] = rrhs; hB[3 * cs + gi] = rrhs; }
+      for (int c = 0; c < 3; ++c) { hA[c * cs + g] = rhs[c]; hB[c * cs + g] = rhs[c]; }
+      if (I.density) { hA[3 * cs + g] = rrhs; hB[3 * cs + g] = rrhs; }
       continue;
     }
-    // time step
-    cplx<T> f1[3], f2[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) { f1[c] = hA[c * cs + gi]; f2[c] = hB[c * cs + gi]; }
     T E, A, B, C;
+    const long long te = I.uniformL ? (long long)(ix * ix + ky_i * ky_i + kz_i * kz_i) : g;   // ETD table entry
     if (I.ab3) {
-      if (stage == 2) {   // fix_fm2! (ETD.jl:130-140)
-        const T f = T(-(dt3 + dt2) / dt2);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) f2[c] = scl(rhs[c] - f1[c], f) + rhs[c];
-      }
       E = T(1); A = At; B = Bt; C = Ct;
-    } else if (I.uniformL) {
-      const int qq = ix * ix + ky_i * ky_i + kz_i * kz_i;
-      const T* e = I.etab + 4 * (size_t)qq;
-      E = e[0]; A = e[1]; B = e[2]; C = e[3];
     } else {
-      double e, a, b, cc;
-      etd_coeffs(c_vel(I, (double)k2), dt, dt2, dt3, stage, e, a, b, cc);
-      E = T(e); A = T(a); B = T(b); C = T(cc);
+      const T* e = I.etab + 4 * te;
+      E = e[0]; A = e[1]; B = e[2]; C = e[3];
     }
+    const bool band = I.forcing && k2 > T(0) && k2 <= I.kf2_t;
     cplx<T> un[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
+      const cplx<T> f1 = hA[c * cs + g];
+      cplx<T> f2 = hB[c * cs + g];
+      if (I.ab3 && stage == 2) f2 = scl(rhs[c] - f1, fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
       // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
-      un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
-    }
-    if (I.forcing && (double)k2 > 0.0 && (double)k2 <= kf2) {
-#pragma unroll
-      for (int c = 0; c < 3; ++c) un[c] = un[c] + scl(u[c], fdt);
+      un[c] = scl(rhs[c], A) + (scl(f1, B) + (scl(f2, C) + scl(u[c], E)));
+      if (band) un[c] = un[c] + scl(u[c], fdt);   // forcing increment (add_forcing!)
     }
     {  // projection after the update (time_step_functions.jl:78)
       const cplx<T> kd = mk(kx * un[0].x + ky * un[1].x + kz * un[2].x, kx * un[0].y + ky * un[1].y + kz * un[2].y);
@@ -738,47 +668,171 @@ __global__ void __launch_bounds__(512) k_fwd_z_update(Inst<T> I, FieldList F, in
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      bad |= !(isfinite((double)un[c].x) && isfinite((double)un[c].y));
-      I.uh[c * cs + gi] = un[c];
-      hB[c * cs + gi] = rhs[c];
+      bad |= !(isfinite(un[c].x) && isfinite(un[c].y));
+      uh[c * cs + g] = un[c];
+      hB[c * cs + g] = rhs[c];
     }
     if (I.density) {
-      cplx<T> r1 = hA[3 * cs + gi], r2 = hB[3 * cs + gi];
+      const cplx<T> r1 = hA[3 * cs + g];
+      cplx<T> r2 = hB[3 * cs + g];
       if (I.ab3) {
-        if (stage == 2) r2 = scl(rrhs - r1, T(-(dt3 + dt2) / dt2)) + rrhs;
+        if (stage == 2) r2 = scl(rrhs - r1, fix2) + rrhs;
         E = T(1); A = At; B = Bt; C = Ct;
-      } else if (I.uniformL) {
-        const int qq = ix * ix + ky_i * ky_i + kz_i * kz_i;
-        const T* e = I.etab_rho + 4 * (size_t)qq;
-        E = e[0]; A = e[1]; B = e[2]; C = e[3];
       } else {
-        double e, a, b, cc;
-        etd_coeffs((double)k2 * (-I.alpha), dt, dt2, dt3, stage, e, a, b, cc);
-        E = T(e); A = T(a); B = T(b); C = T(cc);
+        const T* e = I.etab_rho + 4 * te;
+        E = e[0]; A = e[1]; B = e[2]; C = e[3];
       }
-      cplx<T> rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + scl(rho, E)));
-      bad |= !(isfinite((double)rn.x) && isfinite((double)rn.y));
-      I.uh[3 * cs + gi] = rn;
-      hB[3 * cs + gi] = rrhs;
+      const cplx<T> rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + scl(rho, E)));
+      bad |= !(isfinite(rn.x) && isfinite(rn.y));
+      uh[3 * cs + g] = rn;
+      hB[3 * cs + g] = rrhs;
     }
   }
   if (mode == 0 && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&I.st->err, 1u);
+}
 
-  // 3. stats partials of this CTA (fixed-order reduction: warp shuffle tree, then warps)
-  if (do_stats) {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const long long cta = (long long)blockIdx.y * gridDim.x + blockIdx.x;
-    for (int i = 0; i < Q_COUNT; ++i) {
-      double v = q[i];
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[i][w] = v;
+// ====================================================================================
+// Stats and spectra of the state before the update: u from the spectral state, N, ke,
+// i k.tau from the scratch buffer written by k_fwd_z (stats.jl:64-219,
+// 289-307, 532-561, 608-705, 750-814, 897-980; spec.jl:316-327, 424-450;
+// density_stratification_types.jl:192-211). Grid-stride over the retained modes, FP64
+// accumulation, fixed-order per-CTA partials for k_finalize. Runs at stats/spectrum
+// iterations only (returns at once otherwise).
+// ====================================================================================
+template <typename T>
+__global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
+  const DevState* S = I.st;
+  const long long it = S->iteration;
+  const bool stats_t = (it % I.dt_stat) == 0;
+  const bool spec_t = mode == 0 && (it % I.dt_spec) == 0;
+  if (!stats_t && !spec_t) return;
+  __shared__ double red[Q_COUNT][9];
+  const long long cs = I.cstride;
+  const cplx<T>* sb = I.sbuf;
+  const cplx<T>* ub = I.uh;
+  const long long total = cs;
+  const double fdt = S->dt * S->force_coef;
+  const double kf2 = I.f_kf * I.f_kf;
+  const long long rec = S->nspec;
+  const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
+  double* sp = I.spec + rec * 4LL * stride;
+  double q[Q_COUNT];
+#pragma unroll
+  for (int i = 0; i < Q_COUNT; ++i) q[i] = 0.0;
+  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(g % I.KXP);
+    if (ix >= I.Mx) continue;
+    const long long r = g / I.KXP;
+    const int jc = (int)(r % I.NYR), kc = (int)(r / I.NYR);
+    const int ky_i = ysig(I, jc), kz_i = zsig(I, kc);
+    const double kx = (double)ix / I.lx, ky = (double)ky_i / I.ly, kz = (double)kz_i / I.lz;
+    const double k2 = kx * kx + (ky * ky + kz * kz);
+    const double w = ix > 0 ? 2.0 : 1.0;
+    const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
+    cplx<T> u[3];
+    double a2[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { u[c] = ub[c * cs + g]; a2[c] = proj(u[c], u[c]); }
+    if (spec_t && rec < I.spec_cap) {
+      const double hh = 0.5 * (a2[0] + a2[1]), vv = 0.5 * a2[2];
+      const int nk = (int)rint(fabs(kz) / I.dkz), nj = (int)rint(fabs(ky) / I.maxdkh), nx = (int)rint(fabs(kx) / I.maxdkh);
+      const double vals[2] = {hh, vv};
+#pragma unroll
+      for (int s2 = 0; s2 < 2; ++s2) {
+        double* H = sp + (2 * s2) * stride;
+        double* V = sp + (2 * s2 + 1) * stride;
+        const double ee = vals[s2];
+        if (ix == 0) {
+          if (nj < I.nbinH) { atomicAdd(&H[0], 0.5 * ee); atomicAdd(&H[nj], 0.5 * ee); }
+          if (nk < I.nbinV) atomicAdd(&V[nk], ee);
+        } else {
+          const double e2 = 2.0 * ee;
+          if (nx < I.nbinH) atomicAdd(&H[nx], 0.5 * e2 * I.maxdkh);
+          if (nj < I.nbinH) atomicAdd(&H[nj], 0.5 * e2 * I.maxdkh);
+          if (nk < I.nbinV) atomicAdd(&V[nk], e2 * I.dkz);
+        }
+      }
     }
-    __syncthreads();
-    if (threadIdx.x < Q_COUNT) {
-      double s = 0.0;
-      for (int i = 0; i < nw; ++i) s += red[threadIdx.x][i];
-      I.partials[cta * QPAD + threadIdx.x] = s;
+    if (!stats_t) continue;
+    // velocity moments (velocity_stats, viscosity_stats, d*_squared_mean)
+    if (k0) { q[Q_U1] += (double)u[0].x; q[Q_U2] += (double)u[1].x; q[Q_U3] += (double)u[2].x; }
+    q[Q_U12] += w * a2[0]; q[Q_U22] += w * a2[1]; q[Q_U32] += w * a2[2];
+    q[Q_EH] += w * k2 * (a2[0] + a2[1]); q[Q_EV] += w * k2 * a2[2];
+    q[Q_D1DY] += w * ky * ky * a2[0]; q[Q_D1DX] += w * kx * kx * a2[0];
+    q[Q_D2DY] += w * ky * ky * a2[1]; q[Q_D2DX] += w * kx * kx * a2[1];
+    // non-linear transfer: (N - i k ke) . u (stats.jl:897-917)
+    const cplx<T> ke = sb[3 * cs + g];
+    const double kk[3] = {kx, ky, kz};
+    double rx[3], ry[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const cplx<T> Nc = sb[c * cs + g];
+      rx[c] = (double)Nc.x + kk[c] * (double)ke.y;
+      ry[c] = (double)Nc.y - kk[c] * (double)ke.x;
     }
+    q[Q_NLH] += w * (rx[0] * u[0].x + ry[0] * u[0].y + rx[1] * u[1].x + ry[1] * u[1].y);
+    q[Q_NLV] += w * (rx[2] * u[2].x + ry[2] * u[2].y);
+    // pressure transfer (stats.jl:764-814): rhs - i k ke (+ i k.tau + rho g), projected part
+    if (I.les) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const cplx<T> dT = sb[(4 + c) * cs + g];
+        rx[c] += (double)dT.x; ry[c] += (double)dT.y;
+        const double pr = proj(dT, u[c]);
+        if (c < 2) q[Q_LESH] += w * pr; else q[Q_LESV] += w * pr;
+      }
+    }
+    cplx<T> rho = mk(T(0), T(0));
+    if (I.density) {
+      rho = ub[3 * cs + g];
+      rx[I.gdir] += (double)rho.x * I.gval; ry[I.gdir] += (double)rho.y * I.gval;
+    }
+    const double kdx = kx * rx[0] + ky * rx[1] + kz * rx[2];
+    const double kdy = kx * ry[0] + ky * ry[1] + kz * ry[2];
+    const double inv = k0 ? 0.0 : 1.0 / k2;
+    const double p1x = -kdx * inv, p1y = -kdy * inv;
+    q[Q_PH] += w * (u[0].x * p1x * kx + u[0].y * p1y * kx + u[1].x * p1x * ky + u[1].y * p1y * ky);
+    q[Q_PV] += w * (u[2].x * p1x * kz + u[2].y * p1y * kz);
+    if (I.hv) {
+      double km = 1.0;
+      for (int i = 0; i < I.hv_m; ++i) km *= k2;
+      q[Q_HVH] += w * km * (a2[0] + a2[1]);
+      q[Q_HVV] += w * km * a2[2];
+    }
+    if (I.forcing && mode == 0 && k2 > 0.0 && k2 <= kf2) {
+      q[Q_HP] += w * (fdt * (a2[0] + a2[1]) + 0.5 * fdt * fdt * (a2[0] + a2[1]));
+      q[Q_VP] += w * (fdt * a2[2] + 0.5 * fdt * fdt * a2[2]);
+    }
+    if (I.density) {
+      const double r2 = proj(rho, rho);
+      if (k0) q[Q_RHO] += (double)rho.x;
+      q[Q_RHO2] += w * r2;
+      q[Q_DR1] += w * kx * kx * r2; q[Q_DR2] += w * ky * ky * r2; q[Q_DR3] += w * kz * kz * r2;
+      q[Q_BF] += w * proj(u[I.gdir], rho);
+    }
+    // integral-length plane sums (stats.jl:952-980)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (ix == 0) q[Q_IL0 + 3 * c + 0] += a2[c];
+      if (ky_i == 0) q[Q_IL0 + 3 * c + 1] += w * a2[c];
+      if (kz_i == 0) q[Q_IL0 + 3 * c + 2] += w * a2[c];
+    }
+  }
+  if (!stats_t) return;
+  // fixed-order CTA reduction: warp shuffle tree, then warps in order
+  const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int i = 0; i < Q_COUNT; ++i) {
+    double v = q[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[i][wv] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < Q_COUNT) {
+    double sum = 0.0;
+    for (int i = 0; i < nw; ++i) sum += red[threadIdx.x][i];
+    I.partials[(long long)blockIdx.x * QPAD + threadIdx.x] = sum;
   }
 }
 
@@ -882,9 +936,9 @@ __global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
   constexpr int L = 2 * LYZ_IO;   // up to 4 fields -> 2 complex lines per (y,z)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = I.nx;
-  cplx<T>* sx = reinterpret_cast<cplx<T>*>(smem_raw);   // [n][L+1]
-  cplx<T>* s0 = sx + n * (L + 1);
-  cplx<T>* s1 = s0 + n * L;
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);   // [n][L+1]
+  cplx<T>* s1 = s0 + n * (L + 1);
+  cplx<T>* sx = fft_result_buffer(I.px, s0, s1);
   const int g0 = blockIdx.x * LYZ_IO;
   const long long plane = (long long)I.ny * I.nz * n;
   auto ld = [&](int l, int j) -> cplx<T> {
@@ -896,7 +950,7 @@ __global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
     return mk(a, b);
   };
   auto st = [&](int l, int j, cplx<T> v) { sx[j * (L + 1) + l] = v; };
-  fft_lines<-1, L, T>(I.px, s0, s1, L, I.twx, ld, st);
+  fft_lines<-1, L, T>(I.px, s0, s1, L + 1, I.twx, ld, st);
   const int KXP = I.KXP;
   for (int e = threadIdx.x; e < L * KXP; e += blockDim.x) {
     const int k = e % KXP, l = e / KXP, p = l / LYZ_IO, q = l % LYZ_IO;
@@ -915,7 +969,7 @@ __global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
 
 // wz slots -> compact spectral state: forward z, 1/N scaling, dealias (myfourier!)
 template <typename T, int TX>
-__global__ void __launch_bounds__(512) k_fwd_z_store(Inst<T> I, FieldList F) {
+__global__ void __launch_bounds__(FFS_MAXT) k_fwd_z_store(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + I.nz * TX;

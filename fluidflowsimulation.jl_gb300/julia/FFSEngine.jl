@@ -1,0 +1,173 @@
+# FFSEngine: Julia-side binding of libffs (the GB300 solver-step engine).
+#
+# Drop-in for FluidFlowSimulation.jl's time loop: `run_simulation()` reads the same
+# `global` file and u1.$start/u2.$start/u3.$start (+ rho.$start) fields, runs
+# initialize! and advance_in_time! on the GPU through the C ABI of include/ffs.h, and
+# writes Stats.txt and the field files in the reference formats.
+#
+# Usage (with libffs.so built):  ENV["FFS_LIB"] = "/path/to/libffs.so"
+#   using FFSEngine; run_simulation()
+module FFSEngine
+
+export run_simulation, FFSParams, Engine, initialize!, advance_in_time!, getfields
+
+const LIB = get(ENV, "FFS_LIB", joinpath(@__DIR__, "..", "libffs.so"))
+
+# Layout identical to `ffs_params` in include/ffs.h (natural C alignment).
+mutable struct FFSParams
+    nx::Int32; ny::Int32; nz::Int32
+    lx::Float64; ly::Float64; lz::Float64
+    nu::Float64; cutoff::Float64
+    integrator::Int32; variable_dt::Int32
+    cfl::Float64; dt::Float64
+    hyperviscosity::Int32; hv_nu::Float64; hv_m::Int32
+    les::Int32; smag_c::Float64; filter_width::Float64
+    density::Int32; density_pr::Float64; density_gradient::Float64; gravity::Float64
+    gravity_dir::Int32
+    forcing::Int32; forcing_power::Float64; forcing_kf::Float64
+    precision::Int32; dt_stat::Int32; dt_spec::Int32; write_time::Int32
+    start::Int64; start_time::Float64
+    device::Int32; reference_cfl_slot::Int32
+    stats_capacity::Int32; spec_capacity::Int32
+    FFSParams() = new()
+end
+
+function defaults()
+    p = FFSParams()
+    rc = ccall((:ffs_params_default, LIB), Cint, (Ref{FFSParams},), p)
+    rc == 0 || error("ffs_params_default failed")
+    return p
+end
+
+mutable struct Engine
+    h::Ptr{Cvoid}
+    p::FFSParams
+end
+
+check(e::Engine, rc) = rc == 0 || error(unsafe_string(ccall((:ffs_last_error, LIB), Cstring, (Ptr{Cvoid},), e.h)))
+
+function Engine(p::FFSParams)
+    h = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:ffs_create, LIB), Cint, (Ref{FFSParams}, Ref{Ptr{Cvoid}}), p, h)
+    rc == 0 || error(unsafe_string(ccall((:ffs_last_error, LIB), Cstring, (Ptr{Cvoid},), C_NULL)))
+    e = Engine(h[], p)
+    finalizer(x -> ccall((:ffs_destroy, LIB), Cvoid, (Ptr{Cvoid},), x.h), e)
+    return e
+end
+
+readglobal(path = "global") = Dict(Symbol(first(split(l))) => strip(join(split(l)[2:end], " "))
+                                   for l in eachline(path) if !isempty(strip(l)) && !startswith(strip(l), "//"))
+
+num(s) = Float64(eval(Meta.parse(s)))
+
+# parameters(d) of src/simulationtypes.jl:242-365 for the keys the engine implements
+function parameters(d)
+    p = defaults()
+    p.nx, p.ny, p.nz = parse(Int32, d[:nx]), parse(Int32, d[:ny]), parse(Int32, d[:nz])
+    p.lx, p.ly, p.lz = num(d[:xDomainSize]), num(d[:yDomainSize]), num(d[:zDomainSize])
+    p.nu = num(d[:kinematicViscosity])
+    haskey(d, :cutoff) && (p.cutoff = num(d[:cutoff]))
+    p.start = haskey(d, :start) ? parse(Int, d[:start]) : 0
+    p.start_time = haskey(d, :startTime) ? parse(Float64, d[:startTime]) : 0.0
+    p.dt_stat = parse(Int32, d[:dtStat]); p.dt_spec = parse(Int32, d[:dtSpec]); p.write_time = parse(Int32, d[:writeTime])
+    p.integrator = get(d, :velocityTimeStep, "ETD3rdO") == "Adams_Bashforth3rdO" ? 1 : 0
+    p.variable_dt = haskey(d, :variableTimestepFlag) ? Int32(parse(Bool, d[:variableTimestepFlag])) : 1
+    p.cfl = haskey(d, :cfl) ? parse(Float64, d[:cfl]) : 0.18
+    p.dt = haskey(d, :dt) ? num(d[:dt]) : 0.0
+    if haskey(d, :hyperViscosity)
+        p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
+        p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
+    end
+    if get(d, :lesModel, "") == "Smagorinsky"
+        p.les = 1
+        p.smag_c = haskey(d, :smagorinskyConstant) ? num(d[:smagorinskyConstant]) : 0.17
+        p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) : 0.0
+    end
+    if haskey(d, :densityStratification)
+        p.density = 1; p.density_pr = num(d[:Pr]); p.density_gradient = num(d[:densityGradient])
+        p.gravity = num(d[:zAcceleration]) / num(d[:referenceDensity])
+        p.gravity_dir = Dict("x" => 0, "y" => 1, "z" => 2)[get(d, :gravityDirection, "z")]
+    end
+    if get(d, :forcing, "") == "isotropicBand"
+        p.forcing = 1
+        p.forcing_power = haskey(d, :forcingPower) ? num(d[:forcingPower]) : 0.1
+        p.forcing_kf = haskey(d, :forcingKf) ? num(d[:forcingKf]) : 2.5
+    end
+    p.precision = get(d, :precision, "FP64") == "FP32" ? 1 : 0
+    return p
+end
+
+readfield(f, nx, ny, nz) = (a = Array{Float64}(undef, nx, ny, nz); read!(f, a); a)
+
+function setfields!(e::Engine, u1, u2, u3, rho = nothing)
+    r = rho === nothing ? C_NULL : pointer(rho)
+    GC.@preserve u1 u2 u3 rho check(e, ccall((:ffs_set_fields, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint), e.h, u1, u2, u3, r, 0))
+end
+
+initialize!(e::Engine) = check(e, ccall((:ffs_initialize, LIB), Cint, (Ptr{Cvoid},), e.h))
+advance_in_time!(e::Engine, n::Integer = 1) = check(e, ccall((:ffs_step, LIB), Cint, (Ptr{Cvoid}, Int64), e.h, n))
+iteration(e::Engine) = ccall((:ffs_iteration, LIB), Int64, (Ptr{Cvoid},), e.h)
+simtime(e::Engine) = ccall((:ffs_time, LIB), Float64, (Ptr{Cvoid},), e.h)
+
+function getfields(e::Engine)
+    p = e.p
+    out = [Array{Float64}(undef, p.nx, p.ny, p.nz) for _ in 1:4]
+    rho = p.density == 1 ? pointer(out[4]) : C_NULL
+    GC.@preserve out check(e, ccall((:ffs_get_fields, LIB), Cint,
+        (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint), e.h, out[1], out[2], out[3], rho, 0))
+    return out
+end
+
+function statsrows(e::Engine)
+    nc = ccall((:ffs_record_ncols, LIB), Cint, (Ptr{Cvoid},), e.h)
+    ns = ccall((:ffs_stats_ncols, LIB), Cint, (Ptr{Cvoid},), e.h)
+    n = ccall((:ffs_stats_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, C_NULL, 0)
+    buf = Array{Float64}(undef, nc, max(n, 0))
+    n > 0 && ccall((:ffs_stats_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, buf, n)
+    return buf[1:ns, :]
+end
+
+function statsheader(e::Engine)
+    buf = Vector{UInt8}(undef, 4096)
+    check(e, ccall((:ffs_stats_header, LIB), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64), e.h, buf, 4096))
+    return unsafe_string(pointer(buf))
+end
+
+function writeoutput(e::Engine)
+    f = getfields(e); i = iteration(e)
+    write("u1.$i", f[1]); write("u2.$i", f[2]); write("u3.$i", f[3])
+    e.p.density == 1 && write("rho.$i", f[4])
+end
+
+# run_simulation() of src/FluidFlowSimulation.jl:23-65
+function run_simulation()
+    d = readglobal()
+    p = parameters(d)
+    e = Engine(p)
+    s = p.start
+    u = [open(f -> readfield(f, p.nx, p.ny, p.nz), "u$i.$s") for i in 1:3]
+    rho = (p.density == 1 && isfile("rho.$s")) ? open(f -> readfield(f, p.nx, p.ny, p.nz), "rho.$s") : nothing
+    setfields!(e, u..., rho)
+    s == 0 && open(f -> write(f, statsheader(e), "\n"), "Stats.txt", "w")
+    initialize!(e)
+    total = haskey(d, :nt) ? parse(Int, d[:nt]) : typemax(Int) - s
+    final = s + total
+    flush() = open("Stats.txt", "a+") do f
+        for r in eachcol(statsrows(e))
+            join(f, (Int(r[1]), r[2:end]..., "\n"), ",", "")
+        end
+    end
+    while iteration(e) < final
+        it = iteration(e)
+        nxt = min(final, (it ÷ p.write_time + 1) * p.write_time)
+        advance_in_time!(e, nxt - it)
+        flush()
+        (iteration(e) % p.write_time == 0 && iteration(e) < final) && writeoutput(e)
+    end
+    flush()
+    iteration(e) % p.write_time != 0 && writeoutput(e)
+    return e
+end
+
+end # module

@@ -25,6 +25,8 @@ from dataclasses import dataclass, field
 import numpy as np
 import scipy.fft as sfft
 
+from . import ddmath as dd
+
 _WORKERS = int(os.environ.get("FFS_ORACLE_WORKERS", os.cpu_count() or 1))
 
 
@@ -297,17 +299,18 @@ class ETD3:
         """ETD.jl:142-227 (Taylor branch when -c dt <= 1e-4, zero when c == -Inf)."""
         l1 = self.c
         dt, dt2, dt3 = self.dt, self.dt2, self.dt3
+        # left-to-right evaluation exactly as written in ETD.jl:198-227 / 164-191
         a0 = (dt * (2 * dt * dt + 6 * dt2 * (dt2 + dt3) + 3 * dt * (2 * dt2 + dt3))) / (6 * dt2 * (dt2 + dt3))
-        a1 = (dt * dt * (dt ** 2 + 6 * dt2 * (dt2 + dt3) + 2 * dt * (2 * dt2 + dt3))) / (12 * dt2 * (dt2 + dt3))
+        a1 = (dt * dt * (dt * dt + 6 * dt2 * (dt2 + dt3) + 2 * dt * (2 * dt2 + dt3))) / (12 * dt2 * (dt2 + dt3))
         a2 = (dt * dt * dt * (4 * dt2 * (dt2 + dt3) + dt * (2 * dt2 + dt3))) / (24 * dt2 * (dt2 + dt3))
         a3 = dt * dt * dt * dt / 24
-        b0 = -((dt ** 2 * (2 * dt + 3 * (dt2 + dt3))) / (6 * (dt2 * dt3)))
+        b0 = -((dt * dt * (2 * dt + 3 * (dt2 + dt3))) / (6 * (dt2 * dt3)))
         b1 = -(((dt * dt * dt * (dt + 2 * (dt2 + dt3)))) / (12 * (dt2 * dt3)))
         b2 = -((dt * dt * dt * dt * (dt2 + dt3)) / (24 * (dt2 * dt3)))
         c0 = (dt * dt * (2 * dt + 3 * dt2)) / (6 * dt3 * (dt2 + dt3))
         c1 = (dt * dt * dt * (dt + 2 * dt2)) / (12 * dt3 * (dt2 + dt3))
         c2 = (dt * dt * dt * dt * dt2) / (24 * dt3 * (dt2 + dt3))
-        e1 = dt ** 2 + dt * (2 * dt2 + dt3)
+        e1 = dt * dt + dt * (2 * dt2 + dt3)
         e2 = dt2 * (dt2 + dt3)
         e3 = 2 * dt
         e4 = 2 * dt2 + dt3
@@ -318,15 +321,16 @@ class ETD3:
         e9 = dt3 * (dt2 + dt3)
         l2 = l1 * l1
         l3 = l2 * l1
-        test = -l1 * dt <= 1e-4
+        test = (-l1) * dt <= 1e-4
         with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
-            em = np.expm1(l1 * dt)
-            At = np.where(test, a1 * l1 + (a2 * l2 + (a3 * l3 + a0)),
-                          (2 * em - l2 * (e1 - e2 * em) - l1 * (e3 - e4 * em)) / (l3 * e2))
-            Bt = np.where(test, b1 * l1 + (b2 * l2 + b0),
-                          (e5 * l2 - 2 * em + l1 * (e3 - e6 * em)) / (l3 * e7))
-            Ct = np.where(test, c1 * l1 + (c2 * l2 + c0),
-                          (2 * em - e8 * l2 - l1 * (e3 - dt2 * em)) / (l3 * e9))
+            em = dd.expm1(l1 * dt)
+            # muladd -> single-rounding fma (dd.fma) in the Taylor branch
+            At = np.where(test, dd.fma(a1, l1, dd.fma(a2, l2, dd.fma(a3, l3, a0))),
+                          ((2 * em - l2 * (e1 - e2 * em)) - l1 * (e3 - e4 * em)) / (l3 * e2))
+            Bt = np.where(test, dd.fma(b1, l1, dd.fma(b2, l2, b0)),
+                          ((e5 * l2 - 2 * em) + l1 * (e3 - e6 * em)) / (l3 * e7))
+            Ct = np.where(test, dd.fma(c1, l1, dd.fma(c2, l2, c0)),
+                          ((2 * em - e8 * l2) - l1 * (e3 - dt2 * em)) / (l3 * e9))
         inf = l1 == -np.inf
         self.At = np.where(inf, 0.0, At)
         self.Bt = np.where(inf, 0.0, Bt)
@@ -344,9 +348,9 @@ class ETD3:
                 c2dt3 = cdt2 * cdt
                 c3dt4 = c2dt3 * cdt
                 test = -cdt <= 1e-4
-                phi = np.where(test, dt + 0.5 * cdt2 + c2dt3 / 6 + c3dt4 / 24, np.expm1(cdt) / c)
+                phi = np.where(test, dt + 0.5 * cdt2 + c2dt3 / 6 + c3dt4 / 24, dd.expm1(cdt) / c)
                 phi = np.where(c == -np.inf, 0.0, phi)
-                unew = np.exp(cdt) * u + phi * rhs
+                unew = dd.exp(cdt) * u + phi * rhs
             elif self.iteration == 2:                 # ETD1stand2ndO.jl:37-66
                 dt2 = self.dt2
                 cp2 = c * c
@@ -354,7 +358,7 @@ class ETD3:
                 cdtp2 = cdt * dt
                 c2dtp3 = cdtp2 * cdt
                 c3dtp4 = c2dtp3 * cdt
-                em = np.expm1(cdt)
+                em = dd.expm1(cdt)
                 c2dt2 = c * c * dt2
                 dtp2 = dt * dt
                 dtp3 = dtp2 * dt
@@ -369,11 +373,11 @@ class ETD3:
                 inf = c == -np.inf
                 At = np.where(inf, 0.0, At)
                 Bt = np.where(inf, 0.0, Bt)
-                unew = np.exp(cdt) * u + (At * rhs + Bt * self.fm1)
+                unew = dd.exp(cdt) * u + (At * rhs + Bt * self.fm1)
             else:
                 if self.adaptive:                     # set_coefficients!, ETD.jl:116-123
                     self.set_ABCt()
-                unew = self.At * rhs + (self.Bt * self.fm1 + (self.Ct * self.fm2 + np.exp(c * dt) * u))
+                unew = self.At * rhs + (self.Bt * self.fm1 + (self.Ct * self.fm2 + dd.exp(c * dt) * u))
         self.fm2 = self.fm1
         self.fm1 = rhs.copy()
         return unew
@@ -419,9 +423,16 @@ class OracleSimulation:
         if p.density:
             self.rho = (np.zeros((p.nz, p.ny, p.nx)) if rho_phys is None
                         else np.asarray(rho_phys, dtype=np.float64))
-        c = -p.nu * g.K2                                     # init_c!, ETD.jl:60-69
+        # c = -nu k^2 (init_c!, ETD.jl:60-69) or muladd(k2, -nu, k2^M * -nuh) (init_c_hv!,
+        # ETD.jl:84-95), with k2 = muladd(KX,KX, muladd(KY,KY, KZ*KZ))
+        k2 = dd.fma(*np.broadcast_arrays(g.KX, g.KX, dd.fma(*np.broadcast_arrays(g.KY, g.KY, g.KZ * g.KZ))))
+        c = k2 * (-p.nu)
         if p.hv:
-            c = g.K2 * (-p.nu) + (g.K2 ** p.hv_m) * (-p.hv_nu)  # init_c_hv!, ETD.jl:84-95
+            km = k2.copy()
+            for _ in range(p.hv_m - 1):
+                km = km * k2
+            c = dd.fma(k2, np.full_like(k2, -p.nu), km * (-p.hv_nu))
+        self.k2_ref = k2
         if p.ab3:
             self.ts = AB3(p.variable_dt, p.dt)
         else:
@@ -431,7 +442,7 @@ class OracleSimulation:
             if p.ab3:
                 self.rts = AB3(p.variable_dt, p.dt)
             else:
-                self.rts = ETD3(p.variable_dt, p.dt, -alpha * g.K2)
+                self.rts = ETD3(p.variable_dt, p.dt, k2 * (-alpha))
             self.alpha = alpha
         self.gvec = np.zeros(3)
         if p.density:
@@ -779,16 +790,21 @@ class OracleSimulation:
         nx = np.rint(np.abs(g.kx) / g.MAXDKH).astype(np.int64)
         keep = g.keep
         o = np.where(keep, out, 0.0)
+        # Bins past the end are dropped: the reference writes them under @inbounds (out of
+        # bounds when ny > nx or nz differs), the engine skips them.
+        def add(a, idx, val):
+            ok = idx < len(a)
+            np.add.at(a, idx[ok], val[ok])
         # i = 1 (kx = 0) terms
         e0 = o[:, :, 0]
-        h[0] += 0.5 * float(np.sum(e0))
-        np.add.at(h, nj, 0.5 * np.sum(e0, axis=0))
-        np.add.at(v, nk, np.sum(e0, axis=1))
+        h[0] += 0.5 * float(np.sum(e0[:, nj < len(h)]))
+        add(h, nj, 0.5 * np.sum(e0, axis=0))
+        add(v, nk, np.sum(e0, axis=1))
         # i >= 2 terms
         e = 2.0 * o[:, :, 1:]
-        np.add.at(h, nx[1:], 0.5 * g.MAXDKH * np.sum(e, axis=(0, 1)))
-        np.add.at(h, nj, 0.5 * g.MAXDKH * np.sum(e, axis=(0, 2)))
-        np.add.at(v, nk, g.DKZ * np.sum(e, axis=(1, 2)))
+        add(h, nx[1:], 0.5 * g.MAXDKH * np.sum(e, axis=(0, 1)))
+        add(h, nj, 0.5 * g.MAXDKH * np.sum(e, axis=(0, 2)))
+        add(v, nk, g.DKZ * np.sum(e, axis=(1, 2)))
         return h, v
 
     # ---------------------------------------------------------------- accessors

@@ -1,0 +1,223 @@
+"""Parity of the CUDA engine (through the C ABI) with the FP64 CPU oracle.
+
+Tolerances: FP64 fields 1e-12 relative L2 per component after 10 steps, FP64 stats rows
+1e-10 relative; FP32 fields 1e-4 relative L2 after 10 steps. Adaptive-dt ETD runs are
+an exception (see test_etd_adaptive_parity): their dt comes from a max over FFT output,
+which differs from any other FFT in the last bit, and the reference's own ETD
+coefficient formulas amplify such a difference ~1e7 times.
+"""
+import numpy as np
+import pytest
+
+from oracle.ffs_oracle import Grid, OracleSimulation, Params
+
+pytestmark = pytest.mark.gpu
+
+FP64_FIELD_TOL = 1e-12
+FP64_STATS_TOL = 1e-10
+FP32_FIELD_TOL = 1e-4
+
+
+def gdict(n, integ="Adams_Bashforth3rdO", adaptive=False, dt="0.01", ny=None, nz=None, **kw):
+    d = {"nx": str(n), "ny": str(ny or n), "nz": str(nz or n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": "0.01", "dtStat": "2", "dtSpec": "3", "writeTime": "1000",
+         "velocityTimeStep": integ, "variableTimestepFlag": "true" if adaptive else "false", "cfl": "0.5",
+         "dt": dt}
+    d.update({k: str(v) for k, v in kw.items()})
+    return d
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / nb if nb > 0 else np.linalg.norm(a - b)
+
+
+def make_ic(pkg, d, seed=7, k0=3.0, density=False):
+    nx, ny, nz = int(d["nx"]), int(d["ny"]), int(d["nz"])
+    if nx == ny == nz:
+        u = pkg.random_spectrum(nx, k0=k0, seed=seed)
+    else:
+        rng = np.random.default_rng(seed)
+        g = Grid(nx, ny, nz)
+        uh = np.stack([g.myfourier(rng.standard_normal((nz, ny, nx))) for _ in range(3)])
+        uh = g.project(uh) * np.exp(-np.sqrt(g.K2) / 4)[None]
+        u = tuple(g.real(uh))
+    rho = None
+    if density:
+        rho = 0.1 * pkg.random_spectrum(nx, k0=k0, seed=seed + 1)[0] if nx == ny == nz else None
+    return u, rho
+
+
+def run_pair(pkg, d, steps=10, precision="FP64", seed=7, density=False):
+    u, rho = make_ic(pkg, d, seed=seed, density=density)
+    sim = pkg.Simulation.from_global(d, precision=precision)
+    sim.set_fields(*u, rho)
+    sim.initialize()
+    sim.advance_in_time(steps)
+    ref = OracleSimulation(Params.from_global(d), u, rho)
+    ref.initialize()
+    ref.run(steps)
+    return sim, ref
+
+
+FIXED_CASES = {
+    "ab3-32": gdict(32),
+    "ab3-48-radix3": gdict(48),
+    "ab3-64-hv-forced": gdict(64, hyperViscosity="true", hyperViscosityCoefficient="1e-6",
+                              forcing="isotropicBand", forcingPower="0.1", forcingKf="2.5"),
+    "ab3-noncubic": gdict(32, ny=48, nz=64),
+    "etd-32": gdict(32, "ETD3rdO"),
+    "etd-96": gdict(96, "ETD3rdO", dt="0.005"),
+    "etd-les-density": gdict(32, "ETD3rdO", lesModel="Smagorinsky", densityStratification="true", Pr="1",
+                             densityGradient="1", zAcceleration="1", referenceDensity="1"),
+    "etd-hv-L2": gdict(32, "ETD3rdO", hyperViscosity="true", hyperViscosityCoefficient="1e-5",
+                       xDomainSize="2.0", yDomainSize="2.0", zDomainSize="2.0"),
+    "ab3-adaptive": gdict(32, adaptive=True),
+    "ab3-adaptive-density": gdict(32, adaptive=True, densityStratification="true", Pr="2", densityGradient="1",
+                                  zAcceleration="1", referenceDensity="1"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FIXED_CASES))
+def test_fp64_step_parity(gpu_pkg, name):
+    d = FIXED_CASES[name]
+    sim, ref = run_pair(gpu_pkg, d, density="densityStratification" in d)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= FP64_FIELD_TOL, (name, c)
+    if "densityStratification" in d:
+        assert rel(sim.spectral(3), ref.rho) <= FP64_FIELD_TOL
+    rows = sim.stats_rows()
+    rr = np.array(ref.stats_rows)
+    assert rows.shape == rr.shape
+    assert sim.header.count(",") + 1 == rows.shape[1]
+    # relative error per entry, with an absolute floor of 1e-6 x the table's largest entry
+    # for columns that are mathematically zero (mean velocity, net transfer: ~1e-20 noise)
+    scale = np.maximum(np.abs(rr), 1e-6 * np.abs(rr).max())
+    err = np.abs(rows - rr) / scale
+    assert err.max() <= FP64_STATS_TOL, (name, np.unravel_index(err.argmax(), err.shape), err.max())
+    assert sim.iteration == ref.iteration
+    assert sim.time == pytest.approx(ref.time, rel=1e-14)
+    sim.close()
+
+
+def test_etd_adaptive_parity(gpu_pkg):
+    """Adaptive ETD: dt = cfl dx / max|u| follows the FFT output; a last-bit difference in
+    dt changes the rounding of the reference's cancelling phi formulas (ETD.jl:181-191),
+    so the bar here is the oracle's own sensitivity: 1e-8 after 10 steps."""
+    d = gdict(32, "ETD3rdO", adaptive=True)
+    sim, ref = run_pair(gpu_pkg, d)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= 1e-8
+    assert sim.dt == pytest.approx(ref.get_dt(), rel=1e-13)
+
+
+@pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced"])
+def test_fp32_error(gpu_pkg, name):
+    d = FIXED_CASES[name]
+    sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= FP32_FIELD_TOL, (name, c)
+    sim.close()
+
+
+def test_transform_roundtrip(gpu_pkg):
+    """set_fields = myfourier! (utils.jl:101-106); get_fields = real! (unnormalised c2r)."""
+    n = 48
+    d = gdict(n)
+    u, _ = make_ic(gpu_pkg, d)
+    g = Grid(n, n, n)
+    for prec, tol in (("FP64", 1e-14), ("FP32", 1e-6)):
+        sim = gpu_pkg.Simulation.from_global(d, precision=prec)
+        rng = np.random.default_rng(3)
+        raw = [rng.standard_normal((n, n, n)) for _ in range(3)]
+        sim.set_fields(*raw)
+        for c in range(3):
+            assert rel(sim.spectral(c), g.myfourier(raw[c])) <= tol
+        f = sim.fields()
+        for c in range(3):
+            assert rel(f[c], g.real(g.myfourier(raw[c]))) <= tol
+        # padded layout round trip
+        fp = sim.fields(layout=1)
+        assert fp[0].shape == (n, n, 2 * (n // 2 + 1))
+        assert np.array_equal(fp[0][:, :, :n], f[0]) and not fp[0][:, :, n:].any()
+        sim.close()
+
+
+def test_spectrum_parity(gpu_pkg):
+    d = gdict(32, dtSpec="2")
+    u, _ = make_ic(gpu_pkg, d)
+    sim = gpu_pkg.Simulation.from_global(d)
+    sim.set_fields(*u)
+    sim.initialize()
+    sim.advance_in_time(5)
+    ref = OracleSimulation(Params.from_global(d), u)
+    ref.initialize()
+    ref.run(5)
+    got = sim.spectra()
+    assert [r["iteration"] for r in got] == sorted(ref.spectra)
+    for r in got:
+        e = ref.spectra[r["iteration"]]
+        for key in ("u_h.specH", "u_h.specV", "u.specH", "u_v.specH", "u_v.specV"):
+            assert np.allclose(r[key], e[key], rtol=1e-12, atol=1e-15 * np.abs(e[key]).max()), key
+
+
+def test_errors_and_state_checks(gpu_pkg):
+    d = gdict(32)
+    sim = gpu_pkg.Simulation.from_global(d)
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        sim.advance_in_time(1)           # before initialize
+    assert e.value.code == -7
+    bad = dict(d, nx="40")
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        gpu_pkg.Simulation.from_global(bad)
+    assert e.value.code == -6
+    # a non-finite initial condition is reported, not propagated silently
+    u, _ = make_ic(gpu_pkg, d)
+    u = [x.copy() for x in u]
+    u[0][3, 4, 5] = np.nan
+    sim.set_fields(*u)
+    sim.initialize()
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        sim.advance_in_time(2)
+    assert e.value.code == -4
+    sim.close()
+
+
+def test_restart_continues_like_one_run(gpu_pkg):
+    """Two step calls of 4 and 6 equal one call of 10 (graph replay keeps all state on the device)."""
+    d = gdict(32, "ETD3rdO")
+    u, _ = make_ic(gpu_pkg, d)
+    a = gpu_pkg.Simulation.from_global(d)
+    a.set_fields(*u)
+    a.initialize()
+    a.advance_in_time(10)
+    b = gpu_pkg.Simulation.from_global(d)
+    b.set_fields(*u)
+    b.initialize()
+    b.advance_in_time(4)
+    b.advance_in_time(6)
+    for c in range(3):
+        assert np.array_equal(a.spectral(c), b.spectral(c))
+    assert np.array_equal(a.stats_rows(), b.stats_rows())
+
+
+def test_full_size_properties(gpu_pkg):
+    """256^3 FP32 forced DNS: divergence-free, finite, energy budget consistent."""
+    n = 256
+    d = gdict(n, adaptive=True, kinematicViscosity="1e-3", forcing="isotropicBand", dtStat="1", dtSpec="1000")
+    u = gpu_pkg.random_spectrum(n, k0=4.0, seed=2001)
+    sim = gpu_pkg.Simulation.from_global(d, precision="FP32")
+    sim.set_fields(*u)
+    sim.initialize()
+    sim.advance_in_time(6)
+    g = Grid(n, n, n)
+    uh = [sim.spectral(c) for c in range(3)]
+    div = g.KX * uh[0] + g.KY * uh[1] + g.KZ * uh[2]
+    assert np.abs(div).max() <= 1e-5 * max(np.abs(x).max() for x in uh)
+    rows = sim.stats_rows()
+    assert np.isfinite(rows).all()
+    k = rows[:, 11]
+    assert abs(k[0] - 1.5) < 1e-3            # u_rms = 1 -> k = 3/2
+    # dealiased nonlinear transfer conserves energy: nl + press ~ 0 relative to dissipation
+    assert np.abs(rows[:, 15] + rows[:, 16] + rows[:, 17] + rows[:, 18]).max() < 1e-3 * rows[:, 14].max()
+    sim.close()
