@@ -43,8 +43,15 @@ inline bool make_plan(int n, FftPlan& P) {
     default: return false;
   }
   P.n = n; P.np = np;
-  int mx = 0;
-  for (int i = 0; i < 4; ++i) { P.r[i] = r[i]; mx = std::max(mx, r[i]); }
+  int mx = 0, p = 1;
+  for (int i = 0; i < 4; ++i) {
+    P.r[i] = r[i];
+    mx = std::max(mx, r[i]);
+    P.T[i] = r[i] ? n / r[i] : 0;
+    P.p[i] = p;
+    P.tws[i] = r[i] ? n / (p * r[i]) : 0;
+    if (r[i]) p *= r[i];
+  }
   P.tpl = n / mx;   // threads per line: one butterfly each in the largest-radix pass
   return true;
 }
@@ -205,6 +212,9 @@ class Engine : public EngineBase {
     int rc;
     I.ncomp = I.density ? 4 : 3;
     I.cstride = (long long)I.NZR * I.NYR * I.KXP;
+    I.fd_kxp = make_fastdiv((unsigned)I.KXP);
+    I.fd_nyr = make_fastdiv((unsigned)I.NYR);
+    if (I.cstride >= (1ll << 31)) { err = "grid too large (compact spectral component above 2^31 elements)"; return FFS_EUNSUPPORTED; }
     I.wzs = (long long)p.nz * I.NYR * I.KXP;
     I.wys = (long long)p.nz * p.ny * I.KXP;
     cplx<T>* tw[3];
@@ -273,15 +283,16 @@ class Engine : public EngineBase {
 
     // launch geometry / shared memory
     const size_t cb = sizeof(cplx<T>);
-    smem_z = (size_t)txy * p.nz * cb * (I.pz.np >= 3 ? 2 : 1);
-    smem_y = (size_t)txy * p.ny * cb * (I.py.np >= 3 ? 2 : 1);
+    smem_z = (size_t)txy * srows(p.nz) * cb * (I.pz.np >= 3 ? 2 : 1);
+    smem_y = (size_t)txy * srows(p.ny) * cb * (I.py.np >= 3 ? 2 : 1);
     {
       const int PIN = (nin + 1) / 2;
       const int LIN = PIN * lyz;
       const int MXP = I.Mx | 1;
-      smem_x = cb * ((size_t)p.nx * (LIN + 1) + std::max((size_t)nin * lyz * MXP, (size_t)p.nx * (LIN + 1)));
+      smem_x = cb * ((size_t)srows(p.nx) * (LIN + 1) +
+                     std::max((size_t)nin * lyz * MXP, (size_t)srows(p.nx) * (LIN + 1)));
     }
-    smem_zu = cb * ((size_t)3 * txz * p.nz * (I.pz.np >= 3 ? 2 : 1) +
+    smem_zu = cb * ((size_t)3 * txz * srows(p.nz) * (I.pz.np >= 3 ? 2 : 1) +
                     (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
     if ((rc = set_smem(err))) return rc;
 
@@ -336,7 +347,7 @@ class Engine : public EngineBase {
     return 0;
   }
 
-  size_t io_smem() const { return sizeof(cplx<T>) * (size_t)P.nx * 2 * (2 * LYZ_IO + 1); }
+  size_t io_smem() const { return sizeof(cplx<T>) * (size_t)srows(P.nx) * 2 * (2 * LYZ_IO + 1); }
 
   using XK = void (*)(Inst<T>);
   template <int LY> static XK xsel(bool L, bool D) {

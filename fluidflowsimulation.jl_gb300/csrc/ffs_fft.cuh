@@ -1,7 +1,8 @@
 // Shared-memory Stockham FFT core for line batches (sm_103a).
 //
 // A CTA transforms L lines of length n.  Line l, element j lives in shared memory at
-// buf[j * LS + l] (lines fastest), so a warp touches consecutive addresses.
+// buf[sidx(j, l, LS)] (lines fastest, one padding row every 16), so a warp touches
+// consecutive addresses.
 // Pass 0 reads its inputs through a loader functor (straight from global memory, with
 // any spectral prologue fused in) and the last pass hands its outputs to a storer
 // functor (global store, pruning, or epilogue math), so a two-pass transform
@@ -38,7 +39,33 @@ struct FftPlan {
   int np;     // number of passes
   int r[4];   // radices, product == n
   int tpl;    // threads per line = n / largest radix
+  int T[4];   // butterflies per line in each pass, n / r
+  int p[4];   // sub-transform length entering each pass (a power of two: radix 3 comes last)
+  int tws[4]; // twiddle table stride, n / (p r)
 };
+
+// Shared-memory position of element j of line l: one padding row every 16 rows keeps
+// the stride-R writes of the first pass free of bank conflicts. Buffers hold
+// srows(n) * LS elements.
+__host__ __device__ __forceinline__ int sidx(int j, int l, int LS) { return (j + (j >> 4)) * LS + l; }
+__host__ __device__ __forceinline__ int srows(int n) { return n + (n >> 4) + 1; }
+
+// Division by a runtime constant with a multiply-high (for 0 <= x < 2^31).
+struct FastDiv {
+  unsigned d, m, s;
+};
+__host__ inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.d = d;
+  unsigned s = 0;
+  while ((1ull << s) < d) ++s;
+  f.s = s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ unsigned fdiv(unsigned x, const FastDiv& f) {
+  return (__umulhi(x, f.m) + x) >> f.s;
+}
 
 // ---------------------------------------------------------------------------------
 // Small DFTs in registers. DIR = -1 forward (exp(-i..)), +1 inverse.
@@ -141,21 +168,19 @@ template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<
 // tw: table exp(-2 pi i t / n), t in [0, n).
 // ---------------------------------------------------------------------------------
 template <int R, int DIR, int L, typename T, class LD, class ST>
-__device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, const cplx<T>* in, cplx<T>* out,
-                                         int LS, const cplx<T>* __restrict__ tw, LD& ld, ST& st) {
-  const int T_ = n / R;
+__device__ __forceinline__ void fft_pass(int T_, int p, int tws, bool first, bool last, const cplx<T>* in,
+                                         cplx<T>* out, int LS, const cplx<T>* __restrict__ tw, LD& ld, ST& st) {
   const int nb = L * T_;
-  const int tws = n / (p * R);
   for (int b = threadIdx.x; b < nb; b += blockDim.x) {
     const int l = b % L, i = b / L;
-    const int k = i % p;
+    const int k = i & (p - 1);
     cplx<T> x[R];
     if (first) {
 #pragma unroll
       for (int m = 0; m < R; ++m) x[m] = ld(l, i + m * T_);
     } else {
 #pragma unroll
-      for (int m = 0; m < R; ++m) x[m] = in[(i + m * T_) * LS + l];
+      for (int m = 0; m < R; ++m) x[m] = in[sidx(i + m * T_, l, LS)];
       if (k != 0) {
 #pragma unroll
         for (int m = 1; m < R; ++m) {
@@ -172,7 +197,7 @@ __device__ __forceinline__ void fft_pass(int n, int p, bool first, bool last, co
       for (int m = 0; m < R; ++m) st(l, j + m * p, x[m]);
     } else {
 #pragma unroll
-      for (int m = 0; m < R; ++m) out[(j + m * p) * LS + l] = x[m];
+      for (int m = 0; m < R; ++m) out[sidx(j + m * p, l, LS)] = x[m];
     }
   }
 }
@@ -184,23 +209,23 @@ template <typename T> __device__ __forceinline__ cplx<T>* fft_result_buffer(cons
 }
 
 // Runs the whole plan. Pass 0 writes s0, later passes alternate s0/s1 (s1 is touched
-// only for plans of three or more passes). Ends with a __syncthreads().
+// only for plans of three or more passes); both hold srows(n) * LS elements laid out by
+// sidx(). Ends with a __syncthreads().
 template <int DIR, int L, typename T, class LD, class ST>
 __device__ void fft_lines(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS, const cplx<T>* __restrict__ tw, LD ld,
                           ST st) {
-  int p = 1;
   for (int pass = 0; pass < P.np; ++pass) {
     const bool first = pass == 0, last = pass == P.np - 1;
     const cplx<T>* in = ((pass - 1) & 1) ? s1 : s0;
     cplx<T>* out = (pass & 1) ? s1 : s0;
+    const int T_ = P.T[pass], p = P.p[pass], tws = P.tws[pass];
     switch (P.r[pass]) {
-      case 16: fft_pass<16, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
-      case 8: fft_pass<8, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
-      case 4: fft_pass<4, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
-      case 3: fft_pass<3, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
-      default: fft_pass<2, DIR, L, T>(P.n, p, first, last, in, out, LS, tw, ld, st); break;
+      case 16: fft_pass<16, DIR, L, T>(T_, p, tws, first, last, in, out, LS, tw, ld, st); break;
+      case 8: fft_pass<8, DIR, L, T>(T_, p, tws, first, last, in, out, LS, tw, ld, st); break;
+      case 4: fft_pass<4, DIR, L, T>(T_, p, tws, first, last, in, out, LS, tw, ld, st); break;
+      case 3: fft_pass<3, DIR, L, T>(T_, p, tws, first, last, in, out, LS, tw, ld, st); break;
+      default: fft_pass<2, DIR, L, T>(T_, p, tws, first, last, in, out, LS, tw, ld, st); break;
     }
-    p *= P.r[pass];
     __syncthreads();
   }
 }

@@ -67,6 +67,7 @@ template <typename T> struct Inst {
   cplx<T>* uh;             // 3 velocity comps (+ rho)
   cplx<T>* hist;           // [2][ncomp][...]
   long long cstride;       // elements per compact component = NZR*NYR*KXP
+  FastDiv fd_kxp, fd_nyr;  // index decomposition of the compact layout
   int ncomp;               // 3 or 4
   // work arrays
   cplx<T>* wz;             // [slot][nz][NYR][KXP]

@@ -65,6 +65,15 @@ template <typename T> __device__ __forceinline__ T kval(int i, T L, T iL) {
   return sizeof(T) == 8 ? T(i) / L : T(i) * iL;
 }
 
+// compact index g -> (ix, jc, kc)
+template <typename T> __device__ __forceinline__ void decomp(const Inst<T>& I, unsigned g, int& ix, int& jc, int& kc) {
+  const unsigned r = fdiv(g, I.fd_kxp);
+  ix = (int)(g - r * I.fd_kxp.d);
+  const unsigned q = fdiv(r, I.fd_nyr);
+  jc = (int)(r - q * I.fd_nyr.d);
+  kc = (int)q;
+}
+
 __device__ __forceinline__ void atomic_max_pos(unsigned long long* a, double v) {
   // non-negative doubles order like their bit patterns
   atomicMax(a, (unsigned long long)__double_as_longlong(v));
@@ -83,7 +92,7 @@ template <typename T, int TX>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + I.nz * TX;   // used by plans of three or more passes
+  cplx<T>* s1 = s0 + srows(I.nz) * TX;   // used by plans of three or more passes
   const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
   const int code = F.code[fi];
   const long long cs = I.cstride;
@@ -133,7 +142,7 @@ template <typename T, int TX>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + I.ny * TX;
+  cplx<T>* s1 = s0 + srows(I.ny) * TX;
   const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
   const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)z * I.NYR * I.KXP + kx0;
   cplx<T>* out = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
@@ -154,7 +163,7 @@ template <typename T, int TX>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + I.ny * TX;
+  cplx<T>* s1 = s0 + srows(I.ny) * TX;
   const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
   if (F.code[fi] == R_KE) {
     const long long it = I.st->iteration;
@@ -198,7 +207,7 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   // two buffers of [n][LSX] (the second at least as large as the staged half spectra,
   // which live in it: the first c2r pass reads them and writes the first buffer)
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + (size_t)n * LSX;
+  cplx<T>* s1 = s0 + (size_t)srows(n) * LSX;
   cplx<T>* stage = s1;                                                       // [nin][LYZ][MXP]
   __shared__ double red[32];
 
@@ -208,11 +217,12 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
 
   // 1. stage the half spectra (coalesced along kx)
   {
-    const int per = XF::nin * LYZ * Mx;
-    for (int e = threadIdx.x; e < per; e += blockDim.x) {
-      const int kx = e % Mx, r = e / Mx, q = r % LYZ, f = r / LYZ;
-      const int g = g0 + q;
-      cp_async_elem(stage + (f * LYZ + q) * MXP + kx, I.wy + (long long)f * I.wys + (long long)g * I.KXP + kx);
+    const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int row = wv; row < XF::nin * LYZ; row += nw) {   // row = f * LYZ + q
+      const int q = row % LYZ, f = row / LYZ;
+      const cplx<T>* src = I.wy + (long long)f * I.wys + (long long)(g0 + q) * I.KXP;
+      cplx<T>* dst = stage + row * MXP;
+      for (int kx = lane; kx < Mx; kx += 32) cp_async_elem(dst + kx, src + kx);
     }
     cp_async_wait_all();
   }
@@ -232,7 +242,7 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
     return mk(A.x - B.y, A.y + B.x);
   };
   cplx<T>* ri = fft_result_buffer(I.px, s0, s1);   // physical values end up here
-  auto sti = [&](int l, int j, cplx<T> v) { ri[j * LSX + l] = v; };
+  auto sti = [&](int l, int j, cplx<T> v) { ri[sidx(j, l, LSX)] = v; };
   fft_lines<+1, LIN, T>(I.px, s0, s1, LSX, I.twx, ldi, sti);
 
   // 3. physical space products: inputs from ri, outputs (first POUT pairs) into s1
@@ -240,8 +250,8 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   const T les2 = T(2) * T(I.les_alpha);
   for (int e = threadIdx.x; e < n * LYZ; e += blockDim.x) {
     const int q = e % LYZ, j = e / LYZ;
-    const cplx<T>* row = ri + j * LSX + q;
-    cplx<T>* orow = s1 + j * LSX + q;
+    const cplx<T>* row = ri + sidx(j, q, LSX);
+    cplx<T>* orow = s1 + sidx(j, q, LSX);
     T f[2 * PIN];
 #pragma unroll
     for (int p = 0; p < PIN; ++p) { cplx<T> v = row[p * LYZ]; f[2 * p] = v.x; f[2 * p + 1] = v.y; }
@@ -301,27 +311,33 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
 
   // 4. r2c of the output pairs, result back into sx
   cplx<T>* rf = fft_result_buffer(I.px, s0, s1);
-  auto ldf = [&](int l, int j) -> cplx<T> { return s1[j * LSX + l]; };
-  auto stf = [&](int l, int j, cplx<T> v) { rf[j * LSX + l] = v; };
+  auto ldf = [&](int l, int j) -> cplx<T> { return s1[sidx(j, l, LSX)]; };
+  auto stf = [&](int l, int j, cplx<T> v) { rf[sidx(j, l, LSX)] = v; };
   fft_lines<-1, LOUT, T>(I.px, s0, s1, LSX, I.twx, ldf, stf);
 
   // 5. unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 and store
   const int KXP = I.KXP;
-  const int per = LOUT * KXP;
-  for (int e = threadIdx.x; e < per; e += blockDim.x) {
-    const int k = e % KXP, l = e / KXP, r = l / LYZ, q = l % LYZ;
-    const int g = g0 + q;
-    cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
-    if (k < Mx) {
-      const cplx<T> zk = rf[k * LSX + l];
-      const cplx<T> zm = rf[((n - k) % n) * LSX + l];
-      A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
-      B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+  {
+    const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int l = wv; l < LOUT; l += nw) {   // complex line l = r * LYZ + q carries outputs (2r, 2r+1)
+      const int r = l / LYZ, q = l % LYZ;
+      const int oa = 2 * r, ob = 2 * r + 1;
+      // output 3 is the kinetic-energy field, needed only at stats/spectrum iterations
+      const bool wa = oa < XF::nout && (oa != 3 || want_ke), wb = ob < XF::nout && (ob != 3 || want_ke);
+      cplx<T>* da = I.wy + (long long)I.out_slot[wa ? oa : 0] * I.wys + (long long)(g0 + q) * KXP;
+      cplx<T>* db = I.wy + (long long)I.out_slot[wb ? ob : 0] * I.wys + (long long)(g0 + q) * KXP;
+      for (int k = lane; k < KXP; k += 32) {
+        cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
+        if (k < Mx) {
+          const cplx<T> zk = rf[sidx(k, l, LSX)];
+          const cplx<T> zm = rf[sidx(k == 0 ? 0 : n - k, l, LSX)];
+          A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
+          B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+        }
+        if (wa) da[k] = A;
+        if (wb) db[k] = B;
+      }
     }
-    const int oa = 2 * r, ob = 2 * r + 1;
-    // output 3 is the kinetic-energy field, needed only at stats/spectrum iterations
-    if (oa < XF::nout && (oa != 3 || want_ke)) I.wy[(long long)I.out_slot[oa] * I.wys + (long long)g * KXP + k] = A;
-    if (ob < XF::nout && (ob != 3 || want_ke)) I.wy[(long long)I.out_slot[ob] * I.wys + (long long)g * KXP + k] = B;
   }
 }
 
@@ -453,10 +469,10 @@ __global__ void k_etd_table(Inst<T> I, int mode) {
     if (I.uniformL) {
       k2 = dd::D((double)q, I.lx * I.lx);
     } else {
-      const int ix = (int)(q % I.KXP);
+      int ix, jc, kc;
+      decomp(I, (unsigned)q, ix, jc, kc);
       if (ix >= I.Mx) continue;
-      const long long r = q / I.KXP;
-      k2 = ref_k2(I, ix, ysig(I, (int)(r % I.NYR)), zsig(I, (int)(r / I.NYR)));
+      k2 = ref_k2(I, ix, ysig(I, jc), zsig(I, kc));
     }
     double E, A, B, C;
     etd_coeffs_exact(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
@@ -483,9 +499,9 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int L3 = 3 * TX;
   const int nz = I.nz, NZR = I.NZR;
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);   // [nz][3 TX]
-  cplx<T>* bufB = buf + nz * L3;                         // second buffer (plans of >= 3 passes)
-  cplx<T>* accT = bufB + (I.pz.np >= 3 ? nz * L3 : 0);   // [3][NZR][TX] i k . tau (LES)
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);   // [srows(nz)][3 TX]
+  cplx<T>* bufB = buf + srows(nz) * L3;                  // second buffer (plans of >= 3 passes)
+  cplx<T>* accT = bufB + (I.pz.np >= 3 ? srows(nz) * L3 : 0);   // [3][NZR][TX] i k . tau (LES)
   cplx<T>* accF = accT + 3 * NZR * TX;                   // [NZR][TX]    i k . flux (density)
 
   const long long it = I.st->iteration;
@@ -588,14 +604,14 @@ __global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
   const T fix2 = T(-(dt3 + dt2) / dt2);
   const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   bool bad = false;
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < cs; g += (long long)gridDim.x * blockDim.x) {
-    const int ix = (int)(g % I.KXP);
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += gridDim.x * blockDim.x) {
+    int ix, jc, kc;
+    decomp(I, g, ix, jc, kc);
     if (ix >= I.Mx) {   // padding columns stay zero
       if (mode == 0) for (int c = 0; c < I.ncomp; ++c) uh[c * cs + g] = mk(T(0), T(0));
       continue;
     }
-    const long long r = g / I.KXP;
-    const int ky_i = ysig(I, (int)(r % I.NYR)), kz_i = zsig(I, (int)(r / I.NYR));
+    const int ky_i = ysig(I, jc), kz_i = zsig(I, kc);
     const T kx = kval(ix, Lx, iLx), ky = kval(ky_i, Ly, iLy), kz = kval(kz_i, Lz, iLz);
     const T k2 = kx * kx + (ky * ky + kz * kz);
     const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
@@ -642,7 +658,7 @@ __global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
       continue;
     }
     T E, A, B, C;
-    const long long te = I.uniformL ? (long long)(ix * ix + ky_i * ky_i + kz_i * kz_i) : g;   // ETD table entry
+    const unsigned te = I.uniformL ? (unsigned)(ix * ix + ky_i * ky_i + kz_i * kz_i) : g;   // ETD table entry
     if (I.ab3) {
       E = T(1); A = At; B = Bt; C = Ct;
     } else {
@@ -719,11 +735,10 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   double q[Q_COUNT];
 #pragma unroll
   for (int i = 0; i < Q_COUNT; ++i) q[i] = 0.0;
-  for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += (long long)gridDim.x * blockDim.x) {
-    const int ix = (int)(g % I.KXP);
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)total; g += gridDim.x * blockDim.x) {
+    int ix, jc, kc;
+    decomp(I, g, ix, jc, kc);
     if (ix >= I.Mx) continue;
-    const long long r = g / I.KXP;
-    const int jc = (int)(r % I.NYR), kc = (int)(r / I.NYR);
     const int ky_i = ysig(I, jc), kz_i = zsig(I, kc);
     const double kx = (double)ix / I.lx, ky = (double)ky_i / I.ly, kz = (double)kz_i / I.lz;
     const double k2 = kx * kx + (ky * ky + kz * kz);
@@ -936,8 +951,8 @@ __global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
   constexpr int L = 2 * LYZ_IO;   // up to 4 fields -> 2 complex lines per (y,z)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = I.nx;
-  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);   // [n][L+1]
-  cplx<T>* s1 = s0 + n * (L + 1);
+  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);   // [srows(n)][L+1]
+  cplx<T>* s1 = s0 + srows(n) * (L + 1);
   cplx<T>* sx = fft_result_buffer(I.px, s0, s1);
   const int g0 = blockIdx.x * LYZ_IO;
   const long long plane = (long long)I.ny * I.nz * n;
@@ -949,15 +964,15 @@ __global__ void k_phys_fwd_x(Inst<T> I, int nf, int slot0) {
     const T b = fb < nf ? T(I.phys[fb * plane + base]) : T(0);
     return mk(a, b);
   };
-  auto st = [&](int l, int j, cplx<T> v) { sx[j * (L + 1) + l] = v; };
+  auto st = [&](int l, int j, cplx<T> v) { sx[sidx(j, l, L + 1)] = v; };
   fft_lines<-1, L, T>(I.px, s0, s1, L + 1, I.twx, ld, st);
   const int KXP = I.KXP;
   for (int e = threadIdx.x; e < L * KXP; e += blockDim.x) {
     const int k = e % KXP, l = e / KXP, p = l / LYZ_IO, q = l % LYZ_IO;
     cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
     if (k < I.Mx) {
-      const cplx<T> zk = sx[k * (L + 1) + l];
-      const cplx<T> zm = sx[((n - k) % n) * (L + 1) + l];
+      const cplx<T> zk = sx[sidx(k, l, L + 1)];
+      const cplx<T> zm = sx[sidx((n - k) % n, l, L + 1)];
       A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
       B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
     }
@@ -972,7 +987,7 @@ template <typename T, int TX>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z_store(Inst<T> I, FieldList F) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + I.nz * TX;
+  cplx<T>* s1 = s0 + srows(I.nz) * TX;
   const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
   const int rowstride = I.NYR * I.KXP;
   const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
@@ -994,7 +1009,7 @@ __global__ void k_inv_x_phys(Inst<T> I, int nf) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = I.nx, Mx = I.Mx;
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + n * L;
+  cplx<T>* s1 = s0 + srows(n) * L;
   const int g0 = blockIdx.x * LYZ_IO;
   const long long plane = (long long)I.ny * I.nz * n;
   auto ld = [&](int l, int j) -> cplx<T> {
