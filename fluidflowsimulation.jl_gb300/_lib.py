@@ -21,7 +21,7 @@ EXPORTS = [
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
     "ffs_stats_records", "ffs_spectrum_lengths", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_stream",
-    "ffs_last_error", "ffs_destroy",
+    "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
 ]
 
 
@@ -87,6 +87,8 @@ def load() -> ctypes.CDLL:
         "ffs_launches_per_step": (c_int32, [H]),
         "ffs_device_bytes": (c_int64, [H]),
         "ffs_stream": (c_void_p, [H]),
+        "ffs_fourier_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_double,
+                                         c_double, c_double, c_void_p]),
         "ffs_last_error": (c_char_p, [H]),
         "ffs_destroy": (None, [H]),
     }

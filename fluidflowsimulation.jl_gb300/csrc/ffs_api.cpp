@@ -14,6 +14,14 @@ struct ffs_handle {
 
 namespace {
 thread_local std::string g_create_err;
+}  // namespace
+
+namespace ffsgpu {
+// message for ffs_last_error(NULL) from entry points that have no handle
+void set_global_error(const std::string& msg) { g_create_err = msg; }
+}  // namespace ffsgpu
+
+namespace {
 
 template <typename F> int guarded(ffs_handle* h, F&& f) {
   if (!h) return FFS_EINVAL;

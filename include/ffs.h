@@ -141,6 +141,22 @@ int64_t ffs_device_bytes(const ffs_handle* h);
 /* The handle's cudaStream_t. */
 void* ffs_stream(const ffs_handle* h);
 
+/* No counterpart in the reference. The forward transform of one field (myfourier!:
+ * real 3D FFT, 2/3 dealiasing, 1/(nx ny nz) scaling, FP64) for callers that cannot
+ * allocate device memory: code inside a CUDA stream capture, code whose device memory
+ * belongs to another allocator or pool, hosts that forbid allocations at run time.
+ * phys: device pointer, nx*ny*nz doubles, x fastest. spec: device pointer, complex128
+ * [nz][ny][nx/2+1] (interleaved re,im), zeros outside the retained modes — the layout
+ * ffs_get_spectral returns. stream: a cudaStream_t (NULL: the legacy default stream);
+ * the call only enqueues work. No cudaMalloc/cudaFree: the intermediates live in one
+ * static device array of 24 MiB per GPU (held until exit), so grids whose intermediates
+ * exceed it are rejected with FFS_EINVAL (128^3 with the 2/3 rule fits). The first
+ * call on a device resolves the array's address; make it before any stream capture.
+ * All calls share the array: calls whose work overlaps on the GPU race.
+ * Errors: ffs_last_error(NULL). */
+int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny, int32_t nz, double lx, double ly,
+                        double lz, double cutoff, void* stream);
+
 const char* ffs_last_error(const ffs_handle* h);
 void ffs_destroy(ffs_handle* h);
 
