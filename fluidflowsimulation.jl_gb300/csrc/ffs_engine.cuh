@@ -243,11 +243,8 @@ class Engine : public EngineBase {
     if ((rc = alloc(&I.wz, (size_t)nslots * I.wzs, err))) return rc;
     if ((rc = alloc(&I.wy, (size_t)nslots * I.wys, err))) return rc;
     if ((rc = alloc(&I.st, 1, err))) return rc;
-    {
-      int sms = 0;
-      FFS_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device));
-      nparts = 2 * std::max(sms, 1);   // CTAs of the stats kernel
-    }
+    // CTAs of the stats kernel: at most ~16 modes per thread (per-thread sums stay short)
+    nparts = (int)std::max<long long>(1, std::min<long long>((I.cstride + 4095) / 4096, 8192));
     if ((rc = alloc(&I.partials, (size_t)nparts * QPAD, err))) return rc;
     if ((rc = alloc(&I.sbuf, (size_t)((I.les || I.density) ? 8 : 4) * I.cstride, err))) return rc;
     {

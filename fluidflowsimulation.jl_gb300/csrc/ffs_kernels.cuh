@@ -726,31 +726,35 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   const long long cs = I.cstride;
   const cplx<T>* sb = I.sbuf;
   const cplx<T>* ub = I.uh;
-  const long long total = cs;
-  const double fdt = S->dt * S->force_coef;
-  const double kf2 = I.f_kf * I.f_kf;
+  // per-mode products in T, per-thread sums in T over a few modes (the grid gives every
+  // thread at most ~16 modes), FP64 from the warp reduction on
+  const T fdt = T(S->dt * S->force_coef);
+  const T kf2 = I.kf2_t, gv = I.gval_t;
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   const long long rec = S->nspec;
   const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
   double* sp = I.spec + rec * 4LL * stride;
-  double q[Q_COUNT];
+  T q[Q_COUNT];
 #pragma unroll
-  for (int i = 0; i < Q_COUNT; ++i) q[i] = 0.0;
-  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)total; g += gridDim.x * blockDim.x) {
+  for (int i = 0; i < Q_COUNT; ++i) q[i] = T(0);
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += gridDim.x * blockDim.x) {
     int ix, jc, kc;
     decomp(I, g, ix, jc, kc);
     if (ix >= I.Mx) continue;
     const int ky_i = ysig(I, jc), kz_i = zsig(I, kc);
-    const double kx = (double)ix / I.lx, ky = (double)ky_i / I.ly, kz = (double)kz_i / I.lz;
-    const double k2 = kx * kx + (ky * ky + kz * kz);
-    const double w = ix > 0 ? 2.0 : 1.0;
+    const T kx = kval(ix, Lx, iLx), ky = kval(ky_i, Ly, iLy), kz = kval(kz_i, Lz, iLz);
+    const T k2 = kx * kx + (ky * ky + kz * kz);
+    const T w = ix > 0 ? T(2) : T(1);
     const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
     cplx<T> u[3];
-    double a2[3];
+    T a2[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) { u[c] = ub[c * cs + g]; a2[c] = proj(u[c], u[c]); }
+    for (int c = 0; c < 3; ++c) { u[c] = ub[c * cs + g]; a2[c] = u[c].x * u[c].x + u[c].y * u[c].y; }
     if (spec_t && rec < I.spec_cap) {
-      const double hh = 0.5 * (a2[0] + a2[1]), vv = 0.5 * a2[2];
-      const int nk = (int)rint(fabs(kz) / I.dkz), nj = (int)rint(fabs(ky) / I.maxdkh), nx = (int)rint(fabs(kx) / I.maxdkh);
+      // spectrum_u + calculate_specHV (spec.jl:316-327, 424-450), FP64 bins
+      const double hh = 0.5 * ((double)a2[0] + (double)a2[1]), vv = 0.5 * (double)a2[2];
+      const int nk = (int)rint(fabs((double)kz) / I.dkz), nj = (int)rint(fabs((double)ky) / I.maxdkh);
+      const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
       const double vals[2] = {hh, vv};
 #pragma unroll
       for (int s2 = 0; s2 < 2; ++s2) {
@@ -770,20 +774,20 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
     }
     if (!stats_t) continue;
     // velocity moments (velocity_stats, viscosity_stats, d*_squared_mean)
-    if (k0) { q[Q_U1] += (double)u[0].x; q[Q_U2] += (double)u[1].x; q[Q_U3] += (double)u[2].x; }
+    if (k0) { q[Q_U1] += u[0].x; q[Q_U2] += u[1].x; q[Q_U3] += u[2].x; }
     q[Q_U12] += w * a2[0]; q[Q_U22] += w * a2[1]; q[Q_U32] += w * a2[2];
     q[Q_EH] += w * k2 * (a2[0] + a2[1]); q[Q_EV] += w * k2 * a2[2];
     q[Q_D1DY] += w * ky * ky * a2[0]; q[Q_D1DX] += w * kx * kx * a2[0];
     q[Q_D2DY] += w * ky * ky * a2[1]; q[Q_D2DX] += w * kx * kx * a2[1];
     // non-linear transfer: (N - i k ke) . u (stats.jl:897-917)
     const cplx<T> ke = sb[3 * cs + g];
-    const double kk[3] = {kx, ky, kz};
-    double rx[3], ry[3];
+    const T kk[3] = {kx, ky, kz};
+    T rx[3], ry[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const cplx<T> Nc = sb[c * cs + g];
-      rx[c] = (double)Nc.x + kk[c] * (double)ke.y;
-      ry[c] = (double)Nc.y - kk[c] * (double)ke.x;
+      rx[c] = Nc.x + kk[c] * ke.y;
+      ry[c] = Nc.y - kk[c] * ke.x;
     }
     q[Q_NLH] += w * (rx[0] * u[0].x + ry[0] * u[0].y + rx[1] * u[1].x + ry[1] * u[1].y);
     q[Q_NLV] += w * (rx[2] * u[2].x + ry[2] * u[2].y);
@@ -792,38 +796,38 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const cplx<T> dT = sb[(4 + c) * cs + g];
-        rx[c] += (double)dT.x; ry[c] += (double)dT.y;
-        const double pr = proj(dT, u[c]);
+        rx[c] += dT.x; ry[c] += dT.y;
+        const T pr = dT.x * u[c].x + dT.y * u[c].y;
         if (c < 2) q[Q_LESH] += w * pr; else q[Q_LESV] += w * pr;
       }
     }
     cplx<T> rho = mk(T(0), T(0));
     if (I.density) {
       rho = ub[3 * cs + g];
-      rx[I.gdir] += (double)rho.x * I.gval; ry[I.gdir] += (double)rho.y * I.gval;
+      rx[I.gdir] += rho.x * gv; ry[I.gdir] += rho.y * gv;
     }
-    const double kdx = kx * rx[0] + ky * rx[1] + kz * rx[2];
-    const double kdy = kx * ry[0] + ky * ry[1] + kz * ry[2];
-    const double inv = k0 ? 0.0 : 1.0 / k2;
-    const double p1x = -kdx * inv, p1y = -kdy * inv;
+    const T kdx = kx * rx[0] + ky * rx[1] + kz * rx[2];
+    const T kdy = kx * ry[0] + ky * ry[1] + kz * ry[2];
+    const T inv = k0 ? T(0) : T(1) / k2;
+    const T p1x = -kdx * inv, p1y = -kdy * inv;
     q[Q_PH] += w * (u[0].x * p1x * kx + u[0].y * p1y * kx + u[1].x * p1x * ky + u[1].y * p1y * ky);
     q[Q_PV] += w * (u[2].x * p1x * kz + u[2].y * p1y * kz);
     if (I.hv) {
-      double km = 1.0;
+      T km = T(1);
       for (int i = 0; i < I.hv_m; ++i) km *= k2;
       q[Q_HVH] += w * km * (a2[0] + a2[1]);
       q[Q_HVV] += w * km * a2[2];
     }
-    if (I.forcing && mode == 0 && k2 > 0.0 && k2 <= kf2) {
-      q[Q_HP] += w * (fdt * (a2[0] + a2[1]) + 0.5 * fdt * fdt * (a2[0] + a2[1]));
-      q[Q_VP] += w * (fdt * a2[2] + 0.5 * fdt * fdt * a2[2]);
+    if (I.forcing && mode == 0 && k2 > T(0) && k2 <= kf2) {
+      q[Q_HP] += w * (fdt * (a2[0] + a2[1]) + T(0.5) * fdt * fdt * (a2[0] + a2[1]));
+      q[Q_VP] += w * (fdt * a2[2] + T(0.5) * fdt * fdt * a2[2]);
     }
     if (I.density) {
-      const double r2 = proj(rho, rho);
-      if (k0) q[Q_RHO] += (double)rho.x;
+      const T r2 = rho.x * rho.x + rho.y * rho.y;
+      if (k0) q[Q_RHO] += rho.x;
       q[Q_RHO2] += w * r2;
       q[Q_DR1] += w * kx * kx * r2; q[Q_DR2] += w * ky * ky * r2; q[Q_DR3] += w * kz * kz * r2;
-      q[Q_BF] += w * proj(u[I.gdir], rho);
+      q[Q_BF] += w * (u[I.gdir].x * rho.x + u[I.gdir].y * rho.y);
     }
     // integral-length plane sums (stats.jl:952-980)
 #pragma unroll
@@ -834,11 +838,11 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
     }
   }
   if (!stats_t) return;
-  // fixed-order CTA reduction: warp shuffle tree, then warps in order
+  // fixed-order CTA reduction in FP64: warp shuffle tree, then warps in order
   const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
 #pragma unroll
   for (int i = 0; i < Q_COUNT; ++i) {
-    double v = q[i];
+    double v = (double)q[i];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) red[i][wv] = v;

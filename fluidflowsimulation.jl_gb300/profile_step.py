@@ -1,0 +1,36 @@
+"""Minimal driver for profilers: set_fields + initialize + K steps of the forced-DNS workload.
+
+    python fluidflowsimulation.jl_gb300/profile_step.py [n] [FP32|FP64] [steps]
+
+Runs the same workload as bench.py (seeded random-phase field, k0 = 4, band forcing,
+AB3 with adaptive dt, stats every 100 steps) and nothing else, so a profiler's launch
+list is short: k_phys_fwd_x x2, k_fwd_y, k_fwd_z_store (set_fields), one initialize! step,
+then `steps` steps.
+"""
+import sys
+from pathlib import Path
+
+sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+
+import __graft_entry__ as ge  # noqa: E402
+
+
+def main():
+    n = int(sys.argv[1]) if len(sys.argv) > 1 else 256
+    prec = sys.argv[2] if len(sys.argv) > 2 else "FP32"
+    steps = int(sys.argv[3]) if len(sys.argv) > 3 else 3
+    pkg = ge.load_package()
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
+         "kinematicViscosity": "0.001", "dtStat": "100", "dtSpec": "1000000000", "writeTime": "1000000000",
+         "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true", "cfl": "0.5", "dt": "0.001",
+         "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5"}
+    u = pkg.random_spectrum(n, k0=4.0, seed=2001)
+    sim = pkg.Simulation.from_global(d, precision=prec)
+    sim.set_fields(*u)
+    sim.initialize()
+    sim.advance_in_time(steps)
+    print("ok", n, prec, sim.iteration)
+
+
+if __name__ == "__main__":
+    main()
