@@ -22,7 +22,10 @@ EXPORTS = [
     "ffs_stats_records", "ffs_spectrum_lengths", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_stream",
     "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
+    "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
+    "ffs_fetch_fields", "ffs_release", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
 ]
+FFS_QUEUED, FFS_RUNNING = 1, 2
 
 
 class FFSParams(ctypes.Structure):
@@ -42,8 +45,32 @@ class FFSParams(ctypes.Structure):
         ("precision", c_int32), ("dt_stat", c_int32), ("dt_spec", c_int32), ("write_time", c_int32),
         ("start", c_int64), ("start_time", c_double),
         ("device", c_int32), ("reference_cfl_slot", c_int32),
-        ("stats_capacity", c_int32), ("spec_capacity", c_int32),
+        ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("x_variant", c_int32),
     ]
+
+
+class FFSServerCfg(ctypes.Structure):
+    """Mirror of ``ffs_server_cfg``."""
+    _fields_ = [("device", c_int32), ("memory_budget", c_int64), ("max_active", c_int32), ("max_n", c_int32)]
+
+
+class FFSRequest(ctypes.Structure):
+    """Mirror of ``ffs_request``."""
+    _fields_ = [("params", FFSParams), ("u1", POINTER(c_double)), ("u2", POINTER(c_double)),
+                ("u3", POINTER(c_double)), ("nt", c_int64), ("keep_fields", c_int32)]
+
+
+class FFSResult(ctypes.Structure):
+    """Mirror of ``ffs_result``."""
+    _fields_ = [("status", c_int32), ("iteration", c_int64), ("time", c_double), ("dt", c_double),
+                ("stats_rows", c_int64), ("record_ncols", c_int32), ("submit_s", c_double), ("admit_s", c_double),
+                ("done_s", c_double)]
+
+
+class FFSServerInfo(ctypes.Structure):
+    """Mirror of ``ffs_server_info``."""
+    _fields_ = [("batch_steps", c_int64), ("sim_steps", c_int64), ("active", c_int32), ("queued", c_int32),
+                ("bytes_in_use", c_int64), ("peak_bytes", c_int64), ("peak_active", c_int32)]
 
 
 _lib = None
@@ -91,6 +118,17 @@ def load() -> ctypes.CDLL:
                                          c_double, c_double, c_void_p]),
         "ffs_last_error": (c_char_p, [H]),
         "ffs_destroy": (None, [H]),
+        "ffs_server_default": (c_int32, [POINTER(FFSServerCfg)]),
+        "ffs_server_create": (c_int32, [POINTER(FFSServerCfg), POINTER(c_void_p)]),
+        "ffs_submit": (c_int32, [H, POINTER(FFSRequest), POINTER(ctypes.c_uint64)]),
+        "ffs_poll": (c_int32, [H, ctypes.c_uint64, POINTER(FFSResult)]),
+        "ffs_wait": (c_int32, [H, ctypes.c_uint64, c_double, POINTER(FFSResult)]),
+        "ffs_fetch_stats": (c_int64, [H, ctypes.c_uint64, D, c_int64]),
+        "ffs_fetch_fields": (c_int32, [H, ctypes.c_uint64, D, D, D]),
+        "ffs_release": (c_int32, [H, ctypes.c_uint64]),
+        "ffs_server_stats": (c_int32, [H, POINTER(FFSServerInfo)]),
+        "ffs_server_last_error": (c_char_p, [H]),
+        "ffs_server_destroy": (None, [H]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

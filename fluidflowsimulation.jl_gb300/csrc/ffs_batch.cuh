@@ -1,0 +1,110 @@
+// Batched step kernels: many independent simulations (uneven grids) advance together,
+// one launch per pass. Each launch is a persistent grid that walks a work table of
+// (simulation, block coordinates) entries and runs the same per-block code as the
+// single-simulation kernels on that simulation's parameters and buffers. The tables and
+// the per-simulation parameter blocks live in device memory at fixed addresses, so one
+// captured CUDA graph serves every membership of the batch: admitting or retiring a
+// simulation rewrites the tables, not the graph.
+#pragma once
+#include "ffs_kernels.cuh"
+
+namespace ffsgpu {
+
+struct WorkItem { int inst, x, y, z; };
+
+// The passes of one batched step, in launch order.
+enum BatchPhase : int {
+  BP_INV_Z = 0, BP_INV_Y, BP_X, BP_X_LES, BP_FWD_Y, BP_SCALAR, BP_TABLE, BP_FWD_Z, BP_STATS, BP_UPDATE, BP_FIN,
+  BP_COUNT
+};
+
+struct BatchTables {
+  WorkItem* tab[BP_COUNT];
+  int n[BP_COUNT];
+};
+
+template <typename T> struct BatchInst {
+  Inst<T> I;
+  FieldList inv, fwd;
+  int nparts;   // partial sums of the stats pass
+};
+
+constexpr int BATCH_TX = 8;    // kx lines per CTA in the y/z passes (FP32)
+constexpr int BATCH_LYZ = 4;   // (y,z) lines per CTA in the x pass
+
+#define FFS_BATCH_LOOP(PH)                                                         \
+  const int nwork = Tb->n[PH];                                                     \
+  const WorkItem* __restrict__ W = Tb->tab[PH];                                    \
+  for (int w = blockIdx.x; w < nwork; w += gridDim.x) {                            \
+    const WorkItem it = W[w];                                                      \
+    const BatchInst<T>& BI = B[it.inst];
+
+#define FFS_BATCH_END \
+    __syncthreads();  \
+  }
+
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) kb_inv_z(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_INV_Z)
+  b_inv_z<T, TX>(BI.I, BI.inv, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) kb_inv_y(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_INV_Y)
+  b_inv_y<T, TX>(BI.I, BI.inv, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
+template <typename T, bool LES, int LYZ>
+__global__ void __launch_bounds__(FFS_MAXT) kb_x(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(LES ? BP_X_LES : BP_X)
+  b_x_pass<T, LES, false, LYZ>(BI.I, Blk{it.x, 0, 0, 0});
+  FFS_BATCH_END
+}
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) kb_fwd_y(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_FWD_Y)
+  b_fwd_y<T, TX>(BI.I, BI.fwd, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
+template <typename T>
+__global__ void kb_scalar(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_SCALAR)
+  b_scalar<T>(BI.I, 0, Blk{0, 0, 0, 1});
+  FFS_BATCH_END
+}
+template <typename T>
+__global__ void kb_table(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_TABLE)
+  b_etd_table<T>(BI.I, 0, Blk{it.x, 0, 0, it.y});
+  FFS_BATCH_END
+}
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) kb_fwd_z(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_FWD_Z)
+  b_fwd_z<T, TX>(BI.I, BI.fwd, 0, Blk{it.x, it.y, 0, 0});
+  FFS_BATCH_END
+}
+template <typename T>
+__global__ void __launch_bounds__(256) kb_stats(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_STATS)
+  b_stats<T>(BI.I, 0, Blk{it.x, 0, 0, it.y});
+  FFS_BATCH_END
+}
+template <typename T>
+__global__ void __launch_bounds__(256) kb_update(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_UPDATE)
+  b_update<T>(BI.I, 0, Blk{it.x, 0, 0, it.y});
+  FFS_BATCH_END
+}
+template <typename T>
+__global__ void kb_finalize(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  FFS_BATCH_LOOP(BP_FIN)
+  b_finalize<T>(BI.I, 0, BI.nparts, Blk{0, 0, 0, 1});
+  FFS_BATCH_END
+}
+
+#undef FFS_BATCH_LOOP
+#undef FFS_BATCH_END
+
+}  // namespace ffsgpu

@@ -11,6 +11,8 @@
 
 #include "ffs_engine.h"
 #include "ffs_kernels.cuh"
+#include "ffs_xfused.cuh"
+#include "ffs_batch.cuh"
 
 namespace ffsgpu {
 
@@ -71,6 +73,7 @@ class Engine : public EngineBase {
   FieldList inv_list{}, fwd_list{};
   int nin = 0, nout = 0;
   int lyz = 4;
+  int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass)
   int txz = TX;               // kx lines per CTA in the forward z pass
   int txy = TX;               // kx lines per CTA in the single-field y/z passes
   int nparts = 0;
@@ -124,6 +127,26 @@ class Engine : public EngineBase {
     cnt = pos + neg;
   }
 
+  // physics parameters (everything that does not change buffer sizes or the step's passes)
+  void set_physics(const ffs_params& p) {
+    I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
+    I.ab3 = p.integrator == FFS_AB3; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
+    I.hv = p.hyperviscosity != 0; I.hv_m = p.hv_m; I.hv_nu = p.hv_nu;
+    I.les = p.les != 0;
+    const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
+    I.les_alpha = p.smag_c * p.smag_c * fw * fw;
+    I.density = p.density != 0; I.gdir = p.gravity_dir;
+    I.alpha = p.density ? p.nu / p.density_pr : 0.0;
+    I.dgrad = p.density_gradient; I.gval = p.gravity;
+    I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
+    I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
+    I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
+    I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
+    I.inv_n_t = (T)I.inv_n; I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
+    I.gval_t = (T)p.gravity; I.dgrad_t = (T)p.density_gradient; I.kf2_t = (T)(p.forcing_kf * p.forcing_kf);
+
+  }
+
   int create(const ffs_params& p, std::string& err) override {
     P = p;
     memset(&I, 0, sizeof(I));
@@ -174,22 +197,7 @@ class Engine : public EngineBase {
     if (3 * txz * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
     if (txz < TX / 4) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
 
-    // physics
-    I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
-    I.ab3 = p.integrator == FFS_AB3; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
-    I.hv = p.hyperviscosity != 0; I.hv_m = p.hv_m; I.hv_nu = p.hv_nu;
-    I.les = p.les != 0;
-    const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
-    I.les_alpha = p.smag_c * p.smag_c * fw * fw;
-    I.density = p.density != 0; I.gdir = p.gravity_dir;
-    I.alpha = p.density ? p.nu / p.density_pr : 0.0;
-    I.dgrad = p.density_gradient; I.gval = p.gravity;
-    I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
-    I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
-    I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
-    I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
-    I.inv_n_t = (T)I.inv_n; I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
-    I.gval_t = (T)p.gravity; I.dgrad_t = (T)p.density_gradient; I.kf2_t = (T)(p.forcing_kf * p.forcing_kf);
+    set_physics(p);
 
     // field lists
     nin = 0;
@@ -238,6 +246,31 @@ class Engine : public EngineBase {
       FFS_CK(cudaStreamSynchronize(s));
     }
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
+    xfused = 0;
+    if (sizeof(T) == 4 && !I.les && !I.density && p.x_variant == 0) {
+      int lyzf = 0, rf = 0;
+      switch (p.nx) {
+        case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
+        case 256: lyzf = XFused<256>::LYZ; rf = XFused<256>::R; break;
+        case 512: lyzf = XFused<512>::LYZ; rf = XFused<512>::R; break;
+        case 1024: lyzf = XFused<1024>::LYZ; rf = XFused<1024>::R; break;
+        default: break;
+      }
+      if (lyzf && ((long long)p.ny * p.nz) % lyzf == 0) {
+        xfused = p.nx;
+        const int tpl = p.nx / rf;
+        cplx<T>* t = nullptr;
+        if ((rc = alloc(&t, p.nx, err))) return rc;
+        std::vector<cplx<T>> h(p.nx), base(p.nx);
+        FFS_CK(cudaMemcpyAsync(base.data(), tw[0], p.nx * sizeof(cplx<T>), cudaMemcpyDeviceToHost, s));
+        FFS_CK(cudaStreamSynchronize(s));
+        for (int m = 0; m < rf; ++m)
+          for (int i = 0; i < tpl; ++i) h[m * tpl + i] = base[(i * m) % p.nx];
+        FFS_CK(cudaMemcpyAsync(t, h.data(), p.nx * sizeof(cplx<T>), cudaMemcpyHostToDevice, s));
+        FFS_CK(cudaStreamSynchronize(s));
+        I.twx_r = t;
+      }
+    }
     if ((rc = alloc(&I.uh, (size_t)I.ncomp * I.cstride, err))) return rc;
     if ((rc = alloc(&I.hist, (size_t)2 * I.ncomp * I.cstride, err))) return rc;
     if ((rc = alloc(&I.wz, (size_t)nslots * I.wzs, err))) return rc;
@@ -337,6 +370,15 @@ class Engine : public EngineBase {
     if ((rc = smem_attr(k_fwd_y<T, TX / 2>, smem_y, err))) return rc;
     if ((rc = smem_attr(k_fwd_z_store<T, TX / 2>, smem_z, err))) return rc;
     if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
+    if constexpr (sizeof(T) == 4) {
+      switch (xfused) {
+        case 128: if ((rc = smem_attr(k_x_fused<128>, XFused<128>::smem(), err))) return rc; break;
+        case 256: if ((rc = smem_attr(k_x_fused<256>, XFused<256>::smem(), err))) return rc; break;
+        case 512: if ((rc = smem_attr(k_x_fused<512>, XFused<512>::smem(), err))) return rc; break;
+        case 1024: if ((rc = smem_attr(k_x_fused<1024>, XFused<1024>::smem(), err))) return rc; break;
+        default: break;
+      }
+    }
     if ((rc = smem_attr(zu_ptr(), smem_zu, err))) return rc;
     const size_t io = io_smem();
     if ((rc = smem_attr(k_phys_fwd_x<T>, io, err))) return rc;
@@ -397,7 +439,18 @@ class Engine : public EngineBase {
     if (txy == TX) k_fwd_z_store<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
     else k_fwd_z_store<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
+  template <int N> void launch_x_fused() {
+    if constexpr (sizeof(T) == 4)
+      k_x_fused<N><<<dim3((unsigned)((long long)I.ny * I.nz / XFused<N>::LYZ)), XFused<N>::NT, XFused<N>::smem(), s>>>(I);
+  }
   void launch_x() {
+    switch (xfused) {
+      case 128: launch_x_fused<128>(); return;
+      case 256: launch_x_fused<256>(); return;
+      case 512: launch_x_fused<512>(); return;
+      case 1024: launch_x_fused<1024>(); return;
+      default: break;
+    }
     const int PIN = (nin + 1) / 2;
     xpass_ptr()<<<dim3(I.ny * I.nz / lyz), blk(PIN * lyz, I.px), smem_x, s>>>(I);
   }
@@ -714,6 +767,83 @@ class Engine : public EngineBase {
 
   int64_t device_bytes() const override { return bytes; }
   void* stream() const override { return (void*)s; }
+
+  // ---------------------------------------------------------------- batching
+  // Device bytes create() allocates for p (the same buffer list, no allocation).
+  static int64_t estimate_bytes(const ffs_params& p) {
+    FftPlan a, b, c;
+    if (!make_plan(p.nx, a) || !make_plan(p.ny, b) || !make_plan(p.nz, c)) return -1;
+    int xp, xc, yp, yc, zp, zc;
+    retained(p.nx, p.lx, p.cutoff, true, xp, xc);
+    retained(p.ny, p.ly, p.cutoff, false, yp, yc);
+    retained(p.nz, p.lz, p.cutoff, false, zp, zc);
+    const int64_t KXP = ((xc + 7) / 8) * 8, cb = sizeof(cplx<T>);
+    const int64_t cs = (int64_t)zc * yc * KXP, wzs = (int64_t)p.nz * yc * KXP, wys = (int64_t)p.nz * p.ny * KXP;
+    const int nin = 6 + (p.les ? 5 : 0) + (p.density ? 1 : 0), nslots = std::max(nin, 4);
+    const int ncomp = p.density ? 4 : 3;
+    int64_t t = cb * (2 * (int64_t)(p.nx + p.ny + p.nz));
+    t += cb * (3 * ncomp * cs + (int64_t)nslots * (wzs + wys) + ((p.les || p.density) ? 8 : 4) * cs);
+    t += 8 * (int64_t)std::min<int64_t>((cs + 4095) / 4096, 8192) * QPAD;
+    t += 8 * (int64_t)(p.stats_capacity > 0 ? p.stats_capacity : 256) * 64;   // record columns <= 53
+    t += 8 * (int64_t)(p.spec_capacity > 0 ? p.spec_capacity : 16) * 4 * (std::max(p.nx, std::max(p.ny, p.nz)) / 2 + 1);
+    if (p.integrator != FFS_AB3) t += 2 * (int64_t)sizeof(T) * 4 * cs;
+    t += 16 * (int64_t)p.nx * p.ny * p.nz;   // FP64 staging of two physical fields
+    return t + 4096;
+  }
+
+  int batch_export(void* bi, size_t bi_size, BatchGeom* g, std::string& err) const override {
+    if (bi_size != sizeof(BatchInst<T>)) { err = "batch parameter block size mismatch"; return FFS_EINVAL; }
+    BatchInst<T>* b = reinterpret_cast<BatchInst<T>*>(bi);
+    b->I = I;
+    b->inv = inv_list;
+    b->fwd = fwd_list;
+    b->nparts = nparts;
+    g->nx = P.nx; g->ny = P.ny; g->nz = P.nz;
+    g->nin = inv_list.n; g->nout = fwd_list.n;
+    g->kx_tiles = I.KXP / txy;
+    g->nyr = I.NYR;
+    g->yz_groups = P.ny * P.nz / lyz;
+    g->fwd_z_tiles = I.KXP / txz;
+    g->les = I.les; g->density = I.density; g->etd = !I.ab3;
+    {
+      const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
+      g->table_blocks = use_table() ? (int)std::min<long long>(1024, (count + 255) / 256) : 0;
+    }
+    g->nparts = nparts; g->upd_blocks = upd_blocks;
+    g->txy = txy; g->txz = txz; g->lyz = lyz;
+    return 0;
+  }
+
+  int stream_wait(void* event, std::string& err) override {
+    FFS_CK(cudaStreamWaitEvent(s, (cudaEvent_t)event, 0));
+    return 0;
+  }
+
+  int repurpose(const ffs_params& p, std::string& err) override {
+    const bool same = p.nx == P.nx && p.ny == P.ny && p.nz == P.nz && p.lx == P.lx && p.ly == P.ly &&
+                      p.lz == P.lz && p.cutoff == P.cutoff && p.integrator == P.integrator &&
+                      (p.les != 0) == (P.les != 0) && (p.density != 0) == (P.density != 0) &&
+                      (p.forcing != 0) == (P.forcing != 0) && (p.hyperviscosity != 0) == (P.hyperviscosity != 0) &&
+                      p.precision == P.precision && p.device == P.device && p.x_variant == P.x_variant &&
+                      (p.stats_capacity > 0 ? p.stats_capacity : 256) <= I.rec_cap &&
+                      (p.spec_capacity > 0 ? p.spec_capacity : 16) <= I.spec_cap;
+    if (!same) { err = "repurpose needs the same grid, model and record capacities"; return FFS_EINVAL; }
+    if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
+    if (p.dt_stat <= 0 || p.dt_spec <= 0) { err = "dtStat and dtSpec must be positive"; return FFS_EINVAL; }
+    if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
+    const int rc_cap = I.rec_cap, sp_cap = I.spec_cap;
+    P = p;
+    set_physics(p);
+    I.rec_cap = rc_cap; I.spec_cap = sp_cap;
+    P.stats_capacity = rc_cap; P.spec_capacity = sp_cap;
+    initialized = false;
+    rec_host.clear(); spec_host.clear();
+    return reset_state(err);
+  }
+
+  int sync_host_state(int64_t it_first, int64_t it_last, std::string& err) override {
+    return drain(it_first, it_last, err);
+  }
 };
 
 }  // namespace ffsgpu

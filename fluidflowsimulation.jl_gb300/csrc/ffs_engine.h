@@ -14,6 +14,20 @@ struct KernelTiming {
   double ms;
 };
 
+// Work of one simulation in a batched step (see ffs_batch.cuh), filled by batch_export.
+struct BatchGeom {
+  int nx, ny, nz;
+  int nin, nout;          // fields of the inverse / forward passes
+  int kx_tiles;           // KXP / TX of the y and z passes
+  int nyr;                // retained ky count
+  int yz_groups;          // ny * nz / lyz (x pass CTAs)
+  int fwd_z_tiles;        // KXP / txz
+  int les, density, etd;
+  int table_blocks;       // ETD table CTAs (0: AB3)
+  int nparts, upd_blocks; // stats and update CTAs
+  int txy, txz, lyz;
+};
+
 class EngineBase {
  public:
   virtual ~EngineBase() {}
@@ -30,6 +44,14 @@ class EngineBase {
   virtual int launches_per_step() const = 0;
   virtual int64_t device_bytes() const = 0;
   virtual void* stream() const = 0;
+  // batched stepping: the simulation's parameter block (a BatchInst<T>) and its geometry
+  virtual int batch_export(void* bi, size_t bi_size, BatchGeom* g, std::string& err) const = 0;
+  // the simulation's own stream waits for an event of another stream
+  virtual int stream_wait(void* event, std::string& err) = 0;
+  // reuse the buffers for new physics parameters on the same grid and model
+  virtual int repurpose(const ffs_params& p, std::string& err) = 0;
+  // state after batched steps advanced the simulation outside step()
+  virtual int sync_host_state(int64_t it_first, int64_t it_last, std::string& err) = 0;
   // host-side views
   std::string header;
   int ncols_stats = 0, ncols_rec = 0;
@@ -43,5 +65,7 @@ class EngineBase {
 
 EngineBase* make_engine_f32();
 EngineBase* make_engine_f64();
+// device bytes an FP32 engine allocates for these parameters (before creating it)
+int64_t estimate_bytes_f32(const ffs_params& p);
 
 }  // namespace ffsgpu

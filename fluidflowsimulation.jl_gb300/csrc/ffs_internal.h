@@ -48,7 +48,15 @@ struct DevState {
   long long nspec;         // spectrum records written
   unsigned int err;        // bit 0: non-finite value in the update
   int pad0;
+  // per-step update scalars in both precisions, written by the scalar kernel:
+  // At, Bt, Ct, fix_fm2 factor -(dt3+dt2)/dt2, forcing increment dt*eps/(2 E_f)
+  double coef_d[5];
+  float coef_f[6];
 };
+enum CoefIdx : int { CO_A = 0, CO_B, CO_C, CO_FIX2, CO_FDT };
+template <typename T> __device__ __forceinline__ T step_coef(const DevState* S, int i);
+template <> __device__ __forceinline__ float step_coef<float>(const DevState* S, int i) { return S->coef_f[i]; }
+template <> __device__ __forceinline__ double step_coef<double>(const DevState* S, int i) { return S->coef_d[i]; }
 
 template <typename T> struct Inst {
   // grid
@@ -63,6 +71,7 @@ template <typename T> struct Inst {
   const cplx<T>* twx;
   const cplx<T>* twy;
   const cplx<T>* twz;
+  const cplx<T>* twx_r;     // register-pass twiddles of the fused x pass, [m][i] = tw[i m]
   // resident spectral state, compact [comp][kz'][ky'][KXP]
   cplx<T>* uh;             // 3 velocity comps (+ rho)
   cplx<T>* hist;           // [2][ncomp][...]

@@ -26,6 +26,13 @@ struct FieldList {
   int slot[12];   // work-array slot
 };
 
+// Block coordinates of one unit of work: the launch's own (single simulation) or an
+// entry of a batch work table (many simulations in one launch).
+struct Blk {
+  int x, y, z, nx;   // block index, and the number of blocks along x for grid-stride loops
+  __device__ static Blk here() { return Blk{(int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, (int)gridDim.x}; }
+};
+
 // ------------------------------------------------------------------ index helpers
 template <typename T> __device__ __forceinline__ int ycomp(const Inst<T>& I, int y) {
   if (y < I.ypos) return y;
@@ -89,11 +96,11 @@ template <typename T> __device__ __forceinline__ double proj(cplx<T> a, cplx<T> 
 // grid (nfields, KXP/TX, NYR); block TX * tpl_z
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
+__device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + srows(I.nz) * TX;   // used by plans of three or more passes
-  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, jc = blockIdx.z;
+  const int fi = bk.x, kx0 = bk.y * TX, jc = bk.z;
   const int code = F.code[fi];
   const long long cs = I.cstride;
   const int rowstride = I.NYR * I.KXP;
@@ -134,16 +141,20 @@ __global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
   auto st = [&](int l, int z, cplx<T> v) { out[(long long)z * rowstride + l] = v; };
   fft_lines<+1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
 }
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
+  b_inv_z<T, TX>(I, F, Blk::here());
+}
 
 // ====================================================================================
 // Inverse y pass: grid (nfields, KXP/TX, nz); block TX * tpl_y
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
+__device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + srows(I.ny) * TX;
-  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
+  const int fi = bk.x, kx0 = bk.y * TX, z = bk.z;
   const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)z * I.NYR * I.KXP + kx0;
   cplx<T>* out = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
   auto ld = [&](int l, int y) -> cplx<T> {
@@ -154,17 +165,21 @@ __global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
   auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
   fft_lines<+1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
 }
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
+  b_inv_y<T, TX>(I, F, Blk::here());
+}
 
 // ====================================================================================
 // Forward y pass (keeps retained ky only): grid (nfields, KXP/TX, nz)
 // The kinetic-energy field is transformed only at stats/spectrum iterations.
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
+__device__ __forceinline__ void b_fwd_y(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + srows(I.ny) * TX;
-  const int fi = blockIdx.x, kx0 = blockIdx.y * TX, z = blockIdx.z;
+  const int fi = bk.x, kx0 = bk.y * TX, z = bk.z;
   if (F.code[fi] == R_KE) {
     const long long it = I.st->iteration;
     if ((it % I.dt_stat) != 0 && (it % I.dt_spec) != 0) return;
@@ -178,6 +193,10 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
   };
   fft_lines<-1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
 }
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
+  b_fwd_y<T, TX>(I, F, Blk::here());
+}
 
 // ====================================================================================
 // Fused x pass (realspace! + realspacecalculation! + calc_les! + find_max, models.jl
@@ -188,6 +207,26 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
 // Real fields in:  u(3) w(3) [S(5) if LES] [rho if DEN]
 // Real fields out: N(3) ke [tau(5) if LES] [flux(3) if DEN]
 // ====================================================================================
+// Block-wide max of |u_i| (and |rho|) in T, then one atomicMax per CTA on the state.
+// red: shared scratch of at least 32 T per quantity.
+template <typename T, bool DEN>
+__device__ __forceinline__ void block_max_to_state(const Inst<T>& I, T umax, T rmax, T* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
+    if (DEN) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  }
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  if (lane == 0) { red[w] = umax; if (DEN) red[32 + w] = rmax; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T m = T(0), r = T(0);
+    for (int i = 0; i < nw; ++i) { m = fmax(m, red[i]); if (DEN) r = fmax(r, red[32 + i]); }
+    atomic_max_pos(&I.st->umax_bits, (double)m);
+    if (DEN) atomic_max_pos(&I.st->rhomax_bits, (double)r);
+  }
+}
+
 template <bool LES, bool DEN> struct XFields {
   static constexpr int nin = 6 + (LES ? 5 : 0) + (DEN ? 1 : 0);
   static constexpr int nout = 4 + (LES ? 5 : 0) + (DEN ? 3 : 0);
@@ -196,7 +235,7 @@ template <bool LES, bool DEN> struct XFields {
 };
 
 template <typename T, bool LES, bool DEN, int LYZ>
-__global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
+__device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
   using XF = XFields<LES, DEN>;
   constexpr int PIN = XF::PIN, POUT = XF::POUT;
   constexpr int LIN = PIN * LYZ, LOUT = POUT * LYZ;
@@ -209,9 +248,9 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + (size_t)srows(n) * LSX;
   cplx<T>* stage = s1;                                                       // [nin][LYZ][MXP]
-  __shared__ double red[32];
+  __shared__ T red[64];
 
-  const int g0 = blockIdx.x * LYZ;
+  const int g0 = bk.x * LYZ;
   const long long it = I.st->iteration;
   const bool want_ke = ((it % I.dt_stat) == 0) || ((it % I.dt_spec) == 0);
 
@@ -280,33 +319,8 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
 #pragma unroll
     for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
   }
-  // block max -> one atomic per CTA
-  double umax = (double)umaxt, rmax = (double)rmaxt;
-  if (I.adaptive) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      umax = fmax(umax, __shfl_xor_sync(0xffffffffu, umax, o));
-      rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    }
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
-    if (lane == 0) { red[w] = umax; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double m = 0.0;
-      for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
-      atomic_max_pos(&I.st->umax_bits, m);
-    }
-    __syncthreads();
-    if (DEN) {
-      if (lane == 0) red[w] = rmax;
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        double m = 0.0;
-        for (int i = 0; i < nw; ++i) m = fmax(m, red[i]);
-        atomic_max_pos(&I.st->rhomax_bits, m);
-      }
-    }
-  }
+  // block max -> one atomic per CTA (the max is exact in T; FP64 only for the atomic)
+  if (I.adaptive) block_max_to_state<T, DEN>(I, umaxt, rmaxt, red);
   __syncthreads();
 
   // 4. r2c of the output pairs, result back into sx
@@ -340,6 +354,10 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
     }
   }
 }
+template <typename T, bool LES, bool DEN, int LYZ>
+__global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
+  b_x_pass<T, LES, DEN, LYZ>(I, Blk::here());
+}
 
 // velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95);
 // muladd(modk, m_nu, modk^M * m_nuh) is a single-rounding fma in the reference.
@@ -363,7 +381,7 @@ template <typename T> __device__ __forceinline__ double ref_k2(const Inst<T>& I,
 // One CTA.
 // ====================================================================================
 template <typename T>
-__global__ void k_scalar(Inst<T> I, int mode) {
+__device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk bk) {
   DevState* Sg = I.st;
   __shared__ double sh_ef[256];
   __shared__ double sh_dt;
@@ -452,19 +470,30 @@ __global__ void k_scalar(Inst<T> I, int mode) {
       Sg->force_coef = s > 0.0 ? I.f_eps / (2.0 * s) : 0.0;
     }
   }
+  // the update's scalars once here, so that no update thread does FP64 divisions
+  if (threadIdx.x == 0) {
+    const double dt = Sg->dt, dt2 = Sg->dt2, dt3 = Sg->dt3;
+    const double c[5] = {Sg->At, Sg->Bt, Sg->Ct, -(dt3 + dt2) / dt2, dt * Sg->force_coef};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) { Sg->coef_d[i] = c[i]; Sg->coef_f[i] = (float)c[i]; }
+  }
+}
+template <typename T>
+__global__ void k_scalar(Inst<T> I, int mode) {
+  b_scalar<T>(I, mode, Blk::here());
 }
 
 // ETD coefficient tables for the current stage and dt history: by q = i^2 + j^2 + l^2
 // when k^2 = q / L^2 is exact (uniform domain with L a power of two), else one entry per
 // retained mode (compact index). Multi-CTA; runs after k_scalar.
 template <typename T>
-__global__ void k_etd_table(Inst<T> I, int mode) {
+__device__ __forceinline__ void b_etd_table(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const int stage = S->stage;
   if (mode == 1 || stage == 0) return;
   const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
   const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < count; q += (long long)gridDim.x * blockDim.x) {
+  for (long long q = (long long)bk.x * blockDim.x + threadIdx.x; q < count; q += (long long)bk.nx * blockDim.x) {
     double k2;
     if (I.uniformL) {
       k2 = dd::D((double)q, I.lx * I.lx);
@@ -485,6 +514,10 @@ __global__ void k_etd_table(Inst<T> I, int mode) {
     }
   }
 }
+template <typename T>
+__global__ void k_etd_table(Inst<T> I, int mode) {
+  b_etd_table<T>(I, mode, Blk::here());
+}
 
 // ====================================================================================
 // Forward z pass (myfourier! z-part + dealias + 1/N + rhs[1]=0, models.jl:171-175):
@@ -495,7 +528,7 @@ __global__ void k_etd_table(Inst<T> I, int mode) {
 // grid (KXP/TX, NYR); block 3 TX tpl_z.
 // ====================================================================================
 template <typename T, int TX>
-__global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
+__device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, int mode, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int L3 = 3 * TX;
   const int nz = I.nz, NZR = I.NZR;
@@ -506,7 +539,7 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int 
 
   const long long it = I.st->iteration;
   const bool want_ke = ((it % I.dt_stat) == 0) || (mode == 0 && (it % I.dt_spec) == 0);
-  const int kx0 = blockIdx.x * TX, jc = blockIdx.y;
+  const int kx0 = bk.x * TX, jc = bk.y;
   const int rowstride = I.NYR * I.KXP;
   const long long cs = I.cstride;
   const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
@@ -580,6 +613,10 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int 
     }
   }
 }
+template <typename T, int TX>
+__global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
+  b_fwd_z<T, TX>(I, F, mode, Blk::here());
+}
 
 // ====================================================================================
 // Update (fourierspacep2!, models.jl:282-364; time_step!, models.jl:468-472 and
@@ -589,7 +626,7 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int 
 // mode 1 (initialize!): fm1 = fm2 = rhs, no update.
 // ====================================================================================
 template <typename T>
-__global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
+__device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const long long cs = I.cstride;
   const int par = S->hist_parity;
@@ -598,13 +635,12 @@ __global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
   cplx<T>* __restrict__ uh = I.uh;
   const cplx<T>* __restrict__ sb = I.sbuf;
   const int stage = S->stage;
-  const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
-  const T At = T(S->At), Bt = T(S->Bt), Ct = T(S->Ct);
-  const T fdt = T(dt * S->force_coef);
-  const T fix2 = T(-(dt3 + dt2) / dt2);
+  const T At = step_coef<T>(S, CO_A), Bt = step_coef<T>(S, CO_B), Ct = step_coef<T>(S, CO_C);
+  const T fdt = step_coef<T>(S, CO_FDT);
+  const T fix2 = step_coef<T>(S, CO_FIX2);
   const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   bool bad = false;
-  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += gridDim.x * blockDim.x) {
+  for (unsigned g = bk.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += bk.nx * blockDim.x) {
     int ix, jc, kc;
     decomp(I, g, ix, jc, kc);
     if (ix >= I.Mx) {   // padding columns stay zero
@@ -706,6 +742,10 @@ __global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
   }
   if (mode == 0 && __syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&I.st->err, 1u);
 }
+template <typename T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_update(Inst<T> I, int mode) {
+  b_update<T>(I, mode, Blk::here());
+}
 
 // ====================================================================================
 // Stats and spectra of the state before the update: u from the spectral state, N, ke,
@@ -716,7 +756,7 @@ __global__ void __launch_bounds__(256) k_update(Inst<T> I, int mode) {
 // iterations only (returns at once otherwise).
 // ====================================================================================
 template <typename T>
-__global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
+__device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const long long it = S->iteration;
   const bool stats_t = (it % I.dt_stat) == 0;
@@ -728,7 +768,7 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   const cplx<T>* ub = I.uh;
   // per-mode products in T, per-thread sums in T over a few modes (the grid gives every
   // thread at most ~16 modes), FP64 from the warp reduction on
-  const T fdt = T(S->dt * S->force_coef);
+  const T fdt = step_coef<T>(S, CO_FDT);
   const T kf2 = I.kf2_t, gv = I.gval_t;
   const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   const long long rec = S->nspec;
@@ -737,7 +777,7 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   T q[Q_COUNT];
 #pragma unroll
   for (int i = 0; i < Q_COUNT; ++i) q[i] = T(0);
-  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += gridDim.x * blockDim.x) {
+  for (unsigned g = bk.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += bk.nx * blockDim.x) {
     int ix, jc, kc;
     decomp(I, g, ix, jc, kc);
     if (ix >= I.Mx) continue;
@@ -851,8 +891,12 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   if (threadIdx.x < Q_COUNT) {
     double sum = 0.0;
     for (int i = 0; i < nw; ++i) sum += red[threadIdx.x][i];
-    I.partials[(long long)blockIdx.x * QPAD + threadIdx.x] = sum;
+    I.partials[(long long)bk.x * QPAD + threadIdx.x] = sum;
   }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
+  b_stats<T>(I, mode, Blk::here());
 }
 
 // ====================================================================================
@@ -861,7 +905,7 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
 // (models.jl:14-15). One CTA of 1024 threads. mode 0: step, 1: initialize!.
 // ====================================================================================
 template <typename T>
-__global__ void k_finalize(Inst<T> I, int mode, int nparts) {
+__device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int nparts, const Blk bk) {
   DevState* S = I.st;
   __shared__ double tot[QPAD];
   const long long it = S->iteration;
@@ -942,6 +986,10 @@ __global__ void k_finalize(Inst<T> I, int mode, int nparts) {
   S->time += S->dt;
   S->hist_parity ^= 1;
   S->umax_bits = 0ull; S->rhomax_bits = 0ull;
+}
+template <typename T>
+__global__ void k_finalize(Inst<T> I, int mode, int nparts) {
+  b_finalize<T>(I, mode, nparts, Blk::here());
 }
 
 // ====================================================================================

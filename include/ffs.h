@@ -78,6 +78,7 @@ typedef struct ffs_params {
   int32_t reference_cfl_slot;  /* 1: CFL uses the reference's reused reduction slot */
   int32_t stats_capacity;      /* stats records kept on the device between reads */
   int32_t spec_capacity;       /* spectrum records kept on the device between reads */
+  int32_t x_variant;           /* x-pass kernel: 0 register-fused where available, 1 generic */
 } ffs_params;
 
 /* Fill defaults: reference defaults for every key that has one. */
@@ -159,6 +160,81 @@ int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny
 
 const char* ffs_last_error(const ffs_handle* h);
 void ffs_destroy(ffs_handle* h);
+
+/* ---------------------------------------------------------------------------------
+ * Batched serving. No counterpart in the reference, which runs one simulation per
+ * Julia process through run_simulation() (src/FluidFlowSimulation.jl:23-65); each
+ * request here is that run for nt steps with its own `global` parameters and fields.
+ *
+ * A server owns one GPU stream and a background thread. Requests (FP32 only, grid
+ * sides up to max_n, velocity-only or Smagorinsky LES, ETD3 or AB3) queue on submit;
+ * the thread admits them while the device memory budget and max_active allow, runs
+ * set_fields + initialize! for each on its own stream, and advances every admitted
+ * simulation by one step per replay of a single CUDA graph whose kernels walk a work
+ * table of (simulation, block) entries. Finished simulations leave the table and their
+ * buffers return to a pool for requests of the same grid and model. Each simulation's
+ * arithmetic is the same alone and in any mix.
+ * Thread safety: every ffs_server entry point may be called from any host thread.
+ * --------------------------------------------------------------------------------- */
+typedef struct ffs_server ffs_server;
+
+#define FFS_QUEUED 1  /* ffs_result.status: waiting for admission */
+#define FFS_RUNNING 2 /* ffs_result.status: in the batch */
+
+typedef struct ffs_server_cfg {
+  int32_t device;          /* CUDA device ordinal */
+  int64_t memory_budget;   /* device bytes the simulations may hold (admission limit) */
+  int32_t max_active;      /* simulations advanced together at most */
+  int32_t max_n;           /* largest grid side accepted (<= 128) */
+} ffs_server_cfg;
+
+typedef struct ffs_request {
+  ffs_params params;       /* the simulation's parameters; precision must be FFS_FP32 */
+  const double* u1;        /* initial velocity, nx*ny*nz doubles each, x fastest (copied) */
+  const double* u2;
+  const double* u3;
+  int64_t nt;              /* steps after initialize */
+  int32_t keep_fields;     /* 1: keep the final physical fields for ffs_fetch_fields */
+} ffs_request;
+
+typedef struct ffs_result {
+  int32_t status;          /* FFS_OK (finished), FFS_QUEUED, FFS_RUNNING or an FFS_E* code */
+  int64_t iteration;       /* final s.iteration */
+  double time, dt;         /* final s.time and dt */
+  int64_t stats_rows;      /* stats records kept for ffs_fetch_stats */
+  int32_t record_ncols;    /* columns per record (as ffs_record_ncols) */
+  double submit_s, admit_s, done_s;   /* seconds since ffs_server_create; -1: not yet */
+} ffs_result;
+
+typedef struct ffs_server_info {
+  int64_t batch_steps;     /* graph replays so far */
+  int64_t sim_steps;       /* simulation steps so far (sum over the batch) */
+  int32_t active;          /* simulations in the batch now */
+  int32_t queued;          /* requests waiting */
+  int64_t bytes_in_use;    /* device bytes held by simulations (pool included) */
+  int64_t peak_bytes;      /* largest bytes_in_use so far */
+  int32_t peak_active;     /* largest batch so far */
+} ffs_server_info;
+
+int ffs_server_default(ffs_server_cfg* cfg);
+int ffs_server_create(const ffs_server_cfg* cfg, ffs_server** out);
+/* Queue a request; *id identifies it in later calls. */
+int ffs_submit(ffs_server* s, const ffs_request* r, uint64_t* id);
+/* Status of a request without waiting. */
+int ffs_poll(ffs_server* s, uint64_t id, ffs_result* out);
+/* Wait up to timeout_s seconds for a request to finish (FFS_ETIMEDOUT otherwise). */
+int ffs_wait(ffs_server* s, uint64_t id, double timeout_s, ffs_result* out);
+/* Stats records of a finished request (ffs_stats_records layout); returns rows copied,
+ * or the rows available when out is NULL. */
+int64_t ffs_fetch_stats(ffs_server* s, uint64_t id, double* out, int64_t max_rows);
+/* Final physical fields of a finished request submitted with keep_fields (layout 0). */
+int ffs_fetch_fields(ffs_server* s, uint64_t id, double* u1, double* u2, double* u3);
+/* Forget a finished request and its results. */
+int ffs_release(ffs_server* s, uint64_t id);
+int ffs_server_stats(ffs_server* s, ffs_server_info* out);
+const char* ffs_server_last_error(ffs_server* s);
+/* Stop the server (unfinished requests are dropped) and free its GPU memory. */
+void ffs_server_destroy(ffs_server* s);
 
 #ifdef __cplusplus
 }

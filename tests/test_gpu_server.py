@@ -1,0 +1,147 @@
+"""Batched serving (ffs_server_*) on the GPU.
+
+- A request's results are the same alone and in a mix of uneven grids and models
+  (batch invariance): fields bit-identical, stats rows to 1e-12 relative.
+- The batched step computes what the single-simulation step computes (FP32, the same
+  generic x pass): fields and stats to 1e-6 relative.
+- FP32 batched results are within 1e-4 of the FP64 oracle after 10 steps.
+- Admission respects the memory budget; unsupported requests fail at submit.
+"""
+import numpy as np
+import pytest
+
+from oracle.ffs_oracle import OracleSimulation, Params
+
+pytestmark = pytest.mark.gpu
+
+
+def gdict(n, les=False, integ="Adams_Bashforth3rdO", adaptive=True, nu="0.005", dtstat=4):
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": nu, "dtStat": str(dtstat), "dtSpec": "100000",
+         "writeTime": "100000", "velocityTimeStep": integ, "variableTimestepFlag": "true" if adaptive else "false",
+         "cfl": "0.5", "dt": "0.002"}
+    if les:
+        d.update({"lesModel": "Smagorinsky", "smagorinskyConstant": "0.17"})
+    return d
+
+
+MIX = [  # (n, les, integrator, adaptive, nt, seed)
+    (32, False, "Adams_Bashforth3rdO", True, 12, 1),
+    (48, True, "Adams_Bashforth3rdO", True, 9, 2),
+    (64, False, "ETD3rdO", False, 7, 3),
+    (96, True, "ETD3rdO", False, 5, 4),
+    (32, True, "Adams_Bashforth3rdO", True, 15, 5),
+    (64, False, "Adams_Bashforth3rdO", True, 10, 6),
+]
+
+
+def submit_case(srv, pkg, case):
+    n, les, integ, adaptive, nt, seed = case
+    u = pkg.random_spectrum(n, k0=3.0, seed=seed)
+    return srv.submit(gdict(n, les, integ, adaptive), u, nt, keep_fields=True)
+
+
+def test_batch_invariance(gpu_pkg):
+    with gpu_pkg.Server(max_active=16) as srv:
+        ids = [submit_case(srv, gpu_pkg, c) for c in MIX]
+        mixed = []
+        for rid in ids:
+            r = srv.wait(rid, timeout=600)
+            assert r["status"] == 0
+            mixed.append((srv.fields(rid), srv.stats_rows(rid), r))
+        assert srv.info()["peak_active"] >= 2
+    for case, (fm, sm, rm) in zip(MIX, mixed):
+        with gpu_pkg.Server(max_active=4) as srv:
+            rid = submit_case(srv, gpu_pkg, case)
+            r = srv.wait(rid, timeout=600)
+            fa, sa = srv.fields(rid), srv.stats_rows(rid)
+        assert r["iteration"] == rm["iteration"] == case[4]
+        assert r["time"] == rm["time"]
+        for c in range(3):
+            assert np.array_equal(fa[c], fm[c]), (case, c)
+        assert sa.shape == sm.shape and sa.shape[0] >= 2
+        assert np.allclose(sa, sm, rtol=1e-12, atol=1e-12 * np.abs(sm).max()), case
+
+
+@pytest.mark.parametrize("case", [MIX[1], MIX[2]])
+def test_batched_step_matches_single_engine(gpu_pkg, case):
+    n, les, integ, adaptive, nt, seed = case
+    d = gdict(n, les, integ, adaptive)
+    u = gpu_pkg.random_spectrum(n, k0=3.0, seed=seed)
+    with gpu_pkg.Server() as srv:
+        rid = srv.submit(d, u, nt, keep_fields=True)
+        r = srv.wait(rid, timeout=600)
+        fb, sb = srv.fields(rid), srv.stats_rows(rid)
+    p = gpu_pkg.parameters(d, precision="FP32")
+    p.x_variant = 1
+    sim = gpu_pkg.Simulation(p)
+    sim.set_fields(*u)
+    sim.initialize()
+    sim.advance_in_time(nt)
+    fs, ss = sim.fields(), sim.records()
+    assert sim.iteration == r["iteration"]
+    for c in range(3):
+        assert np.linalg.norm(fb[c] - fs[c]) <= 1e-6 * np.linalg.norm(fs[c])
+    assert sb.shape == ss.shape
+    assert np.allclose(sb, ss, rtol=1e-6, atol=1e-6 * np.abs(ss).max())
+    sim.close()
+
+
+def test_batched_fp32_against_oracle(gpu_pkg):
+    d = gdict(32, adaptive=False, nu="0.01", dtstat=2)
+    d["dt"] = "0.01"
+    u = gpu_pkg.random_spectrum(32, k0=3.0, seed=7)
+    with gpu_pkg.Server() as srv:
+        rid = srv.submit(d, u, 10, keep_fields=True)
+        srv.wait(rid, timeout=600)
+        f = srv.fields(rid)
+    ref = OracleSimulation(Params.from_global(d), u)
+    ref.initialize()
+    ref.run(10)
+    g = ref.g
+    for c in range(3):
+        uh = g.myfourier(f[c])
+        assert np.linalg.norm(uh - ref.u[c]) <= 1e-4 * np.linalg.norm(ref.u[c]), c
+
+
+def test_admission_respects_memory_budget(gpu_pkg):
+    pkg = gpu_pkg
+    d = gdict(64)
+    u = pkg.random_spectrum(64, k0=3.0, seed=9)
+    # one 64^3 simulation's buffers, measured through the single-simulation path
+    sim = pkg.Simulation(pkg.parameters(d, precision="FP32"))
+    one = sim.device_bytes
+    sim.close()
+    with pkg.Server(memory_budget=int(2.5 * one) + (8 << 20), max_active=8) as srv:
+        ids = [srv.submit(d, u, 20) for _ in range(5)]
+        for rid in ids:
+            assert srv.wait(rid, timeout=600)["status"] == 0
+        info = srv.info()
+    assert info["peak_active"] <= 2
+    assert info["peak_bytes"] <= int(2.5 * one) + (8 << 20)
+    assert info["sim_steps"] == 5 * 20
+
+
+def test_zero_steps_and_errors(gpu_pkg):
+    pkg = gpu_pkg
+    d = gdict(32)
+    u = pkg.random_spectrum(32, k0=3.0, seed=4)
+    with pkg.Server() as srv:
+        rid = srv.submit(d, u, 0, keep_fields=True)
+        r = srv.wait(rid, timeout=600)
+        assert r["status"] == 0 and r["iteration"] == 0
+        f = srv.fields(rid)
+        for c in range(3):   # the dealiased initial field
+            assert np.linalg.norm(f[c] - u[c]) <= 1e-2 * np.linalg.norm(u[c])
+        with pytest.raises(pkg.FFSError):
+            srv.submit(gdict(256), [np.zeros((256, 256, 256))] * 3, 1)
+        p64 = pkg.parameters(d, precision="FP64")
+        with pytest.raises(pkg.FFSError):
+            srv.submit(p64, u, 1)
+        rid2 = srv.submit(d, u, 50)
+        with pytest.raises(pkg.FFSError):
+            srv.fields(rid2)   # not finished (or finished without keep_fields)
+        srv.wait(rid2, timeout=600)
+        srv.release(rid2)
+        with pytest.raises(pkg.FFSError):
+            srv.poll(rid2)

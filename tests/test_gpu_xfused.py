@@ -1,0 +1,74 @@
+"""The register-fused FP32 x pass (velocity-only model, nx in {128, 256, 512}) against
+the generic x pass and against the FP64 oracle.
+
+Both x passes compute the same products in FP32 and differ only in the order of the
+FFT's floating-point operations, so fields agree to ~1e-7 relative; the bar is 2e-6
+after 5 steps (fields); stats rows agree to 1e-5 relative plus 1e-6 of the table's
+largest entry (columns that are mathematically zero, such as the mean velocity and the
+net transfer sums, hold FP32 rounding noise).
+"""
+import numpy as np
+import pytest
+
+from oracle.ffs_oracle import OracleSimulation, Params
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 2e-6
+STATS_TOL = 1e-5
+
+
+def gdict(n, **kw):
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": "1e-3", "dtStat": "1", "dtSpec": "2", "writeTime": "1000",
+         "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true", "cfl": "0.5", "dt": "0.001",
+         "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5"}
+    d.update({k: str(v) for k, v in kw.items()})
+    return d
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def make(pkg, d, u, variant):
+    p = pkg.parameters(d, precision="FP32")
+    p.x_variant = variant
+    sim = pkg.Simulation(p)
+    sim.set_fields(*u)
+    sim.initialize()
+    return sim
+
+
+@pytest.mark.parametrize("n,dtstat", [(128, 1), (256, 1), (256, 1000), (512, 2)])
+def test_fused_matches_generic(gpu_pkg, n, dtstat):
+    d = gdict(n, dtStat=dtstat)
+    u = gpu_pkg.random_spectrum(n, k0=4.0, seed=11)
+    a, b = make(gpu_pkg, d, u, 0), make(gpu_pkg, d, u, 1)
+    steps = 5 if n < 512 else 3
+    a.advance_in_time(steps)
+    b.advance_in_time(steps)
+    for c in range(3):
+        assert rel(a.spectral(c), b.spectral(c)) <= FIELD_TOL, (n, c)
+    assert a.dt == pytest.approx(b.dt, rel=1e-6)
+    ra, rb = a.stats_rows(), b.stats_rows()
+    assert ra.shape == rb.shape and ra.shape[0] >= 1
+    assert (np.abs(ra - rb) <= STATS_TOL * np.abs(rb) + 1e-6 * np.abs(rb).max()).all()
+    a.close()
+    b.close()
+
+
+def test_fused_fp32_against_oracle(gpu_pkg):
+    """128^3 forced DNS, adaptive AB3: FP32 (fused x pass) within 1e-4 of the FP64 oracle
+    after 10 steps."""
+    n = 128
+    d = gdict(n, dtStat=5, dtSpec=1000)
+    u = gpu_pkg.random_spectrum(n, k0=4.0, seed=12)
+    sim = make(gpu_pkg, d, u, 0)
+    sim.advance_in_time(10)
+    ref = OracleSimulation(Params.from_global(d), u)
+    ref.initialize()
+    ref.run(10)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= 1e-4, c
+    sim.close()
