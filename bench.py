@@ -284,15 +284,23 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
             if delay > 0:
                 time.sleep(delay)
             ids.append(srv.submit(serve_global(r), fields[r["i"]], r["nt"]))
-        res = [srv.wait(i, 3600) for i in ids]
+        res, errors = [], []
+        for i in ids:
+            try:
+                res.append(srv.wait(i, 3600))
+            except pkg.FFSError as e:
+                errors.append(str(e))
         info = srv.info()
+    if not res:
+        return {"error": errors[:3]}
     lat = [x["done_s"] - x["submit_s"] for x in res]
     span = max(x["done_s"] for x in res) - min(x["submit_s"] for x in res)
     batch_steps = info["batch_steps"] - before["batch_steps"]
     batched = {"solves_per_s": R / span, "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
                "sim_steps_per_s": total_steps / span, "grid_point_updates_per_s": points / span,
                "wall_s": span, "batch_steps": batch_steps, "peak_active": info["peak_active"],
-               "peak_bytes": info["peak_bytes"], "gpu_launches": batch_steps * SERVE_BATCH_LAUNCHES}
+               "peak_bytes": info["peak_bytes"], "gpu_launches": batch_steps * SERVE_BATCH_LAUNCHES,
+               "failed": len(errors), "errors": errors[:3]}
     out = {"workload": f"served ensemble: {R} requests, Poisson arrivals mean {SERVE_RATE:.0f}/s, n ~ U{{32..128}}, "
                        "k0 ~ U{2..6}, nu ~ logU[1e-3,1e-2], nt ~ U{100..1000} AB3 (CFL 0.5), 50% Smagorinsky, "
                        "FP32, 120 GB budget",
@@ -456,7 +464,7 @@ def run_engine_arm(args):
     }
     if args.serve_requests > 0:
         line["serving"] = run_serving(pkg, args.serve_requests, args.serve_seq_budget, local)
-        line["gpu_launches"] += line["serving"]["batched"]["gpu_launches"]
+        line["gpu_launches"] += line["serving"].get("batched", {}).get("gpu_launches", 0)
     print(json.dumps(line), flush=True)
     return 0
 

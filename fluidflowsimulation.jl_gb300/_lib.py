@@ -23,7 +23,7 @@ EXPORTS = [
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_stream",
     "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
-    "ffs_fetch_fields", "ffs_release", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
+    "ffs_fetch_fields", "ffs_release", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
 ]
 FFS_QUEUED, FFS_RUNNING = 1, 2
 
@@ -45,7 +45,7 @@ class FFSParams(ctypes.Structure):
         ("precision", c_int32), ("dt_stat", c_int32), ("dt_spec", c_int32), ("write_time", c_int32),
         ("start", c_int64), ("start_time", c_double),
         ("device", c_int32), ("reference_cfl_slot", c_int32),
-        ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("x_variant", c_int32),
+        ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("kernel_variant", c_int32),
     ]
 
 
@@ -126,6 +126,7 @@ def load() -> ctypes.CDLL:
         "ffs_fetch_stats": (c_int64, [H, ctypes.c_uint64, D, c_int64]),
         "ffs_fetch_fields": (c_int32, [H, ctypes.c_uint64, D, D, D]),
         "ffs_release": (c_int32, [H, ctypes.c_uint64]),
+        "ffs_server_pause": (c_int32, [H, c_int32]),
         "ffs_server_stats": (c_int32, [H, POINTER(FFSServerInfo)]),
         "ffs_server_last_error": (c_char_p, [H]),
         "ffs_server_destroy": (None, [H]),

@@ -64,7 +64,7 @@ int ffs_params_default(ffs_params* p) {
   p->reference_cfl_slot = 1;
   p->stats_capacity = 256;
   p->spec_capacity = 16;
-  p->x_variant = 0;
+  p->kernel_variant = 0;
   return FFS_OK;
 }
 

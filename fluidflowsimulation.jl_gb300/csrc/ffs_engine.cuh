@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -247,7 +248,7 @@ class Engine : public EngineBase {
     }
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
     xfused = 0;
-    if (sizeof(T) == 4 && !I.les && !I.density && p.x_variant == 0) {
+    if (sizeof(T) == 4 && !I.les && !I.density && p.kernel_variant == 0) {
       int lyzf = 0, rf = 0;
       switch (p.nx) {
         case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
@@ -337,7 +338,12 @@ class Engine : public EngineBase {
     return 0;
   }
 
+  // The dynamic shared-memory limit is one value per kernel function for the whole
+  // process, shared by every engine that launches it: only ever raise it (under a lock),
+  // so that an engine of a smaller grid cannot lower it below what a larger one needs.
   template <typename K> int smem_attr(K kern, size_t bytes_, std::string& err) {
+    static std::mutex mu;
+    std::lock_guard<std::mutex> g(mu);
     cudaFuncAttributes fa;
     FFS_CK(cudaFuncGetAttributes(&fa, kern));
     int maxs = 0;
@@ -346,8 +352,8 @@ class Engine : public EngineBase {
       err = "shared memory per CTA (" + std::to_string(fa.sharedSizeBytes + bytes_) + " bytes) exceeds the device limit";
       return FFS_EUNSUPPORTED;
     }
-    // raise the dynamic limit whenever static + dynamic passes the 48 KB default
-    FFS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes_));
+    if ((int)bytes_ > fa.maxDynamicSharedSizeBytes)
+      FFS_CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes_));
     return 0;
   }
 
@@ -371,6 +377,11 @@ class Engine : public EngineBase {
     if ((rc = smem_attr(k_fwd_z_store<T, TX / 2>, smem_z, err))) return rc;
     if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
     if constexpr (sizeof(T) == 4) {
+      if ((rc = ct_attrs<128>(err)) || (rc = ct_attrs<256>(err)) || (rc = ct_attrs<512>(err)) ||
+          (rc = ct_attrs<1024>(err)))
+        return rc;
+    }
+    if constexpr (sizeof(T) == 4) {
       switch (xfused) {
         case 128: if ((rc = smem_attr(k_x_fused<128>, XFused<128>::smem(), err))) return rc; break;
         case 256: if ((rc = smem_attr(k_x_fused<256>, XFused<256>::smem(), err))) return rc; break;
@@ -383,6 +394,16 @@ class Engine : public EngineBase {
     const size_t io = io_smem();
     if ((rc = smem_attr(k_phys_fwd_x<T>, io, err))) return rc;
     if ((rc = smem_attr(k_inv_x_phys<T>, io, err))) return rc;
+    return 0;
+  }
+
+  // shared-memory limits of the compile-time-length kernels this engine launches
+  template <int NC> int ct_attrs(std::string& err) {
+    int rc;
+    if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
+    if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
+    if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
+    if (ctzu() == NC && (rc = smem_attr(k_fwd_z<T, (NC >= 512 ? 2 : TX), NC>, smem_zu, err))) return rc;
     return 0;
   }
 
@@ -423,15 +444,42 @@ class Engine : public EngineBase {
   // ---------------------------------------------------------------- launches
   dim3 blk(int lines, const FftPlan& pl) const { return dim3(round32(lines * pl.tpl)); }
 
+  // compile-time FFT lengths of the FP32 y/z passes (0: runtime plan)
+  int ct_len(int n) const {
+    return (sizeof(T) == 4 && P.kernel_variant == 0 && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
+  }
+  int cty() const { return txy == TX ? ct_len(I.ny) : 0; }
+  int ctz() const { return txy == TX ? ct_len(I.nz) : 0; }
+  int ctzu() const { return ct_len(I.nz) && txz == zu_tile(I.nz) ? I.nz : 0; }
+  static int zu_tile(int n) { return n >= 512 ? 2 : TX; }
+
+#define FFS_CT_SWITCH(NSEL, CALL)                                    \
+  switch (NSEL) {                                                    \
+    case 128: { constexpr int NC = 128; CALL; } return;              \
+    case 256: { constexpr int NC = 256; CALL; } return;              \
+    case 512: { constexpr int NC = 512; CALL; } return;              \
+    case 1024: { constexpr int NC = 1024; CALL; } return;            \
+    default: break;                                                  \
+  }
+
   void launch_inv_z(const FieldList& F) {
+    if constexpr (sizeof(T) == 4) {
+      FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
+    }
     if (txy == TX) k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
     else k_inv_z<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   void launch_inv_y(const FieldList& F) {
+    if constexpr (sizeof(T) == 4) {
+      FFS_CT_SWITCH(cty(), (k_inv_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+    }
     if (txy == TX) k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
     else k_inv_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
   void launch_fwd_y(const FieldList& F) {
+    if constexpr (sizeof(T) == 4) {
+      FFS_CT_SWITCH(cty(), (k_fwd_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+    }
     if (txy == TX) k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
     else k_fwd_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
@@ -463,6 +511,15 @@ class Engine : public EngineBase {
     k_etd_table<T><<<nb, 256, 0, s>>>(I, mode);
   }
   void launch_zu(int mode) {
+    if constexpr (sizeof(T) == 4) {
+      switch (ctzu()) {
+        case 128: k_fwd_z<T, TX, 128><<<dim3(I.KXP / TX, I.NYR), 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 256: k_fwd_z<T, TX, 256><<<dim3(I.KXP / TX, I.NYR), 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 512: k_fwd_z<T, 2, 512><<<dim3(I.KXP / 2, I.NYR), 3 * 2 * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 1024: k_fwd_z<T, 2, 1024><<<dim3(I.KXP / 2, I.NYR), 3 * 2 * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        default: break;
+      }
+    }
     zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(3 * txz, I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
   void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
@@ -824,7 +881,7 @@ class Engine : public EngineBase {
                       p.lz == P.lz && p.cutoff == P.cutoff && p.integrator == P.integrator &&
                       (p.les != 0) == (P.les != 0) && (p.density != 0) == (P.density != 0) &&
                       (p.forcing != 0) == (P.forcing != 0) && (p.hyperviscosity != 0) == (P.hyperviscosity != 0) &&
-                      p.precision == P.precision && p.device == P.device && p.x_variant == P.x_variant &&
+                      p.precision == P.precision && p.device == P.device && p.kernel_variant == P.kernel_variant &&
                       (p.stats_capacity > 0 ? p.stats_capacity : 256) <= I.rec_cap &&
                       (p.spec_capacity > 0 ? p.spec_capacity : 16) <= I.spec_cap;
     if (!same) { err = "repurpose needs the same grid, model and record capacities"; return FFS_EINVAL; }

@@ -167,11 +167,13 @@ template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<
 // (j = i); a storer may therefore write back into the buffer the last pass reads.
 // tw: table exp(-2 pi i t / n), t in [0, n).
 // ---------------------------------------------------------------------------------
-template <int R, int DIR, int L, typename T, class LD, class ST>
+// NT > 0: the CTA has exactly NT threads (compile-time loop bounds).
+template <int R, int DIR, int L, typename T, class LD, class ST, int NT = 0>
 __device__ __forceinline__ void fft_pass(int T_, int p, int tws, bool first, bool last, const cplx<T>* in,
                                          cplx<T>* out, int LS, const cplx<T>* __restrict__ tw, LD& ld, ST& st) {
   const int nb = L * T_;
-  for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+  const int stride = NT > 0 ? NT : (int)blockDim.x;
+  for (int b = threadIdx.x; b < nb; b += stride) {
     const int l = b % L, i = b / L;
     const int k = i & (p - 1);
     cplx<T> x[R];
@@ -228,6 +230,48 @@ __device__ void fft_lines(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS, co
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------------
+// Compile-time plans for the common power-of-two lengths (the radices make_plan picks):
+// every pass constant folds, and the CTA size is the plan's threads per line x L.
+// ---------------------------------------------------------------------------------
+template <int N> struct CtPlan { static constexpr int np = 0; };
+template <> struct CtPlan<128> { static constexpr int np = 2, r0 = 16, r1 = 8, r2 = 0, rmax = 16; };
+template <> struct CtPlan<256> { static constexpr int np = 2, r0 = 16, r1 = 16, r2 = 0, rmax = 16; };
+template <> struct CtPlan<512> { static constexpr int np = 3, r0 = 8, r1 = 8, r2 = 8, rmax = 8; };
+template <> struct CtPlan<1024> { static constexpr int np = 3, r0 = 16, r1 = 8, r2 = 8, rmax = 16; };
+
+template <int N> constexpr bool ct_plan_ok() { return CtPlan<N>::np > 0; }
+template <int N> constexpr int ct_tpl() { return N / CtPlan<N>::rmax; }
+
+template <int DIR, int L, typename T, int N, class LD, class ST>
+__device__ __forceinline__ void fft_lines_ct(cplx<T>* s0, cplx<T>* s1, const cplx<T>* __restrict__ tw, LD ld, ST st) {
+  using C = CtPlan<N>;
+  constexpr int NT = L * ct_tpl<N>();
+  constexpr int LS = L;
+  constexpr int R0 = C::r0, R1 = C::r1, R2 = C::r2;
+  // pass 0: p = 1
+  fft_pass<R0, DIR, L, T, LD, ST, NT>(N / R0, 1, N / R0, true, false, s0, s0, LS, tw, ld, st);
+  __syncthreads();
+  if constexpr (C::np == 2) {
+    fft_pass<R1, DIR, L, T, LD, ST, NT>(N / R1, R0, 1, false, true, s0, s1, LS, tw, ld, st);
+    __syncthreads();
+  } else {
+    fft_pass<R1, DIR, L, T, LD, ST, NT>(N / R1, R0, N / (R0 * R1), false, false, s0, s1, LS, tw, ld, st);
+    __syncthreads();
+    fft_pass<R2, DIR, L, T, LD, ST, NT>(N / R2, R0 * R1, 1, false, true, s1, s0, LS, tw, ld, st);
+    __syncthreads();
+  }
+}
+
+// The compile-time plan when N > 0 (then LS == L and the CTA has L * ct_tpl<N>()
+// threads), else the runtime plan P.
+template <int DIR, int L, typename T, int N, class LD, class ST>
+__device__ __forceinline__ void fft_lines_n(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS,
+                                            const cplx<T>* __restrict__ tw, LD ld, ST st) {
+  if constexpr (N > 0) fft_lines_ct<DIR, L, T, N>(s0, s1, tw, ld, st);
+  else fft_lines<DIR, L, T>(P, s0, s1, LS, tw, ld, st);
 }
 
 }  // namespace ffsgpu

@@ -95,7 +95,7 @@ template <typename T> __device__ __forceinline__ double proj(cplx<T> a, cplx<T> 
 //   velocity, vorticity i k x u, strain sym(i k (x) u), density, each to its own slot.
 // grid (nfields, KXP/TX, NYR); block TX * tpl_z
 // ====================================================================================
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -139,17 +139,17 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
   };
   cplx<T>* out = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
   auto st = [&](int l, int z, cplx<T> v) { out[(long long)z * rowstride + l] = v; };
-  fft_lines<+1, TX, T>(I.pz, s0, s1, TX, I.twz, ld, st);
+  fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
 }
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
-  b_inv_z<T, TX>(I, F, Blk::here());
+  b_inv_z<T, TX, N>(I, F, Blk::here());
 }
 
 // ====================================================================================
 // Inverse y pass: grid (nfields, KXP/TX, nz); block TX * tpl_y
 // ====================================================================================
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -163,18 +163,18 @@ __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, co
     return in[(long long)jc * I.KXP + l];
   };
   auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
-  fft_lines<+1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
+  fft_lines_n<+1, TX, T, N>(I.py, s0, s1, TX, I.twy, ld, st);
 }
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
-  b_inv_y<T, TX>(I, F, Blk::here());
+  b_inv_y<T, TX, N>(I, F, Blk::here());
 }
 
 // ====================================================================================
 // Forward y pass (keeps retained ky only): grid (nfields, KXP/TX, nz)
 // The kinetic-energy field is transformed only at stats/spectrum iterations.
 // ====================================================================================
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __device__ __forceinline__ void b_fwd_y(const Inst<T>& I, const FieldList& F, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
@@ -191,11 +191,11 @@ __device__ __forceinline__ void b_fwd_y(const Inst<T>& I, const FieldList& F, co
     const int jc = ycomp(I, y);
     if (jc >= 0) out[(long long)jc * I.KXP + l] = v;
   };
-  fft_lines<-1, TX, T>(I.py, s0, s1, TX, I.twy, ld, st);
+  fft_lines_n<-1, TX, T, N>(I.py, s0, s1, TX, I.twy, ld, st);
 }
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
-  b_fwd_y<T, TX>(I, F, Blk::here());
+  b_fwd_y<T, TX, N>(I, F, Blk::here());
 }
 
 // ====================================================================================
@@ -527,7 +527,7 @@ __global__ void k_etd_table(Inst<T> I, int mode) {
 // the scratch buffer: [N(3)][ke][i k.tau(3)][i k.flux].
 // grid (KXP/TX, NYR); block 3 TX tpl_z.
 // ====================================================================================
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, int mode, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int L3 = 3 * TX;
@@ -599,7 +599,7 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
       const bool k0 = kzero_col && x == 0 && z == 0;   // rhs.c[1] = 0 (models.jl:174)
       out[c * cs + (long long)kc * rowstride + x] = k0 ? mk(T(0), T(0)) : scl(v, sc);
     };
-    fft_lines<-1, L3, T>(I.pz, buf, bufB, L3, I.twz, ld, st);
+    fft_lines_n<-1, L3, T, N>(I.pz, buf, bufB, L3, I.twz, ld, st);
   }
   if (aux) {
     for (int m = threadIdx.x; m < NZR * TX; m += blockDim.x) {
@@ -613,9 +613,9 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
     }
   }
 }
-template <typename T, int TX>
+template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
-  b_fwd_z<T, TX>(I, F, mode, Blk::here());
+  b_fwd_z<T, TX, N>(I, F, mode, Blk::here());
 }
 
 // ====================================================================================

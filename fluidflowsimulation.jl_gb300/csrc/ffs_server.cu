@@ -97,6 +97,7 @@ class Server {
   std::map<uint64_t, std::shared_ptr<Job>> jobs;     // all known requests
   uint64_t next_id = 1;
   bool stop = false;
+  bool paused = false;        // admission held (ffs_server_pause)
   std::thread th;
   std::chrono::steady_clock::time_point t0;
   std::string fatal;          // error that stopped the serving thread
@@ -151,8 +152,14 @@ class Server {
     }                                                                          \
   } while (0)
 
+  // per-kernel limit shared by every server in the process: only ever raised
   template <typename K> int attr(K k, size_t bytes) {
-    SV_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    static std::mutex amu;
+    std::lock_guard<std::mutex> g(amu);
+    cudaFuncAttributes fa;
+    SV_CK(cudaFuncGetAttributes(&fa, k));
+    if ((int)bytes > fa.maxDynamicSharedSizeBytes)
+      SV_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return 0;
   }
   template <typename K> int occupancy(K k, int ph) {
@@ -304,7 +311,7 @@ class Server {
     auto j = std::make_shared<Job>();
     j->p = p;
     j->p.device = cfg.device;
-    j->p.x_variant = 1;
+    j->p.kernel_variant = 1;
     // records of one run stay on the device until it finishes
     j->p.stats_capacity = (int32_t)std::max<int64_t>(64, r.nt / std::max(1, p.dt_stat) + 4);
     j->p.spec_capacity = (int32_t)std::max<int64_t>(4, r.nt / std::max(1, p.dt_spec) + 4);
@@ -329,7 +336,9 @@ class Server {
     return 0;
   }
 
-  void fill(const Job& j, ffs_result* o) const {
+  void fill(const Job& j, ffs_result* o) {
+    // a failed request's message becomes the server's last error (mu is held)
+    if (j.status < 0) err = "request " + std::to_string(j.id) + ": " + j.err;
     o->status = j.status;
     o->iteration = j.iteration;
     o->time = j.time;
@@ -403,6 +412,15 @@ class Server {
       return FFS_ESTATE;
     }
     jobs.erase(it);
+    return 0;
+  }
+
+  int pause(int on) {
+    {
+      std::lock_guard<std::mutex> g(mu);
+      paused = on != 0;
+    }
+    cv_work.notify_all();
     return 0;
   }
 
@@ -636,10 +654,11 @@ class Server {
       {
         std::unique_lock<std::mutex> g(mu);
         if (stop) break;
-        if (active == 0 && retiring.empty() && queue.empty() && pending.empty())
+        if (active == 0 && retiring.empty() && (queue.empty() || paused) && pending.empty())
           cv_work.wait_for(g, std::chrono::milliseconds(50));
         if (stop) break;
-        while (!queue.empty()) { pending.push_back(queue.front()); queue.pop_front(); }
+        if (!paused)
+          while (!queue.empty()) { pending.push_back(queue.front()); queue.pop_front(); }
       }
       // admission
       while (!pending.empty() && active < cfg.max_active) {
@@ -785,6 +804,7 @@ int ffs_fetch_fields(ffs_server* s, uint64_t id, double* u1, double* u2, double*
   FFS_SERVER_GUARD(s->s.fetch_fields(id, u1, u2, u3))
 }
 int ffs_release(ffs_server* s, uint64_t id) { FFS_SERVER_GUARD(s->s.release(id)) }
+int ffs_server_pause(ffs_server* s, int32_t paused) { FFS_SERVER_GUARD(s->s.pause(paused)) }
 int ffs_server_stats(ffs_server* s, ffs_server_info* o) {
   if (!o) return FFS_EINVAL;
   FFS_SERVER_GUARD(s->s.stats(o))

@@ -21,6 +21,11 @@
 
 namespace ffsgpu {
 
+__device__ __forceinline__ cplx<float> ldg_c(const cplx<float>* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return mk(v.x, v.y);
+}
+
 template <int N> struct XFusedCfg;
 template <> struct XFusedCfg<128> { static constexpr int R = 8, R2 = 2, LYZ = 8, MINB = 4; };
 template <> struct XFusedCfg<256> { static constexpr int R = 16, R2 = 1, LYZ = 8, MINB = 4; };
@@ -61,8 +66,11 @@ __global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(I
   auto no_ld = [](int, int) -> cplx<T> { return mk(T(0), T(0)); };
   auto no_st = [](int, int, cplx<T>) {};
 
-  // ---- inverse pass 0 (radix R, no twiddles): Hermitian extension of the half spectra
-#pragma unroll 1
+  // ---- inverse pass 0 (radix R, no twiddles): Hermitian extension of the half spectra.
+  // Read-only-path loads (each CTA reads its own lines before it writes any of them),
+  // unrolled over the pairs so that the loads of the next pair are in flight during the
+  // DFT of the current one.
+#pragma unroll
   for (int p = 0; p < 3; ++p) {
     const cplx<T>* A = I.wy + (long long)(2 * p) * I.wys + g * KXP;
     const cplx<T>* B = I.wy + (long long)(2 * p + 1) * I.wys + g * KXP;
@@ -73,8 +81,8 @@ __global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(I
       const bool cj = 2 * j > N;
       const int k = cj ? N - j : j;
       cplx<T> a = mk(T(0), T(0)), b = mk(T(0), T(0));
-      if (k < Mx) { a = A[k]; b = B[k]; }
-      if (k == 0) { a.y = T(0); b.y = T(0); }   // c2r ignores Im of the kx = 0 mode
+      if (k < Mx) { a = ldg_c(A + k); b = ldg_c(B + k); }
+      if (k == 0 || 2 * k == N) { a.y = T(0); b.y = T(0); }   // c2r ignores Im at kx = 0 and n/2
       if (cj) { a.y = -a.y; b.y = -b.y; }
       x[m] = mk(a.x - b.y, a.y + b.x);
     }

@@ -28,7 +28,7 @@ mutable struct FFSParams
     precision::Int32; dt_stat::Int32; dt_spec::Int32; write_time::Int32
     start::Int64; start_time::Float64
     device::Int32; reference_cfl_slot::Int32
-    stats_capacity::Int32; spec_capacity::Int32; x_variant::Int32
+    stats_capacity::Int32; spec_capacity::Int32; kernel_variant::Int32
     FFSParams() = new()
 end
 

@@ -71,8 +71,12 @@ class Server:
         self._check(self.L.ffs_wait(self.h, rid, float(timeout), ctypes.byref(res)))
         out = self._dict(res)
         if res.status < 0:
-            raise _lib.FFSError(res.status, f"request {rid} failed")
+            raise _lib.FFSError(res.status, self.L.ffs_server_last_error(self.h).decode())
         return out
+
+    def pause(self, on: bool = True) -> None:
+        """Hold admission (queued requests wait) or resume it."""
+        self._check(self.L.ffs_server_pause(self.h, 1 if on else 0))
 
     def stats_rows(self, rid: int) -> np.ndarray:
         n = self._check(self.L.ffs_fetch_stats(self.h, rid, None, 0))

@@ -78,7 +78,8 @@ typedef struct ffs_params {
   int32_t reference_cfl_slot;  /* 1: CFL uses the reference's reused reduction slot */
   int32_t stats_capacity;      /* stats records kept on the device between reads */
   int32_t spec_capacity;       /* spectrum records kept on the device between reads */
-  int32_t x_variant;           /* x-pass kernel: 0 register-fused where available, 1 generic */
+  int32_t kernel_variant;      /* 0: specialised FP32 kernels where available (register-fused x pass,
+                                  compile-time FFT lengths); 1: runtime-plan kernels only */
 } ffs_params;
 
 /* Fill defaults: reference defaults for every key that has one. */
@@ -220,7 +221,8 @@ int ffs_server_default(ffs_server_cfg* cfg);
 int ffs_server_create(const ffs_server_cfg* cfg, ffs_server** out);
 /* Queue a request; *id identifies it in later calls. */
 int ffs_submit(ffs_server* s, const ffs_request* r, uint64_t* id);
-/* Status of a request without waiting. */
+/* Status of a request without waiting. For a failed request (negative status) the
+ * message is in ffs_server_last_error(s). */
 int ffs_poll(ffs_server* s, uint64_t id, ffs_result* out);
 /* Wait up to timeout_s seconds for a request to finish (FFS_ETIMEDOUT otherwise). */
 int ffs_wait(ffs_server* s, uint64_t id, double timeout_s, ffs_result* out);
@@ -231,6 +233,8 @@ int64_t ffs_fetch_stats(ffs_server* s, uint64_t id, double* out, int64_t max_row
 int ffs_fetch_fields(ffs_server* s, uint64_t id, double* u1, double* u2, double* u3);
 /* Forget a finished request and its results. */
 int ffs_release(ffs_server* s, uint64_t id);
+/* Hold (1) or resume (0) admission: queued requests wait while the batch keeps running. */
+int ffs_server_pause(ffs_server* s, int32_t paused);
 int ffs_server_stats(ffs_server* s, ffs_server_info* out);
 const char* ffs_server_last_error(ffs_server* s);
 /* Stop the server (unfinished requests are dropped) and free its GPU memory. */

@@ -32,27 +32,35 @@ MIX = [  # (n, les, integrator, adaptive, nt, seed)
     (96, True, "ETD3rdO", False, 5, 4),
     (32, True, "Adams_Bashforth3rdO", True, 15, 5),
     (64, False, "Adams_Bashforth3rdO", True, 10, 6),
+    (128, True, "Adams_Bashforth3rdO", True, 6, 7),
+    (128, False, "Adams_Bashforth3rdO", True, 8, 8),
 ]
 
 
-def submit_case(srv, pkg, case):
+def fields_of(pkg, case):
+    return pkg.random_spectrum(case[0], k0=3.0, seed=case[5])
+
+
+def submit_case(srv, case, u):
     n, les, integ, adaptive, nt, seed = case
-    u = pkg.random_spectrum(n, k0=3.0, seed=seed)
     return srv.submit(gdict(n, les, integ, adaptive), u, nt, keep_fields=True)
 
 
 def test_batch_invariance(gpu_pkg):
+    us = [fields_of(gpu_pkg, c) for c in MIX]
     with gpu_pkg.Server(max_active=16) as srv:
-        ids = [submit_case(srv, gpu_pkg, c) for c in MIX]
+        srv.pause()   # queue the whole mix, then admit it at once
+        ids = [submit_case(srv, c, u) for c, u in zip(MIX, us)]
+        srv.pause(False)
         mixed = []
         for rid in ids:
             r = srv.wait(rid, timeout=600)
             assert r["status"] == 0
             mixed.append((srv.fields(rid), srv.stats_rows(rid), r))
-        assert srv.info()["peak_active"] >= 2
-    for case, (fm, sm, rm) in zip(MIX, mixed):
+        assert srv.info()["peak_active"] == len(MIX)
+    for case, u, (fm, sm, rm) in zip(MIX, us, mixed):
         with gpu_pkg.Server(max_active=4) as srv:
-            rid = submit_case(srv, gpu_pkg, case)
+            rid = submit_case(srv, case, u)
             r = srv.wait(rid, timeout=600)
             fa, sa = srv.fields(rid), srv.stats_rows(rid)
         assert r["iteration"] == rm["iteration"] == case[4]
@@ -63,7 +71,7 @@ def test_batch_invariance(gpu_pkg):
         assert np.allclose(sa, sm, rtol=1e-12, atol=1e-12 * np.abs(sm).max()), case
 
 
-@pytest.mark.parametrize("case", [MIX[1], MIX[2]])
+@pytest.mark.parametrize("case", [MIX[1], MIX[2], MIX[6]])
 def test_batched_step_matches_single_engine(gpu_pkg, case):
     n, les, integ, adaptive, nt, seed = case
     d = gdict(n, les, integ, adaptive)
@@ -73,7 +81,7 @@ def test_batched_step_matches_single_engine(gpu_pkg, case):
         r = srv.wait(rid, timeout=600)
         fb, sb = srv.fields(rid), srv.stats_rows(rid)
     p = gpu_pkg.parameters(d, precision="FP32")
-    p.x_variant = 1
+    p.kernel_variant = 1
     sim = gpu_pkg.Simulation(p)
     sim.set_fields(*u)
     sim.initialize()
@@ -145,3 +153,20 @@ def test_zero_steps_and_errors(gpu_pkg):
         srv.release(rid2)
         with pytest.raises(pkg.FFSError):
             srv.poll(rid2)
+
+
+def test_engines_of_different_sizes_coexist(gpu_pkg):
+    """A small engine created after a large one must not break the large one (the
+    per-kernel shared-memory limit is process-wide)."""
+    pkg = gpu_pkg
+    big = pkg.Simulation.from_global(gdict(128, les=True), precision="FP32")
+    big.set_fields(*pkg.random_spectrum(128, k0=3.0, seed=1))
+    big.initialize()
+    small = pkg.Simulation.from_global(gdict(32, les=True), precision="FP32")
+    small.set_fields(*pkg.random_spectrum(32, k0=3.0, seed=2))
+    small.initialize()
+    small.advance_in_time(2)
+    big.advance_in_time(2)
+    assert big.iteration == 2 and small.iteration == 2
+    big.close()
+    small.close()

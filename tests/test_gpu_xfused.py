@@ -1,7 +1,7 @@
-"""The register-fused FP32 x pass (velocity-only model, nx in {128, 256, 512}) against
-the generic x pass and against the FP64 oracle.
+"""The specialised FP32 kernels (register-fused x pass, compile-time-length y/z passes;
+n in {128, 256, 512}) against the runtime-plan kernels and against the FP64 oracle.
 
-Both x passes compute the same products in FP32 and differ only in the order of the
+Both variants compute the same products in FP32 and differ only in the order of the
 FFT's floating-point operations, so fields agree to ~1e-7 relative; the bar is 2e-6
 after 5 steps (fields); stats rows agree to 1e-5 relative plus 1e-6 of the table's
 largest entry (columns that are mathematically zero, such as the mean velocity and the
@@ -33,7 +33,7 @@ def rel(a, b):
 
 def make(pkg, d, u, variant):
     p = pkg.parameters(d, precision="FP32")
-    p.x_variant = variant
+    p.kernel_variant = variant
     sim = pkg.Simulation(p)
     sim.set_fields(*u)
     sim.initialize()
