@@ -223,7 +223,8 @@ SERVE_BATCH_LAUNCHES = 11   # kernels per batched step (one CUDA graph)
 
 def serving_requests(R: int) -> list[dict]:
     """Seeded served-ensemble trace: Poisson arrivals (mean 200/s), n ~ U{32,48,64,96,128},
-    k0 ~ U{2..6}, nu ~ logU[1e-3, 1e-2], nt ~ U{100..1000} AB3 steps, 50% Smagorinsky LES."""
+    k0 ~ U{2..6}, nu ~ logU[1e-3, 1e-2], nt ~ U{100..1000} AB3 steps (adaptive dt at the
+    reference's default CFL 0.18), 50% Smagorinsky LES."""
     import numpy as np
     rng = np.random.default_rng(5000)
     t = np.cumsum(rng.exponential(1.0 / SERVE_RATE, size=R))
@@ -242,7 +243,7 @@ def serve_global(r: dict) -> dict:
     n = str(r["n"])
     d = {"nx": n, "ny": n, "nz": n, "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
          "kinematicViscosity": repr(r["nu"]), "dtStat": "50", "dtSpec": "1000000000", "writeTime": "1000000000",
-         "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true", "cfl": "0.5", "dt": "0.001"}
+         "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true", "cfl": "0.18", "dt": "0.001"}
     if r["les"]:
         d.update({"lesModel": "Smagorinsky", "smagorinskyConstant": "0.17"})
     return d
@@ -296,24 +297,27 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
     lat = [x["done_s"] - x["submit_s"] for x in res]
     span = max(x["done_s"] for x in res) - min(x["submit_s"] for x in res)
     batch_steps = info["batch_steps"] - before["batch_steps"]
-    batched = {"solves_per_s": R / span, "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
+    batched = {"solves_per_s": len(res) / span, "p50_s": _pct(lat, 50), "p99_s": _pct(lat, 99),
                "sim_steps_per_s": total_steps / span, "grid_point_updates_per_s": points / span,
                "wall_s": span, "batch_steps": batch_steps, "peak_active": info["peak_active"],
                "peak_bytes": info["peak_bytes"], "gpu_launches": batch_steps * SERVE_BATCH_LAUNCHES,
                "failed": len(errors), "errors": errors[:3]}
     out = {"workload": f"served ensemble: {R} requests, Poisson arrivals mean {SERVE_RATE:.0f}/s, n ~ U{{32..128}}, "
-                       "k0 ~ U{2..6}, nu ~ logU[1e-3,1e-2], nt ~ U{100..1000} AB3 (CFL 0.5), 50% Smagorinsky, "
+                       "k0 ~ U{2..6}, nu ~ logU[1e-3,1e-2], nt ~ U{100..1000} AB3 (CFL 0.18), 50% Smagorinsky, "
                        "FP32, 120 GB budget",
            "requests": R, "sim_steps": total_steps, "batched": batched}
     for prec in ("FP32", "FP64"):
-        service = []
+        service, failed = [], 0
         t_all = time.perf_counter()
         for r in reqs:
             t = time.perf_counter()
             sim = pkg.Simulation(pkg.parameters(serve_global(r), precision=prec, device=device))
-            sim.set_fields(*fields[r["i"]])
-            sim.initialize()
-            sim.advance_in_time(r["nt"])
+            try:
+                sim.set_fields(*fields[r["i"]])
+                sim.initialize()
+                sim.advance_in_time(r["nt"])
+            except pkg.FFSError:
+                failed += 1     # e.g. a diverged run: it still occupied the GPU until it stopped
             sim.close()
             service.append(time.perf_counter() - t)
             if time.perf_counter() - t_all > seq_budget:
@@ -321,7 +325,8 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
         k = len(service)
         lat_s, span_s = queue_replay(reqs[:k], service)
         out[f"sequential_{prec.lower()}"] = {
-            "requests_run": k, "solves_per_s": k / span_s if span_s > 0 else None, "p50_s": _pct(lat_s, 50),
+            "requests_run": k, "failed": failed, "solves_per_s": (k - failed) / span_s if span_s > 0 else None,
+            "p50_s": _pct(lat_s, 50),
             "p99_s": _pct(lat_s, 99), "mean_service_s": sum(service) / k if k else None,
             "note": "same requests one at a time through Simulation (plain single-simulation path), "
                     "arrival-order queue replayed with the measured service times"

@@ -15,6 +15,7 @@ from pathlib import Path
 import numpy as np
 
 from . import fields as _fields
+from . import scales as _scales
 from ._lib import FFS_FP32, FFSError, FFSParams, load
 from .globalfile import parameters, readglobal
 
@@ -133,6 +134,18 @@ class Simulation:
     def stats_rows(self) -> np.ndarray:
         return self.records()[:, : self.ncols]
 
+    def scales_numbers(self, records: np.ndarray) -> tuple[list[list[float]], list[list[float]]]:
+        """Scales.txt and Numbers.txt rows (with iteration and time) of drained records."""
+        p = self.params
+        names = self.header.split(",")
+        n2 = p.gravity * p.density_gradient if (p.density and p.gravity_dir == 2) else 0.0
+        sc, nu = [], []
+        for r in records:
+            a, b = _scales.scales_numbers(r, names, self.ncols, p.nu, p.lx, p.ly, p.lz, bool(p.density), n2)
+            sc.append([r[0], r[1]] + a)
+            nu.append([r[0], r[1]] + b)
+        return sc, nu
+
     def spectra(self) -> list[dict]:
         rl = 1 + 2 * self.lenH + 2 * self.lenV
         n = self._L.ffs_spectrum_records(self._h, None, 0)
@@ -219,8 +232,10 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     sim.set_fields(*u, rho)
     total = int(d["nt"]) if "nt" in d else (1 << 62) - start
     lengthtime = float(d["timeDuration"]) if "timeDuration" in d else float("inf")
-    if start == 0:
+    if start == 0:   # writeheader (stats.jl:9-37)
         (folder / "Stats.txt").write_text(sim.header + "\n")
+        (folder / "Scales.txt").write_text(_scales.scales_header(bool(p.density)) + "\n")
+        (folder / "Numbers.txt").write_text(_scales.numbers_header(bool(p.density)) + "\n")
     sim.initialize()
     final_step = start + total
     final_time = p.start_time + lengthtime
@@ -230,10 +245,15 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     wt = int(p.write_time)
 
     def flush():
-        rows = sim.stats_rows()
+        recs = sim.records()
         with open(folder / "Stats.txt", "a") as f:
-            for r in rows:
+            for r in recs[:, : sim.ncols]:
                 f.write(stats_line(r))
+        sc, nums = sim.scales_numbers(recs)
+        for name, rows in (("Scales.txt", sc), ("Numbers.txt", nums)):
+            with open(folder / name, "a") as f:
+                for r in rows:
+                    f.write(stats_line(r))
         for rec in sim.spectra():
             write_spectrum_files(folder, rec, KH, KRZ)
 

@@ -410,6 +410,61 @@ def _proj(a, b):
     return a.real * b.real + a.imag * b.imag
 
 
+def scales_numbers_from(u1p2, u2p2, u3p2, k, tdiss, L, D, nu, density, n2):
+    """The scalar part of ``stats`` (stats.jl:64-165) given the integral lengths
+    L = (L11..L33), the derivative means D = (du1dy2, du1dx2, du2dy2, du2dx2), the
+    viscosity and, with density, N^2 = g_z * drho/dz (calculate_N,
+    density_stratification_types.jl:32-34). Returns (Scales.txt row, Numbers.txt row)
+    without iteration and time."""
+    L11, L12, L13, L21, L22, L23, L31, L32, L33 = L
+    du1dyp2, du1dxp2, du2dyp2, du2dxp2 = D
+    u1p2, u2p2, u3p2, k, tdiss = (np.float64(x) for x in (u1p2, u2p2, u3p2, k, tdiss))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        uh = np.sqrt((u1p2 + u2p2) / 2)
+        urms = np.sqrt((u1p2 + u2p2 + u3p2) / 3)
+        lam12 = np.sqrt(2 * u1p2 / du1dyp2)
+        lam21 = np.sqrt(2 * u2p2 / du2dxp2)
+        Lhh = (L11 + L22) / 2
+        Thh = Lhh / urms
+        laml = np.sqrt(2 * (u1p2 + u2p2) / (du1dxp2 + du2dyp2))
+        lamt = np.sqrt(2 * (u1p2 + u2p2) / (du1dyp2 + du2dxp2))
+        Lhv = (L13 + L23) / 2
+        Lvv = L33
+        Lvh = (L31 + L32) / 2
+        Lt = np.sqrt(k * k * k) / tdiss
+        Tt = k / tdiss
+        Lk = np.sqrt(np.sqrt(nu * nu * nu / tdiss))
+        Tk = np.sqrt(nu / tdiss)
+        lamg = np.sqrt(15 * nu / tdiss) * urms
+        lensv = [Lk, Lt, lamg, laml, lamt, Lhh, Lvv, Lhv, Lvh, lam12, lam21, L11, L12, L13, L21, L22, L23, L31,
+                 L32, L33]
+        Reh = uh * Lhh / nu
+        Reh1 = (Lhh / Lk) ** (4 / 3)
+        Relg = urms * lamg / nu
+        Relg1 = (lamg / Lk) ** (4 / 3)
+        Rell = urms * laml / nu
+        Rell1 = (laml / Lk) ** (4 / 3)
+        Relt = urms * lamt / nu
+        Relt1 = (lamt / Lk) ** (4 / 3)
+        if density:
+            Nb = np.sqrt(n2)
+            Lb = 2 * np.pi * urms / Nb
+            Lo = np.sqrt(tdiss / (Nb * Nb * Nb))
+            Lom = np.sqrt(tdiss / (Nb * Nb * Nb / (8 * np.pi * np.pi * np.pi)))
+            Tb = 2 * np.pi / Nb
+            Tbm = 1 / Nb
+            Reb = (Lo / Lk) ** (4 / 3)
+            Rebm = (Lom / Lk) ** (4 / 3)
+            Frh = 2 * np.pi * uh / (Nb * Lhh)
+            Frh1 = Lhv / Lhh
+            lens = lensv + [Lb, Lo, Lom, Tk, Tt, Thh, Tb, Tbm]
+            anums = [Reh, Reh1, Relg, Rell, Relt, Relg1, Rell1, Relt1, Reb, Rebm, Frh, Frh1]
+        else:
+            lens = lensv + [Tk, Tt, Thh]
+            anums = [Reh, Reh1, Rell, Relt, Rell1, Relt1]
+    return [float(x) for x in lens], [float(x) for x in anums]
+
+
 class OracleSimulation:
     """FP64 restatement of the reference Simulation for the in-scope plug-ins."""
 
@@ -453,6 +508,8 @@ class OracleSimulation:
         self.nlstats = (1.0, 1.0)
         self.pressstats = (1.0, 1.0)
         self.stats_rows = []
+        self.scales_rows = []
+        self.numbers_rows = []
         self.spectra = {}
         self.force = None
         self.hp = self.vp = 0.0
@@ -762,8 +819,49 @@ class OracleSimulation:
         return row + [tdiss] + extra
 
     def write_stats(self):
-        """``writestats`` (stats.jl:39-62): one Stats.txt row."""
-        self.stats_rows.append([float(self.iteration), float(self.time)] + self.velocity_row())
+        """``writestats`` (stats.jl:39-62): one row each of Stats.txt, Scales.txt, Numbers.txt."""
+        row = self.velocity_row()
+        lens, anums = self.scales_numbers(row)
+        head = [float(self.iteration), float(self.time)]
+        self.stats_rows.append(head + row)
+        self.scales_rows.append(head + lens)
+        self.numbers_rows.append(head + anums)
+
+    def scales_numbers(self, row):
+        """Length/time scales and dimensionless numbers of ``stats`` (stats.jl:64-165) from
+        the spectral state: integral lengths (integral_lenght_x/y/z, stats.jl:952-980) and
+        the derivative means dx/dy_squared_mean (stats.jl:334-400)."""
+        p, g = self.p, self.g
+        u = self.u
+        a2 = [np.abs(u[i]) ** 2 for i in range(3)]
+        u1p2, u2p2, u3p2 = row[3], row[4], row[5]
+        k, tdiss = row[9], row[19]
+        uh = np.sqrt((u1p2 + u2p2) / 2)
+        urms = np.sqrt((u1p2 + u2p2 + u3p2) / 3)
+        w = np.where(np.arange(g.nxh) > 0, 2.0, 1.0)[None, None, :]
+        kx0 = (g.kx == 0)[None, None, :]
+        ky0 = (g.ky == 0)[None, :, None]
+        kz0 = (g.kz == 0)[:, None, None]
+        keep = g.keep
+
+        def il(a, up2):
+            up2 = np.float64(up2)
+            rx = np.sum(np.where(keep & kx0, a, 0.0))
+            ry = np.sum(np.where(keep & ky0, w * a, 0.0))
+            rz = np.sum(np.where(keep & kz0, w * a, 0.0))
+            with np.errstate(divide="ignore", invalid="ignore"):
+                return p.lx * rx * np.pi / up2, p.ly * ry * np.pi / up2, p.lz * rz * np.pi / up2
+
+        L11, L12, L13 = il(a2[0], u1p2)
+        L21, L22, L23 = il(a2[1], u2p2)
+        L31, L32, L33 = il(a2[2], u3p2)
+        d1dy = self._wsum(g.KY ** 2 * a2[0])
+        d1dx = self._wsum(g.KX ** 2 * a2[0])
+        d2dy = self._wsum(g.KY ** 2 * a2[1])
+        d2dx = self._wsum(g.KX ** 2 * a2[1])
+        return scales_numbers_from(u1p2, u2p2, u3p2, k, tdiss, (L11, L12, L13, L21, L22, L23, L31, L32, L33),
+                                   (d1dy, d1dx, d2dy, d2dx), p.nu, p.density,
+                                   self.gvec[2] * p.density_gradient if p.density else 0.0)
 
     # ---------------------------------------------------------------- spectra
     def spectrum_u(self):

@@ -221,3 +221,19 @@ def test_full_size_properties(gpu_pkg):
     # dealiased nonlinear transfer conserves energy: nl + press ~ 0 relative to dissipation
     assert np.abs(rows[:, 15] + rows[:, 16] + rows[:, 17] + rows[:, 18]).max() < 1e-3 * rows[:, 14].max()
     sim.close()
+
+
+@pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced"])
+def test_scales_and_numbers_parity(gpu_pkg, name):
+    """Scales.txt / Numbers.txt rows (stats.jl:64-165) from the engine's records against
+    the oracle's direct evaluation on its spectral state."""
+    d = FIXED_CASES[name]
+    sim, ref = run_pair(gpu_pkg, d, density="densityStratification" in d)
+    sc, nums = sim.scales_numbers(sim.records())
+    for got, want in ((np.array(sc), np.array(ref.scales_rows)), (np.array(nums), np.array(ref.numbers_rows))):
+        assert got.shape == want.shape and got.shape[0] >= 2
+        ok = np.isfinite(want)
+        assert np.array_equal(ok, np.isfinite(got))
+        scale = np.maximum(np.abs(want[ok]), 1e-6 * np.abs(want[ok]).max())
+        assert (np.abs(got[ok] - want[ok]) / scale).max() <= FP64_STATS_TOL, name
+    sim.close()
