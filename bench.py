@@ -334,6 +334,121 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
     return out
 
 
+# ---------------------------------------------------------------------------------- other configurations
+def workload_config(wl: str):
+    """(global dict, n, precision of the timed arm, IC kind, description) of a configuration."""
+    if wl == "tg64":
+        d = {"nx": "64", "ny": "64", "nz": "64", "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
+             "kinematicViscosity": "0.0333333", "dtStat": "20", "dtSpec": "1000000000", "writeTime": "1000000000",
+             "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "false", "dt": "0.05"}
+        return d, 64, "FP64", "tg", ("Taylor-Green vortex 64^3 FP64 (u1 = cos x sin y sin z, u2 = -sin x cos y "
+                                     "sin z, u3 = 0), nu = 0.0333333, dt = 0.05, AB3, stats every 20 steps")
+    if wl == "les128":
+        d = {"nx": "128", "ny": "128", "nz": "128", "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
+             "kinematicViscosity": "5e-4", "dtStat": "50", "dtSpec": "50", "writeTime": "1000000000",
+             "velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "true", "cfl": "0.18", "dt": "0.001",
+             "lesModel": "Smagorinsky", "smagorinskyConstant": "0.17", "filterWidth": repr(2 * math.pi / 128),
+             "densityStratification": "true", "zAcceleration": "1", "referenceDensity": "1",
+             "densityGradient": "1", "Pr": "1"}
+        return d, 128, "FP32", "random3", ("stably stratified Boussinesq LES 128^3 FP32: random-phase k0 = 3, "
+                                           "rho' = 0, N = 1, Pr = 1, Smagorinsky Cs = 0.17, Delta = 2 pi/128, "
+                                           "nu = 5e-4, ETD3 (CFL 0.18), stats and spectra every 50 steps")
+    if wl == "dns1024":
+        d = {"nx": "1024", "ny": "1024", "nz": "1024", "xDomainSize": "1.0", "yDomainSize": "1.0",
+             "zDomainSize": "1.0", "kinematicViscosity": "2e-4", "dtStat": "100", "dtSpec": "1000000000",
+             "writeTime": "1000000000", "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true",
+             "cfl": "0.5", "dt": "0.0001", "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5",
+             "hyperViscosity": "true", "hyperViscosityCoefficient": "1e-12", "hyperViscosityM": "2"}
+        return d, 1024, "FP32", "modes8", ("large single-instance DNS 1024^3 FP32: random-phase k0 = 8 (spectral "
+                                           "generator, modes |k_i| <= 48), band forcing eps = 0.1, nu = 2e-4, "
+                                           "hyperviscosity 1e-12 k^4, AB3 CFL 0.5")
+    raise ValueError(wl)
+
+
+def make_sim(pkg, d, prec, ic, n, device):
+    sim = pkg.Simulation(pkg.parameters(d, precision=prec, device=device))
+    if ic == "tg":
+        sim.set_fields(*pkg.taylor_green(n))
+    elif ic == "random3":
+        sim.set_fields(*pkg.random_spectrum(n, k0=3.0, seed=3001))
+    else:
+        from importlib import import_module
+        f = import_module(pkg.__name__ + ".fields")
+        kc = 48
+        box = f.random_spectrum_modes(n, 8.0, 4001, kc)
+        for c in range(3):
+            sim.set_spectral(c, f.embed_half_spectrum(box[c], n, kc))
+    sim.initialize()
+    return sim
+
+
+def run_workload(args):
+    """One JSON line for a configuration other than the headline 256^3 run."""
+    import numpy as np
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    pkg.load()
+    d, n, prec, ic, desc = workload_config(args.workload)
+    world, rank, local, dist = dist_setup(args)
+    sim = make_sim(pkg, d, prec, ic, n, local)
+    sim.advance_in_time(max(args.warmup, 3))
+    with ClockSampler(local) as clk:
+        ms = sim.time_steps(args.steps)
+    rate = args.steps / (ms / 1e3)
+    nprof = max(3, min(10, args.steps))
+    prof = sim.profile_kernels(nprof)
+    dev_bytes = sim.device_bytes
+    launches = sim.launches_per_step * args.steps
+    sim.close()
+    out = {"metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": max(args.warmup, 3), "ms_per_step": ms / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32" if prec == "FP32" else "f64", "data": "synthetic",
+           "config": {"workload": desc, "grid": n, "l2": f"{dev_bytes / 1e9:.2f} GB resident per GPU"},
+           "grid_point_updates_per_s": rate * n ** 3,
+           "kernels_ms_per_step": {k: v / nprof for k, v in prof.items()}, "clocks": clk.summary(),
+           "gpu_launches": launches}
+    peak, kind = measured_peaks()
+    elem = 8 if prec == "FP32" else 16
+    A = (n // 2 + 1) * n * n * elem
+    ntr = 23 if "lesModel" in d else 9        # component transforms per step
+    nint = 4 if "densityStratification" in d else 3
+    b_alg = (6 * ntr + 5 * nint) * A
+    out["roofline"] = {"bound": "hbm", "step_algorithmic_bytes": b_alg, "bytes_model":
+                       f"{6 * ntr + 5 * nint}A per step ({ntr} component transforms x 6A + {nint} integrated "
+                       f"fields x 5A), A = (n/2+1) n^2 complex", "achieved": b_alg / (ms / args.steps / 1e3) / 1e9,
+                       "peak": peak, "unit": "GB/s", "peak_source": kind}
+    out["roofline"]["frac"] = out["roofline"]["achieved"] / peak
+    if prec == "FP32":
+        # FP64 plain form on the same initial state, and the FP32 error after 10 steps
+        a, b = make_sim(pkg, d, "FP32", ic, n, local), make_sim(pkg, d, "FP64", ic, n, local)
+        a.advance_in_time(10)
+        b.advance_in_time(10)
+        err = max(float(np.linalg.norm(a.spectral(c) - b.spectral(c)) / np.linalg.norm(b.spectral(c)))
+                  for c in range(3))
+        a.close()
+        k64 = 3 if n >= 1024 else 10
+        ms64 = b.time_steps(k64)
+        b.close()
+        out["fp64"] = {"value": k64 / (ms64 / 1e3), "unit": "steps/s", "steps": k64}
+        out["fp32_vs_fp64_rel_l2_10_steps"] = err
+    if n <= 128 and not args.no_cpu:
+        from oracle.ffs_oracle import OracleSimulation, Params
+        u = pkg.taylor_green(n) if ic == "tg" else pkg.random_spectrum(n, k0=3.0, seed=3001)
+        o = OracleSimulation(Params.from_global(d), u)
+        o.initialize()
+        o.advance()
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < args.cpu_budget and k < 200:
+            o.advance()
+            k += 1
+        v = k / (time.perf_counter() - t0)
+        out["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{k} steps of the same workload, FP64 numpy/pocketfft oracle"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_reference_arm(args):
     world, rank, local, dist = dist_setup(args)
     if rank != 0:
@@ -481,6 +596,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--workload", default="dns256", choices=["dns256", "tg64", "les128", "dns1024"],
+                    help="dns256: the headline run; the others print one line for that configuration")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
@@ -490,6 +607,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.workload != "dns256":
+        return run_workload(args)
     return run_engine_arm(args)
 
 

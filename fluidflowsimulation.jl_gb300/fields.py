@@ -76,3 +76,40 @@ def random_spectrum(n: int, k0: float, seed: int, urms: float = 1.0, cutoff: flo
     s = np.sqrt(np.mean(u[0] ** 2 + u[1] ** 2 + u[2] ** 2) / 3.0)
     u = u * (urms / s)
     return u[0].copy(), u[1].copy(), u[2].copy()
+
+
+def random_spectrum_modes(n: int, k0: float, seed: int, kc: int, urms: float = 1.0, L: float = 1.0):
+    """Spectral form of ``random_spectrum`` for grids too large to build on the host in
+    physical space: the same E(k) ~ k^4 exp(-2 (k/k0)^2), divergence-free random-phase
+    field, generated directly as half-spectrum coefficients on the low-mode box
+    |kx|, |ky|, |kz| <= kc (E(k) is negligible beyond ~4 k0), Hermitian on the kx = 0
+    plane, scaled so that sqrt(<u.u>/3) = urms by Parseval. Returns the box
+    [3][2kc+1 (kz = -kc..kc)][2kc+1 (ky)][kc+1 (kx)]; ``embed_half_spectrum`` places one
+    component into the [nz][ny][nx/2+1] layout of ``Simulation.set_spectral``."""
+    rng = np.random.default_rng(seed)
+    m = np.arange(-kc, kc + 1) / L
+    kx = np.arange(kc + 1) / L
+    KX, KY, KZ = kx[None, None, :], m[None, :, None], m[:, None, None]
+    K2 = KX ** 2 + KY ** 2 + KZ ** 2
+    g = rng.standard_normal((3,) + K2.shape) + 1j * rng.standard_normal((3,) + K2.shape)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        kd = (KX * g[0] + KY * g[1] + KZ * g[2]) / K2
+        g = np.stack([g[0] - kd * KX, g[1] - kd * KY, g[2] - kd * KZ])
+        k = np.sqrt(K2)
+        A = np.sqrt(k ** 4 * np.exp(-2.0 * (k / k0) ** 2) / (4 * np.pi * K2))
+    uh = np.nan_to_num(g) * np.where(K2 > 0, A, 0.0)[None]
+    # Hermitian kx = 0 plane: u(0, -ky, -kz) = conj u(0, ky, kz)
+    p0 = uh[:, :, :, 0]
+    uh[:, :, :, 0] = 0.5 * (p0 + np.conj(p0[:, ::-1, ::-1]))
+    w = np.where(np.arange(kc + 1) > 0, 2.0, 1.0)[None, None, None, :]
+    e = float(np.sum(w * np.abs(uh) ** 2))   # <u.u> by Parseval
+    return uh * (urms * np.sqrt(3.0 / e))
+
+
+def embed_half_spectrum(box: np.ndarray, n: int, kc: int) -> np.ndarray:
+    """One component of ``random_spectrum_modes`` in the [n][n][n/2+1] half-spectrum layout."""
+    out = np.zeros((n, n, n // 2 + 1), dtype=np.complex128)
+    idx = np.r_[np.arange(0, kc + 1), np.arange(n - kc, n)]        # fftfreq order of -kc..kc
+    src = np.r_[np.arange(kc, 2 * kc + 1), np.arange(0, kc)]
+    out[np.ix_(idx, idx, np.arange(kc + 1))] = box[np.ix_(src, src, np.arange(kc + 1))]
+    return out
