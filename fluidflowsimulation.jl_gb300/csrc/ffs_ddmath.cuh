@@ -120,24 +120,33 @@ __device__ inline double exp_cr(double x) {
 // ETD phi-coefficients: u' = E u + A N + B fm1 + C fm2 for stage 1 (ETD1), 2 (ETD2),
 // 3 (ETD3). Each expression follows the reference's left-to-right evaluation; muladd
 // is the emulated single-rounding fma.
+// CR = true: exp/expm1 correctly rounded (double-double), for bit parity of the FP64
+// form. CR = false: CUDA's FP64 exp/expm1 (within an ulp or two), for the FP32 form,
+// whose coefficients are rounded to FP32 afterwards; the formulas are the same.
+template <bool CR>
+__device__ inline double etd_exp(double x) { return CR ? dd::exp_cr(x) : exp(x); }
+template <bool CR>
+__device__ inline double etd_expm1(double x) { return CR ? dd::expm1_cr(x) : expm1(x); }
+
+template <bool CR = true>
 __device__ inline void etd_coeffs_exact(double c, double dt, double dt2, double dt3, int stage, double& E,
                                         double& Ac, double& Bc, double& Cc) {
   using namespace dd;
   const double cdt = M(c, dt);
-  E = exp_cr(cdt);
+  E = etd_exp<CR>(cdt);
   const bool test = M(-c, dt) <= 1e-4;
   const bool inf = (c == -INFINITY);
   if (stage == 1) {   // ETD1stand2ndO.jl:12-26
     const double cdt2 = M(cdt, dt), c2dt3 = M(cdt2, cdt), c3dt4 = M(c2dt3, cdt);
     if (inf) Ac = 0.0;
     else if (test) Ac = A(A(A(dt, M(0.5, cdt2)), D(c2dt3, 6.0)), D(c3dt4, 24.0));
-    else Ac = D(expm1_cr(cdt), c);
+    else Ac = D(etd_expm1<CR>(cdt), c);
     Bc = 0.0; Cc = 0.0;
     return;
   }
   if (stage == 2) {   // ETD1stand2ndO.jl:37-66
     const double cp2 = M(c, c), cdtp2 = M(cdt, dt), c2dtp3 = M(cdtp2, cdt), c3dtp4 = M(c2dtp3, cdt);
-    const double em = expm1_cr(cdt), c2dt2 = M(M(c, c), dt2);
+    const double em = etd_expm1<CR>(cdt), c2dt2 = M(M(c, c), dt2);
     const double dtp2 = M(dt, dt), dtp3 = M(dtp2, dt), dtp4 = M(dtp3, dt);
     if (inf) { Ac = 0.0; Bc = 0.0; }
     else if (test) {
@@ -183,7 +192,7 @@ __device__ inline void etd_coeffs_exact(double c, double dt, double dt2, double 
     Bc = fma_e(b1, l1, fma_e(b2, l2, b0));
     Cc = fma_e(c1, l1, fma_e(c2, l2, c0));
   } else {
-    const double em = expm1_cr(M(l1, dt));
+    const double em = etd_expm1<CR>(M(l1, dt));
     Ac = D(S(S(M(2.0, em), M(l2, S(e1, M(e2, em)))), M(l1, S(e3, M(e4, em)))), M(l3, e2));
     Bc = D(A(S(M(e5, l2), M(2.0, em)), M(l1, S(e3, M(e6, em)))), M(l3, e7));
     Cc = D(S(S(M(2.0, em), M(e8, l2)), M(l1, S(e3, M(dt2, em)))), M(l3, e9));

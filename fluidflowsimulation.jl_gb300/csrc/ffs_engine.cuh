@@ -79,6 +79,7 @@ class Engine : public EngineBase {
   int txy = TX;               // kx lines per CTA in the single-field y/z passes
   int nparts = 0;
   int upd_blocks = 1;
+  int n_sms = 1;
   size_t smem_z = 0, smem_y = 0, smem_x = 0, smem_zu = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -186,9 +187,17 @@ class Engine : public EngineBase {
     while (txy > TX / 2 && txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) txy /= 2;
     if (txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) { err = "grid size too large for this precision"; return FFS_EUNSUPPORTED; }
     {
-      const int pin = ((6 + (p.les ? 5 : 0) + (p.density ? 1 : 0)) + 1) / 2;
+      const int nin_x = 6 + (p.les ? 5 : 0) + (p.density ? 1 : 0);
+      const int pin = (nin_x + 1) / 2;
+      int maxs = 0;
+      FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device));
+      // (y,z) lines per CTA: within the thread budget and the shared-memory limit
+      auto xbytes = [&](int ly) {
+        const size_t lin1 = (size_t)pin * ly + 1, mxp = (size_t)(xc | 1);
+        return sizeof(cplx<T>) * ((size_t)srows(p.nx) * lin1 + std::max((size_t)nin_x * ly * mxp, (size_t)srows(p.nx) * lin1));
+      };
       lyz = 4;
-      while (lyz > 1 && pin * lyz * I.px.tpl > MAXT) lyz /= 2;
+      while (lyz > 1 && (pin * lyz * I.px.tpl > MAXT || xbytes(lyz) + 1024 > (size_t)maxs)) lyz /= 2;
       if (pin * lyz * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
     }
     if (((long long)p.ny * p.nz) % 4 != 0) { err = "ny*nz must be a multiple of 4"; return FFS_EUNSUPPORTED; }
@@ -285,6 +294,7 @@ class Engine : public EngineBase {
       int sms = 0;
       FFS_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p.device));
       upd_blocks = (int)std::min<long long>((I.cstride + 255) / 256, (long long)sms * 16);
+      n_sms = sms;
     }
     // record layout
     ncols_stats = 22 + (I.density ? 8 : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
@@ -504,11 +514,14 @@ class Engine : public EngineBase {
   }
   void launch_scalar(int mode) { k_scalar<T><<<1, 256, 0, s>>>(I, mode); }
   bool use_table() const { return !I.ab3; }
+  // the table is a few thousand FP64-heavy entries: spread them over every SM
+  int table_blocks() const {
+    const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
+    return (int)std::min<long long>((long long)n_sms * 8, (count + 63) / 64);
+  }
   void launch_table(int mode) {
     if (!use_table()) return;
-    const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
-    const int nb = (int)std::min<long long>(1024, (count + 255) / 256);
-    k_etd_table<T><<<nb, 256, 0, s>>>(I, mode);
+    k_etd_table<T><<<table_blocks(), 64, 0, s>>>(I, mode);
   }
   void launch_zu(int mode) {
     if constexpr (sizeof(T) == 4) {
@@ -862,10 +875,7 @@ class Engine : public EngineBase {
     g->yz_groups = P.ny * P.nz / lyz;
     g->fwd_z_tiles = I.KXP / txz;
     g->les = I.les; g->density = I.density; g->etd = !I.ab3;
-    {
-      const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
-      g->table_blocks = use_table() ? (int)std::min<long long>(1024, (count + 255) / 256) : 0;
-    }
+    g->table_blocks = use_table() ? table_blocks() : 0;
     g->nparts = nparts; g->upd_blocks = upd_blocks;
     g->txy = txy; g->txz = txz; g->lyz = lyz;
     return 0;

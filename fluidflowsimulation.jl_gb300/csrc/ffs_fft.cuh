@@ -237,6 +237,10 @@ __device__ void fft_lines(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS, co
 // every pass constant folds, and the CTA size is the plan's threads per line x L.
 // ---------------------------------------------------------------------------------
 template <int N> struct CtPlan { static constexpr int np = 0; };
+template <> struct CtPlan<32> { static constexpr int np = 2, r0 = 8, r1 = 4, r2 = 0, rmax = 8; };
+template <> struct CtPlan<48> { static constexpr int np = 3, r0 = 4, r1 = 4, r2 = 3, rmax = 4; };
+template <> struct CtPlan<64> { static constexpr int np = 2, r0 = 8, r1 = 8, r2 = 0, rmax = 8; };
+template <> struct CtPlan<96> { static constexpr int np = 3, r0 = 8, r1 = 4, r2 = 3, rmax = 8; };
 template <> struct CtPlan<128> { static constexpr int np = 2, r0 = 16, r1 = 8, r2 = 0, rmax = 16; };
 template <> struct CtPlan<256> { static constexpr int np = 2, r0 = 16, r1 = 16, r2 = 0, rmax = 16; };
 template <> struct CtPlan<512> { static constexpr int np = 3, r0 = 8, r1 = 8, r2 = 8, rmax = 8; };

@@ -504,11 +504,11 @@ __device__ __forceinline__ void b_etd_table(const Inst<T>& I, int mode, const Bl
       k2 = ref_k2(I, ix, ysig(I, jc), zsig(I, kc));
     }
     double E, A, B, C;
-    etd_coeffs_exact(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
+    etd_coeffs_exact<sizeof(T) == 8>(c_vel(I, k2), dt, dt2, dt3, stage, E, A, B, C);
     T* e = I.etab + 4 * q;
     e[0] = T(E); e[1] = T(A); e[2] = T(B); e[3] = T(C);
     if (I.density && I.etab_rho) {
-      etd_coeffs_exact(dd::M(k2, -I.alpha), dt, dt2, dt3, stage, E, A, B, C);
+      etd_coeffs_exact<sizeof(T) == 8>(dd::M(k2, -I.alpha), dt, dt2, dt3, stage, E, A, B, C);
       T* r = I.etab_rho + 4 * q;
       r[0] = T(E); r[1] = T(A); r[2] = T(B); r[3] = T(C);
     }
