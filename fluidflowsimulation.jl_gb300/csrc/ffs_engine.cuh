@@ -74,6 +74,7 @@ class Engine : public EngineBase {
   FieldList inv_list{}, fwd_list{};
   int nin = 0, nout = 0;
   int lyz = 4;
+  int lio = LYZ_IO;           // (y,z) lines per CTA of the field-IO x kernels
   int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass)
   int txz = TX;               // kx lines per CTA in the forward z pass
   int txy = TX;               // kx lines per CTA in the single-field y/z passes
@@ -201,7 +202,14 @@ class Engine : public EngineBase {
       if (pin * lyz * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
     }
     if (((long long)p.ny * p.nz) % 4 != 0) { err = "ny*nz must be a multiple of 4"; return FFS_EUNSUPPORTED; }
-    if (2 * LYZ_IO * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
+    // (y,z) lines per CTA of the field-IO x kernels: within the thread and shared-memory limits
+    {
+      int maxs = 0;
+      FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device));
+      lio = LYZ_IO;
+      while (lio > 1 && (2 * lio * I.px.tpl > MAXT || io_bytes(lio, p.nx) + 1024 > (size_t)maxs)) lio /= 2;
+      if (2 * lio * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
+    }
     txz = TX;
     while (txz > 1 && 3 * txz * I.pz.tpl > MAXT) txz /= 2;
     if (3 * txz * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
@@ -402,8 +410,9 @@ class Engine : public EngineBase {
     }
     if ((rc = smem_attr(zu_ptr(), smem_zu, err))) return rc;
     const size_t io = io_smem();
-    if ((rc = smem_attr(k_phys_fwd_x<T>, io, err))) return rc;
-    if ((rc = smem_attr(k_inv_x_phys<T>, io, err))) return rc;
+    if (lio == 4 && ((rc = smem_attr(k_phys_fwd_x<T, 4>, io, err)) || (rc = smem_attr(k_inv_x_phys<T, 4>, io, err)))) return rc;
+    if (lio == 2 && ((rc = smem_attr(k_phys_fwd_x<T, 2>, io, err)) || (rc = smem_attr(k_inv_x_phys<T, 2>, io, err)))) return rc;
+    if (lio == 1 && ((rc = smem_attr(k_phys_fwd_x<T, 1>, io, err)) || (rc = smem_attr(k_inv_x_phys<T, 1>, io, err)))) return rc;
     return 0;
   }
 
@@ -417,7 +426,14 @@ class Engine : public EngineBase {
     return 0;
   }
 
-  size_t io_smem() const { return sizeof(cplx<T>) * (size_t)srows(P.nx) * 2 * (2 * LYZ_IO + 1); }
+  static size_t io_bytes(int l, int nx) { return sizeof(cplx<T>) * (size_t)srows(nx) * 2 * (2 * l + 1); }
+  size_t io_smem() const { return io_bytes(lio, P.nx); }
+  template <int LIO> void phys_fwd_x(int cnt, int f0) {
+    k_phys_fwd_x<T, LIO><<<P.ny * P.nz / LIO, blk(2 * LIO, I.px), io_smem(), s>>>(I, cnt, f0);
+  }
+  template <int LIO> void inv_x_phys(const Inst<T>& J, int cnt) {
+    k_inv_x_phys<T, LIO><<<P.ny * P.nz / LIO, blk(2 * LIO, I.px), io_smem(), s>>>(J, cnt);
+  }
 
   using XK = void (*)(Inst<T>);
   template <int LY> static XK xsel(bool L, bool D) {
@@ -578,7 +594,6 @@ class Engine : public EngineBase {
     std::vector<double> tmp(2 * N, 0.0);
     const double* src[4] = {u1, u2, u3, rho};
     const int nf = I.density ? 4 : 3;
-    const size_t io = io_smem();
     for (int pair = 0; pair < 2; ++pair) {
       const int f0 = 2 * pair;
       const int cnt = std::min(2, nf - f0);
@@ -588,7 +603,9 @@ class Engine : public EngineBase {
         else std::fill(tmp.begin() + k * N, tmp.begin() + (k + 1) * N, 0.0);
       }
       FFS_CK(cudaMemcpyAsync(I.phys, tmp.data(), sizeof(double) * cnt * N, cudaMemcpyHostToDevice, s));
-      k_phys_fwd_x<T><<<P.ny * P.nz / LYZ_IO, blk(2 * LYZ_IO, I.px), io, s>>>(I, cnt, f0);
+      if (lio == 4) phys_fwd_x<4>(cnt, f0);
+      else if (lio == 2) phys_fwd_x<2>(cnt, f0);
+      else phys_fwd_x<1>(cnt, f0);
       FFS_CK(cudaGetLastError());
       FFS_CK(cudaStreamSynchronize(s));
     }
@@ -619,7 +636,6 @@ class Engine : public EngineBase {
     launch_inv_z(F);
     launch_inv_y(F);
     std::vector<double> tmp(2 * N);
-    const size_t io = io_smem();
     for (int pair = 0; pair < 2; ++pair) {
       const int f0 = 2 * pair;
       const int cnt = std::min(2, nf - f0);
@@ -627,7 +643,9 @@ class Engine : public EngineBase {
       // shift the wanted slots to 0/1 by offsetting the wy base
       Inst<T> J = I;
       J.wy = I.wy + (long long)f0 * I.wys;
-      k_inv_x_phys<T><<<P.ny * P.nz / LYZ_IO, blk(2 * LYZ_IO, I.px), io, s>>>(J, cnt);
+      if (lio == 4) inv_x_phys<4>(J, cnt);
+      else if (lio == 2) inv_x_phys<2>(J, cnt);
+      else inv_x_phys<1>(J, cnt);
       FFS_CK(cudaGetLastError());
       FFS_CK(cudaMemcpyAsync(tmp.data(), I.phys, sizeof(double) * cnt * N, cudaMemcpyDeviceToHost, s));
       FFS_CK(cudaStreamSynchronize(s));
@@ -878,6 +896,7 @@ class Engine : public EngineBase {
     g->table_blocks = use_table() ? table_blocks() : 0;
     g->nparts = nparts; g->upd_blocks = upd_blocks;
     g->txy = txy; g->txz = txz; g->lyz = lyz;
+    g->xfused = xfused;
     return 0;
   }
 

@@ -26,6 +26,7 @@ struct BatchGeom {
   int table_blocks;       // ETD table CTAs (0: AB3)
   int nparts, upd_blocks; // stats and update CTAs
   int txy, txz, lyz;
+  int xfused;             // n of the engine's register-fused x pass (0: none)
 };
 
 class EngineBase {

@@ -249,11 +249,11 @@ template <> struct CtPlan<1024> { static constexpr int np = 3, r0 = 16, r1 = 8, 
 template <int N> constexpr bool ct_plan_ok() { return CtPlan<N>::np > 0; }
 template <int N> constexpr int ct_tpl() { return N / CtPlan<N>::rmax; }
 
-template <int DIR, int L, typename T, int N, class LD, class ST>
+// LS: line stride in shared memory; NTB: threads of the CTA (0: L * ct_tpl<N>()).
+template <int DIR, int L, typename T, int N, class LD, class ST, int LS = L, int NTB = 0>
 __device__ __forceinline__ void fft_lines_ct(cplx<T>* s0, cplx<T>* s1, const cplx<T>* __restrict__ tw, LD ld, ST st) {
   using C = CtPlan<N>;
-  constexpr int NT = L * ct_tpl<N>();
-  constexpr int LS = L;
+  constexpr int NT = NTB > 0 ? NTB : L * ct_tpl<N>();
   constexpr int R0 = C::r0, R1 = C::r1, R2 = C::r2;
   // pass 0: p = 1
   fft_pass<R0, DIR, L, T, LD, ST, NT>(N / R0, 1, N / R0, true, false, s0, s0, LS, tw, ld, st);
@@ -269,12 +269,12 @@ __device__ __forceinline__ void fft_lines_ct(cplx<T>* s0, cplx<T>* s1, const cpl
   }
 }
 
-// The compile-time plan when N > 0 (then LS == L and the CTA has L * ct_tpl<N>()
-// threads), else the runtime plan P.
-template <int DIR, int L, typename T, int N, class LD, class ST>
+// The compile-time plan when N > 0 (line stride LSC, CTA of NTB threads, by default
+// L * ct_tpl<N>()), else the runtime plan P.
+template <int DIR, int L, typename T, int N, class LD, class ST, int LSC = L, int NTB = 0>
 __device__ __forceinline__ void fft_lines_n(const FftPlan& P, cplx<T>* s0, cplx<T>* s1, int LS,
                                             const cplx<T>* __restrict__ tw, LD ld, ST st) {
-  if constexpr (N > 0) fft_lines_ct<DIR, L, T, N>(s0, s1, tw, ld, st);
+  if constexpr (N > 0) fft_lines_ct<DIR, L, T, N, LD, ST, LSC, NTB>(s0, s1, tw, ld, st);
   else fft_lines<DIR, L, T>(P, s0, s1, LS, tw, ld, st);
 }
 

@@ -52,6 +52,8 @@ struct DevState {
   // At, Bt, Ct, fix_fm2 factor -(dt3+dt2)/dt2, forcing increment dt*eps/(2 E_f)
   double coef_d[5];
   float coef_f[6];
+  int skip_table;          // 1: the ETD table of the previous step still holds (fixed dt, stage 3)
+  int pad1;
 };
 enum CoefIdx : int { CO_A = 0, CO_B, CO_C, CO_FIX2, CO_FDT };
 template <typename T> __device__ __forceinline__ T step_coef(const DevState* S, int i);

@@ -123,6 +123,10 @@ class Server {
   int grid[BP_COUNT] = {0};
   int block[BP_COUNT] = {0};
   size_t smem[BP_COUNT] = {0};
+  ClassOps cls[BATCH_NCLASS] = {};          // size classes 1..: compile-time shapes
+  ClassLaunch cl[BATCH_NCLASS] = {};
+  cudaStream_t cs[BATCH_NCLASS] = {};       // one branch of the step graph per class
+  cudaEvent_t cev[BATCH_NCLASS + 1] = {};   // fork / join events of the capture
   std::vector<cudaEvent_t> ev_pool;
 
   ~Server() { shutdown(); }
@@ -221,6 +225,16 @@ class Server {
     // one-CTA-per-simulation passes need no more CTAs than simulations
     grid[BP_SCALAR] = std::min(grid[BP_SCALAR], cfg.max_active);
     grid[BP_FIN] = std::min(grid[BP_FIN], cfg.max_active);
+    // size classes with compile-time shapes
+    cls[1] = batch_class_ops_32(); cls[2] = batch_class_ops_48(); cls[3] = batch_class_ops_64();
+    cls[4] = batch_class_ops_96(); cls[5] = batch_class_ops_128();
+    for (int c = 1; c < BATCH_NCLASS; ++c) {
+      if (cls[c].n > cfg.max_n) continue;
+      std::string e;
+      if ((rc = cls[c].prepare(cfg.device, cfg.max_active, &cl[c], &e))) { terr = e; return rc; }
+    }
+    for (int c = 0; c < BATCH_NCLASS; ++c) SV_CK(cudaStreamCreateWithFlags(&cs[c], cudaStreamNonBlocking));
+    for (int c = 0; c <= BATCH_NCLASS; ++c) SV_CK(cudaEventCreateWithFlags(&cev[c], cudaEventDisableTiming));
 
     slots.resize(cfg.max_active);
     SV_CK(cudaMalloc(&d_inst, sizeof(BI) * cfg.max_active));
@@ -232,18 +246,31 @@ class Server {
     for (int i = 0; i < 2; ++i) SV_CK(cudaEventCreateWithFlags(&h_ev[i], cudaEventDisableTiming));
     SV_CK(cudaStreamSynchronize(S));
     // the step graph: one launch per pass, each walking its table
+    // the step graph: S forks one branch per class; each branch is that class's chain
     SV_CK(cudaStreamBeginCapture(S, cudaStreamCaptureModeThreadLocal));
-    kb_inv_z<float, TXB><<<grid[BP_INV_Z], block[BP_INV_Z], smem[BP_INV_Z], S>>>(d_inst, d_tab);
-    kb_inv_y<float, TXB><<<grid[BP_INV_Y], block[BP_INV_Y], smem[BP_INV_Y], S>>>(d_inst, d_tab);
-    kb_x<float, false, LYZB><<<grid[BP_X], block[BP_X], smem[BP_X], S>>>(d_inst, d_tab);
-    kb_x<float, true, LYZB><<<grid[BP_X_LES], block[BP_X_LES], smem[BP_X_LES], S>>>(d_inst, d_tab);
-    kb_fwd_y<float, TXB><<<grid[BP_FWD_Y], block[BP_FWD_Y], smem[BP_FWD_Y], S>>>(d_inst, d_tab);
-    kb_scalar<float><<<grid[BP_SCALAR], block[BP_SCALAR], 0, S>>>(d_inst, d_tab);
-    kb_table<float><<<grid[BP_TABLE], block[BP_TABLE], 0, S>>>(d_inst, d_tab);
-    kb_fwd_z<float, TXB><<<grid[BP_FWD_Z], block[BP_FWD_Z], smem[BP_FWD_Z], S>>>(d_inst, d_tab);
-    kb_stats<float><<<grid[BP_STATS], block[BP_STATS], 0, S>>>(d_inst, d_tab);
-    kb_update<float><<<grid[BP_UPDATE], block[BP_UPDATE], 0, S>>>(d_inst, d_tab);
-    kb_finalize<float><<<grid[BP_FIN], block[BP_FIN], 0, S>>>(d_inst, d_tab);
+    SV_CK(cudaEventRecord(cev[BATCH_NCLASS], S));
+    for (int c = 0; c < BATCH_NCLASS; ++c) {
+      if (c > 0 && cls[c].n > cfg.max_n) continue;
+      cudaStream_t b = cs[c];
+      SV_CK(cudaStreamWaitEvent(b, cev[BATCH_NCLASS], 0));
+      if (c == 0) {
+        kb_inv_z<float, TXB><<<grid[BP_INV_Z], block[BP_INV_Z], smem[BP_INV_Z], b>>>(d_inst, d_tab);
+        kb_inv_y<float, TXB><<<grid[BP_INV_Y], block[BP_INV_Y], smem[BP_INV_Y], b>>>(d_inst, d_tab);
+        kb_x<float, false, LYZB><<<grid[BP_X], block[BP_X], smem[BP_X], b>>>(d_inst, d_tab);
+        kb_x<float, true, LYZB><<<grid[BP_X_LES], block[BP_X_LES], smem[BP_X_LES], b>>>(d_inst, d_tab);
+        kb_fwd_y<float, TXB><<<grid[BP_FWD_Y], block[BP_FWD_Y], smem[BP_FWD_Y], b>>>(d_inst, d_tab);
+        kb_scalar<float><<<grid[BP_SCALAR], block[BP_SCALAR], 0, b>>>(d_inst, d_tab);
+        kb_table<float><<<grid[BP_TABLE], block[BP_TABLE], 0, b>>>(d_inst, d_tab);
+        kb_fwd_z<float, TXB><<<grid[BP_FWD_Z], block[BP_FWD_Z], smem[BP_FWD_Z], b>>>(d_inst, d_tab);
+        kb_stats<float><<<grid[BP_STATS], block[BP_STATS], 0, b>>>(d_inst, d_tab);
+        kb_update<float><<<grid[BP_UPDATE], block[BP_UPDATE], 0, b>>>(d_inst, d_tab);
+        kb_finalize<float><<<grid[BP_FIN], block[BP_FIN], 0, b>>>(d_inst, d_tab);
+      } else {
+        cls[c].enqueue(cl[c], b, d_inst, d_tab);
+      }
+      SV_CK(cudaEventRecord(cev[c], b));
+      SV_CK(cudaStreamWaitEvent(S, cev[c], 0));
+    }
     cudaError_t e = cudaStreamEndCapture(S, &graph);
     if (e != cudaSuccess) { terr = std::string("graph capture: ") + cudaGetErrorString(e); return FFS_ECUDA; }
     SV_CK(cudaGraphInstantiate(&gexec, graph, 0));
@@ -269,6 +296,14 @@ class Server {
     if (d_tab) cudaFree(d_tab);
     if (h_tab) cudaFreeHost(h_tab);
     d_items = nullptr; d_inst = nullptr; h_inst = nullptr; d_tab = nullptr; h_tab = nullptr;
+    for (int c = 0; c < BATCH_NCLASS; ++c) {
+      if (cs[c]) cudaStreamDestroy(cs[c]);
+      cs[c] = nullptr;
+    }
+    for (int c = 0; c <= BATCH_NCLASS; ++c) {
+      if (cev[c]) cudaEventDestroy(cev[c]);
+      cev[c] = nullptr;
+    }
     if (S) cudaStreamDestroy(S);
     S = nullptr;
   }
@@ -311,7 +346,7 @@ class Server {
     auto j = std::make_shared<Job>();
     j->p = p;
     j->p.device = cfg.device;
-    j->p.kernel_variant = 1;
+    j->p.kernel_variant = 0;   // 128^3 velocity-only engines carry the fused x pass twiddles
     // records of one run stay on the device until it finishes
     j->p.stats_capacity = (int32_t)std::max<int64_t>(64, r.nt / std::max(1, p.dt_stat) + 4);
     j->p.spec_capacity = (int32_t)std::max<int64_t>(4, r.nt / std::max(1, p.dt_spec) + 4);
@@ -533,34 +568,47 @@ class Server {
     return true;
   }
 
-  // work tables of the simulations in the batch
-  std::vector<WorkItem> items[BP_COUNT];
+  // size class of a simulation: its cubic side when a class exists for it (128^3
+  // velocity-only runs need the engine's register-pass twiddles), else the generic class
+  int class_of(const BatchGeom& g) const {
+    if (g.nx != g.ny || g.nx != g.nz) return 0;
+    for (int c = 1; c < BATCH_NCLASS; ++c)
+      if (cls[c].n == g.nx && g.nx <= cfg.max_n) return (g.nx == 128 && !g.les && g.xfused != 128) ? 0 : c;
+    return 0;
+  }
+
+  // work tables of the simulations in the batch, per class
+  std::vector<WorkItem> items[BATCH_NCLASS][BP_COUNT];
   int rebuild_tables(const std::vector<int>& dirty) {
-    for (auto& v : items) v.clear();
+    for (auto& c : items)
+      for (auto& v : c) v.clear();
     for (int k = 0; k < (int)slots.size(); ++k) {
       const Slot& s = slots[k];
       if (!s.job || s.retiring) continue;
       const BatchGeom& g = s.g;
+      auto& it = items[class_of(g)];
       for (int f = 0; f < g.nin; ++f)
         for (int t = 0; t < g.kx_tiles; ++t) {
-          for (int jc = 0; jc < g.nyr; ++jc) items[BP_INV_Z].push_back({k, f, t, jc});
-          for (int z = 0; z < g.nz; ++z) items[BP_INV_Y].push_back({k, f, t, z});
+          for (int jc = 0; jc < g.nyr; ++jc) it[BP_INV_Z].push_back({k, f, t, jc});
+          for (int z = 0; z < g.nz; ++z) it[BP_INV_Y].push_back({k, f, t, z});
         }
-      auto& xt = items[g.les ? BP_X_LES : BP_X];
-      for (int b = 0; b < g.yz_groups; ++b) xt.push_back({k, b, 0, 0});
+      auto& xt = it[g.les ? BP_X_LES : BP_X];
+      const int xg = (class_of(g) == 5 && !g.les) ? g.ny * g.nz / 8 : g.yz_groups;   // fused x: 8 lines per CTA
+      for (int b = 0; b < xg; ++b) xt.push_back({k, b, 0, 0});
       for (int f = 0; f < g.nout; ++f)
         for (int t = 0; t < g.kx_tiles; ++t)
-          for (int z = 0; z < g.nz; ++z) items[BP_FWD_Y].push_back({k, f, t, z});
-      items[BP_SCALAR].push_back({k, 0, 0, 0});
-      for (int b = 0; b < g.table_blocks; ++b) items[BP_TABLE].push_back({k, b, g.table_blocks, 0});
+          for (int z = 0; z < g.nz; ++z) it[BP_FWD_Y].push_back({k, f, t, z});
+      it[BP_SCALAR].push_back({k, 0, 0, 0});
+      for (int b = 0; b < g.table_blocks; ++b) it[BP_TABLE].push_back({k, b, g.table_blocks, 0});
       for (int t = 0; t < g.fwd_z_tiles; ++t)
-        for (int jc = 0; jc < g.nyr; ++jc) items[BP_FWD_Z].push_back({k, t, jc, 0});
-      for (int b = 0; b < g.nparts; ++b) items[BP_STATS].push_back({k, b, g.nparts, 0});
-      for (int b = 0; b < g.upd_blocks; ++b) items[BP_UPDATE].push_back({k, b, g.upd_blocks, 0});
-      items[BP_FIN].push_back({k, 0, 0, 0});
+        for (int jc = 0; jc < g.nyr; ++jc) it[BP_FWD_Z].push_back({k, t, jc, 0});
+      for (int b = 0; b < g.nparts; ++b) it[BP_STATS].push_back({k, b, g.nparts, 0});
+      for (int b = 0; b < g.upd_blocks; ++b) it[BP_UPDATE].push_back({k, b, g.upd_blocks, 0});
+      it[BP_FIN].push_back({k, 0, 0, 0});
     }
     size_t total = 0;
-    for (auto& v : items) total += v.size();
+    for (auto& c : items)
+      for (auto& v : c) total += v.size();
     total = std::max<size_t>(total, 1);
     // device table storage (grows; the descriptor carries the pointers)
     if (total > d_cap) {
@@ -580,12 +628,14 @@ class Server {
     }
     size_t off = 0;
     BatchTables t{};
-    for (int ph = 0; ph < BP_COUNT; ++ph) {
-      memcpy(h_items[b] + off, items[ph].data(), sizeof(WorkItem) * items[ph].size());
-      t.tab[ph] = d_items + off;
-      t.n[ph] = (int)items[ph].size();
-      off += items[ph].size();
-    }
+    for (int c = 0; c < BATCH_NCLASS; ++c)
+      for (int ph = 0; ph < BP_COUNT; ++ph) {
+        const auto& v = items[c][ph];
+        memcpy(h_items[b] + off, v.data(), sizeof(WorkItem) * v.size());
+        t.tab[c][ph] = d_items + off;
+        t.n[c][ph] = (int)v.size();
+        off += v.size();
+      }
     SV_CK(cudaEventSynchronize(h_ev[b ^ 1]));   // h_tab / h_inst are shared by both buffers
     *h_tab = t;
     for (int k : dirty) SV_CK(cudaMemcpyAsync(d_inst + k, h_inst + k, sizeof(BI), cudaMemcpyHostToDevice, S));

@@ -46,7 +46,7 @@ template <int N> struct XFused {
 // (lanes i read consecutive entries)
 
 template <int N>
-__global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(Inst<float> I) {
+__device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
   using T = float;
   using C = XFused<N>;
   constexpr int R = C::R, R2 = C::R2, LYZ = C::LYZ, TPL = C::TPL, NL = C::NL, LS = C::LS;
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(I
 
   const int tid = threadIdx.x;
   const int q = tid / TPL, i = tid % TPL;
-  const long long g = (long long)blockIdx.x * LYZ + q;   // (y,z) line
+  const long long g = (long long)bk.x * LYZ + q;   // (y,z) line
   const int Mx = I.Mx, KXP = I.KXP;
   const long long it = I.st->iteration;
   const bool want_ke = ((it % I.dt_stat) == 0) || ((it % I.dt_spec) == 0);
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(I
       const int r = l / LYZ, qq = l % LYZ;
       const int oa = 2 * r, ob = 2 * r + 1;
       const bool wb = ob != 3 || want_ke;   // output 3 (kinetic energy) only at stats iterations
-      const long long row = ((long long)blockIdx.x * LYZ + qq) * KXP;
+      const long long row = ((long long)bk.x * LYZ + qq) * KXP;
       cplx<T>* da = I.wy + (long long)I.out_slot[oa] * I.wys + row;
       cplx<T>* db = I.wy + (long long)I.out_slot[ob] * I.wys + row;
       for (int k = lane; k < KXP; k += 32) {
@@ -188,6 +188,11 @@ __global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(I
       }
     }
   }
+}
+
+template <int N>
+__global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB) k_x_fused(Inst<float> I) {
+  b_x_fused<N>(I, Blk::here());
 }
 
 }  // namespace ffsgpu
