@@ -369,8 +369,10 @@ def workload_config(wl: str):
     raise ValueError(wl)
 
 
-def make_sim(pkg, d, prec, ic, n, device):
-    sim = pkg.Simulation(pkg.parameters(d, precision=prec, device=device))
+def make_sim(pkg, d, prec, ic, n, device, autotune=1):
+    p = pkg.parameters(d, precision=prec, device=device)
+    p.autotune = autotune
+    sim = pkg.Simulation(p)
     if ic == "tg":
         sim.set_fields(*pkg.taylor_green(n))
     elif ic == "random3":
@@ -394,7 +396,8 @@ def run_workload(args):
     pkg.load()
     d, n, prec, ic, desc = workload_config(args.workload)
     world, rank, local, dist = dist_setup(args)
-    sim = make_sim(pkg, d, prec, ic, n, local)
+    sim = make_sim(pkg, d, prec, ic, n, local, 0 if args.no_autotune else 1)
+    tuning = sim.tuning
     sim.advance_in_time(max(args.warmup, 3))
     with ClockSampler(local) as clk:
         ms = sim.time_steps(args.steps)
@@ -410,7 +413,7 @@ def run_workload(args):
            "config": {"workload": desc, "grid": n, "l2": f"{dev_bytes / 1e9:.2f} GB resident per GPU"},
            "grid_point_updates_per_s": rate * n ** 3,
            "kernels_ms_per_step": {k: v / nprof for k, v in prof.items()}, "clocks": clk.summary(),
-           "gpu_launches": launches}
+           "gpu_launches": launches, "tuning": tuning}
     peak, kind = measured_peaks()
     elem = 8 if prec == "FP32" else 16
     A = (n // 2 + 1) * n * n * elem
@@ -491,6 +494,7 @@ def run_engine_arm(args):
 
     def make(prec):
         p = pkg.parameters(d, precision=prec, device=local)
+        p.autotune = 0 if args.no_autotune else 1
         sim = pkg.Simulation(p)
         sim.set_fields(*u)
         sim.initialize()
@@ -498,6 +502,7 @@ def run_engine_arm(args):
 
     # --- device-resident throughput, FP32 chosen form
     sim = make("FP32")
+    tuning = sim.tuning
     sim.advance_in_time(max(args.warmup, 3))
     cuda_sync()
     barrier(dist)
@@ -591,6 +596,7 @@ def run_engine_arm(args):
                             "get_fields (host)"},
         "clocks": clocks,
         "gpu_launches": launches,
+        "tuning": tuning,
     }
     if args.serve_requests > 0:
         line["serving"] = run_serving(pkg, args.serve_requests, args.serve_seq_budget, local)
@@ -609,6 +615,7 @@ def main():
     ap.add_argument("--workload", default="dns256", choices=["dns256", "tg64", "les128", "dns1024"],
                     help="dns256: the headline run; the others print one line for that configuration")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of the tuned ones")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--serve-requests", type=int, default=64, help="served-ensemble requests (0: skip)")

@@ -20,7 +20,8 @@ EXPORTS = [
     "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_get_fields",
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
     "ffs_stats_records", "ffs_spectrum_lengths", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
-    "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_stream",
+    "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_tuning_report",
+    "ffs_stream",
     "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
     "ffs_fetch_fields", "ffs_release", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
@@ -45,7 +46,7 @@ class FFSParams(ctypes.Structure):
         ("precision", c_int32), ("dt_stat", c_int32), ("dt_spec", c_int32), ("write_time", c_int32),
         ("start", c_int64), ("start_time", c_double),
         ("device", c_int32), ("reference_cfl_slot", c_int32),
-        ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("kernel_variant", c_int32),
+        ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("kernel_variant", c_int32), ("autotune", c_int32),
     ]
 
 
@@ -113,6 +114,7 @@ def load() -> ctypes.CDLL:
         "ffs_profile_kernels": (c_int32, [H, c_int64, c_char_p, c_int64, D, c_int32, POINTER(c_int32)]),
         "ffs_launches_per_step": (c_int32, [H]),
         "ffs_device_bytes": (c_int64, [H]),
+        "ffs_tuning_report": (c_int32, [H, c_char_p, c_int64]),
         "ffs_stream": (c_void_p, [H]),
         "ffs_fourier_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_double,
                                          c_double, c_double, c_void_p]),

@@ -65,6 +65,7 @@ int ffs_params_default(ffs_params* p) {
   p->stats_capacity = 256;
   p->spec_capacity = 16;
   p->kernel_variant = 0;
+  p->autotune = 0;
   return FFS_OK;
 }
 
@@ -191,6 +192,14 @@ int ffs_profile_kernels(ffs_handle* h, int64_t nsteps, char* names, int64_t name
 
 int32_t ffs_launches_per_step(const ffs_handle* h) { return h ? h->eng->launches_per_step() : 0; }
 int64_t ffs_device_bytes(const ffs_handle* h) { return h ? h->eng->device_bytes() : 0; }
+
+int ffs_tuning_report(const ffs_handle* h, char* buf, int64_t len) {
+  if (!h || !buf || len <= 0) return FFS_EINVAL;
+  const std::string s = h->eng->tuning();
+  if ((int64_t)s.size() + 1 > len) return FFS_EINVAL;
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return FFS_OK;
+}
 void* ffs_stream(const ffs_handle* h) { return h ? h->eng->stream() : nullptr; }
 
 const char* ffs_last_error(const ffs_handle* h) {

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -76,6 +77,10 @@ class Engine : public EngineBase {
   int lyz = 4;
   int lio = LYZ_IO;           // (y,z) lines per CTA of the field-IO x kernels
   int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass)
+  int xfused_ok = 0;          // n for which the fused x pass is available
+  bool use_ct = true;         // compile-time FFT plans in the FP32 y/z passes
+  bool zseq = false;          // forward z pass: one component at a time (TX lines)
+  std::string tune_report;    // candidates and timings of the autotuner
   int txz = TX;               // kx lines per CTA in the forward z pass
   int txy = TX;               // kx lines per CTA in the single-field y/z passes
   int nparts = 0;
@@ -128,6 +133,22 @@ class Engine : public EngineBase {
     int neg = 0;
     while (neg < n / 2 && !(k[n - 1 - neg] * k[n - 1 - neg] > c)) ++neg;
     cnt = pos + neg;
+  }
+
+  // shared memory of the passes for the current tiles
+  void compute_smem() {
+    const size_t cb = sizeof(cplx<T>);
+    smem_z = (size_t)txy * srows(P.nz) * cb * (I.pz.np >= 3 ? 2 : 1);
+    smem_y = (size_t)txy * srows(P.ny) * cb * (I.py.np >= 3 ? 2 : 1);
+    {
+      const int PIN = (nin + 1) / 2;
+      const int LIN = PIN * lyz;
+      const int MXP = I.Mx | 1;
+      smem_x = cb * ((size_t)srows(P.nx) * (LIN + 1) +
+                     std::max((size_t)nin * lyz * MXP, (size_t)srows(P.nx) * (LIN + 1)));
+    }
+    smem_zu = cb * ((size_t)zu_lines() * srows(P.nz) * (I.pz.np >= 3 ? 2 : 1) +
+                    (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
   }
 
   // physics parameters (everything that does not change buffer sizes or the step's passes)
@@ -275,7 +296,7 @@ class Engine : public EngineBase {
         default: break;
       }
       if (lyzf && ((long long)p.ny * p.nz) % lyzf == 0) {
-        xfused = p.nx;
+        xfused = xfused_ok = p.nx;
         const int tpl = p.nx / rf;
         cplx<T>* t = nullptr;
         if ((rc = alloc(&t, p.nx, err))) return rc;
@@ -331,19 +352,9 @@ class Engine : public EngineBase {
     if ((rc = alloc(&I.phys, (size_t)2 * p.nx * p.ny * p.nz, err))) return rc;
 
     // launch geometry / shared memory
-    const size_t cb = sizeof(cplx<T>);
-    smem_z = (size_t)txy * srows(p.nz) * cb * (I.pz.np >= 3 ? 2 : 1);
-    smem_y = (size_t)txy * srows(p.ny) * cb * (I.py.np >= 3 ? 2 : 1);
-    {
-      const int PIN = (nin + 1) / 2;
-      const int LIN = PIN * lyz;
-      const int MXP = I.Mx | 1;
-      smem_x = cb * ((size_t)srows(p.nx) * (LIN + 1) +
-                     std::max((size_t)nin * lyz * MXP, (size_t)srows(p.nx) * (LIN + 1)));
-    }
-    smem_zu = cb * ((size_t)3 * txz * srows(p.nz) * (I.pz.np >= 3 ? 2 : 1) +
-                    (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
+    compute_smem();
     if ((rc = set_smem(err))) return rc;
+    if (p.autotune && (rc = autotune(err))) return rc;
 
     // state and header
     if ((rc = reset_state(err))) return rc;
@@ -422,7 +433,11 @@ class Engine : public EngineBase {
     if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
-    if (ctzu() == NC && (rc = smem_attr(k_fwd_z<T, (NC >= 512 ? 2 : TX), NC>, smem_zu, err))) return rc;
+    if (ctzu() == NC) {
+      if (NC <= 256) { if ((rc = smem_attr(k_fwd_z<T, TX, NC>, smem_zu, err))) return rc; }
+      else if (zseq) { if ((rc = smem_attr(k_fwd_z<T, TX, NC, true>, smem_zu, err))) return rc; }
+      else if ((rc = smem_attr(k_fwd_z<T, 2, NC>, smem_zu, err))) return rc;
+    }
     return 0;
   }
 
@@ -449,10 +464,12 @@ class Engine : public EngineBase {
   }
   using ZK = void (*)(Inst<T>, FieldList, int);
   ZK zu_ptr() const {
+    if (zseq) return txz == TX ? k_fwd_z<T, TX, 0, true> : k_fwd_z<T, TX / 2, 0, true>;
     if (txz == TX) return k_fwd_z<T, TX>;
     if (txz == TX / 2) return k_fwd_z<T, TX / 2>;
     return k_fwd_z<T, (TX / 4 > 0 ? TX / 4 : 1)>;
   }
+  int zu_lines() const { return (zseq ? 1 : 3) * txz; }
 
   int reset_state(std::string& err) {
     DevState h;
@@ -472,12 +489,18 @@ class Engine : public EngineBase {
 
   // compile-time FFT lengths of the FP32 y/z passes (0: runtime plan)
   int ct_len(int n) const {
-    return (sizeof(T) == 4 && P.kernel_variant == 0 && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
+    return (sizeof(T) == 4 && P.kernel_variant == 0 && use_ct && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
   }
   int cty() const { return txy == TX ? ct_len(I.ny) : 0; }
   int ctz() const { return txy == TX ? ct_len(I.nz) : 0; }
-  int ctzu() const { return ct_len(I.nz) && txz == zu_tile(I.nz) ? I.nz : 0; }
-  static int zu_tile(int n) { return n >= 512 ? 2 : TX; }
+  // compile-time forward z kernels exist for (TX lines, 3 components) at 128/256,
+  // (2 lines, 3 components) and (TX lines, one component at a time) at 512/1024
+  int ctzu() const {
+    const int n = ct_len(I.nz);
+    if (!n) return 0;
+    if (n <= 256) return (txz == TX && !zseq) ? n : 0;
+    return ((txz == 2 && !zseq) || (txz == TX && zseq)) ? n : 0;
+  }
 
 #define FFS_CT_SWITCH(NSEL, CALL)                                    \
   switch (NSEL) {                                                    \
@@ -541,15 +564,22 @@ class Engine : public EngineBase {
   }
   void launch_zu(int mode) {
     if constexpr (sizeof(T) == 4) {
+      const dim3 g(I.KXP / txz, I.NYR);
       switch (ctzu()) {
-        case 128: k_fwd_z<T, TX, 128><<<dim3(I.KXP / TX, I.NYR), 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode); return;
-        case 256: k_fwd_z<T, TX, 256><<<dim3(I.KXP / TX, I.NYR), 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode); return;
-        case 512: k_fwd_z<T, 2, 512><<<dim3(I.KXP / 2, I.NYR), 3 * 2 * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode); return;
-        case 1024: k_fwd_z<T, 2, 1024><<<dim3(I.KXP / 2, I.NYR), 3 * 2 * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 128: k_fwd_z<T, TX, 128><<<g, 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 256: k_fwd_z<T, TX, 256><<<g, 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 512:
+          if (zseq) k_fwd_z<T, TX, 512, true><<<g, TX * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, 2, 512><<<g, 3 * 2 * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
+          return;
+        case 1024:
+          if (zseq) k_fwd_z<T, TX, 1024, true><<<g, TX * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, 2, 1024><<<g, 3 * 2 * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode);
+          return;
         default: break;
       }
     }
-    zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(3 * txz, I.pz), smem_zu, s>>>(I, fwd_list, mode);
+    zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(zu_lines(), I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
   void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
   void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
@@ -852,6 +882,139 @@ class Engine : public EngineBase {
     }
     return drain(it0, it0 + n - 1, err);
   }
+
+  // ---------------------------------------------------------------- autotuning
+  // Times the launch shapes each pass can take on this grid, on the engine's own
+  // buffers, and keeps the fastest:
+  //   y/z passes:  TX or TX/2 lines per CTA, compile-time or runtime FFT plan
+  //   x pass:      register-fused (FP32 velocity-only) or generic, 4/2/1 (y,z) lines
+  //   forward z:   TX, TX/2 or TX/4 lines; three components together or one at a time
+  // Each group is tuned on its own (they are independent passes). The choice is cached
+  // per grid, model and precision for the process, so engines of the same shape tune once.
+  struct TuneChoice {
+    int txy, use_ct, lyz, xfused, txz, zseq;
+    std::string report;
+  };
+  static std::mutex& tune_mu() { static std::mutex m; return m; }
+  static std::map<std::string, TuneChoice>& tune_cache() { static std::map<std::string, TuneChoice> c; return c; }
+
+  int autotune(std::string& err) {
+    const std::string key = std::to_string(sizeof(T)) + ":" + std::to_string(P.nx) + "x" + std::to_string(P.ny) + "x" +
+                            std::to_string(P.nz) + ":" + std::to_string(I.les) + std::to_string(I.density) + ":" +
+                            std::to_string(I.Mx) + "," + std::to_string(I.NYR) + "," + std::to_string(I.NZR) + ":" +
+                            std::to_string(P.kernel_variant);
+    {
+      std::lock_guard<std::mutex> g(tune_mu());
+      auto it = tune_cache().find(key);
+      if (it != tune_cache().end()) {
+        const TuneChoice& c = it->second;
+        txy = c.txy; use_ct = c.use_ct; lyz = c.lyz; xfused = c.xfused; txz = c.txz; zseq = c.zseq;
+        tune_report = c.report + " (cached)";
+        compute_smem();
+        return set_smem(err);
+      }
+    }
+    int maxs = 0;
+    FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, P.device));
+    const double work = (double)P.nx * P.ny * P.nz;
+    const int reps = work > 1.5e8 ? 3 : (work > 2e7 ? 5 : 20);
+    cudaEvent_t a, b;
+    FFS_CK(cudaEventCreate(&a));
+    FFS_CK(cudaEventCreate(&b));
+    std::string rep;
+    int rc = 0;
+    auto timed = [&](auto&& launch, float& ms) -> int {
+      compute_smem();
+      if (smem_z > (size_t)maxs || smem_y > (size_t)maxs || smem_x > (size_t)maxs || smem_zu > (size_t)maxs) {
+        ms = 1e30f;
+        return 0;
+      }
+      int r;
+      if ((r = set_smem(err))) return r;
+      launch();
+      FFS_CK(cudaGetLastError());
+      FFS_CK(cudaEventRecord(a, s));
+      for (int i = 0; i < reps; ++i) launch();
+      FFS_CK(cudaEventRecord(b, s));
+      FFS_CK(cudaEventSynchronize(b));
+      FFS_CK(cudaGetLastError());
+      FFS_CK(cudaEventElapsedTime(&ms, a, b));
+      ms /= reps;
+      return 0;
+    };
+    char line[160];
+    // y/z passes
+    {
+      float best = 1e30f;
+      int bt = txy, bc = use_ct;
+      for (int t : {TX, TX / 2})
+        for (int c : {1, 0}) {
+          if (t * std::max(I.py.tpl, I.pz.tpl) > MAXT) continue;
+          if (c && (sizeof(T) != 4 || t != TX || (!ct_len_raw(P.ny) && !ct_len_raw(P.nz)))) continue;
+          txy = t; use_ct = c;
+          float ms = 0.f;
+          if ((rc = timed([&] { launch_inv_z(inv_list); launch_inv_y(inv_list); launch_fwd_y(fwd_list); }, ms))) break;
+          snprintf(line, sizeof(line), "yz[tx=%d,%s]=%.4fms ", t, c ? "ct" : "rt", ms);
+          rep += line;
+          if (ms < best) { best = ms; bt = t; bc = c; }
+        }
+      txy = bt; use_ct = bc;
+    }
+    // x pass
+    if (!rc) {
+      float best = 1e30f;
+      int bl = lyz, bf = xfused;
+      const int pin = (nin + 1) / 2;
+      std::vector<std::pair<int, int>> cand;   // (fused n, lyz)
+      if (xfused_ok) cand.push_back({xfused_ok, lyz});
+      for (int l : {4, 2, 1})
+        if (pin * l * I.px.tpl <= MAXT) cand.push_back({0, l});
+      for (auto& c : cand) {
+        xfused = c.first; lyz = c.second;
+        float ms = 0.f;
+        if ((rc = timed([&] { launch_x(); }, ms))) break;
+        snprintf(line, sizeof(line), "x[%s%d]=%.4fms ", c.first ? "fused" : "lyz", c.first ? c.first : c.second, ms);
+        rep += line;
+        if (ms < best) { best = ms; bl = c.second; bf = c.first; }
+      }
+      lyz = bl; xfused = bf;
+    }
+    // forward z pass
+    if (!rc) {
+      float best = 1e30f;
+      int bt = txz, bq = zseq;
+      for (int q : {0, 1})
+        for (int t : {TX, TX / 2, TX / 4}) {
+          if (t < 1 || (q ? 1 : 3) * t * I.pz.tpl > MAXT) continue;
+          if (q && t < TX / 2) continue;
+          txz = t; zseq = q;
+          float ms = 0.f;
+          if ((rc = timed([&] { launch_zu(0); }, ms))) break;
+          snprintf(line, sizeof(line), "fwd_z[tx=%d,%s]=%.4fms ", t, q ? "seq" : "3c", ms);
+          rep += line;
+          if (ms < best) { best = ms; bt = t; bq = q; }
+        }
+      txz = bt; zseq = bq;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    snprintf(line, sizeof(line), "-> tx_yz=%d %s, x=%s%d, fwd_z tx=%d %s", txy, use_ct ? "ct" : "rt",
+             xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c");
+    rep += line;
+    tune_report = rep;
+    compute_smem();
+    if ((rc = set_smem(err))) return rc;
+    {
+      std::lock_guard<std::mutex> g(tune_mu());
+      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, rep};
+    }
+    return reset_state(err);
+  }
+  int ct_len_raw(int n) const {
+    return (sizeof(T) == 4 && P.kernel_variant == 0 && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
+  }
+  std::string tuning() const override { return tune_report; }
 
   int64_t device_bytes() const override { return bytes; }
   void* stream() const override { return (void*)s; }

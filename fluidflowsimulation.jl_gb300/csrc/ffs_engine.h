@@ -53,6 +53,8 @@ class EngineBase {
   virtual int repurpose(const ffs_params& p, std::string& err) = 0;
   // state after batched steps advanced the simulation outside step()
   virtual int sync_host_state(int64_t it_first, int64_t it_last, std::string& err) = 0;
+  // launch shapes picked by the autotuner, with the timings of the candidates
+  virtual std::string tuning() const = 0;
   // host-side views
   std::string header;
   int ncols_stats = 0, ncols_rec = 0;

@@ -533,14 +533,15 @@ __global__ void k_etd_table(Inst<T> I, int mode) {
 // the scratch buffer: [N(3)][ke][i k.tau(3)][i k.flux].
 // grid (KXP/TX, NYR); block 3 TX tpl_z.
 // ====================================================================================
-template <typename T, int TX, int N = 0>
+template <typename T, int TX, int N = 0, bool SEQ = false>
 __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, int mode, const Blk bk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int L3 = 3 * TX;
+  constexpr int LB = SEQ ? TX : L3;   // lines held at once: one component (SEQ) or all three
   const int nz = I.nz, NZR = I.NZR;
-  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);   // [srows(nz)][3 TX]
-  cplx<T>* bufB = buf + srows(nz) * L3;                  // second buffer (plans of >= 3 passes)
-  cplx<T>* accT = bufB + (I.pz.np >= 3 ? srows(nz) * L3 : 0);   // [3][NZR][TX] i k . tau (LES)
+  cplx<T>* buf = reinterpret_cast<cplx<T>*>(smem_raw);   // [srows(nz)][LB]
+  cplx<T>* bufB = buf + srows(nz) * LB;                  // second buffer (plans of >= 3 passes)
+  cplx<T>* accT = bufB + (I.pz.np >= 3 ? srows(nz) * LB : 0);   // [3][NZR][TX] i k . tau (LES)
   cplx<T>* accF = accT + 3 * NZR * TX;                   // [NZR][TX]    i k . flux (density)
 
   const long long it = I.st->iteration;
@@ -587,8 +588,21 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
     };
     fft_lines<-1, TX, T>(I.pz, buf, bufB, TX, I.twz, ld, st);
   }
-  // the three components of N together (3 TX lines), straight to the scratch buffer
-  {
+  if constexpr (SEQ) {   // large nz: one component at a time (TX lines), straight to the scratch buffer
+    const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
+#pragma unroll 1
+    for (int c = 0; c < 3; ++c) {
+      const cplx<T>* in = I.wz + (long long)nslot[c] * I.wzs + (long long)jc * I.KXP + kx0;
+      auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
+      auto st = [&](int l, int z, cplx<T> v) {
+        const int kc = zcomp(I, z);
+        if (kc < 0) return;
+        const bool k0 = kzero_col && l == 0 && z == 0;   // rhs.c[1] = 0 (models.jl:174)
+        out[c * cs + (long long)kc * rowstride + l] = k0 ? mk(T(0), T(0)) : scl(v, sc);
+      };
+      fft_lines_n<-1, TX, T, N>(I.pz, buf, bufB, TX, I.twz, ld, st);
+    }
+  } else {   // the three components of N together (3 TX lines), straight to the scratch buffer
     const cplx<T>* in0 = I.wz + (long long)nslot[0] * I.wzs + (long long)jc * I.KXP + kx0;
     const cplx<T>* in1 = I.wz + (long long)nslot[1] * I.wzs + (long long)jc * I.KXP + kx0;
     const cplx<T>* in2 = I.wz + (long long)nslot[2] * I.wzs + (long long)jc * I.KXP + kx0;
@@ -619,9 +633,9 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
     }
   }
 }
-template <typename T, int TX, int N = 0>
+template <typename T, int TX, int N = 0, bool SEQ = false>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
-  b_fwd_z<T, TX, N>(I, F, mode, Blk::here());
+  b_fwd_z<T, TX, N, SEQ>(I, F, mode, Blk::here());
 }
 
 // ====================================================================================

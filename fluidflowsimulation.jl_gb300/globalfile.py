@@ -98,6 +98,8 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
         p.forcing_kf = parse_number(d.get("forcingKf", "2.5"))
     if "referenceCflSlot" in d:
         p.reference_cfl_slot = 1 if _bool(d["referenceCflSlot"]) else 0
+    if "autotune" in d:   # engine key: time the candidate launch shapes at create
+        p.autotune = 1 if _bool(d["autotune"]) else 0
     prec = precision or d.get("precision", "FP64")
     p.precision = FFS_FP32 if prec.upper() == "FP32" else FFS_FP64
     p.device = device

@@ -29,6 +29,7 @@ mutable struct FFSParams
     start::Int64; start_time::Float64
     device::Int32; reference_cfl_slot::Int32
     stats_capacity::Int32; spec_capacity::Int32; kernel_variant::Int32
+    autotune::Int32
     FFSParams() = new()
 end
 

@@ -192,6 +192,13 @@ class Simulation:
         return int(self._L.ffs_launches_per_step(self._h))
 
     @property
+    def tuning(self) -> str:
+        """Launch shapes picked by the autotuner and the candidates' timings ('' if off)."""
+        buf = ctypes.create_string_buffer(8192)
+        self._check(self._L.ffs_tuning_report(self._h, buf, len(buf)))
+        return buf.value.decode()
+
+    @property
     def device_bytes(self) -> int:
         return int(self._L.ffs_device_bytes(self._h))
 

@@ -80,6 +80,7 @@ typedef struct ffs_params {
   int32_t spec_capacity;       /* spectrum records kept on the device between reads */
   int32_t kernel_variant;      /* 0: specialised FP32 kernels where available (register-fused x pass,
                                   compile-time FFT lengths); 1: runtime-plan kernels only */
+  int32_t autotune;            /* 1: time the candidate launch shapes at create, keep the fastest */
 } ffs_params;
 
 /* Fill defaults: reference defaults for every key that has one. */
@@ -140,6 +141,9 @@ int ffs_profile_kernels(ffs_handle* h, int64_t nsteps, char* names, int64_t name
 int32_t ffs_launches_per_step(const ffs_handle* h);
 /* Device bytes held by the handle. */
 int64_t ffs_device_bytes(const ffs_handle* h);
+/* Launch shapes chosen by the autotuner (ffs_params.autotune) with the candidates'
+ * timings, as text; empty when autotuning was off. No counterpart in the reference. */
+int ffs_tuning_report(const ffs_handle* h, char* buf, int64_t len);
 /* The handle's cudaStream_t. */
 void* ffs_stream(const ffs_handle* h);
 
