@@ -425,6 +425,10 @@ def run_workload(args):
                        f"fields x 5A), A = (n/2+1) n^2 complex", "achieved": b_alg / (ms / args.steps / 1e3) / 1e9,
                        "peak": peak, "unit": "GB/s", "peak_source": kind}
     out["roofline"]["frac"] = out["roofline"]["achieved"] / peak
+    if ntr == 9:   # velocity-only: the per-pass split of the 69A model
+        sb = survey_bytes(n, elem)
+        out["roofline"]["per_kernel_frac"] = {k: sb[k] / (prof[k] / nprof / 1e3) / 1e9 / peak
+                                              for k in sb if k in prof and prof[k] > 0}
     if prec == "FP32":
         # FP64 plain form on the same initial state, and the FP32 error after 10 steps
         try:
