@@ -147,10 +147,18 @@ int ffs_spectrum_lengths(const ffs_handle* h, int32_t* lenH, int32_t* lenV) {
   return FFS_OK;
 }
 
+int ffs_spectrum_fields(const ffs_handle* h, char* buf, int64_t len) {
+  if (!h || !buf || len <= 0) return FFS_EINVAL;
+  const std::string& s = h->eng->spec_names;
+  if ((int64_t)s.size() + 1 > len) return FFS_EINVAL;
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return h->eng->nspecf;
+}
+
 int64_t ffs_spectrum_records(ffs_handle* h, double* out, int64_t max_rows) {
   if (!h) return FFS_EINVAL;
   auto& v = h->eng->spec_host;
-  const int64_t rl = 1 + 2 * (int64_t)h->eng->lenH + 2 * (int64_t)h->eng->lenV;
+  const int64_t rl = 1 + (int64_t)h->eng->nspecf * ((int64_t)h->eng->lenH + (int64_t)h->eng->lenV);
   const int64_t have = (int64_t)v.size() / rl;
   if (!out) return have;
   const int64_t n = max_rows < have ? max_rows : have;

@@ -339,7 +339,13 @@ class Engine : public EngineBase {
     I.dkz = 1.0 / p.lz;
     I.nbinH = lenH; I.nbinV = lenV;
     I.spec_cap = p.spec_capacity > 0 ? p.spec_capacity : 16;
-    if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 4 * std::max(lenH, lenV), err))) return rc;
+    I.nspecf = SF_BASE_COUNT + (I.les ? 2 : 0) + (I.hv ? 2 : 0) + (I.density ? 4 : 0);
+    spec_names = "u_h,u_v,vis_h,vis_v,nl_h,nl_v,press_h,press_v";
+    if (I.les) spec_names += ",les_h,les_v";
+    if (I.hv) spec_names += ",hvis_h,hvis_v";
+    if (I.density) spec_names += ",buoyancy_v,rho,rhodiss,rhonl";
+    nspecf = I.nspecf;
+    if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 2 * I.nspecf * std::max(lenH, lenV), err))) return rc;
     // ETD tables
     if (!I.ab3) {
       const long long a = I.Mx - 1, b = std::max(I.ypos - 1, I.NYR - I.ypos), c = std::max(I.zpos - 1, I.NZR - I.zpos);
@@ -582,7 +588,10 @@ class Engine : public EngineBase {
     zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(zu_lines(), I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
   void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
-  void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
+  void launch_stats(int mode) {
+    k_stats<T><<<nparts, 256, 0, s>>>(I, mode);
+    k_spectra<T><<<nparts, 256, 0, s>>>(I, mode);
+  }
   void launch_fin(int mode) { k_finalize<T><<<1, 1024, 0, s>>>(I, mode, nparts); }
 
   void enqueue_step(int mode) {
@@ -597,7 +606,7 @@ class Engine : public EngineBase {
     launch_update(mode);
     launch_fin(mode);
   }
-  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0); }
+  int launches_per_step() const override { return 10 + (use_table() ? 1 : 0); }
 
   // ---------------------------------------------------------------- fields
   void repack_in(const double* src, double* dst, int layout) const {
@@ -777,7 +786,8 @@ class Engine : public EngineBase {
     const long long nsp = std::min<long long>(hs.nspec, I.spec_cap);
     const int stride = std::max(lenH, lenV);
     if (nsp > 0) {
-      std::vector<double> tmp((size_t)nsp * 4 * stride);
+      const int nq = 2 * I.nspecf;
+      std::vector<double> tmp((size_t)nsp * nq * stride);
       FFS_CK(cudaMemcpyAsync(tmp.data(), I.spec, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost, s));
       FFS_CK(cudaStreamSynchronize(s));
       // iterations of the spectrum records in this chunk
@@ -786,8 +796,8 @@ class Engine : public EngineBase {
         if (it % P.dt_spec == 0) its.push_back(it);
       for (long long r = 0; r < nsp; ++r) {
         spec_host.push_back(r < (long long)its.size() ? (double)its[r] : -1.0);
-        const double* rec = tmp.data() + r * 4 * stride;
-        for (int q = 0; q < 4; ++q) {
+        const double* rec = tmp.data() + r * nq * stride;
+        for (int q = 0; q < nq; ++q) {
           const int len = (q % 2 == 0) ? lenH : lenV;
           spec_host.insert(spec_host.end(), rec + q * stride, rec + q * stride + len);
         }

@@ -59,6 +59,8 @@ class EngineBase {
   std::string header;
   int ncols_stats = 0, ncols_rec = 0;
   int lenH = 0, lenV = 0;
+  int nspecf = 4;                  // spectrum fields per record
+  std::string spec_names;          // their names, comma-separated
   std::vector<double> rec_host;    // drained stats records
   std::vector<double> spec_host;   // drained spectrum records (iteration + 4 spectra)
   int64_t iteration = 0;

@@ -18,6 +18,13 @@ enum FieldCode : int {
 // Forward-field roles consumed by the forward z pass.
 enum FwdRole : int { R_NX = 0, R_NY, R_NZ, R_KE, R_TXX, R_TXY, R_TXZ, R_TYY, R_TYZ, R_FX, R_FY, R_FZ };
 
+// Spectrum fields of write_spec (spec.jl:1-171), in record order. The velocity-only
+// fields always come first; LES, hyperviscosity and density add theirs.
+enum SpecField : int {
+  SF_U_H = 0, SF_U_V, SF_VIS_H, SF_VIS_V, SF_NL_H, SF_NL_V, SF_PRESS_H, SF_PRESS_V, SF_BASE_COUNT
+};
+constexpr int SPEC_MAX_FIELDS = 16;
+
 // Stats partial-sum quantities (per CTA of the forward z pass).
 enum StatQ : int {
   Q_U1 = 0, Q_U2, Q_U3, Q_U12, Q_U22, Q_U32, Q_EH, Q_EV, Q_NLH, Q_NLV, Q_PH, Q_PV,
@@ -93,6 +100,7 @@ template <typename T> struct Inst {
   int rec_cap, ncols;
   double* spec;            // spectrum records [cap][4][nbin]
   int spec_cap, nbinH, nbinV;
+  int nspecf;              // spectrum fields per record (each binned into H and V)
   double maxdkh, dkz;
   // ETD coefficient tables [q][4] (E, A, B, C), velocity then density
   T* etab;

@@ -767,6 +767,25 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 1) k_update(Inst<T> 
   b_update<T>(I, mode, Blk::here());
 }
 
+// calculate_specHV (spec.jl:424-450) of one mode's value ee into a field's H and V bins
+// (FP64 atomics): the kx = 0 plane without the dk factors, as in the reference; bins
+// past the ends are dropped (the reference writes them out of bounds).
+template <typename T>
+__device__ __forceinline__ void spec_bin(const Inst<T>& I, double* f, int stride, double ee, int ix, int nx, int nj,
+                                         int nk) {
+  double* H = f;
+  double* V = f + stride;
+  if (ix == 0) {
+    if (nj < I.nbinH) { atomicAdd(&H[0], 0.5 * ee); atomicAdd(&H[nj], 0.5 * ee); }
+    if (nk < I.nbinV) atomicAdd(&V[nk], ee);
+  } else {
+    const double e2 = 2.0 * ee;
+    if (nx < I.nbinH) atomicAdd(&H[nx], 0.5 * e2 * I.maxdkh);
+    if (nj < I.nbinH) atomicAdd(&H[nj], 0.5 * e2 * I.maxdkh);
+    if (nk < I.nbinV) atomicAdd(&V[nk], e2 * I.dkz);
+  }
+}
+
 // ====================================================================================
 // Stats and spectra of the state before the update: u from the spectral state, N, ke,
 // i k.tau from the scratch buffer written by k_fwd_z (stats.jl:64-219,
@@ -793,7 +812,7 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
   const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
   const long long rec = S->nspec;
   const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
-  double* sp = I.spec + rec * 4LL * stride;
+  double* sp = I.spec + rec * 2LL * I.nspecf * stride;
   T q[Q_COUNT];
 #pragma unroll
   for (int i = 0; i < Q_COUNT; ++i) q[i] = T(0);
@@ -815,22 +834,8 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       const double hh = 0.5 * ((double)a2[0] + (double)a2[1]), vv = 0.5 * (double)a2[2];
       const int nk = (int)rint(fabs((double)kz) / I.dkz), nj = (int)rint(fabs((double)ky) / I.maxdkh);
       const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
-      const double vals[2] = {hh, vv};
-#pragma unroll
-      for (int s2 = 0; s2 < 2; ++s2) {
-        double* H = sp + (2 * s2) * stride;
-        double* V = sp + (2 * s2 + 1) * stride;
-        const double ee = vals[s2];
-        if (ix == 0) {
-          if (nj < I.nbinH) { atomicAdd(&H[0], 0.5 * ee); atomicAdd(&H[nj], 0.5 * ee); }
-          if (nk < I.nbinV) atomicAdd(&V[nk], ee);
-        } else {
-          const double e2 = 2.0 * ee;
-          if (nx < I.nbinH) atomicAdd(&H[nx], 0.5 * e2 * I.maxdkh);
-          if (nj < I.nbinH) atomicAdd(&H[nj], 0.5 * e2 * I.maxdkh);
-          if (nk < I.nbinV) atomicAdd(&V[nk], e2 * I.dkz);
-        }
-      }
+      spec_bin(I, sp + (2 * SF_U_H) * stride, stride, hh, ix, nx, nj, nk);
+      spec_bin(I, sp + (2 * SF_U_V) * stride, stride, vv, ix, nx, nj, nk);
     }
     if (!stats_t) continue;
     // velocity moments (velocity_stats, viscosity_stats, d*_squared_mean)
@@ -917,6 +922,108 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
 template <typename T>
 __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
   b_stats<T>(I, mode, Blk::here());
+}
+
+// ====================================================================================
+// The other write_spec spectra (spec.jl:1-146, 196-422) at spectrum iterations, from
+// the same state as the stats (before the update): viscous 2 nu k^2 E(k), non-linear
+// transfer proj(N - i k ke, u), pressure transfer proj(u, p k), LES proj(i k.tau, u),
+// hyperviscous nuh k^2M |u|^2, and with density the buoyancy proj(u_z, g_z rho), rho,
+// rho dissipation alpha k^2 |rho|^2 and rho transfer proj(i k.flux, rho). Each field is
+// binned by calculate_specHV into H and V. Grid-stride over the retained modes.
+// ====================================================================================
+template <typename T>
+__device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk bk) {
+  const DevState* S = I.st;
+  const long long it = S->iteration;
+  if (!(mode == 0 && (it % I.dt_spec) == 0)) return;
+  const long long rec = S->nspec;
+  if (rec >= I.spec_cap) return;
+  const long long cs = I.cstride;
+  const cplx<T>* sb = I.sbuf;
+  const cplx<T>* ub = I.uh;
+  const int stride = I.nbinH > I.nbinV ? I.nbinH : I.nbinV;
+  double* sp = I.spec + rec * 2LL * I.nspecf * stride;
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
+  const double nu = I.nu, nuh = I.hv_nu, alpha = I.alpha;
+  const double gz = (I.density && I.gdir == 2) ? I.gval : 0.0, gv = I.gval;
+  for (unsigned g = bk.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += bk.nx * blockDim.x) {
+    int ix, jc, kc;
+    decomp(I, g, ix, jc, kc);
+    if (ix >= I.Mx) continue;
+    const int ky_i = ysig(I, jc), kz_i = zsig(I, kc);
+    const T kx = kval(ix, Lx, iLx), ky = kval(ky_i, Ly, iLy), kz = kval(kz_i, Lz, iLz);
+    const double k2 = (double)(kx * kx + (ky * ky + kz * kz));
+    const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
+    const int nk = (int)rint(fabs((double)kz) / I.dkz), nj = (int)rint(fabs((double)ky) / I.maxdkh);
+    const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
+    auto bin = [&](int f, double v) { spec_bin(I, sp + (2 * f) * stride, stride, v, ix, nx, nj, nk); };
+    cplx<T> u[3];
+    double a2[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { u[c] = ub[c * cs + g]; a2[c] = (double)u[c].x * u[c].x + (double)u[c].y * u[c].y; }
+    // spectrum_viscosity of spectrum_u
+    bin(SF_VIS_H, 2.0 * nu * k2 * (0.5 * (a2[0] + a2[1])));
+    bin(SF_VIS_V, 2.0 * nu * k2 * (0.5 * a2[2]));
+    // spectrum_non_linear: proj(N - i k ke, u)
+    const cplx<T> ke = sb[3 * cs + g];
+    const T kk[3] = {kx, ky, kz};
+    double rx[3], ry[3], nl[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const cplx<T> Nc = sb[c * cs + g];
+      rx[c] = (double)Nc.x + (double)kk[c] * ke.y;
+      ry[c] = (double)Nc.y - (double)kk[c] * ke.x;
+      nl[c] = rx[c] * u[c].x + ry[c] * u[c].y;
+    }
+    bin(SF_NL_H, nl[0] + nl[1]);
+    bin(SF_NL_V, nl[2]);
+    int f = SF_BASE_COUNT;
+    double les[3] = {0, 0, 0};
+    if (I.les) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const cplx<T> dT = sb[(4 + c) * cs + g];
+        les[c] = (double)dT.x * u[c].x + (double)dT.y * u[c].y;
+        rx[c] += dT.x; ry[c] += dT.y;
+      }
+    }
+    cplx<T> rho = mk(T(0), T(0));
+    if (I.density) {
+      rho = ub[3 * cs + g];
+      rx[I.gdir] += (double)rho.x * gv; ry[I.gdir] += (double)rho.y * gv;
+    }
+    {  // spectrum_pressure: p1 = -(k . rhs')/k^2, proj(u, p1 k)
+      const double kdx = kx * rx[0] + ky * rx[1] + kz * rx[2];
+      const double kdy = kx * ry[0] + ky * ry[1] + kz * ry[2];
+      const double px = k0 ? 0.0 : -kdx / k2, py = k0 ? 0.0 : -kdy / k2;
+      double pr[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) pr[c] = (double)u[c].x * (px * kk[c]) + (double)u[c].y * (py * kk[c]);
+      bin(SF_PRESS_H, pr[0] + pr[1]);
+      bin(SF_PRESS_V, pr[2]);
+    }
+    if (I.les) { bin(f, les[0] + les[1]); bin(f + 1, les[2]); f += 2; }
+    if (I.hv) {   // spectrum_hyperviscosity: nuh (k^2)^M proj(u, u)
+      double km = k2;
+      for (int i = 1; i < I.hv_m; ++i) km *= k2;
+      bin(f, nuh * km * (a2[0] + a2[1]));
+      bin(f + 1, nuh * km * a2[2]);
+      f += 2;
+    }
+    if (I.density) {
+      const double r2 = (double)rho.x * rho.x + (double)rho.y * rho.y;
+      const cplx<T> dF = sb[7 * cs + g];
+      bin(f, gz * ((double)u[2].x * rho.x + (double)u[2].y * rho.y));   // buoyancy_v
+      bin(f + 1, r2);                                                     // rho
+      bin(f + 2, alpha * k2 * r2);                                        // rhodiss
+      bin(f + 3, (double)dF.x * rho.x + (double)dF.y * rho.y);           // rhonl
+    }
+  }
+}
+template <typename T>
+__global__ void __launch_bounds__(256) k_spectra(Inst<T> I, int mode) {
+  b_spectra<T>(I, mode, Blk::here());
 }
 
 // ====================================================================================

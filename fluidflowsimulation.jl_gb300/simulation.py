@@ -146,19 +146,33 @@ class Simulation:
             nu.append([r[0], r[1]] + b)
         return sc, nu
 
+    @property
+    def spectrum_fields(self) -> list[str]:
+        buf = ctypes.create_string_buffer(1024)
+        self._check(self._L.ffs_spectrum_fields(self._h, buf, len(buf)))
+        return buf.value.decode().split(",")
+
     def spectra(self) -> list[dict]:
-        rl = 1 + 2 * self.lenH + 2 * self.lenV
+        """Pending spectrum records as {"iteration", "<field>.specH", "<field>.specV", ...},
+        plus the h + v totals "<name>.specH" of writespectrum (spec.jl:173-194)."""
+        names = self.spectrum_fields
+        H, V = self.lenH, self.lenV
+        rl = 1 + len(names) * (H + V)
         n = self._L.ffs_spectrum_records(self._h, None, 0)
         out = np.empty((max(n, 0), rl))
         if n > 0:
             self._L.ffs_spectrum_records(self._h, out.ctypes.data_as(_D), n)
         res = []
-        H, V = self.lenH, self.lenV
         for r in out:
-            hH, hV = r[1:1 + H], r[1 + H:1 + H + V]
-            vH, vV = r[1 + H + V:1 + 2 * H + V], r[1 + 2 * H + V:]
-            res.append({"iteration": int(r[0]), "u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH,
-                        "u_v.specH": vH, "u_v.specV": vV})
+            rec = {"iteration": int(r[0])}
+            for i, nm in enumerate(names):
+                o = 1 + i * (H + V)
+                rec[f"{nm}.specH"] = r[o:o + H]
+                rec[f"{nm}.specV"] = r[o + H:o + H + V]
+            for base in ("u", "vis", "nl", "press", "les", "hvis"):
+                if f"{base}_h.specH" in rec:
+                    rec[f"{base}.specH"] = rec[f"{base}_h.specH"] + rec[f"{base}_v.specH"]
+            res.append(rec)
         return res
 
     @property
@@ -216,13 +230,24 @@ def stats_line(row) -> str:
     return ",".join([str(int(row[0]))] + [julia_float(v) for v in row[1:]]) + "\n"
 
 
-def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarray) -> None:
-    """``writespectrum("u", ...)`` (spec.jl:173-194): tab-separated (k, E) pairs."""
+def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarray, rhosource: float | None = None
+                         ) -> None:
+    """``write_spec`` (spec.jl:1-146, 173-194): tab-separated (k, E) pairs per spectrum
+    file. rhosource = -drho/dz / g_z turns the buoyancy spectra into rhosource.*."""
     i = rec["iteration"]
-    for name, k in (("u_h.specH", KH), ("u_h.specV", KRZ), ("u.specH", KH), ("u_v.specH", KH), ("u_v.specV", KRZ)):
+
+    def put(name, k, e):
         with open(folder / f"{name}.{i}", "w") as f:
-            for a, b in zip(k, rec[name]):
+            for a, b in zip(k, e):
                 f.write(f"{julia_float(float(a))}\t{julia_float(float(b))}\n")
+
+    for key, e in rec.items():
+        if key == "iteration":
+            continue
+        put(key, KH if key.endswith("specH") else KRZ, e)
+    if rhosource is not None and "buoyancy_v.specH" in rec:
+        put("rhosource.specH", KH, rec["buoyancy_v.specH"] * rhosource)
+        put("rhosource.specV", KRZ, rec["buoyancy_v.specV"] * rhosource)
 
 
 def run_simulation(folder: str | Path = ".", precision: str | None = None, device: int = 0) -> Simulation:
@@ -250,6 +275,8 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     KH = (np.arange(p.nx // 2 + 1) / p.lx) if kx1 >= ky1 else (np.arange(p.ny // 2 + 1) / p.ly)
     KRZ = np.arange(p.nz // 2 + 1) / p.lz
     wt = int(p.write_time)
+    # rhosource = -(buoyancy / g_z) * drho/dz (spec.jl:53-54)
+    rhos = (-p.density_gradient / p.gravity) if (p.density and p.gravity_dir == 2 and p.gravity != 0) else None
 
     def flush():
         recs = sim.records()
@@ -262,7 +289,7 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
                 for r in rows:
                     f.write(stats_line(r))
         for rec in sim.spectra():
-            write_spectrum_files(folder, rec, KH, KRZ)
+            write_spectrum_files(folder, rec, KH, KRZ, rhos)
 
     while sim.iteration < final_step and sim.time < final_time:
         it = sim.iteration

@@ -120,10 +120,15 @@ int32_t ffs_record_ncols(const ffs_handle* h);
 /* Move up to max_rows pending stats records to the host (oldest first). */
 int64_t ffs_stats_records(ffs_handle* h, double* out, int64_t max_rows);
 
-/* u spectra (spectrum_u + calculate_specHV, src/spec.jl:316-327,424-450):
- * lengths of the H and V spectra, then pending records of
- * [iteration, u_h.specH(lenH), u_h.specV(lenV), u_v.specH(lenH), u_v.specV(lenV)]. */
+/* Spectra of write_spec (src/spec.jl:1-146,196-450) at iterations multiple of dtSpec:
+ * every field binned by calculate_specHV into an H spectrum (lenH) and a V spectrum
+ * (lenV). ffs_spectrum_fields gives the field names, comma-separated, in record order
+ * (u_h, u_v, vis_h, vis_v, nl_h, nl_v, press_h, press_v, then les_h, les_v with LES,
+ * hvis_h, hvis_v with hyperviscosity, buoyancy_v, rho, rhodiss, rhonl with density) and
+ * returns their count F. A record is [iteration, then per field: specH(lenH), specV(lenV)],
+ * 1 + F (lenH + lenV) doubles. */
 int ffs_spectrum_lengths(const ffs_handle* h, int32_t* lenH, int32_t* lenV);
+int ffs_spectrum_fields(const ffs_handle* h, char* buf, int64_t len);
 int64_t ffs_spectrum_records(ffs_handle* h, double* out, int64_t max_rows);
 
 int64_t ffs_iteration(const ffs_handle* h);

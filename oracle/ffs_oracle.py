@@ -593,7 +593,10 @@ class OracleSimulation:
         if p.variable_dt:
             self.set_dt()
         if spec_t:
-            self.spectra[self.iteration] = self.spectrum_u()
+            sp = self.spectrum_u()
+            ikflux = (1j * (KX * fluxh[0] + (KY * fluxh[1] + KZ * fluxh[2]))) if p.density else None
+            sp.update(self.spectra_write_spec(nlh, kspec, tauh, ikflux))
+            self.spectra[self.iteration] = sp
         if stats_t:                                               # models.jl:38-46
             self.nlstats = self.non_linear_stats(nlh, kspec)
             self.pressstats = self.pressure_stats(nlh, kspec, tauh)
@@ -877,6 +880,55 @@ class OracleSimulation:
         vH, vV = self.calculate_specHV(vout)
         return {"u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH,
                 "u_v.specH": vH, "u_v.specV": vV}
+
+    def spectra_write_spec(self, nl, ke, tauh, ikflux):
+        """The other spectra of ``write_spec`` (spec.jl:1-146, 196-422), binned by
+        ``calculate_specHV``: viscous, non-linear, pressure, LES, hyperviscous and the
+        density spectra (buoyancy_v, rho, rhodiss, rhonl). Keys '<field>.specH/V'."""
+        p, g = self.p, self.g
+        u = self.u
+        out = {}
+
+        def put(name, field):
+            H, V = self.calculate_specHV(field)
+            out[name + ".specH"], out[name + ".specV"] = H, V
+
+        k2 = g.KX * g.KX + (g.KY * g.KY + g.KZ * g.KZ)
+        uh_ = 0.5 * (_proj(u[0], u[0]) + _proj(u[1], u[1]))
+        uv_ = 0.5 * _proj(u[2], u[2])
+        put("vis_h", 2 * p.nu * k2 * uh_)                         # spectrum_viscosity
+        put("vis_v", 2 * p.nu * k2 * uv_)
+        r = np.stack([nl[0] - 1j * g.KX * ke, nl[1] - 1j * g.KY * ke, nl[2] - 1j * g.KZ * ke])
+        put("nl_h", _proj(r[0], u[0]) + _proj(r[1], u[1]))        # spectrum_non_linear
+        put("nl_v", _proj(r[2], u[2]))
+        if p.les:
+            dt_ = self.div_tau(tauh)
+            r = r + dt_
+        if p.density:
+            for d in range(3):
+                if self.gvec[d] != 0.0:
+                    r[d] = r[d] + self.rho * self.gvec[d]
+        kd = g.KX * r[0] + g.KY * r[1] + g.KZ * r[2]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            p1 = -kd / g.K2
+        p1[0, 0, 0] = 0.0
+        put("press_h", _proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY))   # spectrum_pressure
+        put("press_v", _proj(u[2], p1 * g.KZ))
+        if p.les:
+            put("les_h", _proj(dt_[0], u[0]) + _proj(dt_[1], u[1]))       # spectrum_les
+            put("les_v", _proj(dt_[2], u[2]))
+        if p.hv:
+            km = k2 ** p.hv_m
+            put("hvis_h", p.hv_nu * km * (_proj(u[0], u[0]) + _proj(u[1], u[1])))
+            put("hvis_v", p.hv_nu * km * _proj(u[2], u[2]))
+        if p.density:
+            rho = self.rho
+            put("buoyancy_v", self.gvec[2] * _proj(u[2], rho))            # spectrum_buoyancy
+            r2 = _proj(rho, rho)
+            put("rho", r2)                                                # spectrum_rho
+            put("rhodiss", self.alpha * k2 * r2)                          # spectrum_rhodiss
+            put("rhonl", _proj(ikflux, rho))                              # spectrum_rhonl
+        return out
 
     def calculate_specHV(self, out):
         """spec.jl:424-450 (kx = 0 plane without the dk factors, as in the reference)."""

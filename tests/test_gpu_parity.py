@@ -143,22 +143,31 @@ def test_transform_roundtrip(gpu_pkg):
         sim.close()
 
 
-def test_spectrum_parity(gpu_pkg):
-    d = gdict(32, dtSpec="2")
-    u, _ = make_ic(gpu_pkg, d)
-    sim = gpu_pkg.Simulation.from_global(d)
-    sim.set_fields(*u)
-    sim.initialize()
-    sim.advance_in_time(5)
-    ref = OracleSimulation(Params.from_global(d), u)
-    ref.initialize()
-    ref.run(5)
+SPEC_CASES = {
+    "ab3": gdict(32, dtSpec="2"),
+    "etd-les-density": dict(FIXED_CASES["etd-les-density"], dtSpec="2"),
+    "ab3-hv-forced": dict(FIXED_CASES["ab3-64-hv-forced"], dtSpec="2"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SPEC_CASES))
+def test_spectrum_parity(gpu_pkg, name):
+    """Every write_spec spectrum (spec.jl:1-146, 196-450) against the oracle, FP64."""
+    d = SPEC_CASES[name]
+    density = "densityStratification" in d
+    sim, ref = run_pair(gpu_pkg, d, steps=5, density=density)
     got = sim.spectra()
     assert [r["iteration"] for r in got] == sorted(ref.spectra)
+    fields = sim.spectrum_fields
+    assert fields[:8] == ["u_h", "u_v", "vis_h", "vis_v", "nl_h", "nl_v", "press_h", "press_v"]
     for r in got:
         e = ref.spectra[r["iteration"]]
-        for key in ("u_h.specH", "u_h.specV", "u.specH", "u_v.specH", "u_v.specV"):
-            assert np.allclose(r[key], e[key], rtol=1e-12, atol=1e-15 * np.abs(e[key]).max()), key
+        keys = [f"{f}.{s}" for f in fields for s in ("specH", "specV")] + ["u.specH"]
+        for key in keys:
+            # transfer spectra sum to ~0: the floor is relative to the field's own scale
+            scale = max(np.abs(e[key]).max(), 1e-300)
+            assert np.allclose(r[key], e[key], rtol=1e-10, atol=1e-12 * scale), (name, key)
+    sim.close()
 
 
 def test_errors_and_state_checks(gpu_pkg):
