@@ -3,7 +3,8 @@
 # Drop-in for FluidFlowSimulation.jl's time loop: `run_simulation()` reads the same
 # `global` file and u1.$start/u2.$start/u3.$start (+ rho.$start) fields, runs
 # initialize! and advance_in_time! on the GPU through the C ABI of include/ffs.h, and
-# writes Stats.txt and the field files in the reference formats.
+# writes Stats.txt, Scales.txt, Numbers.txt, the spectra and the field files in the
+# reference formats.
 #
 # Usage (with libffs.so built):  ENV["FFS_LIB"] = "/path/to/libffs.so"
 #   using FFSEngine; run_simulation()
@@ -120,13 +121,95 @@ function getfields(e::Engine)
     return out
 end
 
-function statsrows(e::Engine)
+# pending records: Stats.txt columns, then 9 integral-length plane sums and 4 derivative means
+function records(e::Engine)
     nc = ccall((:ffs_record_ncols, LIB), Cint, (Ptr{Cvoid},), e.h)
-    ns = ccall((:ffs_stats_ncols, LIB), Cint, (Ptr{Cvoid},), e.h)
     n = ccall((:ffs_stats_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, C_NULL, 0)
     buf = Array{Float64}(undef, nc, max(n, 0))
     n > 0 && ccall((:ffs_stats_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, buf, n)
-    return buf[1:ns, :]
+    return buf
+end
+statsncols(e::Engine) = Int(ccall((:ffs_stats_ncols, LIB), Cint, (Ptr{Cvoid},), e.h))
+
+# Scales.txt / Numbers.txt rows of one record (stats.jl:64-165)
+function scalesnumbers(r, names, ns, p::FFSParams)
+    col(n) = r[findfirst(==(n), names)]
+    u1p2, u2p2, u3p2, k, tdiss = col("u1p2"), col("u2p2"), col("u3p2"), col("k"), col("tdiss")
+    s = r[ns+1:ns+9]
+    du1dyp2, du1dxp2, du2dyp2, du2dxp2 = r[ns+10], r[ns+11], r[ns+12], r[ns+13]
+    Ls = (p.lx, p.ly, p.lz); up2 = (u1p2, u2p2, u3p2)
+    L = [Ls[q] * s[3*(c-1)+q] * pi / up2[c] for c in 1:3 for q in 1:3]
+    L11, L12, L13, L21, L22, L23, L31, L32, L33 = L
+    uh = sqrt((u1p2 + u2p2) / 2); urms = sqrt((u1p2 + u2p2 + u3p2) / 3)
+    λ12 = sqrt(2 * u1p2 / du1dyp2); λ21 = sqrt(2 * u2p2 / du2dxp2)
+    Lhh = (L11 + L22) / 2; Thh = Lhh / urms
+    λl = sqrt(2 * (u1p2 + u2p2) / (du1dxp2 + du2dyp2)); λt = sqrt(2 * (u1p2 + u2p2) / (du1dyp2 + du2dxp2))
+    Lhv = (L13 + L23) / 2; Lvv = L33; Lvh = (L31 + L32) / 2
+    ν = p.nu
+    Lt = sqrt(k * k * k) / tdiss; Tt = k / tdiss; Lk = sqrt(sqrt(ν * ν * ν / tdiss)); Tk = sqrt(ν / tdiss)
+    λg = sqrt(15 * ν / tdiss) * urms
+    lensv = (Lk, Lt, λg, λl, λt, Lhh, Lvv, Lhv, Lvh, λ12, λ21, L11, L12, L13, L21, L22, L23, L31, L32, L33)
+    Reh = uh * Lhh / ν; Reh1 = (Lhh / Lk)^(4 / 3)
+    Reλg = urms * λg / ν; Reλg1 = (λg / Lk)^(4 / 3)
+    Reλl = urms * λl / ν; Reλl1 = (λl / Lk)^(4 / 3)
+    Reλt = urms * λt / ν; Reλt1 = (λt / Lk)^(4 / 3)
+    if p.density == 1
+        Nb = sqrt((p.gravity_dir == 2 ? p.gravity : 0.0) * p.density_gradient)
+        Lb = 2π * urms / Nb; Lo = sqrt(tdiss / (Nb * Nb * Nb)); Lom = sqrt(tdiss / (Nb * Nb * Nb / (8 * pi * pi * pi)))
+        Tb = 2π / Nb; Tbm = 1 / Nb
+        return (lensv..., Lb, Lo, Lom, Tk, Tt, Thh, Tb, Tbm),
+               (Reh, Reh1, Reλg, Reλl, Reλt, Reλg1, Reλl1, Reλt1, (Lo / Lk)^(4 / 3), (Lom / Lk)^(4 / 3),
+                2π * uh / (Nb * Lhh), Lhv / Lhh)
+    end
+    return (lensv..., Tk, Tt, Thh), (Reh, Reh1, Reλl, Reλt, Reλl1, Reλt1)
+end
+
+scalesheader(d) = "iteration,time,Lk,Lt,lamg,laml,lamt,Lhh,Lvv,Lhv,Lvh,lam12,lam21,L11,L12,L13,L21,L22,L23,L31,L32,L33" *
+                  (d ? ",Lb,Lo,Lom,Tk,Tt,Thh,Tb,Tbm" : ",Tk,Tt,Thh")
+numbersheader(d) = "iteration,time,Reh,Reh1,Relamg,Relaml,Relamt,Relamg1,Relaml1,Relamt1" * (d ? ",Reb,Rebm,Frh,Frh1" : "")
+
+# write_spec spectra (spec.jl:1-194): every field as name.specH.i / name.specV.i, plus the
+# h + v totals name.specH.i of writespectrum
+writepairs(name, k, e) = open(name, "w") do f
+    for (a, b) in zip(k, e)
+        println(f, a, '\t', b)
+    end
+end
+
+function writespectra(e::Engine)
+    lenH = Ref{Int32}(0); lenV = Ref{Int32}(0)
+    check(e, ccall((:ffs_spectrum_lengths, LIB), Cint, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}), e.h, lenH, lenV))
+    nbuf = Vector{UInt8}(undef, 1024)
+    nf = ccall((:ffs_spectrum_fields, LIB), Cint, (Ptr{Cvoid}, Ptr{UInt8}, Int64), e.h, nbuf, 1024)
+    nf > 0 || error("ffs_spectrum_fields failed")
+    names = split(unsafe_string(pointer(nbuf)), ",")
+    H, V = Int(lenH[]), Int(lenV[])
+    n = ccall((:ffs_spectrum_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, C_NULL, 0)
+    n <= 0 && return nothing
+    buf = Array{Float64}(undef, 1 + length(names) * (H + V), n)
+    ccall((:ffs_spectrum_records, LIB), Int64, (Ptr{Cvoid}, Ptr{Float64}, Int64), e.h, buf, n)
+    p = e.p
+    KH = p.lx <= p.ly ? collect(0:(p.nx ÷ 2)) ./ p.lx : collect(0:(p.ny ÷ 2)) ./ p.ly
+    KRZ = collect(0:(p.nz ÷ 2)) ./ p.lz
+    for r in eachcol(buf)
+        i = Int(r[1])
+        spec(f) = (o = 1 + (f - 1) * (H + V); (r[o+1:o+H], r[o+H+1:o+H+V]))
+        for (f, nm) in enumerate(names)
+            sH, sV = spec(f)
+            writepairs("$nm.specH.$i", KH, sH)
+            writepairs("$nm.specV.$i", KRZ, sV)
+            if nm == "buoyancy_v" && p.gravity_dir == 2 && p.gravity != 0   # spec.jl:53-57
+                writepairs("rhosource.specH.$i", KH, sH .* (-p.density_gradient / p.gravity))
+                writepairs("rhosource.specV.$i", KRZ, sV .* (-p.density_gradient / p.gravity))
+            end
+        end
+        for base in ("u", "vis", "nl", "press", "les", "hvis")
+            ih = findfirst(==("$(base)_h"), names); iv = findfirst(==("$(base)_v"), names)
+            (ih === nothing || iv === nothing) && continue
+            writepairs("$base.specH.$i", KH, spec(ih)[1] .+ spec(iv)[1])
+        end
+    end
+    return nothing
 end
 
 function statsheader(e::Engine)
@@ -150,14 +233,29 @@ function run_simulation()
     u = [open(f -> readfield(f, p.nx, p.ny, p.nz), "u$i.$s") for i in 1:3]
     rho = (p.density == 1 && isfile("rho.$s")) ? open(f -> readfield(f, p.nx, p.ny, p.nz), "rho.$s") : nothing
     setfields!(e, u..., rho)
-    s == 0 && open(f -> write(f, statsheader(e), "\n"), "Stats.txt", "w")
+    if s == 0
+        open(f -> write(f, statsheader(e), "\n"), "Stats.txt", "w")
+        open(f -> write(f, scalesheader(p.density == 1), "\n"), "Scales.txt", "w")
+        open(f -> write(f, numbersheader(p.density == 1), "\n"), "Numbers.txt", "w")
+    end
+    names = split(statsheader(e), ",")
+    ns = statsncols(e)
     initialize!(e)
     total = haskey(d, :nt) ? parse(Int, d[:nt]) : typemax(Int) - s
     final = s + total
-    flush() = open("Stats.txt", "a+") do f
-        for r in eachcol(statsrows(e))
-            join(f, (Int(r[1]), r[2:end]..., "\n"), ",", "")
+    function flush()
+        recs = records(e)
+        open("Stats.txt", "a+") do f
+            for r in eachcol(recs)
+                join(f, (Int(r[1]), r[2:ns]..., "\n"), ",", "")
+            end
         end
+        for r in eachcol(recs)
+            lens, anums = scalesnumbers(r, names, ns, p)
+            open(f -> join(f, (Int(r[1]), r[2], lens..., "\n"), ",", ""), "Scales.txt", "a+")
+            open(f -> join(f, (Int(r[1]), r[2], anums..., "\n"), ",", ""), "Numbers.txt", "a+")
+        end
+        writespectra(e)
     end
     while iteration(e) < final
         it = iteration(e)

@@ -149,7 +149,9 @@ class Simulation:
     @property
     def spectrum_fields(self) -> list[str]:
         buf = ctypes.create_string_buffer(1024)
-        self._check(self._L.ffs_spectrum_fields(self._h, buf, len(buf)))
+        n = self._L.ffs_spectrum_fields(self._h, buf, len(buf))   # the field count, or an error code
+        if n < 0:
+            self._check(n)
         return buf.value.decode().split(",")
 
     def spectra(self) -> list[dict]:
