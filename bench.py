@@ -154,7 +154,9 @@ def algorithmic_bytes(n: int, elem: int) -> dict[str, float]:
             + 3 * V + 3 * V + 15 * C}
 
 
-def dist_setup(args):
+def dist_setup(args, backend: str = "nccl"):
+    """Replicas: one process per GPU, no data-path collective. Only the timing uses the
+    process group (a barrier around the timed region and a max over ranks)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -162,8 +164,9 @@ def dist_setup(args):
     if world > 1:
         import torch
         import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local, dist
 
 
@@ -176,9 +179,17 @@ def max_over_ranks(dist, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(dist, world: int, steps: int, ms_local: float) -> tuple[float, float]:
+    """Whole-job steps/s of independent replicas: all ranks' steps over the slowest
+    rank's time. Returns (steps/s, max ms)."""
+    ms = max_over_ranks(dist, ms_local)
+    return steps * world / (ms / 1e3), ms
 
 
 def cuda_sync():
@@ -514,8 +525,7 @@ def run_engine_arm(args):
         ms = sim.time_steps(args.steps)
     cuda_sync()
     barrier(dist)
-    ms = max_over_ranks(dist, ms)
-    steps_s = args.steps * world / (ms / 1e3)
+    steps_s, ms = replica_rate(dist, world, args.steps, ms)
     launches = sim.launches_per_step * args.steps
     prof = sim.profile_kernels(max(5, min(20, args.steps)))
     nprof = max(5, min(20, args.steps))
