@@ -107,39 +107,60 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
   const cplx<T>* uh = I.uh + (long long)jc * I.KXP + kx0;
   const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
   const T Lx = I.Lx_t, iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
-  auto ld = [&](int l, int z) -> cplx<T> {
-    const int kc = zcomp(I, z);
-    const int ix = kx0 + l;
-    if (kc < 0 || ix >= I.Mx) return mk(T(0), T(0));
-    const cplx<T>* p = uh + (long long)kc * rowstride + l;
-    const T kx = kval(ix, Lx, iLx), ky = kyv, kz = kval(zsig(I, kc), Lz, iLz);
-    switch (code) {
-      case F_UX: return p[0];
-      case F_UY: return p[cs];
-      case F_UZ: return p[2 * cs];
-      case F_RHO: return p[3 * cs];
-      case F_WX: { cplx<T> uy = p[cs], uz = p[2 * cs];   // i (ky uz - kz uy)
-        return mk(-(ky * uz.y - kz * uy.y), ky * uz.x - kz * uy.x); }
-      case F_WY: { cplx<T> ux = p[0], uz = p[2 * cs];    // i (kz ux - kx uz)
-        return mk(-(kz * ux.y - kx * uz.y), kz * ux.x - kx * uz.x); }
-      case F_WZ: { cplx<T> ux = p[0], uy = p[cs];        // i (kx uy - ky ux)
-        return mk(-(kx * uy.y - ky * ux.y), kx * uy.x - ky * ux.x); }
-      case F_SXX: { cplx<T> ux = p[0]; return mk(-kx * ux.y, kx * ux.x); }
-      case F_SYY: { cplx<T> uy = p[cs]; return mk(-ky * uy.y, ky * uy.x); }
-      case F_SXY: { cplx<T> ux = p[0], uy = p[cs];
-        cplx<T> a = mk(kx * uy.x + ky * ux.x, kx * uy.y + ky * ux.y);
-        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
-      case F_SXZ: { cplx<T> ux = p[0], uz = p[2 * cs];
-        cplx<T> a = mk(kx * uz.x + kz * ux.x, kx * uz.y + kz * ux.y);
-        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
-      default: { cplx<T> uy = p[cs], uz = p[2 * cs];     // F_SYZ
-        cplx<T> a = mk(ky * uz.x + kz * uy.x, ky * uz.y + kz * uy.y);
-        return mk(-T(0.5) * a.y, T(0.5) * a.x); }
-    }
+  // The field's prologue is one of three forms, fixed per CTA (so each form gets its own
+  // FFT with a branch-free loader): a copy of a component, a curl component
+  // i (k_b u_c - k_c u_b), or a strain component (i/2)(k_a u_b + k_b u_a).
+  int fam, ca = 0, cb = 0;
+  switch (code) {
+    case F_UX: fam = 0; ca = 0; break;
+    case F_UY: fam = 0; ca = 1; break;
+    case F_UZ: fam = 0; ca = 2; break;
+    case F_RHO: fam = 0; ca = 3; break;
+    case F_WX: fam = 1; ca = 1; cb = 2; break;
+    case F_WY: fam = 1; ca = 2; cb = 0; break;
+    case F_WZ: fam = 1; ca = 0; cb = 1; break;
+    case F_SXX: fam = 2; ca = 0; cb = 0; break;
+    case F_SXY: fam = 2; ca = 0; cb = 1; break;
+    case F_SXZ: fam = 2; ca = 0; cb = 2; break;
+    case F_SYY: fam = 2; ca = 1; cb = 1; break;
+    default: fam = 2; ca = 1; cb = 2; break;   // F_SYZ
+  }
+  const long long oa = ca * cs, ob = cb * cs;
+  // wavenumber of axis d at (kx0 + l, jc, kc)
+  auto kax = [&](int d, int l, int kc) -> T {
+    return d == 0 ? kval(kx0 + l, Lx, iLx) : (d == 1 ? kyv : kval(zsig(I, kc), Lz, iLz));
   };
   cplx<T>* out = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
   auto st = [&](int l, int z, cplx<T> v) { out[(long long)z * rowstride + l] = v; };
-  fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  if (fam == 0) {
+    auto ld = [&](int l, int z) -> cplx<T> {
+      const int kc = zcomp(I, z);
+      if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+      return uh[oa + (long long)kc * rowstride + l];
+    };
+    fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  } else if (fam == 1) {
+    auto ld = [&](int l, int z) -> cplx<T> {   // i (k_b u_c - k_c u_b), (b, c) = (ca, cb)
+      const int kc = zcomp(I, z);
+      if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+      const long long o = (long long)kc * rowstride + l;
+      const cplx<T> ub = uh[oa + o], uc = uh[ob + o];
+      const T kb = kax(ca, l, kc), kc_ = kax(cb, l, kc);
+      return mk(-(kb * uc.y - kc_ * ub.y), kb * uc.x - kc_ * ub.x);
+    };
+    fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  } else {
+    auto ld = [&](int l, int z) -> cplx<T> {   // (i/2)(k_a u_b + k_b u_a), (a, b) = (ca, cb)
+      const int kc = zcomp(I, z);
+      if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+      const long long o = (long long)kc * rowstride + l;
+      const cplx<T> ua = uh[oa + o], ub = uh[ob + o];
+      const T ka = kax(ca, l, kc), kb = kax(cb, l, kc);
+      const cplx<T> q = mk(ka * ub.x + kb * ua.x, ka * ub.y + kb * ua.y);
+      return mk(-T(0.5) * q.y, T(0.5) * q.x);
+    };
+    fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  }
 }
 template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
@@ -671,9 +692,14 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
     const T kx = kval(ix, Lx, iLx), ky = kval(ky_i, Ly, iLy), kz = kval(kz_i, Lz, iLz);
     const T k2 = kx * kx + (ky * ky + kz * kz);
     const bool k0 = (ix == 0) && (ky_i == 0) && (kz_i == 0);
-    cplx<T> rhs[3], u[3];
+    cplx<T> rhs[3], u[3], f1[3], f2[3];
+    // every load of the mode first (history too), so that they are all in flight at once
 #pragma unroll
     for (int c = 0; c < 3; ++c) { rhs[c] = sb[c * cs + g]; u[c] = uh[c * cs + g]; }
+    if (mode == 0) {
+#pragma unroll
+      for (int c = 0; c < 3; ++c) { f1[c] = hA[c * cs + g]; f2[c] = hB[c * cs + g]; }
+    }
     cplx<T> rho = mk(T(0), T(0));
     if (I.density) rho = uh[3 * cs + g];
     if (I.ab3) {   // explicit (hyper)viscosity, models.jl:320-326
@@ -725,11 +751,9 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
     cplx<T> un[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const cplx<T> f1 = hA[c * cs + g];
-      cplx<T> f2 = hB[c * cs + g];
-      if (I.ab3 && stage == 2) f2 = scl(rhs[c] - f1, fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
+      if (I.ab3 && stage == 2) f2[c] = scl(rhs[c] - f1[c], fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
       // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
-      un[c] = scl(rhs[c], A) + (scl(f1, B) + (scl(f2, C) + scl(u[c], E)));
+      un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
       if (band) un[c] = un[c] + scl(u[c], fdt);   // forcing increment (add_forcing!)
     }
     {  // projection after the update (time_step_functions.jl:78)
