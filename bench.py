@@ -229,7 +229,7 @@ def cpu_reference_rate(n: int, budget_s: float, max_steps: int, warmup: int) -> 
 # ---------------------------------------------------------------------------------- serving
 SERVE_SIZES = (32, 48, 64, 96, 128)
 SERVE_RATE = 200.0   # mean Poisson arrivals per second
-SERVE_BATCH_LAUNCHES = 6 * 12   # kernels per batched step: 6 size-class chains of 12 (one CUDA graph)
+SERVE_BATCH_LAUNCHES = 6 * 11   # kernels per batched step: 6 size-class chains of 11 (one CUDA graph)
 
 
 def serving_requests(R: int) -> list[dict]:

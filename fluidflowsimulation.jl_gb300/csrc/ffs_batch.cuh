@@ -109,11 +109,6 @@ template <typename T, int CI = 0>
 __global__ void __launch_bounds__(256) kb_stats(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
   FFS_BATCH_LOOP(BP_STATS)
   b_stats<T>(BI.I, 0, Blk{it.x, 0, 0, it.y});
-  FFS_BATCH_END
-}
-template <typename T, int CI = 0>
-__global__ void __launch_bounds__(256) kb_spectra(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
-  FFS_BATCH_LOOP(BP_STATS)
   b_spectra<T>(BI.I, 0, Blk{it.x, 0, 0, it.y});
   FFS_BATCH_END
 }

@@ -111,7 +111,6 @@ struct BatchClass {
     kb_table<float, CI><<<FFS_CL(BP_TABLE)>>>(B, T);
     kb_fwd_z<float, TX, CI, N><<<FFS_CL(BP_FWD_Z)>>>(B, T);
     kb_stats<float, CI><<<FFS_CL(BP_STATS)>>>(B, T);
-    kb_spectra<float, CI><<<FFS_CL(BP_STATS)>>>(B, T);
     kb_update<float, CI><<<FFS_CL(BP_UPDATE)>>>(B, T);
     kb_finalize<float, CI><<<FFS_CL(BP_FIN)>>>(B, T);
 #undef FFS_CL

@@ -588,10 +588,7 @@ class Engine : public EngineBase {
     zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(zu_lines(), I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
   void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
-  void launch_stats(int mode) {
-    k_stats<T><<<nparts, 256, 0, s>>>(I, mode);
-    k_spectra<T><<<nparts, 256, 0, s>>>(I, mode);
-  }
+  void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
   void launch_fin(int mode) { k_finalize<T><<<1, 1024, 0, s>>>(I, mode, nparts); }
 
   void enqueue_step(int mode) {
@@ -606,7 +603,7 @@ class Engine : public EngineBase {
     launch_update(mode);
     launch_fin(mode);
   }
-  int launches_per_step() const override { return 10 + (use_table() ? 1 : 0); }
+  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0); }
 
   // ---------------------------------------------------------------- fields
   void repack_in(const double* src, double* dst, int layout) const {

@@ -19,7 +19,9 @@
 
 namespace ffsgpu {
 
-template <typename T> struct cplx { T x, y; };
+// aligned to its size, so that one complex moves in one 8-byte (float) or 16-byte (double)
+// load or store instead of two
+template <typename T> struct alignas(2 * sizeof(T)) cplx { T x, y; };
 
 template <typename T> __device__ __forceinline__ cplx<T> mk(T a, T b) { cplx<T> r; r.x = a; r.y = b; return r; }
 template <typename T> __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return mk(a.x + b.x, a.y + b.y); }

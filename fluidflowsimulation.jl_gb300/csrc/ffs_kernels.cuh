@@ -943,10 +943,6 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
     I.partials[(long long)bk.x * QPAD + threadIdx.x] = sum;
   }
 }
-template <typename T>
-__global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
-  b_stats<T>(I, mode, Blk::here());
-}
 
 // ====================================================================================
 // The other write_spec spectra (spec.jl:1-146, 196-422) at spectrum iterations, from
@@ -1045,8 +1041,10 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
     }
   }
 }
+// stats and spectra in one launch: both return at once outside their iterations
 template <typename T>
-__global__ void __launch_bounds__(256) k_spectra(Inst<T> I, int mode) {
+__global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
+  b_stats<T>(I, mode, Blk::here());
   b_spectra<T>(I, mode, Blk::here());
 }
 

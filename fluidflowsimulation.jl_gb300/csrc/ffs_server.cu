@@ -263,7 +263,6 @@ class Server {
         kb_table<float><<<grid[BP_TABLE], block[BP_TABLE], 0, b>>>(d_inst, d_tab);
         kb_fwd_z<float, TXB><<<grid[BP_FWD_Z], block[BP_FWD_Z], smem[BP_FWD_Z], b>>>(d_inst, d_tab);
         kb_stats<float><<<grid[BP_STATS], block[BP_STATS], 0, b>>>(d_inst, d_tab);
-        kb_spectra<float><<<grid[BP_STATS], block[BP_STATS], 0, b>>>(d_inst, d_tab);
         kb_update<float><<<grid[BP_UPDATE], block[BP_UPDATE], 0, b>>>(d_inst, d_tab);
         kb_finalize<float><<<grid[BP_FIN], block[BP_FIN], 0, b>>>(d_inst, d_tab);
       } else {
