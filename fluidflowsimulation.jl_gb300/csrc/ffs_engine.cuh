@@ -79,6 +79,7 @@ class Engine : public EngineBase {
   int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass)
   int xfused_ok = 0;          // n for which the fused x pass is available
   bool use_ct = true;         // compile-time FFT plans in the FP32 y/z passes
+  bool use_ct_z = true;       // compile-time FFT plans in the FP32 forward z pass
   bool zseq = false;          // forward z pass: one component at a time (TX lines)
   std::string tune_report;    // candidates and timings of the autotuner
   int txz = TX;               // kx lines per CTA in the forward z pass
@@ -440,8 +441,8 @@ class Engine : public EngineBase {
     if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
     if (ctzu() == NC) {
-      if (NC <= 256) { if ((rc = smem_attr(k_fwd_z<T, TX, NC>, smem_zu, err))) return rc; }
-      else if (zseq) { if ((rc = smem_attr(k_fwd_z<T, TX, NC, true>, smem_zu, err))) return rc; }
+      if (zseq) { if ((rc = smem_attr(k_fwd_z<T, TX, NC, true>, smem_zu, err))) return rc; }
+      else if (NC <= 256) { if ((rc = smem_attr(k_fwd_z<T, TX, NC>, smem_zu, err))) return rc; }
       else if ((rc = smem_attr(k_fwd_z<T, 2, NC>, smem_zu, err))) return rc;
     }
     return 0;
@@ -499,12 +500,12 @@ class Engine : public EngineBase {
   }
   int cty() const { return txy == TX ? ct_len(I.ny) : 0; }
   int ctz() const { return txy == TX ? ct_len(I.nz) : 0; }
-  // compile-time forward z kernels exist for (TX lines, 3 components) at 128/256,
-  // (2 lines, 3 components) and (TX lines, one component at a time) at 512/1024
+  // compile-time forward z kernels exist for TX lines (3 components together or one at a
+  // time) at 128/256, and for 2 lines (3 together) or TX lines (one at a time) at 512/1024
   int ctzu() const {
-    const int n = ct_len(I.nz);
+    const int n = use_ct_z ? ct_len_raw(I.nz) : 0;
     if (!n) return 0;
-    if (n <= 256) return (txz == TX && !zseq) ? n : 0;
+    if (n <= 256) return txz == TX ? n : 0;
     return ((txz == 2 && !zseq) || (txz == TX && zseq)) ? n : 0;
   }
 
@@ -572,8 +573,14 @@ class Engine : public EngineBase {
     if constexpr (sizeof(T) == 4) {
       const dim3 g(I.KXP / txz, I.NYR);
       switch (ctzu()) {
-        case 128: k_fwd_z<T, TX, 128><<<g, 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode); return;
-        case 256: k_fwd_z<T, TX, 256><<<g, 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode); return;
+        case 128:
+          if (zseq) k_fwd_z<T, TX, 128, true><<<g, TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, TX, 128><<<g, 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode);
+          return;
+        case 256:
+          if (zseq) k_fwd_z<T, TX, 256, true><<<g, TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, TX, 256><<<g, 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode);
+          return;
         case 512:
           if (zseq) k_fwd_z<T, TX, 512, true><<<g, TX * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
           else k_fwd_z<T, 2, 512><<<g, 3 * 2 * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
@@ -899,7 +906,7 @@ class Engine : public EngineBase {
   // Each group is tuned on its own (they are independent passes). The choice is cached
   // per grid, model and precision for the process, so engines of the same shape tune once.
   struct TuneChoice {
-    int txy, use_ct, lyz, xfused, txz, zseq;
+    int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z;
     std::string report;
   };
   static std::mutex& tune_mu() { static std::mutex m; return m; }
@@ -916,6 +923,7 @@ class Engine : public EngineBase {
       if (it != tune_cache().end()) {
         const TuneChoice& c = it->second;
         txy = c.txy; use_ct = c.use_ct; lyz = c.lyz; xfused = c.xfused; txz = c.txz; zseq = c.zseq;
+        use_ct_z = c.use_ct_z;
         tune_report = c.report + " (cached)";
         compute_smem();
         return set_smem(err);
@@ -989,32 +997,34 @@ class Engine : public EngineBase {
     // forward z pass
     if (!rc) {
       float best = 1e30f;
-      int bt = txz, bq = zseq;
+      int bt = txz, bq = zseq, bc = use_ct_z;
       for (int q : {0, 1})
-        for (int t : {TX, TX / 2, TX / 4}) {
-          if (t < 1 || (q ? 1 : 3) * t * I.pz.tpl > MAXT) continue;
-          if (q && t < TX / 2) continue;
-          txz = t; zseq = q;
-          float ms = 0.f;
-          if ((rc = timed([&] { launch_zu(0); }, ms))) break;
-          snprintf(line, sizeof(line), "fwd_z[tx=%d,%s]=%.4fms ", t, q ? "seq" : "3c", ms);
-          rep += line;
-          if (ms < best) { best = ms; bt = t; bq = q; }
-        }
-      txz = bt; zseq = bq;
+        for (int t : {TX, TX / 2, TX / 4})
+          for (int c : {1, 0}) {
+            if (t < 1 || (q ? 1 : 3) * t * I.pz.tpl > MAXT) continue;
+            if (q && t < TX / 2) continue;
+            txz = t; zseq = q; use_ct_z = c;
+            if (c && !ctzu()) continue;   // no compile-time kernel for this shape
+            float ms = 0.f;
+            if ((rc = timed([&] { launch_zu(0); }, ms))) break;
+            snprintf(line, sizeof(line), "fwd_z[tx=%d,%s,%s]=%.4fms ", t, q ? "seq" : "3c", c ? "ct" : "rt", ms);
+            rep += line;
+            if (ms < best) { best = ms; bt = t; bq = q; bc = c; }
+          }
+      txz = bt; zseq = bq; use_ct_z = bc;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
-    snprintf(line, sizeof(line), "-> tx_yz=%d %s, x=%s%d, fwd_z tx=%d %s", txy, use_ct ? "ct" : "rt",
-             xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c");
+    snprintf(line, sizeof(line), "-> tx_yz=%d %s, x=%s%d, fwd_z tx=%d %s %s", txy, use_ct ? "ct" : "rt",
+             xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c", use_ct_z ? "ct" : "rt");
     rep += line;
     tune_report = rep;
     compute_smem();
     if ((rc = set_smem(err))) return rc;
     {
       std::lock_guard<std::mutex> g(tune_mu());
-      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, rep};
+      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, rep};
     }
     return reset_state(err);
   }

@@ -581,10 +581,15 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
     __syncthreads();
   }
   // auxiliary fields one at a time (TX lines each)
-  int nslot[3] = {0, 1, 2};
+  int ns0 = 0, ns1 = 1, ns2 = 2;   // slots of N (scalars: no local-memory array)
   for (int fi = 0; fi < F.n; ++fi) {
     const int role = F.code[fi];
-    if (role <= R_NZ) { nslot[role] = F.slot[fi]; continue; }
+    if (role <= R_NZ) {
+      if (role == R_NX) ns0 = F.slot[fi];
+      else if (role == R_NY) ns1 = F.slot[fi];
+      else ns2 = F.slot[fi];
+      continue;
+    }
     if (role == R_KE && !want_ke) continue;
     const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
     auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
@@ -613,7 +618,8 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
     const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
 #pragma unroll 1
     for (int c = 0; c < 3; ++c) {
-      const cplx<T>* in = I.wz + (long long)nslot[c] * I.wzs + (long long)jc * I.KXP + kx0;
+      const int sl = c == 0 ? ns0 : (c == 1 ? ns1 : ns2);
+      const cplx<T>* in = I.wz + (long long)sl * I.wzs + (long long)jc * I.KXP + kx0;
       auto ld = [&](int l, int z) -> cplx<T> { return in[(long long)z * rowstride + l]; };
       auto st = [&](int l, int z, cplx<T> v) {
         const int kc = zcomp(I, z);
@@ -624,9 +630,9 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
       fft_lines_n<-1, TX, T, N>(I.pz, buf, bufB, TX, I.twz, ld, st);
     }
   } else {   // the three components of N together (3 TX lines), straight to the scratch buffer
-    const cplx<T>* in0 = I.wz + (long long)nslot[0] * I.wzs + (long long)jc * I.KXP + kx0;
-    const cplx<T>* in1 = I.wz + (long long)nslot[1] * I.wzs + (long long)jc * I.KXP + kx0;
-    const cplx<T>* in2 = I.wz + (long long)nslot[2] * I.wzs + (long long)jc * I.KXP + kx0;
+    const cplx<T>* in0 = I.wz + (long long)ns0 * I.wzs + (long long)jc * I.KXP + kx0;
+    const cplx<T>* in1 = I.wz + (long long)ns1 * I.wzs + (long long)jc * I.KXP + kx0;
+    const cplx<T>* in2 = I.wz + (long long)ns2 * I.wzs + (long long)jc * I.KXP + kx0;
     const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
     auto ld = [&](int l, int z) -> cplx<T> {
       const int c = l / TX, x = l % TX;
