@@ -125,7 +125,7 @@ def ncu_traffic(kernel: str, n: int, prec: str) -> float | None:
     return None
 
 
-def survey_bytes(n: int, elem: int) -> dict[str, float]:
+def model_bytes(n: int, elem: int) -> dict[str, float]:
     """Effective-bandwidth byte model of the velocity-only step, per pass.
 
     A = (n/2+1) n^2 complex elements of `elem` bytes (one full half-spectrum component).
@@ -437,7 +437,7 @@ def run_workload(args):
                        "peak": peak, "unit": "GB/s", "peak_source": kind}
     out["roofline"]["frac"] = out["roofline"]["achieved"] / peak
     if ntr == 9:   # velocity-only: the per-pass split of the 69A model
-        sb = survey_bytes(n, elem)
+        sb = model_bytes(n, elem)
         out["roofline"]["per_kernel_frac"] = {k: sb[k] / (prof[k] / nprof / 1e3) / 1e9 / peak
                                               for k in sb if k in prof and prof[k] > 0}
     if prec == "FP32":
@@ -568,7 +568,7 @@ def run_engine_arm(args):
         return 0
     # --- roofline of the dominant kernel
     peak, peak_kind = measured_peaks()
-    sb = survey_bytes(n, 8)
+    sb = model_bytes(n, 8)
     alg = algorithmic_bytes(n, 8)
     top = max(prof, key=prof.get)
     top_ms = prof[top] / nprof

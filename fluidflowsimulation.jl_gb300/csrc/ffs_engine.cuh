@@ -232,9 +232,12 @@ class Engine : public EngineBase {
       while (lio > 1 && (2 * lio * I.px.tpl > MAXT || io_bytes(lio, p.nx) + 1024 > (size_t)maxs)) lio /= 2;
       if (2 * lio * I.px.tpl > MAXT) { err = "nx too large for this precision"; return FFS_EUNSUPPORTED; }
     }
+    // forward z: from nz = 128 on, one component at a time with TX lines (what the
+    // autotuner picks on GB300); below, the three components together
+    zseq = p.nz >= 128;
     txz = TX;
-    while (txz > 1 && 3 * txz * I.pz.tpl > MAXT) txz /= 2;
-    if (3 * txz * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
+    while (txz > 1 && zu_lines() * I.pz.tpl > MAXT) txz /= 2;
+    if (zu_lines() * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
     if (txz < TX / 4) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
 
     set_physics(p);

@@ -3,10 +3,11 @@
     python fluidflowsimulation.jl_gb300/profile_step.py [n] [FP32|FP64] [steps]
 
 Runs the same workload as bench.py (seeded random-phase field, k0 = 4, band forcing,
-AB3 with adaptive dt, stats every 100 steps, autotuned launch shapes) and nothing else,
-so a profiler's launch list is short: the autotuner's timing launches at create, then
-k_phys_fwd_x x2, k_fwd_y, k_fwd_z_store (set_fields), one initialize! step, then `steps`
-steps.
+AB3 with adaptive dt, stats every 100 steps) with the default launch shapes (the
+autotuner's usual picks on GB300; tuning under a profiler would time the candidates
+serialised and cold) and nothing else, so a profiler's launch list is short:
+k_phys_fwd_x x2, k_fwd_y, k_fwd_z_store (set_fields), one initialize! step, then
+`steps` steps.
 """
 import sys
 from pathlib import Path
@@ -24,7 +25,7 @@ def main():
     d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
          "kinematicViscosity": "0.001", "dtStat": "100", "dtSpec": "1000000000", "writeTime": "1000000000",
          "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true", "cfl": "0.5", "dt": "0.001",
-         "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5", "autotune": "true"}
+         "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5"}
     u = pkg.random_spectrum(n, k0=4.0, seed=2001)
     sim = pkg.Simulation.from_global(d, precision=prec)
     sim.set_fields(*u)

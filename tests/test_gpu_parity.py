@@ -73,6 +73,9 @@ FIXED_CASES = {
     "etd-hv-L2": gdict(32, "ETD3rdO", hyperViscosity="true", hyperViscosityCoefficient="1e-5",
                        xDomainSize="2.0", yDomainSize="2.0", zDomainSize="2.0"),
     "ab3-adaptive": gdict(32, adaptive=True),
+    # nz >= 128: the forward z pass runs one component at a time
+    "etd-128-les-density": gdict(128, "ETD3rdO", dt="0.002", lesModel="Smagorinsky", densityStratification="true",
+                                 Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1"),
     "ab3-adaptive-density": gdict(32, adaptive=True, densityStratification="true", Pr="2", densityGradient="1",
                                   zAcceleration="1", referenceDensity="1"),
 }
