@@ -70,6 +70,8 @@ class Engine : public EngineBase {
   Inst<T> I;
   ffs_params P;
   cudaStream_t s = nullptr;
+  cudaStream_t s2 = nullptr;        // side branch of the step (scalar kernel, ETD table)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<void*> allocs;
   int64_t bytes = 0;
   FieldList inv_list{}, fwd_list{};
@@ -96,6 +98,9 @@ class Engine : public EngineBase {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     for (void* p : allocs) cudaFree(p);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (s2) cudaStreamDestroy(s2);
     if (s) cudaStreamDestroy(s);
   }
 
@@ -189,6 +194,9 @@ class Engine : public EngineBase {
     if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
     FFS_CK(cudaSetDevice(p.device));
     FFS_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    FFS_CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+    FFS_CK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    FFS_CK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
 
     I.nx = p.nx; I.ny = p.ny; I.nz = p.nz; I.nxh = p.nx / 2 + 1;
     I.lx = p.lx; I.ly = p.ly; I.lz = p.lz;
@@ -605,10 +613,19 @@ class Engine : public EngineBase {
     launch_inv_z(inv_list);
     launch_inv_y(inv_list);
     launch_x();
-    launch_fwd_y(fwd_list);
+    // dt, the integrator's scalars, the band energy and the ETD table need only the x
+    // pass (max |u|) and the spectral state: a side branch that overlaps the forward y
+    // and z passes, joined before the stats and the update
+    cudaEventRecord(ev_fork, s);
+    cudaStreamWaitEvent(s2, ev_fork, 0);
+    std::swap(s, s2);
     launch_scalar(mode);
     launch_table(mode);
+    std::swap(s, s2);
+    cudaEventRecord(ev_join, s2);
+    launch_fwd_y(fwd_list);
     launch_zu(mode);
+    cudaStreamWaitEvent(s, ev_join, 0);
     launch_stats(mode);
     launch_update(mode);
     launch_fin(mode);
