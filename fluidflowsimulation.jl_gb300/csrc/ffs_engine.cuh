@@ -555,6 +555,13 @@ class Engine : public EngineBase {
     else k_fwd_z_store<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   template <int N> void launch_x_fused() {
+    if constexpr (sizeof(T) == 4) {
+      if (!I.x_pf_dist) {   // CTAs resident at once on the device
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_x_fused<N>, XFused<N>::NT, XFused<N>::smem());
+        I.x_pf_dist = std::max(1, nb) * n_sms;
+      }
+    }
     if constexpr (sizeof(T) == 4)
       k_x_fused<N><<<dim3((unsigned)((long long)I.ny * I.nz / XFused<N>::LYZ)), XFused<N>::NT, XFused<N>::smem(), s>>>(I);
   }
@@ -1083,6 +1090,7 @@ class Engine : public EngineBase {
     if (bi_size != sizeof(BatchInst<T>)) { err = "batch parameter block size mismatch"; return FFS_EINVAL; }
     BatchInst<T>* b = reinterpret_cast<BatchInst<T>*>(bi);
     b->I = I;
+    b->I.x_pf_dist = 0;   // in a batch the CTA order interleaves simulations: no look-ahead
     b->inv = inv_list;
     b->fwd = fwd_list;
     b->nparts = nparts;

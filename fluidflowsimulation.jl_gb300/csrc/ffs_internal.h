@@ -81,6 +81,8 @@ template <typename T> struct Inst {
   const cplx<T>* twy;
   const cplx<T>* twz;
   const cplx<T>* twx_r;     // register-pass twiddles of the fused x pass, [m][i] = tw[i m]
+  int x_pf_dist;            // fused x pass: CTAs resident at once (the CTA that many ahead
+                            // gets its input prefetched into L2); 0: no prefetch
   // resident spectral state, compact [comp][kz'][ky'][KXP]
   cplx<T>* uh;             // 3 velocity comps (+ rho)
   cplx<T>* hist;           // [2][ncomp][...]

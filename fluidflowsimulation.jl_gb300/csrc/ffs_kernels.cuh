@@ -66,6 +66,12 @@ template <typename T> __device__ __forceinline__ void cp_async_elem(cplx<T>* dst
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Bulk prefetch of [p, p + bytes) from global memory into L2 (no registers, no shared
+// memory; p 16-byte aligned, bytes a multiple of 16).
+__device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
+}
+
 // wavenumber i / L: FP64 divides exactly like the reference (KX[i] = i/LX); FP32
 // multiplies by the reciprocal.
 template <typename T> __device__ __forceinline__ T kval(int i, T L, T iL) {

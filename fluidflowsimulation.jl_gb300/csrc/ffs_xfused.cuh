@@ -66,6 +66,16 @@ __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
   auto no_ld = [](int, int) -> cplx<T> { return mk(T(0), T(0)); };
   auto no_st = [](int, int, cplx<T>) {};
 
+  // The CTA x_pf_dist ahead will most likely start when this one retires: bring its six
+  // input slabs (LYZ consecutive lines each, contiguous) into L2 now, so that its pass-0
+  // loads wait on L2 rather than DRAM.
+  if (I.x_pf_dist > 0 && tid < 6) {
+    const long long nb = (long long)bk.x + I.x_pf_dist;
+    const long long ng = (long long)I.ny * I.nz / LYZ;
+    if (nb < ng)
+      prefetch_l2(I.wy + (long long)tid * I.wys + nb * LYZ * KXP, (unsigned)(sizeof(cplx<T>) * LYZ * KXP));
+  }
+
   // ---- inverse pass 0 (radix R, no twiddles): Hermitian extension of the half spectra.
   // Read-only-path loads (each CTA reads its own lines before it writes any of them),
   // unrolled over the pairs so that the loads of the next pair are in flight during the
