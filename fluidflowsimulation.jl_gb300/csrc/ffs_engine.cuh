@@ -529,45 +529,26 @@ class Engine : public EngineBase {
     default: break;                                                  \
   }
 
-  // CTAs of a kernel resident at once (the prefetch distance of the y/z passes)
-  std::map<std::pair<const void*, size_t>, int> res_cache;
-  int resident(const void* k, int block, size_t smem) {
-    auto key = std::make_pair(k, smem);
-    auto it = res_cache.find(key);
-    if (it != res_cache.end()) return it->second;
-    int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) nb = 1;
-    const int v = std::max(1, nb) * n_sms;
-    res_cache[key] = v;
-    return v;
-  }
-  // launch a y/z pass with its look-ahead prefetch distance
-  template <typename... P, typename... A> void go(void (*kern)(Inst<T>, P...), dim3 g, dim3 block, size_t smem, A&&... args) {
-    I.pf_dist = resident((const void*)kern, (int)block.x, smem);
-    kern<<<g, block, smem, s>>>(I, std::forward<A>(args)...);
-    I.pf_dist = 0;
-  }
-
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      FFS_CT_SWITCH(ctz(), (go(k_inv_z<T, TX, NC>, dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, F)))
+      FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
     }
-    if (txy == TX) go(k_inv_z<T, TX>, dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, F);
-    else go(k_inv_z<T, TX / 2>, dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, F);
+    if (txy == TX) k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
+    else k_inv_z<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   void launch_inv_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      FFS_CT_SWITCH(cty(), (go(k_inv_y<T, TX, NC>, dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, F)))
+      FFS_CT_SWITCH(cty(), (k_inv_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
     }
-    if (txy == TX) go(k_inv_y<T, TX>, dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, F);
-    else go(k_inv_y<T, TX / 2>, dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, F);
+    if (txy == TX) k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    else k_inv_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
   void launch_fwd_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      FFS_CT_SWITCH(cty(), (go(k_fwd_y<T, TX, NC>, dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, F)))
+      FFS_CT_SWITCH(cty(), (k_fwd_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
     }
-    if (txy == TX) go(k_fwd_y<T, TX>, dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, F);
-    else go(k_fwd_y<T, TX / 2>, dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, F);
+    if (txy == TX) k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
+    else k_fwd_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
   void launch_fwd_z_store(const FieldList& F) {
     if (txy == TX) k_fwd_z_store<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
@@ -611,25 +592,25 @@ class Engine : public EngineBase {
       const dim3 g(I.KXP / txz, I.NYR);
       switch (ctzu()) {
         case 128:
-          if (zseq) go(k_fwd_z<T, TX, 128, true>, g, TX * ct_tpl<128>(), smem_zu, fwd_list, mode);
-          else go(k_fwd_z<T, TX, 128>, g, 3 * TX * ct_tpl<128>(), smem_zu, fwd_list, mode);
+          if (zseq) k_fwd_z<T, TX, 128, true><<<g, TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, TX, 128><<<g, 3 * TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode);
           return;
         case 256:
-          if (zseq) go(k_fwd_z<T, TX, 256, true>, g, TX * ct_tpl<256>(), smem_zu, fwd_list, mode);
-          else go(k_fwd_z<T, TX, 256>, g, 3 * TX * ct_tpl<256>(), smem_zu, fwd_list, mode);
+          if (zseq) k_fwd_z<T, TX, 256, true><<<g, TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, TX, 256><<<g, 3 * TX * ct_tpl<256>(), smem_zu, s>>>(I, fwd_list, mode);
           return;
         case 512:
-          if (zseq) go(k_fwd_z<T, TX, 512, true>, g, TX * ct_tpl<512>(), smem_zu, fwd_list, mode);
-          else go(k_fwd_z<T, 2, 512>, g, 3 * 2 * ct_tpl<512>(), smem_zu, fwd_list, mode);
+          if (zseq) k_fwd_z<T, TX, 512, true><<<g, TX * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, 2, 512><<<g, 3 * 2 * ct_tpl<512>(), smem_zu, s>>>(I, fwd_list, mode);
           return;
         case 1024:
-          if (zseq) go(k_fwd_z<T, TX, 1024, true>, g, TX * ct_tpl<1024>(), smem_zu, fwd_list, mode);
-          else go(k_fwd_z<T, 2, 1024>, g, 3 * 2 * ct_tpl<1024>(), smem_zu, fwd_list, mode);
+          if (zseq) k_fwd_z<T, TX, 1024, true><<<g, TX * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode);
+          else k_fwd_z<T, 2, 1024><<<g, 3 * 2 * ct_tpl<1024>(), smem_zu, s>>>(I, fwd_list, mode);
           return;
         default: break;
       }
     }
-    go(zu_ptr(), dim3(I.KXP / txz, I.NYR), blk(zu_lines(), I.pz), smem_zu, fwd_list, mode);
+    zu_ptr()<<<dim3(I.KXP / txz, I.NYR), blk(zu_lines(), I.pz), smem_zu, s>>>(I, fwd_list, mode);
   }
   void launch_update(int mode) { k_update<T><<<upd_blocks, 256, 0, s>>>(I, mode); }
   void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
@@ -1110,7 +1091,6 @@ class Engine : public EngineBase {
     BatchInst<T>* b = reinterpret_cast<BatchInst<T>*>(bi);
     b->I = I;
     b->I.x_pf_dist = 0;   // in a batch the CTA order interleaves simulations: no look-ahead
-    b->I.pf_dist = 0;
     b->inv = inv_list;
     b->fwd = fwd_list;
     b->nparts = nparts;

@@ -83,7 +83,6 @@ template <typename T> struct Inst {
   const cplx<T>* twx_r;     // register-pass twiddles of the fused x pass, [m][i] = tw[i m]
   int x_pf_dist;            // fused x pass: CTAs resident at once (the CTA that many ahead
                             // gets its input prefetched into L2); 0: no prefetch
-  int pf_dist;              // the same for the y/z pass being launched (set per launch)
   // resident spectral state, compact [comp][kz'][ky'][KXP]
   cplx<T>* uh;             // 3 velocity comps (+ rho)
   cplx<T>* hist;           // [2][ncomp][...]

@@ -66,27 +66,6 @@ template <typename T> __device__ __forceinline__ void cp_async_elem(cplx<T>* dst
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
-// L2 prefetch of `rows` row segments (each within one 128-byte line) at base + r stride.
-template <typename T>
-__device__ __forceinline__ void prefetch_rows_l2(const cplx<T>* base, long long stride, int rows) {
-  for (int r = threadIdx.x; r < rows; r += blockDim.x)
-    asm volatile("prefetch.global.L2 [%0];\n" ::"l"(base + (long long)r * stride));
-}
-
-// Coordinates of the CTA `dist` positions after this one in launch order (x fastest);
-// false past the end of the grid. With dist = the CTAs resident at once, that CTA will
-// most likely start when this one retires.
-__device__ __forceinline__ bool ahead_block(int dist, int& x, int& y, int& z) {
-  if (dist <= 0) return false;
-  const long long b = blockIdx.x + (long long)gridDim.x * (blockIdx.y + (long long)gridDim.y * blockIdx.z) + dist;
-  if (b >= (long long)gridDim.x * gridDim.y * gridDim.z) return false;
-  x = (int)(b % gridDim.x);
-  const long long r = b / gridDim.x;
-  y = (int)(r % gridDim.y);
-  z = (int)(r / gridDim.y);
-  return true;
-}
-
 // Bulk prefetch of [p, p + bytes) from global memory into L2 (no registers, no shared
 // memory; p 16-byte aligned, bytes a multiple of 16).
 __device__ __forceinline__ void prefetch_l2(const void* p, unsigned bytes) {
@@ -191,10 +170,6 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
 }
 template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
-  int fx, tx, jc;   // the column one resident wave ahead: its spectral rows into L2 (once per column)
-  if (ahead_block(I.pf_dist, fx, tx, jc) && fx == 0)
-    for (int c = 0; c < I.ncomp; ++c)
-      prefetch_rows_l2(I.uh + c * I.cstride + (long long)jc * I.KXP + tx * TX, (long long)I.NYR * I.KXP, I.NZR);
   b_inv_z<T, TX, N>(I, F, Blk::here());
 }
 
@@ -219,9 +194,6 @@ __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, co
 }
 template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_inv_y(Inst<T> I, FieldList F) {
-  int fx, tx, z;   // input rows of the CTA one resident wave ahead into L2
-  if (ahead_block(I.pf_dist, fx, tx, z))
-    prefetch_rows_l2(I.wz + (long long)F.slot[fx] * I.wzs + (long long)z * I.NYR * I.KXP + tx * TX, I.KXP, I.NYR);
   b_inv_y<T, TX, N>(I, F, Blk::here());
 }
 
@@ -250,9 +222,6 @@ __device__ __forceinline__ void b_fwd_y(const Inst<T>& I, const FieldList& F, co
 }
 template <typename T, int TX, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
-  int fx, tx, z;   // input rows of the CTA one resident wave ahead into L2
-  if (ahead_block(I.pf_dist, fx, tx, z))
-    prefetch_rows_l2(I.wy + (long long)F.slot[fx] * I.wys + (long long)z * I.ny * I.KXP + tx * TX, I.KXP, I.ny);
   b_fwd_y<T, TX, N>(I, F, Blk::here());
 }
 
@@ -699,11 +668,6 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
 }
 template <typename T, int TX, int N = 0, bool SEQ = false>
 __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z(Inst<T> I, FieldList F, int mode) {
-  int tx, jc, unused;   // the N rows of the column one resident wave ahead into L2
-  if (ahead_block(I.pf_dist, tx, jc, unused))
-    for (int c = 0; c < 3; ++c)
-      prefetch_rows_l2(I.wz + (long long)F.slot[c] * I.wzs + (long long)jc * I.KXP + tx * TX, (long long)I.NYR * I.KXP,
-                       I.nz);
   b_fwd_z<T, TX, N, SEQ>(I, F, mode, Blk::here());
 }
 
