@@ -310,14 +310,19 @@ class Engine : public EngineBase {
       if (lyzf && ((long long)p.ny * p.nz) % lyzf == 0) {
         xfused = xfused_ok = p.nx;
         const int tpl = p.nx / rf;
+        // register-pass twiddles [m][i] as (c, c, s, s): both lanes of a packed pair
         cplx<T>* t = nullptr;
-        if ((rc = alloc(&t, p.nx, err))) return rc;
-        std::vector<cplx<T>> h(p.nx), base(p.nx);
+        if ((rc = alloc(&t, 2 * (size_t)p.nx, err))) return rc;
+        std::vector<cplx<T>> h(2 * (size_t)p.nx), base(p.nx);
         FFS_CK(cudaMemcpyAsync(base.data(), tw[0], p.nx * sizeof(cplx<T>), cudaMemcpyDeviceToHost, s));
         FFS_CK(cudaStreamSynchronize(s));
         for (int m = 0; m < rf; ++m)
-          for (int i = 0; i < tpl; ++i) h[m * tpl + i] = base[(i * m) % p.nx];
-        FFS_CK(cudaMemcpyAsync(t, h.data(), p.nx * sizeof(cplx<T>), cudaMemcpyHostToDevice, s));
+          for (int i = 0; i < tpl; ++i) {
+            const cplx<T> w = base[(i * m) % p.nx];
+            h[2 * (m * tpl + i)] = cplx<T>{w.x, w.x};
+            h[2 * (m * tpl + i) + 1] = cplx<T>{w.y, w.y};
+          }
+        FFS_CK(cudaMemcpyAsync(t, h.data(), 2 * p.nx * sizeof(cplx<T>), cudaMemcpyHostToDevice, s));
         FFS_CK(cudaStreamSynchronize(s));
         I.twx_r = t;
       }
@@ -1076,7 +1081,7 @@ class Engine : public EngineBase {
     const int64_t cs = (int64_t)zc * yc * KXP, wzs = (int64_t)p.nz * yc * KXP, wys = (int64_t)p.nz * p.ny * KXP;
     const int nin = 6 + (p.les ? 5 : 0) + (p.density ? 1 : 0), nslots = std::max(nin, 4);
     const int ncomp = p.density ? 4 : 3;
-    int64_t t = cb * (2 * (int64_t)(p.nx + p.ny + p.nz));
+    int64_t t = cb * (2 * (int64_t)(2 * p.nx + p.ny + p.nz));   // twiddle tables, packed x table
     t += cb * (3 * ncomp * cs + (int64_t)nslots * (wzs + wys) + ((p.les || p.density) ? 8 : 4) * cs);
     t += 8 * (int64_t)std::min<int64_t>((cs + 4095) / 4096, 8192) * QPAD;
     t += 8 * (int64_t)(p.stats_capacity > 0 ? p.stats_capacity : 256) * 64;   // record columns <= 53

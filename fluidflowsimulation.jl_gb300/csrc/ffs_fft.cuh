@@ -30,6 +30,23 @@ template <typename T> __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cp
   return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 template <typename T> __device__ __forceinline__ cplx<T> scl(cplx<T> a, T s) { return mk(a.x * s, a.y * s); }
+
+// Packed FP32 (sm_100 and later): a float2 is two independent lanes, and cplx<float2>
+// carries two complex numbers (re of both, im of both), so the same DFT code advances two
+// lines with half the FP32 instructions. Each lane rounds exactly as the scalar operation.
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+__device__ __forceinline__ float2 operator*(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 operator-(float2 a) { return __fmul2_rn(a, make_float2(-1.f, -1.f)); }
+
+// a constant in the arithmetic type (both lanes for float2)
+template <typename T> __device__ __forceinline__ T cst(double v) { return T(v); }
+template <> __device__ __forceinline__ float2 cst<float2>(double v) { return make_float2((float)v, (float)v); }
+
+// a * b + c, rounded once
+__device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float2 fma_(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 template <typename T> __device__ __forceinline__ cplx<T> cjg(cplx<T> a) { return mk(a.x, -a.y); }
 // multiply by +i (DIR=+1) or -i (DIR=-1)
 template <int DIR, typename T> __device__ __forceinline__ cplx<T> mul_i(cplx<T> a) {
@@ -83,25 +100,29 @@ template <int DIR, typename T> __device__ __forceinline__ void dft2(cplx<T>& a, 
 }
 
 template <int DIR, typename T> __device__ __forceinline__ void dft4(cplx<T>& x0, cplx<T>& x1, cplx<T>& x2, cplx<T>& x3) {
-  cplx<T> a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, a3 = mul_i<DIR>(x1 - x3);
-  x0 = a0 + a2; x2 = a0 - a2; x1 = a1 + a3; x3 = a1 - a3;
+  cplx<T> a0 = x0 + x2, a1 = x0 - x2, a2 = x1 + x3, d = x1 - x3;
+  x0 = a0 + a2; x2 = a0 - a2;
+  // x1 = a1 + (DIR i) d, x3 = a1 - (DIR i) d, with the rotation folded into the adds
+  if (DIR > 0) { x1 = mk(a1.x - d.y, a1.y + d.x); x3 = mk(a1.x + d.y, a1.y - d.x); }
+  else { x1 = mk(a1.x + d.y, a1.y - d.x); x3 = mk(a1.x - d.y, a1.y + d.x); }
 }
 
 template <int DIR, typename T> __device__ __forceinline__ void dft3(cplx<T>& x0, cplx<T>& x1, cplx<T>& x2) {
-  const T h = T(0.5), s = T(FFS_R3);
+  const T nh = cst<T>(-0.5), s = cst<T>(FFS_R3), ns = cst<T>(-FFS_R3);
   cplx<T> t1 = x1 + x2, t2 = x1 - x2;
-  cplx<T> c = mk(x0.x - h * t1.x, x0.y - h * t1.y);
-  cplx<T> d = scl(mul_i<DIR>(t2), s);
+  cplx<T> c = mk(fma_(nh, t1.x, x0.x), fma_(nh, t1.y, x0.y));
+  // d = (DIR i) sqrt(3)/2 t2
+  cplx<T> d = DIR > 0 ? mk(t2.y * ns, t2.x * s) : mk(t2.y * s, t2.x * ns);
   x0 = x0 + t1; x1 = c + d; x2 = c - d;
 }
 
 // multiply by exp(DIR * 2 pi i t / 8), t = 1,2,3
 template <int DIR, int t, typename T> __device__ __forceinline__ cplx<T> w8(cplx<T> a) {
-  const T r = T(FFS_R2);
+  const T r = cst<T>(FFS_R2), nr = cst<T>(-FFS_R2);
   if (t == 1) return DIR > 0 ? mk(r * (a.x - a.y), r * (a.x + a.y)) : mk(r * (a.x + a.y), r * (a.y - a.x));
   if (t == 2) return mul_i<DIR>(a);
   // t == 3: exp(DIR 3 pi i/4) = (-r, DIR r)
-  return DIR > 0 ? mk(-r * (a.x + a.y), r * (a.x - a.y)) : mk(r * (a.y - a.x), -r * (a.x + a.y));
+  return DIR > 0 ? mk(nr * (a.x + a.y), r * (a.x - a.y)) : mk(r * (a.y - a.x), nr * (a.x + a.y));
 }
 
 template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T>* x) {
@@ -117,18 +138,17 @@ template <int DIR, typename T> __device__ __forceinline__ void dft8(cplx<T>* x) 
 
 // multiply by exp(DIR * 2 pi i t / 16) for t in {1,2,3,4,6,9}
 template <int DIR, int t, typename T> __device__ __forceinline__ cplx<T> w16(cplx<T> a) {
-  const T c = T(FFS_C8), s = T(FFS_S8);
-  if (t == 0) return a;
-  if (t == 2) return w8<DIR, 1>(a);
-  if (t == 4) return mul_i<DIR>(a);
-  if (t == 6) return w8<DIR, 3>(a);
-  // general: (cos th, DIR sin th) * a
-  T cr, si;
-  if (t == 1) { cr = c; si = s; }
-  else if (t == 3) { cr = s; si = c; }
-  else { cr = -c; si = -s; }  // t == 9: cos(9pi/8) = -cos(pi/8), sin(9pi/8) = -sin(pi/8)
-  si = DIR > 0 ? si : -si;
-  return mk(a.x * cr - a.y * si, a.x * si + a.y * cr);
+  if constexpr (t == 0) return a;
+  else if constexpr (t == 2) return w8<DIR, 1>(a);
+  else if constexpr (t == 4) return mul_i<DIR>(a);
+  else if constexpr (t == 6) return w8<DIR, 3>(a);
+  else {
+    // general: (cos th, DIR sin th) * a; t == 9: cos(9pi/8) = -cos(pi/8), sin(9pi/8) = -sin(pi/8)
+    constexpr double cr = t == 1 ? FFS_C8 : t == 3 ? FFS_S8 : -FFS_C8;
+    constexpr double s0 = t == 1 ? FFS_S8 : t == 3 ? FFS_C8 : -FFS_S8;
+    constexpr double si = DIR > 0 ? s0 : -s0;
+    return mk(fma_(a.x, cst<T>(cr), a.y * cst<T>(-si)), fma_(a.x, cst<T>(si), a.y * cst<T>(cr)));
+  }
 }
 
 template <int DIR, typename T> __device__ __forceinline__ void dft16(cplx<T>* x) {
@@ -154,11 +174,11 @@ template <int DIR, typename T> __device__ __forceinline__ void dft16(cplx<T>* x)
 }
 
 template <int R, int DIR, typename T> __device__ __forceinline__ void dftR(cplx<T>* x) {
-  if (R == 2) dft2<DIR>(x[0], x[1]);
-  else if (R == 3) dft3<DIR>(x[0], x[1], x[2]);
-  else if (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
-  else if (R == 8) dft8<DIR>(x);
-  else if (R == 16) dft16<DIR>(x);
+  if constexpr (R == 2) dft2<DIR>(x[0], x[1]);
+  else if constexpr (R == 3) dft3<DIR>(x[0], x[1], x[2]);
+  else if constexpr (R == 4) dft4<DIR>(x[0], x[1], x[2], x[3]);
+  else if constexpr (R == 8) dft8<DIR>(x);
+  else if constexpr (R == 16) dft16<DIR>(x);
 }
 
 // ---------------------------------------------------------------------------------

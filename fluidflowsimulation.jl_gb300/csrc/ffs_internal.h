@@ -80,7 +80,7 @@ template <typename T> struct Inst {
   const cplx<T>* twx;
   const cplx<T>* twy;
   const cplx<T>* twz;
-  const cplx<T>* twx_r;     // register-pass twiddles of the fused x pass, [m][i] = tw[i m]
+  const cplx<T>* twx_r;     // register-pass twiddles of the fused x pass, [m][i] = (c, c, s, s) of tw[i m]
   int x_pf_dist;            // fused x pass: CTAs resident at once (the CTA that many ahead
                             // gets its input prefetched into L2); 0: no prefetch
   // resident spectral state, compact [comp][kz'][ky'][KXP]

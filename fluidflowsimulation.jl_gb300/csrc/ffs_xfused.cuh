@@ -13,10 +13,15 @@
 //   [-> middle pass -> smem] -> last forward pass (in place) -> Hermitian unpack -> global
 //
 // Six real input fields ride as three complex lines (ux+i uy, uz+i wx, wy+i wz) and four
-// outputs as two (Nx+i Ny, Nz+i ke). Shared lines are stored line-fastest with an odd
-// line stride and a padding row every 16, which keeps the radix-R strided accesses of
-// the register passes free of bank conflicts.
+// outputs as two (Nx+i Ny, Nz+i ke). The first two input lines and both output lines are
+// transformed as pairs on the packed FP32 pipe (cplx<float2>: one instruction advances
+// both lines); the third input line runs alone. Pairs live in shared memory as one
+// 16-byte element per position (the "pair plane", XOR-swizzled so that the strided
+// accesses of the register passes are free of bank conflicts), the third line in a plane
+// of 8-byte elements with an odd line stride and a padding row every 16.
 #pragma once
+#include <type_traits>
+
 #include "ffs_kernels.cuh"
 
 namespace ffsgpu {
@@ -34,25 +39,97 @@ template <> struct XFusedCfg<1024> { static constexpr int R = 8, R2 = 16, LYZ = 
 
 template <int N> struct XFused {
   static constexpr int R = XFusedCfg<N>::R, R2 = XFusedCfg<N>::R2, LYZ = XFusedCfg<N>::LYZ;
+  static constexpr int LOG2R = R == 16 ? 4 : 3;
   static constexpr int TPL = N / R;        // threads per (y,z) line
   static constexpr int NT = LYZ * TPL;     // threads per CTA
-  static constexpr int NL = 3 * LYZ;       // complex lines per CTA
-  static constexpr int LS = NL + 1;        // odd line stride
   static constexpr int NBUF = R2 > 1 ? 2 : 1;
-  static size_t smem() { return sizeof(cplx<float>) * (size_t)NBUF * srows(N) * LS; }
+  static constexpr int PE = N * LYZ;                   // 16-byte elements of one pair plane
+  static constexpr int QLS = LYZ == 1 ? 1 : LYZ + 1;   // odd line stride of a single plane
+  static constexpr int QE = (N + (N >> 4) + 1) * QLS;  // 8-byte elements of one single plane
+  static size_t smem() { return (size_t)NBUF * (16 * (size_t)PE + 8 * (size_t)QE); }
+
+  // Pair-plane position of element j of line q. Rows of 128 bytes (8 elements: the LYZ
+  // lines of 1, 2 or 4 consecutive j) with the column XOR-ed by a function of the row, so
+  // that each quarter warp (the unit of a 16-byte shared access) touches 8 distinct bank
+  // groups both for 8 consecutive j (register passes, middle passes, unpack) and for j
+  // stepping by R (the stores of pass 0).
+  static __device__ __forceinline__ int pix(int j, int q) {
+    if constexpr (LYZ == 8) {
+      return j * 8 + (q ^ ((j ^ (j >> LOG2R)) & 7));
+    } else if constexpr (LYZ == 2) {
+      const int s = j >> 2, w = ((j & 3) << 1) | q;
+      return s * 8 + (w ^ (((s >> 1) ^ (s & 1)) & 7));
+    } else {
+      const int s = j >> 3;
+      return s * 8 + ((j & 7) ^ (s & 7));
+    }
+  }
 };
 
-// twiddle table of the register passes, [m][i] = exp(-2 pi i * i m / n), m < R, i < n/R
-// (lanes i read consecutive entries)
+// v * w (DIR < 0) or v * conj(w) (DIR > 0) for both lanes of v, with w = (c, s) given as
+// C = (c, c), S = (s, s)
+template <int DIR>
+__device__ __forceinline__ cplx<float2> twmul2(cplx<float2> v, float2 C, float2 S) {
+  const float2 NS = -S;
+  const float2 P = v.x * C, Q = v.y * C;
+  if (DIR < 0) return mk(fma_(v.y, NS, P), fma_(v.x, S, Q));
+  return mk(fma_(v.y, S, P), fma_(v.x, NS, Q));
+}
+template <int DIR>
+__device__ __forceinline__ cplx<float> twmul1(cplx<float> v, float c, float s) {
+  if (DIR < 0) return mk(fmaf(v.y, -s, v.x * c), fmaf(v.x, s, v.y * c));
+  return mk(fmaf(v.y, s, v.x * c), fmaf(v.x, -s, v.y * c));
+}
+
+// One Stockham middle pass (radix R2, sub-transform length p = R entering, T_ = n/R2
+// butterflies per line) over the LYZ lines of a pair plane or, with PAIR false, of a
+// single plane. tw: exp(-2 pi i t / n).
+template <int N, bool PAIR, int DIR>
+__device__ __forceinline__ void xf_mid_pass(const void* in_, void* out_, const cplx<float>* __restrict__ tw) {
+  using C = XFused<N>;
+  constexpr int R = C::R, R2 = C::R2, LYZ = C::LYZ, T_ = N / R2, p = R, tws = N / (R * R2);
+  using V = typename std::conditional<PAIR, cplx<float2>, cplx<float>>::type;
+  const V* in = reinterpret_cast<const V*>(in_);
+  V* out = reinterpret_cast<V*>(out_);
+  auto at = [](int j, int l) { return PAIR ? C::pix(j, l) : sidx(j, l, C::QLS); };
+#pragma unroll 1
+  for (int b = threadIdx.x; b < LYZ * T_; b += C::NT) {
+    const int l = b % LYZ, i = b / LYZ;
+    const int k = i & (p - 1);
+    V x[R2];
+#pragma unroll
+    for (int m = 0; m < R2; ++m) x[m] = in[at(i + m * T_, l)];
+    if (k != 0) {
+#pragma unroll
+      for (int m = 1; m < R2; ++m) {
+        const cplx<float> w = tw[k * m * tws];
+        if constexpr (PAIR) x[m] = twmul2<DIR>(x[m], make_float2(w.x, w.x), make_float2(w.y, w.y));
+        else x[m] = twmul1<DIR>(x[m], w.x, w.y);
+      }
+    }
+    dftR<R2, DIR>(x);
+    const int j = (i - k) * R2 + k;
+#pragma unroll
+    for (int m = 0; m < R2; ++m) out[at(j + m * p, l)] = x[m];
+  }
+}
+
+// Register-pass twiddles, [m][i] = (c, c, s, s) with exp(-2 pi i * i m / n) = (c, s),
+// m < R, i < n/R (lanes i read consecutive entries)
 
 template <int N>
 __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
   using T = float;
   using C = XFused<N>;
-  constexpr int R = C::R, R2 = C::R2, LYZ = C::LYZ, TPL = C::TPL, NL = C::NL, LS = C::LS;
+  constexpr int R = C::R, R2 = C::R2, LYZ = C::LYZ, TPL = C::TPL, QLS = C::QLS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
-  cplx<T>* s1 = s0 + (R2 > 1 ? srows(N) * LS : 0);
+  // [pair plane 0][pair plane 1][single plane 0][single plane 1] (second of each when R2 > 1)
+  cplx<float2>* P0 = reinterpret_cast<cplx<float2>*>(smem_raw);
+  cplx<float2>* P1 = P0 + (R2 > 1 ? C::PE : 0);
+  cplx<T>* Q0 = reinterpret_cast<cplx<T>*>(P0 + C::NBUF * C::PE);
+  cplx<T>* Q1 = Q0 + (R2 > 1 ? C::QE : 0);
+  cplx<float2>* Pl = R2 > 1 ? P1 : P0;   // planes the last radix passes read
+  cplx<T>* Ql = R2 > 1 ? Q1 : Q0;
   __shared__ T red[64];
 
   const int tid = threadIdx.x;
@@ -61,10 +138,7 @@ __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
   const int Mx = I.Mx, KXP = I.KXP;
   const long long it = I.st->iteration;
   const bool want_ke = ((it % I.dt_stat) == 0) || ((it % I.dt_spec) == 0);
-  const cplx<T>* __restrict__ tw = I.twx;
-  const cplx<T>* __restrict__ twr = I.twx_r;
-  auto no_ld = [](int, int) -> cplx<T> { return mk(T(0), T(0)); };
-  auto no_st = [](int, int, cplx<T>) {};
+  const cplx<float2>* __restrict__ twr = reinterpret_cast<const cplx<float2>*>(I.twx_r);
 
   // The CTA x_pf_dist ahead will most likely start when this one retires: bring its six
   // input slabs (LYZ consecutive lines each, contiguous) into L2 now, so that its pass-0
@@ -77,125 +151,136 @@ __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
   }
 
   // ---- inverse pass 0 (radix R, no twiddles): Hermitian extension of the half spectra.
-  // Read-only-path loads (each CTA reads its own lines before it writes any of them),
-  // unrolled over the pairs so that the loads of the next pair are in flight during the
-  // DFT of the current one.
+  // Read-only-path loads (each CTA reads its own lines before it writes any of them).
+  {
+    const cplx<T>* F0 = I.wy + g * KXP;
+    const long long fs = I.wys;
+    cplx<float2> x[R];
 #pragma unroll
-  for (int p = 0; p < 3; ++p) {
-    const cplx<T>* A = I.wy + (long long)(2 * p) * I.wys + g * KXP;
-    const cplx<T>* B = I.wy + (long long)(2 * p + 1) * I.wys + g * KXP;
+    for (int m = 0; m < R; ++m) {
+      const int j = i + m * TPL;
+      const bool cj = 2 * j > N;
+      const int k = cj ? N - j : j;
+      cplx<T> a0 = mk(T(0), T(0)), b0 = a0, a1 = a0, b1 = a0;
+      if (k < Mx) { a0 = ldg_c(F0 + k); b0 = ldg_c(F0 + fs + k); a1 = ldg_c(F0 + 2 * fs + k); b1 = ldg_c(F0 + 3 * fs + k); }
+      if (k == 0 || 2 * k == N) { a0.y = T(0); b0.y = T(0); a1.y = T(0); b1.y = T(0); }   // c2r ignores Im there
+      if (cj) { a0.y = -a0.y; b0.y = -b0.y; a1.y = -a1.y; b1.y = -b1.y; }
+      x[m] = mk(make_float2(a0.x - b0.y, a1.x - b1.y), make_float2(a0.y + b0.x, a1.y + b1.x));
+    }
+    dftR<R, +1>(x);
+#pragma unroll
+    for (int m = 0; m < R; ++m) P0[C::pix(i * R + m, q)] = x[m];
+  }
+  {
+    const cplx<T>* A = I.wy + 4 * I.wys + g * KXP;
+    const cplx<T>* B = A + I.wys;
     cplx<T> x[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) {
       const int j = i + m * TPL;
       const bool cj = 2 * j > N;
       const int k = cj ? N - j : j;
-      cplx<T> a = mk(T(0), T(0)), b = mk(T(0), T(0));
+      cplx<T> a = mk(T(0), T(0)), b = a;
       if (k < Mx) { a = ldg_c(A + k); b = ldg_c(B + k); }
-      if (k == 0 || 2 * k == N) { a.y = T(0); b.y = T(0); }   // c2r ignores Im at kx = 0 and n/2
+      if (k == 0 || 2 * k == N) { a.y = T(0); b.y = T(0); }
       if (cj) { a.y = -a.y; b.y = -b.y; }
       x[m] = mk(a.x - b.y, a.y + b.x);
     }
     dftR<R, +1>(x);
-    const int l = p * LYZ + q;
 #pragma unroll
-    for (int m = 0; m < R; ++m) s0[sidx(i * R + m, l, LS)] = x[m];
+    for (int m = 0; m < R; ++m) Q0[sidx(i * R + m, q, QLS)] = x[m];
   }
   __syncthreads();
-  if (R2 > 1) {   // middle radix pass, p = R
-    fft_pass<R2, +1, NL, T>(N / R2, R, N / (R * R2), false, false, s0, s1, LS, tw, no_ld, no_st);
+  if constexpr (R2 > 1) {
+    xf_mid_pass<N, true, +1>(P0, P1, I.twx);
+    xf_mid_pass<N, false, +1>(Q0, Q1, I.twx);
     __syncthreads();
   }
-  cplx<T>* sl = R2 > 1 ? s1 : s0;   // buffer of the last radix pass
 
-  // ---- last inverse pass in registers: fields (2p, 2p+1) at j = i + m TPL
+  // ---- last inverse pass in registers: fields 0..5 at j = i + m TPL
   T f[6][R];
+  {
+    cplx<float2> x[R];
 #pragma unroll
-  for (int p = 0; p < 3; ++p) {
-    const int l = p * LYZ + q;
-    cplx<T> x[R];
+    for (int m = 0; m < R; ++m) x[m] = Pl[C::pix(i + m * TPL, q)];
 #pragma unroll
-    for (int m = 0; m < R; ++m) x[m] = sl[sidx(i + m * TPL, l, LS)];
-#pragma unroll
-    for (int m = 1; m < R; ++m) x[m] = x[m] * cjg(twr[m * TPL + i]);
+    for (int m = 1; m < R; ++m) { const cplx<float2> w = twr[m * TPL + i]; x[m] = twmul2<+1>(x[m], w.x, w.y); }
     dftR<R, +1>(x);
 #pragma unroll
-    for (int m = 0; m < R; ++m) { f[2 * p][m] = x[m].x; f[2 * p + 1][m] = x[m].y; }
+    for (int m = 0; m < R; ++m) { f[0][m] = x[m].x.x; f[1][m] = x[m].y.x; f[2][m] = x[m].x.y; f[3][m] = x[m].y.y; }
+  }
+  {
+    cplx<T> x[R];
+#pragma unroll
+    for (int m = 0; m < R; ++m) x[m] = Ql[sidx(i + m * TPL, q, QLS)];
+#pragma unroll
+    for (int m = 1; m < R; ++m) { const cplx<float2> w = twr[m * TPL + i]; x[m] = twmul1<+1>(x[m], w.x.x, w.y.x); }
+    dftR<R, +1>(x);
+#pragma unroll
+    for (int m = 0; m < R; ++m) { f[4][m] = x[m].x; f[5][m] = x[m].y; }
   }
 
-  // ---- physical-space products (models.jl:224, 260) and max |u_i| (utils.jl:247-258)
+  // ---- physical-space products (models.jl:224, 260) and max |u_i| (utils.jl:247-258),
+  // packed as the forward pair (Nx + i Ny, Nz + i ke)
   T umax = T(0);
+  cplx<float2> y[R];
 #pragma unroll
   for (int m = 0; m < R; ++m) {
     const T ux = f[0][m], uy = f[1][m], uz = f[2][m], wx = f[3][m], wy = f[4][m], wz = f[5][m];
     umax = fmaxf(umax, fmaxf(fabsf(ux), fmaxf(fabsf(uy), fabsf(uz))));
-    f[0][m] = uy * wz - uz * wy;
-    f[1][m] = uz * wx - ux * wz;
-    f[2][m] = ux * wy - uy * wx;
-    f[3][m] = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);
+    const T nx = uy * wz - uz * wy, ny = uz * wx - ux * wz, nz = ux * wy - uy * wx;
+    const T ke = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);
+    y[m] = mk(make_float2(nx, nz), make_float2(ny, ke));
   }
 
   // ---- forward pass 0 in registers (radix R, no twiddles)
-  cplx<T> y[2][R];
+  dftR<R, -1>(y);
+  if (R2 == 1) __syncthreads();   // P0 is the plane the register pass just read
 #pragma unroll
-  for (int r = 0; r < 2; ++r) {
-#pragma unroll
-    for (int m = 0; m < R; ++m) y[r][m] = mk(f[2 * r][m], f[2 * r + 1][m]);
-    dftR<R, -1>(y[r]);
-  }
-  cplx<T>* sf = s0;   // s0 is free when a middle pass exists; otherwise wait for all reads
-  if (R2 == 1) __syncthreads();
-#pragma unroll
-  for (int r = 0; r < 2; ++r) {
-    const int l = r * LYZ + q;
-#pragma unroll
-    for (int m = 0; m < R; ++m) sf[sidx(i * R + m, l, LS)] = y[r][m];
-  }
+  for (int m = 0; m < R; ++m) P0[C::pix(i * R + m, q)] = y[m];
   if (I.adaptive) block_max_to_state<T, false>(I, umax, T(0), red);   // contains a __syncthreads
   else __syncthreads();
-  if (R2 > 1) {
-    fft_pass<R2, -1, 2 * LYZ, T>(N / R2, R, N / (R * R2), false, false, s0, s1, LS, tw, no_ld, no_st);
+  if constexpr (R2 > 1) {
+    xf_mid_pass<N, true, -1>(P0, P1, I.twx);
     __syncthreads();
   }
 
   // ---- last forward pass (each thread rewrites the positions it read)
-#pragma unroll 1
-  for (int r = 0; r < 2; ++r) {
-    const int l = r * LYZ + q;
-    cplx<T> x[R];
+  {
+    cplx<float2> x[R];
 #pragma unroll
-    for (int m = 0; m < R; ++m) x[m] = sl[sidx(i + m * TPL, l, LS)];
+    for (int m = 0; m < R; ++m) x[m] = Pl[C::pix(i + m * TPL, q)];
 #pragma unroll
-    for (int m = 1; m < R; ++m) x[m] = x[m] * twr[m * TPL + i];
+    for (int m = 1; m < R; ++m) { const cplx<float2> w = twr[m * TPL + i]; x[m] = twmul2<-1>(x[m], w.x, w.y); }
     dftR<R, -1>(x);
 #pragma unroll
-    for (int m = 0; m < R; ++m) sl[sidx(i + m * TPL, l, LS)] = x[m];
+    for (int m = 0; m < R; ++m) Pl[C::pix(i + m * TPL, q)] = x[m];
   }
   __syncthreads();
 
-  // ---- unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 and store kx < KXP
+  // ---- unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 of both lines of
+  // the pair and store kx < KXP; thread (q, i) writes k = i, i + TPL, ... of line q
   {
-    const int wv = tid >> 5, lane = tid & 31;
-    constexpr int NW = C::NT / 32;
+    const long long row = g * KXP;
+    cplx<T>* d0 = I.wy + (long long)I.out_slot[0] * I.wys + row;
+    cplx<T>* d1 = I.wy + (long long)I.out_slot[1] * I.wys + row;
+    cplx<T>* d2 = I.wy + (long long)I.out_slot[2] * I.wys + row;
+    cplx<T>* d3 = I.wy + (long long)I.out_slot[3] * I.wys + row;
 #pragma unroll 1
-    for (int l = wv; l < 2 * LYZ; l += NW) {   // l = r LYZ + q' carries outputs (2r, 2r+1)
-      const int r = l / LYZ, qq = l % LYZ;
-      const int oa = 2 * r, ob = 2 * r + 1;
-      const bool wb = ob != 3 || want_ke;   // output 3 (kinetic energy) only at stats iterations
-      const long long row = ((long long)bk.x * LYZ + qq) * KXP;
-      cplx<T>* da = I.wy + (long long)I.out_slot[oa] * I.wys + row;
-      cplx<T>* db = I.wy + (long long)I.out_slot[ob] * I.wys + row;
-      for (int k = lane; k < KXP; k += 32) {
-        cplx<T> a = mk(T(0), T(0)), b = mk(T(0), T(0));
-        if (k < Mx) {
-          const cplx<T> zk = sl[sidx(k, l, LS)];
-          const cplx<T> zm = sl[sidx(k == 0 ? 0 : N - k, l, LS)];
-          a = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
-          b = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
-        }
-        da[k] = a;
-        if (wb) db[k] = b;
+    for (int k = i; k < KXP; k += TPL) {
+      cplx<T> a0 = mk(T(0), T(0)), b0 = a0, a1 = a0, b1 = a0;
+      if (k < Mx) {
+        const cplx<float2> zk = Pl[C::pix(k, q)];
+        const cplx<float2> zm = Pl[C::pix(k == 0 ? 0 : N - k, q)];
+        a0 = mk(T(0.5) * (zk.x.x + zm.x.x), T(0.5) * (zk.y.x - zm.y.x));
+        b0 = mk(T(0.5) * (zk.y.x + zm.y.x), T(-0.5) * (zk.x.x - zm.x.x));
+        a1 = mk(T(0.5) * (zk.x.y + zm.x.y), T(0.5) * (zk.y.y - zm.y.y));
+        b1 = mk(T(0.5) * (zk.y.y + zm.y.y), T(-0.5) * (zk.x.y - zm.x.y));
       }
+      d0[k] = a0;
+      d1[k] = b0;
+      d2[k] = a1;
+      if (want_ke) d3[k] = b1;   // output 3 (kinetic energy) only at stats iterations
     }
   }
 }
