@@ -13,6 +13,7 @@
 
 #include "ffs_engine.h"
 #include "ffs_kernels.cuh"
+#include "ffs_pairs.cuh"
 #include "ffs_xfused.cuh"
 #include "ffs_batch.cuh"
 
@@ -82,6 +83,10 @@ class Engine : public EngineBase {
   int xfused_ok = 0;          // n for which the fused x pass is available
   bool use_ct = true;         // compile-time FFT plans in the FP32 y/z passes
   bool use_ct_z = true;       // compile-time FFT plans in the FP32 forward z pass
+  // form of each compile-time y/z pass: 0 one line per thread, 1 line pairs on the packed
+  // FP32 pipe
+  int v_iz = 0, v_iy = 0, v_fy = 1;
+  bool pair_z = true;         // compile-time one-component forward z pass on line pairs
   bool zseq = false;          // forward z pass: one component at a time (TX lines)
   std::string tune_report;    // candidates and timings of the autotuner
   int txz = TX;               // kx lines per CTA in the forward z pass
@@ -243,6 +248,12 @@ class Engine : public EngineBase {
     // forward z: from nz = 128 on, one component at a time with TX lines (what the
     // autotuner picks on GB300); below, the three components together
     zseq = p.nz >= 128;
+    // default forms of the compile-time y/z passes (the autotuner's picks at 256^3);
+    // kernel_variant 2 / 3: every one in its line-pair / one-line-per-thread form
+    v_iz = 0; v_iy = 0; v_fy = 1;
+    pair_z = p.kernel_variant != 3;
+    if (p.kernel_variant == 2) v_iz = v_iy = v_fy = 1;
+    if (p.kernel_variant == 3) v_iz = v_iy = v_fy = 0;
     txz = TX;
     while (txz > 1 && zu_lines() * I.pz.tpl > MAXT) txz /= 2;
     if (zu_lines() * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
@@ -298,7 +309,7 @@ class Engine : public EngineBase {
     }
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
     xfused = 0;
-    if (sizeof(T) == 4 && !I.les && !I.density && p.kernel_variant == 0) {
+    if (sizeof(T) == 4 && !I.les && !I.density && p.kernel_variant != 1) {
       int lyzf = 0, rf = 0;
       switch (p.nx) {
         case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
@@ -453,6 +464,13 @@ class Engine : public EngineBase {
   // shared-memory limits of the compile-time-length kernels this engine launches
   template <int NC> int ct_attrs(std::string& err) {
     int rc;
+    if constexpr (sizeof(T) == 4) {
+      constexpr size_t ps = pair_smem<NC, PAIR_LP>();
+      if (v_iz == 1 && ctz() == NC && (rc = smem_attr(k_inv_z2<NC, PAIR_LP>, ps, err))) return rc;
+      if (v_iy == 1 && cty() == NC && (rc = smem_attr(k_inv_y2<NC, PAIR_LP>, ps, err))) return rc;
+      if (v_fy == 1 && cty() == NC && (rc = smem_attr(k_fwd_y2<NC, PAIR_LP>, ps, err))) return rc;
+      if (zpair() && ctzu() == NC && (rc = smem_attr(k_fwd_z2<NC, PAIR_LP>, ps, err))) return rc;
+    }
     if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
@@ -512,9 +530,10 @@ class Engine : public EngineBase {
 
   // compile-time FFT lengths of the FP32 y/z passes (0: runtime plan)
   int ct_len(int n) const {
-    return (sizeof(T) == 4 && P.kernel_variant == 0 && use_ct && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
+    return (sizeof(T) == 4 && P.kernel_variant != 1 && use_ct && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
   }
   int cty() const { return txy == TX ? ct_len(I.ny) : 0; }
+  static const char* vname_of(int v) { return v == 1 ? "pair" : "1"; }
   int ctz() const { return txy == TX ? ct_len(I.nz) : 0; }
   // compile-time forward z kernels exist for TX lines (3 components together or one at a
   // time) at 128/256, and for 2 lines (3 together) or TX lines (one at a time) at 512/1024
@@ -534,8 +553,14 @@ class Engine : public EngineBase {
     default: break;                                                  \
   }
 
+  // the paired one-component forward z pass applies (velocity-only, TX lines, ct plan)
+  bool zpair() const { return sizeof(T) == 4 && pair_z && zseq && txz == TX && !I.les && !I.density; }
+
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
+      if (v_iz == 1)
+        FFS_CT_SWITCH(ctz(), (k_inv_z2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.NYR), PAIR_LP * ct_tpl<NC>(),
+                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
       FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
     }
     if (txy == TX) k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
@@ -543,6 +568,9 @@ class Engine : public EngineBase {
   }
   void launch_inv_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
+      if (v_iy == 1)
+        FFS_CT_SWITCH(cty(), (k_inv_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
+                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
       FFS_CT_SWITCH(cty(), (k_inv_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
     }
     if (txy == TX) k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
@@ -550,6 +578,9 @@ class Engine : public EngineBase {
   }
   void launch_fwd_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
+      if (v_fy == 1)
+        FFS_CT_SWITCH(cty(), (k_fwd_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
+                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
       FFS_CT_SWITCH(cty(), (k_fwd_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
     }
     if (txy == TX) k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
@@ -595,6 +626,9 @@ class Engine : public EngineBase {
   void launch_zu(int mode) {
     if constexpr (sizeof(T) == 4) {
       const dim3 g(I.KXP / txz, I.NYR);
+      if (zpair())
+        FFS_CT_SWITCH(ctzu(), (k_fwd_z2<NC, PAIR_LP><<<g, PAIR_LP * ct_tpl<NC>(), pair_smem<NC, PAIR_LP>(), s>>>(
+                                  I, fwd_list, mode)))
       switch (ctzu()) {
         case 128:
           if (zseq) k_fwd_z<T, TX, 128, true><<<g, TX * ct_tpl<128>(), smem_zu, s>>>(I, fwd_list, mode);
@@ -938,7 +972,7 @@ class Engine : public EngineBase {
   // Each group is tuned on its own (they are independent passes). The choice is cached
   // per grid, model and precision for the process, so engines of the same shape tune once.
   struct TuneChoice {
-    int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z;
+    int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy;
     std::string report;
   };
   static std::mutex& tune_mu() { static std::mutex m; return m; }
@@ -955,7 +989,7 @@ class Engine : public EngineBase {
       if (it != tune_cache().end()) {
         const TuneChoice& c = it->second;
         txy = c.txy; use_ct = c.use_ct; lyz = c.lyz; xfused = c.xfused; txz = c.txz; zseq = c.zseq;
-        use_ct_z = c.use_ct_z;
+        use_ct_z = c.use_ct_z; pair_z = c.pair_z; v_iz = c.v_iz; v_iy = c.v_iy; v_fy = c.v_fy;
         tune_report = c.report + " (cached)";
         compute_smem();
         return set_smem(err);
@@ -994,6 +1028,7 @@ class Engine : public EngineBase {
     {
       float best = 1e30f;
       int bt = txy, bc = use_ct;
+      v_iz = v_iy = v_fy = 0;
       for (int t : {TX, TX / 2})
         for (int c : {1, 0}) {
           if (t * std::max(I.py.tpl, I.pz.tpl) > MAXT) continue;
@@ -1006,6 +1041,26 @@ class Engine : public EngineBase {
           if (ms < best) { best = ms; bt = t; bc = c; }
         }
       txy = bt; use_ct = bc;
+      // then the form of each compile-time pass on its own
+      auto pick = [&](int& v, const char* name, int n, auto&& launch) -> int {
+        if (!n) return 0;
+        float bms = 1e30f;
+        int bv = 0;
+        for (int c = 0; c < 2; ++c) {
+          v = c;
+          float ms = 0.f;
+          int r;
+          if ((r = timed(launch, ms))) return r;
+          snprintf(line, sizeof(line), "%s[%s]=%.4fms ", name, vname_of(c), ms);
+          rep += line;
+          if (ms < bms) { bms = ms; bv = c; }
+        }
+        v = bv;
+        return 0;
+      };
+      if (!rc) rc = pick(v_iz, "z_inv", ctz(), [&] { launch_inv_z(inv_list); });
+      if (!rc) rc = pick(v_iy, "y_inv", cty(), [&] { launch_inv_y(inv_list); });
+      if (!rc) rc = pick(v_fy, "y_fwd", cty(), [&] { launch_fwd_y(fwd_list); });
     }
     // x pass
     if (!rc) {
@@ -1029,39 +1084,42 @@ class Engine : public EngineBase {
     // forward z pass
     if (!rc) {
       float best = 1e30f;
-      int bt = txz, bq = zseq, bc = use_ct_z;
+      int bt = txz, bq = zseq, bc = use_ct_z, bp = pair_z;
       for (int q : {0, 1})
         for (int t : {TX, TX / 2, TX / 4})
-          for (int c : {1, 0}) {
+          for (int c : {2, 1, 0}) {
             if (t < 1 || (q ? 1 : 3) * t * I.pz.tpl > MAXT) continue;
             if (q && t < TX / 2) continue;
-            txz = t; zseq = q; use_ct_z = c;
+            txz = t; zseq = q; use_ct_z = c > 0; pair_z = c == 2;
             if (c && !ctzu()) continue;   // no compile-time kernel for this shape
+            if (c == 2 && !zpair()) continue;
             float ms = 0.f;
             if ((rc = timed([&] { launch_zu(0); }, ms))) break;
-            snprintf(line, sizeof(line), "fwd_z[tx=%d,%s,%s]=%.4fms ", t, q ? "seq" : "3c", c ? "ct" : "rt", ms);
+            snprintf(line, sizeof(line), "fwd_z[tx=%d,%s,%s]=%.4fms ", t, q ? "seq" : "3c", c == 2 ? "ct2" : c ? "ct" : "rt", ms);
             rep += line;
-            if (ms < best) { best = ms; bt = t; bq = q; bc = c; }
+            if (ms < best) { best = ms; bt = t; bq = q; bc = c > 0; bp = c == 2; }
           }
-      txz = bt; zseq = bq; use_ct_z = bc;
+      txz = bt; zseq = bq; use_ct_z = bc; pair_z = bp;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
-    snprintf(line, sizeof(line), "-> tx_yz=%d %s, x=%s%d, fwd_z tx=%d %s %s", txy, use_ct ? "ct" : "rt",
-             xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c", use_ct_z ? "ct" : "rt");
+    snprintf(line, sizeof(line), "-> tx_yz=%d %s [z_inv %s, y_inv %s, y_fwd %s], x=%s%d, fwd_z tx=%d %s %s", txy,
+             use_ct ? "ct" : "rt", vname_of(v_iz), vname_of(v_iy), vname_of(v_fy),
+             xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c",
+             use_ct_z ? (zpair() ? "ct2" : "ct") : "rt");
     rep += line;
     tune_report = rep;
     compute_smem();
     if ((rc = set_smem(err))) return rc;
     {
       std::lock_guard<std::mutex> g(tune_mu());
-      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, rep};
+      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, rep};
     }
     return reset_state(err);
   }
   int ct_len_raw(int n) const {
-    return (sizeof(T) == 4 && P.kernel_variant == 0 && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
+    return (sizeof(T) == 4 && P.kernel_variant != 1 && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
   }
   std::string tuning() const override { return tune_report; }
 

@@ -291,6 +291,102 @@ __device__ __forceinline__ void fft_lines_ct(cplx<T>* s0, cplx<T>* s1, const cpl
   }
 }
 
+// v * w (DIR < 0) or v * conj(w) (DIR > 0) for both lanes of v, with w = (c, s) given as
+// C = (c, c), S = (s, s)
+template <int DIR>
+__device__ __forceinline__ cplx<float2> twmul2(cplx<float2> v, float2 C, float2 S) {
+  const float2 NS = -S;
+  const float2 P = v.x * C, Q = v.y * C;
+  if (DIR < 0) return mk(fma_(v.y, NS, P), fma_(v.x, S, Q));
+  return mk(fma_(v.y, S, P), fma_(v.x, NS, Q));
+}
+template <int DIR>
+__device__ __forceinline__ cplx<float> twmul1(cplx<float> v, float c, float s) {
+  if (DIR < 0) return mk(fmaf(v.y, -s, v.x * c), fmaf(v.x, s, v.y * c));
+  return mk(fmaf(v.y, s, v.x * c), fmaf(v.x, -s, v.y * c));
+}
+
+// ---------------------------------------------------------------------------------
+// Paired lines (FP32, compile-time plans): the L = 2 LP lines of a CTA as LP pairs
+// (2 lp, 2 lp + 1), each pair transformed at once on the packed FP32 pipe by LP * tpl
+// threads. Shared memory holds one 16-byte cplx<float2> per (position, pair); row j (LP
+// elements) sits at row j ^ ((j >> S) & 1), S = log2 of the first radix, so that the two
+// rows a quarter warp touches in every pass (j and j + 1, or j and j + R0 in the first
+// pass) fall in opposite halves of the banks. The loader ld2(lp, j) returns and the
+// storer st2(lp, j, v) takes both lines of a pair.
+// ---------------------------------------------------------------------------------
+template <int N> constexpr int ct_log2r0() {
+  return CtPlan<N>::r0 == 16 ? 4 : CtPlan<N>::r0 == 8 ? 3 : CtPlan<N>::r0 == 4 ? 2 : 1;
+}
+template <int N, int LP> __device__ __forceinline__ int ppos(int j, int lp) {
+  return (j ^ ((j >> ct_log2r0<N>()) & 1)) * LP + lp;
+}
+
+template <int R, int DIR, int LP, int N, class LD, class ST, int NT>
+__device__ __forceinline__ void fft_pass2(int T_, int p, int tws, bool first, bool last, const cplx<float2>* in,
+                                          cplx<float2>* out, const cplx<float>* __restrict__ tw, LD& ld, ST& st) {
+#pragma unroll 1
+  for (int b = threadIdx.x; b < LP * T_; b += NT) {
+    const int lp = b % LP, i = b / LP;
+    const int k = i & (p - 1);
+    cplx<float2> x[R];
+    if (first) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) x[m] = ld(lp, i + m * T_);
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m) x[m] = in[ppos<N, LP>(i + m * T_, lp)];
+      if (k != 0) {
+#pragma unroll
+        for (int m = 1; m < R; ++m) {
+          const cplx<float> w = tw[k * m * tws];
+          x[m] = twmul2<DIR>(x[m], make_float2(w.x, w.x), make_float2(w.y, w.y));
+        }
+      }
+    }
+    dftR<R, DIR>(x);
+    const int j = (i - k) * R + k;
+    if (last) {
+#pragma unroll
+      for (int m = 0; m < R; ++m) st(lp, j + m * p, x[m]);
+    } else {
+#pragma unroll
+      for (int m = 0; m < R; ++m) out[ppos<N, LP>(j + m * p, lp)] = x[m];
+    }
+  }
+}
+
+// Whole compile-time plan over LP pairs; s0 (and s1 for three-pass plans) hold N * LP
+// elements. Ends with a __syncthreads().
+template <int DIR, int LP, int N, class LD, class ST>
+__device__ __forceinline__ void fft_lines_ct2(cplx<float2>* s0, cplx<float2>* s1, const cplx<float>* __restrict__ tw,
+                                              LD ld, ST st) {
+  using C = CtPlan<N>;
+  constexpr int NT = LP * ct_tpl<N>();
+  constexpr int R0 = C::r0, R1 = C::r1, R2 = C::r2;
+  fft_pass2<R0, DIR, LP, N, LD, ST, NT>(N / R0, 1, N / R0, true, false, s0, s0, tw, ld, st);
+  __syncthreads();
+  if constexpr (C::np == 2) {
+    fft_pass2<R1, DIR, LP, N, LD, ST, NT>(N / R1, R0, 1, false, true, s0, s1, tw, ld, st);
+    __syncthreads();
+  } else {
+    fft_pass2<R1, DIR, LP, N, LD, ST, NT>(N / R1, R0, N / (R0 * R1), false, false, s0, s1, tw, ld, st);
+    __syncthreads();
+    fft_pass2<R2, DIR, LP, N, LD, ST, NT>(N / R2, R0 * R1, 1, false, true, s1, s0, tw, ld, st);
+    __syncthreads();
+  }
+}
+
+// 16-byte global accesses of a line pair (two adjacent complex values)
+__device__ __forceinline__ cplx<float2> ldg_pair(const cplx<float>* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  return mk(make_float2(v.x, v.z), make_float2(v.y, v.w));
+}
+__device__ __forceinline__ void st_pair(cplx<float>* p, cplx<float2> v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.x.x, v.y.x, v.x.y, v.y.y);
+}
+__device__ __forceinline__ cplx<float2> zero_pair() { return mk(make_float2(0.f, 0.f), make_float2(0.f, 0.f)); }
+
 // The compile-time plan when N > 0 (line stride LSC, CTA of NTB threads, by default
 // L * ct_tpl<N>()), else the runtime plan P.
 template <int DIR, int L, typename T, int N, class LD, class ST, int LSC = L, int NTB = 0>

@@ -66,21 +66,6 @@ template <int N> struct XFused {
   }
 };
 
-// v * w (DIR < 0) or v * conj(w) (DIR > 0) for both lanes of v, with w = (c, s) given as
-// C = (c, c), S = (s, s)
-template <int DIR>
-__device__ __forceinline__ cplx<float2> twmul2(cplx<float2> v, float2 C, float2 S) {
-  const float2 NS = -S;
-  const float2 P = v.x * C, Q = v.y * C;
-  if (DIR < 0) return mk(fma_(v.y, NS, P), fma_(v.x, S, Q));
-  return mk(fma_(v.y, S, P), fma_(v.x, NS, Q));
-}
-template <int DIR>
-__device__ __forceinline__ cplx<float> twmul1(cplx<float> v, float c, float s) {
-  if (DIR < 0) return mk(fmaf(v.y, -s, v.x * c), fmaf(v.x, s, v.y * c));
-  return mk(fmaf(v.y, s, v.x * c), fmaf(v.x, -s, v.y * c));
-}
-
 // One Stockham middle pass (radix R2, sub-transform length p = R entering, T_ = n/R2
 // butterflies per line) over the LYZ lines of a pair plane or, with PAIR false, of a
 // single plane. tw: exp(-2 pi i t / n).

@@ -79,7 +79,9 @@ typedef struct ffs_params {
   int32_t stats_capacity;      /* stats records kept on the device between reads */
   int32_t spec_capacity;       /* spectrum records kept on the device between reads */
   int32_t kernel_variant;      /* 0: specialised FP32 kernels where available (register-fused x pass,
-                                  compile-time FFT lengths); 1: runtime-plan kernels only */
+                                  compile-time FFT lengths); 1: runtime-plan kernels only;
+                                  2: as 0 with every compile-time y/z pass on line pairs (packed FP32);
+                                  3: as 0 with every compile-time y/z pass one line per thread */
   int32_t autotune;            /* 1: time the candidate launch shapes at create, keep the fastest */
 } ffs_params;
 

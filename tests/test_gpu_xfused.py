@@ -1,5 +1,7 @@
 """The specialised FP32 kernels (register-fused x pass, compile-time-length y/z passes;
-n in {128, 256, 512}) against the runtime-plan kernels and against the FP64 oracle.
+n in {128, 256, 512}; kernel_variant 2 and 3 force the line-pair and the
+one-line-per-thread forms of the y/z passes) against the runtime-plan kernels and
+against the FP64 oracle.
 
 Both variants compute the same products in FP32 and differ only in the order of the
 FFT's floating-point operations, so fields agree to ~1e-7 relative; the bar is 2e-6
@@ -40,11 +42,12 @@ def make(pkg, d, u, variant):
     return sim
 
 
-@pytest.mark.parametrize("n,dtstat", [(128, 1), (256, 1), (256, 1000), (512, 2)])
-def test_fused_matches_generic(gpu_pkg, n, dtstat):
+@pytest.mark.parametrize("n,dtstat,variant", [(128, 1, 0), (256, 1, 0), (256, 1000, 0), (512, 2, 0),
+                                               (128, 1, 2), (256, 1, 2), (512, 2, 2), (128, 1, 3), (256, 1, 3)])
+def test_fused_matches_generic(gpu_pkg, n, dtstat, variant):
     d = gdict(n, dtStat=dtstat)
     u = gpu_pkg.random_spectrum(n, k0=4.0, seed=11)
-    a, b = make(gpu_pkg, d, u, 0), make(gpu_pkg, d, u, 1)
+    a, b = make(gpu_pkg, d, u, variant), make(gpu_pkg, d, u, 1)
     steps = 5 if n < 512 else 3
     a.advance_in_time(steps)
     b.advance_in_time(steps)
