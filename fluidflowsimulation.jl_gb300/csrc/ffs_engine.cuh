@@ -15,6 +15,7 @@
 #include "ffs_kernels.cuh"
 #include "ffs_pairs.cuh"
 #include "ffs_xfused.cuh"
+#include "ffs_xles.cuh"
 #include "ffs_batch.cuh"
 
 namespace ffsgpu {
@@ -79,7 +80,8 @@ class Engine : public EngineBase {
   int nin = 0, nout = 0;
   int lyz = 4;
   int lio = LYZ_IO;           // (y,z) lines per CTA of the field-IO x kernels
-  int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass)
+  int xfused = 0;             // n of the register-fused x pass in use (0: generic x pass);
+                              // the velocity-only form, or with LES the twelve-field form
   int xfused_ok = 0;          // n for which the fused x pass is available
   bool use_ct = true;         // compile-time FFT plans in the FP32 y/z passes
   bool use_ct_z = true;       // compile-time FFT plans in the FP32 forward z pass
@@ -309,14 +311,18 @@ class Engine : public EngineBase {
     }
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
     xfused = 0;
-    if (sizeof(T) == 4 && !I.les && !I.density && p.kernel_variant != 1) {
+    if (sizeof(T) == 4 && (I.les || !I.density) && p.kernel_variant != 1) {
       int lyzf = 0, rf = 0;
-      switch (p.nx) {
-        case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
-        case 256: lyzf = XFused<256>::LYZ; rf = XFused<256>::R; break;
-        case 512: lyzf = XFused<512>::LYZ; rf = XFused<512>::R; break;
-        case 1024: lyzf = XFused<1024>::LYZ; rf = XFused<1024>::R; break;
-        default: break;
+      if (I.les) {   // LES (with or without density): n in {64, 128}
+        if (p.nx == 64 || p.nx == 128) { lyzf = XLes<128>::LYZ; rf = XLes<128>::RR; }
+      } else {
+        switch (p.nx) {
+          case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
+          case 256: lyzf = XFused<256>::LYZ; rf = XFused<256>::R; break;
+          case 512: lyzf = XFused<512>::LYZ; rf = XFused<512>::R; break;
+          case 1024: lyzf = XFused<1024>::LYZ; rf = XFused<1024>::R; break;
+          default: break;
+        }
       }
       if (lyzf && ((long long)p.ny * p.nz) % lyzf == 0) {
         xfused = xfused_ok = p.nx;
@@ -445,7 +451,14 @@ class Engine : public EngineBase {
         return rc;
     }
     if constexpr (sizeof(T) == 4) {
-      switch (xfused) {
+      if (I.les) {
+        if (xfused == 64 && ((rc = smem_attr(k_x_les<64, false>, XLes<64>::smem(), err)) ||
+                             (rc = smem_attr(k_x_les<64, true>, XLes<64>::smem(), err))))
+          return rc;
+        if (xfused == 128 && ((rc = smem_attr(k_x_les<128, false>, XLes<128>::smem(), err)) ||
+                              (rc = smem_attr(k_x_les<128, true>, XLes<128>::smem(), err))))
+          return rc;
+      } else switch (xfused) {
         case 128: if ((rc = smem_attr(k_x_fused<128>, XFused<128>::smem(), err))) return rc; break;
         case 256: if ((rc = smem_attr(k_x_fused<256>, XFused<256>::smem(), err))) return rc; break;
         case 512: if ((rc = smem_attr(k_x_fused<512>, XFused<512>::smem(), err))) return rc; break;
@@ -601,7 +614,23 @@ class Engine : public EngineBase {
     if constexpr (sizeof(T) == 4)
       k_x_fused<N><<<dim3((unsigned)((long long)I.ny * I.nz / XFused<N>::LYZ)), XFused<N>::NT, XFused<N>::smem(), s>>>(I);
   }
+  template <int N> void launch_x_les() {
+    if constexpr (sizeof(T) == 4) {
+      auto k = I.density ? k_x_les<N, true> : k_x_les<N, false>;
+      if (!I.x_pf_dist) {   // CTAs resident at once on the device
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, XLes<N>::NT, XLes<N>::smem());
+        I.x_pf_dist = std::max(1, nb) * n_sms;
+      }
+      k<<<dim3((unsigned)((long long)I.ny * I.nz / XLes<N>::LYZ)), XLes<N>::NT, XLes<N>::smem(), s>>>(I);
+    }
+  }
   void launch_x() {
+    if (xfused && I.les) {
+      if (xfused == 64) launch_x_les<64>();
+      else launch_x_les<128>();
+      return;
+    }
     switch (xfused) {
       case 128: launch_x_fused<128>(); return;
       case 256: launch_x_fused<256>(); return;

@@ -75,3 +75,43 @@ def test_fused_fp32_against_oracle(gpu_pkg):
     for c in range(3):
         assert rel(sim.spectral(c), ref.u[c]) <= 1e-4, c
     sim.close()
+
+
+def les_dict(n, den):
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": "5e-4", "dtStat": "1", "dtSpec": "2", "writeTime": "1000",
+         "velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "true", "cfl": "0.18", "dt": "0.001",
+         "lesModel": "Smagorinsky", "smagorinskyConstant": "0.17", "filterWidth": repr(2 * np.pi / n)}
+    if den:
+        d.update({"densityStratification": "true", "zAcceleration": "1", "referenceDensity": "1",
+                  "densityGradient": "1", "Pr": "1"})
+    return d
+
+
+@pytest.mark.parametrize("n,den", [(64, False), (128, False), (64, True), (128, True)])
+def test_les_fused_matches_generic(gpu_pkg, n, den):
+    """The twelve-field register-fused x pass (Smagorinsky LES, with and without
+    Boussinesq density; n = 64, 128) against the generic x pass."""
+    d = les_dict(n, den)
+    u = gpu_pkg.random_spectrum(n, k0=3.0, seed=13)
+    sims = []
+    for variant in (0, 1):
+        p = gpu_pkg.parameters(d, precision="FP32")
+        p.kernel_variant = variant
+        sim = gpu_pkg.Simulation(p)
+        sim.set_fields(*u, rho=np.zeros_like(u[0]) if den else None)
+        sim.initialize()
+        sim.advance_in_time(5)
+        sims.append(sim)
+    a, b = sims
+    for c in range(3):
+        assert rel(a.spectral(c), b.spectral(c)) <= FIELD_TOL, (n, c)
+    if den:   # rho starts at zero and grows from its source term over the 5 steps, so the
+        # two FP32 operation orders differ by ~2e-6 of it; the bar is 1e-5
+        assert rel(a.spectral(3), b.spectral(3)) <= 1e-5, n
+    assert a.dt == pytest.approx(b.dt, rel=1e-6)
+    ra, rb = a.stats_rows(), b.stats_rows()
+    assert ra.shape == rb.shape and ra.shape[0] >= 1
+    assert (np.abs(ra - rb) <= STATS_TOL * np.abs(rb) + 1e-6 * np.abs(rb).max()).all()
+    a.close()
+    b.close()
