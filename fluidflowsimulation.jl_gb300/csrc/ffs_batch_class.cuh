@@ -1,6 +1,6 @@
 // One size class of the batched step (cubic side N, class index CI): compile-time FFT
-// plans, CTAs of exactly the threads each plan needs, and for N = 128 the register-fused
-// x pass of velocity-only runs. Included by one small translation unit per class, which
+// plans, CTAs of exactly the threads each plan needs, for N = 128 the register-fused x
+// pass of velocity-only runs and for N = 64, 128 the register-fused x pass of LES runs. Included by one small translation unit per class, which
 // defines batch_class_ops_<N>().
 #pragma once
 #include <mutex>
@@ -9,6 +9,7 @@
 #include "../../include/ffs.h"
 #include "ffs_batch.cuh"
 #include "ffs_xfused.cuh"
+#include "ffs_xles.cuh"
 
 namespace ffsgpu {
 
@@ -21,12 +22,23 @@ kb_x_fused128(const BatchInst<float>* __restrict__ B, const BatchTables* __restr
   FFS_BATCH_END
 }
 
+// the twelve-field fused x pass of LES runs (n = 64, 128; the batch serves no density)
+template <int N, int CI>
+__global__ void __launch_bounds__(XLes<N>::NT, XLesCfg<N>::MINB)
+kb_x_les(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  using T = float;
+  FFS_BATCH_LOOP(BP_X_LES)
+  b_x_les<N, false>(BI.I, Blk{it.x, 0, 0, 0});
+  FFS_BATCH_END
+}
+
 template <int N, int CI>
 struct BatchClass {
   static constexpr int TX = BATCH_TX, LYZ = BATCH_LYZ;
   static constexpr int tpl = ct_tpl<N>();
   static constexpr int nbuf = CtPlan<N>::np >= 3 ? 2 : 1;
-  static constexpr bool FUSED = N == 128;
+  static constexpr bool FUSED = N == 128;               // velocity-only fused x pass
+  static constexpr bool LESF = N == 64 || N == 128;     // LES fused x pass
 
   // per-kernel limits are process-wide: only ever raised, under a lock
   template <typename K> static int attr(K k, size_t bytes, std::string* err) {
@@ -63,8 +75,8 @@ struct BatchClass {
     L->smem[BP_INV_Z] = L->smem[BP_INV_Y] = L->smem[BP_FWD_Y] = (size_t)TX * srows(N) * cb * nbuf;
     if (FUSED) { L->block[BP_X] = XFused<128>::NT; L->smem[BP_X] = XFused<128>::smem(); }
     else { L->block[BP_X] = ((3 * LYZ * tpl + 31) / 32) * 32; L->smem[BP_X] = xs(6); }
-    L->block[BP_X_LES] = 6 * LYZ * tpl;
-    L->smem[BP_X_LES] = xs(11);
+    if (LESF) { L->block[BP_X_LES] = XLes<LESF ? N : 64>::NT; L->smem[BP_X_LES] = XLes<LESF ? N : 64>::smem(); }
+    else { L->block[BP_X_LES] = 6 * LYZ * tpl; L->smem[BP_X_LES] = xs(11); }
     L->block[BP_FWD_Z] = 3 * TX * tpl;
     L->smem[BP_FWD_Z] = cb * ((size_t)3 * TX * srows(N) * nbuf + (size_t)4 * N * TX);
     L->block[BP_SCALAR] = 256; L->block[BP_TABLE] = 64; L->block[BP_STATS] = 256; L->block[BP_UPDATE] = 256;
@@ -75,9 +87,15 @@ struct BatchClass {
     if ((rc = attr(kb_inv_z<float, TX, CI, N>, L->smem[BP_INV_Z], err)) ||
         (rc = attr(kb_inv_y<float, TX, CI, N>, L->smem[BP_INV_Y], err)) ||
         (rc = attr(kb_fwd_y<float, TX, CI, N>, L->smem[BP_FWD_Y], err)) ||
-        (rc = attr(kb_x<float, true, LYZ, CI, N>, L->smem[BP_X_LES], err)) ||
         (rc = attr(kb_fwd_z<float, TX, CI, N>, L->smem[BP_FWD_Z], err)))
       return rc;
+    if constexpr (LESF) {
+      if ((rc = attr(kb_x_les<N, CI>, L->smem[BP_X_LES], err))) return rc;
+      if ((rc = occ(kb_x_les<N, CI>, L, BP_X_LES, sms, big, err))) return rc;
+    } else {
+      if ((rc = attr(kb_x<float, true, LYZ, CI, N>, L->smem[BP_X_LES], err))) return rc;
+      if ((rc = occ(kb_x<float, true, LYZ, CI, N>, L, BP_X_LES, sms, big, err))) return rc;
+    }
     if constexpr (FUSED) {
       if ((rc = attr(kb_x_fused128<CI>, L->smem[BP_X], err))) return rc;
       if ((rc = occ(kb_x_fused128<CI>, L, BP_X, sms, big, err))) return rc;
@@ -87,7 +105,6 @@ struct BatchClass {
     }
     if ((rc = occ(kb_inv_z<float, TX, CI, N>, L, BP_INV_Z, sms, big, err)) ||
         (rc = occ(kb_inv_y<float, TX, CI, N>, L, BP_INV_Y, sms, big, err)) ||
-        (rc = occ(kb_x<float, true, LYZ, CI, N>, L, BP_X_LES, sms, big, err)) ||
         (rc = occ(kb_fwd_y<float, TX, CI, N>, L, BP_FWD_Y, sms, big, err)) ||
         (rc = occ(kb_scalar<float, CI>, L, BP_SCALAR, sms, max_active, err)) ||
         (rc = occ(kb_table<float, CI>, L, BP_TABLE, sms, big, err)) ||
@@ -105,7 +122,8 @@ struct BatchClass {
     kb_inv_y<float, TX, CI, N><<<FFS_CL(BP_INV_Y)>>>(B, T);
     if constexpr (FUSED) kb_x_fused128<CI><<<FFS_CL(BP_X)>>>(B, T);
     else kb_x<float, false, LYZ, CI, N><<<FFS_CL(BP_X)>>>(B, T);
-    kb_x<float, true, LYZ, CI, N><<<FFS_CL(BP_X_LES)>>>(B, T);
+    if constexpr (LESF) kb_x_les<N, CI><<<FFS_CL(BP_X_LES)>>>(B, T);
+    else kb_x<float, true, LYZ, CI, N><<<FFS_CL(BP_X_LES)>>>(B, T);
     kb_fwd_y<float, TX, CI, N><<<FFS_CL(BP_FWD_Y)>>>(B, T);
     kb_scalar<float, CI><<<FFS_CL(BP_SCALAR)>>>(B, T);
     kb_table<float, CI><<<FFS_CL(BP_TABLE)>>>(B, T);

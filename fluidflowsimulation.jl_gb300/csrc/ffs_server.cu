@@ -346,7 +346,7 @@ class Server {
     auto j = std::make_shared<Job>();
     j->p = p;
     j->p.device = cfg.device;
-    j->p.kernel_variant = 0;   // 128^3 velocity-only engines carry the fused x pass twiddles
+    j->p.kernel_variant = 0;   // engines carry the fused x passes' twiddles (128^3; 64^3 and 128^3 LES)
     // records of one run stay on the device until it finishes
     j->p.stats_capacity = (int32_t)std::max<int64_t>(64, r.nt / std::max(1, p.dt_stat) + 4);
     j->p.spec_capacity = (int32_t)std::max<int64_t>(4, r.nt / std::max(1, p.dt_spec) + 4);
@@ -568,12 +568,15 @@ class Server {
     return true;
   }
 
-  // size class of a simulation: its cubic side when a class exists for it (128^3
-  // velocity-only runs need the engine's register-pass twiddles), else the generic class
+  // the classes whose x pass is register-fused for this model (they need the engine's
+  // register-pass twiddles): 128^3 velocity-only, 64^3 and 128^3 LES
+  static bool fused_x(const BatchGeom& g) { return g.les ? (g.nx == 64 || g.nx == 128) : g.nx == 128; }
+  // size class of a simulation: its cubic side when a class exists for it, else the
+  // generic class
   int class_of(const BatchGeom& g) const {
     if (g.nx != g.ny || g.nx != g.nz) return 0;
     for (int c = 1; c < BATCH_NCLASS; ++c)
-      if (cls[c].n == g.nx && g.nx <= cfg.max_n) return (g.nx == 128 && !g.les && g.xfused != 128) ? 0 : c;
+      if (cls[c].n == g.nx && g.nx <= cfg.max_n) return (fused_x(g) && g.xfused != g.nx) ? 0 : c;
     return 0;
   }
 
@@ -593,7 +596,7 @@ class Server {
           for (int z = 0; z < g.nz; ++z) it[BP_INV_Y].push_back({k, f, t, z});
         }
       auto& xt = it[g.les ? BP_X_LES : BP_X];
-      const int xg = (class_of(g) == 5 && !g.les) ? g.ny * g.nz / 8 : g.yz_groups;   // fused x: 8 lines per CTA
+      const int xg = (class_of(g) != 0 && fused_x(g)) ? g.ny * g.nz / 8 : g.yz_groups;   // fused x: 8 lines per CTA
       for (int b = 0; b < xg; ++b) xt.push_back({k, b, 0, 0});
       for (int f = 0; f < g.nout; ++f)
         for (int t = 0; t < g.kx_tiles; ++t)
