@@ -1,6 +1,6 @@
 // One size class of the batched step (cubic side N, class index CI): compile-time FFT
-// plans, CTAs of exactly the threads each plan needs, for N = 128 the register-fused x
-// pass of velocity-only runs and for N = 64, 128 the register-fused x pass of LES runs. Included by one small translation unit per class, which
+// plans, CTAs of exactly the threads each plan needs, and for N = 64, 128 the
+// register-fused x passes of velocity-only and LES runs. Included by one small translation unit per class, which
 // defines batch_class_ops_<N>().
 #pragma once
 #include <mutex>
@@ -13,12 +13,12 @@
 
 namespace ffsgpu {
 
-template <int CI>
-__global__ void __launch_bounds__(XFused<128>::NT, XFusedCfg<128>::MINB)
-kb_x_fused128(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+template <int N, int CI>
+__global__ void __launch_bounds__(XFused<N>::NT, XFusedCfg<N>::MINB)
+kb_x_fused(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
   using T = float;
   FFS_BATCH_LOOP(BP_X)
-  b_x_fused<128>(BI.I, Blk{it.x, 0, 0, 0});
+  b_x_fused<N>(BI.I, Blk{it.x, 0, 0, 0});
   FFS_BATCH_END
 }
 
@@ -37,7 +37,7 @@ struct BatchClass {
   static constexpr int TX = BATCH_TX, LYZ = BATCH_LYZ;
   static constexpr int tpl = ct_tpl<N>();
   static constexpr int nbuf = CtPlan<N>::np >= 3 ? 2 : 1;
-  static constexpr bool FUSED = N == 128;               // velocity-only fused x pass
+  static constexpr bool FUSED = N == 64 || N == 128;    // velocity-only fused x pass
   static constexpr bool LESF = N == 64 || N == 128;     // LES fused x pass
 
   // per-kernel limits are process-wide: only ever raised, under a lock
@@ -73,7 +73,7 @@ struct BatchClass {
     };
     L->block[BP_INV_Z] = L->block[BP_INV_Y] = L->block[BP_FWD_Y] = TX * tpl;
     L->smem[BP_INV_Z] = L->smem[BP_INV_Y] = L->smem[BP_FWD_Y] = (size_t)TX * srows(N) * cb * nbuf;
-    if (FUSED) { L->block[BP_X] = XFused<128>::NT; L->smem[BP_X] = XFused<128>::smem(); }
+    if (FUSED) { L->block[BP_X] = XFused<FUSED ? N : 128>::NT; L->smem[BP_X] = XFused<FUSED ? N : 128>::smem(); }
     else { L->block[BP_X] = ((3 * LYZ * tpl + 31) / 32) * 32; L->smem[BP_X] = xs(6); }
     if (LESF) { L->block[BP_X_LES] = XLes<LESF ? N : 64>::NT; L->smem[BP_X_LES] = XLes<LESF ? N : 64>::smem(); }
     else { L->block[BP_X_LES] = 6 * LYZ * tpl; L->smem[BP_X_LES] = xs(11); }
@@ -97,8 +97,8 @@ struct BatchClass {
       if ((rc = occ(kb_x<float, true, LYZ, CI, N>, L, BP_X_LES, sms, big, err))) return rc;
     }
     if constexpr (FUSED) {
-      if ((rc = attr(kb_x_fused128<CI>, L->smem[BP_X], err))) return rc;
-      if ((rc = occ(kb_x_fused128<CI>, L, BP_X, sms, big, err))) return rc;
+      if ((rc = attr(kb_x_fused<N, CI>, L->smem[BP_X], err))) return rc;
+      if ((rc = occ(kb_x_fused<N, CI>, L, BP_X, sms, big, err))) return rc;
     } else {
       if ((rc = attr(kb_x<float, false, LYZ, CI, N>, L->smem[BP_X], err))) return rc;
       if ((rc = occ(kb_x<float, false, LYZ, CI, N>, L, BP_X, sms, big, err))) return rc;
@@ -120,7 +120,7 @@ struct BatchClass {
 #define FFS_CL(PH) L.grid[PH], L.block[PH], L.smem[PH], s
     kb_inv_z<float, TX, CI, N><<<FFS_CL(BP_INV_Z)>>>(B, T);
     kb_inv_y<float, TX, CI, N><<<FFS_CL(BP_INV_Y)>>>(B, T);
-    if constexpr (FUSED) kb_x_fused128<CI><<<FFS_CL(BP_X)>>>(B, T);
+    if constexpr (FUSED) kb_x_fused<N, CI><<<FFS_CL(BP_X)>>>(B, T);
     else kb_x<float, false, LYZ, CI, N><<<FFS_CL(BP_X)>>>(B, T);
     if constexpr (LESF) kb_x_les<N, CI><<<FFS_CL(BP_X_LES)>>>(B, T);
     else kb_x<float, true, LYZ, CI, N><<<FFS_CL(BP_X_LES)>>>(B, T);

@@ -317,6 +317,7 @@ class Engine : public EngineBase {
         if (p.nx == 64 || p.nx == 128) { lyzf = XLes<128>::LYZ; rf = XLes<128>::RR; }
       } else {
         switch (p.nx) {
+          case 64: lyzf = XFused<64>::LYZ; rf = XFused<64>::R; break;
           case 128: lyzf = XFused<128>::LYZ; rf = XFused<128>::R; break;
           case 256: lyzf = XFused<256>::LYZ; rf = XFused<256>::R; break;
           case 512: lyzf = XFused<512>::LYZ; rf = XFused<512>::R; break;
@@ -459,6 +460,7 @@ class Engine : public EngineBase {
                               (rc = smem_attr(k_x_les<128, true>, XLes<128>::smem(), err))))
           return rc;
       } else switch (xfused) {
+        case 64: if ((rc = smem_attr(k_x_fused<64>, XFused<64>::smem(), err))) return rc; break;
         case 128: if ((rc = smem_attr(k_x_fused<128>, XFused<128>::smem(), err))) return rc; break;
         case 256: if ((rc = smem_attr(k_x_fused<256>, XFused<256>::smem(), err))) return rc; break;
         case 512: if ((rc = smem_attr(k_x_fused<512>, XFused<512>::smem(), err))) return rc; break;
@@ -632,6 +634,7 @@ class Engine : public EngineBase {
       return;
     }
     switch (xfused) {
+      case 64: launch_x_fused<64>(); return;
       case 128: launch_x_fused<128>(); return;
       case 256: launch_x_fused<256>(); return;
       case 512: launch_x_fused<512>(); return;

@@ -346,7 +346,7 @@ class Server {
     auto j = std::make_shared<Job>();
     j->p = p;
     j->p.device = cfg.device;
-    j->p.kernel_variant = 0;   // engines carry the fused x passes' twiddles (128^3; 64^3 and 128^3 LES)
+    j->p.kernel_variant = 0;   // engines carry the fused x passes' twiddles (64^3, 128^3)
     // records of one run stay on the device until it finishes
     j->p.stats_capacity = (int32_t)std::max<int64_t>(64, r.nt / std::max(1, p.dt_stat) + 4);
     j->p.spec_capacity = (int32_t)std::max<int64_t>(4, r.nt / std::max(1, p.dt_spec) + 4);
@@ -569,8 +569,8 @@ class Server {
   }
 
   // the classes whose x pass is register-fused for this model (they need the engine's
-  // register-pass twiddles): 128^3 velocity-only, 64^3 and 128^3 LES
-  static bool fused_x(const BatchGeom& g) { return g.les ? (g.nx == 64 || g.nx == 128) : g.nx == 128; }
+  // register-pass twiddles): 64^3 and 128^3, velocity-only and LES
+  static bool fused_x(const BatchGeom& g) { return g.nx == 64 || g.nx == 128; }
   // size class of a simulation: its cubic side when a class exists for it, else the
   // generic class
   int class_of(const BatchGeom& g) const {

@@ -32,6 +32,7 @@ __device__ __forceinline__ cplx<float> ldg_c(const cplx<float>* p) {
 }
 
 template <int N> struct XFusedCfg;
+template <> struct XFusedCfg<64> { static constexpr int R = 8, R2 = 1, LYZ = 8, MINB = 8; };
 template <> struct XFusedCfg<128> { static constexpr int R = 8, R2 = 2, LYZ = 8, MINB = 4; };
 template <> struct XFusedCfg<256> { static constexpr int R = 16, R2 = 1, LYZ = 8, MINB = 4; };
 template <> struct XFusedCfg<512> { static constexpr int R = 8, R2 = 8, LYZ = 2, MINB = 3; };

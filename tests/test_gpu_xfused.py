@@ -1,5 +1,5 @@
 """The specialised FP32 kernels (register-fused x pass, compile-time-length y/z passes;
-n in {128, 256, 512}; kernel_variant 2 and 3 force the line-pair and the
+n in {64, 128, 256, 512}; kernel_variant 2 and 3 force the line-pair and the
 one-line-per-thread forms of the y/z passes) against the runtime-plan kernels and
 against the FP64 oracle.
 
@@ -42,7 +42,7 @@ def make(pkg, d, u, variant):
     return sim
 
 
-@pytest.mark.parametrize("n,dtstat,variant", [(128, 1, 0), (256, 1, 0), (256, 1000, 0), (512, 2, 0),
+@pytest.mark.parametrize("n,dtstat,variant", [(64, 1, 0), (128, 1, 0), (256, 1, 0), (256, 1000, 0), (512, 2, 0),
                                                (128, 1, 2), (256, 1, 2), (512, 2, 2), (128, 1, 3), (256, 1, 3)])
 def test_fused_matches_generic(gpu_pkg, n, dtstat, variant):
     d = gdict(n, dtStat=dtstat)
