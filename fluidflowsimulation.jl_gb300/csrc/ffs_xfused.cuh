@@ -31,6 +31,21 @@ __device__ __forceinline__ cplx<float> ldg_c(const cplx<float>* p) {
   return mk(v.x, v.y);
 }
 
+// Hermitian extension of a half spectrum for the first inverse radix pass: thread i takes
+// element j = i + m n/R (m < R) of the full line; it reads half-spectrum entry k and uses
+// a + i b -> (a.x - s b.y, s a.y + b.x) for a line packing two real fields a, b, where
+// s = 1 for j < n/2, -1 for j > n/2 (k = n - j, conjugate) and 0 where c2r ignores the
+// imaginary part (k = 0, k = n/2). With m known at compile time only m = 0 and m = R/2
+// need run-time tests.
+template <int N, int R>
+__device__ __forceinline__ void herm_index(int i, int m, int& k, float& s) {
+  constexpr int TPL = N / R;
+  const int j = i + m * TPL;
+  if (m < R / 2) { k = j; s = (m == 0 && i == 0) ? 0.f : 1.f; }
+  else if (m > R / 2) { k = N - j; s = -1.f; }
+  else { k = N / 2 - i; s = i == 0 ? 0.f : -1.f; }
+}
+
 template <int N> struct XFusedCfg;
 template <> struct XFusedCfg<64> { static constexpr int R = 8, R2 = 1, LYZ = 8, MINB = 8; };
 template <> struct XFusedCfg<128> { static constexpr int R = 8, R2 = 2, LYZ = 8, MINB = 4; };
@@ -144,14 +159,13 @@ __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
     cplx<float2> x[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) {
-      const int j = i + m * TPL;
-      const bool cj = 2 * j > N;
-      const int k = cj ? N - j : j;
+      int k;
+      T sg;
+      herm_index<N, R>(i, m, k, sg);
       cplx<T> a0 = mk(T(0), T(0)), b0 = a0, a1 = a0, b1 = a0;
       if (k < Mx) { a0 = ldg_c(F0 + k); b0 = ldg_c(F0 + fs + k); a1 = ldg_c(F0 + 2 * fs + k); b1 = ldg_c(F0 + 3 * fs + k); }
-      if (k == 0 || 2 * k == N) { a0.y = T(0); b0.y = T(0); a1.y = T(0); b1.y = T(0); }   // c2r ignores Im there
-      if (cj) { a0.y = -a0.y; b0.y = -b0.y; a1.y = -a1.y; b1.y = -b1.y; }
-      x[m] = mk(make_float2(a0.x - b0.y, a1.x - b1.y), make_float2(a0.y + b0.x, a1.y + b1.x));
+      x[m] = mk(make_float2(fmaf(-sg, b0.y, a0.x), fmaf(-sg, b1.y, a1.x)),
+                make_float2(fmaf(sg, a0.y, b0.x), fmaf(sg, a1.y, b1.x)));
     }
     dftR<R, +1>(x);
 #pragma unroll
@@ -163,14 +177,12 @@ __device__ __forceinline__ void b_x_fused(const Inst<float>& I, const Blk bk) {
     cplx<T> x[R];
 #pragma unroll
     for (int m = 0; m < R; ++m) {
-      const int j = i + m * TPL;
-      const bool cj = 2 * j > N;
-      const int k = cj ? N - j : j;
+      int k;
+      T sg;
+      herm_index<N, R>(i, m, k, sg);
       cplx<T> a = mk(T(0), T(0)), b = a;
       if (k < Mx) { a = ldg_c(A + k); b = ldg_c(B + k); }
-      if (k == 0 || 2 * k == N) { a.y = T(0); b.y = T(0); }
-      if (cj) { a.y = -a.y; b.y = -b.y; }
-      x[m] = mk(a.x - b.y, a.y + b.x);
+      x[m] = mk(fmaf(-sg, b.y, a.x), fmaf(sg, a.y, b.x));
     }
     dftR<R, +1>(x);
 #pragma unroll

@@ -75,17 +75,16 @@ __device__ __forceinline__ void b_x_les(const Inst<float>& I, const Blk bk) {
     cplx<float2> x[R0];
 #pragma unroll
     for (int m = 0; m < R0; ++m) {
-      const int j = ii + m * T0;
-      const bool cj = 2 * j > N;
-      const int k = cj ? N - j : j;
+      int k;
+      T sg;
+      herm_index<N, R0>(ii, m, k, sg);
       cplx<T> a0 = mk(T(0), T(0)), b0 = a0, a1 = a0, b1 = a0;
       if (k < Mx) {
         a0 = ldg_c(F0 + k); b0 = ldg_c(F0 + fs + k); a1 = ldg_c(F0 + 2 * fs + k);
         if (f3) b1 = ldg_c(F0 + 3 * fs + k);
       }
-      if (k == 0 || 2 * k == N) { a0.y = T(0); b0.y = T(0); a1.y = T(0); b1.y = T(0); }   // c2r ignores Im there
-      if (cj) { a0.y = -a0.y; b0.y = -b0.y; a1.y = -a1.y; b1.y = -b1.y; }
-      x[m] = mk(make_float2(a0.x - b0.y, a1.x - b1.y), make_float2(a0.y + b0.x, a1.y + b1.x));
+      x[m] = mk(make_float2(fmaf(-sg, b0.y, a0.x), fmaf(-sg, b1.y, a1.x)),
+                make_float2(fmaf(sg, a0.y, b0.x), fmaf(sg, a1.y, b1.x)));
     }
     dftR<R0, +1>(x);
 #pragma unroll
