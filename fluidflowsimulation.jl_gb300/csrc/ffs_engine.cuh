@@ -484,7 +484,7 @@ class Engine : public EngineBase {
       if (v_iz == 1 && ctz() == NC && (rc = smem_attr(k_inv_z2<NC, PAIR_LP>, ps, err))) return rc;
       if (v_iy == 1 && cty() == NC && (rc = smem_attr(k_inv_y2<NC, PAIR_LP>, ps, err))) return rc;
       if (v_fy == 1 && cty() == NC && (rc = smem_attr(k_fwd_y2<NC, PAIR_LP>, ps, err))) return rc;
-      if (zpair() && ctzu() == NC && (rc = smem_attr(k_fwd_z2<NC, PAIR_LP>, ps, err))) return rc;
+      if (zpair() && ctzu() == NC && (rc = smem_attr(k_fwd_z2<NC, PAIR_LP>, ps + z2_aux(), err))) return rc;
     }
     if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
     if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
@@ -568,8 +568,10 @@ class Engine : public EngineBase {
     default: break;                                                  \
   }
 
-  // the paired one-component forward z pass applies (velocity-only, TX lines, ct plan)
-  bool zpair() const { return sizeof(T) == 4 && pair_z && zseq && txz == TX && !I.les && !I.density; }
+  // the paired one-field-at-a-time forward z pass applies (FP32, TX lines, ct plan)
+  bool zpair() const { return sizeof(T) == 4 && pair_z && zseq && txz == TX; }
+  // its shared accumulators of i k.tau and i k.flux (LES / density)
+  size_t z2_aux() const { return (I.les || I.density) ? fwd_z2_aux_bytes<TX>(I.NZR) : 0; }
 
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
@@ -659,7 +661,7 @@ class Engine : public EngineBase {
     if constexpr (sizeof(T) == 4) {
       const dim3 g(I.KXP / txz, I.NYR);
       if (zpair())
-        FFS_CT_SWITCH(ctzu(), (k_fwd_z2<NC, PAIR_LP><<<g, PAIR_LP * ct_tpl<NC>(), pair_smem<NC, PAIR_LP>(), s>>>(
+        FFS_CT_SWITCH(ctzu(), (k_fwd_z2<NC, PAIR_LP><<<g, PAIR_LP * ct_tpl<NC>(), pair_smem<NC, PAIR_LP>() + z2_aux(), s>>>(
                                   I, fwd_list, mode)))
       switch (ctzu()) {
         case 128:

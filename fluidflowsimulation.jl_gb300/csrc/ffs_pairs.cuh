@@ -155,11 +155,16 @@ __global__ void __launch_bounds__(LP * ct_tpl<N>()) k_fwd_y2(Inst<float> I, Fiel
 }
 
 // ------------------------------------------------------------------------------------
-// Forward z pass of the velocity-only model, one component at a time (the SEQ form of
-// b_fwd_z): N (3 components) and, at stats/spectrum iterations, the kinetic energy,
-// scaled by 1/n^3 and pruned to the retained kz, into the scratch spectrum.
-// grid (KXP/TX, NYR)
+// Forward z pass, one field at a time (the SEQ form of b_fwd_z): N (3 components) and,
+// at stats/spectrum iterations, the kinetic energy, scaled by 1/n^3 and pruned to the
+// retained kz, into the scratch spectrum. With LES / density the stress and flux fields
+// are transformed the same way and accumulated as i k.tau and i k.flux (models.jl:330,
+// density_stratification_types.jl) in shared memory, then written scaled.
+// grid (KXP/TX, NYR); shared memory: the pair plane(s), then with LES / density
+// [3][NZR][TX] i k.tau and [NZR][TX] i k.flux (aux_bytes())
 // ------------------------------------------------------------------------------------
+template <int TX> size_t fwd_z2_aux_bytes(int NZR) { return sizeof(cplx<float>) * (size_t)4 * NZR * TX; }
+
 template <int N, int LP>
 __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& F, int mode, const Blk bk) {
   using T = float;
@@ -167,6 +172,9 @@ __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<float2>* s0 = reinterpret_cast<cplx<float2>*>(smem_raw);
   cplx<float2>* s1 = s0 + N * LP;
+  cplx<T>* accT = reinterpret_cast<cplx<T>*>(s0 + (size_t)N * LP * (CtPlan<N>::np >= 3 ? 2 : 1));
+  const int NZR = I.NZR;
+  cplx<T>* accF = accT + 3 * NZR * TX;
   const long long it = I.st->iteration;
   const bool want_ke = ((it % I.dt_stat) == 0) || (mode == 0 && (it % I.dt_spec) == 0);
   const int kx0 = bk.x * TX, jc = bk.y;
@@ -175,29 +183,69 @@ __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& 
   const float2 sc = make_float2(I.inv_n_t, I.inv_n_t);
   cplx<T>* out = I.sbuf + (long long)jc * I.KXP + kx0;   // + c * cs + kc * rowstride + l
   const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
-  int s_nx = 0, s_ny = 1, s_nz = 2, s_ke = -1;
+  const bool aux = I.les || I.density;
+  if (aux) {
+    for (int e = threadIdx.x; e < 4 * NZR * TX; e += blockDim.x) accT[e] = mk(T(0), T(0));
+    __syncthreads();
+  }
+  const T iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
+  const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
+#pragma unroll 1
   for (int fi = 0; fi < F.n; ++fi) {
     const int role = F.code[fi];
-    if (role == R_NX) s_nx = F.slot[fi];
-    else if (role == R_NY) s_ny = F.slot[fi];
-    else if (role == R_NZ) s_nz = F.slot[fi];
-    else if (role == R_KE) s_ke = F.slot[fi];
-  }
-  const int nc = (want_ke && s_ke >= 0) ? 4 : 3;
-#pragma unroll 1
-  for (int c = 0; c < nc; ++c) {
-    const int sl = c == 0 ? s_nx : (c == 1 ? s_ny : (c == 2 ? s_nz : s_ke));
-    const cplx<T>* in = I.wz + (long long)sl * I.wzs + (long long)jc * I.KXP + kx0;
-    cplx<T>* o = out + (long long)c * cs;   // the kinetic energy goes to slot 3 of the scratch spectrum
+    if (role == R_KE && !want_ke) continue;
+    const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)jc * I.KXP + kx0;
     auto ld = [&](int lp, int z) -> cplx<float2> { return ldg_pair(in + (long long)z * rowstride + 2 * lp); };
-    auto st = [&](int lp, int z, cplx<float2> v) {
-      const int kc = zcomp(I, z);
-      if (kc < 0) return;
-      cplx<float2> r = mk(v.x * sc, v.y * sc);
-      if (c < 3 && kzero_col && lp == 0 && z == 0) { r.x.x = 0.f; r.y.x = 0.f; }   // rhs.c[1] = 0 (models.jl:174)
-      st_pair(o + (long long)kc * rowstride + 2 * lp, r);
-    };
-    fft_lines_ct2<-1, LP, N>(s0, s1, I.twz, ld, st);
+    if (role <= R_KE) {   // N components and the kinetic energy: scratch slots 0..3
+      const int c = role;
+      cplx<T>* o = out + (long long)c * cs;
+      auto st = [&](int lp, int z, cplx<float2> v) {
+        const int kc = zcomp(I, z);
+        if (kc < 0) return;
+        cplx<float2> r = mk(v.x * sc, v.y * sc);
+        if (c < 3 && kzero_col && lp == 0 && z == 0) { r.x.x = 0.f; r.y.x = 0.f; }   // rhs.c[1] = 0 (models.jl:174)
+        st_pair(o + (long long)kc * rowstride + 2 * lp, r);
+      };
+      fft_lines_ct2<-1, LP, N>(s0, s1, I.twz, ld, st);
+    } else {   // stress / flux: accumulate i k . tau (traceless symmetric, zz = -xx - yy), i k . flux
+      auto st = [&](int lp, int z, cplx<float2> v) {
+        const int kc = zcomp(I, z);
+        if (kc < 0) return;
+        const int m = kc * TX + 2 * lp;
+        const T kz = kval(zsig(I, kc), Lz, iLz);
+        const T kxa = T(kx0 + 2 * lp) * iLx, kxb = T(kx0 + 2 * lp + 1) * iLx;
+        // d += i k v for both lines of the pair (k per line)
+        auto add = [&](cplx<T>* d, T ka, T kb) {
+          d[0].x -= ka * v.y.x; d[0].y += ka * v.x.x;
+          d[1].x -= kb * v.y.y; d[1].y += kb * v.x.y;
+        };
+        cplx<T>* t0 = accT + m;
+        cplx<T>* t1 = accT + NZR * TX + m;
+        cplx<T>* t2 = accT + 2 * NZR * TX + m;
+        switch (role) {
+          case R_TXX: add(t0, kxa, kxb); add(t2, -kz, -kz); break;
+          case R_TXY: add(t0, kyv, kyv); add(t1, kxa, kxb); break;
+          case R_TXZ: add(t0, kz, kz); add(t2, kxa, kxb); break;
+          case R_TYY: add(t1, kyv, kyv); add(t2, -kz, -kz); break;
+          case R_TYZ: add(t1, kz, kz); add(t2, kyv, kyv); break;
+          case R_FX: add(accF + m, kxa, kxb); break;
+          case R_FY: add(accF + m, kyv, kyv); break;
+          default: add(accF + m, kz, kz); break;
+        }
+      };
+      fft_lines_ct2<-1, LP, N>(s0, s1, I.twz, ld, st);
+    }
+  }
+  if (aux) {
+    for (int m = threadIdx.x; m < NZR * TX; m += blockDim.x) {
+      const int l = m % TX, kc = m / TX;
+      const long long o = (long long)kc * rowstride + l;
+      if (I.les) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) out[(4 + c) * cs + o] = scl(accT[c * NZR * TX + m], I.inv_n_t);
+      }
+      if (I.density) out[7 * cs + o] = scl(accF[m], I.inv_n_t);
+    }
   }
 }
 template <int N, int LP>

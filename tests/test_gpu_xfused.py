@@ -88,14 +88,16 @@ def les_dict(n, den):
     return d
 
 
-@pytest.mark.parametrize("n,den", [(64, False), (128, False), (64, True), (128, True)])
-def test_les_fused_matches_generic(gpu_pkg, n, den):
+@pytest.mark.parametrize("n,den,variant", [(64, False, 0), (128, False, 0), (64, True, 0), (128, True, 0),
+                                           (128, True, 3)])
+def test_les_fused_matches_generic(gpu_pkg, n, den, variant):
     """The twelve-field register-fused x pass (Smagorinsky LES, with and without
-    Boussinesq density; n = 64, 128) against the generic x pass."""
+    Boussinesq density; n = 64, 128) and the line-pair forward z pass with the stress and
+    flux fields (128; variant 3: one line per thread) against the generic kernels."""
     d = les_dict(n, den)
     u = gpu_pkg.random_spectrum(n, k0=3.0, seed=13)
     sims = []
-    for variant in (0, 1):
+    for variant in (variant, 1):
         p = gpu_pkg.parameters(d, precision="FP32")
         p.kernel_variant = variant
         sim = gpu_pkg.Simulation(p)
