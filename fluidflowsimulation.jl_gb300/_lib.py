@@ -19,7 +19,7 @@ FFS_FP64, FFS_FP32 = 0, 1
 EXPORTS = [
     "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_get_fields",
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
-    "ffs_stats_records", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
+    "ffs_stats_records", "ffs_stats", "ffs_spectrum", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_tuning_report",
     "ffs_stream",
     "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
@@ -105,6 +105,8 @@ def load() -> ctypes.CDLL:
         "ffs_stats_ncols": (c_int32, [H]),
         "ffs_record_ncols": (c_int32, [H]),
         "ffs_stats_records": (c_int64, [H, D, c_int64]),
+        "ffs_stats": (c_int32, [H, D, c_int32]),
+        "ffs_spectrum": (c_int32, [H, D, D, c_int64, c_int64]),
         "ffs_spectrum_lengths": (c_int32, [H, POINTER(c_int32), POINTER(c_int32)]),
         "ffs_spectrum_fields": (c_int32, [H, c_char_p, c_int64]),
         "ffs_spectrum_records": (c_int64, [H, D, c_int64]),

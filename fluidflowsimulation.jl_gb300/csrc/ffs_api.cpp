@@ -140,6 +140,30 @@ int64_t ffs_stats_records(ffs_handle* h, double* out, int64_t max_rows) {
   return n;
 }
 
+int ffs_stats(ffs_handle* h, double* row, int32_t ncols) {
+  if (!h || !row) return FFS_EINVAL;
+  const auto& r = h->eng->last_rec;
+  if (r.empty()) {
+    h->err = "no stats record yet (stats are taken at iterations that are multiples of dtStat)";
+    return FFS_ESTATE;
+  }
+  if (ncols < h->eng->ncols_stats) {
+    h->err = "row buffer shorter than the Stats.txt columns";
+    return FFS_EINVAL;
+  }
+  memcpy(row, r.data(), sizeof(double) * h->eng->ncols_stats);
+  return FFS_OK;
+}
+
+int ffs_spectrum(ffs_handle* h, double* specH, double* specV, int64_t lenH, int64_t lenV) {
+  if (!h || !specH || !specV) return FFS_EINVAL;
+  if (lenH != h->eng->lenH || lenV != h->eng->lenV) {
+    h->err = "spectrum lengths differ from ffs_spectrum_lengths";
+    return FFS_EINVAL;
+  }
+  return guarded(h, [&] { return h->eng->spectrum_u(specH, specV, h->err); });
+}
+
 int ffs_spectrum_lengths(const ffs_handle* h, int32_t* lenH, int32_t* lenV) {
   if (!h || !lenH || !lenV) return FFS_EINVAL;
   *lenH = h->eng->lenH;

@@ -823,6 +823,23 @@ class Engine : public EngineBase {
     return 0;
   }
 
+  int spectrum_u(double* H, double* V, std::string& err) override {
+    const int stride = std::max(lenH, lenV);
+    double* d = nullptr;
+    FFS_CK(cudaMalloc(&d, sizeof(double) * 2 * stride));
+    cudaError_t e = cudaMemsetAsync(d, 0, sizeof(double) * 2 * stride, s);
+    if (e == cudaSuccess) {
+      k_spectrum_u<T><<<std::max(1, std::min(n_sms * 4, (int)((I.cstride + 255) / 256))), 256, 0, s>>>(I, d, stride);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(H, d, sizeof(double) * lenH, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(V, d + stride, sizeof(double) * lenV, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(d);
+    if (e != cudaSuccess) { err = std::string("spectrum: ") + cudaGetErrorString(e); return FFS_ECUDA; }
+    return 0;
+  }
+
   int set_spectral(int comp, const double* in, std::string& err) override {
     if (comp < 0 || comp >= I.ncomp) { err = "component out of range"; return FFS_EINVAL; }
     std::vector<cplx<T>> h((size_t)I.cstride);
@@ -886,6 +903,8 @@ class Engine : public EngineBase {
       const size_t off = rec_host.size();
       rec_host.resize(off + (size_t)nrec * I.ncols);
       FFS_CK(cudaMemcpyAsync(rec_host.data() + off, I.records, sizeof(double) * nrec * I.ncols, cudaMemcpyDeviceToHost, s));
+      FFS_CK(cudaStreamSynchronize(s));
+      last_rec.assign(rec_host.end() - I.ncols, rec_host.end());
     }
     const long long nsp = std::min<long long>(hs.nspec, I.spec_cap);
     const int stride = std::max(lenH, lenV);

@@ -39,6 +39,8 @@ class EngineBase {
   virtual int step(int64_t n, std::string& err) = 0;
   virtual int get_fields(double* u1, double* u2, double* u3, double* rho, int layout, std::string& err) = 0;
   virtual int get_spectral(int comp, double* out, std::string& err) = 0;
+  // u spectrum of the current state: H (lenH) horizontal bins, V (lenV) vertical bins
+  virtual int spectrum_u(double* H, double* V, std::string& err) = 0;
   virtual int set_spectral(int comp, const double* in, std::string& err) = 0;
   virtual int time_steps(int64_t n, double* ms, std::string& err) = 0;
   virtual int profile(int64_t n, std::vector<KernelTiming>& out, std::string& err) = 0;
@@ -62,6 +64,7 @@ class EngineBase {
   int nspecf = 4;                  // spectrum fields per record
   std::string spec_names;          // their names, comma-separated
   std::vector<double> rec_host;    // drained stats records
+  std::vector<double> last_rec;    // the most recent stats record (kept when rec_host is read)
   std::vector<double> spec_host;   // drained spectrum records (iteration + 4 spectra)
   int64_t iteration = 0;
   double time = 0.0, dt = 0.0;

@@ -822,6 +822,32 @@ __device__ __forceinline__ void spec_bin(const Inst<T>& I, double* f, int stride
   }
 }
 
+// u spectrum of the current state on demand (ffs_spectrum): spectrum_u +
+// calculate_specHV (spec.jl:316-327, 424-450) of the total energy 1/2 |u|^2, i.e. the
+// reference's u.specH on the horizontal bins and u_h.specV + u_v.specV on the vertical
+// ones. out: [stride] H then [stride] V, zeroed by the caller; FP64 bins.
+template <typename T>
+__global__ void k_spectrum_u(Inst<T> I, double* out, int stride) {
+  const long long cs = I.cstride;
+  const T Lx = I.Lx_t, iLx = I.iLx_t, Ly = I.Ly_t, iLy = I.iLy_t, Lz = I.Lz_t, iLz = I.iLz_t;
+  for (unsigned g = blockIdx.x * blockDim.x + threadIdx.x; g < (unsigned)cs; g += gridDim.x * blockDim.x) {
+    int ix, jc, kc;
+    decomp(I, g, ix, jc, kc);
+    if (ix >= I.Mx) continue;
+    const T kx = kval(ix, Lx, iLx), ky = kval(ysig(I, jc), Ly, iLy), kz = kval(zsig(I, kc), Lz, iLz);
+    double ee = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const cplx<T> u = I.uh[c * cs + g];
+      ee += (double)u.x * u.x + (double)u.y * u.y;
+    }
+    ee *= 0.5;
+    const int nk = (int)rint(fabs((double)kz) / I.dkz), nj = (int)rint(fabs((double)ky) / I.maxdkh);
+    const int nx = (int)rint(fabs((double)kx) / I.maxdkh);
+    spec_bin(I, out, stride, ee, ix, nx, nj, nk);
+  }
+}
+
 // ====================================================================================
 // Stats and spectra of the state before the update: u from the spectral state, N, ke,
 // i k.tau from the scratch buffer written by k_fwd_z (stats.jl:64-219,

@@ -131,6 +131,23 @@ function records(e::Engine)
 end
 statsncols(e::Engine) = Int(ccall((:ffs_stats_ncols, LIB), Cint, (Ptr{Cvoid},), e.h))
 
+# the Stats.txt row of the most recent stats iteration (pending records stay pending)
+function stats(e::Engine)
+    row = Vector{Float64}(undef, statsncols(e))
+    check(e, ccall((:ffs_stats, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Cint), e.h, row, length(row)))
+    return row
+end
+
+# u spectrum of the current state: (u.specH, u_h.specV + u_v.specV) (spec.jl:316-327, 424-450)
+function spectrum(e::Engine)
+    lh, lv = Ref{Cint}(0), Ref{Cint}(0)
+    check(e, ccall((:ffs_spectrum_lengths, LIB), Cint, (Ptr{Cvoid}, Ref{Cint}, Ref{Cint}), e.h, lh, lv))
+    H, V = Vector{Float64}(undef, lh[]), Vector{Float64}(undef, lv[])
+    check(e, ccall((:ffs_spectrum, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Int64, Int64),
+                   e.h, H, V, length(H), length(V)))
+    return H, V
+end
+
 # Scales.txt / Numbers.txt rows of one record (stats.jl:64-165)
 function scalesnumbers(r, names, ns, p::FFSParams)
     col(n) = r[findfirst(==(n), names)]

@@ -134,6 +134,20 @@ class Simulation:
     def stats_rows(self) -> np.ndarray:
         return self.records()[:, : self.ncols]
 
+    def stats(self) -> np.ndarray:
+        """The Stats.txt row of the most recent stats iteration (``ffs_stats``); pending
+        records stay available to ``records``/``stats_rows``."""
+        out = np.empty(self.ncols)
+        self._check(self._L.ffs_stats(self._h, out.ctypes.data_as(_D), self.ncols))
+        return out
+
+    def spectrum(self) -> tuple[np.ndarray, np.ndarray]:
+        """u spectrum of the current state (``ffs_spectrum``): the reference's u.specH on
+        the horizontal bins and u_h.specV + u_v.specV on the vertical bins."""
+        H, V = np.empty(self.lenH), np.empty(self.lenV)
+        self._check(self._L.ffs_spectrum(self._h, H.ctypes.data_as(_D), V.ctypes.data_as(_D), self.lenH, self.lenV))
+        return H, V
+
     def scales_numbers(self, records: np.ndarray) -> tuple[list[list[float]], list[list[float]]]:
         """Scales.txt and Numbers.txt rows (with iteration and time) of drained records."""
         p = self.params

@@ -129,6 +129,15 @@ int64_t ffs_stats_records(ffs_handle* h, double* out, int64_t max_rows);
  * hvis_h, hvis_v with hyperviscosity, buoyancy_v, rho, rhodiss, rhonl with density) and
  * returns their count F. A record is [iteration, then per field: specH(lenH), specV(lenV)],
  * 1 + F (lenH + lenV) doubles. */
+/* The Stats.txt row of the most recent stats iteration (writestats, stats.jl:1-62;
+ * ffs_stats_ncols columns), without consuming ffs_stats_records. FFS_ESTATE before the
+ * first stats iteration. */
+int ffs_stats(ffs_handle* h, double* row, int32_t ncols);
+/* u spectrum of the current state (spectrum_u + calculate_specHV, spec.jl:316-327,
+ * 424-450): specH = the reference's u.specH (total 1/2 |u|^2 on the horizontal bins KH),
+ * specV = u_h.specV + u_v.specV (on the vertical bins KRZ). lenH, lenV must equal
+ * ffs_spectrum_lengths. */
+int ffs_spectrum(ffs_handle* h, double* specH, double* specV, int64_t lenH, int64_t lenV);
 int ffs_spectrum_lengths(const ffs_handle* h, int32_t* lenH, int32_t* lenV);
 int ffs_spectrum_fields(const ffs_handle* h, char* buf, int64_t len);
 int64_t ffs_spectrum_records(ffs_handle* h, double* out, int64_t max_rows);

@@ -249,3 +249,29 @@ def test_scales_and_numbers_parity(gpu_pkg, name):
         scale = np.maximum(np.abs(want[ok]), 1e-6 * np.abs(want[ok]).max())
         assert (np.abs(got[ok] - want[ok]) / scale).max() <= FP64_STATS_TOL, name
     sim.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("FP64", 1e-10), ("FP32", 1e-4)])
+def test_current_stats_and_spectrum(gpu_pkg, precision, tol):
+    """ffs_stats (the latest Stats.txt row, left in the pending records) and ffs_spectrum
+    (u spectrum of the current state: u.specH and u_h.specV + u_v.specV) against the
+    drained rows and the oracle's spectrum_u of the same state."""
+    d = gdict(32, integ="ETD3rdO", dtStat=1)
+    u, _ = make_ic(gpu_pkg, d)
+    sim = gpu_pkg.Simulation.from_global(d, precision=precision)
+    sim.set_fields(*u)
+    sim.initialize()
+    with pytest.raises(gpu_pkg.FFSError):   # no stats iteration yet
+        sim.stats()
+    sim.advance_in_time(3)
+    last = sim.stats()
+    rows = sim.stats_rows()
+    assert rows.shape[0] == 3 and np.array_equal(last, rows[-1])
+    H, V = sim.spectrum()
+    ref = OracleSimulation(Params.from_global(d), u)
+    ref.initialize()
+    ref.run(3)
+    sp = ref.spectrum_u()
+    assert rel(H, sp["u.specH"]) <= tol
+    assert rel(V, sp["u_h.specV"] + sp["u_v.specV"]) <= tol
+    sim.close()
