@@ -168,8 +168,11 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
     fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
   }
 }
+// with a compile-time plan the CTA has exactly TX * ct_tpl threads; the register cap
+// lets 9 CTAs share an SM
 template <typename T, int TX, int N = 0>
-__global__ void __launch_bounds__(FFS_MAXT) k_inv_z(Inst<T> I, FieldList F) {
+__global__ void __launch_bounds__(N > 0 ? TX * ct_tpl<(N > 0 ? N : 128)>() : FFS_MAXT, N > 0 ? 9 : 1)
+k_inv_z(Inst<T> I, FieldList F) {
   b_inv_z<T, TX, N>(I, F, Blk::here());
 }
 
