@@ -8,6 +8,7 @@
 
 #include "../../include/ffs.h"
 #include "ffs_batch.cuh"
+#include "ffs_pairs.cuh"
 #include "ffs_xfused.cuh"
 #include "ffs_xles.cuh"
 
@@ -32,6 +33,25 @@ kb_x_les(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__
   FFS_BATCH_END
 }
 
+// forward y and z passes on line pairs (packed FP32; n >= 64, where a CTA is at least a
+// warp)
+template <int N, int CI>
+__global__ void __launch_bounds__(PAIR_LP * ct_tpl<N>())
+kb_fwd_y2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  using T = float;
+  FFS_BATCH_LOOP(BP_FWD_Y)
+  b_fwd_y2<N, PAIR_LP>(BI.I, BI.fwd, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
+template <int N, int CI>
+__global__ void __launch_bounds__(PAIR_LP * ct_tpl<N>())
+kb_fwd_z2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  using T = float;
+  FFS_BATCH_LOOP(BP_FWD_Z)
+  b_fwd_z2<N, PAIR_LP>(BI.I, BI.fwd, 0, Blk{it.x, it.y, 0, 0});
+  FFS_BATCH_END
+}
+
 template <int N, int CI>
 struct BatchClass {
   static constexpr int TX = BATCH_TX, LYZ = BATCH_LYZ;
@@ -39,6 +59,8 @@ struct BatchClass {
   static constexpr int nbuf = CtPlan<N>::np >= 3 ? 2 : 1;
   static constexpr bool FUSED = N == 64 || N == 128;    // velocity-only fused x pass
   static constexpr bool LESF = N == 64 || N == 128;     // LES fused x pass
+  static constexpr bool PAIRF = N >= 64;                 // forward y/z passes on line pairs
+  static_assert(2 * PAIR_LP == TX, "line pairs cover the TX lines of a tile");
 
   // per-kernel limits are process-wide: only ever raised, under a lock
   template <typename K> static int attr(K k, size_t bytes, std::string* err) {
@@ -79,6 +101,12 @@ struct BatchClass {
     else { L->block[BP_X_LES] = 6 * LYZ * tpl; L->smem[BP_X_LES] = xs(11); }
     L->block[BP_FWD_Z] = 3 * TX * tpl;
     L->smem[BP_FWD_Z] = cb * ((size_t)3 * TX * srows(N) * nbuf + (size_t)4 * N * TX);
+    if (PAIRF) {   // (the i k.tau accumulators for NZR <= N rows)
+      constexpr int NP = PAIRF ? N : 64;
+      L->block[BP_FWD_Y] = L->block[BP_FWD_Z] = PAIR_LP * ct_tpl<NP>();
+      L->smem[BP_FWD_Y] = pair_smem<NP, PAIR_LP>();
+      L->smem[BP_FWD_Z] = pair_smem<NP, PAIR_LP>() + fwd_z2_aux_bytes<TX>(N);
+    }
     L->block[BP_SCALAR] = 256; L->block[BP_TABLE] = 64; L->block[BP_STATS] = 256; L->block[BP_UPDATE] = 256;
     L->block[BP_FIN] = 1024;
     L->smem[BP_SCALAR] = L->smem[BP_TABLE] = L->smem[BP_STATS] = L->smem[BP_UPDATE] = L->smem[BP_FIN] = 0;
@@ -86,9 +114,18 @@ struct BatchClass {
     const int big = 1 << 30;
     if ((rc = attr(kb_inv_z<float, TX, CI, N>, L->smem[BP_INV_Z], err)) ||
         (rc = attr(kb_inv_y<float, TX, CI, N>, L->smem[BP_INV_Y], err)) ||
-        (rc = attr(kb_fwd_y<float, TX, CI, N>, L->smem[BP_FWD_Y], err)) ||
-        (rc = attr(kb_fwd_z<float, TX, CI, N>, L->smem[BP_FWD_Z], err)))
+        (rc = PAIRF ? 0 : attr(kb_fwd_y<float, TX, CI, N>, L->smem[BP_FWD_Y], err)) ||
+        (rc = PAIRF ? 0 : attr(kb_fwd_z<float, TX, CI, N>, L->smem[BP_FWD_Z], err)))
       return rc;
+    if constexpr (PAIRF) {
+      if ((rc = attr(kb_fwd_y2<N, CI>, L->smem[BP_FWD_Y], err)) || (rc = attr(kb_fwd_z2<N, CI>, L->smem[BP_FWD_Z], err)) ||
+          (rc = occ(kb_fwd_y2<N, CI>, L, BP_FWD_Y, sms, big, err)) || (rc = occ(kb_fwd_z2<N, CI>, L, BP_FWD_Z, sms, big, err)))
+        return rc;
+    } else {
+      if ((rc = occ(kb_fwd_y<float, TX, CI, N>, L, BP_FWD_Y, sms, big, err)) ||
+          (rc = occ(kb_fwd_z<float, TX, CI, N>, L, BP_FWD_Z, sms, big, err)))
+        return rc;
+    }
     if constexpr (LESF) {
       if ((rc = attr(kb_x_les<N, CI>, L->smem[BP_X_LES], err))) return rc;
       if ((rc = occ(kb_x_les<N, CI>, L, BP_X_LES, sms, big, err))) return rc;
@@ -105,10 +142,8 @@ struct BatchClass {
     }
     if ((rc = occ(kb_inv_z<float, TX, CI, N>, L, BP_INV_Z, sms, big, err)) ||
         (rc = occ(kb_inv_y<float, TX, CI, N>, L, BP_INV_Y, sms, big, err)) ||
-        (rc = occ(kb_fwd_y<float, TX, CI, N>, L, BP_FWD_Y, sms, big, err)) ||
         (rc = occ(kb_scalar<float, CI>, L, BP_SCALAR, sms, max_active, err)) ||
         (rc = occ(kb_table<float, CI>, L, BP_TABLE, sms, big, err)) ||
-        (rc = occ(kb_fwd_z<float, TX, CI, N>, L, BP_FWD_Z, sms, big, err)) ||
         (rc = occ(kb_stats<float, CI>, L, BP_STATS, sms, big, err)) ||
         (rc = occ(kb_update<float, CI>, L, BP_UPDATE, sms, big, err)) ||
         (rc = occ(kb_finalize<float, CI>, L, BP_FIN, sms, max_active, err)))
@@ -124,10 +159,12 @@ struct BatchClass {
     else kb_x<float, false, LYZ, CI, N><<<FFS_CL(BP_X)>>>(B, T);
     if constexpr (LESF) kb_x_les<N, CI><<<FFS_CL(BP_X_LES)>>>(B, T);
     else kb_x<float, true, LYZ, CI, N><<<FFS_CL(BP_X_LES)>>>(B, T);
-    kb_fwd_y<float, TX, CI, N><<<FFS_CL(BP_FWD_Y)>>>(B, T);
+    if constexpr (PAIRF) kb_fwd_y2<N, CI><<<FFS_CL(BP_FWD_Y)>>>(B, T);
+    else kb_fwd_y<float, TX, CI, N><<<FFS_CL(BP_FWD_Y)>>>(B, T);
     kb_scalar<float, CI><<<FFS_CL(BP_SCALAR)>>>(B, T);
     kb_table<float, CI><<<FFS_CL(BP_TABLE)>>>(B, T);
-    kb_fwd_z<float, TX, CI, N><<<FFS_CL(BP_FWD_Z)>>>(B, T);
+    if constexpr (PAIRF) kb_fwd_z2<N, CI><<<FFS_CL(BP_FWD_Z)>>>(B, T);
+    else kb_fwd_z<float, TX, CI, N><<<FFS_CL(BP_FWD_Z)>>>(B, T);
     kb_stats<float, CI><<<FFS_CL(BP_STATS)>>>(B, T);
     kb_update<float, CI><<<FFS_CL(BP_UPDATE)>>>(B, T);
     kb_finalize<float, CI><<<FFS_CL(BP_FIN)>>>(B, T);
