@@ -33,8 +33,23 @@ kb_x_les(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__
   FFS_BATCH_END
 }
 
-// forward y and z passes on line pairs (packed FP32; n >= 64, where a CTA is at least a
-// warp)
+// y and z passes on line pairs (packed FP32; n >= 64, where a CTA is at least a warp)
+template <int N, int CI>
+__global__ void __launch_bounds__(PAIR_LP * ct_tpl<N>())
+kb_inv_z2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  using T = float;
+  FFS_BATCH_LOOP(BP_INV_Z)
+  b_inv_z2<N, PAIR_LP>(BI.I, BI.inv, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
+template <int N, int CI>
+__global__ void __launch_bounds__(PAIR_LP * ct_tpl<N>())
+kb_inv_y2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+  using T = float;
+  FFS_BATCH_LOOP(BP_INV_Y)
+  b_inv_y2<N, PAIR_LP>(BI.I, BI.inv, Blk{it.x, it.y, it.z, 0});
+  FFS_BATCH_END
+}
 template <int N, int CI>
 __global__ void __launch_bounds__(PAIR_LP * ct_tpl<N>())
 kb_fwd_y2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ Tb) {
@@ -59,7 +74,7 @@ struct BatchClass {
   static constexpr int nbuf = CtPlan<N>::np >= 3 ? 2 : 1;
   static constexpr bool FUSED = N == 64 || N == 128;    // velocity-only fused x pass
   static constexpr bool LESF = N == 64 || N == 128;     // LES fused x pass
-  static constexpr bool PAIRF = N >= 64;                 // forward y/z passes on line pairs
+  static constexpr bool PAIRF = N >= 64;                 // y/z passes on line pairs
   static_assert(2 * PAIR_LP == TX, "line pairs cover the TX lines of a tile");
 
   // per-kernel limits are process-wide: only ever raised, under a lock
@@ -103,8 +118,8 @@ struct BatchClass {
     L->smem[BP_FWD_Z] = cb * ((size_t)3 * TX * srows(N) * nbuf + (size_t)4 * N * TX);
     if (PAIRF) {   // (the i k.tau accumulators for NZR <= N rows)
       constexpr int NP = PAIRF ? N : 64;
-      L->block[BP_FWD_Y] = L->block[BP_FWD_Z] = PAIR_LP * ct_tpl<NP>();
-      L->smem[BP_FWD_Y] = pair_smem<NP, PAIR_LP>();
+      L->block[BP_FWD_Y] = L->block[BP_FWD_Z] = L->block[BP_INV_Z] = L->block[BP_INV_Y] = PAIR_LP * ct_tpl<NP>();
+      L->smem[BP_FWD_Y] = L->smem[BP_INV_Z] = L->smem[BP_INV_Y] = pair_smem<NP, PAIR_LP>();
       L->smem[BP_FWD_Z] = pair_smem<NP, PAIR_LP>() + fwd_z2_aux_bytes<TX>(N);
     }
     L->block[BP_SCALAR] = 256; L->block[BP_TABLE] = 64; L->block[BP_STATS] = 256; L->block[BP_UPDATE] = 256;
@@ -112,18 +127,22 @@ struct BatchClass {
     L->smem[BP_SCALAR] = L->smem[BP_TABLE] = L->smem[BP_STATS] = L->smem[BP_UPDATE] = L->smem[BP_FIN] = 0;
     int rc;
     const int big = 1 << 30;
-    if ((rc = attr(kb_inv_z<float, TX, CI, N>, L->smem[BP_INV_Z], err)) ||
-        (rc = attr(kb_inv_y<float, TX, CI, N>, L->smem[BP_INV_Y], err)) ||
+    if ((rc = PAIRF ? 0 : attr(kb_inv_z<float, TX, CI, N>, L->smem[BP_INV_Z], err)) ||
+        (rc = PAIRF ? 0 : attr(kb_inv_y<float, TX, CI, N>, L->smem[BP_INV_Y], err)) ||
         (rc = PAIRF ? 0 : attr(kb_fwd_y<float, TX, CI, N>, L->smem[BP_FWD_Y], err)) ||
         (rc = PAIRF ? 0 : attr(kb_fwd_z<float, TX, CI, N>, L->smem[BP_FWD_Z], err)))
       return rc;
     if constexpr (PAIRF) {
       if ((rc = attr(kb_fwd_y2<N, CI>, L->smem[BP_FWD_Y], err)) || (rc = attr(kb_fwd_z2<N, CI>, L->smem[BP_FWD_Z], err)) ||
-          (rc = occ(kb_fwd_y2<N, CI>, L, BP_FWD_Y, sms, big, err)) || (rc = occ(kb_fwd_z2<N, CI>, L, BP_FWD_Z, sms, big, err)))
+          (rc = occ(kb_fwd_y2<N, CI>, L, BP_FWD_Y, sms, big, err)) || (rc = occ(kb_fwd_z2<N, CI>, L, BP_FWD_Z, sms, big, err)) ||
+          (rc = attr(kb_inv_z2<N, CI>, L->smem[BP_INV_Z], err)) || (rc = attr(kb_inv_y2<N, CI>, L->smem[BP_INV_Y], err)) ||
+          (rc = occ(kb_inv_z2<N, CI>, L, BP_INV_Z, sms, big, err)) || (rc = occ(kb_inv_y2<N, CI>, L, BP_INV_Y, sms, big, err)))
         return rc;
     } else {
       if ((rc = occ(kb_fwd_y<float, TX, CI, N>, L, BP_FWD_Y, sms, big, err)) ||
-          (rc = occ(kb_fwd_z<float, TX, CI, N>, L, BP_FWD_Z, sms, big, err)))
+          (rc = occ(kb_fwd_z<float, TX, CI, N>, L, BP_FWD_Z, sms, big, err)) ||
+          (rc = occ(kb_inv_z<float, TX, CI, N>, L, BP_INV_Z, sms, big, err)) ||
+          (rc = occ(kb_inv_y<float, TX, CI, N>, L, BP_INV_Y, sms, big, err)))
         return rc;
     }
     if constexpr (LESF) {
@@ -140,9 +159,7 @@ struct BatchClass {
       if ((rc = attr(kb_x<float, false, LYZ, CI, N>, L->smem[BP_X], err))) return rc;
       if ((rc = occ(kb_x<float, false, LYZ, CI, N>, L, BP_X, sms, big, err))) return rc;
     }
-    if ((rc = occ(kb_inv_z<float, TX, CI, N>, L, BP_INV_Z, sms, big, err)) ||
-        (rc = occ(kb_inv_y<float, TX, CI, N>, L, BP_INV_Y, sms, big, err)) ||
-        (rc = occ(kb_scalar<float, CI>, L, BP_SCALAR, sms, max_active, err)) ||
+    if ((rc = occ(kb_scalar<float, CI>, L, BP_SCALAR, sms, max_active, err)) ||
         (rc = occ(kb_table<float, CI>, L, BP_TABLE, sms, big, err)) ||
         (rc = occ(kb_stats<float, CI>, L, BP_STATS, sms, big, err)) ||
         (rc = occ(kb_update<float, CI>, L, BP_UPDATE, sms, big, err)) ||
@@ -153,8 +170,13 @@ struct BatchClass {
 
   static void enqueue(const ClassLaunch& L, cudaStream_t s, const BatchInst<float>* B, const BatchTables* T) {
 #define FFS_CL(PH) L.grid[PH], L.block[PH], L.smem[PH], s
-    kb_inv_z<float, TX, CI, N><<<FFS_CL(BP_INV_Z)>>>(B, T);
-    kb_inv_y<float, TX, CI, N><<<FFS_CL(BP_INV_Y)>>>(B, T);
+    if constexpr (PAIRF) {
+      kb_inv_z2<N, CI><<<FFS_CL(BP_INV_Z)>>>(B, T);
+      kb_inv_y2<N, CI><<<FFS_CL(BP_INV_Y)>>>(B, T);
+    } else {
+      kb_inv_z<float, TX, CI, N><<<FFS_CL(BP_INV_Z)>>>(B, T);
+      kb_inv_y<float, TX, CI, N><<<FFS_CL(BP_INV_Y)>>>(B, T);
+    }
     if constexpr (FUSED) kb_x_fused<N, CI><<<FFS_CL(BP_X)>>>(B, T);
     else kb_x<float, false, LYZ, CI, N><<<FFS_CL(BP_X)>>>(B, T);
     if constexpr (LESF) kb_x_les<N, CI><<<FFS_CL(BP_X_LES)>>>(B, T);
