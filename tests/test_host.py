@@ -27,6 +27,15 @@ def test_library_exports_every_declared_symbol(pkg):
         assert hasattr(L, n), n
 
 
+def test_julia_binding_calls_only_declared_symbols():
+    """Every entry point the Julia ccall shim binds is declared in include/ffs.h (the shim
+    cannot run here: no Julia in the image)."""
+    src = (ROOT / "fluidflowsimulation.jl_gb300" / "julia" / "FFSEngine.jl").read_text()
+    called = set(re.findall(r"ccall\(\(:(ffs_[a-z_]+)", src))
+    assert called, "no ccall found"
+    assert called <= set(header_functions()), sorted(called - set(header_functions()))
+
+
 def test_params_default_matches_reference_defaults(pkg):
     p = pkg.FFSParams()
     assert pkg.load().ffs_params_default(ctypes.byref(p)) == 0
