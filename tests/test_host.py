@@ -36,6 +36,22 @@ def test_julia_binding_calls_only_declared_symbols():
     assert called <= set(header_functions()), sorted(called - set(header_functions()))
 
 
+def test_julia_params_struct_matches_header():
+    """The Julia FFSParams mirrors ffs_params field by field (names, order, C types)."""
+    h = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / "ffs.h").read_text(), flags=re.S)
+    body = re.search(r"typedef struct ffs_params \{(.*?)\} ffs_params;", h, flags=re.S).group(1)
+    cfields = []
+    for decl in body.split(";"):
+        m = re.match(r"\s*(int32_t|int64_t|double)\s+(.+)", decl.strip())
+        if m:
+            cfields += [(n.strip(), m.group(1)) for n in m.group(2).split(",")]
+    jl = (ROOT / "fluidflowsimulation.jl_gb300" / "julia" / "FFSEngine.jl").read_text()
+    jbody = re.search(r"mutable struct FFSParams(.*?)FFSParams\(\) = new\(\)", jl, flags=re.S).group(1)
+    jmap = {"Int32": "int32_t", "Int64": "int64_t", "Float64": "double"}
+    jfields = [(n, jmap[t]) for n, t in re.findall(r"(\w+)::(\w+)", jbody)]
+    assert jfields == cfields
+
+
 def test_params_default_matches_reference_defaults(pkg):
     p = pkg.FFSParams()
     assert pkg.load().ffs_params_default(ctypes.byref(p)) == 0
