@@ -71,7 +71,7 @@ def test_batch_invariance(gpu_pkg):
         assert np.allclose(sa, sm, rtol=1e-12, atol=1e-12 * np.abs(sm).max()), case
 
 
-@pytest.mark.parametrize("case", [MIX[1], MIX[2], MIX[6]])
+@pytest.mark.parametrize("case", [MIX[1], MIX[2], MIX[3], MIX[6], MIX[7]])
 def test_batched_step_matches_single_engine(gpu_pkg, case):
     n, les, integ, adaptive, nt, seed = case
     d = gdict(n, les, integ, adaptive)
