@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(LP * ct_tpl<N>()) k_fwd_y2(Inst<float> I, Fiel
 // are transformed the same way and accumulated as i k.tau and i k.flux (models.jl:330,
 // density_stratification_types.jl) in shared memory, then written scaled.
 // grid (KXP/TX, NYR); shared memory: the pair plane(s), then with LES / density
-// [3][NZR][TX] i k.tau and [NZR][TX] i k.flux (aux_bytes())
+// [3][NZR][TX] i k.tau and [NZR][TX] i k.flux (fwd_z2_aux_bytes)
 // ------------------------------------------------------------------------------------
 template <int TX> size_t fwd_z2_aux_bytes(int NZR) { return sizeof(cplx<float>) * (size_t)4 * NZR * TX; }
 
