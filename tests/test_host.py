@@ -185,3 +185,21 @@ def test_taylor_green_matches_readme(pkg):
     assert u1[7, 5, 3] == pytest.approx(np.cos(x) * np.sin(y) * np.sin(z))
     assert u2[7, 5, 3] == pytest.approx(-np.sin(x) * np.cos(y) * np.sin(z))
     assert not u3.any()
+
+
+def test_bench_byte_models():
+    """The roofline byte models of bench.py: the 69A effective-bandwidth convention per
+    pass adds up to the step, and the retained-mode minimum counts the pruned sizes
+    C = Mx NYR NZR, V = Mx NYR n, U = Mx n^2 (256^3: Mx = 86, NYR = NZR = 171)."""
+    import sys
+    sys.path.insert(0, str(ROOT))
+    import bench
+    n, elem = 256, 8
+    m = bench.model_bytes(n, elem)
+    A = (n // 2 + 1) * n * n * elem
+    assert m["step"] == 69 * A
+    assert sum(v for k, v in m.items() if k != "step") == m["step"]
+    r = bench.algorithmic_bytes(n, elem)
+    C, V, U = 86 * 171 * 171 * elem, 86 * 171 * n * elem, 86 * n * n * elem
+    assert r["inv_z"] == 3 * C + 6 * V and r["x_pass"] == 9 * U
+    assert r["step"] == 18 * C + 18 * V + 18 * U
