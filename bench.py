@@ -1,11 +1,13 @@
 """Benchmark: steps/s of the pseudo-spectral solver step, forced isotropic DNS 256^3.
 
-Workload (the FP32 chosen form of the forced-DNS configuration): seeded random-phase,
-divergence-free field with E(k) ~ k^4 exp(-2 (k/k0)^2), k0 = 4, u_rms = 1; isotropic band
-forcing |k| <= 2.5 at constant power eps = 0.1; nu = 1e-3; AB3 with adaptive dt (CFL 0.5);
-2/3 dealiasing; stats every 100 steps. A step is one advance_in_time! (one CUDA-graph
-launch of the whole step). The FP64 plain form is timed beside it and the FP32 error
-against FP64 after 10 steps is stated.
+Workload: seeded random-phase, divergence-free field with E(k) ~ k^4 exp(-2 (k/k0)^2),
+k0 = 4, u_rms = 1; isotropic band forcing |k| <= 2.5 at constant power eps = 0.1;
+nu = 1e-3; AB3 with adaptive dt (CFL 0.5); 2/3 dealiasing; stats every 100 steps. A step
+is one advance_in_time! (one CUDA-graph launch of the whole step).
+
+The headline value is the FP64 plain form: the reference's own arithmetic, so it compares
+like for like with the FP64 reference arm (--impl reference). The FP32 chosen form is
+timed beside it (key "fp32") with its error against FP64 after 10 steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--grid n]
 
@@ -15,6 +17,7 @@ path); value = steps of all ranks / max time over ranks.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import math
 import os
@@ -140,18 +143,42 @@ def model_bytes(n: int, elem: int) -> dict[str, float]:
             "step": 69 * A}
 
 
+def retained(n: int) -> tuple[int, int]:
+    """Retained kx count Mx and retained ky (= kz) count NYR of the 2/3 rule on n points."""
+    mx = int(math.floor((2.0 / 3.0) * (n // 2) + 1e-12)) + 1
+    return mx, 2 * mx - 1
+
+
 def algorithmic_bytes(n: int, elem: int) -> dict[str, float]:
-    """Minimal bytes each pass must move for the velocity-only step (retained modes only).
+    """Minimal bytes each pass of the velocity-only step must move (retained modes only):
+    what it has to read and write once, with nothing re-read.
 
     C = Mx*NYR*NZR (compact spectral component), V = Mx*NYR*n (after the z pass),
-    U = Mx*n*n (after the y pass), complex elements of `elem` bytes.
+    U = Mx*n*n (after the y pass), complex elements of `elem` bytes. inv_z reads u (3C)
+    and writes u, w (6V); inv_y 6V -> 6U; the x pass 6U -> 3U; fwd_y 3U -> 3V; fwd_z
+    3V -> 3C; the update reads u, N, fm1, fm2 and writes u and the new rhs (18C).
     """
-    mx = int(math.floor((2.0 / 3.0) * (n // 2) + 1e-12)) + 1
-    nr = 2 * mx - 1
+    mx, nr = retained(n)
     C, V, U = mx * nr * nr * elem, mx * nr * n * elem, mx * n * n * elem
-    return {"inv_z": 3 * C + 6 * V, "inv_y": 6 * V + 6 * U, "x_pass": 6 * U + 3 * U, "fwd_y": 3 * U + 3 * V,
-            "fwd_z_update": 3 * V + 9 * C + 6 * C, "step": 3 * C + 6 * V + 6 * V + 6 * U + 6 * U + 3 * U + 3 * U
-            + 3 * V + 3 * V + 15 * C}
+    k = {"inv_z": 3 * C + 6 * V, "inv_y": 6 * V + 6 * U, "x_pass": 6 * U + 3 * U, "fwd_y": 3 * U + 3 * V,
+         "fwd_z": 3 * V + 3 * C, "update": 18 * C}
+    k["step"] = sum(k.values())
+    return k
+
+
+def algorithmic_flops(n: int) -> dict[str, float]:
+    """Floating-point operations of the transforms each pass performs (velocity-only step),
+    pruned to the retained modes like the kernels: 5 L log2 L per complex line of length L,
+    2.5 L log2 L per real line. The x pass transforms 9 real fields on all n^2 (y,z) lines;
+    the y and z passes only the Mx retained kx columns (and inv_z / fwd_z only the NYR
+    retained ky rows). Pointwise products, projections and the update are not counted."""
+    mx, nr = retained(n)
+    lg = math.log2(n)
+    cl = 5.0 * n * lg
+    f = {"x_pass": 9 * n * n * 2.5 * n * lg, "inv_y": 6 * mx * n * cl, "inv_z": 6 * mx * nr * cl,
+         "fwd_y": 3 * mx * n * cl, "fwd_z": 3 * mx * nr * cl}
+    f["step"] = sum(f.values())
+    return f
 
 
 def dist_setup(args, backend: str = "nccl"):
@@ -497,50 +524,82 @@ def run_reference_arm(args):
     return 0
 
 
+def kernel_roofline_hbm(prof: dict, nprof: int, n: int, elem: int, prec: str, peak: float, peak_kind: str,
+                        ms_step: float) -> dict:
+    """HBM roofline of the dominant kernel of a form: achieved = the kernel's retained-mode
+    algorithmic bytes (what it must read and write once) / its event-timed duration;
+    traffic = its ncu DRAM bytes per launch (profiles/traffic.txt); dram_frac = traffic /
+    duration / peak. The 69A effective-bandwidth figure is kept as a labelled extra."""
+    alg = algorithmic_bytes(n, elem)
+    sb = model_bytes(n, elem)
+    cand = {k: v for k, v in prof.items() if k in alg}
+    top = max(cand, key=cand.get)
+    top_ms = prof[top] / nprof
+    achieved = alg[top] / (top_ms / 1e3) / 1e9
+    traffic = ncu_traffic(top, n, prec)
+    r = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+         "traffic": traffic, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+         "algorithmic_bytes_per_launch": alg[top],
+         "bytes_model": "retained-mode minimum per pass (C = Mx NYR NZR, V = Mx NYR n, U = Mx n^2 complex)",
+         "step_algorithmic_bytes": alg["step"], "step_frac": alg["step"] / (ms_step / 1e3) / 1e9 / peak,
+         "per_kernel_frac": {k: alg[k] / (prof[k] / nprof / 1e3) / 1e9 / peak for k in alg
+                             if k != "step" and prof.get(k, 0) > 0},
+         "effective_69A_frac": sb.get(top, 0.0) / (top_ms / 1e3) / 1e9 / peak}
+    if traffic:
+        r["dram_achieved"] = traffic / (top_ms / 1e3) / 1e9
+        r["dram_frac"] = r["dram_achieved"] / peak
+    return r
+
+
 def run_engine_arm(args):
     import numpy as np
     import __graft_entry__ as ge
     world, rank, local, dist = dist_setup(args)
     pkg = ge.load_package()
-    pkg.load()
+    L = pkg.load()
     n = args.grid
     d = global_dict(n)
     u = pkg.random_spectrum(n, k0=K0, seed=2001)
 
-    def make(prec):
+    def make(prec, autotune=None):
         p = pkg.parameters(d, precision=prec, device=local)
-        p.autotune = 0 if args.no_autotune else 1
+        p.autotune = (0 if args.no_autotune else 1) if autotune is None else autotune
         sim = pkg.Simulation(p)
         sim.set_fields(*u)
         sim.initialize()
         return sim
 
-    # --- device-resident throughput, FP32 chosen form
-    sim = make("FP32")
-    tuning = sim.tuning
-    sim.advance_in_time(max(args.warmup, 3))
+    # --- headline: the FP64 plain form (the reference's arithmetic), inputs resident in HBM
+    sim64 = make("FP64")
+    tuning64 = sim64.tuning
+    sim64.advance_in_time(max(args.warmup, 3))
     cuda_sync()
     barrier(dist)
     with ClockSampler(local) as clk:
-        ms = sim.time_steps(args.steps)
+        ms = sim64.time_steps(args.steps)
     cuda_sync()
     barrier(dist)
     steps_s, ms = replica_rate(dist, world, args.steps, ms)
-    launches = sim.launches_per_step * args.steps
-    prof = sim.profile_kernels(max(5, min(20, args.steps)))
-    nprof = max(5, min(20, args.steps))
-    dev_bytes = sim.device_bytes
-    sim.close()
-
-    # --- FP64 plain form
-    sim64 = make("FP64")
-    sim64.advance_in_time(3)
-    k64 = max(5, args.steps // 10)
-    ms64 = sim64.time_steps(k64)
+    launches = sim64.launches_per_step * args.steps
+    nprof = max(3, min(10, args.steps))
+    prof64 = sim64.profile_kernels(nprof)
+    dev_bytes = sim64.device_bytes
     sim64.close()
 
-    # --- FP32 vs FP64 error after 10 steps (same initial fields)
-    a, b = make("FP32"), make("FP64")
+    # --- the FP32 chosen form on the same initial fields
+    sim = make("FP32")
+    tuning32 = sim.tuning
+    sim.advance_in_time(max(args.warmup, 3))
+    k32 = max(20, min(args.steps * 10, 1000))
+    ms32 = sim.time_steps(k32)
+    nprof32 = max(5, min(20, args.steps))
+    prof32 = sim.profile_kernels(nprof32)
+    launches += sim.launches_per_step * k32
+    sim.close()
+
+    # --- FP32 vs FP64 error after 10 steps (same initial fields; the FP64 engine matches
+    # the oracle to 1e-12 at this size, tests/test_gpu_configs.py)
+    a, b = make("FP32", 0), make("FP64", 0)
     a.advance_in_time(10)
     b.advance_in_time(10)
     err = max(float(np.linalg.norm(a.spectral(c) - b.spectral(c)) / np.linalg.norm(b.spectral(c)))
@@ -548,33 +607,63 @@ def run_engine_arm(args):
     a.close()
     b.close()
 
-    # --- end to end through the public API with host buffers
-    nb = 3 * u[0].nbytes
-    host = [np.ascontiguousarray(x) for x in u]
-    cuda_sync()
-    t0 = time.perf_counter()
-    e = pkg.Simulation(pkg.parameters(d, precision="FP32", device=local))
-    e.set_fields(*host)
-    e.initialize()
-    e.advance_in_time(args.steps)
-    rows = e.stats_rows()
-    out = e.fields()
-    t1 = time.perf_counter()
-    e.close()
-    e2e_s = max_over_ranks(dist, t1 - t0)
+    # --- end to end through the public API with host buffers (the engine already created:
+    # allocation and plans are one-time setup): set_fields from host memory, initialize!,
+    # K steps, the run's tail, the Stats rows and the final fields back to the host
+    def e2e(prec):
+        host = [np.ascontiguousarray(x) for x in u]
+        p = pkg.parameters(d, precision=prec, device=local)
+        e = pkg.Simulation(p)
+        cuda_sync()
+        t0 = time.perf_counter()
+        e.set_fields(*host)
+        e.initialize()
+        e.advance_in_time(args.steps)
+        e.finalize()
+        rows = e.stats_rows()
+        out = e.fields()
+        t1 = time.perf_counter()
+        e.close()
+        return max_over_ranks(dist, t1 - t0), rows.nbytes + sum(x.nbytes for x in out), sum(x.nbytes for x in host)
+
+    e2e_s, d2h, h2d = e2e("FP64")
     e2e_rate = args.steps * world / e2e_s
+    e2e32_s, _, _ = e2e("FP32")
+    launches += (sim.launches_per_step + 1) * (args.steps + 2)
+
+    # --- the FP64 arithmetic peak of this GPU (roofline denominator of the FP64 form)
+    fma_tf, add_tf = ctypes.c_double(), ctypes.c_double()
+    rc = L.ffs_measure_fp64_peak(local, ctypes.byref(fma_tf), ctypes.byref(add_tf))
+    fp64_peak = fma_tf.value if rc == 0 else None
 
     if rank != 0:
         return 0
-    # --- roofline of the dominant kernel
     peak, peak_kind = measured_peaks()
-    sb = model_bytes(n, 8)
-    alg = algorithmic_bytes(n, 8)
-    top = max(prof, key=prof.get)
-    top_ms = prof[top] / nprof
-    achieved = sb.get(top, 0.0) / (top_ms / 1e3) / 1e9
-    traffic = ncu_traffic(top, n, "fp32")
     ms_step = ms / args.steps
+    fl = algorithmic_flops(n)
+    cand = {k: v for k, v in prof64.items() if k in fl}
+    top64 = max(cand, key=cand.get)
+    top64_ms = prof64[top64] / nprof
+    tr64 = ncu_traffic(top64, n, "fp64")
+    roof64 = {"bound": "fp64", "kernel": top64, "achieved": fl[top64] / (top64_ms / 1e3) / 1e12,
+              "peak": fp64_peak, "unit": "TFLOP/s",
+              "frac": (fl[top64] / (top64_ms / 1e3) / 1e12 / fp64_peak) if fp64_peak else None,
+              "traffic": tr64,
+              "peak_source": "measured in this run: ffs_measure_fp64_peak (FP64 FMA chains on every SM, 2 flops "
+                             "per FMA); no FP64 figure is in MEASURED_PEAKS.json",
+              "fp64_add_peak": add_tf.value if rc == 0 else None,
+              "flop_model": "pruned transform flops per pass: 5 L log2 L per complex line, 2.5 L log2 L per real "
+                            "line, retained columns only",
+              "algorithmic_flops_per_launch": fl[top64],
+              "step_algorithmic_flops": fl["step"],
+              "step_frac": (fl["step"] / (ms_step / 1e3) / 1e12 / fp64_peak) if fp64_peak else None,
+              "per_kernel_frac": ({k: fl[k] / (prof64[k] / nprof / 1e3) / 1e12 / fp64_peak for k in fl
+                                   if k != "step" and prof64.get(k, 0) > 0} if fp64_peak else None),
+              "hbm": kernel_roofline_hbm(prof64, nprof, n, 16, "fp64", peak, peak_kind, ms_step)}
+    if tr64:
+        roof64["dram_frac"] = tr64 / (top64_ms / 1e3) / 1e9 / peak
+    ms32_step = ms32 / k32
+    roof32 = kernel_roofline_hbm(prof32, nprof32, n, 8, "fp32", peak, peak_kind, ms32_step)
     cpu_rate, cpu_k, cores = (None, 0, 0)
     if not args.no_cpu:
         cpu_rate, cpu_k, cores = cpu_reference_rate(n, budget_s=args.cpu_budget, max_steps=50, warmup=1)
@@ -582,40 +671,109 @@ def run_engine_arm(args):
     line = {
         "metric": METRIC, "value": steps_s, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(n), "grid": n, "precision": "FP32 transforms/products/updates, "
-                   "FP64 twiddles, phi-coefficients and reductions", "parallelism": f"replicas x{world}",
-                   "l2": f"inputs larger than L2: {dev_bytes / 1e9:.2f} GB resident per GPU"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(n), "grid": n,
+                   "precision": "FP64 plain form (the reference's arithmetic); the FP32 chosen form is in fp32",
+                   "parallelism": f"replicas x{world}",
+                   "l2": f"inputs larger than L2: {dev_bytes / 1e9:.2f} GB resident per GPU (FP64)"},
         "grid_point_updates_per_s": steps_s * n ** 3,
-        "fp64": {"value": k64 / (ms64 / 1e3), "unit": "steps/s", "ms_per_step": ms64 / k64, "steps": k64},
-        "fp32_speedup_vs_fp64": (steps_s / world) / (k64 / (ms64 / 1e3)),
-        "fp32_vs_fp64_rel_l2_10_steps": err,
-        "kernels_ms_per_step": {k: v / nprof for k, v in prof.items()},
-        "roofline": {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": sb.get(top),
-                     "bytes_model": "69A per step, A = (n/2+1) n^2 complex FP32 (3 sweeps x read+write per "
-                                    "component transform, 5A per integrated component)",
-                     "step_algorithmic_bytes": sb["step"],
-                     "step_achieved": sb["step"] / (ms_step / 1e3) / 1e9,
-                     "step_frac": sb["step"] / (ms_step / 1e3) / 1e9 / peak,
-                     "retained_mode_bytes_per_launch": alg.get(top),
-                     "retained_mode_frac": alg.get(top, 0.0) / (top_ms / 1e3) / 1e9 / peak},
+        "kernels_ms_per_step": {k: v / nprof for k, v in prof64.items()},
+        "roofline": roof64,
+        "fp32": {"value": k32 / (ms32 / 1e3) * world, "unit": "steps/s", "ms_per_step": ms32_step, "steps": k32,
+                 "speedup_vs_fp64": (k32 / (ms32 / 1e3)) / (steps_s / world),
+                 "rel_l2_vs_fp64_10_steps": err,
+                 "precision": "FP32 transforms/products/updates; FP64 twiddles, phi-coefficients and reductions",
+                 "kernels_ms_per_step": {k: v / nprof32 for k, v in prof32.items()},
+                 "roofline": roof32,
+                 "e2e": {"value": args.steps * world / e2e32_s, "unit": "steps/s"},
+                 "tuning": tuning32},
         "cpu_baseline": ({"value": cpu_rate, "unit": "steps/s", "cores": cores, "kind": "port",
                           "sample": f"{cpu_k} steps of the same {n}^3 workload, FP64 numpy/pocketfft oracle"}
                          if cpu_rate else None),
-        "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": nb / args.steps,
-                "d2h_bytes_per_step": (sum(x.nbytes for x in out) + rows.nbytes) / args.steps,
-                "includes": "Simulation(), set_fields (host), initialize, advance_in_time(K), stats rows, "
-                            "get_fields (host)"},
+        "e2e": {"value": e2e_rate, "unit": "steps/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps,
+                "includes": "set_fields from host memory, initialize!, advance_in_time(K), run tail, stats rows "
+                            "and final fields to host memory (FP64; engine creation is one-time setup, outside)"},
         "clocks": clocks,
         "gpu_launches": launches,
-        "tuning": tuning,
+        "tuning": tuning64,
     }
     if args.serve_requests > 0:
         line["serving"] = run_serving(pkg, args.serve_requests, args.serve_seq_budget, local)
         line["gpu_launches"] += line["serving"].get("batched", {}).get("gpu_launches", 0)
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def fp32_error_run(pkg, name: str, nt: int, device: int) -> dict:
+    """FP32 chosen form against the FP64 plain form over a configuration's full run, from
+    the same initial state: relative differences of the energy (k), dissipation (diss) and
+    total dissipation (tdiss) series of the Stats rows (every dtStat steps, plus the run's
+    tail) and of the final u spectrum; the per-component relative L2 after 10 steps."""
+    import numpy as np
+    if name == "dns256":
+        d, n, ic = dict(global_dict(256), dtStat="100"), 256, "dns256"
+    else:
+        d, n, _, ic, _ = workload_config(name)
+    d = dict(d, dtSpec="1000000000")
+    out = {"steps": nt, "grid": n, "dt_stat": int(d["dtStat"])}
+
+    def make(prec):
+        if ic == "dns256":
+            p = pkg.parameters(d, precision=prec, device=device)
+            sim = pkg.Simulation(p)
+            sim.set_fields(*pkg.random_spectrum(n, k0=K0, seed=2001))
+            sim.initialize()
+            return sim
+        return make_sim(pkg, d, prec, ic, n, device, autotune=0)
+
+    runs = {}
+    for prec in ("FP32", "FP64"):
+        sim = make(prec)
+        sim.advance_in_time(10)
+        u10 = [sim.spectral(c) for c in range(3)]
+        t0 = time.perf_counter()
+        sim.advance_in_time(nt - 10)
+        sim.finalize()
+        wall = time.perf_counter() - t0
+        rows = sim.stats_rows()
+        H, V = sim.spectrum()
+        runs[prec] = (u10, rows, H, V, wall, sim.header.split(","))
+        sim.close()
+    (a10, ra, Ha, Va, wa, names), (b10, rb, Hb, Vb, wb, _) = runs["FP32"], runs["FP64"]
+    out["rel_l2_10_steps"] = [float(np.linalg.norm(a10[c] - b10[c]) / np.linalg.norm(b10[c])) for c in range(3)]
+    out["rows"] = int(rb.shape[0])
+    out["final_iteration"] = int(rb[-1, 0])
+    cols = ["k", "diss", "tdiss"] + (["rhop2"] if "rhop2" in names else [])
+    for c in cols:
+        j = names.index(c)
+        rd = np.abs(ra[:, j] - rb[:, j]) / np.abs(rb[:, j])
+        out[f"{c}_max_rel_diff"] = float(rd.max())
+        out[f"{c}_final_rel_diff"] = float(rd[-1])
+    kmax = len(Hb) * 2 // 3
+    sl = slice(1, kmax)
+    out["specH_final_max_rel_diff_k<=kmax"] = float((np.abs(Ha[sl] - Hb[sl]) / np.abs(Hb[sl])).max())
+    out["specH_final_rel_l2"] = float(np.linalg.norm(Ha - Hb) / np.linalg.norm(Hb))
+    out["specV_final_rel_l2"] = float(np.linalg.norm(Va - Vb) / np.linalg.norm(Vb))
+    out["wall_s"] = {"FP32": wa, "FP64": wb}
+    return out
+
+
+def run_fp32_error(args):
+    """--fp32-error: the FP32 chosen form's stated error over every configuration's full run."""
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    pkg.load()
+    plan = {"dns256": 2000, "les128": 5000, "dns1024": 200}
+    want = args.configs.split(",") if args.configs else list(plan)
+    res = {}
+    for name in want:
+        try:
+            res[name] = fp32_error_run(pkg, name, plan[name], 0)
+        except pkg.FFSError as e:
+            res[name] = {"error": str(e)}
+        print(json.dumps({name: res[name]}), flush=True)
+    print(json.dumps({"fp32_error": res}), flush=True)
     return 0
 
 
@@ -629,6 +787,9 @@ def main():
     ap.add_argument("--workload", default="dns256", choices=["dns256", "tg64", "les128", "dns1024"],
                     help="dns256: the headline run; the others print one line for that configuration")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--fp32-error", action="store_true",
+                    help="FP32 vs FP64 over each configuration's full run (not part of the default bench)")
+    ap.add_argument("--configs", default="", help="with --fp32-error: comma-separated subset of dns256,les128,dns1024")
     ap.add_argument("--no-autotune", action="store_true", help="default launch shapes instead of the tuned ones")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
@@ -638,6 +799,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.fp32_error:
+        return run_fp32_error(args)
     if args.workload != "dns256":
         return run_workload(args)
     return run_engine_arm(args)

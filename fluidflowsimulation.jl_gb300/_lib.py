@@ -17,12 +17,13 @@ FFS_FP64, FFS_FP32 = 0, 1
 
 # Every symbol include/ffs.h declares (checked by the CPU test suite).
 EXPORTS = [
-    "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_get_fields",
+    "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_finalize",
+    "ffs_get_fields",
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
     "ffs_stats_records", "ffs_stats", "ffs_spectrum", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_tuning_report",
     "ffs_stream",
-    "ffs_fourier_noalloc", "ffs_last_error", "ffs_destroy",
+    "ffs_fourier_noalloc", "ffs_measure_fp64_peak", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
     "ffs_fetch_fields", "ffs_release", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
 ]
@@ -98,6 +99,7 @@ def load() -> ctypes.CDLL:
         "ffs_set_fields": (c_int32, [H, D, D, D, D, c_int32]),
         "ffs_initialize": (c_int32, [H]),
         "ffs_step": (c_int32, [H, c_int64]),
+        "ffs_finalize": (c_int32, [H]),
         "ffs_get_fields": (c_int32, [H, D, D, D, D, c_int32]),
         "ffs_get_spectral": (c_int32, [H, c_int32, D]),
         "ffs_set_spectral": (c_int32, [H, c_int32, D]),
@@ -121,6 +123,7 @@ def load() -> ctypes.CDLL:
         "ffs_stream": (c_void_p, [H]),
         "ffs_fourier_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_double,
                                          c_double, c_double, c_void_p]),
+        "ffs_measure_fp64_peak": (c_int32, [c_int32, D, D]),
         "ffs_last_error": (c_char_p, [H]),
         "ffs_destroy": (None, [H]),
         "ffs_server_default": (c_int32, [POINTER(FFSServerCfg)]),

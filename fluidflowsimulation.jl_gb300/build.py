@@ -16,7 +16,8 @@ CSRC = HERE / "csrc"
 OBJ = HERE / "_build"
 LIB = HERE / "libffs.so"
 SOURCES = ["ffs_engine_f32.cu", "ffs_engine_f64.cu", "ffs_noalloc.cu", "ffs_server.cu", "ffs_batch_c32.cu",
-           "ffs_batch_c48.cu", "ffs_batch_c64.cu", "ffs_batch_c96.cu", "ffs_batch_c128.cu", "ffs_api.cpp"]
+           "ffs_batch_c48.cu", "ffs_batch_c64.cu", "ffs_batch_c96.cu", "ffs_batch_c128.cu", "ffs_probe.cu",
+           "ffs_api.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

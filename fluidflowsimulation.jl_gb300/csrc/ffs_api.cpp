@@ -103,6 +103,10 @@ int ffs_step(ffs_handle* h, int64_t nsteps) {
   return guarded(h, [&] { return h->eng->step(nsteps, h->err); });
 }
 
+int ffs_finalize(ffs_handle* h) {
+  return guarded(h, [&] { return h->eng->finish(h->err); });
+}
+
 int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout) {
   return guarded(h, [&] { return h->eng->get_fields(u1, u2, u3, rho, layout, h->err); });
 }

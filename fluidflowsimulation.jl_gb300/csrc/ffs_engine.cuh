@@ -707,7 +707,7 @@ class Engine : public EngineBase {
     launch_zu(mode);
     cudaStreamWaitEvent(s, ev_join, 0);
     launch_stats(mode);
-    launch_update(mode);
+    if (mode != 2) launch_update(mode);   // the run's tail evaluates the rhs and stats only
     launch_fin(mode);
   }
   int launches_per_step() const override { return 9 + (use_table() ? 1 : 0); }
@@ -872,6 +872,16 @@ class Engine : public EngineBase {
     if ((rc = pull_state(err))) return rc;
     initialized = true;
     return 0;
+  }
+
+  // The tail of run_simulation (FluidFlowSimulation.jl:46-49): calculate_rhs! (set_dt!
+  // included), the forcing, and writestats at the current iteration, without an update.
+  int finish(std::string& err) override {
+    if (!initialized) { err = "ffs_initialize must be called before ffs_finalize"; return FFS_ESTATE; }
+    enqueue_step(2);
+    FFS_CK(cudaGetLastError());
+    FFS_CK(cudaStreamSynchronize(s));
+    return drain(iteration, iteration, err);
   }
 
   int build_graph(std::string& err) {

@@ -409,7 +409,8 @@ template <typename T> __device__ __forceinline__ double ref_k2(const Inst<T>& I,
 // ====================================================================================
 // Scalar kernel: set_dt! (time_step_functions.jl:86-129), integrator dt history
 // (Adams_Bashforth.jl:37-47, ETD.jl:110-114), AB3 coefficients (Adams_Bashforth.jl
-// 49-89), forcing energy of the band. mode 0: a step; mode 1: initialize!.
+// 49-89), forcing energy of the band. mode 0: a step; mode 1: initialize!; mode 2: the
+// run's tail (set_dt! and the forcing of calculate_rhs!, no integrator call).
 // One CTA.
 // ====================================================================================
 template <typename T>
@@ -455,7 +456,7 @@ __device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk b
       S.dt2 = S.dt; S.dt3 = S.dt;
       S.stage = 0;
       S.skip_table = 0;
-    } else {
+    } else if (mode == 0) {
       const int prev_stage = S.stage;
       S.ts_iter += 1;
       const long long i = S.ts_iter;
@@ -477,7 +478,7 @@ __device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk b
     sh_dt = S.dt;
   }
   // isotropic band forcing: E_f = sum_{0<|k|<=kf} 1/2 w |u|^2 from the current u
-  if (I.forcing && mode == 0) {
+  if (I.forcing && mode != 1) {
     const int bx = (int)floor(I.f_kf * I.lx) + 1, by = (int)floor(I.f_kf * I.ly) + 1, bz = (int)floor(I.f_kf * I.lz) + 1;
     const int cnt = bx * (2 * by + 1) * (2 * bz + 1);
     double e = 0.0;
@@ -526,7 +527,7 @@ template <typename T>
 __device__ __forceinline__ void b_etd_table(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const int stage = S->stage;
-  if (mode == 1 || stage == 0 || S->skip_table) return;
+  if (mode != 0 || stage == 0 || S->skip_table) return;
   const double dt = S->dt, dt2 = S->dt2, dt3 = S->dt3;
   const long long count = I.uniformL ? (long long)I.qmax + 1 : I.cstride;
   for (long long q = (long long)bk.x * blockDim.x + threadIdx.x; q < count; q += (long long)bk.nx * blockDim.x) {
@@ -575,7 +576,7 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
   cplx<T>* accF = accT + 3 * NZR * TX;                   // [NZR][TX]    i k . flux (density)
 
   const long long it = I.st->iteration;
-  const bool want_ke = ((it % I.dt_stat) == 0) || (mode == 0 && (it % I.dt_spec) == 0);
+  const bool want_ke = ((it % I.dt_stat) == 0) || (mode != 1 && (it % I.dt_spec) == 0);
   const int kx0 = bk.x * TX, jc = bk.y;
   const int rowstride = I.NYR * I.KXP;
   const long long cs = I.cstride;
@@ -863,8 +864,8 @@ template <typename T>
 __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const long long it = S->iteration;
-  const bool stats_t = (it % I.dt_stat) == 0;
-  const bool spec_t = mode == 0 && (it % I.dt_spec) == 0;
+  const bool stats_t = (it % I.dt_stat) == 0 || mode == 2;   // the run's tail always writes a row
+  const bool spec_t = mode != 1 && (it % I.dt_spec) == 0;
   if (!stats_t && !spec_t) return;
   __shared__ double red[Q_COUNT][9];
   const long long cs = I.cstride;
@@ -948,7 +949,7 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       q[Q_HVH] += w * km * (a2[0] + a2[1]);
       q[Q_HVV] += w * km * a2[2];
     }
-    if (I.forcing && mode == 0 && k2 > T(0) && k2 <= kf2) {
+    if (I.forcing && mode != 1 && k2 > T(0) && k2 <= kf2) {
       q[Q_HP] += w * (fdt * (a2[0] + a2[1]) + T(0.5) * fdt * fdt * (a2[0] + a2[1]));
       q[Q_VP] += w * (fdt * a2[2] + T(0.5) * fdt * fdt * a2[2]);
     }
@@ -997,7 +998,7 @@ template <typename T>
 __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk bk) {
   const DevState* S = I.st;
   const long long it = S->iteration;
-  if (!(mode == 0 && (it % I.dt_spec) == 0)) return;
+  if (!(mode != 1 && (it % I.dt_spec) == 0)) return;
   const long long rec = S->nspec;
   if (rec >= I.spec_cap) return;
   const long long cs = I.cstride;
@@ -1092,14 +1093,18 @@ __global__ void __launch_bounds__(256) k_stats(Inst<T> I, int mode) {
 // ====================================================================================
 // Finalize: stats record (stats.jl:64-219), reference reductionh reuse for the next
 // CFL (time_step_functions.jl:87 with utils.jl:247-258), iteration/time advance
-// (models.jl:14-15). One CTA of 1024 threads. mode 0: step, 1: initialize!.
+// (models.jl:14-15). One CTA of 1024 threads. mode 0: step, 1: initialize!, 2: the run's
+// tail (writestats at the final iteration, FluidFlowSimulation.jl:46-49: a row whatever the
+// iteration, non-linear and pressure columns from the last stats iteration unless this one
+// is one, as s.nlstats/s.pressstats are; no iteration or time advance).
 // ====================================================================================
 template <typename T>
 __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int nparts, const Blk bk) {
   DevState* S = I.st;
   __shared__ double tot[QPAD];
   const long long it = S->iteration;
-  const bool stats_t = (it % I.dt_stat) == 0;
+  const bool fresh = (it % I.dt_stat) == 0;   // calculate_rhs! took the nl/pressure stats
+  const bool stats_t = fresh || mode == 2;
   if (stats_t) {
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     for (int qi = w; qi < Q_COUNT; qi += nw) {
@@ -1111,7 +1116,7 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
     __syncthreads();
   }
   if (threadIdx.x != 0) return;
-  if (stats_t) {
+  if (fresh) {
     S->nl_h = tot[Q_NLH]; S->nl_v = tot[Q_NLV];
     S->press_h = tot[Q_PH]; S->press_v = tot[Q_PV];
   }
@@ -1128,7 +1133,7 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       const double u12 = tot[Q_U12], u22 = tot[Q_U22], u32 = tot[Q_U32];
       const double kh = (u12 + u22) / 2, kv = u32 / 2;
       const double eh = I.nu * tot[Q_EH], ev = I.nu * tot[Q_EV];
-      const double nlh = tot[Q_NLH], nlv = tot[Q_NLV], ph = tot[Q_PH], pv = tot[Q_PV];
+      const double nlh = S->nl_h, nlv = S->nl_v, ph = S->press_h, pv = S->press_v;
       int c = 0;
       row[c++] = (double)it; row[c++] = S->time;
       row[c++] = tot[Q_U1]; row[c++] = tot[Q_U2]; row[c++] = tot[Q_U3];
@@ -1171,7 +1176,8 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       if (I.density) S->slot_rho = tot[Q_BF];
     }
   }
-  if (mode == 0 && (it % I.dt_spec) == 0) S->nspec += 1;
+  if (mode != 1 && (it % I.dt_spec) == 0) S->nspec += 1;
+  if (mode == 2) { S->umax_bits = 0ull; S->rhomax_bits = 0ull; return; }
   S->iteration = it + 1;
   S->time += S->dt;
   S->hist_parity ^= 1;

@@ -176,7 +176,7 @@ __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& 
   const int NZR = I.NZR;
   cplx<T>* accF = accT + 3 * NZR * TX;
   const long long it = I.st->iteration;
-  const bool want_ke = ((it % I.dt_stat) == 0) || (mode == 0 && (it % I.dt_spec) == 0);
+  const bool want_ke = ((it % I.dt_stat) == 0) || (mode != 1 && (it % I.dt_spec) == 0);
   const int kx0 = bk.x * TX, jc = bk.y;
   const int rowstride = I.NYR * I.KXP;
   const long long cs = I.cstride;

@@ -10,7 +10,7 @@
 #   using FFSEngine; run_simulation()
 module FFSEngine
 
-export run_simulation, FFSParams, Engine, initialize!, advance_in_time!, getfields
+export run_simulation, FFSParams, Engine, initialize!, advance_in_time!, finalize!, getfields
 
 const LIB = get(ENV, "FFS_LIB", joinpath(@__DIR__, "..", "libffs.so"))
 
@@ -109,6 +109,8 @@ end
 
 initialize!(e::Engine) = check(e, ccall((:ffs_initialize, LIB), Cint, (Ptr{Cvoid},), e.h))
 advance_in_time!(e::Engine, n::Integer = 1) = check(e, ccall((:ffs_step, LIB), Cint, (Ptr{Cvoid}, Int64), e.h, n))
+# the tail of run_simulation (FluidFlowSimulation.jl:46-49): calculate_rhs!, forcing, writestats
+finalize!(e::Engine) = check(e, ccall((:ffs_finalize, LIB), Cint, (Ptr{Cvoid},), e.h))
 iteration(e::Engine) = ccall((:ffs_iteration, LIB), Int64, (Ptr{Cvoid},), e.h)
 simtime(e::Engine) = ccall((:ffs_time, LIB), Float64, (Ptr{Cvoid},), e.h)
 
@@ -259,7 +261,9 @@ function run_simulation()
     ns = statsncols(e)
     initialize!(e)
     total = haskey(d, :nt) ? parse(Int, d[:nt]) : typemax(Int) - s
+    lengthtime = haskey(d, :timeDuration) ? parse(Float64, d[:timeDuration]) : Inf   # FluidFlowSimulation.jl:26
     final = s + total
+    finaltime = simtime(e) + lengthtime
     function flush()
         recs = records(e)
         open("Stats.txt", "a+") do f
@@ -274,15 +278,21 @@ function run_simulation()
         end
         writespectra(e)
     end
-    while iteration(e) < final
+    # the loop of FluidFlowSimulation.jl:42-44; a time-limited run checks the clock every step
+    while iteration(e) < final && simtime(e) < finaltime
         it = iteration(e)
-        nxt = min(final, (it ÷ p.write_time + 1) * p.write_time)
+        nxt = isfinite(lengthtime) ? it + 1 : min(final, (it ÷ p.write_time + 1) * p.write_time)
         advance_in_time!(e, nxt - it)
         flush()
-        (iteration(e) % p.write_time == 0 && iteration(e) < final) && writeoutput(e)
+        # the reference writes u.N from calculate_rhs! when the next step starts at N
+        (iteration(e) % p.write_time == 0 && iteration(e) < final && simtime(e) < finaltime) && writeoutput(e)
     end
+    # the tail (FluidFlowSimulation.jl:46-58): a Stats row at the final iteration, and the
+    # final fields (written by the tail's calculate_rhs! when the iteration is a multiple
+    # of writeTime, else by the explicit writeoutput)
+    finalize!(e)
     flush()
-    iteration(e) % p.write_time != 0 && writeoutput(e)
+    writeoutput(e)
     return e
 end
 

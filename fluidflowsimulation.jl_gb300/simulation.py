@@ -107,6 +107,12 @@ class Simulation:
         """``advance_in_time!(s)`` repeated ``nsteps`` times (src/models.jl:3-17)."""
         self._check(self._L.ffs_step(self._h, int(nsteps)))
 
+    def finalize(self):
+        """The tail of ``run_simulation`` after its time loop (src/FluidFlowSimulation.jl:46-49):
+        ``calculate_rhs!``, the forcing and ``writestats`` at the current iteration (one
+        Stats record whatever the iteration; fields, iteration and time unchanged)."""
+        self._check(self._L.ffs_finalize(self._h))
+
     def fields(self, layout: int = 0):
         shape = (self.nz, self.ny, self.nx if layout == 0 else 2 * (self.nx // 2 + 1))
         out = [np.empty(shape) for _ in range(4 if self.has_density else 3)]
@@ -307,20 +313,23 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         for rec in sim.spectra():
             write_spectrum_files(folder, rec, KH, KRZ, rhos)
 
-    while sim.iteration < final_step and sim.time < final_time:
+    while sim.iteration < final_step and sim.time < final_time:     # FluidFlowSimulation.jl:42-44
         it = sim.iteration
         nxt = min(final_step, (it // wt + 1) * wt)
         if lengthtime != float("inf"):
             nxt = it + 1       # time-limited runs check the clock every step
         sim.advance_in_time(nxt - it)
         flush()
-        if sim.iteration % wt == 0 and sim.iteration < final_step:
+        # the reference writes u.N from calculate_rhs! when the step from N starts
+        # (is_output_time, simulationtypes.jl:102, models.jl:158)
+        if sim.iteration % wt == 0 and sim.iteration < final_step and sim.time < final_time:
             _write_output(folder, sim)
-    # tail of run_simulation (FluidFlowSimulation.jl:46-58): the final fields are written
-    # only when the last iteration is not a multiple of writeTime
+    # the tail (FluidFlowSimulation.jl:46-58): calculate_rhs!, forcing and a Stats row at the
+    # final iteration; the final fields are written either way (by the tail's calculate_rhs!
+    # when the iteration is a multiple of writeTime, else by the explicit writeoutput)
+    sim.finalize()
     flush()
-    if sim.iteration % wt != 0:
-        _write_output(folder, sim)
+    _write_output(folder, sim)
     return sim
 
 

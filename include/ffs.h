@@ -105,6 +105,14 @@ int ffs_initialize(ffs_handle* h);
  * iterations multiple of dtStat and u spectra at multiples of dtSpec on the device. */
 int ffs_step(ffs_handle* h, int64_t nsteps);
 
+/* The tail of run_simulation after its time loop (src/FluidFlowSimulation.jl:46-49):
+ * calculate_rhs!(s) (set_dt! included), the forcing, and writestats(s) at the current
+ * iteration. Records one Stats row whatever the iteration (its non-linear and pressure
+ * columns are those of the last stats iteration unless this is one, as the reference's
+ * s.nlstats/s.pressstats are) and, at a multiple of dtSpec, a spectrum record. Fields,
+ * iteration and time do not change. Meant as the run's last call, as in the reference. */
+int ffs_finalize(ffs_handle* h);
+
 /* Physical fields at the current iteration (real!(s.u), src/output.jl:1-8). */
 int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout);
 
@@ -163,21 +171,32 @@ int ffs_tuning_report(const ffs_handle* h, char* buf, int64_t len);
 /* The handle's cudaStream_t. */
 void* ffs_stream(const ffs_handle* h);
 
-/* No counterpart in the reference. The forward transform of one field (myfourier!:
- * real 3D FFT, 2/3 dealiasing, 1/(nx ny nz) scaling, FP64) for callers that cannot
- * allocate device memory: code inside a CUDA stream capture, code whose device memory
- * belongs to another allocator or pool, hosts that forbid allocations at run time.
+/* No counterpart in the reference. The forward transform of one field (real 3D FFT,
+ * 2/3 dealiasing, 1/(nx ny nz) scaling, FP64) for callers that cannot allocate device
+ * memory: hosts whose device memory belongs to another allocator or pool (a cudaMalloc
+ * of their own would bypass its accounting and fragment it), loops that must not
+ * allocate once running (cudaMalloc/cudaFree can synchronise the device and take an
+ * unbounded time), plug-in hosts that grant only the buffers they pass in.
  * phys: device pointer, nx*ny*nz doubles, x fastest. spec: device pointer, complex128
- * [nz][ny][nx/2+1] (interleaved re,im), zeros outside the retained modes — the layout
+ * [nz][ny][nx/2+1] (interleaved re,im), zeros outside the retained modes -- the layout
  * ffs_get_spectral returns. stream: a cudaStream_t (NULL: the legacy default stream);
- * the call only enqueues work. No cudaMalloc/cudaFree: the intermediates live in one
- * static device array of 24 MiB per GPU (held until exit), so grids whose intermediates
- * exceed it are rejected with FFS_EINVAL (128^3 with the 2/3 rule fits). The first
- * call on a device resolves the array's address; make it before any stream capture.
- * All calls share the array: calls whose work overlaps on the GPU race.
- * Errors: ffs_last_error(NULL). */
+ * the call only enqueues device work (four kernels and a memset of spec) and reads no
+ * host memory from the device. No cudaMalloc/cudaFree: the twiddle tables and the
+ * intermediates live in one static device array of 24 MiB per GPU (held until exit), so
+ * grids whose intermediates exceed it are rejected with FFS_EINVAL (128^3 with the 2/3
+ * rule fits). The first call on a device resolves the array's address
+ * (cudaGetSymbolAddress, cached); make that first call before any stream capture.
+ * Every call rewrites the twiddles and intermediates in that one array: calls whose
+ * work overlaps on the GPU race. Errors: ffs_last_error(NULL). */
 int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny, int32_t nz, double lx, double ly,
                         double lz, double cutoff, void* stream);
+
+/* No counterpart in the reference. FP64 arithmetic rate of a GPU measured with this
+ * library's own register-chain kernels (every SM x 8 CTAs x 256 threads, 8 independent
+ * chains per thread): fused multiply-adds (2 flops each) and adds (1 flop each), in
+ * TFLOP/s. The denominator of the FP64 plain form's roofline (its transforms are FP64-
+ * pipe-bound on GB300). Allocates 8 bytes of device memory for the duration. */
+int ffs_measure_fp64_peak(int32_t device, double* fma_tflops, double* add_tflops);
 
 const char* ffs_last_error(const ffs_handle* h);
 void ffs_destroy(ffs_handle* h);

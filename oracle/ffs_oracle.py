@@ -514,6 +514,11 @@ class OracleSimulation:
         self.force = None
         self.hp = self.vp = 0.0
         self.umax_hist = []
+        # Optional Delta t sequence that replaces the CFL value of each set_dt! call, in
+        # call order (parity tests feed the engine's own sequence here); newdt_hist
+        # records the values set_dt! produced or took.
+        self.dt_sequence = None
+        self.newdt_hist = []
 
     # ---------------------------------------------------------------- time helpers
     def get_dt(self):
@@ -666,6 +671,9 @@ class OracleSimulation:
                 newdt = max(dt / 1.25, newdt)
             else:
                 newdt = min(1.25 * dt, newdt)
+        if self.dt_sequence is not None:
+            newdt = float(self.dt_sequence[len(self.newdt_hist)])
+        self.newdt_hist.append(newdt)
         self.ts.set_dt(newdt)
         if p.density:
             self.rts.set_dt(newdt)

@@ -1,7 +1,7 @@
 """Minimal driver for profilers: set_fields + initialize + K steps of the forced-DNS workload
 (or, with the fourth argument ``les``, of the stratified Smagorinsky LES workload).
 
-    python fluidflowsimulation.jl_gb300/profile_step.py [n] [FP32|FP64] [steps] [dns|les]
+    python profile_step.py [n] [FP32|FP64] [steps] [dns|les]
 
 Runs the same workload as bench.py (seeded random-phase field, k0 = 4, band forcing,
 AB3 with adaptive dt, stats every 100 steps) with the default launch shapes (the
@@ -16,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 import __graft_entry__ as ge  # noqa: E402
 

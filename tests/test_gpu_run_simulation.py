@@ -1,0 +1,109 @@
+"""File-level drop-in test: ``run_simulation()`` on a case directory (a `global` file and
+u1.0/u2.0/u3.0) against the oracle run the way the reference's run_simulation runs it
+(src/FluidFlowSimulation.jl:23-65).
+
+Compared, FP64: every Stats.txt, Scales.txt and Numbers.txt line (1e-10), every
+spectrum file (1e-10), and the u1.N/u2.N/u3.N files (sizes 8 nx ny nz bytes, contents
+1e-12 relative L2). The oracle side restates the loop: the fields are written from
+calculate_rhs! when a step starts at a multiple of writeTime (is_output_time,
+src/simulationtypes.jl:102, src/models.jl:158) and once more at the end; the tail runs
+calculate_rhs!, the forcing and writestats at the final iteration.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle.ffs_oracle import OracleSimulation, Params, stats_header
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_run(d, u):
+    """FluidFlowSimulation.jl:23-65 on the oracle; returns its rows, spectra and outputs."""
+    s = OracleSimulation(Params.from_global(d), u)
+    total = int(d["nt"]) if "nt" in d else (1 << 62)
+    lengthtime = float(d["timeDuration"]) if "timeDuration" in d else math.inf
+    wt = int(d["writeTime"])
+    s.initialize()
+    final, finaltime = s.iteration + total, s.time + lengthtime
+    outputs = {}
+    calls = 0                                    # the integrator's call count
+    while s.iteration < final and s.time < finaltime:
+        if calls != 0 and s.iteration % wt == 0:
+            outputs[s.iteration] = s.u_physical()
+        s.advance()
+        calls += 1
+    s.finalize()                                 # calculate_rhs!, forcing, writestats
+    outputs[s.iteration] = s.u_physical()        # tail calculate_rhs! or the explicit writeoutput
+    return s, outputs
+
+
+def read_rows(path):
+    lines = path.read_text().splitlines()
+    return lines[0], np.array([[float(x) for x in ln.split(",")] for ln in lines[1:]])
+
+
+def rows_err(got, want):
+    got, want = np.asarray(got), np.asarray(want)
+    assert got.shape == want.shape, (got.shape, want.shape)
+    ok = np.isfinite(want)
+    assert np.array_equal(ok, np.isfinite(got))
+    scale = np.maximum(np.abs(want[ok]), 1e-6 * np.abs(want[ok]).max())
+    return float((np.abs(got[ok] - want[ok]) / scale).max())
+
+
+CASES = {
+    # ETD3, fixed dt, band forcing: stats at 0,3,6,9 + the tail at 12, spectra at 0,4,8,12,
+    # fields at 5, 10 and 12
+    "etd-forced-nt": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "12",
+                      "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5"},
+    # AB3, adaptive dt, stopped by timeDuration at an iteration that is not a stats
+    # iteration (the tail row then keeps the last non-linear/pressure columns)
+    "ab3-adaptive-timeDuration": {"velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true",
+                                  "cfl": "0.4", "dt": "0.01", "nt": "1000", "timeDuration": "0.05"},
+}
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
+    n = 32
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": "0.01", "dtStat": "3", "dtSpec": "4", "writeTime": "5",
+         **CASES[case]}
+    u = gpu_pkg.random_spectrum(n, k0=3.0, seed=11)
+    (tmp_path / "global").write_text("// case\n" + "".join(f"{k} {v}\n" for k, v in d.items()))
+    for i in range(3):
+        gpu_pkg.write_field(tmp_path / f"u{i + 1}.0", u[i])
+    sim = gpu_pkg.run_simulation(tmp_path, precision="FP64")
+    ref, outputs = oracle_run(d, u)
+    assert sim.iteration == ref.iteration
+    sim.close()
+    p = Params.from_global(d)
+    # Stats.txt, Scales.txt, Numbers.txt
+    head, rows = read_rows(tmp_path / "Stats.txt")
+    assert head == stats_header(p)
+    assert rows[-1, 0] == ref.iteration
+    assert rows_err(rows, ref.stats_rows) <= 1e-10
+    for name, want in (("Scales.txt", ref.scales_rows), ("Numbers.txt", ref.numbers_rows)):
+        _, got = read_rows(tmp_path / name)
+        assert rows_err(got, want) <= 1e-10, name
+    # spectra: every (field, iteration) the oracle recorded is a file with its values
+    assert ref.spectra
+    for it, sp in ref.spectra.items():
+        for key, want in sp.items():
+            f = tmp_path / f"{key}.{it}"
+            assert f.exists(), f.name
+            got = np.loadtxt(f)
+            assert got.shape == (len(want), 2)
+            scale = max(np.abs(want).max(), 1e-300)
+            assert np.allclose(got[:, 1], want, rtol=1e-10, atol=1e-12 * scale), f.name
+    # field files: exactly the oracle's output iterations, raw Float64 n^3
+    written = sorted(int(f.name.split(".")[1]) for f in tmp_path.glob("u1.*") if f.name != "u1.0")
+    assert written == sorted(outputs)
+    for it, ur in outputs.items():
+        for c in range(3):
+            f = tmp_path / f"u{c + 1}.{it}"
+            assert f.stat().st_size == 8 * n ** 3
+            got = gpu_pkg.read_field(f, n, n, n)
+            assert np.linalg.norm(got - ur[c]) <= 1e-12 * np.linalg.norm(ur[c]), (it, c)

@@ -13,7 +13,7 @@ ROOT = Path(__file__).resolve().parent.parent
 def header_functions():
     src = (ROOT / "include" / "ffs.h").read_text()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(ffs_[a-z_]+)\s*\(", src)))
+    return sorted(set(re.findall(r"\b(ffs_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_library_exports_every_declared_symbol(pkg):
@@ -31,7 +31,7 @@ def test_julia_binding_calls_only_declared_symbols():
     """Every entry point the Julia ccall shim binds is declared in include/ffs.h (the shim
     cannot run here: no Julia in the image)."""
     src = (ROOT / "fluidflowsimulation.jl_gb300" / "julia" / "FFSEngine.jl").read_text()
-    called = set(re.findall(r"ccall\(\(:(ffs_[a-z_]+)", src))
+    called = set(re.findall(r"ccall\(\(:(ffs_[a-z0-9_]+)", src))
     assert called, "no ccall found"
     assert called <= set(header_functions()), sorted(called - set(header_functions()))
 
@@ -201,5 +201,9 @@ def test_bench_byte_models():
     assert sum(v for k, v in m.items() if k != "step") == m["step"]
     r = bench.algorithmic_bytes(n, elem)
     C, V, U = 86 * 171 * 171 * elem, 86 * 171 * n * elem, 86 * n * n * elem
-    assert r["inv_z"] == 3 * C + 6 * V and r["x_pass"] == 9 * U
-    assert r["step"] == 18 * C + 18 * V + 18 * U
+    assert r["inv_z"] == 3 * C + 6 * V and r["x_pass"] == 9 * U and r["update"] == 18 * C
+    assert r["step"] == 24 * C + 18 * V + 18 * U
+    f = bench.algorithmic_flops(n)
+    assert f["x_pass"] == 9 * n * n * 2.5 * n * 8
+    assert f["inv_z"] == 6 * 86 * 171 * 5 * n * 8
+    assert sum(v for k, v in f.items() if k != "step") == f["step"]

@@ -165,3 +165,39 @@ def test_reference_cfl_slot_semantics():
     s2.initialize()
     s2.run(2)
     assert s2.slot_u == pytest.approx(s2.umax_hist[-1])
+
+
+def test_taylor_green_64_ab3_at_its_dt_blows_up():
+    """The Taylor-Green 64^3 configuration as written (AB3, nu = 0.0333333, dt = 0.05):
+    AB3 treats the viscous term explicitly and nu k_max^2 dt = 0.0333333 * 3 * 21^2 * 0.05
+    = 2.2 lies far outside its stability interval, so the energy explodes within 40
+    steps. The configuration therefore runs on ETD3 (the reference's default integrator),
+    which integrates the viscous term exactly."""
+    p = tg_params(n=64, dt_stat=1000, dt_spec=1000)
+    s = OracleSimulation(p, taylor_green(64))
+    s.initialize()
+    e0 = float(np.sum(np.abs(s.u) ** 2))
+    for _ in range(40):
+        s.advance()
+    e = float(np.sum(np.abs(s.u) ** 2))
+    assert not (e < 1e6 * e0)      # blown up (or NaN)
+    # the same run on ETD3 decays smoothly
+    q = tg_params(n=64, integrator="ETD3rdO", dt_stat=1000, dt_spec=1000)
+    t = OracleSimulation(q, taylor_green(64))
+    t.initialize()
+    for _ in range(10):
+        t.advance()
+    assert 0 < float(np.sum(np.abs(t.u) ** 2)) < e0
+
+
+def test_config_fixture_is_the_oracle_run():
+    """The Taylor-Green 64^3 full-run fixture (tests/golden/configs) starts the way the
+    oracle runs now: its first two rows (iterations 0 and 20)."""
+    from pathlib import Path
+    z = np.load(Path(__file__).resolve().parent / "golden" / "configs" / "tg64_etd3_500.npz")
+    d = dict(zip([str(k) for k in z["keys"]], [str(v) for v in z["values"]]))
+    s = OracleSimulation(Params.from_global(d), taylor_green(64))
+    s.initialize()
+    s.run(21)
+    assert np.allclose(np.array(s.stats_rows), z["stats"][:2], rtol=1e-12, atol=1e-15)
+    assert z["stats"].shape[0] == 26 and z["stats"][-1, 0] == 500
