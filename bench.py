@@ -116,9 +116,10 @@ def measured_peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str, n: int, prec: str) -> float | None:
-    """Per-launch DRAM bytes of a kernel from the committed ncu summary (profiles/traffic.txt)."""
-    p = ROOT / "profiles" / "traffic.txt"
+def ncu_traffic(kernel: str, n: int, prec: str, name: str = "traffic.txt") -> float | None:
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary (profiles/traffic.txt),
+    or another per-launch figure of the same format (profiles/fp64_instructions.txt)."""
+    p = ROOT / "profiles" / name
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
@@ -662,6 +663,12 @@ def run_engine_arm(args):
               "hbm": kernel_roofline_hbm(prof64, nprof, n, 16, "fp64", peak, peak_kind, ms_step)}
     if tr64:
         roof64["dram_frac"] = tr64 / (top64_ms / 1e3) / 1e9 / peak
+    ins64 = ncu_traffic(top64, n, "fp64", "fp64_instructions.txt")
+    if ins64 and fp64_peak:
+        # FP64-pipe occupancy: the kernel's counted FP64 warp instructions (one ncu capture)
+        # per event-timed launch against the pipe's rate at the measured peak (1 FMA = 2 flops)
+        roof64["fp64_pipe_frac"] = ins64 * 32 / (top64_ms / 1e3) / (fp64_peak * 1e12 / 2)
+        roof64["fp64_warp_instructions_per_launch"] = ins64
     ms32_step = ms32 / k32
     roof32 = kernel_roofline_hbm(prof32, nprof32, n, 8, "fp32", peak, peak_kind, ms32_step)
     cpu_rate, cpu_k, cores = (None, 0, 0)

@@ -11,8 +11,9 @@ LIB_PATH = HERE / "libffs.so"
 
 FFS_OK = 0
 ERRORS = {-1: "FFS_EINVAL", -2: "FFS_ENOMEM", -3: "FFS_ECUDA", -4: "FFS_ENAN", -5: "FFS_ETIMEDOUT",
-          -6: "FFS_EUNSUPPORTED", -7: "FFS_ESTATE"}
+          -6: "FFS_EUNSUPPORTED", -7: "FFS_ESTATE", -8: "FFS_ECANCELED"}
 FFS_ETD3, FFS_AB3 = 0, 1
+LES_MODELS = {"Smagorinsky": 0, "Vreman": 1, "productionViscosity": 2, "Silvis": 3, "stableNonLinear": 4}
 FFS_FP64, FFS_FP32 = 0, 1
 
 # Every symbol include/ffs.h declares (checked by the CPU test suite).
@@ -25,7 +26,7 @@ EXPORTS = [
     "ffs_stream",
     "ffs_fourier_noalloc", "ffs_measure_fp64_peak", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
-    "ffs_fetch_fields", "ffs_release", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
+    "ffs_fetch_fields", "ffs_release", "ffs_cancel", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
 ]
 FFS_QUEUED, FFS_RUNNING = 1, 2
 
@@ -48,6 +49,8 @@ class FFSParams(ctypes.Structure):
         ("start", c_int64), ("start_time", c_double),
         ("device", c_int32), ("reference_cfl_slot", c_int32),
         ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("kernel_variant", c_int32), ("autotune", c_int32),
+        ("les_model", c_int32), ("les_cp", c_double), ("sandp_cb", c_double),
+        ("passive_scalar", c_int32), ("scalar_pr", c_double), ("scalar_gradient", c_double), ("scalar_dir", c_int32),
     ]
 
 
@@ -134,6 +137,7 @@ def load() -> ctypes.CDLL:
         "ffs_fetch_stats": (c_int64, [H, ctypes.c_uint64, D, c_int64]),
         "ffs_fetch_fields": (c_int32, [H, ctypes.c_uint64, D, D, D]),
         "ffs_release": (c_int32, [H, ctypes.c_uint64]),
+        "ffs_cancel": (c_int32, [H, ctypes.c_uint64]),
         "ffs_server_pause": (c_int32, [H, c_int32]),
         "ffs_server_stats": (c_int32, [H, POINTER(FFSServerInfo)]),
         "ffs_server_last_error": (c_char_p, [H]),

@@ -172,7 +172,9 @@ class Engine : public EngineBase {
     I.les = p.les != 0;
     const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
     I.les_alpha = p.smag_c * p.smag_c * fw * fw;
+    I.les_model = p.les_model; I.les_c = p.smag_c; I.les_d2 = fw * fw; I.les_cp = p.les_cp; I.les_cb = p.sandp_cb;
     I.density = p.density != 0; I.gdir = p.gravity_dir;
+    I.scalar = p.passive_scalar != 0;
     I.alpha = p.density ? p.nu / p.density_pr : 0.0;
     I.dgrad = p.density_gradient; I.gval = p.gravity;
     I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
@@ -184,7 +186,24 @@ class Engine : public EngineBase {
 
   }
 
-  int create(const ffs_params& p, std::string& err) override {
+  int create(const ffs_params& p_in, std::string& err) override {
+    // a passive scalar rides the density's buffers and passes, with g = 0
+    // (simulationtypes.jl:198-213): the transport, mean-gradient source and diffusion are
+    // the same; buoyancy, the CFL cap, the stats columns and the spectra differ (I.scalar)
+    if (p_in.passive_scalar && (p_in.density || p_in.les)) {
+      err = p_in.density ? "a passive scalar together with density stratification is not supported"
+                         : "the passive scalar's LES eddy diffusion is not supported";
+      return FFS_EUNSUPPORTED;
+    }
+    ffs_params p = p_in;
+    if (p.passive_scalar) {
+      if (!(p.scalar_pr > 0) || p.scalar_dir < 0 || p.scalar_dir > 2) { err = "bad passive scalar parameters"; return FFS_EINVAL; }
+      p.density = 1;
+      p.density_pr = p.scalar_pr;
+      p.density_gradient = p.scalar_gradient;
+      p.gravity = 0.0;
+      p.gravity_dir = p.scalar_dir;
+    }
     P = p;
     memset(&I, 0, sizeof(I));
     if (p.nx <= 0 || p.ny <= 0 || p.nz <= 0) { err = "grid sizes must be positive"; return FFS_EINVAL; }
@@ -199,6 +218,14 @@ class Engine : public EngineBase {
     if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
     if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
     if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
+    if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_STABLE_NL)) {
+      err = "unknown LES model";
+      return FFS_EINVAL;
+    }
+    if (p.les && p.sandp_cb != 0.0 && p.les_model > FFS_LES_PRODUCTION) {
+      err = "SandP takes the Smagorinsky, Vreman or production-viscosity model";
+      return FFS_EINVAL;
+    }
     FFS_CK(cudaSetDevice(p.device));
     FFS_CK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     FFS_CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
@@ -311,7 +338,9 @@ class Engine : public EngineBase {
     }
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
     xfused = 0;
-    if (sizeof(T) == 4 && (I.les || !I.density) && p.kernel_variant != 1) {
+    // the register-fused LES x pass computes the Smagorinsky model only
+    const bool smag_only = !p.les || (p.les_model == FFS_LES_SMAGORINSKY && p.sandp_cb == 0.0);
+    if (sizeof(T) == 4 && (I.les || !I.density) && p.kernel_variant != 1 && smag_only) {
       int lyzf = 0, rf = 0;
       if (I.les) {   // LES (with or without density): n in {64, 128}
         if (p.nx == 64 || p.nx == 128) { lyzf = XLes<128>::LYZ; rf = XLes<128>::RR; }
@@ -361,7 +390,7 @@ class Engine : public EngineBase {
       n_sms = sms;
     }
     // record layout
-    ncols_stats = 22 + (I.density ? 8 : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
+    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
     ncols_rec = ncols_stats + 13;
     I.ncols = ncols_rec;
     I.rec_cap = p.stats_capacity > 0 ? p.stats_capacity : 256;
@@ -374,11 +403,11 @@ class Engine : public EngineBase {
     I.dkz = 1.0 / p.lz;
     I.nbinH = lenH; I.nbinV = lenV;
     I.spec_cap = p.spec_capacity > 0 ? p.spec_capacity : 16;
-    I.nspecf = SF_BASE_COUNT + (I.les ? 2 : 0) + (I.hv ? 2 : 0) + (I.density ? 4 : 0);
+    I.nspecf = SF_BASE_COUNT + (I.les ? 2 : 0) + (I.hv ? 2 : 0) + ((I.density && !I.scalar) ? 4 : 0);
     spec_names = "u_h,u_v,vis_h,vis_v,nl_h,nl_v,press_h,press_v";
     if (I.les) spec_names += ",les_h,les_v";
     if (I.hv) spec_names += ",hvis_h,hvis_v";
-    if (I.density) spec_names += ",buoyancy_v,rho,rhodiss,rhonl";
+    if (I.density && !I.scalar) spec_names += ",buoyancy_v,rho,rhodiss,rhonl";
     nspecf = I.nspecf;
     if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 2 * I.nspecf * std::max(lenH, lenV), err))) return rc;
     // ETD tables
@@ -400,7 +429,8 @@ class Engine : public EngineBase {
     // state and header
     if ((rc = reset_state(err))) return rc;
     header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
-    if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
+    if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
+    else if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
     if (I.les) header += ",prh,prv,praniso,pr";
     if (I.forcing) header += ",hp,vp,tp";
     if (I.hv) header += ",hdissh,hdissv,hdiss";

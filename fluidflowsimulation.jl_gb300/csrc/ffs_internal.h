@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/ffs.h"
 #include "ffs_fft.cuh"
 
 namespace ffsgpu {
@@ -115,7 +116,12 @@ template <typename T> struct Inst {
   double hv_nu;
   int les;
   double les_alpha;        // c^2 Delta^2
-  int density, gdir;
+  int les_model;           // FFS_LES_* (Smagorinsky, Vreman, production, Silvis, stable non-linear)
+  double les_c, les_d2;    // the model's constant c and Delta^2
+  double les_cp;           // Silvis P constant
+  double les_cb;           // SandP: cb (0: no P term)
+  int density, gdir;      // density: a fourth field (density, or with scalar the passive scalar)
+  int scalar;              // the fourth field is a passive scalar: no buoyancy, no CFL cap, own stats
   double alpha, dgrad, gval;
   int forcing;
   double f_eps, f_kf;

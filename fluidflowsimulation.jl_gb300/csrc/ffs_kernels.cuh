@@ -257,6 +257,127 @@ __device__ __forceinline__ void block_max_to_state(const Inst<T>& I, T umax, T r
   }
 }
 
+// tau of the pointwise LES models other than plain Smagorinsky (calc_les!,
+// les_real_calc.jl:13-139), from the strain S (traceless: xx, xy, xz, yy, yz) and the
+// vorticity w at one point. Om = AntiSymTen(w/2) is the rotation tensor (FluidTensors'
+// AntiSymTen(v) is taken as the cross-product matrix of v); Lie(A, B) = A B - B A.
+//   Vreman (VremanLESModel.jl): a = S - Om = grad u^T, beta = D^2 a^T a,
+//     nu_t = c sqrt(max(B_beta, 0) / a:a), tau = 2 nu_t S
+//   production viscosity (ProductionViscosityLESModel.jl): nu_t = max(0, c D^2 (Om^2:S - S^2:S) / (2 S:S))
+//   Silvis (silvismodel.jl): f = |S w| / (|S| |w|), nu_t = c^2 D^2 f^3 |S| / 2, nu_p = cp D^2 f^4 / 4,
+//     tau = 2 nu_t S + nu_p Lie(S, Om)
+//   stable non-linear (stablenonlinearmodel.jl): T = traceless(Om^2 + Lie(S, Om) - S^2),
+//     m = -min(0, c D^2 (Om^2:S - S^2:S) / (2 S:S)), tau = c D^2 T + 2 m S
+//   SandP (les_real_calc.jl:104-111): tau += cb D^2 Lie(S, Om)
+template <typename T>
+__device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz, T yy, T yz, T wx, T wy, T wz,
+                                              T* o) {
+  const T zz = -xx - yy;
+  const T S[3][3] = {{xx, xy, xz}, {xy, yy, yz}, {xz, yz, zz}};
+  const T p = T(0.5) * wx, q = T(0.5) * wy, r = T(0.5) * wz;
+  const T Om[3][3] = {{T(0), -r, q}, {r, T(0), -p}, {-q, p, T(0)}};
+  const T c = T(I.les_c), d2 = T(I.les_d2);
+  T t[3][3];
+  T ss = T(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) ss += S[i][j] * S[i][j];
+  // Lie(S, Om) = S Om - Om S, Om^2, S^2
+  T lie[3][3], om2[3][3], s2[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T a = T(0), b = T(0), e = T(0), g = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        a += S[i][k] * Om[k][j];
+        b += Om[i][k] * S[k][j];
+        e += Om[i][k] * Om[k][j];
+        g += S[i][k] * S[k][j];
+      }
+      lie[i][j] = a - b;
+      om2[i][j] = e;
+      s2[i][j] = g;
+    }
+  T om2s = T(0), s2s = T(0);
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) { om2s += om2[i][j] * S[i][j]; s2s += s2[i][j] * S[i][j]; }
+  const int m = I.les_model;
+  if (m == FFS_LES_VREMAN) {
+    T a[3][3], aa = T(0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { a[i][j] = S[i][j] - Om[i][j]; aa += a[i][j] * a[i][j]; }
+    T b[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        T v = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) v += a[k][i] * a[k][j];
+        b[i][j] = d2 * v;
+      }
+    T B = b[0][0] * (b[1][1] + b[2][2]) + b[1][1] * b[2][2] - (b[0][1] * b[0][1] + b[0][2] * b[0][2] + b[1][2] * b[1][2]);
+    B = B < T(0) ? T(0) : B;
+    const T nut = c * sqrt(B / aa);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] = T(2) * nut * S[i][j];
+  } else if (m == FFS_LES_PRODUCTION) {
+    const T qv = c * d2 * (om2s - s2s) / (T(2) * ss);
+    const T nut = ss == T(0) ? T(0) : (qv > T(0) ? qv : T(0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] = T(2) * nut * S[i][j];
+  } else if (m == FFS_LES_SILVIS) {
+    T sw[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) sw[i] = S[i][0] * wx + S[i][1] * wy + S[i][2] * wz;
+    const T fv = sqrt(sw[0] * sw[0] + sw[1] * sw[1] + sw[2] * sw[2]) / (sqrt(ss) * sqrt(wx * wx + wy * wy + wz * wz));
+    const T nut = c * c * d2 * fv * fv * fv * sqrt(ss) / T(2);
+    const T nup = T(I.les_cp) * d2 * fv * fv * fv * fv / T(4);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] = T(2) * nut * S[i][j] + nup * lie[i][j];
+  } else if (m == FFS_LES_STABLE_NL) {
+    T tt[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) tt[i][j] = om2[i][j] + lie[i][j] - s2[i][j];
+    const T tr = (tt[0][0] + tt[1][1] + tt[2][2]) / T(3);
+    const T qv = c * d2 * (om2s - s2s) / (T(2) * ss);
+    const T mnu = ss == T(0) ? T(0) : (qv < T(0) ? -qv : T(0));
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] = c * d2 * (tt[i][j] - (i == j ? tr : T(0))) + T(2) * mnu * S[i][j];
+  } else {   // Smagorinsky (with the SandP term below)
+    const T nut = c * c * d2 * sqrt(ss);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] = T(2) * nut * S[i][j];
+  }
+  if (I.les_cb != 0.0) {
+    const T beta = T(I.les_cb) * d2;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[i][j] += beta * lie[i][j];
+  }
+  o[0] = t[0][0]; o[1] = t[0][1]; o[2] = t[0][2]; o[3] = t[1][1]; o[4] = t[1][2];
+}
+
 template <bool LES, bool DEN> struct XFields {
   static constexpr int nin = 6 + (LES ? 5 : 0) + (DEN ? 1 : 0);
   static constexpr int nout = 4 + (LES ? 5 : 0) + (DEN ? 3 : 0);
@@ -337,10 +458,14 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
     umaxt = fmax(umaxt, fmax(fabs(ux), fmax(fabs(uy), fabs(uz))));
     if (LES) {
       const T xx = f[6], xy = f[7], xz = f[8], yy = f[9], yz = f[10];
-      const T zz = -xx - yy;
-      const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
-      const T two_nut = les2 * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
-      o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
+      if (I.les_model == FFS_LES_SMAGORINSKY && I.les_cb == 0.0) {
+        const T zz = -xx - yy;
+        const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
+        const T two_nut = les2 * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
+        o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
+      } else {
+        les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4);
+      }
     }
     if (DEN) {
       constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
@@ -436,7 +561,7 @@ __device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk b
       else if (it == 2) cfl *= 0.4;
       else if (it == 3) cfl *= 0.8;
       double newdt = dd::D(dd::M(cfl, dx), umax);
-      if (I.density) {
+      if (I.density && !I.scalar) {   // buoyancy cap (the passive scalar has none)
         const double den = dd::M(S.slot_rho, fabs(I.gval));
         newdt = fmin(newdt, dd::M(cfl, sqrt(dd::D(dx, den))));
       }
@@ -545,7 +670,15 @@ __device__ __forceinline__ void b_etd_table(const Inst<T>& I, int mode, const Bl
     T* e = I.etab + 4 * q;
     e[0] = T(E); e[1] = T(A); e[2] = T(B); e[3] = T(C);
     if (I.density && I.etab_rho) {
-      etd_coeffs_exact<sizeof(T) == 8>(dd::M(k2, -I.alpha), dt, dt2, dt3, stage, E, A, B, C);
+      // c = -alpha k^2; the passive scalar's ETD3rdO takes the velocity's hyperviscosity
+      // (simulationtypes.jl:336): muladd(k2, -alpha, k2^M * -nuh)
+      double cr = dd::M(k2, -I.alpha);
+      if (I.scalar && I.hv) {
+        double km = k2;
+        for (int m = 1; m < I.hv_m; ++m) km = dd::M(km, k2);
+        cr = dd::fma_e(k2, -I.alpha, dd::M(km, -I.hv_nu));
+      }
+      etd_coeffs_exact<sizeof(T) == 8>(cr, dt, dt2, dt3, stage, E, A, B, C);
       T* r = I.etab_rho + 4 * q;
       r[0] = T(E); r[1] = T(A); r[2] = T(B); r[3] = T(C);
     }
@@ -1073,7 +1206,7 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
       bin(f + 1, nuh * km * a2[2]);
       f += 2;
     }
-    if (I.density) {
+    if (I.density && !I.scalar) {
       const double r2 = (double)rho.x * rho.x + (double)rho.y * rho.y;
       const cplx<T> dF = sb[7 * cs + g];
       bin(f, gz * ((double)u[2].x * rho.x + (double)u[2].y * rho.y));   // buoyancy_v
@@ -1146,10 +1279,11 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       if (I.les) tdiss += -tot[Q_LESH] - tot[Q_LESV];
       if (I.hv) tdiss += I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);
       row[c++] = tdiss;
-      if (I.density) {
+      if (I.density) {   // density (BoussinesqApproximation stats) or scalar_stats (stats.jl:221-233)
         const double rd = I.alpha * (tot[Q_DR1] + tot[Q_DR2] + tot[Q_DR3]);
         row[c++] = tot[Q_RHO]; row[c++] = tot[Q_RHO2]; row[c++] = tot[Q_DR1]; row[c++] = tot[Q_DR2];
-        row[c++] = tot[Q_DR3]; row[c++] = rd; row[c++] = rd; row[c++] = -I.gval * tot[Q_BF];
+        row[c++] = tot[Q_DR3]; row[c++] = rd;
+        if (!I.scalar) { row[c++] = rd; row[c++] = -I.gval * tot[Q_BF]; }
       }
       if (I.les) {
         const double prh = -tot[Q_LESH], prv = -tot[Q_LESV];

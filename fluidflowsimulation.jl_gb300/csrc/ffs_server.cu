@@ -12,6 +12,11 @@
 //             -> simulations that reached nt leave the tables; after the next replay has
 //                been enqueued, their results are read on their own streams (ordered by
 //                an event after their last step) and the engine returns to the pool
+//             -> every kHealthEvery replays a one-CTA kernel copies each simulation's
+//                error flag (non-finite value seen by its update) to pinned host memory;
+//                the host reads the copy one interval later and retires a diverged
+//                simulation at once with FFS_ENAN, freeing its slot; cancelled requests
+//                (ffs_cancel) leave the queue or the batch the same way
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -44,6 +49,7 @@ struct Job {
   std::vector<double> u;   // initial fields, 3 * N
   double t_submit = -1, t_admit = -1, t_done = -1;
   int status = FFS_QUEUED;
+  bool cancel = false;     // ffs_cancel asked for it while pending or running
   std::string err;
   std::vector<double> stats;
   int ncols = 0;
@@ -60,8 +66,24 @@ struct Slot {
   bool retiring = false;
   int64_t done = 0;        // batched steps taken by the current job
   int64_t it0 = 0;         // iteration at admission
+  int early = 0;           // FFS_ENAN / FFS_ECANCELED: leaves the batch before nt
   BatchGeom g{};
 };
+
+// Error flags of the simulations in the batch (DevState::err), one per slot, gathered
+// from the finalize tables (one entry per simulation) so that only live parameter
+// blocks are read.
+__global__ void k_batch_health(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict__ T,
+                               unsigned* __restrict__ out) {
+  for (int c = 0; c < BATCH_NCLASS; ++c) {
+    const int n = T->n[c][BP_FIN];
+    for (int w = threadIdx.x; w < n; w += blockDim.x) {
+      const int k = T->tab[c][BP_FIN][w].inst;
+      out[k] = B[k].I.st->err;
+    }
+  }
+}
+constexpr int kHealthEvery = 8;   // replays between two health snapshots
 
 // plan threads per line (n / largest radix) and pass count, as make_plan builds them
 void plan_shape(int n, int& tpl, int& np) {
@@ -128,6 +150,12 @@ class Server {
   cudaStream_t cs[BATCH_NCLASS] = {};       // one branch of the step graph per class
   cudaEvent_t cev[BATCH_NCLASS + 1] = {};   // fork / join events of the capture
   std::vector<cudaEvent_t> ev_pool;
+  unsigned* d_health = nullptr;             // [max_active] error flags of the last snapshot
+  unsigned* h_health = nullptr;             // pinned copy
+  cudaEvent_t health_ev = nullptr;
+  std::vector<uint64_t> health_job;         // job id each slot held when the snapshot was taken
+  bool health_pending = false;
+  int64_t health_at = 0;                    // batch step of the pending snapshot
 
   ~Server() { shutdown(); }
 
@@ -244,6 +272,10 @@ class Server {
     memset(h_tab, 0, sizeof(BatchTables));
     SV_CK(cudaMemcpyAsync(d_tab, h_tab, sizeof(BatchTables), cudaMemcpyHostToDevice, S));
     for (int i = 0; i < 2; ++i) SV_CK(cudaEventCreateWithFlags(&h_ev[i], cudaEventDisableTiming));
+    SV_CK(cudaMalloc(&d_health, sizeof(unsigned) * cfg.max_active));
+    SV_CK(cudaMallocHost(&h_health, sizeof(unsigned) * cfg.max_active));
+    SV_CK(cudaEventCreateWithFlags(&health_ev, cudaEventDisableTiming));
+    health_job.assign(cfg.max_active, 0);
     SV_CK(cudaStreamSynchronize(S));
     // the step graph: one launch per pass, each walking its table
     // the step graph: S forks one branch per class; each branch is that class's chain
@@ -293,6 +325,10 @@ class Server {
     ev_pool.clear();
     if (d_inst) cudaFree(d_inst);
     if (h_inst) cudaFreeHost(h_inst);
+    if (d_health) cudaFree(d_health);
+    if (h_health) cudaFreeHost(h_health);
+    if (health_ev) cudaEventDestroy(health_ev);
+    d_health = nullptr; h_health = nullptr; health_ev = nullptr;
     if (d_tab) cudaFree(d_tab);
     if (h_tab) cudaFreeHost(h_tab);
     d_items = nullptr; d_inst = nullptr; h_inst = nullptr; d_tab = nullptr; h_tab = nullptr;
@@ -332,7 +368,10 @@ class Server {
   int submit(const ffs_request& r, uint64_t* id) {
     const ffs_params& p = r.params;
     if (p.precision != FFS_FP32) return fail_api(FFS_EUNSUPPORTED, "the server runs FP32 simulations only");
-    if (p.density) return fail_api(FFS_EUNSUPPORTED, "the server does not batch density-stratified runs");
+    if (p.density || p.passive_scalar)
+      return fail_api(FFS_EUNSUPPORTED, "the server does not batch density-stratified or passive-scalar runs");
+    if (p.les && (p.les_model != FFS_LES_SMAGORINSKY || p.sandp_cb != 0.0))
+      return fail_api(FFS_EUNSUPPORTED, "the server batches the Smagorinsky LES model only");
     int tpl, np;
     for (int n : {p.nx, p.ny, p.nz}) {
       plan_shape(n, tpl, np);
@@ -416,7 +455,7 @@ class Server {
     auto it = jobs.find(id);
     if (it == jobs.end()) { err = "unknown request id"; return FFS_EINVAL; }
     const Job& j = *it->second;
-    if (j.status != FFS_OK) { err = "request not finished"; return FFS_ESTATE; }
+    if (j.status == FFS_QUEUED || j.status == FFS_RUNNING) { err = "request not finished"; return FFS_ESTATE; }
     const int64_t have = j.ncols ? (int64_t)j.stats.size() / j.ncols : 0;
     if (!out) return have;
     const int64_t n = std::min(have, max_rows);
@@ -435,6 +474,29 @@ class Server {
     double* d[3] = {u1, u2, u3};
     for (int c = 0; c < 3; ++c)
       if (d[c]) memcpy(d[c], j.fields.data() + c * N, sizeof(double) * N);
+    return 0;
+  }
+
+  // cancel a queued or running request: a queued one leaves the queue now, a pending or
+  // running one when the serving thread next looks (before its next replay)
+  int cancel(uint64_t id) {
+    std::shared_ptr<Job> j;
+    {
+      std::lock_guard<std::mutex> g(mu);
+      auto it = jobs.find(id);
+      if (it == jobs.end()) { err = "unknown request id"; return FFS_EINVAL; }
+      j = it->second;
+      if (j->status != FFS_QUEUED && j->status != FFS_RUNNING) { err = "request already finished"; return FFS_ESTATE; }
+      j->cancel = true;
+      auto q = std::find(queue.begin(), queue.end(), j);
+      if (q == queue.end()) {
+        cv_work.notify_all();
+        return 0;
+      }
+      queue.erase(q);
+      info.queued = (int32_t)queue.size();
+    }
+    finish_job(j, FFS_ECANCELED, "cancelled while queued");
     return 0;
   }
 
@@ -665,7 +727,18 @@ class Server {
     std::shared_ptr<Job> j = s.job;
     std::string e;
     int rc = ev ? s.eng->stream_wait(ev, e) : 0;
-    if (!rc && j->nt > 0) rc = s.eng->sync_host_state(s.it0, s.it0 + j->nt - 1, e);
+    const int64_t steps = s.early ? s.done : j->nt;   // steps the simulation took in the batch
+    if (!rc && steps > 0) rc = s.eng->sync_host_state(s.it0, s.it0 + steps - 1, e);
+    if (s.early == FFS_ENAN && rc == 0) {   // the flag was seen; the drain did not (cannot happen)
+      rc = FFS_ENAN;
+      e = "non-finite value in the spectral state (simulation diverged)";
+    }
+    if (s.early == FFS_ECANCELED) {
+      rc = FFS_ECANCELED;
+      e = "cancelled after " + std::to_string(s.done) + " of " + std::to_string(j->nt) + " steps";
+    } else if (s.early == FFS_ENAN) {
+      e += "; retired after " + std::to_string(s.done) + " of " + std::to_string(j->nt) + " steps";
+    }
     std::vector<double> fields;
     if (!rc && j->keep_fields) {
       const size_t N = (size_t)j->p.nx * j->p.ny * j->p.nz;
@@ -684,6 +757,66 @@ class Server {
     finish_job(j, rc, e);
     s.job.reset();
     s.retiring = false;
+    s.early = 0;
+  }
+
+  // Health snapshot and cancellations, before the next replay. A simulation found
+  // diverged (its update saw a non-finite value) or cancelled leaves the tables now; its
+  // results are read after the replays already queued for it, like a normal finisher's.
+  void check_early(int& active, bool& changed, std::vector<std::pair<int, cudaEvent_t>>& retiring) {
+    std::vector<int> out;
+    int64_t bs;
+    {
+      std::lock_guard<std::mutex> g(mu);
+      bs = info.batch_steps;
+    }
+    // a snapshot one interval old is waited for: the host then never runs more than two
+    // intervals of replays ahead of the GPU, which bounds how long a diverged simulation
+    // keeps its slot
+    if (health_pending && (bs - health_at >= kHealthEvery ? cudaEventSynchronize(health_ev)
+                                                           : cudaEventQuery(health_ev)) == cudaSuccess) {
+      health_pending = false;
+      for (int k = 0; k < (int)slots.size(); ++k) {
+        Slot& s = slots[k];
+        if (s.job && !s.retiring && health_job[k] == s.job->id && (h_health[k] & 1u)) {
+          s.early = FFS_ENAN;
+          out.push_back(k);
+        }
+      }
+    }
+    {
+      std::lock_guard<std::mutex> g(mu);
+      for (int k = 0; k < (int)slots.size(); ++k) {
+        Slot& s = slots[k];
+        if (s.job && !s.retiring && !s.early && s.job->cancel) {
+          s.early = FFS_ECANCELED;
+          out.push_back(k);
+        }
+      }
+    }
+    if (out.empty()) return;
+    cudaEvent_t ev = get_event();
+    cudaEventRecord(ev, S);   // after every replay enqueued so far
+    for (int k : out) {
+      slots[k].retiring = true;
+      --active;
+      changed = true;
+      retiring.push_back({k, ev});
+    }
+  }
+
+  // enqueue a health snapshot behind the replays enqueued so far
+  void snapshot_health() {
+    if (health_pending) return;
+    cudaMemsetAsync(d_health, 0, sizeof(unsigned) * slots.size(), S);
+    k_batch_health<<<1, 256, 0, S>>>(d_inst, d_tab, d_health);
+    cudaMemcpyAsync(h_health, d_health, sizeof(unsigned) * slots.size(), cudaMemcpyDeviceToHost, S);
+    for (int k = 0; k < (int)slots.size(); ++k)
+      health_job[k] = (slots[k].job && !slots[k].retiring) ? slots[k].job->id : 0;
+    cudaEventRecord(health_ev, S);
+    health_pending = true;
+    std::lock_guard<std::mutex> g(mu);
+    health_at = info.batch_steps;
   }
 
   void loop() {
@@ -713,7 +846,18 @@ class Server {
         if (!paused)
           while (!queue.empty()) { pending.push_back(queue.front()); queue.pop_front(); }
       }
-      // admission
+      // admission (a request cancelled after it left the queue is dropped here)
+      {
+        std::vector<std::shared_ptr<Job>> dropped;
+        {
+          std::lock_guard<std::mutex> g(mu);
+          for (auto it = pending.begin(); it != pending.end();) {
+            if ((*it)->cancel) { dropped.push_back(*it); it = pending.erase(it); }
+            else ++it;
+          }
+        }
+        for (auto& j : dropped) finish_job(j, FFS_ECANCELED, "cancelled before admission");
+      }
       while (!pending.empty() && active < cfg.max_active) {
         if (!admit(pending.front(), dirty)) break;
         const bool running = pending.front()->status == FFS_RUNNING;
@@ -728,6 +872,7 @@ class Server {
         info.bytes_in_use = bytes_in_use;
         info.peak_bytes = std::max(info.peak_bytes, bytes_in_use);
       }
+      if (active > 0) check_early(active, changed, retiring);
       if (changed) {
         if (rebuild_tables(dirty)) { fail(err); break; }
         dirty.clear();
@@ -752,11 +897,14 @@ class Server {
             now.push_back({k, ev});
           }
         }
+        int64_t bs;
         {
           std::lock_guard<std::mutex> g(mu);
           info.batch_steps += 1;
           info.sim_steps += sims;
+          bs = info.batch_steps;
         }
+        if (bs % kHealthEvery == 0) snapshot_health();
         if (now.empty()) ev_pool.push_back(ev);
         // results of the previous replay's finishers, while this replay runs
         for (auto& r : retiring) retire(r.first, r.second);
@@ -857,6 +1005,7 @@ int ffs_fetch_fields(ffs_server* s, uint64_t id, double* u1, double* u2, double*
   FFS_SERVER_GUARD(s->s.fetch_fields(id, u1, u2, u3))
 }
 int ffs_release(ffs_server* s, uint64_t id) { FFS_SERVER_GUARD(s->s.release(id)) }
+int ffs_cancel(ffs_server* s, uint64_t id) { FFS_SERVER_GUARD(s->s.cancel(id)) }
 int ffs_server_pause(ffs_server* s, int32_t paused) { FFS_SERVER_GUARD(s->s.pause(paused)) }
 int ffs_server_stats(ffs_server* s, ffs_server_info* o) {
   if (!o) return FFS_EINVAL;

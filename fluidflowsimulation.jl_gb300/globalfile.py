@@ -12,7 +12,7 @@ import math
 import re
 from pathlib import Path
 
-from ._lib import FFS_AB3, FFS_ETD3, FFS_FP32, FFS_FP64, FFSParams, load
+from ._lib import FFS_AB3, FFS_ETD3, FFS_FP32, FFS_FP64, LES_MODELS, FFSParams, load
 
 
 def readglobal(path: str | Path = "global") -> dict[str, str]:
@@ -38,6 +38,43 @@ def parse_number(s: str) -> float:
 
 def _bool(s: str) -> bool:
     return s.strip().lower() == "true"
+
+
+# constant key and default of each pointwise LES model (les_types.jl:360-395)
+_LES_CONST = {"Smagorinsky": ("smagorinskyConstant", 0.17), "Vreman": ("vremanConstant", 0.032),
+              "productionViscosity": ("productionConstant", 0.4), "Silvis": ("silvisConstant", math.sqrt(0.17)),
+              "stableNonLinear": ("nlConstant", 0.1)}
+
+
+def _set_les(p: FFSParams, d: dict[str, str]) -> None:
+    """lesModel (les_types.jl:360-395): Smagorinsky, Vreman, productionViscosity, Silvis,
+    stableNonLinear, or SandP (the P tensor term on top of sLesModel = Smagorinsky, Vreman
+    or productionViscosity). The dynamic models (test-filtered coefficient) are not built."""
+    m = d["lesModel"]
+    base = m
+    if m == "SandP":
+        base = d.get("sLesModel", "")
+        if base not in ("Smagorinsky", "Vreman", "productionViscosity"):
+            raise ValueError(f"SandP with sLesModel {base!r} is not supported (Smagorinsky, Vreman, "
+                             "productionViscosity)")
+        p.sandp_cb = parse_number(d.get("pConstant", "0.09"))
+    if base not in _LES_CONST:
+        raise ValueError(f"lesModel {m!r} is not supported (Smagorinsky, Vreman, productionViscosity, Silvis, "
+                         "stableNonLinear, SandP)")
+    key, dflt = _LES_CONST[base]
+    if m == "SandP" and base == "productionViscosity":
+        dflt = 0.1                                           # les_types.jl:402
+    p.les = 1
+    p.les_model = LES_MODELS[base]
+    p.smag_c = parse_number(d[key]) if key in d else dflt
+    if base == "Silvis":
+        p.les_cp = parse_number(d.get("silvisPConstant", "5.0"))
+    if "filterWidth" in d:
+        p.filter_width = parse_number(d["filterWidth"])
+    elif m == "SandP" and base == "Smagorinsky":             # les_types.jl:395: twice the default
+        p.filter_width = 2 * (p.lx * 2 * math.pi / p.nx) / p.cutoff
+    else:
+        p.filter_width = 0.0                                 # the engine's default (lx 2 pi / nx) / cutoff
 
 
 def parameters(d: dict[str, str], precision: str | None = None, device: int = 0) -> FFSParams:
@@ -73,11 +110,7 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
         p.hv_nu = float(d["hyperViscosityCoefficient"])
         p.hv_m = int(d.get("hyperViscosityM", "2"))
     if "lesModel" in d:
-        if d["lesModel"] != "Smagorinsky":
-            raise ValueError(f"lesModel {d['lesModel']!r} is not supported (Smagorinsky)")
-        p.les = 1
-        p.smag_c = parse_number(d.get("smagorinskyConstant", "0.17"))
-        p.filter_width = parse_number(d["filterWidth"]) if "filterWidth" in d else 0.0
+        _set_les(p, d)
     if "densityStratification" in d:
         p.density = 1
         p.density_pr = parse_number(d["Pr"])
@@ -86,8 +119,15 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
         p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
         if "densityLesModel" in d or "densityHyperViscosity" in d:
             raise ValueError("density LES / density hyperviscosity are not supported")
-    if "passiveScalar" in d:
-        raise ValueError("passiveScalar is not supported")
+    if "passiveScalar" in d:   # simulationtypes.jl:320-352
+        if "lesModel" in d or "scalarLesModel" in d:
+            raise ValueError("the passive scalar's LES eddy diffusion is not supported")
+        if "densityStratification" in d:
+            raise ValueError("a passive scalar together with density stratification is not supported")
+        p.passive_scalar = 1
+        p.scalar_pr = parse_number(d["scalarPr"])
+        p.scalar_gradient = parse_number(d["scalarGradient"])
+        p.scalar_dir = {"x": 0, "y": 1, "z": 2}[d.get("scalarDirection", "z")]
     if d.get("equation", "") == "NS":
         raise ValueError("equation NS (conservation form) is not supported")
     if "forcing" in d:

@@ -31,6 +31,8 @@ mutable struct FFSParams
     device::Int32; reference_cfl_slot::Int32
     stats_capacity::Int32; spec_capacity::Int32; kernel_variant::Int32
     autotune::Int32
+    les_model::Int32; les_cp::Float64; sandp_cb::Float64
+    passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     FFSParams() = new()
 end
 
@@ -80,10 +82,25 @@ function parameters(d)
         p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
         p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
     end
-    if get(d, :lesModel, "") == "Smagorinsky"
-        p.les = 1
-        p.smag_c = haskey(d, :smagorinskyConstant) ? num(d[:smagorinskyConstant]) : 0.17
-        p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) : 0.0
+    if haskey(d, :lesModel)   # pointwise models of les_types (les_types.jl:360-395)
+        m = d[:lesModel]; base = m == "SandP" ? d[:sLesModel] : m
+        consts = Dict("Smagorinsky" => (:smagorinskyConstant, 0.17), "Vreman" => (:vremanConstant, 0.032),
+                      "productionViscosity" => (:productionConstant, m == "SandP" ? 0.1 : 0.4),
+                      "Silvis" => (:silvisConstant, sqrt(0.17)), "stableNonLinear" => (:nlConstant, 0.1))
+        haskey(consts, base) || error("lesModel $m is not supported")
+        models = Dict("Smagorinsky" => 0, "Vreman" => 1, "productionViscosity" => 2, "Silvis" => 3,
+                      "stableNonLinear" => 4)
+        key, dflt = consts[base]
+        p.les = 1; p.les_model = models[base]
+        p.smag_c = haskey(d, key) ? num(d[key]) : dflt
+        p.les_cp = haskey(d, :silvisPConstant) ? num(d[:silvisPConstant]) : 5.0
+        p.sandp_cb = m == "SandP" ? (haskey(d, :pConstant) ? num(d[:pConstant]) : 0.09) : 0.0
+        p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) :
+                         (m == "SandP" && base == "Smagorinsky") ? 2 * (p.lx * 2π / p.nx) / p.cutoff : 0.0
+    end
+    if haskey(d, :passiveScalar)   # simulationtypes.jl:320-352 (no scalar LES here)
+        p.passive_scalar = 1; p.scalar_pr = num(d[:scalarPr]); p.scalar_gradient = num(d[:scalarGradient])
+        p.scalar_dir = Dict("x" => 0, "y" => 1, "z" => 2)[get(d, :scalarDirection, "z")]
     end
     if haskey(d, :densityStratification)
         p.density = 1; p.density_pr = num(d[:Pr]); p.density_gradient = num(d[:densityGradient])
@@ -117,7 +134,7 @@ simtime(e::Engine) = ccall((:ffs_time, LIB), Float64, (Ptr{Cvoid},), e.h)
 function getfields(e::Engine)
     p = e.p
     out = [Array{Float64}(undef, p.nx, p.ny, p.nz) for _ in 1:4]
-    rho = p.density == 1 ? pointer(out[4]) : C_NULL
+    rho = (p.density == 1 || p.passive_scalar == 1) ? pointer(out[4]) : C_NULL
     GC.@preserve out check(e, ccall((:ffs_get_fields, LIB), Cint,
         (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Cint), e.h, out[1], out[2], out[3], rho, 0))
     return out
@@ -241,6 +258,7 @@ function writeoutput(e::Engine)
     f = getfields(e); i = iteration(e)
     write("u1.$i", f[1]); write("u2.$i", f[2]); write("u3.$i", f[3])
     e.p.density == 1 && write("rho.$i", f[4])
+    e.p.passive_scalar == 1 && write("scalar.$i", f[4])   # output.jl: scalar.N
 end
 
 # run_simulation() of src/FluidFlowSimulation.jl:23-65
@@ -250,7 +268,9 @@ function run_simulation()
     e = Engine(p)
     s = p.start
     u = [open(f -> readfield(f, p.nx, p.ny, p.nz), "u$i.$s") for i in 1:3]
-    rho = (p.density == 1 && isfile("rho.$s")) ? open(f -> readfield(f, p.nx, p.ny, p.nz), "rho.$s") : nothing
+    fname = p.passive_scalar == 1 ? "scalar.$s" : "rho.$s"
+    rho = ((p.density == 1 || p.passive_scalar == 1) && isfile(fname)) ?
+          open(f -> readfield(f, p.nx, p.ny, p.nz), fname) : nothing
     setfields!(e, u..., rho)
     if s == 0
         open(f -> write(f, statsheader(e), "\n"), "Stats.txt", "w")

@@ -93,6 +93,10 @@ class Server:
         self._check(self.L.ffs_fetch_fields(self.h, rid, *(_ptr(x) for x in u)))
         return tuple(u)
 
+    def cancel(self, rid: int) -> None:
+        """Cancel a queued or running request (it finishes with FFS_ECANCELED)."""
+        self._check(self.L.ffs_cancel(self.h, rid))
+
     def release(self, rid: int) -> None:
         self._check(self.L.ffs_release(self.h, rid))
         self._shape.pop(rid, None)

@@ -65,7 +65,8 @@ class Simulation:
         lh, lv = c_int32(), c_int32()
         self._check(self._L.ffs_spectrum_lengths(h, byref(lh), byref(lv)))
         self.lenH, self.lenV = lh.value, lv.value
-        self.has_density = bool(params.density)
+        self.has_density = bool(params.density or params.passive_scalar)   # a fourth field
+        self.scalar_name = "scalar" if params.passive_scalar else "rho"
 
     @classmethod
     def from_global(cls, d: dict, precision: str | None = None, device: int = 0) -> "Simulation":
@@ -280,9 +281,9 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     p = sim.params
     start = int(p.start)
     u = [_fields.read_field(folder / f"u{i}.{start}", p.nx, p.ny, p.nz) for i in (1, 2, 3)]
-    rho = None
-    if p.density and (folder / f"rho.{start}").exists():
-        rho = _fields.read_field(folder / f"rho.{start}", p.nx, p.ny, p.nz)
+    rho = None   # rho.$start (density_stratification_types.jl:166) or scalar.$start (simulationtypes.jl:325)
+    if sim.has_density and (folder / f"{sim.scalar_name}.{start}").exists():
+        rho = _fields.read_field(folder / f"{sim.scalar_name}.{start}", p.nx, p.ny, p.nz)
     sim.set_fields(*u, rho)
     total = int(d["nt"]) if "nt" in d else (1 << 62) - start
     lengthtime = float(d["timeDuration"]) if "timeDuration" in d else float("inf")
@@ -334,10 +335,10 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
 
 
 def _write_output(folder: Path, sim: Simulation) -> None:
-    """``writeoutput`` (src/output.jl:1-8): u1.N u2.N u3.N (+ rho.N)."""
+    """``writeoutput`` (src/output.jl:1-30): u1.N u2.N u3.N (+ rho.N or scalar.N)."""
     f = sim.fields()
     i = sim.iteration
     for k in range(3):
         _fields.write_field(folder / f"u{k + 1}.{i}", f[k])
     if sim.has_density:
-        _fields.write_field(folder / f"rho.{i}", f[3])
+        _fields.write_field(folder / f"{sim.scalar_name}.{i}", f[3])

@@ -34,6 +34,7 @@ extern "C" {
 #define FFS_ETIMEDOUT (-5)
 #define FFS_EUNSUPPORTED (-6)
 #define FFS_ESTATE (-7)
+#define FFS_ECANCELED (-8)
 
 #define FFS_ETD3 0 /* ETD3rdO (src/time_step_functions/ETD.jl) */
 #define FFS_AB3 1  /* Adams_Bashforth3rdO (src/time_step_functions/Adams_Bashforth.jl) */
@@ -83,7 +84,24 @@ typedef struct ffs_params {
                                   2: as 0 with every compile-time y/z pass on line pairs (packed FP32);
                                   3: as 0 with every compile-time y/z pass one line per thread */
   int32_t autotune;            /* 1: time the candidate launch shapes at create, keep the fastest */
+  int32_t les_model;           /* with les != 0, the eddy-viscosity model of lesModel (les_types.jl:360-395):
+                                  FFS_LES_SMAGORINSKY, FFS_LES_VREMAN, FFS_LES_PRODUCTION, FFS_LES_SILVIS,
+                                  FFS_LES_STABLE_NL; smag_c holds that model's constant */
+  double les_cp;               /* silvisPConstant (Silvis model) */
+  double sandp_cb;             /* lesModel SandP: pConstant of the P tensor term (0: none) */
+  int32_t passive_scalar;      /* passiveScalar (simulationtypes.jl:198-213, :320-352): a scalar phi
+                                  transported like the density, without buoyancy; the fourth
+                                  field of ffs_set_fields / ffs_get_fields (scalar.N files) */
+  double scalar_pr;            /* scalarPr: diffusivity nu / scalarPr */
+  double scalar_gradient;      /* scalarGradient: mean gradient d phi / d(direction) */
+  int32_t scalar_dir;          /* scalarDirection: 0 x, 1 y, 2 z */
 } ffs_params;
+
+#define FFS_LES_SMAGORINSKY 0 /* nu_t = c^2 D^2 |S| (les_real_calc.jl:77-79) */
+#define FFS_LES_VREMAN 1      /* VremanLESModel.jl, les_real_calc.jl:132-139 */
+#define FFS_LES_PRODUCTION 2  /* ProductionViscosityLESModel.jl */
+#define FFS_LES_SILVIS 3      /* silvismodel.jl */
+#define FFS_LES_STABLE_NL 4   /* stablenonlinearmodel.jl */
 
 /* Fill defaults: reference defaults for every key that has one. */
 int ffs_params_default(ffs_params* p);
@@ -213,7 +231,9 @@ void ffs_destroy(ffs_handle* h);
  * simulation by one step per replay of a single CUDA graph whose kernels walk a work
  * table of (simulation, block) entries. Finished simulations leave the table and their
  * buffers return to a pool for requests of the same grid and model. Each simulation's
- * arithmetic is the same alone and in any mix.
+ * arithmetic is the same alone and in any mix. Every few replays the thread reads each
+ * simulation's error flag; a simulation that produced a non-finite value leaves the
+ * batch at once with status FFS_ENAN and frees its slot.
  * Thread safety: every ffs_server entry point may be called from any host thread.
  * --------------------------------------------------------------------------------- */
 typedef struct ffs_server ffs_server;
@@ -272,6 +292,10 @@ int64_t ffs_fetch_stats(ffs_server* s, uint64_t id, double* out, int64_t max_row
 int ffs_fetch_fields(ffs_server* s, uint64_t id, double* u1, double* u2, double* u3);
 /* Forget a finished request and its results. */
 int ffs_release(ffs_server* s, uint64_t id);
+/* Cancel a queued or running request: it finishes with status FFS_ECANCELED (a running
+ * one before its next batched step; the stats records of the steps it took stay
+ * fetchable). FFS_ESTATE when the request has already finished. */
+int ffs_cancel(ffs_server* s, uint64_t id);
 /* Hold (1) or resume (0) admission: queued requests wait while the batch keeps running. */
 int ffs_server_pause(ffs_server* s, int32_t paused);
 int ffs_server_stats(ffs_server* s, ffs_server_info* out);

@@ -146,8 +146,15 @@ class Params:
     hv_nu: float = 0.0
     hv_m: int = 2
     les: bool = False
-    smag_c: float = 0.17
+    les_model: str = "Smagorinsky"       # Smagorinsky, Vreman, productionViscosity, Silvis, stableNonLinear
+    smag_c: float = 0.17                 # the model's constant c
+    les_cp: float = 5.0                  # silvisPConstant
+    sandp_cb: float = 0.0                # SandP: pConstant (0: no P term)
     filter_width: float | None = None
+    scalar: bool = False                 # passiveScalar (simulationtypes.jl:198-213, :320-352)
+    scalar_pr: float = 1.0
+    scalar_gradient: float = 0.0
+    scalar_dir: int = 2
     density: bool = False
     density_pr: float = 1.0
     density_gradient: float = 0.0
@@ -185,17 +192,23 @@ class Params:
             p.hv = True
             p.hv_nu = float(d["hyperViscosityCoefficient"])
             p.hv_m = int(d.get("hyperViscosityM", 2))
-        if d.get("lesModel") == "Smagorinsky":
-            p.les = True
-            p.smag_c = _num(d.get("smagorinskyConstant", "0.17"))
-            p.filter_width = (_num(d["filterWidth"]) if "filterWidth" in d
-                              else (p.lx * 2 * math.pi / p.nx) / p.cutoff)   # les_types.jl:366
+        if "lesModel" in d:
+            p.set_les(d)
         if "densityStratification" in d:
             p.density = True
             p.density_pr = _num(d["Pr"])
             p.density_gradient = _num(d["densityGradient"])
             p.gravity = _num(d["zAcceleration"]) / _num(d["referenceDensity"])
             p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
+        if "passiveScalar" in d:
+            if "densityStratification" in d:
+                raise ValueError("a passive scalar together with density stratification is not restated")
+            if "lesModel" in d:
+                raise ValueError("the passive scalar's LES eddy diffusion is not restated")
+            p.scalar = True
+            p.scalar_pr = _num(d["scalarPr"])
+            p.scalar_gradient = _num(d["scalarGradient"])
+            p.scalar_dir = {"x": 0, "y": 1, "z": 2}[d.get("scalarDirection", "z")]
         if d.get("forcing") == "isotropicBand":
             p.forcing = True
             p.forcing_power = _num(d.get("forcingPower", "0.1"))
@@ -203,6 +216,44 @@ class Params:
         if "referenceCflSlot" in d:
             p.reference_cfl_slot = d["referenceCflSlot"].strip().lower() == "true"
         return p
+
+    def set_les(self, d: dict) -> None:
+        """The pointwise LES models of ``les_types`` (les_types.jl:360-395): the model's
+        constant and filter width with the reference's defaults; SandP adds the P tensor
+        to an eddy-viscosity model (sLesModel)."""
+        m = d["lesModel"]
+        base = m
+        if m == "SandP":
+            base = d["sLesModel"]
+            self.sandp_cb = _num(d.get("pConstant", "0.09"))
+        consts = {"Smagorinsky": ("smagorinskyConstant", 0.17), "Vreman": ("vremanConstant", 0.032),
+                  "productionViscosity": ("productionConstant", 0.1 if m == "SandP" else 0.4),
+                  "Silvis": ("silvisConstant", math.sqrt(0.17)), "stableNonLinear": ("nlConstant", 0.1)}
+        if base not in consts or (m == "SandP" and base in ("Silvis", "stableNonLinear")):
+            raise ValueError(f"LES model {m} / {base} is not restated")
+        key, dflt = consts[base]
+        self.les = True
+        self.les_model = base
+        self.smag_c = _num(d[key]) if key in d else dflt
+        if base == "Silvis":
+            self.les_cp = _num(d["silvisPConstant"]) if "silvisPConstant" in d else 5.0
+        dx = (self.lx * 2 * math.pi / self.nx) / self.cutoff
+        if m == "SandP" and base == "Smagorinsky":
+            dx = 2 * dx                                         # les_types.jl:395
+        self.filter_width = _num(d["filterWidth"]) if "filterWidth" in d else dx
+
+    @property
+    def fld(self) -> bool:
+        """A transported scalar field rides beside the velocity (density or passive scalar)."""
+        return self.density or self.scalar
+
+    @property
+    def fld_grad(self) -> float:
+        return self.density_gradient if self.density else self.scalar_gradient
+
+    @property
+    def fld_dir(self) -> int:
+        return self.gravity_dir if self.density else self.scalar_dir
 
     @property
     def ab3(self) -> bool:
@@ -394,6 +445,8 @@ STATS_HEADER = ("iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dis
 def stats_header(p: Params) -> str:
     """``statsheader`` (stats.jl:1-7); plug-in order = sim_fields (macros.jl:48)."""
     cols = [STATS_HEADER]
+    if p.scalar:
+        cols.append("scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss")
     if p.density:
         cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux")
     if p.les:
@@ -465,6 +518,84 @@ def scales_numbers_from(u1p2, u2p2, u3p2, k, tdiss, L, D, nu, density, n2):
     return [float(x) for x in lens], [float(x) for x in anums]
 
 
+def _sym33(Sr):
+    """3x3 symmetric tensor field from the 5 traceless components xx, xy, xz, yy, yz."""
+    xx, xy, xz, yy, yz = Sr
+    zz = -xx - yy
+    return np.array([[xx, xy, xz], [xy, yy, yz], [xz, yz, zz]])
+
+
+def _antisym(v):
+    """AntiSymTen(v) of FluidTensors, taken as the cross-product matrix [v]x (A b = v x b),
+    so that AntiSymTen(w/2) is the rotation tensor (grad u - grad u^T)/2 for w = curl u."""
+    x, y, z = v
+    o = np.zeros_like(x)
+    return np.array([[o, -z, y], [z, o, -x], [-y, x, o]])
+
+
+def _mm(a, b):
+    return np.einsum("ik...,kj...->ij...", a, b)
+
+
+def _ddot(a, b):
+    return np.einsum("ij...,ij...->...", a, b)
+
+
+def _to5(t):
+    """Traceless symmetric tensor field -> the 5 stored components."""
+    return np.stack([t[0, 0], t[0, 1], t[0, 2], t[1, 1], t[1, 2]])
+
+
+def les_stress(p: "Params", Sr, wr):
+    """tau of the pointwise LES models in physical space (calc_les!, les_real_calc.jl:13-139):
+    Smagorinsky nu_t = c^2 D^2 |S| (:77-79); Vreman (:132-139, VremanLESModel.jl); the
+    production-viscosity model (ProductionViscosityLESModel.jl); Silvis (silvismodel.jl);
+    the stable non-linear model (stablenonlinearmodel.jl); the SandP P term
+    cb D^2 Lie(S, AntiSymTen(w/2)) (:104-111). |S| is the Frobenius norm sqrt(S:S);
+    Lie(A, B) = A B - B A."""
+    S = _sym33(Sr)
+    d2 = p.filter_width ** 2
+    c = p.smag_c
+    ss = _ddot(S, S)
+    m = p.les_model
+    with np.errstate(divide="ignore", invalid="ignore"):
+        if m == "Smagorinsky":
+            xx, xy, xz, yy, yz = Sr
+            zz = -xx - yy
+            nrm = np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
+            t = 2.0 * (c * c * d2 * nrm) * S
+        elif m == "Vreman":
+            a = S + _antisym(-0.5 * wr)
+            b = d2 * _mm(np.swapaxes(a, 0, 1), a)
+            B = b[0, 0] * (b[1, 1] + b[2, 2]) + b[1, 1] * b[2, 2] - (b[0, 1] ** 2 + b[0, 2] ** 2 + b[1, 2] ** 2)
+            B = np.where(B < 0.0, 0.0, B)
+            t = 2.0 * (c * np.sqrt(B / _ddot(a, a))) * S
+        elif m == "productionViscosity":
+            W = _antisym(-0.5 * wr)
+            q = c * d2 * (_ddot(_mm(W, W), S) - _ddot(_mm(S, S), S)) / (2 * ss)
+            t = 2.0 * np.where(ss == 0.0, 0.0, np.maximum(0.0, q)) * S
+        elif m == "Silvis":
+            Sw = np.einsum("ij...,j...->i...", S, wr)
+            fv = np.sqrt(_ddot(Sw[:, None], Sw[:, None])) / (np.sqrt(ss) * np.sqrt(np.sum(wr * wr, axis=0)))
+            nut = c * c * d2 * fv * fv * fv * np.sqrt(ss) / 2
+            nup = p.les_cp * d2 * fv * fv * fv * fv / 4
+            Om = _antisym(0.5 * wr)
+            t = 2.0 * nut * S + nup * (_mm(S, Om) - _mm(Om, S))
+        elif m == "stableNonLinear":
+            W = _antisym(-0.5 * wr)
+            T = _mm(W, W) - (_mm(S, W) - _mm(W, S)) - _mm(S, S)
+            T = T - (np.trace(T) / 3.0) * np.eye(3).reshape(3, 3, *([1] * (T.ndim - 2)))
+            q = c * d2 * (_ddot(_mm(W, W), S) - _ddot(_mm(S, S), S)) / (2 * ss)
+            mnu = np.where(ss == 0.0, 0.0, -np.minimum(0.0, q))
+            t = c * d2 * T + 2.0 * mnu * S
+        else:
+            raise ValueError(m)
+        if p.sandp_cb:
+            Om = _antisym(0.5 * wr)
+            t = t + (p.sandp_cb * d2) * (_mm(S, Om) - _mm(Om, S))
+    return _to5(t)
+
+
 class OracleSimulation:
     """FP64 restatement of the reference Simulation for the in-scope plug-ins."""
 
@@ -474,8 +605,8 @@ class OracleSimulation:
         self.iteration = p.start
         self.time = p.start_time
         self.u = np.stack([np.asarray(x, dtype=np.float64) for x in u_phys])   # physical at first
-        self.rho = None
-        if p.density:
+        self.rho = None                   # density, or the passive scalar phi
+        if p.fld:
             self.rho = (np.zeros((p.nz, p.ny, p.nx)) if rho_phys is None
                         else np.asarray(rho_phys, dtype=np.float64))
         # c = -nu k^2 (init_c!, ETD.jl:60-69) or muladd(k2, -nu, k2^M * -nuh) (init_c_hv!,
@@ -492,10 +623,14 @@ class OracleSimulation:
             self.ts = AB3(p.variable_dt, p.dt)
         else:
             self.ts = ETD3(p.variable_dt, p.dt, c)
-        if p.density:
-            alpha = p.nu / p.density_pr
+        if p.fld:
+            alpha = p.nu / (p.density_pr if p.density else p.scalar_pr)
             if p.ab3:
                 self.rts = AB3(p.variable_dt, p.dt)
+            elif p.scalar and p.hv:
+                # the scalar's ETD3rdO takes the velocity's hyperviscosity (simulationtypes.jl
+                # :336 passes the hyperviscositytype of :293-305): muladd(k2, -alpha, k2^M -nuh)
+                self.rts = ETD3(p.variable_dt, p.dt, dd.fma(k2, np.full_like(k2, -alpha), km * (-p.hv_nu)))
             else:
                 self.rts = ETD3(p.variable_dt, p.dt, k2 * (-alpha))
             self.alpha = alpha
@@ -535,12 +670,12 @@ class OracleSimulation:
         """``initialize!(s)`` (FluidFlowSimulation.jl:67-91)."""
         g = self.g
         self.u = g.myfourier(self.u)
-        if self.p.density:
+        if self.p.fld:
             self.rho = g.myfourier(self.rho)
         self.calculate_rhs()
         dt_now = self.get_dt()
         self.ts.initialize(self.rhs, dt_now)
-        if self.p.density:
+        if self.p.fld:
             self.rts.initialize(self.rhorhs, dt_now)
 
     # ---------------------------------------------------------------- calculate_rhs!
@@ -563,22 +698,16 @@ class OracleSimulation:
         kspec = None
         if spec_t or stats_t:                                     # :130-134
             kspec = g.myfourier(0.5 * (ur[0] * ur[0] + ur[1] * ur[1] + ur[2] * ur[2]))
-        if p.density:
+        if p.fld:
             rhor = g.real(self.rho)
         if p.les:
             Sr = g.real(S)
-            # calc_les! Smagorinsky (les_real_calc.jl:77-79): nu_t = c^2 D^2 |S|, tau = 2 nu_t S
-            xx, xy, xz, yy, yz = Sr
-            zz = -xx - yy
-            nrm = np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
-            alpha_les = p.smag_c * p.smag_c * p.filter_width ** 2
-            nut = alpha_les * nrm
-            taur = 2.0 * nut[None] * Sr
+            taur = les_stress(p, Sr, wr)
         # realspacecalculation! (models.jl:236-280): rhs = u x w ; flux = -rho u
         nl = np.stack([ur[1] * wr[2] - ur[2] * wr[1], ur[2] * wr[0] - ur[0] * wr[2],
                        ur[0] * wr[1] - ur[1] * wr[0]])
-        if p.density:
-            flux = -rhor[None] * ur
+        if p.fld:
+            flux = -rhor[None] * ur                               # models.jl:265-275
         if p.variable_dt:                                         # find_max, utils.jl:247-258
             m = float(np.max(np.abs(ur)))
             self.slot_u = max(m, self.slot_u) if p.reference_cfl_slot else m
@@ -590,7 +719,7 @@ class OracleSimulation:
         nlh[:, 0, 0, 0] = 0.0                                     # models.jl:174
         # u round trip + projection (models.jl:192-193)
         self.u = u = g.project(g.myfourier(ur))
-        if p.density:
+        if p.fld:
             fluxh = g.myfourier(flux)
             self.rho = g.myfourier(rhor)
         tauh = g.myfourier(taur) if p.les else None
@@ -623,9 +752,9 @@ class OracleSimulation:
         self.rhs = rhs
         self.kspec = kspec
         self.tauh = tauh
-        if p.density:                                             # div!, vectorfunctions.jl:93-103
-            wdir = u[p.gravity_dir]
-            rr = 1j * (KX * fluxh[0] + (KY * fluxh[1] + KZ * fluxh[2])) + (-p.density_gradient) * wdir
+        if p.fld:                                                 # div!, vectorfunctions.jl:93-103
+            wdir = u[p.fld_dir]
+            rr = 1j * (KX * fluxh[0] + (KY * fluxh[1] + KZ * fluxh[2])) + (-p.fld_grad) * wdir
             if p.ab3:
                 rr = rr + (-self.alpha * g.K2) * self.rho
             rr[g.dealias] = 0.0
@@ -720,7 +849,7 @@ class OracleSimulation:
             u = u + self.force
         self.u = g.project(u)
         self.u[:, g.dealias] = 0.0
-        if p.density:
+        if p.fld:
             self.rho = self.rts.step(self.rho, self.rhorhs)
             self.rho[g.dealias] = 0.0
         self.iteration += 1
@@ -796,6 +925,13 @@ class OracleSimulation:
         # derivative variances used for the Taylor scales (stats.jl:79-94); the last one
         # (dx_squared_mean of u2) is what stays in reductionh[1]
         slot = self._wsum(g.KX ** 2 * a2[1])
+        if p.scalar:                                              # scalar_stats, stats.jl:221-233
+            phi = self.rho
+            r2 = np.abs(phi) ** 2
+            d1 = self._wsum(g.KX ** 2 * r2)
+            d2 = self._wsum(g.KY ** 2 * r2)
+            d3 = self._wsum(g.KZ ** 2 * r2)
+            extra += [phi[0, 0, 0].real, self._wsum(r2), d1, d2, d3, self.alpha * (d1 + d2 + d3)]
         if p.density:
             rho = self.rho
             r2 = np.abs(rho) ** 2

@@ -9,7 +9,7 @@ coefficient formulas amplify such a difference ~1e7 times.
 import numpy as np
 import pytest
 
-from oracle.ffs_oracle import Grid, OracleSimulation, Params
+from oracle.ffs_oracle import Grid, OracleSimulation, Params, stats_header
 
 pytestmark = pytest.mark.gpu
 
@@ -78,21 +78,38 @@ FIXED_CASES = {
                                  Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1"),
     "ab3-adaptive-density": gdict(32, adaptive=True, densityStratification="true", Pr="2", densityGradient="1",
                                   zAcceleration="1", referenceDensity="1"),
+    # the other pointwise LES models of les_types (les_types.jl:360-395)
+    "etd-vreman": gdict(32, "ETD3rdO", lesModel="Vreman", vremanConstant="0.07"),
+    "ab3-production-viscosity": gdict(32, lesModel="productionViscosity"),
+    "etd-silvis": gdict(32, "ETD3rdO", lesModel="Silvis"),
+    "ab3-stable-nonlinear": gdict(32, lesModel="stableNonLinear", nlConstant="0.05"),
+    "etd-sandp-smagorinsky": gdict(32, "ETD3rdO", lesModel="SandP", sLesModel="Smagorinsky"),
+    # passive scalar (simulationtypes.jl:198-213): the density's transport without buoyancy
+    "etd-scalar": gdict(32, "ETD3rdO", passiveScalar="true", scalarPr="0.7", scalarGradient="1"),
+    "ab3-adaptive-scalar-y": gdict(32, adaptive=True, passiveScalar="true", scalarPr="2", scalarGradient="0.5",
+                                   scalarDirection="y"),
+    # the scalar's ETD takes the velocity's hyperviscosity (simulationtypes.jl:336)
+    "etd-scalar-hv": gdict(32, "ETD3rdO", passiveScalar="true", scalarPr="1", scalarGradient="1",
+                           hyperViscosity="true", hyperViscosityCoefficient="1e-5"),
+    "ab3-sandp-vreman-density": gdict(48, lesModel="SandP", sLesModel="Vreman", densityStratification="true",
+                                      Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1"),
 }
 
 
 @pytest.mark.parametrize("name", sorted(FIXED_CASES))
 def test_fp64_step_parity(gpu_pkg, name):
     d = FIXED_CASES[name]
-    sim, ref = run_pair(gpu_pkg, d, density="densityStratification" in d)
+    fld = "densityStratification" in d or "passiveScalar" in d
+    sim, ref = run_pair(gpu_pkg, d, density=fld)
     for c in range(3):
         assert rel(sim.spectral(c), ref.u[c]) <= FP64_FIELD_TOL, (name, c)
-    if "densityStratification" in d:
+    if fld:
         assert rel(sim.spectral(3), ref.rho) <= FP64_FIELD_TOL
     rows = sim.stats_rows()
     rr = np.array(ref.stats_rows)
     assert rows.shape == rr.shape
     assert sim.header.count(",") + 1 == rows.shape[1]
+    assert sim.header == stats_header(Params.from_global(d))
     # relative error per entry, with an absolute floor of 1e-6 x the table's largest entry
     # for columns that are mathematically zero (mean velocity, net transfer: ~1e-20 noise)
     scale = np.maximum(np.abs(rr), 1e-6 * np.abs(rr).max())
@@ -114,7 +131,8 @@ def test_etd_adaptive_parity(gpu_pkg):
     assert sim.dt == pytest.approx(ref.get_dt(), rel=1e-13)
 
 
-@pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced"])
+@pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
+                                  "ab3-stable-nonlinear"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)
@@ -150,6 +168,7 @@ SPEC_CASES = {
     "ab3": gdict(32, dtSpec="2"),
     "etd-les-density": dict(FIXED_CASES["etd-les-density"], dtSpec="2"),
     "ab3-hv-forced": dict(FIXED_CASES["ab3-64-hv-forced"], dtSpec="2"),
+    "etd-scalar": dict(FIXED_CASES["etd-scalar"], dtSpec="2"),
 }
 
 
@@ -157,7 +176,7 @@ SPEC_CASES = {
 def test_spectrum_parity(gpu_pkg, name):
     """Every write_spec spectrum (spec.jl:1-146, 196-450) against the oracle, FP64."""
     d = SPEC_CASES[name]
-    density = "densityStratification" in d
+    density = "densityStratification" in d or "passiveScalar" in d
     sim, ref = run_pair(gpu_pkg, d, steps=5, density=density)
     got = sim.spectra()
     assert [r["iteration"] for r in got] == sorted(ref.spectra)

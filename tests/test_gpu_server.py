@@ -171,3 +171,117 @@ def test_engines_of_different_sizes_coexist(gpu_pkg):
     assert big.iteration == 2 and small.iteration == 2
     big.close()
     small.close()
+
+
+def _wait_until(pred, timeout=120.0):
+    import time
+    t0 = time.perf_counter()
+    while not pred():
+        assert time.perf_counter() - t0 < timeout, "condition not reached in time"
+        time.sleep(0.002)
+
+
+def _alone(pkg, case, u):
+    with pkg.Server(max_active=4) as srv:
+        rid = submit_case(srv, case, u)
+        r = srv.wait(rid, timeout=600)
+        return srv.fields(rid), srv.stats_rows(rid), r
+
+
+STAGGERED = [  # (n, les, integrator, adaptive, nt, seed): the first runs long, the others join it
+    (64, False, "Adams_Bashforth3rdO", True, 400, 21),
+    (32, True, "Adams_Bashforth3rdO", True, 120, 22),
+    (128, False, "Adams_Bashforth3rdO", True, 40, 23),
+    (48, True, "ETD3rdO", False, 60, 24),
+]
+
+
+def test_continuous_batching_requests_join_a_running_batch(gpu_pkg):
+    """Requests submitted while others are on the GPU (no pause: each is submitted only
+    after the batch has taken steps with the earlier ones) are admitted into the running
+    batch, overlap with it, and give bit-identical fields (stats rows to 1e-12) to the
+    same request run alone."""
+    pkg = gpu_pkg
+    us = [fields_of(pkg, c) for c in STAGGERED]
+    with pkg.Server(max_active=8) as srv:
+        ids = [submit_case(srv, STAGGERED[0], us[0])]
+        for case, u in zip(STAGGERED[1:], us[1:]):
+            prev = ids[-1]
+            _wait_until(lambda: srv.poll(prev)["state"] == "running")
+            steps = srv.info()["batch_steps"]
+            _wait_until(lambda: srv.info()["batch_steps"] >= steps + 10)
+            ids.append(submit_case(srv, case, u))
+        res = [srv.wait(rid, timeout=600) for rid in ids]
+        mixed = [(srv.fields(rid), srv.stats_rows(rid)) for rid in ids]
+        info = srv.info()
+    # each later request was admitted while the first one was still running
+    first = res[0]
+    for r in res[1:]:
+        assert first["admit_s"] < r["admit_s"] < first["done_s"]
+    assert info["peak_active"] >= 2
+    for case, u, (fm, sm), rm in zip(STAGGERED, us, mixed, res):
+        fa, sa, ra = _alone(pkg, case, u)
+        assert ra["iteration"] == rm["iteration"] == case[4]
+        for c in range(3):
+            assert np.array_equal(fa[c], fm[c]), (case, c)
+        assert sa.shape == sm.shape
+        assert np.allclose(sa, sm, rtol=1e-12, atol=1e-12 * np.abs(sm).max()), case
+
+
+def test_diverged_request_leaves_the_batch_early(gpu_pkg):
+    """A request whose initial field holds a NaN (injected on the host) is retired with
+    FFS_ENAN within a few health intervals, long before its nt, and frees its slot; the
+    requests beside it finish unchanged (bit-identical to alone)."""
+    pkg = gpu_pkg
+    good = [(64, False, "Adams_Bashforth3rdO", True, 150, 31), (48, True, "Adams_Bashforth3rdO", True, 100, 32)]
+    us = [fields_of(pkg, c) for c in good]
+    bad_case = (32, False, "Adams_Bashforth3rdO", True, 5000, 33)
+    ub = [x.copy() for x in fields_of(pkg, bad_case)]
+    ub[1][5, 6, 7] = np.nan
+    with pkg.Server(max_active=3) as srv:
+        srv.pause()
+        ids = [submit_case(srv, c, u) for c, u in zip(good, us)]
+        bad = submit_case(srv, bad_case, ub)
+        srv.pause(False)
+        with pytest.raises(pkg.FFSError) as e:
+            srv.wait(bad, timeout=600)
+        assert e.value.code == -4
+        rb = srv.poll(bad)
+        assert rb["status"] == -4
+        assert 0 < rb["iteration"] <= 64          # retired after a few health intervals
+        # its slot is free again: a further request is admitted and finishes
+        extra = submit_case(srv, good[1], us[1])
+        res = [srv.wait(rid, timeout=600) for rid in ids + [extra]]
+        mixed = [srv.fields(rid) for rid in ids + [extra]]
+    assert all(r["status"] == 0 for r in res)
+    for case, u, fm in zip(good + [good[1]], us + [us[1]], mixed):
+        fa, _, _ = _alone(pkg, case, u)
+        for c in range(3):
+            assert np.array_equal(fa[c], fm[c]), (case, c)
+
+
+def test_cancel_queued_and_running_requests(gpu_pkg):
+    pkg = gpu_pkg
+    long_case = (64, False, "Adams_Bashforth3rdO", True, 200000, 41)
+    short_case = (32, False, "Adams_Bashforth3rdO", True, 20, 42)
+    ul, us_ = fields_of(pkg, long_case), fields_of(pkg, short_case)
+    with pkg.Server(max_active=1) as srv:
+        a = submit_case(srv, long_case, ul)
+        _wait_until(lambda: srv.poll(a)["state"] == "running")
+        b = submit_case(srv, short_case, us_)          # waits: one slot, held by a
+        assert srv.poll(b)["state"] == "queued"
+        srv.cancel(b)
+        _wait_until(lambda: srv.poll(b)["status"] == -8, timeout=30)
+        steps = srv.info()["batch_steps"]
+        _wait_until(lambda: srv.info()["batch_steps"] >= steps + 5)
+        srv.cancel(a)
+        with pytest.raises(pkg.FFSError) as e:
+            srv.wait(a, timeout=600)
+        assert e.value.code == -8
+        ra = srv.poll(a)
+        assert 0 < ra["iteration"] < long_case[4]
+        assert srv.stats_rows(a).shape[0] >= 1        # the records of the steps it took
+        c = submit_case(srv, short_case, us_)          # the slot is free again
+        assert srv.wait(c, timeout=600)["status"] == 0
+        with pytest.raises(pkg.FFSError):
+            srv.cancel(c)                              # already finished

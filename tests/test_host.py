@@ -128,9 +128,42 @@ def test_parameters_requires_dtspec(pkg):
 
 def test_parameters_rejects_out_of_scope_models(pkg):
     d = {"nx": "8", "ny": "8", "nz": "8", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
-         "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1", "lesModel": "Vreman"}
+         "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1",
+         "lesModel": "dynamicSmagorinsky"}
     with pytest.raises(ValueError):
         pkg.parameters(d)
+    with pytest.raises(ValueError):
+        pkg.parameters(dict(d, lesModel="SandP", sLesModel="Silvis"))
+
+
+def test_parameters_les_models(pkg):
+    """lesModel keys and defaults of les_types (les_types.jl:360-395), the same in the
+    oracle's Params."""
+    import math
+    from oracle.ffs_oracle import Params
+    base = {"nx": "32", "ny": "32", "nz": "32", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+            "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1"}
+    dx = 2 * math.pi / 32 / (2 / 3)
+    cases = {  # lesModel keys -> (model id, constant, cp, cb, filter width passed to the engine)
+        ("Vreman",): (1, 0.032, None, 0.0, 0.0),
+        ("productionViscosity",): (2, 0.4, None, 0.0, 0.0),
+        ("Silvis",): (3, math.sqrt(0.17), 5.0, 0.0, 0.0),
+        ("stableNonLinear",): (4, 0.1, None, 0.0, 0.0),
+        ("SandP", "Smagorinsky"): (0, 0.17, None, 0.09, 2 * dx),
+        ("SandP", "productionViscosity"): (2, 0.1, None, 0.09, 0.0),
+    }
+    for keys, (mid, c, cp, cb, fw) in cases.items():
+        d = dict(base, lesModel=keys[0])
+        if len(keys) > 1:
+            d["sLesModel"] = keys[1]
+        p = pkg.parameters(d)
+        assert (p.les, p.les_model, p.sandp_cb) == (1, mid, cb), keys
+        assert p.smag_c == pytest.approx(c) and p.filter_width == pytest.approx(fw)
+        if cp is not None:
+            assert p.les_cp == cp
+        o = Params.from_global(d)
+        assert o.les and o.smag_c == pytest.approx(c) and o.sandp_cb == cb
+        assert o.filter_width == pytest.approx(fw if fw else dx)
 
 
 def test_parse_number(pkg):
