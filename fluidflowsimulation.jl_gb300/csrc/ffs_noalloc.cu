@@ -1,25 +1,31 @@
-// ffs_fourier_noalloc: the forward transform of one field (myfourier!: real 3D FFT,
-// 2/3 dealiasing, 1/(nx ny nz) scaling) for callers that cannot allocate device memory.
+// ffs_fourier_noalloc: the forward transform of one field (real 3D FFT, 2/3 dealiasing,
+// 1/(nx ny nz) scaling, FP64) for callers that cannot allocate device memory.
 //
-// Who needs it: code that runs inside a CUDA stream capture (cudaMalloc cannot be
-// captured), code whose device memory is owned by another allocator or memory pool, and
-// embedded hosts that forbid allocations once they are running. Such callers hand in
-// their own device buffers for the input and the output; everything in between (twiddle
-// tables and the two intermediate passes) lives in one fixed device array declared at
-// file scope below.
+// Who needs it: hosts whose device memory belongs to another allocator or memory pool
+// (a framework's caching allocator, an arena sized at start-up: a cudaMalloc of its own
+// would go around the pool's accounting and fragment what the pool manages), loops that
+// must not allocate once running (cudaMalloc and cudaFree can synchronise the device and
+// take an unbounded time), and plug-in hosts that grant a component only the buffers
+// they pass in. Such callers hand in their own device buffers for the input and the
+// output; everything in between (the twiddle tables and the two intermediate passes)
+// lives in one fixed device array declared at file scope below.
 //
 // Limits and rules (also stated in include/ffs.h):
 //   * the scratch array holds FFS_NOALLOC_SCRATCH_BYTES (24 MiB) on every GPU that loads
 //     the library, until the process exits; grids whose intermediates do not fit are
 //     rejected with FFS_EINVAL (128^3 with the 2/3 rule fits);
 //   * the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call before any
-//     stream capture;
-//   * every call shares the array: calls whose work overlaps on the GPU race;
+//     cudaGetSymbolAddress (with that device current) and caches it; make that first
+//     call before any stream capture;
+//   * each call enqueues four kernels and one memset of the caller's output: a kernel
+//     that writes the twiddle tables into the array, then the three transform passes.
+//     No host memory is read by the device work;
+//   * every call rewrites the twiddles and intermediates in the shared array, so calls
+//     whose work overlaps on the GPU (different streams, or different host threads)
+//     race on it; order them on one stream or synchronise between them;
 //   * no cudaMalloc, cudaFree or allocating library routine is called.
 #include <mutex>
 #include <string>
-#include <vector>
 
 #include "ffs_engine.cuh"
 
@@ -63,20 +69,25 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_z_full(Inst<double> I, cplx<do
   fft_lines<-1, TX, double>(I.pz, s0, s1, TX, I.twz, ld, st);
 }
 
-static void twiddles(int n, std::vector<cplx<double>>& h) {
-  h.resize(n);
-  for (int t = 0; t < n; ++t) {   // same table as the engine: exp(-2 pi i t / n)
-    const double ang = -2.0 * M_PI * (double)t / n;
-    double c = cos(ang), sn = sin(ang);
+// Twiddle tables exp(-2 pi i t / n) of the three axes, written into the scratch array
+// on the device: sincospi of the FP64 angle fraction -2t/n, exact at multiples of pi/4.
+__global__ void k_noalloc_twiddles(cplx<double>* twx, int nx, cplx<double>* twy, int ny, cplx<double>* twz, int nz) {
+  const int total = nx + ny + nz;
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+    cplx<double>* tw = twx;
+    int n = nx, t = g;
+    if (t >= nx) { t -= nx; tw = twy; n = ny; if (t >= ny) { t -= ny; tw = twz; n = nz; } }
+    double sn, c;
+    sincospi(-2.0 * (double)t / (double)n, &sn, &c);
     if ((8 * t) % n == 0) {
       const int o = (8 * t) / n;
-      const double r = sqrt(0.5);
-      const double cs8[8] = {1, r, 0, -r, -1, -r, 0, r};
+      const double r = 0.70710678118654752440;   // sqrt(1/2) rounded to FP64
+      const double cs8[8] = {1.0, r, 0.0, -r, -1.0, -r, 0.0, r};
       c = cs8[o];
       sn = -cs8[(o + 6) % 8];
     }
-    h[t].x = c;
-    h[t].y = sn;
+    tw[t].x = c;
+    tw[t].y = sn;
   }
 }
 
@@ -84,8 +95,10 @@ static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 }  // namespace ffsgpu
 
-extern "C" int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny, int32_t nz, double lx,
-                                   double ly, double lz, double cutoff, void* stream) {
+namespace {
+
+int fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny, int32_t nz, double lx, double ly,
+                    double lz, double cutoff, void* stream) {
   using namespace ffsgpu;
   using Eng = Engine<double>;
   auto fail = [](int code, const std::string& m) { set_global_error(m); return code; };
@@ -140,14 +153,11 @@ extern "C" int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx,
   I.wy = reinterpret_cast<cplx<double>*>(base + o_wy);
   I.wz = reinterpret_cast<cplx<double>*>(base + o_wz);
   I.phys = const_cast<double*>(phys);
-  std::vector<cplx<double>> tx, ty, tz;
-  twiddles(nx, tx);
-  twiddles(ny, ty);
-  twiddles(nz, tz);
-  // pageable sources: cudaMemcpyAsync stages them before returning
-  cudaError_t e = cudaMemcpyAsync((void*)I.twx, tx.data(), nx * cb, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync((void*)I.twy, ty.data(), ny * cb, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync((void*)I.twz, tz.data(), nz * cb, cudaMemcpyHostToDevice, s);
+  const int ntw = nx + ny + nz;
+  k_noalloc_twiddles<<<(ntw + 255) / 256, 256, 0, s>>>(reinterpret_cast<cplx<double>*>(base), nx,
+                                                      reinterpret_cast<cplx<double>*>(base + o_twy), ny,
+                                                      reinterpret_cast<cplx<double>*>(base + o_twz), nz);
+  cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemsetAsync(spec, 0, (size_t)nz * ny * I.nxh * cb, s);
   if (e != cudaSuccess) return fail(FFS_ECUDA, std::string("ffs_fourier_noalloc: ") + cudaGetErrorString(e));
   const size_t io = cb * (size_t)srows(nx) * 2 * (2 * LYZ_IO + 1);
@@ -165,4 +175,19 @@ extern "C" int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx,
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(FFS_ECUDA, std::string("ffs_fourier_noalloc launch: ") + cudaGetErrorString(e));
   return FFS_OK;
+}
+
+}  // namespace
+
+// No exception crosses the C ABI: std::string work above can throw (bad_alloc).
+extern "C" int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny, int32_t nz, double lx,
+                                   double ly, double lz, double cutoff, void* stream) {
+  try {
+    return fourier_noalloc(phys, spec, nx, ny, nz, lx, ly, lz, cutoff, stream);
+  } catch (const std::exception& ex) {
+    ffsgpu::set_global_error(std::string("ffs_fourier_noalloc: internal error: ") + ex.what());
+  } catch (...) {
+    ffsgpu::set_global_error("ffs_fourier_noalloc: internal error");
+  }
+  return FFS_EINVAL;
 }
