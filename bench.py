@@ -754,12 +754,15 @@ def fp32_error_run(pkg, name: str, nt: int, device: int) -> dict:
     cols = ["k", "diss", "tdiss"] + (["rhop2"] if "rhop2" in names else [])
     for c in cols:
         j = names.index(c)
-        rd = np.abs(ra[:, j] - rb[:, j]) / np.abs(rb[:, j])
+        ok = np.abs(rb[:, j]) > 1e-12 * np.abs(rb[:, j]).max()   # rows where the quantity is not ~0 (rho = 0 at t = 0)
+        rd = np.abs(ra[ok, j] - rb[ok, j]) / np.abs(rb[ok, j])
         out[f"{c}_max_rel_diff"] = float(rd.max())
         out[f"{c}_final_rel_diff"] = float(rd[-1])
-    kmax = len(Hb) * 2 // 3
-    sl = slice(1, kmax)
-    out["specH_final_max_rel_diff_k<=kmax"] = float((np.abs(Ha[sl] - Hb[sl]) / np.abs(Hb[sl])).max())
+    # the spectrum's bins that hold energy (above 1e-12 of its peak)
+    sl = np.abs(Hb) > 1e-12 * np.abs(Hb).max()
+    sl[0] = False
+    out["specH_final_max_rel_diff_energetic_bins"] = float((np.abs(Ha[sl] - Hb[sl]) / np.abs(Hb[sl])).max())
+    out["specH_final_energetic_bins"] = int(sl.sum())
     out["specH_final_rel_l2"] = float(np.linalg.norm(Ha - Hb) / np.linalg.norm(Hb))
     out["specV_final_rel_l2"] = float(np.linalg.norm(Va - Vb) / np.linalg.norm(Vb))
     out["wall_s"] = {"FP32": wa, "FP64": wb}

@@ -19,6 +19,7 @@ FFS_FP64, FFS_FP32 = 0, 1
 # Every symbol include/ffs.h declares (checked by the CPU test suite).
 EXPORTS = [
     "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_finalize",
+    "ffs_forcing_shells", "ffs_forcing_array",
     "ffs_get_fields",
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
     "ffs_stats_records", "ffs_stats", "ffs_spectrum", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
@@ -51,6 +52,8 @@ class FFSParams(ctypes.Structure):
         ("stats_capacity", c_int32), ("spec_capacity", c_int32), ("kernel_variant", c_int32), ("autotune", c_int32),
         ("les_model", c_int32), ("les_cp", c_double), ("sandp_cb", c_double),
         ("passive_scalar", c_int32), ("scalar_pr", c_double), ("scalar_gradient", c_double), ("scalar_dir", c_int32),
+        ("plane_forcing", c_int32), ("pf_tf", c_double), ("pf_alpha", c_double), ("pf_kf", c_double),
+        ("pf_zf_tanh", c_int32), ("pf_qp", c_double), ("pf_qc", c_double), ("pf_qkf", c_double),
     ]
 
 
@@ -103,6 +106,8 @@ def load() -> ctypes.CDLL:
         "ffs_initialize": (c_int32, [H]),
         "ffs_step": (c_int32, [H, c_int64]),
         "ffs_finalize": (c_int32, [H]),
+        "ffs_forcing_shells": (c_int32, [H]),
+        "ffs_forcing_array": (c_int32, [H, c_int32, D, c_int32, c_int32]),
         "ffs_get_fields": (c_int32, [H, D, D, D, D, c_int32]),
         "ffs_get_spectral": (c_int32, [H, c_int32, D]),
         "ffs_set_spectral": (c_int32, [H, c_int32, D]),

@@ -19,7 +19,10 @@ SOURCES = ["ffs_engine_f32.cu", "ffs_engine_f64.cu", "ffs_noalloc.cu", "ffs_serv
            "ffs_batch_c48.cu", "ffs_batch_c64.cu", "ffs_batch_c96.cu", "ffs_batch_c128.cu", "ffs_probe.cu",
            "ffs_api.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# host code without FMA contraction: host-side tables (twiddles, shells) round like the
+# oracle's separate multiplies and adds on every host architecture
+FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+         "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:

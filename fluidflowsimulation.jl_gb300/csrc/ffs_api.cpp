@@ -103,6 +103,12 @@ int ffs_step(ffs_handle* h, int64_t nsteps) {
   return guarded(h, [&] { return h->eng->step(nsteps, h->err); });
 }
 
+int ffs_forcing_shells(const ffs_handle* h) { return h ? h->eng->forcing_shells() : FFS_EINVAL; }
+
+int ffs_forcing_array(ffs_handle* h, int32_t which, double* v, int32_t n, int32_t set) {
+  return guarded(h, [&] { return h->eng->forcing_array(which, v, n, set, h->err); });
+}
+
 int ffs_finalize(ffs_handle* h) {
   return guarded(h, [&] { return h->eng->finish(h->err); });
 }

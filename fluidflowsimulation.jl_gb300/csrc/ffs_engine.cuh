@@ -178,6 +178,7 @@ class Engine : public EngineBase {
     I.alpha = p.density ? p.nu / p.density_pr : 0.0;
     I.dgrad = p.density_gradient; I.gval = p.gravity;
     I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
+    I.pforce = p.plane_forcing; I.pf_kf = p.pf_kf; I.pf_tf = p.pf_tf; I.pf_alpha = p.pf_alpha; I.pf_cfl = p.cfl;
     I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
     I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
     I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
@@ -221,6 +222,12 @@ class Engine : public EngineBase {
     if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_STABLE_NL)) {
       err = "unknown LES model";
       return FFS_EINVAL;
+    }
+    if (p.plane_forcing) {
+      if (p.plane_forcing < FFS_PF_RF || p.plane_forcing > FFS_PF_QF) { err = "unknown plane forcing"; return FFS_EINVAL; }
+      if (p.forcing) { err = "isotropicBand and kz = 0 plane forcing together are not supported"; return FFS_EINVAL; }
+      if (p.nz < 16) { err = "kz = 0 plane forcing needs nz >= 16 (it forces kz = +-1..+-5)"; return FFS_EUNSUPPORTED; }
+      if (p.plane_forcing != FFS_PF_QF && !(p.pf_tf > 0)) { err = "TF must be positive"; return FFS_EINVAL; }
     }
     if (p.les && p.sandp_cb != 0.0 && p.les_model > FFS_LES_PRODUCTION) {
       err = "SandP takes the Smagorinsky, Vreman or production-viscosity model";
@@ -390,7 +397,9 @@ class Engine : public EngineBase {
       n_sms = sms;
     }
     // record layout
-    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) + (I.forcing ? 3 : 0) + (I.hv ? 3 : 0);
+    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) + ((I.forcing || I.pforce) ? 3 : 0) +
+                  (I.hv ? 3 : 0);
+    if (I.pforce && (rc = plane_forcing_tables(p, err))) return rc;
     ncols_rec = ncols_stats + 13;
     I.ncols = ncols_rec;
     I.rec_cap = p.stats_capacity > 0 ? p.stats_capacity : 256;
@@ -432,7 +441,7 @@ class Engine : public EngineBase {
     if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
     else if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
     if (I.les) header += ",prh,prv,praniso,pr";
-    if (I.forcing) header += ",hp,vp,tp";
+    if (I.forcing || I.pforce) header += ",hp,vp,tp";
     if (I.hv) header += ",hdissh,hdissv,hdiss";
     FFS_CK(cudaStreamSynchronize(s));
     return 0;
@@ -730,6 +739,7 @@ class Engine : public EngineBase {
     cudaStreamWaitEvent(s2, ev_fork, 0);
     std::swap(s, s2);
     launch_scalar(mode);
+    launch_plane_forcing(mode);
     launch_table(mode);
     std::swap(s, s2);
     cudaEventRecord(ev_join, s2);
@@ -740,7 +750,115 @@ class Engine : public EngineBase {
     if (mode != 2) launch_update(mode);   // the run's tail evaluates the rhs and stats only
     launch_fin(mode);
   }
-  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0); }
+  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0); }
+  void launch_plane_forcing(int mode) {
+    if (I.pforce) k_plane_forcing<T><<<1, 256, 0, s>>>(I, mode);
+  }
+
+  // kz = 0 plane forcing: 2D shells (compute_shells2D, utils.jl:161-182), Zf (utils.jl
+  // :184-198), the Qf power spectrum (build_Qf_power_spectrum!, forcing_types.jl:303-330),
+  // and the retained kz = 0 modes listed by shell, on the host in FP64
+  int plane_forcing_tables(const ffs_params& p, std::string& err) {
+    const int nxh = p.nx / 2 + 1;
+    const int nsh = std::min(nxh, p.ny / 2);
+    if (nsh + 1 > FFS_PF_MAXSH) { err = "too many forcing shells"; return FFS_EUNSUPPORTED; }
+    auto kxv = [&](int i) { return (double)i / p.lx; };
+    auto kyv = [&](int y) { return (double)(y < p.ny / 2 ? y : y - p.ny) / p.ly; };   // fftfreq, Nyquist negative
+    const double maxdk = std::max(kxv(1), kyv(1));
+    std::vector<double> kh(nsh, 0.0), zf(nsh, 0.0), qr(nsh, 0.0);
+    std::vector<long long> cnt(nsh, 0);
+    for (int j = 0; j < p.ny; ++j)
+      for (int i = 0; i < nxh; ++i) {
+        const double kx = kxv(i), ky = kyv(j);
+        const double K = sqrt(kx * kx + ky * ky);
+        const long long ii = llrint(K / maxdk);
+        if (ii >= nsh) break;
+        kh[ii] += K;
+        cnt[ii] += 1;
+      }
+    for (int i = 0; i < nsh; ++i) kh[i] /= (double)cnt[i];
+    const double kf = p.pf_kf;
+    for (int i = 0; i < nsh; ++i)
+      zf[i] = p.pf_zf_tanh ? tanh((kf - kh[i]) / (0.25 * kf)) * (((kf - kh[i]) <= 0.0) ? 0.0 : 1.0)
+                           : (kh[i] <= kf ? 1.0 : 0.0);
+    if (p.plane_forcing == FFS_PF_QF) {
+      double integral = 0.0;
+      for (int i = 1; i < nsh; ++i)
+        if (kh[i] <= kf) {
+          const double q = (kh[i] - p.pf_qkf) / p.pf_qc;
+          const double term = exp(-(q * q));
+          qr[i] = p.pf_qp * term;
+          integral += term;
+        }
+      for (int i = 0; i < nsh; ++i) qr[i] /= integral;
+      if (p.les) {   // lfilter: the LES filter width's Gaussian, squared
+        const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
+        const double d2 = fw * fw;
+        for (int i = 1; i < nsh; ++i)
+          if (kh[i] <= kf) {
+            const double G = exp((-d2 / 24) * (kh[i] * kh[i]));
+            qr[i] *= G * G;
+          }
+      }
+    }
+    // retained kz = 0 modes: spectrum shell (CSR) and forcing shell
+    const int plane = I.NYR * I.KXP;
+    std::vector<std::vector<int>> byshell(nsh);
+    std::vector<int> nmode(plane, -1);
+    for (int jc = 0; jc < I.NYR; ++jc) {
+      const int y = jc < I.ypos ? jc : p.ny - I.NYR + jc;
+      for (int ix = 0; ix < I.Mx; ++ix) {
+        const double kx = kxv(ix), ky = kyv(y);
+        const int m = jc * I.KXP + ix;
+        const long long ns = llrint(sqrt(kx * kx + ky * ky) / maxdk);
+        if (ns < nsh) byshell[ns].push_back(m);
+        const long long nf = llrint(sqrt(std::fma(kx, kx, ky * ky)) / maxdk);
+        if (nf >= 1 && nf < nsh && kh[nf] <= kf) nmode[m] = (int)nf;
+      }
+    }
+    std::vector<int> start(nsh + 1, 0), modes;
+    for (int n = 0; n < nsh; ++n) {
+      start[n] = (int)modes.size();
+      modes.insert(modes.end(), byshell[n].begin(), byshell[n].end());
+    }
+    start[nsh] = (int)modes.size();
+    std::vector<double> d(6 * (size_t)nsh, 0.0);
+    for (int i = 0; i < nsh; ++i) { d[3 * nsh + i] = kh[i]; d[4 * nsh + i] = zf[i]; d[5 * nsh + i] = qr[i]; }
+    int rc;
+    double* dd_ = nullptr;
+    int *ds = nullptr, *dm = nullptr, *dn = nullptr;
+    cplx<T>* df = nullptr;
+    if ((rc = alloc(&dd_, d.size(), err)) || (rc = alloc(&ds, start.size(), err)) ||
+        (rc = alloc(&dm, std::max<size_t>(modes.size(), 1), err)) || (rc = alloc(&dn, nmode.size(), err)) ||
+        (rc = alloc(&df, 2 * (size_t)plane + 20, err)))
+      return rc;
+    FFS_CK(cudaMemcpyAsync(dd_, d.data(), sizeof(double) * d.size(), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaMemcpyAsync(ds, start.data(), sizeof(int) * start.size(), cudaMemcpyHostToDevice, s));
+    if (!modes.empty()) FFS_CK(cudaMemcpyAsync(dm, modes.data(), sizeof(int) * modes.size(), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaMemcpyAsync(dn, nmode.data(), sizeof(int) * nmode.size(), cudaMemcpyHostToDevice, s));
+    FFS_CK(cudaMemsetAsync(df, 0, sizeof(cplx<T>) * (2 * (size_t)plane + 20), s));
+    FFS_CK(cudaStreamSynchronize(s));
+    I.pf_nsh = nsh; I.pf_maxdk = maxdk;
+    I.pf_d = dd_; I.pf_start = ds; I.pf_modes = dm; I.pf_nmode = dn; I.pf_force = df;
+    pf_avgk = kh;
+    return 0;
+  }
+  std::vector<double> pf_avgk;
+
+  int forcing_shells() const override { return I.pforce ? I.pf_nsh : 0; }
+  int forcing_array(int which, double* v, int n, int set, std::string& err) override {
+    if (!I.pforce) { err = "no kz = 0 plane forcing in this simulation"; return FFS_ESTATE; }
+    if (!v || n != I.pf_nsh || which < 0 || which > 2 || (which == 2 && set)) {
+      err = "forcing array: which must be 0 (R), 1 (Em) or 2 (avgK, read only), n the shell count";
+      return FFS_EINVAL;
+    }
+    if (which == 2) { std::copy(pf_avgk.begin(), pf_avgk.end(), v); return 0; }
+    double* dst = I.pf_d + (size_t)which * I.pf_nsh;
+    if (set) FFS_CK(cudaMemcpyAsync(dst, v, sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    else FFS_CK(cudaMemcpyAsync(v, dst, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    return 0;
+  }
 
   // ---------------------------------------------------------------- fields
   void repack_in(const double* src, double* dst, int layout) const {
@@ -1034,7 +1152,8 @@ class Engine : public EngineBase {
       launch_inv_y(inv_list); FFS_CK(cudaEventRecord(ev[2], s));
       launch_x(); FFS_CK(cudaEventRecord(ev[3], s));
       launch_fwd_y(fwd_list); FFS_CK(cudaEventRecord(ev[4], s));
-      launch_scalar(0); FFS_CK(cudaEventRecord(ev[5], s));
+      launch_scalar(0);
+      launch_plane_forcing(0); FFS_CK(cudaEventRecord(ev[5], s));
       launch_table(0); FFS_CK(cudaEventRecord(ev[6], s));
       launch_zu(0); FFS_CK(cudaEventRecord(ev[7], s));
       launch_stats(0); FFS_CK(cudaEventRecord(ev[8], s));

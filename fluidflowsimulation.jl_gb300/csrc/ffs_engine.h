@@ -39,6 +39,9 @@ class EngineBase {
   virtual int step(int64_t n, std::string& err) = 0;
   // run_simulation's tail: rhs, forcing and a stats record at the current iteration
   virtual int finish(std::string& err) = 0;
+  // kz = 0 plane forcing state per 2D shell (0: R, 1: Em, 2: avgK)
+  virtual int forcing_shells() const = 0;
+  virtual int forcing_array(int which, double* v, int n, int set, std::string& err) = 0;
   virtual int get_fields(double* u1, double* u2, double* u3, double* rho, int layout, std::string& err) = 0;
   virtual int get_spectral(int comp, double* out, std::string& err) = 0;
   // u spectrum of the current state: H (lenH) horizontal bins, V (lenV) vertical bins

@@ -35,6 +35,7 @@ enum StatQ : int {
   Q_COUNT = Q_IL0 + 9
 };
 constexpr int QPAD = 40;
+constexpr int FFS_PF_MAXSH = 520;   // 2D shells of the kz = 0 plane forcing: min(nx/2+1, ny/2) <= 513
 
 // Device-resident scalar state (one per simulation).
 struct DevState {
@@ -51,6 +52,7 @@ struct DevState {
   unsigned long long rhomax_bits;  // running max |rho|
   double force_coef;       // isotropic band forcing: eps / (2 E_f)
   double Ef;
+  double pf_hp, pf_vp;     // kz = 0 plane forcing: horizontal and vertical power of the last call
   double nl_h, nl_v, press_h, press_v;  // last non-linear / pressure stats
   long long nrec;          // stats records written
   long long nspec;         // spectrum records written
@@ -125,6 +127,14 @@ template <typename T> struct Inst {
   double alpha, dgrad, gval;
   int forcing;
   double f_eps, f_kf;
+  // kz = 0 plane forcing (FFS_PF_*): per-shell state and tables, plane-mode lists, force
+  int pforce, pf_nsh;
+  double pf_maxdk, pf_kf, pf_tf, pf_alpha, pf_cfl;
+  double* pf_d;            // [6][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum
+  const int* pf_start;     // [nsh + 1]: retained kz = 0 modes of each spectrum shell (CSR)
+  const int* pf_modes;     //   their plane index jc * KXP + ix
+  const int* pf_nmode;     // [NYR * KXP]: forcing shell of each plane mode (-1: not forced)
+  cplx<T>* pf_force;       // [2][NYR * KXP] force on the kz = 0 plane, then [2][10] (0, 0, kz) modes
   int dt_stat, dt_spec;
   // the same constants in the arithmetic type (no per-element conversions)
   T Lx_t, Ly_t, Lz_t, iLx_t, iLy_t, iLz_t;

@@ -645,6 +645,149 @@ __global__ void k_scalar(Inst<T> I, int mode) {
   b_scalar<T>(I, mode, Blk::here());
 }
 
+// ====================================================================================
+// kz = 0 plane forcing (rfForcing forcing.jl:6-114, cRfForcing cforcing.jl:1-97,
+// QfForcing qfforcing.jl:1-81), from the current u after set_dt! (models.jl:6-9). One CTA,
+// FP64. mode 1 (initialize!): the target spectrum Em of the initial field
+// (forcing_types.jl:66-73); mode 0 / 2: the force of this step into pf_force and the
+// powers hp, vp. Shell sums run one thread per shell over the shell's modes in a fixed
+// order, the power sums through a fixed-order block reduction: every call is
+// deterministic.
+// ====================================================================================
+template <typename T>
+__global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
+  DevState* S = I.st;
+  const int nsh = I.pf_nsh;
+  double* R = I.pf_d;
+  double* Em = R + nsh;
+  double* fac = Em + nsh;
+  const double* kh = fac + nsh;
+  const double* Zf = kh + nsh;
+  const double* QR = Zf + nsh;
+  const bool qf = I.pforce == FFS_PF_QF;
+  const long long cs = I.cstride;
+  const int plane = I.NYR * I.KXP;
+  __shared__ double Ef[FFS_PF_MAXSH];
+  __shared__ double red[2][256];
+  // calculate_u1u2_spectrum! / calculate_u1u2_mag_spectrum! (spectrum.jl:1-65)
+  for (int n = threadIdx.x; n < nsh; n += blockDim.x) {
+    double e = 0.0;
+    for (int q = I.pf_start[n]; q < I.pf_start[n + 1]; ++q) {
+      const int m = I.pf_modes[q];
+      const cplx<T> a = I.uh[m], b = I.uh[cs + m];
+      const double cf = (m % I.KXP) > 0 ? 2.0 : 1.0;
+      const double a2 = (double)a.x * a.x + (double)a.y * a.y + ((double)b.x * b.x + (double)b.y * b.y);
+      e += qf ? cf * sqrt(a2) : 0.5 * cf * a2;
+    }
+    Ef[n] = e;
+  }
+  __syncthreads();
+  if (mode == 1) {
+    if (!qf) for (int n = threadIdx.x; n < nsh; n += blockDim.x) Em[n] = Ef[n];
+    return;
+  }
+  const double dt = S->dt;
+  const long long it = S->iteration;
+  const double kf = I.pf_kf;
+  if (!qf) {   // the shells' ODE (forcing.jl:47-53)
+    double omega;
+    if (I.pforce == FFS_PF_RF) {
+      double ts = dt / I.pf_cfl;
+      if (I.adaptive) {
+        if (it == 0) ts /= 0.1;
+        else if (it == 1) ts /= 0.2;
+        else if (it == 2) ts /= 0.4;
+        else if (it == 3) ts /= 0.8;
+      }
+      omega = (2 * M_PI) / (I.pf_tf * ts);
+    } else {
+      omega = (2 * M_PI) / I.pf_tf;
+    }
+    const double alpha = I.pf_alpha, eps = 2.220446049250313e-16;
+    for (int n = 1 + threadIdx.x; n < nsh; n += blockDim.x) {
+      if (kh[n] <= kf) {
+        double r = R[n] + dt * (-2 * alpha * omega * R[n] - omega * omega * (Ef[n] - Em[n]));
+        r = fmax(0.0, r);
+        R[n] = r;
+        fac[n] = sqrt(r / fmax(Ef[n], eps)) * Zf[n] * dt;
+      }
+    }
+  }
+  __syncthreads();
+  // horizontal forcing of the kz = 0 plane (forcing.jl:57-77, qfforcing.jl:22-45)
+  double ff = 0.0, fv = 0.0;
+  for (int m = threadIdx.x; m < plane; m += blockDim.x) {
+    const int n = I.pf_nmode[m];
+    cplx<T> f1 = mk(T(0), T(0)), f2 = f1;
+    if (n >= 0) {
+      const cplx<T> a = I.uh[m], b = I.uh[cs + m];
+      const double ax = a.x, ay = a.y, bx = b.x, by = b.y;
+      const double cf = (m % I.KXP) > 0 ? 2.0 : 1.0;
+      double s1x, s1y, s2x, s2y;
+      if (qf) {
+        const double umag = sqrt(ax * ax + ay * ay + (bx * bx + by * by));
+        const double fkn = dt * QR[n] * 0.99 / Ef[n];
+        s1x = (ax / umag) * fkn; s1y = (ay / umag) * fkn; s2x = (bx / umag) * fkn; s2y = (by / umag) * fkn;
+        fv += (fma(ax, s1x / dt, ay * (s1y / dt)) + fma(bx, s2x / dt, by * (s2y / dt))) * cf;
+      } else {
+        const double g = fac[n];
+        s1x = ax * g; s1y = ay * g; s2x = bx * g; s2y = by * g;
+        ff += (s1x * s1x + s1y * s1y + (s2x * s2x + s2y * s2y)) * cf;
+        fv += (fma(ax, s1x, ay * s1y) + fma(bx, s2x, by * s2y)) * cf;
+      }
+      f1 = mk(T(s1x), T(s1y));
+      f2 = mk(T(s2x), T(s2y));
+    }
+    I.pf_force[m] = f1;
+    I.pf_force[plane + m] = f2;
+  }
+  red[0][threadIdx.x] = ff;
+  red[1][threadIdx.x] = fv;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) { red[0][threadIdx.x] += red[0][threadIdx.x + o]; red[1][threadIdx.x] += red[1][threadIdx.x + o]; }
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  const double hp = qf ? red[1][0] : red[0][0] * 0.5 / dt + red[1][0] / dt;
+  // vertical forcing of the (0, 0, kz) modes, kz = +-1..+-5 (Rf) or +-3..+-5 (Qf)
+  cplx<T>* fvert = I.pf_force + 2 * plane;
+  auto at = [&](int kz) -> long long {   // compact index of (0, 0, kz)
+    const int kc = kz >= 0 ? kz : I.NZR + kz;
+    return (long long)kc * I.NYR * I.KXP;
+  };
+  double usum = 0.0;
+  for (int k = 1; k <= 5; ++k)
+    for (int sg = 1; sg >= -1; sg -= 2) {
+      if (qf && k < 3) continue;
+      const long long g = at(sg * k);
+      const double a2 = (double)I.uh[g].x * I.uh[g].x + (double)I.uh[g].y * I.uh[g].y;
+      const double b2 = (double)I.uh[cs + g].x * I.uh[cs + g].x + (double)I.uh[cs + g].y * I.uh[cs + g].y;
+      usum += qf ? a2 + b2 : sqrt(a2 + b2);
+    }
+  const double f = qf ? dt * hp * (1 - 0.99) / (usum * 0.99) : dt * sqrt(2.0 * hp * (1.0 - 0.99)) / usum;
+  double ffv = 0.0, fvv = 0.0;
+  for (int k = 1; k <= 5; ++k)
+    for (int sg = 1; sg >= -1; sg -= 2) {
+      const int slot = (k - 1) + (sg > 0 ? 0 : 5);
+      const bool on = !(qf && k < 3);
+      const long long g = at(sg * k);
+      const double ax = I.uh[g].x, ay = I.uh[g].y, bx = I.uh[cs + g].x, by = I.uh[cs + g].y;
+      const double s1x = on ? ax * f : 0.0, s1y = on ? ay * f : 0.0, s2x = on ? bx * f : 0.0, s2y = on ? by * f : 0.0;
+      fvert[slot] = mk(T(s1x), T(s1y));
+      fvert[10 + slot] = mk(T(s2x), T(s2y));
+      if (!on) continue;
+      if (qf) {
+        fvv += fma(ax, s1x / dt, ay * (s1y / dt)) + fma(bx, s2x / dt, by * (s2y / dt));
+      } else {
+        ffv += s1x * s1x + s1y * s1y + (s2x * s2x + s2y * s2y);
+        fvv += fma(ax, s1x, ay * s1y) + fma(bx, s2x, by * s2y);
+      }
+    }
+  S->pf_hp = hp;
+  S->pf_vp = qf ? fvv : ffv * 0.5 / dt + fvv / dt;
+}
+
 // ETD coefficient tables for the current stage and dt history: by q = i^2 + j^2 + l^2
 // when k^2 = q / L^2 is exact (uniform domain with L a power of two), else one entry per
 // retained mode (compact index). Multi-CTA; runs after k_scalar.
@@ -904,6 +1047,17 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
       // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
       un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
       if (band) un[c] = un[c] + scl(u[c], fdt);   // forcing increment (add_forcing!)
+    }
+    if (I.pforce) {   // add_Rf_forcing! (forcing_types.jl:54-64): the kz = 0 plane, then (0, 0, kz)
+      const int plane = I.NYR * I.KXP;
+      if (kz_i == 0) {
+        un[0] = un[0] + I.pf_force[g];
+        un[1] = un[1] + I.pf_force[plane + g];
+      } else if (ix == 0 && ky_i == 0 && kz_i >= -5 && kz_i <= 5) {
+        const int slot = kz_i > 0 ? kz_i - 1 : 4 - kz_i;
+        un[0] = un[0] + I.pf_force[2 * plane + slot];
+        un[1] = un[1] + I.pf_force[2 * plane + 10 + slot];
+      }
     }
     {  // projection after the update (time_step_functions.jl:78)
       const cplx<T> kd = mk(kx * un[0].x + ky * un[1].x + kz * un[2].x, kx * un[0].y + ky * un[1].y + kz * un[2].y);
@@ -1292,6 +1446,8 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       if (I.forcing) {
         const double dt = S->dt;
         row[c++] = tot[Q_HP] / dt; row[c++] = tot[Q_VP] / dt; row[c++] = (tot[Q_HP] + tot[Q_VP]) / dt;
+      } else if (I.pforce) {   // stats(a::RfForcing) (forcing_types.jl:33): F.hp, F.vp of the last call
+        row[c++] = S->pf_hp; row[c++] = S->pf_vp; row[c++] = S->pf_hp + S->pf_vp;
       }
       if (I.hv) {
         row[c++] = I.hv_nu * tot[Q_HVH]; row[c++] = I.hv_nu * tot[Q_HVV]; row[c++] = I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);

@@ -368,6 +368,7 @@ class Server {
   int submit(const ffs_request& r, uint64_t* id) {
     const ffs_params& p = r.params;
     if (p.precision != FFS_FP32) return fail_api(FFS_EUNSUPPORTED, "the server runs FP32 simulations only");
+    if (p.plane_forcing) return fail_api(FFS_EUNSUPPORTED, "the server does not batch kz = 0 plane forcing");
     if (p.density || p.passive_scalar)
       return fail_api(FFS_EUNSUPPORTED, "the server does not batch density-stratified or passive-scalar runs");
     if (p.les && (p.les_model != FFS_LES_SMAGORINSKY || p.sandp_cb != 0.0))

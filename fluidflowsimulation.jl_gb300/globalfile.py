@@ -77,6 +77,9 @@ def _set_les(p: FFSParams, d: dict[str, str]) -> None:
         p.filter_width = 0.0                                 # the engine's default (lx 2 pi / nx) / cutoff
 
 
+PLANE_FORCING = {"rfForcing": 1, "cRfForcing": 2, "QfForcing": 3}
+
+
 def parameters(d: dict[str, str], precision: str | None = None, device: int = 0) -> FFSParams:
     """Build ``ffs_params`` from a `global` dict (src/simulationtypes.jl:242-365)."""
     p = FFSParams()
@@ -131,11 +134,21 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
     if d.get("equation", "") == "NS":
         raise ValueError("equation NS (conservation form) is not supported")
     if "forcing" in d:
-        if d["forcing"] != "isotropicBand":
-            raise ValueError(f"forcing {d['forcing']!r} is not supported (isotropicBand)")
-        p.forcing = 1
-        p.forcing_power = parse_number(d.get("forcingPower", "0.1"))
-        p.forcing_kf = parse_number(d.get("forcingKf", "2.5"))
+        f = d["forcing"]
+        if f == "isotropicBand":
+            p.forcing = 1
+            p.forcing_power = parse_number(d.get("forcingPower", "0.1"))
+            p.forcing_kf = parse_number(d.get("forcingKf", "2.5"))
+        elif f in PLANE_FORCING:   # forcing_model (forcing_types.jl:335-450)
+            p.plane_forcing = PLANE_FORCING[f]
+            p.pf_kf = float(d["kf"])
+            if f == "QfForcing":
+                p.pf_qp, p.pf_qc, p.pf_qkf = (float(d[k]) for k in ("alveliusP", "alveliusC", "alveliusKf"))
+            else:
+                p.pf_tf, p.pf_alpha = float(d["TF"]), float(d["alphac"])
+                p.pf_zf_tanh = 0 if d.get("Zf", "cutoff") == "cutoff" else 1
+        else:
+            raise ValueError(f"forcing {f!r} is not supported (isotropicBand, rfForcing, cRfForcing, QfForcing)")
     if "referenceCflSlot" in d:
         p.reference_cfl_slot = 1 if _bool(d["referenceCflSlot"]) else 0
     if "autotune" in d:   # engine key: time the candidate launch shapes at create

@@ -10,6 +10,8 @@
 #   using FFSEngine; run_simulation()
 module FFSEngine
 
+using DelimitedFiles
+
 export run_simulation, FFSParams, Engine, initialize!, advance_in_time!, finalize!, getfields
 
 const LIB = get(ENV, "FFS_LIB", joinpath(@__DIR__, "..", "libffs.so"))
@@ -33,6 +35,8 @@ mutable struct FFSParams
     autotune::Int32
     les_model::Int32; les_cp::Float64; sandp_cb::Float64
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
+    plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
+    pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
     FFSParams() = new()
 end
 
@@ -111,6 +115,16 @@ function parameters(d)
         p.forcing = 1
         p.forcing_power = haskey(d, :forcingPower) ? num(d[:forcingPower]) : 0.1
         p.forcing_kf = haskey(d, :forcingKf) ? num(d[:forcingKf]) : 2.5
+    elseif get(d, :forcing, "") in ("rfForcing", "cRfForcing", "QfForcing")   # forcing_types.jl:335-450
+        p.plane_forcing = Dict("rfForcing" => 1, "cRfForcing" => 2, "QfForcing" => 3)[d[:forcing]]
+        p.pf_kf = parse(Float64, d[:kf])
+        if d[:forcing] == "QfForcing"
+            p.pf_qp = parse(Float64, d[:alveliusP]); p.pf_qc = parse(Float64, d[:alveliusC])
+            p.pf_qkf = parse(Float64, d[:alveliusKf])
+        else
+            p.pf_tf = parse(Float64, d[:TF]); p.pf_alpha = parse(Float64, d[:alphac])
+            p.pf_zf_tanh = get(d, :Zf, "cutoff") == "cutoff" ? 0 : 1
+        end
     end
     p.precision = get(d, :precision, "FP64") == "FP32" ? 1 : 0
     return p
@@ -129,6 +143,14 @@ advance_in_time!(e::Engine, n::Integer = 1) = check(e, ccall((:ffs_step, LIB), C
 # the tail of run_simulation (FluidFlowSimulation.jl:46-49): calculate_rhs!, forcing, writestats
 finalize!(e::Engine) = check(e, ccall((:ffs_finalize, LIB), Cint, (Ptr{Cvoid},), e.h))
 iteration(e::Engine) = ccall((:ffs_iteration, LIB), Int64, (Ptr{Cvoid},), e.h)
+forcingshells(e::Engine) = Int(ccall((:ffs_forcing_shells, LIB), Cint, (Ptr{Cvoid},), e.h))
+function forcingarray(e::Engine, which::Integer)
+    v = zeros(forcingshells(e))
+    check(e, ccall((:ffs_forcing_array, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint), e.h, which, v, length(v), 0))
+    return v
+end
+forcingarray!(e::Engine, which::Integer, v::Vector{Float64}) =
+    check(e, ccall((:ffs_forcing_array, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint), e.h, which, v, length(v), 1))
 simtime(e::Engine) = ccall((:ffs_time, LIB), Float64, (Ptr{Cvoid},), e.h)
 
 function getfields(e::Engine)
@@ -280,6 +302,18 @@ function run_simulation()
     names = split(statsheader(e), ",")
     ns = statsncols(e)
     initialize!(e)
+    if forcingshells(e) > 0   # initialize!(f::RfForcing): targSpectrum.dat, R.$start (forcing_types.jl:66-83)
+        if p.plane_forcing != 3 && isfile("targSpectrum.dat")
+            data = readdlm("targSpectrum.dat", skipstart = 1)
+            kh = forcingarray(e, 2)
+            Em = [begin
+                      i = searchsortedlast(data[:, 1], k); i = clamp(i, 1, size(data, 1) - 1)
+                      t = (k - data[i, 1]) / (data[i + 1, 1] - data[i, 1]); (1 - t) * data[i, 2] + t * data[i + 1, 2]
+                  end for k in kh]
+            forcingarray!(e, 1, Em)
+        end
+        isfile("R.$s") && forcingarray!(e, 0, vec(readdlm("R.$s", Float64)))
+    end
     total = haskey(d, :nt) ? parse(Int, d[:nt]) : typemax(Int) - s
     lengthtime = haskey(d, :timeDuration) ? parse(Float64, d[:timeDuration]) : Inf   # FluidFlowSimulation.jl:26
     final = s + total
@@ -313,6 +347,9 @@ function run_simulation()
     finalize!(e)
     flush()
     writeoutput(e)
+    if p.plane_forcing == 1   # writedlm("R.$(iteration)", R) (FluidFlowSimulation.jl:60-62)
+        open(f -> foreach(v -> println(f, v), forcingarray(e, 0)), "R.$(iteration(e))", "w")
+    end
     return e
 end
 

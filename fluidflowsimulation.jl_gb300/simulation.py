@@ -114,6 +114,20 @@ class Simulation:
         Stats record whatever the iteration; fields, iteration and time unchanged)."""
         self._check(self._L.ffs_finalize(self._h))
 
+    @property
+    def forcing_shells(self) -> int:
+        """2D shells of the kz = 0 plane forcing (0 without it)."""
+        return int(self._L.ffs_forcing_shells(self._h))
+
+    def forcing_array(self, which: str, values=None) -> np.ndarray:
+        """Per-shell state of the kz = 0 plane forcing: "R" (the ODE state of the R.N files),
+        "Em" (target spectrum) or "avgK" (mean wavenumber, read only). With values, set it."""
+        w = {"R": 0, "Em": 1, "avgK": 2}[which]
+        n = self.forcing_shells
+        a = np.zeros(n) if values is None else np.ascontiguousarray(values, dtype=np.float64)
+        self._check(self._L.ffs_forcing_array(self._h, w, a.ctypes.data_as(_D), n, 0 if values is None else 1))
+        return a
+
     def fields(self, layout: int = 0):
         shape = (self.nz, self.ny, self.nx if layout == 0 else 2 * (self.nx // 2 + 1))
         out = [np.empty(shape) for _ in range(4 if self.has_density else 3)]
@@ -292,6 +306,17 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         (folder / "Scales.txt").write_text(_scales.scales_header(bool(p.density)) + "\n")
         (folder / "Numbers.txt").write_text(_scales.numbers_header(bool(p.density)) + "\n")
     sim.initialize()
+    if sim.forcing_shells:
+        # initialize!(f::RfForcing) (forcing_types.jl:66-73): the target spectrum from
+        # targSpectrum.dat when present (calculate_Em!, linear interpolation at avgK), else
+        # the initial field's; R from R.$start when present
+        tf = folder / "targSpectrum.dat"
+        if p.plane_forcing != 3 and tf.exists():
+            data = np.loadtxt(tf, skiprows=1)
+            sim.forcing_array("Em", np.interp(sim.forcing_array("avgK"), data[:, 0], data[:, 1]))
+        rf = folder / f"R.{start}"
+        if rf.exists():
+            sim.forcing_array("R", np.loadtxt(rf).reshape(-1))
     final_step = start + total
     final_time = p.start_time + lengthtime
     kx1, ky1 = 1.0 / p.lx, 1.0 / p.ly
@@ -331,6 +356,10 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     sim.finalize()
     flush()
     _write_output(folder, sim)
+    if p.plane_forcing == 1:   # writedlm("R.$(iteration)", R) for rfForcing (FluidFlowSimulation.jl:60-62)
+        with open(folder / f"R.{sim.iteration}", "w") as f:
+            for v in sim.forcing_array("R"):
+                f.write(julia_float(float(v)) + "\n")
     return sim
 
 

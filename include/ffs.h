@@ -95,7 +95,19 @@ typedef struct ffs_params {
   double scalar_pr;            /* scalarPr: diffusivity nu / scalarPr */
   double scalar_gradient;      /* scalarGradient: mean gradient d phi / d(direction) */
   int32_t scalar_dir;          /* scalarDirection: 0 x, 1 y, 2 z */
+  int32_t plane_forcing;       /* the reference's kz = 0 plane forcing (forcing_types.jl:335-450):
+                                  FFS_PF_RF (rfForcing), FFS_PF_CRF (cRfForcing), FFS_PF_QF (QfForcing) */
+  double pf_tf;                /* TF */
+  double pf_alpha;             /* alphac */
+  double pf_kf;                /* kf */
+  int32_t pf_zf_tanh;          /* Zf tanh (default: cutoff) */
+  double pf_qp, pf_qc, pf_qkf; /* alveliusP, alveliusC, alveliusKf (QfForcing) */
 } ffs_params;
+
+#define FFS_PF_NONE 0
+#define FFS_PF_RF 1  /* RfForcing functor, src/Forcing_methods/forcing.jl:6-114 */
+#define FFS_PF_CRF 2 /* CRfForcing, src/Forcing_methods/cforcing.jl:1-97 */
+#define FFS_PF_QF 3  /* QfForcing, src/Forcing_methods/qfforcing.jl:1-81 */
 
 #define FFS_LES_SMAGORINSKY 0 /* nu_t = c^2 D^2 |S| (les_real_calc.jl:77-79) */
 #define FFS_LES_VREMAN 1      /* VremanLESModel.jl, les_real_calc.jl:132-139 */
@@ -130,6 +142,16 @@ int ffs_step(ffs_handle* h, int64_t nsteps);
  * s.nlstats/s.pressstats are) and, at a multiple of dtSpec, a spectrum record. Fields,
  * iteration and time do not change. Meant as the run's last call, as in the reference. */
 int ffs_finalize(ffs_handle* h);
+
+/* State of the kz = 0 plane forcing, per 2D shell (compute_shells2D, src/utils.jl:161-182).
+ * ffs_forcing_shells: the shell count (0 without plane forcing). ffs_forcing_array moves
+ * one per-shell array to (set 0) or from (set 1) the host: which 0 = R, the ODE state of
+ * rfForcing/cRfForcing (the reference's R.N files, forcing_types.jl:70-72,
+ * FluidFlowSimulation.jl:60-62); 1 = Em, the target spectrum (from the initial field at
+ * ffs_initialize, or set from targSpectrum.dat after it, forcing_types.jl:76-83);
+ * 2 = the shells' mean wavenumber avgK (read only). n must equal the shell count. */
+int ffs_forcing_shells(const ffs_handle* h);
+int ffs_forcing_array(ffs_handle* h, int32_t which, double* v, int32_t n, int32_t set);
 
 /* Physical fields at the current iteration (real!(s.u), src/output.jl:1-8). */
 int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout);

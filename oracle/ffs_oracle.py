@@ -163,6 +163,15 @@ class Params:
     forcing: bool = False
     forcing_power: float = 0.1
     forcing_kf: float = 2.5
+    # the reference's kz = 0 plane forcing (forcing_types.jl:335-450): rfForcing, cRfForcing, QfForcing
+    plane_forcing: str = ""
+    pf_tf: float = 0.0                   # TF
+    pf_alpha: float = 0.0                # alphac
+    pf_kf: float = 0.0                   # kf
+    pf_zf_tanh: bool = False             # Zf tanh (else cutoff)
+    pf_qp: float = 0.0                   # alveliusP
+    pf_qc: float = 0.0                   # alveliusC
+    pf_qkf: float = 0.0                  # alveliusKf
     dt_stat: int = 1
     dt_spec: int = 1
     write_time: int = 1 << 30
@@ -209,6 +218,14 @@ class Params:
             p.scalar_pr = _num(d["scalarPr"])
             p.scalar_gradient = _num(d["scalarGradient"])
             p.scalar_dir = {"x": 0, "y": 1, "z": 2}[d.get("scalarDirection", "z")]
+        if d.get("forcing") in ("rfForcing", "cRfForcing", "QfForcing"):
+            p.plane_forcing = d["forcing"]
+            p.pf_kf = float(d["kf"])
+            if p.plane_forcing == "QfForcing":
+                p.pf_qp, p.pf_qc, p.pf_qkf = (float(d[k]) for k in ("alveliusP", "alveliusC", "alveliusKf"))
+            else:
+                p.pf_tf, p.pf_alpha = float(d["TF"]), float(d["alphac"])
+                p.pf_zf_tanh = d.get("Zf", "cutoff") != "cutoff"
         if d.get("forcing") == "isotropicBand":
             p.forcing = True
             p.forcing_power = _num(d.get("forcingPower", "0.1"))
@@ -442,6 +459,146 @@ STATS_HEADER = ("iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dis
                 "nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss")
 
 
+class PlaneForcing:
+    """The reference's forcing of the kz = 0 plane (forcing.jl:6-114 rfForcing,
+    cforcing.jl:1-97 cRfForcing, qfforcing.jl:1-81 QfForcing): horizontal velocity of the
+    kx-ky modes in 2D shells |k_h| <= kf, scaled per shell, plus a few (0, 0, kz) modes
+    that take 1 % of the power; applied after the integrator (add_Rf_forcing!,
+    forcing_types.jl:54-64)."""
+
+    def __init__(self, p: "Params", g: Grid, lfilter: bool = False):
+        self.p, self.g = p, g
+        # compute_shells2D (utils.jl:161-182) over the stored half plane, all ky
+        self.nsh = min(g.nxh, g.ny // 2)
+        self.maxdk = max(g.kx[1], g.ky[1])
+        kh = np.zeros(self.nsh)
+        cnt = np.zeros(self.nsh, dtype=np.int64)
+        for j in range(g.ny):
+            for i in range(g.nxh):
+                K = math.sqrt(g.kx[i] ** 2 + g.ky[j] ** 2)
+                ii = int(np.rint(K / self.maxdk))
+                if ii >= self.nsh:
+                    break
+                kh[ii] += K
+                cnt[ii] += 1
+        self.kh = kh / cnt
+        kf = p.pf_kf
+        if p.plane_forcing == "QfForcing":
+            # build_Qf_power_spectrum! (forcing_types.jl:303-330)
+            R = np.zeros(self.nsh)
+            integral = 0.0
+            for i in range(1, self.nsh):
+                if self.kh[i] <= kf:
+                    term = math.exp(-((self.kh[i] - p.pf_qkf) / p.pf_qc) ** 2)
+                    R[i] = p.pf_qp * term
+                    integral += term
+            R /= integral
+            if lfilter:
+                d2 = p.filter_width ** 2
+                for i in range(1, self.nsh):
+                    if self.kh[i] <= kf:
+                        G = math.exp((-d2 / 24) * (self.kh[i] * self.kh[i]))
+                        R[i] *= G * G
+            self.R = R
+        else:
+            if p.pf_zf_tanh:   # calculate_Zf (utils.jl:184-198)
+                self.Zf = np.array([math.tanh((kf - k) / (0.25 * kf)) * (0.0 if (kf - k) <= 0.0 else 1.0)
+                                    for k in self.kh])
+            else:
+                self.Zf = (self.kh <= kf).astype(np.float64)
+            self.R = np.zeros(self.nsh)
+            self.Em = np.zeros(self.nsh)
+            self.factor = np.zeros(self.nsh)
+        # plane modes: shell index n (0-based) of each (ky, kx) with the force loop's
+        # K = sqrt(muladd(kx, kx, ky^2))
+        K = np.sqrt(dd.fma(*np.broadcast_arrays(g.kx[None, :], g.kx[None, :], (g.ky ** 2)[:, None])))
+        self.nmode = np.rint(K / self.maxdk).astype(np.int64)
+        Ks = np.sqrt(g.kx[None, :] ** 2 + (g.ky ** 2)[:, None])
+        self.nspec = np.rint(Ks / self.maxdk).astype(np.int64)
+        self.cf = np.where(np.arange(g.nxh) > 0, 2.0, 1.0)[None, :]
+        self.keep = g.keep[0]
+        self.hp = self.vp = 0.0
+
+    def plane_spectrum(self, u, mag: bool):
+        """calculate_u1u2_spectrum! / calculate_u1u2_mag_spectrum! (spectrum.jl:1-65) on kz = 0."""
+        a2 = np.abs(u[0][0]) ** 2 + np.abs(u[1][0]) ** 2
+        v = self.cf * np.sqrt(a2) if mag else 0.5 * self.cf * a2
+        E = np.zeros(self.nsh)
+        ok = self.keep & (self.nspec < self.nsh)
+        np.add.at(E, self.nspec[ok], v[ok])
+        return E
+
+    def initialize(self, u):
+        """initialize!(f::RfForcing, s) (forcing.jl / forcing_types.jl:66-73): the target
+        spectrum of the initial field (no targSpectrum.dat)."""
+        if self.p.plane_forcing != "QfForcing":
+            self.Em = self.plane_spectrum(u, False)
+
+    def __call__(self, u, dt, it, cfl, variable_dt):
+        """The force (fx, fy) for this step and hp, vp."""
+        p, g = self.p, self.g
+        kf = p.pf_kf
+        nz = g.nz
+        fx = np.zeros_like(u[0])
+        fy = np.zeros_like(u[1])
+        sel = self.keep & (self.nmode >= 1) & (self.nmode < self.nsh)
+        sel &= np.where(self.nmode < self.nsh, self.kh[np.minimum(self.nmode, self.nsh - 1)] <= kf, False)
+        u1, u2 = u[0][0], u[1][0]
+        vk = list(range(1, 6)) + [nz - k for k in range(1, 6)]   # Julia k = 2..6 and NZ-k+2
+        if p.plane_forcing == "QfForcing":
+            Ef = self.plane_spectrum(u, True)
+            umag = np.sqrt(np.abs(u1) ** 2 + np.abs(u2) ** 2)
+            n = np.minimum(self.nmode, self.nsh - 1)
+            fkn = dt * self.R[n] * 0.99 / Ef[n]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                s1 = np.where(sel, (u1 / umag) * fkn, 0.0)
+                s2 = np.where(sel, (u2 / umag) * fkn, 0.0)
+            fx[0], fy[0] = s1, s2
+            fv = np.sum(self.cf * (_proj(u1, s1 / dt) + _proj(u2, s2 / dt)))
+            hp = fv
+            usq = sum(abs(u[0][k, 0, 0]) ** 2 + abs(u[1][k, 0, 0]) ** 2 for k in (3, 4, 5, nz - 3, nz - 4, nz - 5))
+            f = dt * hp * (1 - 0.99) / (usq * 0.99)
+            vp = 0.0
+            for k in (3, 4, 5, nz - 3, nz - 4, nz - 5):
+                fx[k, 0, 0] = u[0][k, 0, 0] * f
+                fy[k, 0, 0] = u[1][k, 0, 0] * f
+                vp += _proj(u[0][k, 0, 0], fx[k, 0, 0] / dt) + _proj(u[1][k, 0, 0], fy[k, 0, 0] / dt)
+        else:
+            if p.plane_forcing == "rfForcing":
+                ts = dt / cfl
+                if variable_dt and it <= 3:
+                    ts /= (0.1, 0.2, 0.4, 0.8)[it]
+                omega = 2 * math.pi / (p.pf_tf * ts)
+            else:                                              # cRfForcing: ts = Tf
+                omega = 2 * math.pi / p.pf_tf
+            Ef = self.plane_spectrum(u, False)
+            alpha = p.pf_alpha
+            eps = np.finfo(np.float64).eps
+            for i in range(1, self.nsh):
+                if self.kh[i] <= kf:
+                    self.R[i] += dt * (-2 * alpha * omega * self.R[i] - omega * omega * (Ef[i] - self.Em[i]))
+                    self.R[i] = max(0.0, self.R[i])
+                    self.factor[i] = math.sqrt(self.R[i] / max(Ef[i], eps)) * self.Zf[i] * dt
+            fac = self.factor[np.minimum(self.nmode, self.nsh - 1)]
+            s1 = np.where(sel, u1 * fac, 0.0)
+            s2 = np.where(sel, u2 * fac, 0.0)
+            fx[0], fy[0] = s1, s2
+            ff = np.sum(self.cf * (np.abs(s1) ** 2 + np.abs(s2) ** 2))
+            fv = np.sum(self.cf * (_proj(u1, s1) + _proj(u2, s2)))
+            hp = ff * 0.5 / dt + fv / dt
+            umag = sum(math.sqrt(abs(u[0][k, 0, 0]) ** 2 + abs(u[1][k, 0, 0]) ** 2) for k in vk)
+            f = dt * math.sqrt(2.0 * hp * (1.0 - 0.99)) / umag
+            ff = fv = 0.0
+            for k in vk:
+                fx[k, 0, 0] = u[0][k, 0, 0] * f
+                fy[k, 0, 0] = u[1][k, 0, 0] * f
+                ff += abs(fx[k, 0, 0]) ** 2 + abs(fy[k, 0, 0]) ** 2
+                fv += _proj(u[0][k, 0, 0], fx[k, 0, 0]) + _proj(u[1][k, 0, 0], fy[k, 0, 0])
+            vp = ff * 0.5 / dt + fv / dt
+        self.hp, self.vp = float(hp), float(vp)
+        return fx, fy
+
+
 def stats_header(p: Params) -> str:
     """``statsheader`` (stats.jl:1-7); plug-in order = sim_fields (macros.jl:48)."""
     cols = [STATS_HEADER]
@@ -451,7 +608,7 @@ def stats_header(p: Params) -> str:
         cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux")
     if p.les:
         cols.append("prh,prv,praniso,pr")
-    if p.forcing:
+    if p.forcing or p.plane_forcing:
         cols.append("hp,vp,tp")
     if p.hv:
         cols.append("hdissh,hdissv,hdiss")
@@ -648,6 +805,8 @@ class OracleSimulation:
         self.spectra = {}
         self.force = None
         self.hp = self.vp = 0.0
+        self.pforce = PlaneForcing(p, g, lfilter=p.les) if p.plane_forcing else None
+        self.pforce_xy = None
         self.umax_hist = []
         # Optional Delta t sequence that replaces the CFL value of each set_dt! call, in
         # call order (parity tests feed the engine's own sequence here); newdt_hist
@@ -674,6 +833,8 @@ class OracleSimulation:
             self.rho = g.myfourier(self.rho)
         self.calculate_rhs()
         dt_now = self.get_dt()
+        if self.pforce is not None:                               # initialize!(s.forcing, s)
+            self.pforce.initialize(self.u)
         self.ts.initialize(self.rhs, dt_now)
         if self.p.fld:
             self.rts.initialize(self.rhorhs, dt_now)
@@ -804,7 +965,7 @@ class OracleSimulation:
             newdt = float(self.dt_sequence[len(self.newdt_hist)])
         self.newdt_hist.append(newdt)
         self.ts.set_dt(newdt)
-        if p.density:
+        if p.fld:   # density and passive scalar integrators (time_step_functions.jl:126-128)
             self.rts.set_dt(newdt)
 
     # ---------------------------------------------------------------- forcing (new)
@@ -832,12 +993,20 @@ class OracleSimulation:
         self.vp = float(np.sum((wb * sv)[band])) / dt
 
     # ---------------------------------------------------------------- advance_in_time!
+    def plane_force(self):
+        """s.forcing(s) of the kz = 0 plane family, from the current u (models.jl:6-9)."""
+        p = self.p
+        self.pforce_xy = self.pforce(self.u, self.get_dt(), self.iteration, p.cfl, p.variable_dt)
+        self.hp, self.vp = self.pforce.hp, self.pforce.vp
+
     def advance(self):
         """``advance_in_time!`` (models.jl:3-17)."""
         p, g = self.p, self.g
         self.calculate_rhs()
         if p.forcing:
             self.compute_forcing()
+        if self.pforce is not None:
+            self.plane_force()
         if self.is_stats_time():
             self.write_stats()
         # time_step! (models.jl:468-472) -> VectorTimeStep (time_step_functions.jl:72-80)
@@ -847,6 +1016,10 @@ class OracleSimulation:
             u = self.ts.step(self.u, self.rhs)
         if p.forcing:
             u = u + self.force
+        if self.pforce is not None:                               # add_Rf_forcing!, forcing_types.jl:54-64
+            u = u.copy()
+            u[0] = u[0] + self.pforce_xy[0]
+            u[1] = u[1] + self.pforce_xy[1]
         self.u = g.project(u)
         self.u[:, g.dealias] = 0.0
         if p.fld:
@@ -864,6 +1037,8 @@ class OracleSimulation:
         self.calculate_rhs()
         if self.p.forcing:
             self.compute_forcing()
+        if self.pforce is not None:
+            self.plane_force()
         self.write_stats()
 
     # ---------------------------------------------------------------- stats
@@ -953,7 +1128,7 @@ class OracleSimulation:
             extra += [prh, prv, (2 * prv) / prh, prh + prv]
             tdiss += prh + prv
             slot = hraw
-        if p.forcing:
+        if p.forcing or p.plane_forcing:
             extra += [self.hp, self.vp, self.hp + self.vp]
         if p.hv:
             hraw = self._wsum((g.K2 ** p.hv_m) * (a2[0] + a2[1]))

@@ -84,6 +84,11 @@ FIXED_CASES = {
     "etd-silvis": gdict(32, "ETD3rdO", lesModel="Silvis"),
     "ab3-stable-nonlinear": gdict(32, lesModel="stableNonLinear", nlConstant="0.05"),
     "etd-sandp-smagorinsky": gdict(32, "ETD3rdO", lesModel="SandP", sLesModel="Smagorinsky"),
+    # the reference's kz = 0 plane forcing family (forcing_types.jl:335-450)
+    "ab3-adaptive-rf-forcing": gdict(32, adaptive=True, forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
+    "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
+    "ab3-adaptive-qf-forcing-les": gdict(32, adaptive=True, forcing="QfForcing", alveliusP="0.1", alveliusC="1.0",
+                                         alveliusKf="2.0", kf="4.0", lesModel="Smagorinsky"),
     # passive scalar (simulationtypes.jl:198-213): the density's transport without buoyancy
     "etd-scalar": gdict(32, "ETD3rdO", passiveScalar="true", scalarPr="0.7", scalarGradient="1"),
     "ab3-adaptive-scalar-y": gdict(32, adaptive=True, passiveScalar="true", scalarPr="2", scalarGradient="0.5",

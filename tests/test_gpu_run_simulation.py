@@ -62,6 +62,9 @@ CASES = {
     # iteration (the tail row then keeps the last non-linear/pressure columns)
     "ab3-adaptive-timeDuration": {"velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true",
                                   "cfl": "0.4", "dt": "0.01", "nt": "1000", "timeDuration": "0.05"},
+    # rfForcing: the run ends by writing the shells' ODE state R.N (FluidFlowSimulation.jl:60-62)
+    "etd-rf-forcing": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "10",
+                       "forcing": "rfForcing", "TF": "2.0", "alphac": "1.0", "kf": "3.0"},
 }
 
 
@@ -98,6 +101,9 @@ def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
             assert got.shape == (len(want), 2)
             scale = max(np.abs(want).max(), 1e-300)
             assert np.allclose(got[:, 1], want, rtol=1e-10, atol=1e-12 * scale), f.name
+    if d.get("forcing") == "rfForcing":
+        R = np.loadtxt(tmp_path / f"R.{ref.iteration}")
+        assert np.allclose(R, ref.pforce.R, rtol=1e-10, atol=1e-14 * np.abs(ref.pforce.R).max())
     # field files: exactly the oracle's output iterations, raw Float64 n^3
     written = sorted(int(f.name.split(".")[1]) for f in tmp_path.glob("u1.*") if f.name != "u1.0")
     assert written == sorted(outputs)

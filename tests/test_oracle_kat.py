@@ -5,7 +5,7 @@ import math
 import numpy as np
 import pytest
 
-from oracle.ffs_oracle import ETD3, AB3, Grid, OracleSimulation, Params, fftfreq, rfftfreq, taylor_green
+from oracle.ffs_oracle import ETD3, AB3, Grid, OracleSimulation, Params, fftfreq, rfftfreq, stats_header, taylor_green
 
 
 def tg_params(n=32, **kw):
@@ -201,3 +201,35 @@ def test_config_fixture_is_the_oracle_run():
     s.run(21)
     assert np.allclose(np.array(s.stats_rows), z["stats"][:2], rtol=1e-12, atol=1e-15)
     assert z["stats"].shape[0] == 26 and z["stats"][-1, 0] == 500
+
+
+def test_qf_forcing_injects_its_power_split_99_to_1():
+    """QfForcing (qfforcing.jl:1-81): the horizontal kz = 0 modes take 0.99 P and the
+    (0, 0, kz) modes 0.01 P of the power alveliusP, at every step."""
+    d = {"nx": "32", "ny": "32", "nz": "32", "xDomainSize": "1.0", "yDomainSize": "1.0", "zDomainSize": "1.0",
+         "kinematicViscosity": "0.01", "dtStat": "1", "dtSpec": "100", "writeTime": "1000",
+         "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "false", "dt": "0.01",
+         "forcing": "QfForcing", "alveliusP": "0.25", "alveliusC": "1.0", "alveliusKf": "2.0", "kf": "4.0"}
+    rng = np.random.default_rng(3)
+    g = Grid(32, 32, 32)
+    uh = g.project(np.stack([g.myfourier(rng.standard_normal((32, 32, 32))) for _ in range(3)]))
+    s = OracleSimulation(Params.from_global(d), list(g.real(uh * np.exp(-g.K2 / 20)[None])))
+    s.initialize()
+    s.run(3)
+    r = np.array(s.stats_rows)
+    assert np.allclose(r[:, -3], 0.99 * 0.25, rtol=1e-12) and np.allclose(r[:, -2], 0.01 * 0.25, rtol=1e-12)
+    assert s.stats_rows and stats_header(s.p).endswith("hp,vp,tp")
+
+
+def test_rf_forcing_shells_match_compute_shells2D():
+    """compute_shells2D (utils.jl:161-182) at 32^3: 16 shells, shell 0 is k = 0 alone and
+    shell n averages |k_h| over the half plane with round(|k_h|) = n."""
+    from oracle.ffs_oracle import PlaneForcing
+    p = Params(nx=32, ny=32, nz=32, plane_forcing="rfForcing", pf_tf=1.0, pf_alpha=1.0, pf_kf=3.0)
+    f = PlaneForcing(p, Grid(32, 32, 32))
+    assert f.nsh == 16 and f.kh[0] == 0.0
+    kx, ky = np.arange(17), np.fft.fftfreq(32, 1 / 32)
+    K = np.sqrt(kx[None, :] ** 2 + ky[:, None] ** 2)
+    for n in (1, 5, 15):
+        assert f.kh[n] == pytest.approx(K[np.rint(K) == n].mean(), rel=1e-14)
+    assert np.array_equal(f.Zf, (f.kh <= 3.0).astype(np.float64)) and f.Zf[2] == 1.0 and f.Zf[4] == 0.0
