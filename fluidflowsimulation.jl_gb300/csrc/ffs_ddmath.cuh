@@ -8,6 +8,14 @@
 // correctly rounded value (except in vanishingly rare ties), and writing every
 // operation with __d*_rn pins the order, so the coefficients do not depend on the
 // compiler. The same sequence of operations is used by the CPU oracle.
+//
+// The error-free transformations are the published ones: Veltkamp's splitting and
+// Dekker's exact product (T. J. Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971), Knuth's branch-free exact sum (D. E.
+// Knuth, TAOCP vol. 2, section 4.2.2), and double-double addition, multiplication and
+// renormalisation as in Hida, Li and Bailey's QD library ("Algorithms for quad-double
+// precision floating point arithmetic", ARITH-15, 2001). exp/expm1 reduce the argument
+// by k ln 2 (ln 2 held as a double-double) and sum the Taylor series in double-double.
 #pragma once
 #include <cuda_runtime.h>
 

@@ -77,6 +77,11 @@ class Engine : public EngineBase {
   std::vector<void*> allocs;
   int64_t bytes = 0;
   FieldList inv_list{}, fwd_list{};
+  // the inverse z pass's fields by prologue family (copy, curl, strain), each launched on
+  // its own when split_iz: every CTA of a launch then runs one code path of the kernel
+  FieldList inv_fam[3]{};
+  int n_fam = 0;
+  int split_iz = 0;
   int nin = 0, nout = 0;
   int lyz = 4;
   int lio = LYZ_IO;           // (y,z) lines per CTA of the field-IO x kernels
@@ -303,6 +308,20 @@ class Engine : public EngineBase {
     if (I.les) for (int c = F_SXX; c <= F_SYZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
     if (I.density) { inv_list.code[nin] = F_RHO; inv_list.slot[nin] = nin; ++nin; }
     inv_list.n = nin;
+    {
+      FieldList fam[3]{};
+      for (int i = 0; i < nin; ++i) {
+        const int c = inv_list.code[i];
+        const int f = (c <= F_UZ || c == F_RHO) ? 0 : (c <= F_WZ ? 1 : 2);
+        fam[f].code[fam[f].n] = c;
+        fam[f].slot[fam[f].n] = inv_list.slot[i];
+        ++fam[f].n;
+      }
+      n_fam = 0;
+      for (int f = 0; f < 3; ++f)
+        if (fam[f].n) inv_fam[n_fam++] = fam[f];
+    }
+    split_iz = p.nz >= 128 ? 1 : 0;
     nout = 0;
     auto addo = [&](int role, int slot) { fwd_list.code[nout] = role; fwd_list.slot[nout] = slot; ++nout; };
     addo(R_NX, 0); addo(R_NY, 1); addo(R_NZ, 2); addo(R_KE, 3);
@@ -728,8 +747,15 @@ class Engine : public EngineBase {
   void launch_stats(int mode) { k_stats<T><<<nparts, 256, 0, s>>>(I, mode); }
   void launch_fin(int mode) { k_finalize<T><<<1, 1024, 0, s>>>(I, mode, nparts); }
 
+  void launch_inv_z_step() {
+    if (split_iz && n_fam > 1) {
+      for (int f = 0; f < n_fam; ++f) launch_inv_z(inv_fam[f]);
+    } else {
+      launch_inv_z(inv_list);
+    }
+  }
   void enqueue_step(int mode) {
-    launch_inv_z(inv_list);
+    launch_inv_z_step();
     launch_inv_y(inv_list);
     launch_x();
     // dt, the integrator's scalars, the band energy and the ETD table need only the x
@@ -750,7 +776,9 @@ class Engine : public EngineBase {
     if (mode != 2) launch_update(mode);   // the run's tail evaluates the rhs and stats only
     launch_fin(mode);
   }
-  int launches_per_step() const override { return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0); }
+  int launches_per_step() const override {
+    return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0) + ((split_iz && n_fam > 1) ? n_fam - 1 : 0);
+  }
   void launch_plane_forcing(int mode) {
     if (I.pforce) k_plane_forcing<T><<<1, 256, 0, s>>>(I, mode);
   }
@@ -1148,7 +1176,7 @@ class Engine : public EngineBase {
     const int64_t it0 = iteration;
     for (int64_t i = 0; i < n; ++i) {
       FFS_CK(cudaEventRecord(ev[0], s));
-      launch_inv_z(inv_list); FFS_CK(cudaEventRecord(ev[1], s));
+      launch_inv_z_step(); FFS_CK(cudaEventRecord(ev[1], s));
       launch_inv_y(inv_list); FFS_CK(cudaEventRecord(ev[2], s));
       launch_x(); FFS_CK(cudaEventRecord(ev[3], s));
       launch_fwd_y(fwd_list); FFS_CK(cudaEventRecord(ev[4], s));
@@ -1184,7 +1212,7 @@ class Engine : public EngineBase {
   // Each group is tuned on its own (they are independent passes). The choice is cached
   // per grid, model and precision for the process, so engines of the same shape tune once.
   struct TuneChoice {
-    int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy;
+    int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, split_iz;
     std::string report;
   };
   static std::mutex& tune_mu() { static std::mutex m; return m; }
@@ -1202,6 +1230,7 @@ class Engine : public EngineBase {
         const TuneChoice& c = it->second;
         txy = c.txy; use_ct = c.use_ct; lyz = c.lyz; xfused = c.xfused; txz = c.txz; zseq = c.zseq;
         use_ct_z = c.use_ct_z; pair_z = c.pair_z; v_iz = c.v_iz; v_iy = c.v_iy; v_fy = c.v_fy;
+        split_iz = c.split_iz;
         tune_report = c.report + " (cached)";
         compute_smem();
         return set_smem(err);
@@ -1271,6 +1300,20 @@ class Engine : public EngineBase {
         return 0;
       };
       if (!rc) rc = pick(v_iz, "z_inv", ctz(), [&] { launch_inv_z(inv_list); });
+      // one launch for every field family, or one per family
+      if (!rc && n_fam > 1) {
+        float bms = 1e30f;
+        int bs = 0;
+        for (int sp = 0; sp < 2 && !rc; ++sp) {
+          split_iz = sp;
+          float ms = 0.f;
+          rc = timed([&] { launch_inv_z_step(); }, ms);
+          snprintf(line, sizeof(line), "z_inv[%s]=%.4fms ", sp ? "split" : "joint", ms);
+          rep += line;
+          if (ms < bms) { bms = ms; bs = sp; }
+        }
+        split_iz = bs;
+      }
       if (!rc) rc = pick(v_iy, "y_inv", cty(), [&] { launch_inv_y(inv_list); });
       if (!rc) rc = pick(v_fy, "y_fwd", cty(), [&] { launch_fwd_y(fwd_list); });
     }
@@ -1316,8 +1359,8 @@ class Engine : public EngineBase {
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
-    snprintf(line, sizeof(line), "-> tx_yz=%d %s [z_inv %s, y_inv %s, y_fwd %s], x=%s%d, fwd_z tx=%d %s %s", txy,
-             use_ct ? "ct" : "rt", vname_of(v_iz), vname_of(v_iy), vname_of(v_fy),
+    snprintf(line, sizeof(line), "-> tx_yz=%d %s [z_inv %s%s, y_inv %s, y_fwd %s], x=%s%d, fwd_z tx=%d %s %s", txy,
+             use_ct ? "ct" : "rt", vname_of(v_iz), split_iz ? " split" : "", vname_of(v_iy), vname_of(v_fy),
              xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c",
              use_ct_z ? (zpair() ? "ct2" : "ct") : "rt");
     rep += line;
@@ -1326,7 +1369,8 @@ class Engine : public EngineBase {
     if ((rc = set_smem(err))) return rc;
     {
       std::lock_guard<std::mutex> g(tune_mu());
-      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, rep};
+      tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, split_iz,
+                                     rep};
     }
     return reset_state(err);
   }

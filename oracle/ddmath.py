@@ -12,6 +12,11 @@ ties. The GPU engine runs the identical sequence of IEEE operations
 
 Every function is elementwise on float64 numpy arrays; operation order is fixed and
 must stay in step with the device code.
+
+Methods: Veltkamp's splitting and Dekker's exact product (Dekker, Numer. Math. 18, 1971),
+Knuth's exact sum (TAOCP vol. 2, section 4.2.2), double-double arithmetic as in Hida, Li
+and Bailey's QD library (ARITH-15, 2001); exp/expm1 by k ln 2 argument reduction and a
+double-double Taylor series.
 """
 from __future__ import annotations
 
