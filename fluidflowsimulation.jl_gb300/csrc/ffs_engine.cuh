@@ -229,7 +229,7 @@ class Engine : public EngineBase {
       return FFS_EINVAL;
     }
     if (p.plane_forcing) {
-      if (p.plane_forcing < FFS_PF_RF || p.plane_forcing > FFS_PF_QF) { err = "unknown plane forcing"; return FFS_EINVAL; }
+      if (p.plane_forcing < FFS_PF_RF || p.plane_forcing > FFS_PF_A) { err = "unknown plane forcing"; return FFS_EINVAL; }
       if (p.forcing) { err = "isotropicBand and kz = 0 plane forcing together are not supported"; return FFS_EINVAL; }
       if (p.nz < 16) { err = "kz = 0 plane forcing needs nz >= 16 (it forces kz = +-1..+-5)"; return FFS_EUNSUPPORTED; }
       if (p.plane_forcing != FFS_PF_QF && !(p.pf_tf > 0)) { err = "TF must be positive"; return FFS_EINVAL; }
@@ -321,7 +321,7 @@ class Engine : public EngineBase {
       for (int f = 0; f < 3; ++f)
         if (fam[f].n) inv_fam[n_fam++] = fam[f];
     }
-    split_iz = p.nz >= 128 ? 1 : 0;
+    split_iz = 0;   // one launch for all families (0.076 ms against 0.097 ms split at 256^3)
     nout = 0;
     auto addo = [&](int role, int slot) { fwd_list.code[nout] = role; fwd_list.slot[nout] = slot; ++nout; };
     addo(R_NX, 0); addo(R_NY, 1); addo(R_NZ, 2); addo(R_KE, 3);
@@ -416,8 +416,8 @@ class Engine : public EngineBase {
       n_sms = sms;
     }
     // record layout
-    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) + ((I.forcing || I.pforce) ? 3 : 0) +
-                  (I.hv ? 3 : 0);
+    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) +
+                  (I.pforce == FFS_PF_A ? 2 : ((I.forcing || I.pforce) ? 3 : 0)) + (I.hv ? 3 : 0);
     if (I.pforce && (rc = plane_forcing_tables(p, err))) return rc;
     ncols_rec = ncols_stats + 13;
     I.ncols = ncols_rec;
@@ -460,7 +460,8 @@ class Engine : public EngineBase {
     if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
     else if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
     if (I.les) header += ",prh,prv,praniso,pr";
-    if (I.forcing || I.pforce) header += ",hp,vp,tp";
+    if (I.pforce == FFS_PF_A) header += ",hp,vp";
+    else if (I.forcing || I.pforce) header += ",hp,vp,tp";
     if (I.hv) header += ",hdissh,hdissv,hdiss";
     FFS_CK(cudaStreamSynchronize(s));
     return 0;
@@ -765,13 +766,14 @@ class Engine : public EngineBase {
     cudaStreamWaitEvent(s2, ev_fork, 0);
     std::swap(s, s2);
     launch_scalar(mode);
-    launch_plane_forcing(mode);
+    if (!pf_after_fwd()) launch_plane_forcing(mode);
     launch_table(mode);
     std::swap(s, s2);
     cudaEventRecord(ev_join, s2);
     launch_fwd_y(fwd_list);
     launch_zu(mode);
     cudaStreamWaitEvent(s, ev_join, 0);
+    if (pf_after_fwd()) launch_plane_forcing(mode);   // reads the step's right-hand side
     launch_stats(mode);
     if (mode != 2) launch_update(mode);   // the run's tail evaluates the rhs and stats only
     launch_fin(mode);
@@ -779,6 +781,8 @@ class Engine : public EngineBase {
   int launches_per_step() const override {
     return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0) + ((split_iz && n_fam > 1) ? n_fam - 1 : 0);
   }
+  // nRf / cNRf use the plane's non-linear transfer, so they wait for the forward passes
+  bool pf_after_fwd() const { return I.pforce == FFS_PF_NRF || I.pforce == FFS_PF_CNRF; }
   void launch_plane_forcing(int mode) {
     if (I.pforce) k_plane_forcing<T><<<1, 256, 0, s>>>(I, mode);
   }
@@ -809,6 +813,7 @@ class Engine : public EngineBase {
     for (int i = 0; i < nsh; ++i)
       zf[i] = p.pf_zf_tanh ? tanh((kf - kh[i]) / (0.25 * kf)) * (((kf - kh[i]) <= 0.0) ? 0.0 : 1.0)
                            : (kh[i] <= kf ? 1.0 : 0.0);
+    const bool af = p.plane_forcing == FFS_PF_A;
     if (p.plane_forcing == FFS_PF_QF) {
       double integral = 0.0;
       for (int i = 1; i < nsh; ++i)
@@ -833,6 +838,7 @@ class Engine : public EngineBase {
     const int plane = I.NYR * I.KXP;
     std::vector<std::vector<int>> byshell(nsh);
     std::vector<int> nmode(plane, -1);
+    std::vector<double> zf2(plane, 0.0);   // aForcing: calculate_Zf(d, kf, kx, ky) per mode
     for (int jc = 0; jc < I.NYR; ++jc) {
       const int y = jc < I.ypos ? jc : p.ny - I.NYR + jc;
       for (int ix = 0; ix < I.Mx; ++ix) {
@@ -840,8 +846,16 @@ class Engine : public EngineBase {
         const int m = jc * I.KXP + ix;
         const long long ns = llrint(sqrt(kx * kx + ky * ky) / maxdk);
         if (ns < nsh) byshell[ns].push_back(m);
-        const long long nf = llrint(sqrt(std::fma(kx, kx, ky * ky)) / maxdk);
-        if (nf >= 1 && nf < nsh && kh[nf] <= kf) nmode[m] = (int)nf;
+        if (af) {   // 0 < |k_h| <= kf with |k_h| = sqrt(muladd(kx, kx, ky^2)) (aforcing.jl)
+          const double K = sqrt(std::fma(kx, kx, ky * ky));
+          if (K > 0 && K <= kf) nmode[m] = 0;
+          const double Kz = sqrt(kx * kx + ky * ky);
+          zf2[m] = p.pf_zf_tanh ? tanh((kf - Kz) / (0.25 * kf)) * (((kf - Kz) <= 0.0) ? 0.0 : 1.0)
+                                : (Kz <= kf ? 1.0 : 0.0);
+        } else {
+          const long long nf = llrint(sqrt(std::fma(kx, kx, ky * ky)) / maxdk);
+          if (nf >= 1 && nf < nsh && kh[nf] <= kf) nmode[m] = (int)nf;
+        }
       }
     }
     std::vector<int> start(nsh + 1, 0), modes;
@@ -850,8 +864,9 @@ class Engine : public EngineBase {
       modes.insert(modes.end(), byshell[n].begin(), byshell[n].end());
     }
     start[nsh] = (int)modes.size();
-    std::vector<double> d(6 * (size_t)nsh, 0.0);
+    std::vector<double> d(8 * (size_t)nsh + 4 * (size_t)plane, 0.0);
     for (int i = 0; i < nsh; ++i) { d[3 * nsh + i] = kh[i]; d[4 * nsh + i] = zf[i]; d[5 * nsh + i] = qr[i]; }
+    for (int m = 0; m < plane; ++m) d[8 * (size_t)nsh + 3 * (size_t)plane + m] = zf2[m];
     int rc;
     double* dd_ = nullptr;
     int *ds = nullptr, *dm = nullptr, *dn = nullptr;
@@ -873,15 +888,15 @@ class Engine : public EngineBase {
   }
   std::vector<double> pf_avgk;
 
-  int forcing_shells() const override { return I.pforce ? I.pf_nsh : 0; }
+  int forcing_shells() const override { return (I.pforce && I.pforce != FFS_PF_A) ? I.pf_nsh : 0; }
   int forcing_array(int which, double* v, int n, int set, std::string& err) override {
-    if (!I.pforce) { err = "no kz = 0 plane forcing in this simulation"; return FFS_ESTATE; }
-    if (!v || n != I.pf_nsh || which < 0 || which > 2 || (which == 2 && set)) {
-      err = "forcing array: which must be 0 (R), 1 (Em) or 2 (avgK, read only), n the shell count";
+    if (!I.pforce || I.pforce == FFS_PF_A) { err = "no per-shell plane forcing in this simulation"; return FFS_ESTATE; }
+    if (!v || n != I.pf_nsh || which < 0 || which > 3 || (which == 2 && set)) {
+      err = "forcing array: which must be 0 (R), 1 (Em), 2 (avgK, read only) or 3 (N), n the shell count";
       return FFS_EINVAL;
     }
     if (which == 2) { std::copy(pf_avgk.begin(), pf_avgk.end(), v); return 0; }
-    double* dst = I.pf_d + (size_t)which * I.pf_nsh;
+    double* dst = I.pf_d + (size_t)(which == 3 ? 6 : which) * I.pf_nsh;
     if (set) FFS_CK(cudaMemcpyAsync(dst, v, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     else FFS_CK(cudaMemcpyAsync(v, dst, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     FFS_CK(cudaStreamSynchronize(s));

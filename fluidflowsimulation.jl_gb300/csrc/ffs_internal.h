@@ -130,10 +130,12 @@ template <typename T> struct Inst {
   // kz = 0 plane forcing (FFS_PF_*): per-shell state and tables, plane-mode lists, force
   int pforce, pf_nsh;
   double pf_maxdk, pf_kf, pf_tf, pf_alpha, pf_cfl;
-  double* pf_d;            // [6][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum
+  double* pf_d;            // [8][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum, N, Nm1;
+                           // then aForcing's [4][NYR * KXP]: R, Em, factor, Zf per plane mode
   const int* pf_start;     // [nsh + 1]: retained kz = 0 modes of each spectrum shell (CSR)
   const int* pf_modes;     //   their plane index jc * KXP + ix
-  const int* pf_nmode;     // [NYR * KXP]: forcing shell of each plane mode (-1: not forced)
+  const int* pf_nmode;     // [NYR * KXP]: forcing shell of each plane mode (-1: not forced;
+                           // aForcing: 0 for the forced modes)
   cplx<T>* pf_force;       // [2][NYR * KXP] force on the kz = 0 plane, then [2][10] (0, 0, kz) modes
   int dt_stat, dt_spec;
   // the same constants in the arithmetic type (no per-element conversions)

@@ -647,13 +647,56 @@ __global__ void k_scalar(Inst<T> I, int mode) {
 
 // ====================================================================================
 // kz = 0 plane forcing (rfForcing forcing.jl:6-114, cRfForcing cforcing.jl:1-97,
-// QfForcing qfforcing.jl:1-81), from the current u after set_dt! (models.jl:6-9). One CTA,
-// FP64. mode 1 (initialize!): the target spectrum Em of the initial field
-// (forcing_types.jl:66-73); mode 0 / 2: the force of this step into pf_force and the
-// powers hp, vp. Shell sums run one thread per shell over the shell's modes in a fixed
-// order, the power sums through a fixed-order block reduction: every call is
-// deterministic.
+// nRfForcing nrforcing.jl, cNRfForcing cnrforcing.jl, aForcing aforcing.jl, QfForcing
+// qfforcing.jl:1-81), from the current u after set_dt! (models.jl:6-9). One CTA, FP64.
+// mode 1 (initialize!): the target spectrum Em of the initial field (forcing_types.jl
+// :66-73; nRf/cNRf also N = Nm1 from the initial right-hand side; aForcing per mode);
+// mode 0 / 2: the force of this step into pf_force and the powers hp, vp. Shell sums
+// run one thread per shell over the shell's modes in a fixed order, the power sums
+// through a fixed-order block reduction: every call is deterministic. nRf/cNRf read the
+// step's right-hand side, so they run after the forward passes.
 // ====================================================================================
+// The projected right-hand side of a kz = 0 mode, as the update forms it
+// (fourierspacep2!, models.jl:282-341): N + (AB3) explicit (hyper)viscosity + i k.tau
+// + rho g, then the projection.
+template <typename T>
+__device__ __forceinline__ void plane_rhs(const Inst<T>& I, int m, double* out) {
+  const long long cs = I.cstride;
+  const int ix = m % I.KXP, jc = m / I.KXP;
+  const int ky_i = ysig(I, jc);
+  const T kx = kval(ix, I.Lx_t, I.iLx_t), ky = kval(ky_i, I.Ly_t, I.iLy_t), kz = T(0);
+  const T k2 = kx * kx + (ky * ky + kz * kz);
+  const bool k0 = ix == 0 && ky_i == 0;
+  cplx<T> rhs[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) rhs[c] = I.sbuf[c * cs + m];
+  if (I.ab3) {
+    T cv;
+    if (sizeof(T) == 8) {
+      const double kd = (double)k2;
+      double km = kd;
+      for (int i = 1; i < I.hv_m; ++i) km = dd::M(km, kd);
+      cv = T(I.hv ? dd::A(dd::M(kd, -I.nu), dd::M(km, -I.hv_nu)) : dd::M(kd, -I.nu));
+    } else {
+      cv = k2 * (-I.nu_t);
+      if (I.hv) { T km = k2; for (int i = 1; i < I.hv_m; ++i) km *= k2; cv += km * (-I.hvnu_t); }
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + scl(I.uh[c * cs + m], cv);
+  }
+  if (I.les) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + I.sbuf[(4 + c) * cs + m];
+  }
+  if (I.density) rhs[I.gdir] = rhs[I.gdir] + scl(I.uh[3 * cs + m], I.gval_t);
+  const cplx<T> kd = mk(kx * rhs[0].x + ky * rhs[1].x + kz * rhs[2].x, kx * rhs[0].y + ky * rhs[1].y + kz * rhs[2].y);
+  const T inv = k0 ? T(0) : T(1) / k2;
+  const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
+  rhs[0] = rhs[0] + scl(p1, kx);
+  rhs[1] = rhs[1] + scl(p1, ky);
+  out[0] = rhs[0].x; out[1] = rhs[0].y; out[2] = rhs[1].x; out[3] = rhs[1].y;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
   DevState* S = I.st;
@@ -664,57 +707,102 @@ __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
   const double* kh = fac + nsh;
   const double* Zf = kh + nsh;
   const double* QR = Zf + nsh;
-  const bool qf = I.pforce == FFS_PF_QF;
+  double* Nn = const_cast<double*>(QR) + nsh;
+  double* Nm1 = Nn + nsh;
+  const int kind = I.pforce;
+  const bool qf = kind == FFS_PF_QF, af = kind == FFS_PF_A;
+  const bool nl = kind == FFS_PF_NRF || kind == FFS_PF_CNRF;
   const long long cs = I.cstride;
   const int plane = I.NYR * I.KXP;
+  double* R2 = Nm1 + nsh;          // aForcing, per plane mode
+  double* Em2 = R2 + plane;
+  double* fac2 = Em2 + plane;
+  const double* Zf2 = fac2 + plane;
   __shared__ double Ef[FFS_PF_MAXSH];
+  __shared__ double NS[FFS_PF_MAXSH];
   __shared__ double red[2][256];
-  // calculate_u1u2_spectrum! / calculate_u1u2_mag_spectrum! (spectrum.jl:1-65)
-  for (int n = threadIdx.x; n < nsh; n += blockDim.x) {
-    double e = 0.0;
-    for (int q = I.pf_start[n]; q < I.pf_start[n + 1]; ++q) {
-      const int m = I.pf_modes[q];
-      const cplx<T> a = I.uh[m], b = I.uh[cs + m];
-      const double cf = (m % I.KXP) > 0 ? 2.0 : 1.0;
-      const double a2 = (double)a.x * a.x + (double)a.y * a.y + ((double)b.x * b.x + (double)b.y * b.y);
-      e += qf ? cf * sqrt(a2) : 0.5 * cf * a2;
+  const double nu = I.nu;
+  auto modes_a2 = [&](int m) {
+    const cplx<T> a = I.uh[m], b = I.uh[cs + m];
+    return (double)a.x * a.x + (double)a.y * a.y + ((double)b.x * b.x + (double)b.y * b.y);
+  };
+  // calculate_u1u2_spectrum! / calculate_u1u2_mag_spectrum! (spectrum.jl:1-65) and, for
+  // nRf/cNRf, calculate_nn_spectrum! (nrforcing.jl: proj(u, rhs - nu k^2 u) per shell)
+  if (!af) {
+    for (int n = threadIdx.x; n < nsh; n += blockDim.x) {
+      double e = 0.0, en = 0.0;
+      for (int q = I.pf_start[n]; q < I.pf_start[n + 1]; ++q) {
+        const int m = I.pf_modes[q];
+        const double cf = (m % I.KXP) > 0 ? 2.0 : 1.0;
+        const double a2 = modes_a2(m);
+        e += qf ? cf * sqrt(a2) : 0.5 * cf * a2;
+        if (nl) {
+          double r[4];
+          plane_rhs<T>(I, m, r);
+          const int ix = m % I.KXP;
+          const double kx = ix / I.lx, ky = ysig(I, m / I.KXP) / I.ly;
+          const double k2 = kx * kx + ky * ky;
+          const double ax = I.uh[m].x, ay = I.uh[m].y, bx = I.uh[cs + m].x, by = I.uh[cs + m].y;
+          const double nk = nu * k2;
+          en += cf * (fma(ax, r[0] - nk * ax, ay * (r[1] - nk * ay)) + fma(bx, r[2] - nk * bx, by * (r[3] - nk * by)));
+        }
+      }
+      Ef[n] = e;
+      NS[n] = en;
     }
-    Ef[n] = e;
   }
   __syncthreads();
+  const double eps = 2.220446049250313e-16;
   if (mode == 1) {
-    if (!qf) for (int n = threadIdx.x; n < nsh; n += blockDim.x) Em[n] = Ef[n];
+    if (af) {
+      for (int m = threadIdx.x; m < plane; m += blockDim.x)
+        Em2[m] = 0.5 * ((m % I.KXP) > 0 ? 2.0 : 1.0) * modes_a2(m);
+    } else if (!qf) {
+      for (int n = threadIdx.x; n < nsh; n += blockDim.x) {
+        Em[n] = Ef[n];
+        if (nl) { Nn[n] = NS[n]; Nm1[n] = NS[n]; }
+      }
+    }
     return;
   }
   const double dt = S->dt;
   const long long it = S->iteration;
-  const double kf = I.pf_kf;
-  if (!qf) {   // the shells' ODE (forcing.jl:47-53)
-    double omega;
-    if (I.pforce == FFS_PF_RF) {
-      double ts = dt / I.pf_cfl;
-      if (I.adaptive) {
-        if (it == 0) ts /= 0.1;
-        else if (it == 1) ts /= 0.2;
-        else if (it == 2) ts /= 0.4;
-        else if (it == 3) ts /= 0.8;
-      }
-      omega = (2 * M_PI) / (I.pf_tf * ts);
-    } else {
-      omega = (2 * M_PI) / I.pf_tf;
+  const double kf = I.pf_kf, alpha = I.pf_alpha;
+  double omega = 0.0;
+  if (kind == FFS_PF_RF || kind == FFS_PF_NRF) {   // ts = dt / cfl with the CFL ramp
+    double ts = dt / I.pf_cfl;
+    if (I.adaptive) {
+      if (it == 0) ts /= 0.1;
+      else if (it == 1) ts /= 0.2;
+      else if (it == 2) ts /= 0.4;
+      else if (it == 3) ts /= 0.8;
     }
-    const double alpha = I.pf_alpha, eps = 2.220446049250313e-16;
+    omega = (2 * M_PI) / (I.pf_tf * ts);
+  } else if (kind == FFS_PF_CRF) {
+    omega = (2 * M_PI) / I.pf_tf;                   // ts = Tf, omega = 2 pi / ts
+  } else if (kind == FFS_PF_CNRF) {
+    omega = (2 * M_PI) / (I.pf_tf * I.pf_tf);       // ts = Tf, omega = 2 pi / (Tf ts)
+  } else if (af) {
+    omega = (2 * M_PI) / (I.pf_tf * (10 * dt));     // ts = 10 dt
+  }
+  if (!qf && !af) {   // the shells' ODE (forcing.jl:47-53, nrforcing.jl)
+    const double dtm2 = S->dt2;
     for (int n = 1 + threadIdx.x; n < nsh; n += blockDim.x) {
+      if (nl) { Nm1[n] = Nn[n]; Nn[n] = NS[n]; }
       if (kh[n] <= kf) {
-        double r = R[n] + dt * (-2 * alpha * omega * R[n] - omega * omega * (Ef[n] - Em[n]));
+        double r;
+        if (nl) r = R[n] + dt * (-2 * alpha * omega * (R[n] + Nn[n]) - (Nn[n] - Nm1[n]) / dtm2 -
+                                 omega * omega * (Ef[n] - Em[n]));
+        else r = R[n] + dt * (-2 * alpha * omega * R[n] - omega * omega * (Ef[n] - Em[n]));
         r = fmax(0.0, r);
         R[n] = r;
         fac[n] = sqrt(r / fmax(Ef[n], eps)) * Zf[n] * dt;
       }
     }
+    if (nl && threadIdx.x == 0) { Nm1[0] = Nn[0]; Nn[0] = NS[0]; }
   }
   __syncthreads();
-  // horizontal forcing of the kz = 0 plane (forcing.jl:57-77, qfforcing.jl:22-45)
+  // horizontal forcing of the kz = 0 plane (forcing.jl:57-77, aforcing.jl, qfforcing.jl:22-45)
   double ff = 0.0, fv = 0.0;
   for (int m = threadIdx.x; m < plane; m += blockDim.x) {
     const int n = I.pf_nmode[m];
@@ -730,7 +818,16 @@ __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
         s1x = (ax / umag) * fkn; s1y = (ay / umag) * fkn; s2x = (bx / umag) * fkn; s2y = (by / umag) * fkn;
         fv += (fma(ax, s1x / dt, ay * (s1y / dt)) + fma(bx, s2x / dt, by * (s2y / dt))) * cf;
       } else {
-        const double g = fac[n];
+        double g;
+        if (af) {   // the ODE of this mode (aforcing.jl)
+          const double e = 0.5 * cf * (ax * ax + ay * ay + (bx * bx + by * by));
+          const double r = fmax(0.0, R2[m] + dt * (-2 * alpha * omega * R2[m] - omega * omega * (e - Em2[m])));
+          R2[m] = r;
+          g = sqrt(r / fmax(e, eps)) * Zf2[m] * dt;
+          fac2[m] = g;
+        } else {
+          g = fac[n];
+        }
         s1x = ax * g; s1y = ay * g; s2x = bx * g; s2y = by * g;
         ff += (s1x * s1x + s1y * s1y + (s2x * s2x + s2y * s2y)) * cf;
         fv += (fma(ax, s1x, ay * s1y) + fma(bx, s2x, by * s2y)) * cf;
@@ -750,7 +847,7 @@ __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
   }
   if (threadIdx.x != 0) return;
   const double hp = qf ? red[1][0] : red[0][0] * 0.5 / dt + red[1][0] / dt;
-  // vertical forcing of the (0, 0, kz) modes, kz = +-1..+-5 (Rf) or +-3..+-5 (Qf)
+  // vertical forcing of the (0, 0, kz) modes, kz = +-1..+-5 (Rf family) or +-3..+-5 (Qf)
   cplx<T>* fvert = I.pf_force + 2 * plane;
   auto at = [&](int kz) -> long long {   // compact index of (0, 0, kz)
     const int kc = kz >= 0 ? kz : I.NZR + kz;
@@ -1446,6 +1543,8 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       if (I.forcing) {
         const double dt = S->dt;
         row[c++] = tot[Q_HP] / dt; row[c++] = tot[Q_VP] / dt; row[c++] = (tot[Q_HP] + tot[Q_VP]) / dt;
+      } else if (I.pforce == FFS_PF_A) {   // stats(a::AForcing) (forcing_types.jl:98): hp, vp
+        row[c++] = S->pf_hp; row[c++] = S->pf_vp;
       } else if (I.pforce) {   // stats(a::RfForcing) (forcing_types.jl:33): F.hp, F.vp of the last call
         row[c++] = S->pf_hp; row[c++] = S->pf_vp; row[c++] = S->pf_hp + S->pf_vp;
       }

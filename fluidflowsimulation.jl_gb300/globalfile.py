@@ -77,7 +77,7 @@ def _set_les(p: FFSParams, d: dict[str, str]) -> None:
         p.filter_width = 0.0                                 # the engine's default (lx 2 pi / nx) / cutoff
 
 
-PLANE_FORCING = {"rfForcing": 1, "cRfForcing": 2, "QfForcing": 3}
+PLANE_FORCING = {"rfForcing": 1, "cRfForcing": 2, "QfForcing": 3, "nRfForcing": 4, "cNRfForcing": 5, "aForcing": 6}
 
 
 def parameters(d: dict[str, str], precision: str | None = None, device: int = 0) -> FFSParams:
@@ -148,7 +148,8 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
                 p.pf_tf, p.pf_alpha = float(d["TF"]), float(d["alphac"])
                 p.pf_zf_tanh = 0 if d.get("Zf", "cutoff") == "cutoff" else 1
         else:
-            raise ValueError(f"forcing {f!r} is not supported (isotropicBand, rfForcing, cRfForcing, QfForcing)")
+            raise ValueError(f"forcing {f!r} is not supported (isotropicBand, rfForcing, cRfForcing, nRfForcing, "
+                             "cNRfForcing, aForcing, QfForcing)")
     if "referenceCflSlot" in d:
         p.reference_cfl_slot = 1 if _bool(d["referenceCflSlot"]) else 0
     if "autotune" in d:   # engine key: time the candidate launch shapes at create

@@ -115,8 +115,10 @@ function parameters(d)
         p.forcing = 1
         p.forcing_power = haskey(d, :forcingPower) ? num(d[:forcingPower]) : 0.1
         p.forcing_kf = haskey(d, :forcingKf) ? num(d[:forcingKf]) : 2.5
-    elseif get(d, :forcing, "") in ("rfForcing", "cRfForcing", "QfForcing")   # forcing_types.jl:335-450
-        p.plane_forcing = Dict("rfForcing" => 1, "cRfForcing" => 2, "QfForcing" => 3)[d[:forcing]]
+    elseif get(d, :forcing, "") in ("rfForcing", "cRfForcing", "QfForcing", "nRfForcing", "cNRfForcing", "aForcing")
+        # forcing_model (forcing_types.jl:335-450)
+        p.plane_forcing = Dict("rfForcing" => 1, "cRfForcing" => 2, "QfForcing" => 3, "nRfForcing" => 4,
+                               "cNRfForcing" => 5, "aForcing" => 6)[d[:forcing]]
         p.pf_kf = parse(Float64, d[:kf])
         if d[:forcing] == "QfForcing"
             p.pf_qp = parse(Float64, d[:alveliusP]); p.pf_qc = parse(Float64, d[:alveliusC])

@@ -121,8 +121,9 @@ class Simulation:
 
     def forcing_array(self, which: str, values=None) -> np.ndarray:
         """Per-shell state of the kz = 0 plane forcing: "R" (the ODE state of the R.N files),
-        "Em" (target spectrum) or "avgK" (mean wavenumber, read only). With values, set it."""
-        w = {"R": 0, "Em": 1, "avgK": 2}[which]
+        "Em" (target spectrum), "avgK" (mean wavenumber, read only) or "N" (nRf/cNRf: the
+        plane's non-linear transfer, the N.N files). With values, set it."""
+        w = {"R": 0, "Em": 1, "avgK": 2, "N": 3}[which]
         n = self.forcing_shells
         a = np.zeros(n) if values is None else np.ascontiguousarray(values, dtype=np.float64)
         self._check(self._L.ffs_forcing_array(self._h, w, a.ctypes.data_as(_D), n, 0 if values is None else 1))
@@ -317,6 +318,9 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         rf = folder / f"R.{start}"
         if rf.exists():
             sim.forcing_array("R", np.loadtxt(rf).reshape(-1))
+        nf = folder / f"N.{start}"   # nRfForcing / cNRfForcing (forcing_types.jl:114-116)
+        if p.plane_forcing in (4, 5) and nf.exists():
+            sim.forcing_array("N", np.loadtxt(nf).reshape(-1))
     final_step = start + total
     final_time = p.start_time + lengthtime
     kx1, ky1 = 1.0 / p.lx, 1.0 / p.ly

@@ -96,7 +96,8 @@ typedef struct ffs_params {
   double scalar_gradient;      /* scalarGradient: mean gradient d phi / d(direction) */
   int32_t scalar_dir;          /* scalarDirection: 0 x, 1 y, 2 z */
   int32_t plane_forcing;       /* the reference's kz = 0 plane forcing (forcing_types.jl:335-450):
-                                  FFS_PF_RF (rfForcing), FFS_PF_CRF (cRfForcing), FFS_PF_QF (QfForcing) */
+                                  FFS_PF_RF (rfForcing), FFS_PF_CRF (cRfForcing), FFS_PF_QF (QfForcing),
+                                  FFS_PF_NRF (nRfForcing), FFS_PF_CNRF (cNRfForcing), FFS_PF_A (aForcing) */
   double pf_tf;                /* TF */
   double pf_alpha;             /* alphac */
   double pf_kf;                /* kf */
@@ -108,6 +109,9 @@ typedef struct ffs_params {
 #define FFS_PF_RF 1  /* RfForcing functor, src/Forcing_methods/forcing.jl:6-114 */
 #define FFS_PF_CRF 2 /* CRfForcing, src/Forcing_methods/cforcing.jl:1-97 */
 #define FFS_PF_QF 3  /* QfForcing, src/Forcing_methods/qfforcing.jl:1-81 */
+#define FFS_PF_NRF 4 /* NRfForcing, src/Forcing_methods/nrforcing.jl:1-138 */
+#define FFS_PF_CNRF 5 /* CNRfForcing, src/Forcing_methods/cnrforcing.jl:1-126 */
+#define FFS_PF_A 6   /* AForcing (mode by mode; Stats columns hp,vp), src/Forcing_methods/aforcing.jl:1-87 */
 
 #define FFS_LES_SMAGORINSKY 0 /* nu_t = c^2 D^2 |S| (les_real_calc.jl:77-79) */
 #define FFS_LES_VREMAN 1      /* VremanLESModel.jl, les_real_calc.jl:132-139 */
@@ -149,7 +153,9 @@ int ffs_finalize(ffs_handle* h);
  * rfForcing/cRfForcing (the reference's R.N files, forcing_types.jl:70-72,
  * FluidFlowSimulation.jl:60-62); 1 = Em, the target spectrum (from the initial field at
  * ffs_initialize, or set from targSpectrum.dat after it, forcing_types.jl:76-83);
- * 2 = the shells' mean wavenumber avgK (read only). n must equal the shell count. */
+ * 2 = the shells' mean wavenumber avgK (read only); 3 = N, the plane's non-linear transfer
+ * spectrum of nRfForcing/cNRfForcing (the N.N files, forcing_types.jl:114-116). n must
+ * equal the shell count. aForcing keeps its state per mode and has no shells here. */
 int ffs_forcing_shells(const ffs_handle* h);
 int ffs_forcing_array(ffs_handle* h, int32_t which, double* v, int32_t n, int32_t set);
 

@@ -149,6 +149,8 @@ class Params:
     les_model: str = "Smagorinsky"       # Smagorinsky, Vreman, productionViscosity, Silvis, stableNonLinear
     smag_c: float = 0.17                 # the model's constant c
     les_cp: float = 5.0                  # silvisPConstant
+    les_test_width: float = 0.0          # dynamicSmagorinsky: TestFilterWidth (default 2 filterWidth)
+    les_cmin: float = 0.0                # dynamicSmagorinsky: cmin
     sandp_cb: float = 0.0                # SandP: pConstant (0: no P term)
     filter_width: float | None = None
     scalar: bool = False                 # passiveScalar (simulationtypes.jl:198-213, :320-352)
@@ -218,7 +220,7 @@ class Params:
             p.scalar_pr = _num(d["scalarPr"])
             p.scalar_gradient = _num(d["scalarGradient"])
             p.scalar_dir = {"x": 0, "y": 1, "z": 2}[d.get("scalarDirection", "z")]
-        if d.get("forcing") in ("rfForcing", "cRfForcing", "QfForcing"):
+        if d.get("forcing") in PLANE_KINDS:
             p.plane_forcing = d["forcing"]
             p.pf_kf = float(d["kf"])
             if p.plane_forcing == "QfForcing":
@@ -240,6 +242,15 @@ class Params:
         to an eddy-viscosity model (sLesModel)."""
         m = d["lesModel"]
         base = m
+        if m == "dynamicSmagorinsky":                       # les_types.jl:388-392
+            self.les = True
+            self.les_model = m
+            dx = (self.lx * 2 * math.pi / self.nx) / self.cutoff
+            self.filter_width = _num(d["filterWidth"]) if "filterWidth" in d else dx
+            self.les_test_width = (_num(d["TestFilterWidth"]) if "TestFilterWidth" in d
+                                   else 2 * self.filter_width)
+            self.les_cmin = float(d["cmin"]) if "cmin" in d else 0.0
+            return
         if m == "SandP":
             base = d["sLesModel"]
             self.sandp_cb = _num(d.get("pConstant", "0.09"))
@@ -459,12 +470,16 @@ STATS_HEADER = ("iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dis
                 "nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss")
 
 
+PLANE_KINDS = ("rfForcing", "cRfForcing", "nRfForcing", "cNRfForcing", "aForcing", "QfForcing")
+
+
 class PlaneForcing:
     """The reference's forcing of the kz = 0 plane (forcing.jl:6-114 rfForcing,
-    cforcing.jl:1-97 cRfForcing, qfforcing.jl:1-81 QfForcing): horizontal velocity of the
-    kx-ky modes in 2D shells |k_h| <= kf, scaled per shell, plus a few (0, 0, kz) modes
-    that take 1 % of the power; applied after the integrator (add_Rf_forcing!,
-    forcing_types.jl:54-64)."""
+    cforcing.jl:1-97 cRfForcing, nrforcing.jl nRfForcing, cnrforcing.jl cNRfForcing,
+    aforcing.jl aForcing, qfforcing.jl:1-81 QfForcing): horizontal velocity of the kx-ky
+    modes in 2D shells |k_h| <= kf (aForcing: mode by mode), scaled per shell, plus a few
+    (0, 0, kz) modes that take 1 % of the power; applied after the integrator
+    (add_Rf_forcing!, forcing_types.jl:54-64)."""
 
     def __init__(self, p: "Params", g: Grid, lfilter: bool = False):
         self.p, self.g = p, g
@@ -500,6 +515,15 @@ class PlaneForcing:
                         G = math.exp((-d2 / 24) * (self.kh[i] * self.kh[i]))
                         R[i] *= G * G
             self.R = R
+        elif p.plane_forcing == "aForcing":
+            # per-mode state over the kz = 0 plane (aforcing.jl); Zf by calculate_Zf(d,kf,kx,ky)
+            Kz = np.sqrt(g.kx[None, :] ** 2 + (g.ky ** 2)[:, None])
+            if p.pf_zf_tanh:
+                self.Zf2 = np.tanh((kf - Kz) / (0.25 * kf)) * np.where((kf - Kz) <= 0.0, 0.0, 1.0)
+            else:
+                self.Zf2 = (Kz <= kf).astype(np.float64)
+            shape = (g.ny, g.nxh)
+            self.R2, self.Em2, self.factor2 = np.zeros(shape), np.zeros(shape), np.zeros(shape)
         else:
             if p.pf_zf_tanh:   # calculate_Zf (utils.jl:184-198)
                 self.Zf = np.array([math.tanh((kf - k) / (0.25 * kf)) * (0.0 if (kf - k) <= 0.0 else 1.0)
@@ -509,6 +533,8 @@ class PlaneForcing:
             self.R = np.zeros(self.nsh)
             self.Em = np.zeros(self.nsh)
             self.factor = np.zeros(self.nsh)
+            self.N = np.zeros(self.nsh)
+            self.Nm1 = np.zeros(self.nsh)
         # plane modes: shell index n (0-based) of each (ky, kx) with the force loop's
         # K = sqrt(muladd(kx, kx, ky^2))
         K = np.sqrt(dd.fma(*np.broadcast_arrays(g.kx[None, :], g.kx[None, :], (g.ky ** 2)[:, None])))
@@ -516,6 +542,7 @@ class PlaneForcing:
         Ks = np.sqrt(g.kx[None, :] ** 2 + (g.ky ** 2)[:, None])
         self.nspec = np.rint(Ks / self.maxdk).astype(np.int64)
         self.cf = np.where(np.arange(g.nxh) > 0, 2.0, 1.0)[None, :]
+        self.Kmode = K
         self.keep = g.keep[0]
         self.hp = self.vp = 0.0
 
@@ -528,19 +555,40 @@ class PlaneForcing:
         np.add.at(E, self.nspec[ok], v[ok])
         return E
 
-    def initialize(self, u):
-        """initialize!(f::RfForcing, s) (forcing.jl / forcing_types.jl:66-73): the target
-        spectrum of the initial field (no targSpectrum.dat)."""
-        if self.p.plane_forcing != "QfForcing":
-            self.Em = self.plane_spectrum(u, False)
+    def nn_spectrum(self, u, rhs):
+        """calculate_nn_spectrum! (nrforcing.jl / cnrforcing.jl:103-126): per shell,
+        cf (proj(u1, rhs1 - nu k^2 u1) + proj(u2, rhs2 - nu k^2 u2)) on kz = 0."""
+        g, nu = self.g, self.p.nu
+        k2 = g.kx[None, :] ** 2 + (g.ky ** 2)[:, None]
+        u1, u2, r1, r2 = u[0][0], u[1][0], rhs[0][0], rhs[1][0]
+        v = self.cf * (_proj(u1, r1 - (nu * k2) * u1) + _proj(u2, r2 - (nu * k2) * u2))
+        N = np.zeros(self.nsh)
+        ok = self.keep & (self.nspec < self.nsh)
+        np.add.at(N, self.nspec[ok], v[ok])
+        return N
 
-    def __call__(self, u, dt, it, cfl, variable_dt):
+    def initialize(self, u, rhs=None):
+        """initialize! of the forcing (forcing_types.jl:66-73,107-119, aforcing.jl): the
+        target spectrum of the initial field (no targSpectrum.dat); nRf/cNRf also N = Nm1
+        from the initial right-hand side; aForcing its per-mode energies."""
+        kind = self.p.plane_forcing
+        if kind == "aForcing":
+            self.Em2 = 0.5 * self.cf * (np.abs(u[0][0]) ** 2 + np.abs(u[1][0]) ** 2)
+        elif kind != "QfForcing":
+            self.Em = self.plane_spectrum(u, False)
+            if kind in ("nRfForcing", "cNRfForcing"):
+                self.N = self.nn_spectrum(u, rhs)
+                self.Nm1 = self.N.copy()
+
+    def __call__(self, u, dt, it, cfl, variable_dt, rhs=None, dt2=None):
         """The force (fx, fy) for this step and hp, vp."""
         p, g = self.p, self.g
         kf = p.pf_kf
         nz = g.nz
         fx = np.zeros_like(u[0])
         fy = np.zeros_like(u[1])
+        if p.plane_forcing == "aForcing":
+            return self._a_forcing(u, dt, fx, fy)
         sel = self.keep & (self.nmode >= 1) & (self.nmode < self.nsh)
         sel &= np.where(self.nmode < self.nsh, self.kh[np.minimum(self.nmode, self.nsh - 1)] <= kf, False)
         u1, u2 = u[0][0], u[1][0]
@@ -564,19 +612,30 @@ class PlaneForcing:
                 fy[k, 0, 0] = u[1][k, 0, 0] * f
                 vp += _proj(u[0][k, 0, 0], fx[k, 0, 0] / dt) + _proj(u[1][k, 0, 0], fy[k, 0, 0] / dt)
         else:
-            if p.plane_forcing == "rfForcing":
+            kind = p.plane_forcing
+            if kind in ("rfForcing", "nRfForcing"):
                 ts = dt / cfl
                 if variable_dt and it <= 3:
                     ts /= (0.1, 0.2, 0.4, 0.8)[it]
                 omega = 2 * math.pi / (p.pf_tf * ts)
-            else:                                              # cRfForcing: ts = Tf
+            elif kind == "cRfForcing":                         # ts = Tf, omega = 2 pi / ts
                 omega = 2 * math.pi / p.pf_tf
+            else:                                              # cNRfForcing: ts = Tf, omega = 2 pi / (Tf ts)
+                omega = 2 * math.pi / (p.pf_tf * p.pf_tf)
             Ef = self.plane_spectrum(u, False)
             alpha = p.pf_alpha
             eps = np.finfo(np.float64).eps
+            nl = kind in ("nRfForcing", "cNRfForcing")
+            if nl:                                             # nrforcing.jl: copyto!(Nm1, N); N = nn spectrum
+                self.Nm1 = self.N.copy()
+                self.N = self.nn_spectrum(u, rhs)
             for i in range(1, self.nsh):
                 if self.kh[i] <= kf:
-                    self.R[i] += dt * (-2 * alpha * omega * self.R[i] - omega * omega * (Ef[i] - self.Em[i]))
+                    if nl:
+                        self.R[i] += dt * (-2 * alpha * omega * (self.R[i] + self.N[i])
+                                           - (self.N[i] - self.Nm1[i]) / dt2 - omega * omega * (Ef[i] - self.Em[i]))
+                    else:
+                        self.R[i] += dt * (-2 * alpha * omega * self.R[i] - omega * omega * (Ef[i] - self.Em[i]))
                     self.R[i] = max(0.0, self.R[i])
                     self.factor[i] = math.sqrt(self.R[i] / max(Ef[i], eps)) * self.Zf[i] * dt
             fac = self.factor[np.minimum(self.nmode, self.nsh - 1)]
@@ -598,6 +657,43 @@ class PlaneForcing:
         self.hp, self.vp = float(hp), float(vp)
         return fx, fy
 
+    def _vertical(self, u, fx, fy, dt, hp):
+        """(0, 0, kz) modes, kz = +-1..+-5: 1 % of the horizontal power (forcing.jl:86-113)."""
+        nz = self.g.nz
+        vk = list(range(1, 6)) + [nz - k for k in range(1, 6)]
+        umag = sum(math.sqrt(abs(u[0][k, 0, 0]) ** 2 + abs(u[1][k, 0, 0]) ** 2) for k in vk)
+        f = dt * math.sqrt(2.0 * hp * (1.0 - 0.99)) / umag
+        ff = fv = 0.0
+        for k in vk:
+            fx[k, 0, 0] = u[0][k, 0, 0] * f
+            fy[k, 0, 0] = u[1][k, 0, 0] * f
+            ff += abs(fx[k, 0, 0]) ** 2 + abs(fy[k, 0, 0]) ** 2
+            fv += _proj(u[0][k, 0, 0], fx[k, 0, 0]) + _proj(u[1][k, 0, 0], fy[k, 0, 0])
+        return ff * 0.5 / dt + fv / dt
+
+    def _a_forcing(self, u, dt, fx, fy):
+        """aForcing (aforcing.jl): the ODE per kz = 0 mode with 0 < |k_h| <= kf, ts = 10 dt."""
+        p = self.p
+        omega = 2 * math.pi / (p.pf_tf * (10 * dt))
+        alpha, eps = p.pf_alpha, np.finfo(np.float64).eps
+        sel = self.keep & (self.Kmode > 0) & (self.Kmode <= p.pf_kf)
+        u1, u2 = u[0][0], u[1][0]
+        Ef = 0.5 * self.cf * (np.abs(u1) ** 2 + np.abs(u2) ** 2)
+        R = self.R2 + dt * (-2 * alpha * omega * self.R2 - omega * omega * (Ef - self.Em2))
+        R = np.maximum(0.0, R)
+        self.R2 = np.where(sel, R, self.R2)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            fac = np.sqrt(self.R2 / np.maximum(Ef, eps)) * self.Zf2 * dt
+        self.factor2 = np.where(sel, fac, self.factor2)
+        s1 = np.where(sel, u1 * self.factor2, 0.0)
+        s2 = np.where(sel, u2 * self.factor2, 0.0)
+        fx[0], fy[0] = s1, s2
+        ff = np.sum(self.cf * (np.abs(s1) ** 2 + np.abs(s2) ** 2))
+        fv = np.sum(self.cf * (_proj(u1, s1) + _proj(u2, s2)))
+        hp = ff * 0.5 / dt + fv / dt
+        self.hp, self.vp = float(hp), float(self._vertical(u, fx, fy, dt, hp))
+        return fx, fy
+
 
 def stats_header(p: Params) -> str:
     """``statsheader`` (stats.jl:1-7); plug-in order = sim_fields (macros.jl:48)."""
@@ -608,7 +704,9 @@ def stats_header(p: Params) -> str:
         cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux")
     if p.les:
         cols.append("prh,prv,praniso,pr")
-    if p.forcing or p.plane_forcing:
+    if p.plane_forcing == "aForcing":
+        cols.append("hp,vp")                                     # statsheader(a::AForcing)
+    elif p.forcing or p.plane_forcing:
         cols.append("hp,vp,tp")
     if p.hv:
         cols.append("hdissh,hdissv,hdiss")
@@ -834,7 +932,7 @@ class OracleSimulation:
         self.calculate_rhs()
         dt_now = self.get_dt()
         if self.pforce is not None:                               # initialize!(s.forcing, s)
-            self.pforce.initialize(self.u)
+            self.pforce.initialize(self.u, self.rhs)
         self.ts.initialize(self.rhs, dt_now)
         if self.p.fld:
             self.rts.initialize(self.rhorhs, dt_now)
@@ -863,7 +961,10 @@ class OracleSimulation:
             rhor = g.real(self.rho)
         if p.les:
             Sr = g.real(S)
-            taur = les_stress(p, Sr, wr)
+            if p.les_model == "dynamicSmagorinsky":
+                taur = self.dynamic_smagorinsky(u, ur, S, Sr)
+            else:
+                taur = les_stress(p, Sr, wr)
         # realspacecalculation! (models.jl:236-280): rhs = u x w ; flux = -rho u
         nl = np.stack([ur[1] * wr[2] - ur[2] * wr[1], ur[2] * wr[0] - ur[0] * wr[2],
                        ur[0] * wr[1] - ur[1] * wr[0]])
@@ -920,6 +1021,51 @@ class OracleSimulation:
                 rr = rr + (-self.alpha * g.K2) * self.rho
             rr[g.dealias] = 0.0
             self.rhorhs = rr
+
+    def dynamic_smagorinsky(self, u, ur, S, Sr):
+        """The dynamic Smagorinsky model (dynamic_smagorinsky.jl:3-217, les_real_calc.jl:3-11,
+        71-73): test-filtered u and S (fourierspacep1!, models.jl:99-108), Sa = D^2 |S| S and
+        L = u u filtered over the full spectrum (fourierspace_dynamic_les_calculation!), the
+        Germano coefficient c = clamp(L:M / 2 M:M, -1, 1) with L = traceless(u^ u^ - (uu)^)
+        and M = (D^^2 + D^2) |S^| S^ - (D^2 |S| S)^, c averaged by the same filter
+        (average_c!, dynamic_piomelli.jl:13-26), then nu_t = max(cmin, min(0.4, c)) D^2 |S|.
+        The filter is Gaussfilter (utils.jl:220-225): exp(-D^^2 k^2 / 24)."""
+        p, g = self.p, self.g
+        d2 = p.filter_width ** 2
+        dh2 = p.les_test_width ** 2
+        G = np.exp((-dh2 / 24) * g.K2)
+
+        def full_filter(f):            # fullfourier!, multiply by G on every mode, real!
+            c = sfft.rfftn(f, axes=(-3, -2, -1), workers=_WORKERS) * (1.0 / g.N)
+            return g.real(c * G)
+
+        def nrm5(t):
+            xx, xy, xz, yy, yz = t
+            zz = -xx - yy
+            return np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
+
+        uf = g.real(G[None] * u)                                   # u^ (physical)
+        Sh = g.real(G[None] * S)                                   # S^ (physical)
+        Sa = d2 * nrm5(Sr)[None] * Sr                              # D^2 |S| S
+        ux, uy, uz = ur
+        Lr = np.stack([ux * ux, ux * uy, ux * uz, uy * uy, uy * uz, uz * uz])
+        Saf = np.stack([full_filter(x) for x in Sa])
+        Lf = np.stack([full_filter(x) for x in Lr])
+        a, b, c_ = uf
+        L6 = np.stack([a * a, a * b, a * c_, b * b, b * c_, c_ * c_]) - Lf
+        tr = (L6[0] + L6[3] + L6[5]) / 3
+        L6[0] -= tr
+        L6[3] -= tr
+        L6[5] -= tr
+        M5 = (dh2 + d2) * nrm5(Sh)[None] * Sh - Saf
+        mxx, mxy, mxz, myy, myz = M5
+        mzz = -mxx - myy
+        lm = (L6[0] * mxx + L6[3] * myy + L6[5] * mzz + 2.0 * (L6[1] * mxy + L6[2] * mxz + L6[4] * myz))
+        mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
+        cf = np.maximum(-1.0, np.minimum(1.0, 0.5 * (lm / mm)))
+        cf = full_filter(cf)                                       # average_c!
+        nut = np.maximum(p.les_cmin, np.minimum(0.4, cf)) * d2 * nrm5(Sr)
+        return 2.0 * nut[None] * Sr
 
     def div_tau(self, tauh):
         """(i k) . tau for a symmetric traceless tau (models.jl:330)."""
@@ -996,7 +1142,8 @@ class OracleSimulation:
     def plane_force(self):
         """s.forcing(s) of the kz = 0 plane family, from the current u (models.jl:6-9)."""
         p = self.p
-        self.pforce_xy = self.pforce(self.u, self.get_dt(), self.iteration, p.cfl, p.variable_dt)
+        self.pforce_xy = self.pforce(self.u, self.get_dt(), self.iteration, p.cfl, p.variable_dt, self.rhs,
+                                     self.ts.dt2)
         self.hp, self.vp = self.pforce.hp, self.pforce.vp
 
     def advance(self):
@@ -1128,7 +1275,9 @@ class OracleSimulation:
             extra += [prh, prv, (2 * prv) / prh, prh + prv]
             tdiss += prh + prv
             slot = hraw
-        if p.forcing or p.plane_forcing:
+        if p.plane_forcing == "aForcing":
+            extra += [self.hp, self.vp]
+        elif p.forcing or p.plane_forcing:
             extra += [self.hp, self.vp, self.hp + self.vp]
         if p.hv:
             hraw = self._wsum((g.K2 ** p.hv_m) * (a2[0] + a2[1]))

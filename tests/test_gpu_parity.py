@@ -89,6 +89,10 @@ FIXED_CASES = {
     "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
     "ab3-adaptive-qf-forcing-les": gdict(32, adaptive=True, forcing="QfForcing", alveliusP="0.1", alveliusC="1.0",
                                          alveliusKf="2.0", kf="4.0", lesModel="Smagorinsky"),
+    "ab3-adaptive-nrf-forcing": gdict(32, adaptive=True, forcing="nRfForcing", TF="2.0", alphac="1.0", kf="3.0"),
+    "etd-cnrf-forcing-les": gdict(32, "ETD3rdO", forcing="cNRfForcing", TF="0.5", alphac="1.0", kf="3.0",
+                                  lesModel="Smagorinsky"),
+    "ab3-a-forcing-tanh": gdict(32, forcing="aForcing", TF="2.0", alphac="1.0", kf="3.0", Zf="tanh"),
     # passive scalar (simulationtypes.jl:198-213): the density's transport without buoyancy
     "etd-scalar": gdict(32, "ETD3rdO", passiveScalar="true", scalarPr="0.7", scalarGradient="1"),
     "ab3-adaptive-scalar-y": gdict(32, adaptive=True, passiveScalar="true", scalarPr="2", scalarGradient="0.5",
