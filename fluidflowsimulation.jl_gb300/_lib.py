@@ -13,7 +13,8 @@ FFS_OK = 0
 ERRORS = {-1: "FFS_EINVAL", -2: "FFS_ENOMEM", -3: "FFS_ECUDA", -4: "FFS_ENAN", -5: "FFS_ETIMEDOUT",
           -6: "FFS_EUNSUPPORTED", -7: "FFS_ESTATE", -8: "FFS_ECANCELED"}
 FFS_ETD3, FFS_AB3 = 0, 1
-LES_MODELS = {"Smagorinsky": 0, "Vreman": 1, "productionViscosity": 2, "Silvis": 3, "stableNonLinear": 4}
+LES_MODELS = {"Smagorinsky": 0, "Vreman": 1, "productionViscosity": 2, "Silvis": 3, "stableNonLinear": 4,
+              "dynamicSmagorinsky": 5}
 FFS_FP64, FFS_FP32 = 0, 1
 
 # Every symbol include/ffs.h declares (checked by the CPU test suite).
@@ -54,6 +55,7 @@ class FFSParams(ctypes.Structure):
         ("passive_scalar", c_int32), ("scalar_pr", c_double), ("scalar_gradient", c_double), ("scalar_dir", c_int32),
         ("plane_forcing", c_int32), ("pf_tf", c_double), ("pf_alpha", c_double), ("pf_kf", c_double),
         ("pf_zf_tanh", c_int32), ("pf_qp", c_double), ("pf_qc", c_double), ("pf_qkf", c_double),
+        ("les_test_width", c_double), ("les_cmin", c_double),
     ]
 
 

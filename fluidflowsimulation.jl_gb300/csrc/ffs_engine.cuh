@@ -17,6 +17,7 @@
 #include "ffs_xfused.cuh"
 #include "ffs_xles.cuh"
 #include "ffs_batch.cuh"
+#include "ffs_dynamic.cuh"
 
 namespace ffsgpu {
 
@@ -105,6 +106,12 @@ class Engine : public EngineBase {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int n_launch = 0;
+  // dynamic Smagorinsky: full-spectrum slots (x-spectral and z-line layouts), the
+  // averaged coefficient in physical space, shared memory of its kernels
+  DynFull<T> dfull{};
+  cplx<T>* dfz = nullptr;
+  double* dync = nullptr;
+  size_t smem_d0 = 0, smem_d1 = 0, smem_dzf = 0;
 
   ~Engine() override {
     if (gexec) cudaGraphExecDestroy(gexec);
@@ -167,6 +174,11 @@ class Engine : public EngineBase {
     }
     smem_zu = cb * ((size_t)zu_lines() * srows(P.nz) * (I.pz.np >= 3 ? 2 : 1) +
                     (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
+    if (I.dyn) {
+      smem_d0 = DynX<0>::smem(P.nx, cb);
+      smem_d1 = DynX<1>::smem(P.nx, cb);
+      smem_dzf = 2 * (size_t)txy * srows(P.nz) * cb;
+    }
   }
 
   // physics parameters (everything that does not change buffer sizes or the step's passes)
@@ -178,6 +190,12 @@ class Engine : public EngineBase {
     const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
     I.les_alpha = p.smag_c * p.smag_c * fw * fw;
     I.les_model = p.les_model; I.les_c = p.smag_c; I.les_d2 = fw * fw; I.les_cp = p.les_cp; I.les_cb = p.sandp_cb;
+    I.dyn = I.les && p.les_model == FFS_LES_DYNAMIC;
+    {
+      const double tw = p.les_test_width > 0 ? p.les_test_width : 2 * fw;   // les_types.jl:390
+      I.dyn_d2h = I.dyn ? tw * tw : 0.0;
+      I.les_cmin = p.les_cmin;
+    }
     I.density = p.density != 0; I.gdir = p.gravity_dir;
     I.scalar = p.passive_scalar != 0;
     I.alpha = p.density ? p.nu / p.density_pr : 0.0;
@@ -224,7 +242,7 @@ class Engine : public EngineBase {
     if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
     if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
     if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
-    if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_STABLE_NL)) {
+    if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_DYNAMIC)) {
       err = "unknown LES model";
       return FFS_EINVAL;
     }
@@ -308,9 +326,13 @@ class Engine : public EngineBase {
     if (I.les) for (int c = F_SXX; c <= F_SYZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
     if (I.density) { inv_list.code[nin] = F_RHO; inv_list.slot[nin] = nin; ++nin; }
     inv_list.n = nin;
+    // the dynamic model's test-filtered u^, S^: transformed with the others, read by its
+    // own x kernels only (the x pass reads slots 0..nin-1)
+    if (I.dyn)
+      for (int c = F_GUX; c <= F_GSYZ; ++c) { inv_list.code[inv_list.n] = c; inv_list.slot[inv_list.n] = inv_list.n; ++inv_list.n; }
     {
       FieldList fam[3]{};
-      for (int i = 0; i < nin; ++i) {
+      for (int i = 0; i < inv_list.n; ++i) {
         const int c = inv_list.code[i];
         const int f = (c <= F_UZ || c == F_RHO) ? 0 : (c <= F_WZ ? 1 : 2);
         fam[f].code[fam[f].n] = c;
@@ -331,7 +353,7 @@ class Engine : public EngineBase {
     I.nin = nin; I.nout = nout;
     for (int i = 0; i < nout; ++i) { I.out_role[i] = fwd_list.code[i]; I.out_slot[i] = fwd_list.slot[i]; }
     for (int i = 0; i < nin; ++i) I.in_code[i] = inv_list.code[i];
-    const int nslots = std::max(nin, 4);
+    const int nslots = std::max(inv_list.n, 4);
 
     // buffers
     int rc;
@@ -448,6 +470,16 @@ class Engine : public EngineBase {
     }
     // staging for two physical FP64 fields
     if ((rc = alloc(&I.phys, (size_t)2 * p.nx * p.ny * p.nz, err))) return rc;
+    if (I.dyn) {
+      dfull.kxf = ((I.nxh + 7) / 8) * 8;
+      dfull.fys = (long long)p.nz * p.ny * dfull.kxf;
+      dfull.gslot0 = nin;
+      if ((rc = alloc(&dfull.fy, (size_t)DYN_NSLOTS * dfull.fys, err))) return rc;
+      if ((rc = alloc(&dfz, (size_t)DYN_NSLOTS * dfull.fys, err))) return rc;
+      if ((rc = alloc(&dync, (size_t)p.nx * p.ny * p.nz, err))) return rc;
+      FFS_CK(cudaMemsetAsync(dync, 0, sizeof(double) * (size_t)p.nx * p.ny * p.nz, s));
+      I.dyn_c = dync;
+    }
 
     // launch geometry / shared memory
     compute_smem();
@@ -489,7 +521,7 @@ class Engine : public EngineBase {
   int set_smem(std::string& err) {
     int dev = P.device, maxs = 0;
     FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    size_t need[4] = {smem_z, smem_y, smem_x, smem_zu};
+    size_t need[7] = {smem_z, smem_y, smem_x, smem_zu, smem_d0, smem_d1, smem_dzf};
     for (size_t v : need)
       if (v > (size_t)maxs) {
         err = "shared memory per CTA (" + std::to_string(v) + " bytes) exceeds the device limit " + std::to_string(maxs);
@@ -505,6 +537,10 @@ class Engine : public EngineBase {
     if ((rc = smem_attr(k_fwd_y<T, TX / 2>, smem_y, err))) return rc;
     if ((rc = smem_attr(k_fwd_z_store<T, TX / 2>, smem_z, err))) return rc;
     if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
+    if (I.dyn && ((rc = smem_attr(k_dyn_x<T, 0>, smem_d0, err)) || (rc = smem_attr(k_dyn_x<T, 1>, smem_d1, err)) ||
+                  (rc = smem_attr(k_dyn_zfilter<T, TX>, smem_dzf, err)) ||
+                  (rc = smem_attr(k_dyn_zfilter<T, TX / 2>, smem_dzf, err))))
+      return rc;
     if constexpr (sizeof(T) == 4) {
       if ((rc = ct_attrs<128>(err)) || (rc = ct_attrs<256>(err)) || (rc = ct_attrs<512>(err)) ||
           (rc = ct_attrs<1024>(err)))
@@ -634,7 +670,7 @@ class Engine : public EngineBase {
 
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      if (v_iz == 1)
+      if (v_iz == 1 && !I.dyn)
         FFS_CT_SWITCH(ctz(), (k_inv_z2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.NYR), PAIR_LP * ct_tpl<NC>(),
                                                      pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
       FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
@@ -755,9 +791,49 @@ class Engine : public EngineBase {
       launch_inv_z(inv_list);
     }
   }
+  // the full-spectrum instance of the dynamic model's filter passes: every kx, ky, kz kept
+  Inst<T> full_inst() const {
+    Inst<T> J = I;
+    J.Mx = I.nxh; J.KXP = dfull.kxf;
+    J.NYR = P.ny; J.ypos = P.ny / 2; J.NZR = P.nz; J.zpos = P.nz / 2;
+    J.wy = dfull.fy; J.wz = dfz; J.wys = J.wzs = dfull.fys;
+    return J;
+  }
+  // forward y, the z test filter, inverse y on nf full slots from slot0
+  void launch_dyn_filter(const Inst<T>& J, int slot0, int nf) {
+    FieldList F{};
+    F.n = nf;
+    for (int i = 0; i < nf; ++i) { F.code[i] = -1; F.slot[i] = slot0 + i; }
+    const int t = txy;
+    if (t == TX) {
+      k_fwd_y<T, TX><<<dim3(nf, J.KXP / TX, P.nz), blk(TX, I.py), smem_y, s>>>(J, F);
+      k_dyn_zfilter<T, TX><<<dim3(nf, J.KXP / TX, P.ny), blk(TX, I.pz), smem_dzf, s>>>(J, slot0);
+      k_inv_y<T, TX><<<dim3(nf, J.KXP / TX, P.nz), blk(TX, I.py), smem_y, s>>>(J, F);
+    } else {
+      k_fwd_y<T, TX / 2><<<dim3(nf, J.KXP / (TX / 2), P.nz), blk(TX / 2, I.py), smem_y, s>>>(J, F);
+      k_dyn_zfilter<T, TX / 2><<<dim3(nf, J.KXP / (TX / 2), P.ny), blk(TX / 2, I.pz), smem_dzf, s>>>(J, slot0);
+      k_inv_y<T, TX / 2><<<dim3(nf, J.KXP / (TX / 2), P.nz), blk(TX / 2, I.py), smem_y, s>>>(J, F);
+    }
+  }
+  // the dynamic coefficient of this step (realspace_LES_calculation!, les_real_calc.jl:3-11)
+  void launch_dynamic() {
+    const Inst<T> J = full_inst();
+    const unsigned lines = (unsigned)((long long)P.ny * P.nz);
+    k_dyn_x<T, 0><<<lines, 256, smem_d0, s>>>(I, dfull);
+    launch_dyn_filter(J, 0, DYN_NSA);
+    k_dyn_x<T, 1><<<lines, 256, smem_d1, s>>>(I, dfull);
+    launch_dyn_filter(J, DYN_SLOT_C, 1);
+    Inst<T> C = J;   // physical c from the x-spectral full slot
+    C.wy = dfull.fy + (long long)DYN_SLOT_C * dfull.fys;
+    C.phys = dync;
+    if (lio == 4) inv_x_phys<4>(C, 1);
+    else if (lio == 2) inv_x_phys<2>(C, 1);
+    else inv_x_phys<1>(C, 1);
+  }
   void enqueue_step(int mode) {
     launch_inv_z_step();
     launch_inv_y(inv_list);
+    if (I.dyn) launch_dynamic();
     launch_x();
     // dt, the integrator's scalars, the band energy and the ETD table need only the x
     // pass (max |u|) and the spectral state: a side branch that overlaps the forward y
@@ -779,7 +855,8 @@ class Engine : public EngineBase {
     launch_fin(mode);
   }
   int launches_per_step() const override {
-    return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0) + ((split_iz && n_fam > 1) ? n_fam - 1 : 0);
+    return 9 + (use_table() ? 1 : 0) + (I.pforce ? 1 : 0) + ((split_iz && n_fam > 1) ? n_fam - 1 : 0) +
+           (I.dyn ? 9 : 0);
   }
   // nRf / cNRf use the plane's non-linear transfer, so they wait for the forward passes
   bool pf_after_fwd() const { return I.pforce == FFS_PF_NRF || I.pforce == FFS_PF_CNRF; }
@@ -1235,7 +1312,8 @@ class Engine : public EngineBase {
 
   int autotune(std::string& err) {
     const std::string key = std::to_string(sizeof(T)) + ":" + std::to_string(P.nx) + "x" + std::to_string(P.ny) + "x" +
-                            std::to_string(P.nz) + ":" + std::to_string(I.les) + std::to_string(I.density) + ":" +
+                            std::to_string(P.nz) + ":" + std::to_string(I.les) + std::to_string(I.density) +
+                            std::to_string(I.dyn) + ":" +
                             std::to_string(I.Mx) + "," + std::to_string(I.NYR) + "," + std::to_string(I.NZR) + ":" +
                             std::to_string(P.kernel_variant);
     {
@@ -1314,7 +1392,7 @@ class Engine : public EngineBase {
         v = bv;
         return 0;
       };
-      if (!rc) rc = pick(v_iz, "z_inv", ctz(), [&] { launch_inv_z(inv_list); });
+      if (!rc) rc = pick(v_iz, "z_inv", I.dyn ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
       // one launch for every field family, or one per family
       if (!rc && n_fam > 1) {
         float bms = 1e30f;

@@ -13,7 +13,11 @@ enum FieldCode : int {
   F_UX = 0, F_UY, F_UZ,          // velocity
   F_WX, F_WY, F_WZ,              // vorticity  i k x u
   F_SXX, F_SXY, F_SXZ, F_SYY, F_SYZ,   // strain sym(i k (x) u), traceless, 5 comps
-  F_RHO                          // density perturbation
+  F_RHO,                         // density perturbation
+  // dynamic Smagorinsky: the test-filtered velocity G u and strain G S (fourierspacep1!,
+  // models.jl:99-103), G = exp(-D^2 k^2 / 24) with the test filter width D
+  F_GUX, F_GUY, F_GUZ,
+  F_GSXX, F_GSXY, F_GSXZ, F_GSYY, F_GSYZ
 };
 
 // Forward-field roles consumed by the forward z pass.
@@ -122,6 +126,10 @@ template <typename T> struct Inst {
   double les_c, les_d2;    // the model's constant c and Delta^2
   double les_cp;           // Silvis P constant
   double les_cb;           // SandP: cb (0: no P term)
+  int dyn;                 // dynamic Smagorinsky (FFS_LES_DYNAMIC)
+  double dyn_d2h;          //   test filter width^2
+  double les_cmin;         //   smallest coefficient kept (cmin)
+  const double* dyn_c;     //   averaged coefficient in physical space [z][y][x]
   int density, gdir;      // density: a fourth field (density, or with scalar the passive scalar)
   int scalar;              // the fourth field is a passive scalar: no buoyancy, no CFL cap, own stats
   double alpha, dgrad, gval;

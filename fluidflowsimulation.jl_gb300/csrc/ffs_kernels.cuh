@@ -22,8 +22,8 @@ constexpr int LYZ_IO = 4;  // (y,z) lines per CTA in the transform-only x kernel
 
 struct FieldList {
   int n;
-  int code[12];   // FieldCode (inverse z) or role (forward passes)
-  int slot[12];   // work-array slot
+  int code[20];   // FieldCode (inverse z) or role (forward passes)
+  int slot[20];   // work-array slot
 };
 
 // Block coordinates of one unit of work: the launch's own (single simulation) or an
@@ -115,9 +115,16 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
   const T Lx = I.Lx_t, iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
   // The field's prologue is one of three forms, fixed per CTA (so each form gets its own
   // FFT with a branch-free loader): a copy of a component, a curl component
-  // i (k_b u_c - k_c u_b), or a strain component (i/2)(k_a u_b + k_b u_a).
+  // i (k_b u_c - k_c u_b), or a strain component (i/2)(k_a u_b + k_b u_a); the dynamic
+  // model adds the copy and the strain times the test filter G (families 3 and 4).
   int fam, ca = 0, cb = 0;
   switch (code) {
+    case F_GUX: case F_GUY: case F_GUZ: fam = 3; ca = code - F_GUX; break;
+    case F_GSXX: fam = 4; ca = 0; cb = 0; break;
+    case F_GSXY: fam = 4; ca = 0; cb = 1; break;
+    case F_GSXZ: fam = 4; ca = 0; cb = 2; break;
+    case F_GSYY: fam = 4; ca = 1; cb = 1; break;
+    case F_GSYZ: fam = 4; ca = 1; cb = 2; break;
     case F_UX: fam = 0; ca = 0; break;
     case F_UY: fam = 0; ca = 1; break;
     case F_UZ: fam = 0; ca = 2; break;
@@ -155,7 +162,7 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
       return mk(-(kb * uc.y - kc_ * ub.y), kb * uc.x - kc_ * ub.x);
     };
     fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
-  } else {
+  } else if (fam == 2) {
     auto ld = [&](int l, int z) -> cplx<T> {   // (i/2)(k_a u_b + k_b u_a), (a, b) = (ca, cb)
       const int kc = zcomp(I, z);
       if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
@@ -166,6 +173,33 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
       return mk(-T(0.5) * q.y, T(0.5) * q.x);
     };
     fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  } else {
+    // Gaussfilter (utils.jl:220-225): exp(-D^2 k.k / 24), k.k = kx kx + (ky ky + kz kz)
+    const T aux = T(-I.dyn_d2h / 24.0);
+    auto gk = [&](int l, int kc) -> T {
+      const T kx = kax(0, l, kc), kz = kax(2, l, kc);
+      return exp(aux * (kx * kx + (kyv * kyv + kz * kz)));
+    };
+    if (fam == 3) {
+      auto ld = [&](int l, int z) -> cplx<T> {
+        const int kc = zcomp(I, z);
+        if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+        return scl(uh[oa + (long long)kc * rowstride + l], gk(l, kc));
+      };
+      fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+    } else {
+      auto ld = [&](int l, int z) -> cplx<T> {   // G (i/2)(k_a u_b + k_b u_a)
+        const int kc = zcomp(I, z);
+        if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+        const long long o = (long long)kc * rowstride + l;
+        const cplx<T> ua = uh[oa + o], ub = uh[ob + o];
+        const T ka = kax(ca, l, kc), kb = kax(cb, l, kc);
+        const cplx<T> q = mk(ka * ub.x + kb * ua.x, ka * ub.y + kb * ua.y);
+        const T g = gk(l, kc);
+        return mk(g * (-T(0.5) * q.y), g * (T(0.5) * q.x));
+      };
+      fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+    }
   }
 }
 // with a compile-time plan the CTA has exactly TX * ct_tpl threads; the register cap
@@ -462,6 +496,15 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         const T zz = -xx - yy;
         const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
         const T two_nut = les2 * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
+        o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
+      } else if (I.dyn) {
+        // dynamic Smagorinsky (les_real_calc.jl:71-73): nu_t = max(cmin, min(0.4, c)) D^2 |S|,
+        // c the averaged coefficient at this point (NaN kept, as Julia's min/max do)
+        const T zz = -xx - yy;
+        const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
+        T cc = T(I.dyn_c[(long long)(g0 + q) * n + j]);
+        if (!isnan(cc)) cc = fmax(T(I.les_cmin), fmin(T(0.4), cc));
+        const T two_nut = T(2) * (cc * T(I.les_d2) * nrm);
         o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
       } else {
         les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4);

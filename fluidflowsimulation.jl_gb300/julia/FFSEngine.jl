@@ -37,6 +37,7 @@ mutable struct FFSParams
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
+    les_test_width::Float64; les_cmin::Float64
     FFSParams() = new()
 end
 
@@ -86,7 +87,12 @@ function parameters(d)
         p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
         p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
     end
-    if haskey(d, :lesModel)   # pointwise models of les_types (les_types.jl:360-395)
+    if haskey(d, :lesModel) && d[:lesModel] == "dynamicSmagorinsky"   # les_types.jl:388-392
+        p.les = 1; p.les_model = 5
+        p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) : 0.0
+        p.les_test_width = haskey(d, :TestFilterWidth) ? num(d[:TestFilterWidth]) : 0.0
+        p.les_cmin = haskey(d, :cmin) ? parse(Float64, d[:cmin]) : 0.0
+    elseif haskey(d, :lesModel)   # pointwise models of les_types (les_types.jl:360-395)
         m = d[:lesModel]; base = m == "SandP" ? d[:sLesModel] : m
         consts = Dict("Smagorinsky" => (:smagorinskyConstant, 0.17), "Vreman" => (:vremanConstant, 0.032),
                       "productionViscosity" => (:productionConstant, m == "SandP" ? 0.1 : 0.4),

@@ -86,7 +86,8 @@ typedef struct ffs_params {
   int32_t autotune;            /* 1: time the candidate launch shapes at create, keep the fastest */
   int32_t les_model;           /* with les != 0, the eddy-viscosity model of lesModel (les_types.jl:360-395):
                                   FFS_LES_SMAGORINSKY, FFS_LES_VREMAN, FFS_LES_PRODUCTION, FFS_LES_SILVIS,
-                                  FFS_LES_STABLE_NL; smag_c holds that model's constant */
+                                  FFS_LES_STABLE_NL, FFS_LES_DYNAMIC; smag_c holds the constant of the
+                                  pointwise models */
   double les_cp;               /* silvisPConstant (Silvis model) */
   double sandp_cb;             /* lesModel SandP: pConstant of the P tensor term (0: none) */
   int32_t passive_scalar;      /* passiveScalar (simulationtypes.jl:198-213, :320-352): a scalar phi
@@ -103,6 +104,8 @@ typedef struct ffs_params {
   double pf_kf;                /* kf */
   int32_t pf_zf_tanh;          /* Zf tanh (default: cutoff) */
   double pf_qp, pf_qc, pf_qkf; /* alveliusP, alveliusC, alveliusKf (QfForcing) */
+  double les_test_width;       /* dynamicSmagorinsky: TestFilterWidth (<= 0: twice the filter width) */
+  double les_cmin;             /* dynamicSmagorinsky: cmin, the smallest coefficient kept */
 } ffs_params;
 
 #define FFS_PF_NONE 0
@@ -118,6 +121,9 @@ typedef struct ffs_params {
 #define FFS_LES_PRODUCTION 2  /* ProductionViscosityLESModel.jl */
 #define FFS_LES_SILVIS 3      /* silvismodel.jl */
 #define FFS_LES_STABLE_NL 4   /* stablenonlinearmodel.jl */
+#define FFS_LES_DYNAMIC 5     /* dynamic Smagorinsky: Germano coefficient from a Gaussian test filter,
+                                 averaged by the same filter (dynamic_smagorinsky.jl, dynamic_piomelli.jl
+                                 :13-26, les_real_calc.jl:71-73); grids with nx <= 512 in FP64 */
 
 /* Fill defaults: reference defaults for every key that has one. */
 int ffs_params_default(ffs_params* p);

@@ -84,6 +84,13 @@ FIXED_CASES = {
     "etd-silvis": gdict(32, "ETD3rdO", lesModel="Silvis"),
     "ab3-stable-nonlinear": gdict(32, lesModel="stableNonLinear", nlConstant="0.05"),
     "etd-sandp-smagorinsky": gdict(32, "ETD3rdO", lesModel="SandP", sLesModel="Smagorinsky"),
+    # the dynamic Smagorinsky model (dynamic_smagorinsky.jl): full-spectrum test filter of
+    # Sa and L, Germano coefficient, filtered again; radix-2, radix-3 and non-cubic grids
+    "etd-dynamic-smagorinsky": gdict(32, "ETD3rdO", lesModel="dynamicSmagorinsky"),
+    "ab3-dynamic-48-cmin-density": gdict(48, lesModel="dynamicSmagorinsky", TestFilterWidth="0.4", cmin="-0.05",
+                                         densityStratification="true", Pr="1", densityGradient="1",
+                                         zAcceleration="1", referenceDensity="1"),
+    "etd-dynamic-noncubic": gdict(32, "ETD3rdO", ny=48, nz=64, lesModel="dynamicSmagorinsky", filterWidth="0.3"),
     # the reference's kz = 0 plane forcing family (forcing_types.jl:335-450)
     "ab3-adaptive-rf-forcing": gdict(32, adaptive=True, forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
     "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
@@ -141,7 +148,7 @@ def test_etd_adaptive_parity(gpu_pkg):
 
 
 @pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
-                                  "ab3-stable-nonlinear"])
+                                  "ab3-stable-nonlinear", "etd-dynamic-smagorinsky"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)

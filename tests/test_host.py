@@ -129,11 +129,16 @@ def test_parameters_requires_dtspec(pkg):
 def test_parameters_rejects_out_of_scope_models(pkg):
     d = {"nx": "8", "ny": "8", "nz": "8", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
          "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1",
-         "lesModel": "dynamicSmagorinsky"}
+         "lesModel": "piomelliSmagorinsky"}
     with pytest.raises(ValueError):
         pkg.parameters(d)
+    for m in ("dynamicSandP", "piomelliSandP"):
+        with pytest.raises(ValueError):
+            pkg.parameters(dict(d, lesModel=m, sLesModel="dynamicSmagorinsky"))
     with pytest.raises(ValueError):
         pkg.parameters(dict(d, lesModel="SandP", sLesModel="Silvis"))
+    with pytest.raises(ValueError):
+        pkg.parameters(dict(d, lesModel="SandP", sLesModel="dynamicSmagorinsky"))
 
 
 def test_parameters_les_models(pkg):
@@ -164,6 +169,17 @@ def test_parameters_les_models(pkg):
         o = Params.from_global(d)
         assert o.les and o.smag_c == pytest.approx(c) and o.sandp_cb == cb
         assert o.filter_width == pytest.approx(fw if fw else dx)
+    # dynamicSmagorinsky (les_types.jl:388-392): test filter twice the filter width unless
+    # TestFilterWidth is given, cmin default 0
+    p = pkg.parameters(dict(base, lesModel="dynamicSmagorinsky"))
+    assert (p.les, p.les_model, p.filter_width, p.les_test_width, p.les_cmin) == (1, 5, 0.0, 0.0, 0.0)
+    o = Params.from_global(dict(base, lesModel="dynamicSmagorinsky"))
+    assert (o.les_model, o.les_cmin) == ("dynamicSmagorinsky", 0.0)
+    assert o.filter_width == pytest.approx(dx) and o.les_test_width == pytest.approx(2 * dx)
+    d = dict(base, lesModel="dynamicSmagorinsky", filterWidth="0.2", TestFilterWidth="0.5", cmin="-0.1")
+    p, o = pkg.parameters(d), Params.from_global(d)
+    assert (p.filter_width, p.les_test_width, p.les_cmin) == (0.2, 0.5, -0.1)
+    assert (o.filter_width, o.les_test_width, o.les_cmin) == (0.2, 0.5, -0.1)
 
 
 def test_parse_number(pkg):
