@@ -203,6 +203,11 @@ class Engine : public EngineBase {
     I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
     I.pforce = p.plane_forcing; I.pf_kf = p.pf_kf; I.pf_tf = p.pf_tf; I.pf_alpha = p.pf_alpha; I.pf_cfl = p.cfl;
     I.dt_stat = p.dt_stat; I.dt_spec = p.dt_spec;
+    {   // SPEC_FIL_D2 = (2 pi LX nf / NRX)^2 (Globals.jl:173-178)
+      const double d = 2 * M_PI * p.lx * p.spec_fil / p.nx;
+      I.fil_d2 = d * d;
+      I.sfil = I.fil_d2 != 0.0;
+    }
     I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
     I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
     I.inv_n_t = (T)I.inv_n; I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
@@ -441,7 +446,9 @@ class Engine : public EngineBase {
     ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) +
                   (I.pforce == FFS_PF_A ? 2 : ((I.forcing || I.pforce) ? 3 : 0)) + (I.hv ? 3 : 0);
     if (I.pforce && (rc = plane_forcing_tables(p, err))) return rc;
-    ncols_rec = ncols_stats + 13;
+    // a record: the Stats.txt row, 13 Scales.txt inputs, then with specFil the
+    // Stats_fil.txt row without iteration and time
+    ncols_rec = ncols_stats + 13 + (I.sfil ? ncols_stats - 2 : 0);
     I.ncols = ncols_rec;
     I.rec_cap = p.stats_capacity > 0 ? p.stats_capacity : 256;
     if ((rc = alloc(&I.records, (size_t)I.rec_cap * I.ncols, err))) return rc;
@@ -458,6 +465,12 @@ class Engine : public EngineBase {
     if (I.les) spec_names += ",les_h,les_v";
     if (I.hv) spec_names += ",hvis_h,hvis_v";
     if (I.density && !I.scalar) spec_names += ",buoyancy_v,rho,rhodiss,rhonl";
+    if (I.sfil) {   // write_spec's *_fil spectra (spec.jl:17-40, 81-123, 140-143)
+      I.nspecf += 8 + (I.hv ? 2 : 0) + ((I.density && !I.scalar) ? 4 : 0);
+      spec_names += ",u_fil_h,u_fil_v,vis_fil_h,vis_fil_v,nl_fil_h,nl_fil_v,press_fil_h,press_fil_v";
+      if (I.hv) spec_names += ",hvis_fil_h,hvis_fil_v";
+      if (I.density && !I.scalar) spec_names += ",buoyancy_fil_v,rho_fil,rhodiss_fil,rhonl_fil";
+    }
     nspecf = I.nspecf;
     if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 2 * I.nspecf * std::max(lenH, lenV), err))) return rc;
     // ETD tables
@@ -629,6 +642,7 @@ class Engine : public EngineBase {
     h.time = P.start_time;
     h.dt = h.dt2 = h.dt3 = P.dt;
     h.nl_h = h.nl_v = h.press_h = h.press_v = 1.0;   // simulationtypes.jl:94-95
+    h.nl_hf = h.nl_vf = h.press_hf = h.press_vf = 1.0;
     FFS_CK(cudaMemcpyAsync(I.st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
     FFS_CK(cudaStreamSynchronize(s));
     iteration = h.iteration; time = h.time; dt = h.dt;

@@ -28,7 +28,7 @@ enum FwdRole : int { R_NX = 0, R_NY, R_NZ, R_KE, R_TXX, R_TXY, R_TXZ, R_TYY, R_T
 enum SpecField : int {
   SF_U_H = 0, SF_U_V, SF_VIS_H, SF_VIS_V, SF_NL_H, SF_NL_V, SF_PRESS_H, SF_PRESS_V, SF_BASE_COUNT
 };
-constexpr int SPEC_MAX_FIELDS = 16;
+constexpr int SPEC_MAX_FIELDS = 32;
 
 // Stats partial-sum quantities (per CTA of the forward z pass).
 enum StatQ : int {
@@ -36,9 +36,13 @@ enum StatQ : int {
   Q_D1DY, Q_D1DX, Q_D2DY, Q_D2DX, Q_LESH, Q_LESV, Q_HVH, Q_HVV,
   Q_RHO, Q_RHO2, Q_DR1, Q_DR2, Q_DR3, Q_BF, Q_HP, Q_VP,
   Q_IL0,  // 9 integral-length plane sums: [component][plane x,y,z]
-  Q_COUNT = Q_IL0 + 9
+  // the same sums weighted by the squared Gaussian filter (Stats_fil.txt); Q_FDR1 keeps
+  // only the last retained kx of each line, as the reference's filtered dx_squared_mean
+  Q_FU12 = Q_IL0 + 9, Q_FU22, Q_FU32, Q_FEH, Q_FEV, Q_FNLH, Q_FNLV, Q_FLESH, Q_FLESV, Q_FHVH, Q_FHVV,
+  Q_FRHO2, Q_FDR1, Q_FDR2, Q_FDR3, Q_FBF,
+  Q_COUNT
 };
-constexpr int QPAD = 40;
+constexpr int QPAD = 56;
 constexpr int FFS_PF_MAXSH = 520;   // 2D shells of the kz = 0 plane forcing: min(nx/2+1, ny/2) <= 513
 
 // Device-resident scalar state (one per simulation).
@@ -58,6 +62,7 @@ struct DevState {
   double Ef;
   double pf_hp, pf_vp;     // kz = 0 plane forcing: horizontal and vertical power of the last call
   double nl_h, nl_v, press_h, press_v;  // last non-linear / pressure stats
+  double nl_hf, nl_vf, press_hf, press_vf;  // their filtered twins (Stats_fil.txt)
   long long nrec;          // stats records written
   long long nspec;         // spectrum records written
   unsigned int err;        // bit 0: non-finite value in the update
@@ -129,6 +134,8 @@ template <typename T> struct Inst {
   int dyn;                 // dynamic Smagorinsky (FFS_LES_DYNAMIC)
   double dyn_d2h;          //   test filter width^2
   double les_cmin;         //   smallest coefficient kept (cmin)
+  int sfil;                // filtered stats and spectra (specFil)
+  double fil_d2;           //   filter width^2 (SPEC_FIL_D2)
   const double* dyn_c;     //   averaged coefficient in physical space [z][y][x]
   int density, gdir;      // density: a fourth field (density, or with scalar the passive scalar)
   int scalar;              // the fourth field is a passive scalar: no buoyancy, no CFL cap, own stats

@@ -1331,10 +1331,17 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       spec_bin(I, sp + (2 * SF_U_V) * stride, stride, vv, ix, nx, nj, nk);
     }
     if (!stats_t) continue;
+    // STAT_FIL weight Gaussfilter(SPEC_FIL_D2, k.k)^2 (utils.jl:220-225)
+    T G2 = T(0);
+    if (I.sfil) { const T G = exp(T(-I.fil_d2 / 24.0) * k2); G2 = G * G; }
     // velocity moments (velocity_stats, viscosity_stats, d*_squared_mean)
     if (k0) { q[Q_U1] += u[0].x; q[Q_U2] += u[1].x; q[Q_U3] += u[2].x; }
     q[Q_U12] += w * a2[0]; q[Q_U22] += w * a2[1]; q[Q_U32] += w * a2[2];
     q[Q_EH] += w * k2 * (a2[0] + a2[1]); q[Q_EV] += w * k2 * a2[2];
+    if (I.sfil) {
+      q[Q_FU12] += w * a2[0] * G2; q[Q_FU22] += w * a2[1] * G2; q[Q_FU32] += w * a2[2] * G2;
+      q[Q_FEH] += w * k2 * (a2[0] + a2[1]) * G2; q[Q_FEV] += w * k2 * a2[2] * G2;
+    }
     q[Q_D1DY] += w * ky * ky * a2[0]; q[Q_D1DX] += w * kx * kx * a2[0];
     q[Q_D2DY] += w * ky * ky * a2[1]; q[Q_D2DX] += w * kx * kx * a2[1];
     // non-linear transfer: (N - i k ke) . u (stats.jl:897-917)
@@ -1347,8 +1354,12 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       rx[c] = Nc.x + kk[c] * ke.y;
       ry[c] = Nc.y - kk[c] * ke.x;
     }
-    q[Q_NLH] += w * (rx[0] * u[0].x + ry[0] * u[0].y + rx[1] * u[1].x + ry[1] * u[1].y);
-    q[Q_NLV] += w * (rx[2] * u[2].x + ry[2] * u[2].y);
+    {
+      const T lh = w * (rx[0] * u[0].x + ry[0] * u[0].y + rx[1] * u[1].x + ry[1] * u[1].y);
+      const T lv = w * (rx[2] * u[2].x + ry[2] * u[2].y);
+      q[Q_NLH] += lh; q[Q_NLV] += lv;
+      if (I.sfil) { q[Q_FNLH] += lh * G2; q[Q_FNLV] += lv * G2; }
+    }
     // pressure transfer (stats.jl:764-814): rhs - i k ke (+ i k.tau + rho g), projected part
     if (I.les) {
 #pragma unroll
@@ -1357,6 +1368,7 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
         rx[c] += dT.x; ry[c] += dT.y;
         const T pr = dT.x * u[c].x + dT.y * u[c].y;
         if (c < 2) q[Q_LESH] += w * pr; else q[Q_LESV] += w * pr;
+        if (I.sfil) { if (c < 2) q[Q_FLESH] += w * pr * G2; else q[Q_FLESV] += w * pr * G2; }
       }
     }
     cplx<T> rho = mk(T(0), T(0));
@@ -1368,13 +1380,19 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
     const T kdy = kx * ry[0] + ky * ry[1] + kz * ry[2];
     const T inv = k0 ? T(0) : T(1) / k2;
     const T p1x = -kdx * inv, p1y = -kdy * inv;
-    q[Q_PH] += w * (u[0].x * p1x * kx + u[0].y * p1y * kx + u[1].x * p1x * ky + u[1].y * p1y * ky);
-    q[Q_PV] += w * (u[2].x * p1x * kz + u[2].y * p1y * kz);
+    {
+      const T lh = w * (u[0].x * p1x * kx + u[0].y * p1y * kx + u[1].x * p1x * ky + u[1].y * p1y * ky);
+      const T lv = w * (u[2].x * p1x * kz + u[2].y * p1y * kz);
+      q[Q_PH] += lh; q[Q_PV] += lv;
+      // STAT_FIL (stats.jl:880-885): the filtered terms land in the unfiltered sums
+      if (I.sfil) { q[Q_PH] += lh * G2; q[Q_PV] += lv * G2; }
+    }
     if (I.hv) {
       T km = T(1);
       for (int i = 0; i < I.hv_m; ++i) km *= k2;
       q[Q_HVH] += w * km * (a2[0] + a2[1]);
       q[Q_HVV] += w * km * a2[2];
+      if (I.sfil) { q[Q_FHVH] += w * km * (a2[0] + a2[1]) * G2; q[Q_FHVV] += w * km * a2[2] * G2; }
     }
     if (I.forcing && mode != 1 && k2 > T(0) && k2 <= kf2) {
       q[Q_HP] += w * (fdt * (a2[0] + a2[1]) + T(0.5) * fdt * fdt * (a2[0] + a2[1]));
@@ -1386,6 +1404,12 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       q[Q_RHO2] += w * r2;
       q[Q_DR1] += w * kx * kx * r2; q[Q_DR2] += w * ky * ky * r2; q[Q_DR3] += w * kz * kz * r2;
       q[Q_BF] += w * (u[I.gdir].x * rho.x + u[I.gdir].y * rho.y);
+      if (I.sfil) {
+        q[Q_FRHO2] += w * r2 * G2;
+        if (ix == I.Mx - 1) q[Q_FDR1] += w * kx * kx * r2 * G2;   // stats.jl:370 (ee_fil = ...)
+        q[Q_FDR2] += w * ky * ky * r2 * G2; q[Q_FDR3] += w * kz * kz * r2 * G2;
+        q[Q_FBF] += w * (u[I.gdir].x * rho.x + u[I.gdir].y * rho.y) * G2;
+      }
     }
     // integral-length plane sums (stats.jl:952-980)
 #pragma unroll
@@ -1454,6 +1478,18 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
     // spectrum_viscosity of spectrum_u
     bin(SF_VIS_H, 2.0 * nu * k2 * (0.5 * (a2[0] + a2[1])));
     bin(SF_VIS_V, 2.0 * nu * k2 * (0.5 * a2[2]));
+    // filter_spectrum! (spec.jl:452-472): the *_fil spectra after the unfiltered fields
+    double G2 = 0.0;
+    int ff = I.nspecf;
+    if (I.sfil) {
+      const double G = exp(-I.fil_d2 / 24.0 * k2);
+      G2 = G * G;
+      ff = I.nspecf - 8 - (I.hv ? 2 : 0) - ((I.density && !I.scalar) ? 4 : 0);
+      bin(ff, G2 * (0.5 * (a2[0] + a2[1])));                  // u_fil_h, u_fil_v
+      bin(ff + 1, G2 * (0.5 * a2[2]));
+      bin(ff + 2, 2.0 * nu * k2 * (G2 * (0.5 * (a2[0] + a2[1]))));   // vis_fil of u_fil
+      bin(ff + 3, 2.0 * nu * k2 * (G2 * (0.5 * a2[2])));
+    }
     // spectrum_non_linear: proj(N - i k ke, u)
     const cplx<T> ke = sb[3 * cs + g];
     const T kk[3] = {kx, ky, kz};
@@ -1467,6 +1503,7 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
     }
     bin(SF_NL_H, nl[0] + nl[1]);
     bin(SF_NL_V, nl[2]);
+    if (I.sfil) { bin(ff + 4, G2 * (nl[0] + nl[1])); bin(ff + 5, G2 * nl[2]); }
     int f = SF_BASE_COUNT;
     double les[3] = {0, 0, 0};
     if (I.les) {
@@ -1491,6 +1528,7 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
       for (int c = 0; c < 3; ++c) pr[c] = (double)u[c].x * (px * kk[c]) + (double)u[c].y * (py * kk[c]);
       bin(SF_PRESS_H, pr[0] + pr[1]);
       bin(SF_PRESS_V, pr[2]);
+      if (I.sfil) { bin(ff + 6, G2 * (pr[0] + pr[1])); bin(ff + 7, G2 * pr[2]); }
     }
     if (I.les) { bin(f, les[0] + les[1]); bin(f + 1, les[2]); f += 2; }
     if (I.hv) {   // spectrum_hyperviscosity: nuh (k^2)^M proj(u, u)
@@ -1498,6 +1536,7 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
       for (int i = 1; i < I.hv_m; ++i) km *= k2;
       bin(f, nuh * km * (a2[0] + a2[1]));
       bin(f + 1, nuh * km * a2[2]);
+      if (I.sfil) { bin(ff + 8, G2 * (nuh * km * (a2[0] + a2[1]))); bin(ff + 9, G2 * (nuh * km * a2[2])); }
       f += 2;
     }
     if (I.density && !I.scalar) {
@@ -1507,6 +1546,13 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
       bin(f + 1, r2);                                                     // rho
       bin(f + 2, alpha * k2 * r2);                                        // rhodiss
       bin(f + 3, (double)dF.x * rho.x + (double)dF.y * rho.y);           // rhonl
+      if (I.sfil) {   // buoyancy_fil_v, rho_fil, rhodiss_fil (of the filtered rho, filtered again), rhonl_fil
+        const int fd = ff + 8 + (I.hv ? 2 : 0);
+        bin(fd, G2 * (gz * ((double)u[2].x * rho.x + (double)u[2].y * rho.y)));
+        bin(fd + 1, G2 * r2);
+        bin(fd + 2, G2 * (alpha * k2 * (G2 * r2)));
+        bin(fd + 3, G2 * ((double)dF.x * rho.x + (double)dF.y * rho.y));
+      }
     }
   }
 }
@@ -1546,6 +1592,10 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
   if (fresh) {
     S->nl_h = tot[Q_NLH]; S->nl_v = tot[Q_NLV];
     S->press_h = tot[Q_PH]; S->press_v = tot[Q_PV];
+    if (I.sfil) {   // the filtered pressure sums are never accumulated (stats.jl:832-893)
+      S->nl_hf = tot[Q_FNLH]; S->nl_vf = tot[Q_FNLV];
+      S->press_hf = 0.0; S->press_vf = 0.0;
+    }
   }
   if (mode == 1) {
     // calculate_rhs! at initialize!: pressure_stats leaves its sum in reductionh[1]
@@ -1557,51 +1607,65 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
     const long long r = S->nrec;
     if (r < I.rec_cap) {
       double* row = I.records + r * I.ncols;
-      const double u12 = tot[Q_U12], u22 = tot[Q_U22], u32 = tot[Q_U32];
-      const double kh = (u12 + u22) / 2, kv = u32 / 2;
-      const double eh = I.nu * tot[Q_EH], ev = I.nu * tot[Q_EV];
-      const double nlh = S->nl_h, nlv = S->nl_v, ph = S->press_h, pv = S->press_v;
+      // the Stats.txt columns after iteration and time (stats.jl:64-165); f: the
+      // Stats_fil.txt twin (filtered sums, the same means and forcing columns)
+      auto stats_cols = [&](int c, bool f) -> int {
+        const double u12 = tot[f ? Q_FU12 : Q_U12], u22 = tot[f ? Q_FU22 : Q_U22], u32 = tot[f ? Q_FU32 : Q_U32];
+        const double kh = (u12 + u22) / 2, kv = u32 / 2;
+        const double eh = I.nu * tot[f ? Q_FEH : Q_EH], ev = I.nu * tot[f ? Q_FEV : Q_EV];
+        const double nlh = f ? S->nl_hf : S->nl_h, nlv = f ? S->nl_vf : S->nl_v;
+        const double ph = f ? S->press_hf : S->press_h, pv = f ? S->press_vf : S->press_v;
+        row[c++] = tot[Q_U1]; row[c++] = tot[Q_U2]; row[c++] = tot[Q_U3];
+        row[c++] = u12; row[c++] = u22; row[c++] = u32;
+        row[c++] = kh; row[c++] = kv; row[c++] = 2 * kv / kh; row[c++] = kh + kv;
+        row[c++] = eh; row[c++] = ev; row[c++] = eh + ev;
+        row[c++] = nlh; row[c++] = nlv; row[c++] = ph; row[c++] = pv;
+        row[c++] = -(nlh + ph); row[c++] = nlv + pv;
+        const double lesh = tot[f ? Q_FLESH : Q_LESH], lesv = tot[f ? Q_FLESV : Q_LESV];
+        const double hvh = tot[f ? Q_FHVH : Q_HVH], hvv = tot[f ? Q_FHVV : Q_HVV];
+        double tdiss = eh + ev;
+        if (I.les) tdiss += -lesh - lesv;
+        if (I.hv) tdiss += I.hv_nu * (hvh + hvv);
+        row[c++] = tdiss;
+        if (I.density) {   // density (BoussinesqApproximation stats) or scalar_stats (stats.jl:221-233)
+          const double d1 = tot[f ? Q_FDR1 : Q_DR1], d2 = tot[f ? Q_FDR2 : Q_DR2], d3 = tot[f ? Q_FDR3 : Q_DR3];
+          const double rd = I.alpha * (d1 + d2 + d3);
+          row[c++] = tot[Q_RHO]; row[c++] = tot[f ? Q_FRHO2 : Q_RHO2]; row[c++] = d1; row[c++] = d2;
+          row[c++] = d3; row[c++] = rd;
+          if (!I.scalar) { row[c++] = rd; row[c++] = -I.gval * tot[f ? Q_FBF : Q_BF]; }
+        }
+        if (I.les) {
+          const double prh = -lesh, prv = -lesv;
+          row[c++] = prh; row[c++] = prv; row[c++] = (2 * prv) / prh; row[c++] = prh + prv;
+        }
+        if (I.forcing) {
+          const double dt = S->dt;
+          row[c++] = tot[Q_HP] / dt; row[c++] = tot[Q_VP] / dt; row[c++] = (tot[Q_HP] + tot[Q_VP]) / dt;
+        } else if (I.pforce == FFS_PF_A) {   // stats(a::AForcing) (forcing_types.jl:98): hp, vp
+          row[c++] = S->pf_hp; row[c++] = S->pf_vp;
+        } else if (I.pforce) {   // stats(a::RfForcing) (forcing_types.jl:33): F.hp, F.vp of the last call
+          row[c++] = S->pf_hp; row[c++] = S->pf_vp; row[c++] = S->pf_hp + S->pf_vp;
+        }
+        if (I.hv) {
+          row[c++] = I.hv_nu * hvh; row[c++] = I.hv_nu * hvv; row[c++] = I.hv_nu * (hvh + hvv);
+        }
+        return c;
+      };
       int c = 0;
       row[c++] = (double)it; row[c++] = S->time;
-      row[c++] = tot[Q_U1]; row[c++] = tot[Q_U2]; row[c++] = tot[Q_U3];
-      row[c++] = u12; row[c++] = u22; row[c++] = u32;
-      row[c++] = kh; row[c++] = kv; row[c++] = 2 * kv / kh; row[c++] = kh + kv;
-      row[c++] = eh; row[c++] = ev; row[c++] = eh + ev;
-      row[c++] = nlh; row[c++] = nlv; row[c++] = ph; row[c++] = pv;
-      row[c++] = -(nlh + ph); row[c++] = nlv + pv;
-      double tdiss = eh + ev;
-      if (I.les) tdiss += -tot[Q_LESH] - tot[Q_LESV];
-      if (I.hv) tdiss += I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);
-      row[c++] = tdiss;
-      if (I.density) {   // density (BoussinesqApproximation stats) or scalar_stats (stats.jl:221-233)
-        const double rd = I.alpha * (tot[Q_DR1] + tot[Q_DR2] + tot[Q_DR3]);
-        row[c++] = tot[Q_RHO]; row[c++] = tot[Q_RHO2]; row[c++] = tot[Q_DR1]; row[c++] = tot[Q_DR2];
-        row[c++] = tot[Q_DR3]; row[c++] = rd;
-        if (!I.scalar) { row[c++] = rd; row[c++] = -I.gval * tot[Q_BF]; }
-      }
-      if (I.les) {
-        const double prh = -tot[Q_LESH], prv = -tot[Q_LESV];
-        row[c++] = prh; row[c++] = prv; row[c++] = (2 * prv) / prh; row[c++] = prh + prv;
-      }
-      if (I.forcing) {
-        const double dt = S->dt;
-        row[c++] = tot[Q_HP] / dt; row[c++] = tot[Q_VP] / dt; row[c++] = (tot[Q_HP] + tot[Q_VP]) / dt;
-      } else if (I.pforce == FFS_PF_A) {   // stats(a::AForcing) (forcing_types.jl:98): hp, vp
-        row[c++] = S->pf_hp; row[c++] = S->pf_vp;
-      } else if (I.pforce) {   // stats(a::RfForcing) (forcing_types.jl:33): F.hp, F.vp of the last call
-        row[c++] = S->pf_hp; row[c++] = S->pf_vp; row[c++] = S->pf_hp + S->pf_vp;
-      }
-      if (I.hv) {
-        row[c++] = I.hv_nu * tot[Q_HVH]; row[c++] = I.hv_nu * tot[Q_HVV]; row[c++] = I.hv_nu * (tot[Q_HVH] + tot[Q_HVV]);
-      }
+      c = stats_cols(c, false);
       // 9 integral-length plane sums and 4 derivative variances (Scales.txt inputs)
       for (int i = 0; i < 9; ++i) row[c++] = tot[Q_IL0 + i];
       row[c++] = tot[Q_D1DY]; row[c++] = tot[Q_D1DX]; row[c++] = tot[Q_D2DY]; row[c++] = tot[Q_D2DX];
+      if (I.sfil) stats_cols(c, true);   // the Stats_fil.txt row (stats.jl:48-52)
     }
     S->nrec = r + 1;
     if (I.adaptive && I.ref_slot) {
       // the last reduction of writestats that reuses reductionh / density reduction
       double slot = tot[Q_D2DX];
+      // STAT_FIL: the scalar's and the density's filtered sums go through reductionh
+      // (scalar_stats, buoyancy_flux: density_stratification_types.jl:192-210)
+      if (I.sfil && I.density) slot = I.scalar ? tot[Q_FDR3] : tot[Q_FBF];
       if (I.les) slot = tot[Q_LESH];
       if (I.hv) slot = tot[Q_HVH];
       S->slot_u = slot;

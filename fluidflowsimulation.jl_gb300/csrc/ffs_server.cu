@@ -373,6 +373,7 @@ class Server {
       return fail_api(FFS_EUNSUPPORTED, "the server does not batch density-stratified or passive-scalar runs");
     if (p.les && (p.les_model != FFS_LES_SMAGORINSKY || p.sandp_cb != 0.0))
       return fail_api(FFS_EUNSUPPORTED, "the server batches the Smagorinsky LES model only");
+    if (p.spec_fil != 0.0) return fail_api(FFS_EUNSUPPORTED, "the server does not batch filtered statistics (specFil)");
     int tpl, np;
     for (int n : {p.nx, p.ny, p.nz}) {
       plan_shape(n, tpl, np);

@@ -104,6 +104,7 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
     p.start_time = float(d.get("startTime", "0.0"))
     p.dt_stat = int(d["dtStat"])
     p.dt_spec = int(d["dtSpec"])          # the reference raises KeyError without it (:262)
+    p.spec_fil = float(d["specFil"]) if "specFil" in d else 0.0   # Globals.jl:173-178
     p.write_time = int(d["writeTime"])
     integ = d.get("velocityTimeStep", "ETD3rdO")
     if integ == "Adams_Bashforth3rdO":

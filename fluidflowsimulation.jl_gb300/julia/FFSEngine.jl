@@ -37,7 +37,7 @@ mutable struct FFSParams
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
-    les_test_width::Float64; les_cmin::Float64
+    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64
     FFSParams() = new()
 end
 
@@ -79,6 +79,7 @@ function parameters(d)
     p.start = haskey(d, :start) ? parse(Int, d[:start]) : 0
     p.start_time = haskey(d, :startTime) ? parse(Float64, d[:startTime]) : 0.0
     p.dt_stat = parse(Int32, d[:dtStat]); p.dt_spec = parse(Int32, d[:dtSpec]); p.write_time = parse(Int32, d[:writeTime])
+    p.spec_fil = haskey(d, :specFil) ? parse(Float64, d[:specFil]) : 0.0   # Globals.jl:173-178
     p.integrator = get(d, :velocityTimeStep, "ETD3rdO") == "Adams_Bashforth3rdO" ? 1 : 0
     p.variable_dt = haskey(d, :variableTimestepFlag) ? Int32(parse(Bool, d[:variableTimestepFlag])) : 1
     p.cfl = haskey(d, :cfl) ? parse(Float64, d[:cfl]) : 0.18
@@ -264,12 +265,13 @@ function writespectra(e::Engine)
             sH, sV = spec(f)
             writepairs("$nm.specH.$i", KH, sH)
             writepairs("$nm.specV.$i", KRZ, sV)
-            if nm == "buoyancy_v" && p.gravity_dir == 2 && p.gravity != 0   # spec.jl:53-57
-                writepairs("rhosource.specH.$i", KH, sH .* (-p.density_gradient / p.gravity))
-                writepairs("rhosource.specV.$i", KRZ, sV .* (-p.density_gradient / p.gravity))
+            if (nm == "buoyancy_v" || nm == "buoyancy_fil_v") && p.gravity_dir == 2 && p.gravity != 0
+                rs = nm == "buoyancy_v" ? "rhosource" : "rhosource_fil"   # spec.jl:53-57, 85-95
+                writepairs("$rs.specH.$i", KH, sH .* (-p.density_gradient / p.gravity))
+                writepairs("$rs.specV.$i", KRZ, sV .* (-p.density_gradient / p.gravity))
             end
         end
-        for base in ("u", "vis", "nl", "press", "les", "hvis")
+        for base in ("u", "vis", "nl", "press", "les", "hvis", "u_fil", "vis_fil", "nl_fil", "press_fil", "hvis_fil")
             ih = findfirst(==("$(base)_h"), names); iv = findfirst(==("$(base)_v"), names)
             (ih === nothing || iv === nothing) && continue
             writepairs("$base.specH.$i", KH, spec(ih)[1] .+ spec(iv)[1])
@@ -302,8 +304,10 @@ function run_simulation()
     rho = ((p.density == 1 || p.passive_scalar == 1) && isfile(fname)) ?
           open(f -> readfield(f, p.nx, p.ny, p.nz), fname) : nothing
     setfields!(e, u..., rho)
+    fil = p.spec_fil != 0   # Stats_fil.txt (stats.jl:14-18, 48-52)
     if s == 0
         open(f -> write(f, statsheader(e), "\n"), "Stats.txt", "w")
+        fil && open(f -> write(f, statsheader(e), "\n"), "Stats_fil.txt", "w")
         open(f -> write(f, scalesheader(p.density == 1), "\n"), "Scales.txt", "w")
         open(f -> write(f, numbersheader(p.density == 1), "\n"), "Numbers.txt", "w")
     end
@@ -331,6 +335,11 @@ function run_simulation()
         open("Stats.txt", "a+") do f
             for r in eachcol(recs)
                 join(f, (Int(r[1]), r[2:ns]..., "\n"), ",", "")
+            end
+        end
+        fil && open("Stats_fil.txt", "a+") do f   # after the 13 Scales inputs of each record
+            for r in eachcol(recs)
+                join(f, (Int(r[1]), r[2], r[ns+14:2ns+11]..., "\n"), ",", "")
             end
         end
         for r in eachcol(recs)

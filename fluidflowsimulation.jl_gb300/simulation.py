@@ -146,7 +146,8 @@ class Simulation:
         self._check(self._L.ffs_set_spectral(self._h, comp, a.ctypes.data_as(_D)))
 
     def records(self) -> np.ndarray:
-        """Pending stats records: Stats.txt columns then 13 Scales.txt inputs."""
+        """Pending stats records, drained by the read: the Stats.txt columns, 13 Scales.txt
+        inputs, then with specFil the Stats_fil.txt columns (``stats_fil_rows``)."""
         n = self._L.ffs_stats_records(self._h, None, 0)
         out = np.empty((max(n, 0), self.rec_ncols))
         if n > 0:
@@ -155,6 +156,17 @@ class Simulation:
 
     def stats_rows(self) -> np.ndarray:
         return self.records()[:, : self.ncols]
+
+    @property
+    def has_stats_fil(self) -> bool:
+        """specFil != 0: every record also carries the Stats_fil.txt row (stats.jl:48-52)."""
+        return self.rec_ncols > self.ncols + 13
+
+    def stats_fil_rows(self, records: np.ndarray | None = None) -> np.ndarray:
+        """Stats_fil.txt rows (iteration, time, then the filtered columns) of records."""
+        r = self.records() if records is None else records
+        o = self.ncols + 13
+        return np.concatenate([r[:, :2], r[:, o:o + self.ncols - 2]], axis=1)
 
     def stats(self) -> np.ndarray:
         """The Stats.txt row of the most recent stats iteration (``ffs_stats``); pending
@@ -207,7 +219,8 @@ class Simulation:
                 o = 1 + i * (H + V)
                 rec[f"{nm}.specH"] = r[o:o + H]
                 rec[f"{nm}.specV"] = r[o + H:o + H + V]
-            for base in ("u", "vis", "nl", "press", "les", "hvis"):
+            for base in ("u", "vis", "nl", "press", "les", "hvis", "u_fil", "vis_fil", "nl_fil", "press_fil",
+                         "hvis_fil"):
                 if f"{base}_h.specH" in rec:
                     rec[f"{base}.specH"] = rec[f"{base}_h.specH"] + rec[f"{base}_v.specH"]
             res.append(rec)
@@ -286,6 +299,9 @@ def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarra
     if rhosource is not None and "buoyancy_v.specH" in rec:
         put("rhosource.specH", KH, rec["buoyancy_v.specH"] * rhosource)
         put("rhosource.specV", KRZ, rec["buoyancy_v.specV"] * rhosource)
+    if rhosource is not None and "buoyancy_fil_v.specH" in rec:   # spec.jl:85-95
+        put("rhosource_fil.specH", KH, rec["buoyancy_fil_v.specH"] * rhosource)
+        put("rhosource_fil.specV", KRZ, rec["buoyancy_fil_v.specV"] * rhosource)
 
 
 def run_simulation(folder: str | Path = ".", precision: str | None = None, device: int = 0) -> Simulation:
@@ -304,6 +320,8 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     lengthtime = float(d["timeDuration"]) if "timeDuration" in d else float("inf")
     if start == 0:   # writeheader (stats.jl:9-37)
         (folder / "Stats.txt").write_text(sim.header + "\n")
+        if sim.has_stats_fil:
+            (folder / "Stats_fil.txt").write_text(sim.header + "\n")
         (folder / "Scales.txt").write_text(_scales.scales_header(bool(p.density)) + "\n")
         (folder / "Numbers.txt").write_text(_scales.numbers_header(bool(p.density)) + "\n")
     sim.initialize()
@@ -335,6 +353,10 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         with open(folder / "Stats.txt", "a") as f:
             for r in recs[:, : sim.ncols]:
                 f.write(stats_line(r))
+        if sim.has_stats_fil:
+            with open(folder / "Stats_fil.txt", "a") as f:
+                for r in sim.stats_fil_rows(recs):
+                    f.write(stats_line(r))
         sc, nums = sim.scales_numbers(recs)
         for name, rows in (("Scales.txt", sc), ("Numbers.txt", nums)):
             with open(folder / name, "a") as f:

@@ -106,6 +106,10 @@ typedef struct ffs_params {
   double pf_qp, pf_qc, pf_qkf; /* alveliusP, alveliusC, alveliusKf (QfForcing) */
   double les_test_width;       /* dynamicSmagorinsky: TestFilterWidth (<= 0: twice the filter width) */
   double les_cmin;             /* dynamicSmagorinsky: cmin, the smallest coefficient kept */
+  double spec_fil;             /* specFil nf (Globals.jl:173-182): with nf != 0 every stats record also
+                                  carries the Stats_fil.txt row (quadratic sums weighted by the Gaussian
+                                  filter squared, D = 2 pi lx nf / nx) and the spectrum records the
+                                  *_fil spectra; 0: off */
 } ffs_params;
 
 #define FFS_PF_NONE 0

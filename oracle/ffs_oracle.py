@@ -176,10 +176,16 @@ class Params:
     pf_qkf: float = 0.0                  # alveliusKf
     dt_stat: int = 1
     dt_spec: int = 1
+    spec_fil: float = 0.0                # specFil: filtered stats and spectra (0: off)
     write_time: int = 1 << 30
     start: int = 0
     start_time: float = 0.0
     reference_cfl_slot: bool = True
+
+    @property
+    def fil_d2(self) -> float:
+        """SPEC_FIL_D2 = (2 pi LX nf / NRX)^2 (Globals.jl:173-178); STAT_FIL = fil_d2 != 0."""
+        return (2 * math.pi * self.lx * self.spec_fil / self.nx) ** 2 if self.spec_fil else 0.0
 
     @classmethod
     def from_global(cls, d: dict) -> "Params":
@@ -194,6 +200,8 @@ class Params:
         p.start_time = float(d.get("startTime", 0.0))
         p.dt_stat = int(d["dtStat"])
         p.dt_spec = int(d["dtSpec"])                       # KeyError like :262
+        if "specFil" in d:                                 # Globals.jl:173-178
+            p.spec_fil = float(d["specFil"])
         p.write_time = int(d["writeTime"])
         p.integrator = d.get("velocityTimeStep", "ETD3rdO")
         p.variable_dt = d.get("variableTimestepFlag", "true").strip().lower() == "true"
@@ -897,7 +905,17 @@ class OracleSimulation:
         self.slot_rho = 0.0
         self.nlstats = (1.0, 1.0)
         self.pressstats = (1.0, 1.0)
+        self.nlstats_fil = (1.0, 1.0)                      # simulationtypes.jl:94-95
         self.stats_rows = []
+        self.stats_fil_rows = []                           # Stats_fil.txt (stats.jl:48-52)
+        # STAT_FIL weight Gaussfilter(SPEC_FIL_D2, k.k)^2 (utils.jl:220-225, stats.jl)
+        if p.spec_fil:
+            G = np.exp((-p.fil_d2 / 24) * g.K2)
+            self.G2 = G * G
+            mx = int(np.argmax(g.dealias[0, 0, :])) if g.dealias[0, 0, :].any() else g.nxh
+            self.ix_last = mx - 1                          # last index of XRANGE
+        else:
+            self.G2 = None
         self.scales_rows = []
         self.numbers_rows = []
         self.spectra = {}
@@ -1193,12 +1211,17 @@ class OracleSimulation:
         return float(np.sum(self.g.w * a))
 
     def non_linear_stats(self, nl, ke):
-        """stats.jl:897-917."""
+        """stats.jl:897-917 (with STAT_FIL also the G^2-weighted sums, :919-949, kept in
+        nlstats_fil)."""
         g = self.g
         u = self.u
         r = [nl[0] - 1j * g.KX * ke, nl[1] - 1j * g.KY * ke, nl[2] - 1j * g.KZ * ke]
-        h = self._wsum(_proj(r[0], u[0]) + _proj(r[1], u[1]))
-        v = self._wsum(_proj(r[2], u[2]))
+        hh = _proj(r[0], u[0]) + _proj(r[1], u[1])
+        vv = _proj(r[2], u[2])
+        h = self._wsum(hh)
+        v = self._wsum(vv)
+        if self.G2 is not None:
+            self.nlstats_fil = (self._wsum(hh * self.G2), self._wsum(vv * self.G2))
         if self.p.variable_dt and self.p.reference_cfl_slot:
             self.slot_u = h
         return h, v
@@ -1218,8 +1241,15 @@ class OracleSimulation:
         with np.errstate(divide="ignore", invalid="ignore"):
             p1 = -kd / g.K2
         p1[0, 0, 0] = 0.0
-        h = self._wsum(_proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY))
-        v = self._wsum(_proj(u[2], p1 * g.KZ))
+        hh = _proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY)
+        vv = _proj(u[2], p1 * g.KZ)
+        if self.G2 is not None:
+            # STAT_FIL branch (stats.jl:832-893): the G^2-weighted terms are added to the
+            # unfiltered sums (eeh += leeh*G2) and the filtered sums stay 0
+            hh = hh + hh * self.G2
+            vv = vv + vv * self.G2
+        h = self._wsum(hh)
+        v = self._wsum(vv)
         if self.p.variable_dt and self.p.reference_cfl_slot:
             self.slot_u = h
         return h, v
@@ -1285,9 +1315,72 @@ class OracleSimulation:
             extra += [p.hv_nu * hraw, p.hv_nu * vraw, p.hv_nu * (hraw + vraw)]
             tdiss += p.hv_nu * (hraw + vraw)
             slot = hraw
+        if self.G2 is not None:
+            fil, fslot = self._velocity_row_fil(a2)
+            self.fil_row = fil
+            if fslot is not None and not (p.les or p.hv):
+                slot = fslot
         if p.variable_dt and p.reference_cfl_slot:
             self.slot_u = slot
         return row + [tdiss] + extra
+
+    def _velocity_row_fil(self, a2):
+        """The Stats_fil.txt row (STAT_FIL branches of velocity_stats, scalar_stats,
+        buoyancy_flux, les_stats, hyperviscosity_stats; stats.jl:168-233, 354-376,
+        501-524, 563-606, 637-677, 707-747, density_stratification_types.jl:46-87,
+        192-210): every quadratic sum weighted by G^2, the means unweighted, the pressure
+        columns 0 (their filtered sums are never accumulated, stats.jl:880-891), and the
+        forcing columns as in Stats.txt. dx_squared_mean's filtered sum keeps only the
+        last kx of each line (`ee_fil = ...` where the others accumulate, stats.jl:370).
+        Returns the row and the value the reductionh slot holds after the scalar and
+        density stats (None without them)."""
+        p, g = self.p, self.g
+        u, G2 = self.u, self.G2
+        ws = lambda a: self._wsum(a * G2)   # noqa: E731
+        u12, u22, u32 = (ws(a) for a in a2)
+        kh = (u12 + u22) / 2
+        kv = u32 / 2
+        k = kh + kv
+        eh, ev = p.nu * ws(g.K2 * (a2[0] + a2[1])), p.nu * ws(g.K2 * a2[2])
+        nlh, nlv = self.nlstats_fil
+        ph = pv = 0.0
+        row = [u[0][0, 0, 0].real, u[1][0, 0, 0].real, u[2][0, 0, 0].real, u12, u22, u32,
+               kh, kv, 2 * kv / kh, k, eh, ev, eh + ev, nlh, nlv, ph, pv, -(nlh + ph), (nlv + pv)]
+        tdiss = eh + ev
+        extra = []
+        fslot = None
+
+        def scalar_fil(f):
+            r2 = np.abs(f) ** 2
+            i = self.ix_last
+            d1 = float(np.sum((g.w * g.KX ** 2 * r2 * G2)[:, :, i]))
+            d2, d3 = ws(g.KY ** 2 * r2), ws(g.KZ ** 2 * r2)
+            return [f[0, 0, 0].real, ws(r2), d1, d2, d3, self.alpha * (d1 + d2 + d3)], d3
+
+        if p.scalar:
+            vals, fslot = scalar_fil(self.rho)
+            extra += vals
+        if p.density:
+            vals, fslot = scalar_fil(self.rho)
+            bf_raw = ws(_proj(u[p.gravity_dir], self.rho))
+            extra += vals + [vals[-1], -self.gvec[p.gravity_dir] * bf_raw]
+            fslot = bf_raw
+        if p.les:
+            t = self.div_tau(self.tauh)
+            prh = -ws(_proj(t[0], u[0]) + _proj(t[1], u[1]))
+            prv = -ws(_proj(t[2], u[2]))
+            extra += [prh, prv, (2 * prv) / prh, prh + prv]
+            tdiss += prh + prv
+        if p.plane_forcing == "aForcing":
+            extra += [self.hp, self.vp]
+        elif p.forcing or p.plane_forcing:
+            extra += [self.hp, self.vp, self.hp + self.vp]
+        if p.hv:
+            hraw = ws((g.K2 ** p.hv_m) * (a2[0] + a2[1]))
+            vraw = ws((g.K2 ** p.hv_m) * a2[2])
+            extra += [p.hv_nu * hraw, p.hv_nu * vraw, p.hv_nu * (hraw + vraw)]
+            tdiss += p.hv_nu * (hraw + vraw)
+        return row + [tdiss] + extra, fslot
 
     def write_stats(self):
         """``writestats`` (stats.jl:39-62): one row each of Stats.txt, Scales.txt, Numbers.txt."""
@@ -1295,6 +1388,8 @@ class OracleSimulation:
         lens, anums = self.scales_numbers(row)
         head = [float(self.iteration), float(self.time)]
         self.stats_rows.append(head + row)
+        if self.G2 is not None:
+            self.stats_fil_rows.append(head + self.fil_row)
         self.scales_rows.append(head + lens)
         self.numbers_rows.append(head + anums)
 
@@ -1346,8 +1441,13 @@ class OracleSimulation:
         vout = 0.5 * _proj(u[2], u[2])
         hH, hV = self.calculate_specHV(hout)
         vH, vV = self.calculate_specHV(vout)
-        return {"u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH,
-                "u_v.specH": vH, "u_v.specV": vV}
+        out = {"u_h.specH": hH, "u_h.specV": hV, "u.specH": hH + vH, "u_v.specH": vH, "u_v.specV": vV}
+        if self.G2 is not None:                     # u_fil: filter_spectrum! (spec.jl:17-20, 452-472)
+            hH, hV = self.calculate_specHV(self.G2 * hout)
+            vH, vV = self.calculate_specHV(self.G2 * vout)
+            out.update({"u_fil_h.specH": hH, "u_fil_h.specV": hV, "u_fil.specH": hH + vH,
+                        "u_fil_v.specH": vH, "u_fil_v.specV": vV})
+        return out
 
     def spectra_write_spec(self, nl, ke, tauh, ikflux):
         """The other spectra of ``write_spec`` (spec.jl:1-146, 196-422), binned by
@@ -1356,19 +1456,23 @@ class OracleSimulation:
         p, g = self.p, self.g
         u = self.u
         out = {}
+        G2 = self.G2
 
-        def put(name, field):
+        def put(name, field, fil=None):
             H, V = self.calculate_specHV(field)
             out[name + ".specH"], out[name + ".specV"] = H, V
+            if G2 is not None and fil is not None:   # the filter_spectrum! twin (spec.jl:13-142)
+                H, V = self.calculate_specHV(G2 * field)
+                out[fil + ".specH"], out[fil + ".specV"] = H, V
 
         k2 = g.KX * g.KX + (g.KY * g.KY + g.KZ * g.KZ)
         uh_ = 0.5 * (_proj(u[0], u[0]) + _proj(u[1], u[1]))
         uv_ = 0.5 * _proj(u[2], u[2])
-        put("vis_h", 2 * p.nu * k2 * uh_)                         # spectrum_viscosity
-        put("vis_v", 2 * p.nu * k2 * uv_)
+        put("vis_h", 2 * p.nu * k2 * uh_, "vis_fil_h")            # spectrum_viscosity
+        put("vis_v", 2 * p.nu * k2 * uv_, "vis_fil_v")
         r = np.stack([nl[0] - 1j * g.KX * ke, nl[1] - 1j * g.KY * ke, nl[2] - 1j * g.KZ * ke])
-        put("nl_h", _proj(r[0], u[0]) + _proj(r[1], u[1]))        # spectrum_non_linear
-        put("nl_v", _proj(r[2], u[2]))
+        put("nl_h", _proj(r[0], u[0]) + _proj(r[1], u[1]), "nl_fil_h")   # spectrum_non_linear
+        put("nl_v", _proj(r[2], u[2]), "nl_fil_v")
         if p.les:
             dt_ = self.div_tau(tauh)
             r = r + dt_
@@ -1380,22 +1484,27 @@ class OracleSimulation:
         with np.errstate(divide="ignore", invalid="ignore"):
             p1 = -kd / g.K2
         p1[0, 0, 0] = 0.0
-        put("press_h", _proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY))   # spectrum_pressure
-        put("press_v", _proj(u[2], p1 * g.KZ))
+        put("press_h", _proj(u[0], p1 * g.KX) + _proj(u[1], p1 * g.KY), "press_fil_h")   # spectrum_pressure
+        put("press_v", _proj(u[2], p1 * g.KZ), "press_fil_v")
         if p.les:
             put("les_h", _proj(dt_[0], u[0]) + _proj(dt_[1], u[1]))       # spectrum_les
             put("les_v", _proj(dt_[2], u[2]))
         if p.hv:
             km = k2 ** p.hv_m
-            put("hvis_h", p.hv_nu * km * (_proj(u[0], u[0]) + _proj(u[1], u[1])))
-            put("hvis_v", p.hv_nu * km * _proj(u[2], u[2]))
+            put("hvis_h", p.hv_nu * km * (_proj(u[0], u[0]) + _proj(u[1], u[1])), "hvis_fil_h")
+            put("hvis_v", p.hv_nu * km * _proj(u[2], u[2]), "hvis_fil_v")
         if p.density:
             rho = self.rho
-            put("buoyancy_v", self.gvec[2] * _proj(u[2], rho))            # spectrum_buoyancy
+            put("buoyancy_v", self.gvec[2] * _proj(u[2], rho), "buoyancy_fil_v")   # spectrum_buoyancy
             r2 = _proj(rho, rho)
-            put("rho", r2)                                                # spectrum_rho
+            put("rho", r2, "rho_fil")                                     # spectrum_rho
             put("rhodiss", self.alpha * k2 * r2)                          # spectrum_rhodiss
-            put("rhonl", _proj(ikflux, rho))                              # spectrum_rhonl
+            put("rhonl", _proj(ikflux, rho), "rhonl_fil")                 # spectrum_rhonl
+            if G2 is not None:
+                # rhodiss_fil: spectrum_rhodiss of the filtered rho spectrum, filtered once
+                # more (spec.jl:97-108), so G^4
+                H, V = self.calculate_specHV(G2 * (self.alpha * k2 * (G2 * r2)))
+                out["rhodiss_fil.specH"], out["rhodiss_fil.specV"] = H, V
         return out
 
     def calculate_specHV(self, out):

@@ -109,6 +109,16 @@ FIXED_CASES = {
                            hyperViscosity="true", hyperViscosityCoefficient="1e-5"),
     "ab3-sandp-vreman-density": gdict(48, lesModel="SandP", sLesModel="Vreman", densityStratification="true",
                                       Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1"),
+    # specFil (Globals.jl:173-182): the Stats_fil.txt row beside every Stats.txt row, and
+    # the reference's STAT_FIL side effects on Stats.txt (pressure columns) and on the
+    # CFL slot (adaptive cases)
+    "etd-les-density-hv-specfil": gdict(32, "ETD3rdO", lesModel="Smagorinsky", densityStratification="true", Pr="1",
+                                        densityGradient="1", zAcceleration="1", referenceDensity="1",
+                                        hyperViscosity="true", hyperViscosityCoefficient="1e-5", specFil="2"),
+    "ab3-adaptive-density-specfil": gdict(32, adaptive=True, densityStratification="true", Pr="2", densityGradient="1",
+                                          zAcceleration="1", referenceDensity="1", specFil="3"),
+    "ab3-adaptive-scalar-specfil": gdict(32, adaptive=True, passiveScalar="true", scalarPr="0.7", scalarGradient="1",
+                                         specFil="1.5", forcing="isotropicBand", forcingPower="0.1", forcingKf="2.5"),
 }
 
 
@@ -121,7 +131,8 @@ def test_fp64_step_parity(gpu_pkg, name):
         assert rel(sim.spectral(c), ref.u[c]) <= FP64_FIELD_TOL, (name, c)
     if fld:
         assert rel(sim.spectral(3), ref.rho) <= FP64_FIELD_TOL
-    rows = sim.stats_rows()
+    recs = sim.records()                 # reading drains the pending records
+    rows = recs[:, : sim.ncols]
     rr = np.array(ref.stats_rows)
     assert rows.shape == rr.shape
     assert sim.header.count(",") + 1 == rows.shape[1]
@@ -131,6 +142,13 @@ def test_fp64_step_parity(gpu_pkg, name):
     scale = np.maximum(np.abs(rr), 1e-6 * np.abs(rr).max())
     err = np.abs(rows - rr) / scale
     assert err.max() <= FP64_STATS_TOL, (name, np.unravel_index(err.argmax(), err.shape), err.max())
+    assert sim.has_stats_fil == ("specFil" in d)
+    if sim.has_stats_fil:   # Stats_fil.txt rows, same bar
+        fr, fe = sim.stats_fil_rows(recs), np.array(ref.stats_fil_rows)
+        assert fr.shape == fe.shape == rr.shape
+        scale = np.maximum(np.abs(fe), 1e-6 * np.abs(fe).max())
+        err = np.abs(fr - fe) / scale
+        assert err.max() <= FP64_STATS_TOL, (name, "fil", np.unravel_index(err.argmax(), err.shape), err.max())
     assert sim.iteration == ref.iteration
     assert sim.time == pytest.approx(ref.time, rel=1e-14)
     sim.close()
@@ -185,6 +203,7 @@ SPEC_CASES = {
     "etd-les-density": dict(FIXED_CASES["etd-les-density"], dtSpec="2"),
     "ab3-hv-forced": dict(FIXED_CASES["ab3-64-hv-forced"], dtSpec="2"),
     "etd-scalar": dict(FIXED_CASES["etd-scalar"], dtSpec="2"),
+    "etd-les-density-hv-specfil": dict(FIXED_CASES["etd-les-density-hv-specfil"], dtSpec="2"),
 }
 
 

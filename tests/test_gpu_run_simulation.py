@@ -65,6 +65,9 @@ CASES = {
     # rfForcing: the run ends by writing the shells' ODE state R.N (FluidFlowSimulation.jl:60-62)
     "etd-rf-forcing": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "10",
                        "forcing": "rfForcing", "TF": "2.0", "alphac": "1.0", "kf": "3.0"},
+    # specFil: Stats_fil.txt and the *_fil spectrum files (stats.jl:14-18, 48-52; spec.jl:13-142)
+    "etd-specfil-hv": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "8",
+                       "hyperViscosity": "true", "hyperViscosityCoefficient": "1e-5", "specFil": "2"},
 }
 
 
@@ -91,6 +94,11 @@ def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
     for name, want in (("Scales.txt", ref.scales_rows), ("Numbers.txt", ref.numbers_rows)):
         _, got = read_rows(tmp_path / name)
         assert rows_err(got, want) <= 1e-10, name
+    assert (tmp_path / "Stats_fil.txt").exists() == ("specFil" in d)
+    if "specFil" in d:
+        head, rows = read_rows(tmp_path / "Stats_fil.txt")
+        assert head == stats_header(p)
+        assert rows_err(rows, ref.stats_fil_rows) <= 1e-10
     # spectra: every (field, iteration) the oracle recorded is a file with its values
     assert ref.spectra
     for it, sp in ref.spectra.items():
