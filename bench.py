@@ -427,6 +427,46 @@ def make_sim(pkg, d, prec, ic, n, device, autotune=1):
     return sim
 
 
+def run_large(pkg, device: int, steps: int, autotune: int) -> dict:
+    """The large single-instance configuration (DNS 1024^3 + hyperviscosity, FP32) measured
+    inside the default run: K graph replays after 3 warm-up steps, per-kernel event times
+    and their HBM fractions against the 69A effective-bytes model, DRAM traffic per launch
+    from the committed ncu captures (profiles/traffic.txt; 1024^3 rows scaled from the
+    512^3 capture, see the file), clocks sampled during the timed replays."""
+    d, n, prec, ic, desc = workload_config("dns1024")
+    try:
+        sim = make_sim(pkg, d, prec, ic, n, device, autotune)
+    except pkg.FFSError as e:
+        return {"workload": desc, "error": str(e)}
+    sim.advance_in_time(3)
+    with ClockSampler(device) as clk:
+        ms = sim.time_steps(steps)
+    nprof = 3
+    prof = sim.profile_kernels(nprof)
+    out = {"workload": desc, "value": steps / (ms / 1e3), "unit": "steps/s", "steps": steps, "warmup": 3,
+           "ms_per_step": ms / steps, "grid_point_updates_per_s": steps / (ms / 1e3) * n ** 3,
+           "device_gb": sim.device_bytes / 1e9, "kernels_ms_per_step": {k: v / nprof for k, v in prof.items()},
+           "gpu_launches": sim.launches_per_step * (steps + nprof), "clocks": clk.summary(), "tuning": sim.tuning}
+    sim.close()
+    peak, kind = measured_peaks()
+    sb = model_bytes(n, 8)
+    roof = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": kind,
+            "bytes_model": "69A per step, A = (n/2+1) n^2 complex FP32 (hyperviscosity adds no passes)",
+            "step_frac": sb["step"] / (ms / steps / 1e3) / 1e9 / peak, "per_kernel": {}}
+    for k in ("inv_z", "inv_y", "x_pass", "fwd_y", "fwd_z", "update"):
+        if prof.get(k, 0) <= 0:
+            continue
+        t = prof[k] / nprof / 1e3
+        e = {"ms": t * 1e3, "model_frac": sb[k] / t / 1e9 / peak}
+        tr = ncu_traffic(k, n, "fp32")
+        if tr:
+            e["traffic"] = tr
+            e["dram_frac"] = tr / t / 1e9 / peak
+        roof["per_kernel"][k] = e
+    out["roofline"] = roof
+    return out
+
+
 def run_workload(args):
     """One JSON line for a configuration other than the headline 256^3 run."""
     import numpy as np
@@ -708,6 +748,9 @@ def run_engine_arm(args):
     if args.serve_requests > 0:
         line["serving"] = run_serving(pkg, args.serve_requests, args.serve_seq_budget, local)
         line["gpu_launches"] += line["serving"].get("batched", {}).get("gpu_launches", 0)
+    if args.large_steps > 0 and world == 1:
+        line["dns1024"] = run_large(pkg, local, args.large_steps, 0 if args.no_autotune else 1)
+        line["gpu_launches"] += line["dns1024"].get("gpu_launches", 0)
     print(json.dumps(line), flush=True)
     return 0
 
@@ -806,6 +849,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=64, help="served-ensemble requests (0: skip)")
     ap.add_argument("--serve-seq-budget", type=float, default=60.0,
                     help="seconds for each one-at-a-time baseline of the served ensemble")
+    ap.add_argument("--large-steps", type=int, default=10,
+                    help="timed steps of the 1024^3 FP32 configuration in the default run (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)

@@ -28,7 +28,7 @@ EXPORTS = [
     "ffs_stream",
     "ffs_fourier_noalloc", "ffs_measure_fp64_peak", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
-    "ffs_fetch_fields", "ffs_release", "ffs_cancel", "ffs_server_pause", "ffs_server_stats", "ffs_server_last_error", "ffs_server_destroy",
+    "ffs_fetch_fields", "ffs_release", "ffs_cancel", "ffs_server_pause", "ffs_server_stats", "ffs_server_tuning", "ffs_server_last_error", "ffs_server_destroy",
 ]
 FFS_QUEUED, FFS_RUNNING = 1, 2
 
@@ -55,13 +55,14 @@ class FFSParams(ctypes.Structure):
         ("passive_scalar", c_int32), ("scalar_pr", c_double), ("scalar_gradient", c_double), ("scalar_dir", c_int32),
         ("plane_forcing", c_int32), ("pf_tf", c_double), ("pf_alpha", c_double), ("pf_kf", c_double),
         ("pf_zf_tanh", c_int32), ("pf_qp", c_double), ("pf_qc", c_double), ("pf_qkf", c_double),
-        ("les_test_width", c_double), ("les_cmin", c_double), ("spec_fil", c_double),
+        ("les_test_width", c_double), ("les_cmin", c_double), ("spec_fil", c_double), ("radix_split", c_int32),
     ]
 
 
 class FFSServerCfg(ctypes.Structure):
     """Mirror of ``ffs_server_cfg``."""
-    _fields_ = [("device", c_int32), ("memory_budget", c_int64), ("max_active", c_int32), ("max_n", c_int32)]
+    _fields_ = [("device", c_int32), ("memory_budget", c_int64), ("max_active", c_int32), ("max_n", c_int32),
+                ("autotune", c_int32), ("class_forms", c_int32)]
 
 
 class FFSRequest(ctypes.Structure):
@@ -147,6 +148,7 @@ def load() -> ctypes.CDLL:
         "ffs_cancel": (c_int32, [H, ctypes.c_uint64]),
         "ffs_server_pause": (c_int32, [H, c_int32]),
         "ffs_server_stats": (c_int32, [H, POINTER(FFSServerInfo)]),
+        "ffs_server_tuning": (c_int64, [H, ctypes.c_char_p, c_int64]),
         "ffs_server_last_error": (c_char_p, [H]),
         "ffs_server_destroy": (None, [H]),
     }

@@ -42,14 +42,24 @@ template <typename T> struct BatchInst {
   int nparts;   // partial sums of the stats pass
 };
 
-constexpr int BATCH_TX = 8;    // kx lines per CTA in the y/z passes (FP32)
-constexpr int BATCH_LYZ = 4;   // (y,z) lines per CTA in the x pass
+constexpr int BATCH_TX = 8;    // kx lines per CTA in the y/z passes of the generic class (FP32)
+constexpr int BATCH_LYZ = 4;   // (y,z) lines per CTA in its x pass
+
+// Kernel forms of a size class's passes, picked per pass by the server's autotuner:
+//   y/z passes: line pairs on the packed FP32 pipe (8 kx lines a tile, n >= 64), or
+//               one line per thread with 8 or 4 kx lines a tile;
+//   x passes:   the register-fused pass (n = 64, 128), or the generic one with 4 or 2
+//               (y,z) lines a CTA.
+enum BatchYZForm : int { YZ_PAIR = 0, YZ_TX8 = 1, YZ_TX4 = 2, YZ_NFORMS = 3 };
+enum BatchXForm : int { XF_FUSED = 0, XF_LYZ4 = 1, XF_LYZ2 = 2, XF_NFORMS = 3 };
 
 // launch shape of one class's chain
 struct ClassLaunch {
   int grid[BP_COUNT];
   int block[BP_COUNT];
   size_t smem[BP_COUNT];
+  int form[BP_COUNT];   // BatchYZForm (y/z passes) or BatchXForm (x passes); 0 elsewhere
+  int tile[BP_COUNT];   // kx lines of a work item (y/z passes), (y,z) lines (x passes), else 1
 };
 
 #define FFS_BATCH_LOOP(PH)                                                         \
@@ -119,19 +129,23 @@ __global__ void __launch_bounds__(256) kb_update(const BatchInst<T>* __restrict_
   FFS_BATCH_END
 }
 template <typename T, int CI = 0>
-__global__ void kb_finalize(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
+__global__ void __launch_bounds__(1024) kb_finalize(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
   FFS_BATCH_LOOP(BP_FIN)
   b_finalize<T>(BI.I, 0, BI.nparts, Blk{0, 0, 0, 1});
   FFS_BATCH_END
 }
 
 // Host side of one size class (ffs_batch_class.cuh, one translation unit per class):
-// prepare() sets the kernels' shared-memory limits and computes the persistent grids;
-// enqueue() launches the class's chain on a stream.
+// prepare() takes the form of each pass (null: the defaults), sets the kernels'
+// shared-memory limits and computes the persistent grids; enqueue() launches the
+// class's chain on a stream; launch() one pass (for the autotuner); forms() the bit
+// mask of the forms a pass has.
 struct ClassOps {
   int n;   // cubic side
-  int (*prepare)(int device, int max_active, ClassLaunch* L, std::string* err);
+  int (*prepare)(int device, int max_active, const int* form, ClassLaunch* L, std::string* err);
   void (*enqueue)(const ClassLaunch& L, cudaStream_t s, const BatchInst<float>* B, const BatchTables* T);
+  void (*launch)(const ClassLaunch& L, int phase, cudaStream_t s, const BatchInst<float>* B, const BatchTables* T);
+  unsigned (*forms)(int phase);
 };
 ClassOps batch_class_ops_32();
 ClassOps batch_class_ops_48();

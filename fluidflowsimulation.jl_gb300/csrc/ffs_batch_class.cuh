@@ -1,7 +1,9 @@
 // One size class of the batched step (cubic side N, class index CI): compile-time FFT
-// plans, CTAs of exactly the threads each plan needs, and for N = 64, 128 the
-// register-fused x passes of velocity-only and LES runs. Included by one small translation unit per class, which
-// defines batch_class_ops_<N>().
+// plans, CTAs of exactly the threads each plan needs, every pass in each of its kernel
+// forms (line pairs or one line per thread with 8 or 4 kx lines a tile for the y/z
+// passes; for N = 64, 128 the register-fused x passes, else the generic x pass with 4
+// or 2 (y,z) lines a CTA), so that the server's autotuner can pick one per pass. Included
+// by one small translation unit per class, which defines batch_class_ops_<N>().
 #pragma once
 #include <mutex>
 #include <string>
@@ -69,16 +71,106 @@ kb_fwd_z2(const BatchInst<float>* __restrict__ B, const BatchTables* __restrict_
 
 template <int N, int CI>
 struct BatchClass {
-  static constexpr int TX = BATCH_TX, LYZ = BATCH_LYZ;
   static constexpr int tpl = ct_tpl<N>();
   static constexpr int nbuf = CtPlan<N>::np >= 3 ? 2 : 1;
   static constexpr bool FUSED = N == 64 || N == 128;    // velocity-only fused x pass
   static constexpr bool LESF = N == 64 || N == 128;     // LES fused x pass
   static constexpr bool PAIRF = N >= 64;                 // y/z passes on line pairs
-  static_assert(2 * PAIR_LP == TX, "line pairs cover the TX lines of a tile");
+  static constexpr int PT = 2 * PAIR_LP;                 // kx lines of a line-pair tile
+  using KB = void (*)(const BatchInst<float>*, const BatchTables*);
+
+  static bool yz(int ph) { return ph == BP_INV_Z || ph == BP_INV_Y || ph == BP_FWD_Y || ph == BP_FWD_Z; }
+  static unsigned forms(int ph) {
+    if (yz(ph)) return (PAIRF ? 1u << YZ_PAIR : 0u) | (1u << YZ_TX8) | (1u << YZ_TX4);
+    if (ph == BP_X) return (FUSED ? 1u << XF_FUSED : 0u) | (1u << XF_LYZ4) | (1u << XF_LYZ2);
+    if (ph == BP_X_LES) return (LESF ? 1u << XF_FUSED : 0u) | (1u << XF_LYZ4) | (1u << XF_LYZ2);
+    return 1u;
+  }
+  static int default_form(int ph) {
+    if (yz(ph)) return PAIRF ? YZ_PAIR : YZ_TX8;
+    if (ph == BP_X) return FUSED ? XF_FUSED : XF_LYZ4;
+    if (ph == BP_X_LES) return LESF ? XF_FUSED : XF_LYZ4;
+    return 0;
+  }
+
+  // the kernel of a pass in a form (every batched kernel has the same signature)
+  static KB kernel(int ph, int f) {
+    switch (ph) {
+      case BP_INV_Z:
+        if constexpr (PAIRF) { if (f == YZ_PAIR) return kb_inv_z2<N, CI>; }
+        return f == YZ_TX4 ? kb_inv_z<float, 4, CI, N> : kb_inv_z<float, 8, CI, N>;
+      case BP_INV_Y:
+        if constexpr (PAIRF) { if (f == YZ_PAIR) return kb_inv_y2<N, CI>; }
+        return f == YZ_TX4 ? kb_inv_y<float, 4, CI, N> : kb_inv_y<float, 8, CI, N>;
+      case BP_FWD_Y:
+        if constexpr (PAIRF) { if (f == YZ_PAIR) return kb_fwd_y2<N, CI>; }
+        return f == YZ_TX4 ? kb_fwd_y<float, 4, CI, N> : kb_fwd_y<float, 8, CI, N>;
+      case BP_FWD_Z:
+        if constexpr (PAIRF) { if (f == YZ_PAIR) return kb_fwd_z2<N, CI>; }
+        return f == YZ_TX4 ? kb_fwd_z<float, 4, CI, N> : kb_fwd_z<float, 8, CI, N>;
+      case BP_X:
+        if constexpr (FUSED) { if (f == XF_FUSED) return kb_x_fused<N, CI>; }
+        return f == XF_LYZ2 ? kb_x<float, false, 2, CI, N> : kb_x<float, false, 4, CI, N>;
+      case BP_X_LES:
+        if constexpr (LESF) { if (f == XF_FUSED) return kb_x_les<N, CI>; }
+        return f == XF_LYZ2 ? kb_x<float, true, 2, CI, N> : kb_x<float, true, 4, CI, N>;
+      case BP_SCALAR: return kb_scalar<float, CI>;
+      case BP_TABLE: return kb_table<float, CI>;
+      case BP_STATS: return kb_stats<float, CI>;
+      case BP_UPDATE: return kb_update<float, CI>;
+      default: return kb_finalize<float, CI>;
+    }
+  }
+
+  // CTA size, dynamic shared memory and work-item tile of a pass in a form; a
+  // compile-time plan needs exactly its threads (lines x threads per line, whole warps
+  // for the x pass)
+  static void shape(int ph, int f, int& block, size_t& smem, int& tile) {
+    const size_t cb = sizeof(cplx<float>);
+    const size_t mxp = (size_t)(N / 2 + 1) | 1;
+    auto xs = [&](int nin, int lyz) {
+      const size_t lin1 = (size_t)((nin + 1) / 2) * lyz + 1;
+      return cb * ((size_t)srows(N) * lin1 + std::max((size_t)nin * lyz * mxp, (size_t)srows(N) * lin1));
+    };
+    constexpr int NP = PAIRF ? N : 64;
+    block = 256; smem = 0; tile = 1;
+    if (yz(ph)) {
+      if (f == YZ_PAIR) {
+        block = PAIR_LP * ct_tpl<NP>();
+        smem = pair_smem<NP, PAIR_LP>() + (ph == BP_FWD_Z ? fwd_z2_aux_bytes<PT>(N) : 0);
+        tile = PT;
+      } else {
+        const int tx = f == YZ_TX4 ? 4 : 8;
+        // the forward z pass: three components together (and the i k.tau accumulators
+        // for NZR <= N rows)
+        block = (ph == BP_FWD_Z ? 3 : 1) * tx * tpl;
+        smem = ph == BP_FWD_Z ? cb * ((size_t)3 * tx * srows(N) * nbuf + (size_t)4 * N * tx)
+                              : (size_t)tx * srows(N) * cb * nbuf;
+        tile = tx;
+      }
+      return;
+    }
+    if (ph == BP_X || ph == BP_X_LES) {
+      const bool les = ph == BP_X_LES;
+      if (f == XF_FUSED) {
+        constexpr int NF = (N == 64 || N == 128) ? N : 64;
+        block = les ? XLes<NF>::NT : XFused<NF>::NT;
+        smem = les ? XLes<NF>::smem() : XFused<NF>::smem();
+        tile = les ? XLes<NF>::LYZ : XFused<NF>::LYZ;
+      } else {
+        const int lyz = f == XF_LYZ2 ? 2 : 4, pin = les ? 6 : 3;
+        block = ((pin * lyz * tpl + 31) / 32) * 32;
+        smem = xs(les ? 11 : 6, lyz);
+        tile = lyz;
+      }
+      return;
+    }
+    if (ph == BP_TABLE) block = 64;
+    if (ph == BP_FIN) block = 1024;
+  }
 
   // per-kernel limits are process-wide: only ever raised, under a lock
-  template <typename K> static int attr(K k, size_t bytes, std::string* err) {
+  static int attr(KB k, size_t bytes, std::string* err) {
     static std::mutex mu;
     std::lock_guard<std::mutex> g(mu);
     cudaFuncAttributes fa;
@@ -88,109 +180,44 @@ struct BatchClass {
     if (e != cudaSuccess) { *err = std::string("batch class attribute: ") + cudaGetErrorString(e); return FFS_ECUDA; }
     return 0;
   }
-  template <typename K> static int occ(K k, ClassLaunch* L, int ph, int sms, int cap, std::string* err) {
-    int nb = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, L->block[ph], L->smem[ph]);
-    if (e != cudaSuccess || nb < 1) { *err = "batch class kernel does not fit on an SM"; return FFS_EUNSUPPORTED; }
-    L->grid[ph] = std::min(nb * sms, cap);
-    return 0;
-  }
 
-  static int prepare(int device, int max_active, ClassLaunch* L, std::string* err) {
-    int sms = 0;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+  static int prepare(int device, int max_active, const int* form, ClassLaunch* L, std::string* err) {
+    int sms = 0, maxs = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess) {
       *err = "device attribute query failed";
       return FFS_ECUDA;
     }
-    const size_t cb = sizeof(cplx<float>);
-    const size_t mxp = (size_t)(N / 2 + 1) | 1;
-    auto xs = [&](int nin) {
-      const size_t lin1 = (size_t)((nin + 1) / 2) * LYZ + 1;
-      return cb * ((size_t)srows(N) * lin1 + std::max((size_t)nin * LYZ * mxp, (size_t)srows(N) * lin1));
-    };
-    L->block[BP_INV_Z] = L->block[BP_INV_Y] = L->block[BP_FWD_Y] = TX * tpl;
-    L->smem[BP_INV_Z] = L->smem[BP_INV_Y] = L->smem[BP_FWD_Y] = (size_t)TX * srows(N) * cb * nbuf;
-    if (FUSED) { L->block[BP_X] = XFused<FUSED ? N : 128>::NT; L->smem[BP_X] = XFused<FUSED ? N : 128>::smem(); }
-    else { L->block[BP_X] = ((3 * LYZ * tpl + 31) / 32) * 32; L->smem[BP_X] = xs(6); }
-    if (LESF) { L->block[BP_X_LES] = XLes<LESF ? N : 64>::NT; L->smem[BP_X_LES] = XLes<LESF ? N : 64>::smem(); }
-    else { L->block[BP_X_LES] = 6 * LYZ * tpl; L->smem[BP_X_LES] = xs(11); }
-    L->block[BP_FWD_Z] = 3 * TX * tpl;
-    L->smem[BP_FWD_Z] = cb * ((size_t)3 * TX * srows(N) * nbuf + (size_t)4 * N * TX);
-    if (PAIRF) {   // (the i k.tau accumulators for NZR <= N rows)
-      constexpr int NP = PAIRF ? N : 64;
-      L->block[BP_FWD_Y] = L->block[BP_FWD_Z] = L->block[BP_INV_Z] = L->block[BP_INV_Y] = PAIR_LP * ct_tpl<NP>();
-      L->smem[BP_FWD_Y] = L->smem[BP_INV_Z] = L->smem[BP_INV_Y] = pair_smem<NP, PAIR_LP>();
-      L->smem[BP_FWD_Z] = pair_smem<NP, PAIR_LP>() + fwd_z2_aux_bytes<TX>(N);
+    for (int ph = 0; ph < BP_COUNT; ++ph) {
+      const int f = form ? form[ph] : default_form(ph);
+      if (f < 0 || f > 2 || !((forms(ph) >> f) & 1u)) { *err = "batch class: no such kernel form"; return FFS_EINVAL; }
+      L->form[ph] = f;
+      shape(ph, f, L->block[ph], L->smem[ph], L->tile[ph]);
+      const KB k = kernel(ph, f);
+      cudaFuncAttributes fa;
+      if (cudaFuncGetAttributes(&fa, k) != cudaSuccess || L->block[ph] > fa.maxThreadsPerBlock ||
+          L->smem[ph] > (size_t)maxs) {
+        *err = "batch class: form does not fit";
+        return FFS_EUNSUPPORTED;
+      }
+      int rc;
+      if (L->smem[ph] && (rc = attr(k, L->smem[ph], err))) return rc;
+      int nb = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, L->block[ph], L->smem[ph]);
+      if (e != cudaSuccess || nb < 1) { *err = "batch class kernel does not fit on an SM"; return FFS_EUNSUPPORTED; }
+      // one-CTA-per-simulation passes need no more CTAs than simulations
+      L->grid[ph] = (ph == BP_SCALAR || ph == BP_FIN) ? std::min(nb * sms, max_active) : nb * sms;
     }
-    L->block[BP_SCALAR] = 256; L->block[BP_TABLE] = 64; L->block[BP_STATS] = 256; L->block[BP_UPDATE] = 256;
-    L->block[BP_FIN] = 1024;
-    L->smem[BP_SCALAR] = L->smem[BP_TABLE] = L->smem[BP_STATS] = L->smem[BP_UPDATE] = L->smem[BP_FIN] = 0;
-    int rc;
-    const int big = 1 << 30;
-    if ((rc = PAIRF ? 0 : attr(kb_inv_z<float, TX, CI, N>, L->smem[BP_INV_Z], err)) ||
-        (rc = PAIRF ? 0 : attr(kb_inv_y<float, TX, CI, N>, L->smem[BP_INV_Y], err)) ||
-        (rc = PAIRF ? 0 : attr(kb_fwd_y<float, TX, CI, N>, L->smem[BP_FWD_Y], err)) ||
-        (rc = PAIRF ? 0 : attr(kb_fwd_z<float, TX, CI, N>, L->smem[BP_FWD_Z], err)))
-      return rc;
-    if constexpr (PAIRF) {
-      if ((rc = attr(kb_fwd_y2<N, CI>, L->smem[BP_FWD_Y], err)) || (rc = attr(kb_fwd_z2<N, CI>, L->smem[BP_FWD_Z], err)) ||
-          (rc = occ(kb_fwd_y2<N, CI>, L, BP_FWD_Y, sms, big, err)) || (rc = occ(kb_fwd_z2<N, CI>, L, BP_FWD_Z, sms, big, err)) ||
-          (rc = attr(kb_inv_z2<N, CI>, L->smem[BP_INV_Z], err)) || (rc = attr(kb_inv_y2<N, CI>, L->smem[BP_INV_Y], err)) ||
-          (rc = occ(kb_inv_z2<N, CI>, L, BP_INV_Z, sms, big, err)) || (rc = occ(kb_inv_y2<N, CI>, L, BP_INV_Y, sms, big, err)))
-        return rc;
-    } else {
-      if ((rc = occ(kb_fwd_y<float, TX, CI, N>, L, BP_FWD_Y, sms, big, err)) ||
-          (rc = occ(kb_fwd_z<float, TX, CI, N>, L, BP_FWD_Z, sms, big, err)) ||
-          (rc = occ(kb_inv_z<float, TX, CI, N>, L, BP_INV_Z, sms, big, err)) ||
-          (rc = occ(kb_inv_y<float, TX, CI, N>, L, BP_INV_Y, sms, big, err)))
-        return rc;
-    }
-    if constexpr (LESF) {
-      if ((rc = attr(kb_x_les<N, CI>, L->smem[BP_X_LES], err))) return rc;
-      if ((rc = occ(kb_x_les<N, CI>, L, BP_X_LES, sms, big, err))) return rc;
-    } else {
-      if ((rc = attr(kb_x<float, true, LYZ, CI, N>, L->smem[BP_X_LES], err))) return rc;
-      if ((rc = occ(kb_x<float, true, LYZ, CI, N>, L, BP_X_LES, sms, big, err))) return rc;
-    }
-    if constexpr (FUSED) {
-      if ((rc = attr(kb_x_fused<N, CI>, L->smem[BP_X], err))) return rc;
-      if ((rc = occ(kb_x_fused<N, CI>, L, BP_X, sms, big, err))) return rc;
-    } else {
-      if ((rc = attr(kb_x<float, false, LYZ, CI, N>, L->smem[BP_X], err))) return rc;
-      if ((rc = occ(kb_x<float, false, LYZ, CI, N>, L, BP_X, sms, big, err))) return rc;
-    }
-    if ((rc = occ(kb_scalar<float, CI>, L, BP_SCALAR, sms, max_active, err)) ||
-        (rc = occ(kb_table<float, CI>, L, BP_TABLE, sms, big, err)) ||
-        (rc = occ(kb_stats<float, CI>, L, BP_STATS, sms, big, err)) ||
-        (rc = occ(kb_update<float, CI>, L, BP_UPDATE, sms, big, err)) ||
-        (rc = occ(kb_finalize<float, CI>, L, BP_FIN, sms, max_active, err)))
-      return rc;
     return 0;
   }
 
+  static void launch(const ClassLaunch& L, int ph, cudaStream_t s, const BatchInst<float>* B, const BatchTables* T) {
+    kernel(ph, L.form[ph])<<<L.grid[ph], L.block[ph], L.smem[ph], s>>>(B, T);
+  }
   static void enqueue(const ClassLaunch& L, cudaStream_t s, const BatchInst<float>* B, const BatchTables* T) {
-#define FFS_CL(PH) L.grid[PH], L.block[PH], L.smem[PH], s
-    if constexpr (PAIRF) {
-      kb_inv_z2<N, CI><<<FFS_CL(BP_INV_Z)>>>(B, T);
-      kb_inv_y2<N, CI><<<FFS_CL(BP_INV_Y)>>>(B, T);
-    } else {
-      kb_inv_z<float, TX, CI, N><<<FFS_CL(BP_INV_Z)>>>(B, T);
-      kb_inv_y<float, TX, CI, N><<<FFS_CL(BP_INV_Y)>>>(B, T);
-    }
-    if constexpr (FUSED) kb_x_fused<N, CI><<<FFS_CL(BP_X)>>>(B, T);
-    else kb_x<float, false, LYZ, CI, N><<<FFS_CL(BP_X)>>>(B, T);
-    if constexpr (LESF) kb_x_les<N, CI><<<FFS_CL(BP_X_LES)>>>(B, T);
-    else kb_x<float, true, LYZ, CI, N><<<FFS_CL(BP_X_LES)>>>(B, T);
-    if constexpr (PAIRF) kb_fwd_y2<N, CI><<<FFS_CL(BP_FWD_Y)>>>(B, T);
-    else kb_fwd_y<float, TX, CI, N><<<FFS_CL(BP_FWD_Y)>>>(B, T);
-    kb_scalar<float, CI><<<FFS_CL(BP_SCALAR)>>>(B, T);
-    kb_table<float, CI><<<FFS_CL(BP_TABLE)>>>(B, T);
-    if constexpr (PAIRF) kb_fwd_z2<N, CI><<<FFS_CL(BP_FWD_Z)>>>(B, T);
-    else kb_fwd_z<float, TX, CI, N><<<FFS_CL(BP_FWD_Z)>>>(B, T);
-    kb_stats<float, CI><<<FFS_CL(BP_STATS)>>>(B, T);
-    kb_update<float, CI><<<FFS_CL(BP_UPDATE)>>>(B, T);
-    kb_finalize<float, CI><<<FFS_CL(BP_FIN)>>>(B, T);
-#undef FFS_CL
+    for (int ph : {BP_INV_Z, BP_INV_Y, BP_X, BP_X_LES, BP_FWD_Y, BP_SCALAR, BP_TABLE, BP_FWD_Z, BP_STATS, BP_UPDATE,
+                   BP_FIN})
+      launch(L, ph, s, B, T);
   }
 };
 
@@ -199,6 +226,7 @@ struct BatchClass {
 #define FFS_DEFINE_BATCH_CLASS(NN, CI)                                                        \
   namespace ffsgpu {                                                                          \
   ClassOps batch_class_ops_##NN() {                                                           \
-    return ClassOps{NN, &BatchClass<NN, CI>::prepare, &BatchClass<NN, CI>::enqueue};          \
+    return ClassOps{NN, &BatchClass<NN, CI>::prepare, &BatchClass<NN, CI>::enqueue,           \
+                    &BatchClass<NN, CI>::launch, &BatchClass<NN, CI>::forms};                 \
   }                                                                                           \
   }

@@ -30,25 +30,42 @@ namespace ffsgpu {
     }                                                                                    \
   } while (0)
 
-// Radix plans (product == n), largest radix first; radix-3 last.
-inline bool make_plan(int n, FftPlan& P) {
-  int r[4] = {0, 0, 0, 0}, np = 0;
+// Radix plans (product == n), radix-3 last. Variant 0 is the default (largest radix
+// first, fewest passes); the others are the alternative splits the autotuner times for
+// the runtime-plan passes. Returns false for an unsupported n or variant.
+inline int plan_variants(int n) {
   switch (n) {
-    case 8: r[0] = 8; np = 1; break;
-    case 16: r[0] = 16; np = 1; break;
-    case 32: r[0] = 8; r[1] = 4; np = 2; break;
-    case 48: r[0] = 4; r[1] = 4; r[2] = 3; np = 3; break;
-    case 64: r[0] = 8; r[1] = 8; np = 2; break;
-    case 96: r[0] = 8; r[1] = 4; r[2] = 3; np = 3; break;
-    case 128: r[0] = 16; r[1] = 8; np = 2; break;
-    case 192: r[0] = 8; r[1] = 8; r[2] = 3; np = 3; break;
-    case 256: r[0] = 16; r[1] = 16; np = 2; break;
-    case 384: r[0] = 16; r[1] = 8; r[2] = 3; np = 3; break;
-    case 512: r[0] = 8; r[1] = 8; r[2] = 8; np = 3; break;
-    case 768: r[0] = 16; r[1] = 16; r[2] = 3; np = 3; break;
-    case 1024: r[0] = 16; r[1] = 8; r[2] = 8; np = 3; break;
-    default: return false;
+    case 8: return 1;
+    case 16: case 32: case 48: case 64: case 96: case 128: case 192: case 256: case 384: case 512: case 768:
+    case 1024: return n == 16 || n == 384 || n == 768 ? 2 : 3;
+    default: return 0;
   }
+}
+inline bool make_plan(int n, FftPlan& P, int variant = 0) {
+  static const int kRad[][3][4] = {
+      // n = 8 .. 1024: up to three splits each, {0} = absent
+      {{8}, {0}, {0}},                                              // 8
+      {{16}, {4, 4}, {0}},                                          // 16
+      {{8, 4}, {4, 8}, {16, 2}},                                    // 32
+      {{4, 4, 3}, {16, 3}, {8, 2, 3}},                              // 48
+      {{8, 8}, {16, 4}, {4, 16}},                                   // 64
+      {{8, 4, 3}, {4, 8, 3}, {16, 2, 3}},                           // 96
+      {{16, 8}, {8, 16}, {8, 4, 4}},                                // 128
+      {{8, 8, 3}, {16, 4, 3}, {4, 16, 3}},                          // 192
+      {{16, 16}, {16, 4, 4}, {8, 8, 4}},                            // 256
+      {{16, 8, 3}, {8, 16, 3}, {0}},                                // 384
+      {{8, 8, 8}, {16, 8, 4}, {16, 16, 2}},                         // 512
+      {{16, 16, 3}, {16, 4, 4, 3}, {0}},                            // 768
+      {{16, 8, 8}, {16, 16, 4}, {8, 8, 16}},                        // 1024
+  };
+  static const int kN[] = {8, 16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024};
+  int row = -1;
+  for (int i = 0; i < 13; ++i)
+    if (kN[i] == n) row = i;
+  if (row < 0 || variant < 0 || variant >= plan_variants(n)) return false;
+  int r[4] = {0, 0, 0, 0}, np = 0, prod = 1;
+  for (int i = 0; i < 4 && kRad[row][variant][i]; ++i) { r[i] = kRad[row][variant][i]; prod *= r[i]; ++np; }
+  if (prod != n) return false;
   P.n = n; P.np = np;
   int mx = 0, p = 1;
   for (int i = 0; i < 4; ++i) {
@@ -83,6 +100,7 @@ class Engine : public EngineBase {
   FieldList inv_fam[3]{};
   int n_fam = 0;
   int split_iz = 0;
+  int rad[3] = {0, 0, 0};     // radix-split variant of the x, y, z runtime FFT plans
   int nin = 0, nout = 0;
   int lyz = 4;
   int lio = LYZ_IO;           // (y,z) lines per CTA of the field-IO x kernels
@@ -239,6 +257,13 @@ class Engine : public EngineBase {
     if (!make_plan(p.nx, I.px) || !make_plan(p.ny, I.py) || !make_plan(p.nz, I.pz)) {
       err = "unsupported grid size: each of nx, ny, nz must be one of 8,16,32,48,64,96,128,192,256,384,512,768,1024";
       return FFS_EUNSUPPORTED;
+    }
+    if (p.radix_split < 0 || p.radix_split > 2) { err = "radix_split must be 0, 1 or 2"; return FFS_EINVAL; }
+    {   // an alternative radix split on every axis that has one
+      const int ns[3] = {p.nx, p.ny, p.nz};
+      FftPlan* pls[3] = {&I.px, &I.py, &I.pz};
+      for (int a = 0; a < 3; ++a)
+        if (p.radix_split < plan_variants(ns[a])) { make_plan(ns[a], *pls[a], p.radix_split); rad[a] = p.radix_split; }
     }
     if (!(p.lx > 0 && p.ly > 0 && p.lz > 0)) { err = "domain sizes must be positive"; return FFS_EINVAL; }
     if (!(p.cutoff > 0 && p.cutoff <= 1.0)) { err = "cutoff must be in (0, 1]"; return FFS_EINVAL; }
@@ -1319,6 +1344,7 @@ class Engine : public EngineBase {
   // per grid, model and precision for the process, so engines of the same shape tune once.
   struct TuneChoice {
     int txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, split_iz;
+    int rad[3];
     std::string report;
   };
   static std::mutex& tune_mu() { static std::mutex m; return m; }
@@ -1338,6 +1364,8 @@ class Engine : public EngineBase {
         txy = c.txy; use_ct = c.use_ct; lyz = c.lyz; xfused = c.xfused; txz = c.txz; zseq = c.zseq;
         use_ct_z = c.use_ct_z; pair_z = c.pair_z; v_iz = c.v_iz; v_iy = c.v_iy; v_fy = c.v_fy;
         split_iz = c.split_iz;
+        for (int a = 0; a < 3; ++a) rad[a] = c.rad[a];
+        make_plan(P.nx, I.px, rad[0]); make_plan(P.ny, I.py, rad[1]); make_plan(P.nz, I.pz, rad[2]);
         tune_report = c.report + " (cached)";
         compute_smem();
         return set_smem(err);
@@ -1463,6 +1491,44 @@ class Engine : public EngineBase {
           }
       txz = bt; zseq = bq; use_ct_z = bc; pair_z = bp;
     }
+    // radix splits of the runtime FFT plans, per axis, timed on the passes that run them
+    // (every pass in FP64; in FP32 the ones without a compile-time plan)
+    if (!rc) {
+      const int pin = (nin + 1) / 2;
+      const int ns[3] = {P.nx, P.ny, P.nz};
+      FftPlan* pls[3] = {&I.px, &I.py, &I.pz};
+      const char* an[3] = {"x", "y", "z"};
+      for (int ax = 0; ax < 3 && !rc; ++ax) {
+        const bool used = ax == 0 ? xfused == 0 : (ax == 1 ? cty() == 0 : (ctz() == 0 || ctzu() == 0));
+        const int nv = plan_variants(ns[ax]);
+        if (!used || nv < 2) continue;
+        const FftPlan keep = *pls[ax];
+        float bms = 1e30f;
+        int bv = rad[ax];
+        for (int v = 0; v < nv && !rc; ++v) {
+          FftPlan c;
+          if (!make_plan(ns[ax], c, v)) continue;
+          // the launch shapes stay within the thread budget with this plan's threads per line
+          const int tpl_yz = std::max(ax == 1 ? c.tpl : I.py.tpl, ax == 2 ? c.tpl : I.pz.tpl);
+          if (ax == 0 && (pin * lyz * c.tpl > MAXT || 2 * lio * c.tpl > MAXT)) continue;
+          if (ax > 0 && (txy * tpl_yz > MAXT || (ax == 2 && zu_lines() * c.tpl > MAXT))) continue;
+          *pls[ax] = c;
+          float ms = 0.f;
+          if (ax == 0) rc = timed([&] { launch_x(); }, ms);
+          else if (ax == 1) rc = timed([&] { launch_inv_y(inv_list); launch_fwd_y(fwd_list); }, ms);
+          else rc = timed([&] { launch_inv_z_step(); launch_zu(0); }, ms);
+          char rs[32];
+          int o = 0;
+          for (int i = 0; i < c.np; ++i) o += snprintf(rs + o, sizeof(rs) - o, i ? "x%d" : "%d", c.r[i]);
+          snprintf(line, sizeof(line), "radix_%s[%s]=%.4fms ", an[ax], rs, ms);
+          rep += line;
+          if (ms < bms) { bms = ms; bv = v; }
+        }
+        *pls[ax] = keep;
+        rad[ax] = bv;
+        make_plan(ns[ax], *pls[ax], bv);
+      }
+    }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
@@ -1471,13 +1537,15 @@ class Engine : public EngineBase {
              xfused ? "fused" : "lyz", xfused ? xfused : lyz, txz, zseq ? "seq" : "3c",
              use_ct_z ? (zpair() ? "ct2" : "ct") : "rt");
     rep += line;
+    snprintf(line, sizeof(line), ", radix variants x%d y%d z%d", rad[0], rad[1], rad[2]);
+    rep += line;
     tune_report = rep;
     compute_smem();
     if ((rc = set_smem(err))) return rc;
     {
       std::lock_guard<std::mutex> g(tune_mu());
       tune_cache()[key] = TuneChoice{txy, use_ct, lyz, xfused, txz, zseq, use_ct_z, pair_z, v_iz, v_iy, v_fy, split_iz,
-                                     rep};
+                                     {rad[0], rad[1], rad[2]}, rep};
     }
     return reset_state(err);
   }
@@ -1523,6 +1591,7 @@ class Engine : public EngineBase {
     g->nx = P.nx; g->ny = P.ny; g->nz = P.nz;
     g->nin = inv_list.n; g->nout = fwd_list.n;
     g->kx_tiles = I.KXP / txy;
+    g->kxp = I.KXP;
     g->nyr = I.NYR;
     g->yz_groups = P.ny * P.nz / lyz;
     g->fwd_z_tiles = I.KXP / txz;

@@ -27,6 +27,7 @@ struct BatchGeom {
   int nparts, upd_blocks; // stats and update CTAs
   int txy, txz, lyz;
   int xfused;             // n of the engine's register-fused x pass (0: none)
+  int kxp;                // padded kx row length (tiles of a size class: kxp / tile)
 };
 
 class EngineBase {

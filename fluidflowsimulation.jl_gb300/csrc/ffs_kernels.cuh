@@ -1680,7 +1680,7 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
   S->umax_bits = 0ull; S->rhomax_bits = 0ull;
 }
 template <typename T>
-__global__ void k_finalize(Inst<T> I, int mode, int nparts) {
+__global__ void __launch_bounds__(1024) k_finalize(Inst<T> I, int mode, int nparts) {
   b_finalize<T>(I, mode, nparts, Blk::here());
 }
 

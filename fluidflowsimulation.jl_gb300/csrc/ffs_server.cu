@@ -12,12 +12,16 @@
 //             -> simulations that reached nt leave the tables; after the next replay has
 //                been enqueued, their results are read on their own streams (ordered by
 //                an event after their last step) and the engine returns to the pool
+//   start     -> with cfg.autotune, each size class's passes are timed in every kernel
+//                form on probe simulations and the fastest form per pass is kept; the
+//                work tables are cut in the tiles of the chosen forms
 //             -> every kHealthEvery replays a one-CTA kernel copies each simulation's
 //                error flag (non-finite value seen by its update) to pinned host memory;
 //                the host reads the copy one interval later and retires a diverged
 //                simulation at once with FFS_ENAN, freeing its slot; cancelled requests
 //                (ffs_cancel) leave the queue or the batch the same way
 #include <cuda_runtime.h>
+#include <math.h>
 #include <string.h>
 
 #include <algorithm>
@@ -102,6 +106,44 @@ const int kSizes[] = {8, 16, 32, 48, 64, 96, 128};
 
 inline int r32(int x) { return ((x + 31) / 32) * 32; }
 
+// Work items of one pass of one simulation (k: its parameter block), in tiles of `tile`
+// kx lines (y/z passes) or (y,z) lines (x passes).
+void append_items(int ph, int tile, const BatchGeom& g, int k, std::vector<WorkItem>& v) {
+  const int kt = g.kxp / tile;
+  switch (ph) {
+    case BP_INV_Z:
+      for (int f = 0; f < g.nin; ++f)
+        for (int t = 0; t < kt; ++t)
+          for (int jc = 0; jc < g.nyr; ++jc) v.push_back({k, f, t, jc});
+      break;
+    case BP_INV_Y:
+      for (int f = 0; f < g.nin; ++f)
+        for (int t = 0; t < kt; ++t)
+          for (int z = 0; z < g.nz; ++z) v.push_back({k, f, t, z});
+      break;
+    case BP_X:
+    case BP_X_LES:
+      for (int b = 0; b < g.ny * g.nz / tile; ++b) v.push_back({k, b, 0, 0});
+      break;
+    case BP_FWD_Y:
+      for (int f = 0; f < g.nout; ++f)
+        for (int t = 0; t < kt; ++t)
+          for (int z = 0; z < g.nz; ++z) v.push_back({k, f, t, z});
+      break;
+    case BP_FWD_Z:
+      for (int t = 0; t < kt; ++t)
+        for (int jc = 0; jc < g.nyr; ++jc) v.push_back({k, t, jc, 0});
+      break;
+    default:
+      break;
+  }
+}
+
+// size-class tuning results of this process: (device, side, max_active) -> forms, report
+struct ClassTune { int form[BP_COUNT]; std::string report; };
+std::mutex& class_tune_mu() { static std::mutex m; return m; }
+std::map<std::string, ClassTune>& class_tune_cache() { static std::map<std::string, ClassTune> c; return c; }
+
 double now_s(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
@@ -153,6 +195,7 @@ class Server {
   unsigned* d_health = nullptr;             // [max_active] error flags of the last snapshot
   unsigned* h_health = nullptr;             // pinned copy
   cudaEvent_t health_ev = nullptr;
+  std::string tune_report;                  // forms picked per size class and the timings
   std::vector<uint64_t> health_job;         // job id each slot held when the snapshot was taken
   bool health_pending = false;
   int64_t health_at = 0;                    // batch step of the pending snapshot
@@ -164,6 +207,7 @@ class Server {
     if (cfg.max_n <= 0 || cfg.max_n > 128) { err = "max_n must be in 1..128"; return FFS_EINVAL; }
     if (cfg.max_active <= 0) { err = "max_active must be positive"; return FFS_EINVAL; }
     if (cfg.memory_budget <= 0) { err = "memory_budget must be positive"; return FFS_EINVAL; }
+    if (cfg.class_forms < 0 || cfg.class_forms > 2) { err = "class_forms must be 0, 1 or 2"; return FFS_EINVAL; }
     t0 = std::chrono::steady_clock::now();
     int rc = setup();
     if (rc) {
@@ -256,10 +300,23 @@ class Server {
     // size classes with compile-time shapes
     cls[1] = batch_class_ops_32(); cls[2] = batch_class_ops_48(); cls[3] = batch_class_ops_64();
     cls[4] = batch_class_ops_96(); cls[5] = batch_class_ops_128();
+    for (int ph = 0; ph < BP_COUNT; ++ph)   // the generic class's tiles
+      cl[0].tile[ph] = (ph == BP_X || ph == BP_X_LES) ? LYZB : (ph == BP_INV_Z || ph == BP_INV_Y || ph == BP_FWD_Y ||
+                                                                   ph == BP_FWD_Z) ? TXB : 1;
     for (int c = 1; c < BATCH_NCLASS; ++c) {
       if (cls[c].n > cfg.max_n) continue;
       std::string e;
-      if ((rc = cls[c].prepare(cfg.device, cfg.max_active, &cl[c], &e))) { terr = e; return rc; }
+      int form[BP_COUNT] = {0};
+      const bool forced = !cfg.autotune && (cfg.class_forms == 1 || cfg.class_forms == 2);
+      if (forced)
+        for (int ph : {BP_INV_Z, BP_INV_Y, BP_FWD_Y, BP_FWD_Z, BP_X, BP_X_LES})
+          form[ph] = (ph == BP_X || ph == BP_X_LES) ? (cfg.class_forms == 1 ? XF_LYZ4 : XF_LYZ2)
+                                                    : (cfg.class_forms == 1 ? YZ_TX8 : YZ_TX4);
+      if (cfg.autotune && (rc = tune_class(c, form))) return rc;
+      if ((rc = cls[c].prepare(cfg.device, cfg.max_active, (cfg.autotune || forced) ? form : nullptr, &cl[c], &e))) {
+        terr = e;
+        return rc;
+      }
     }
     for (int c = 0; c < BATCH_NCLASS; ++c) SV_CK(cudaStreamCreateWithFlags(&cs[c], cudaStreamNonBlocking));
     for (int c = 0; c <= BATCH_NCLASS; ++c) SV_CK(cudaEventCreateWithFlags(&cev[c], cudaEventDisableTiming));
@@ -306,6 +363,148 @@ class Server {
     cudaError_t e = cudaStreamEndCapture(S, &graph);
     if (e != cudaSuccess) { terr = std::string("graph capture: ") + cudaGetErrorString(e); return FFS_ECUDA; }
     SV_CK(cudaGraphInstantiate(&gexec, graph, 0));
+    return 0;
+  }
+
+  // Autotuner of one size class: probe simulations of the class's side (enough that a
+  // pass's work is close to one 128^3 simulation's), then per tunable pass every kernel
+  // form timed on them (work tables cut in that form's tiles, the other passes at their
+  // current picks); the fastest form stays. Velocity-only probes time the y/z passes and
+  // the x pass, LES probes the LES x pass. The probes are freed afterwards; the choice is
+  // kept for the process.
+  int tune_class(int c, int form[BP_COUNT]) {
+    const ClassOps& ops = cls[c];
+    const int n = ops.n;
+    std::string e;
+    ClassLaunch L{};
+    int rc = ops.prepare(cfg.device, cfg.max_active, nullptr, &L, &e);
+    if (rc) { terr = e; return rc; }
+    for (int ph = 0; ph < BP_COUNT; ++ph) form[ph] = L.form[ph];
+    const std::string key = std::to_string(cfg.device) + ":" + std::to_string(n) + ":" + std::to_string(cfg.max_active);
+    {
+      std::lock_guard<std::mutex> g(class_tune_mu());
+      auto it = class_tune_cache().find(key);
+      if (it != class_tune_cache().end()) {
+        for (int ph = 0; ph < BP_COUNT; ++ph) form[ph] = it->second.form[ph];
+        tune_report += it->second.report + " (cached); ";
+        return 0;
+      }
+    }
+    const int want = std::max(1, (128 / n) * (128 / n) * (128 / n));
+    const size_t N = (size_t)n * n * n;
+    std::vector<double> u(3 * N);
+    for (int z = 0; z < n; ++z)   // a smooth divergence-free field: (sin y, sin z, sin x)
+      for (int y = 0; y < n; ++y)
+        for (int x = 0; x < n; ++x) {
+          const size_t i = ((size_t)z * n + y) * n + x;
+          u[i] = sin(2 * M_PI * y / n); u[N + i] = sin(2 * M_PI * z / n); u[2 * N + i] = sin(2 * M_PI * x / n);
+        }
+    std::vector<std::unique_ptr<EngineBase>> probes;
+    std::vector<BatchGeom> geo[2];
+    std::vector<BI> hb;
+    for (int les = 0; les < 2; ++les) {
+      ffs_params p;
+      ffs_params_default(&p);
+      p.nx = p.ny = p.nz = n; p.precision = FFS_FP32; p.integrator = FFS_AB3; p.variable_dt = 1; p.cfl = 0.2;
+      p.nu = 1e-3; p.dt_stat = p.dt_spec = 1 << 30; p.les = les; p.device = cfg.device;
+      const int64_t pb = std::max<int64_t>(1, estimate_bytes_f32(p));
+      const int64_t fit = std::max<int64_t>(1, cfg.memory_budget / 4 / pb);
+      const int k = (int)std::min<int64_t>({(int64_t)want, (int64_t)cfg.max_active, (int64_t)64, fit});
+      for (int i = 0; i < k; ++i) {
+        std::unique_ptr<EngineBase> eng(make_engine_f32());
+        BatchGeom g{};
+        BI b{};
+        if ((rc = eng->create(p, e)) || (rc = eng->set_fields(u.data(), u.data() + N, u.data() + 2 * N, nullptr, 0, e)) ||
+            (rc = eng->initialize(e)) || (rc = eng->batch_export(&b, sizeof(BI), &g, e))) {
+          terr = "size class tuning: " + e;
+          return rc;
+        }
+        geo[les].push_back(g);
+        hb.push_back(b);
+        probes.push_back(std::move(eng));
+      }
+    }
+    const int base[2] = {0, (int)geo[0].size()};
+    BI* d_b = nullptr;
+    BatchTables* d_t = nullptr;
+    WorkItem* d_it = nullptr;
+    size_t cap = 0;
+    cudaEvent_t a = nullptr, b = nullptr;
+    auto cleanup = [&] {
+      if (d_b) cudaFree(d_b);
+      if (d_t) cudaFree(d_t);
+      if (d_it) cudaFree(d_it);
+      if (a) cudaEventDestroy(a);
+      if (b) cudaEventDestroy(b);
+    };
+    auto ck = [&](cudaError_t r, const char* what) {
+      if (r != cudaSuccess && !rc) { terr = std::string("size class tuning: ") + what + ": " + cudaGetErrorString(r); rc = FFS_ECUDA; }
+      return r == cudaSuccess;
+    };
+    std::string rep = "n=" + std::to_string(n) + " (" + std::to_string(geo[0].size()) + "+" +
+                      std::to_string(geo[1].size()) + " probes):";
+    if (ck(cudaMalloc(&d_b, sizeof(BI) * hb.size()), "malloc") && ck(cudaMalloc(&d_t, sizeof(BatchTables)), "malloc") &&
+        ck(cudaMemcpy(d_b, hb.data(), sizeof(BI) * hb.size(), cudaMemcpyHostToDevice), "upload") &&
+        ck(cudaEventCreate(&a), "event") && ck(cudaEventCreate(&b), "event")) {
+      const char* pn[BP_COUNT] = {"inv_z", "inv_y", "x", "x_les", "fwd_y", "", "", "fwd_z", "", "", ""};
+      const char* fn_yz[3] = {"pair", "tx8", "tx4"};
+      const char* fn_x[3] = {"fused", "lyz4", "lyz2"};
+      for (int ph : {BP_INV_Z, BP_INV_Y, BP_X, BP_FWD_Y, BP_FWD_Z, BP_X_LES}) {
+        const unsigned m = ops.forms(ph);
+        if (rc || __builtin_popcount(m) < 2) continue;
+        const int set = ph == BP_X_LES ? 1 : 0;
+        float best = 1e30f;
+        int bf = form[ph];
+        for (int f = 0; f < 3 && !rc; ++f) {
+          if (!((m >> f) & 1u)) continue;
+          int fc[BP_COUNT];
+          for (int q = 0; q < BP_COUNT; ++q) fc[q] = form[q];
+          fc[ph] = f;
+          ClassLaunch Lc{};
+          if (ops.prepare(cfg.device, cfg.max_active, fc, &Lc, &e)) continue;   // form does not fit
+          std::vector<WorkItem> items;
+          for (size_t i = 0; i < geo[set].size(); ++i) append_items(ph, Lc.tile[ph], geo[set][i], base[set] + (int)i, items);
+          if (items.size() > cap) {
+            if (d_it) cudaFree(d_it);
+            d_it = nullptr;
+            cap = items.size();
+            if (!ck(cudaMalloc(&d_it, sizeof(WorkItem) * cap), "malloc")) break;
+          }
+          BatchTables t{};
+          t.tab[c][ph] = d_it;
+          t.n[c][ph] = (int)items.size();
+          if (!ck(cudaMemcpy(d_it, items.data(), sizeof(WorkItem) * items.size(), cudaMemcpyHostToDevice), "upload") ||
+              !ck(cudaMemcpy(d_t, &t, sizeof(t), cudaMemcpyHostToDevice), "upload"))
+            break;
+          const int reps = n >= 96 ? 10 : 20;
+          ops.launch(Lc, ph, S, d_b, d_t);
+          ck(cudaEventRecord(a, S), "event");
+          for (int r = 0; r < reps; ++r) ops.launch(Lc, ph, S, d_b, d_t);
+          ck(cudaEventRecord(b, S), "event");
+          ck(cudaEventSynchronize(b), "synchronize");
+          ck(cudaGetLastError(), "launch");
+          float ms = 0.f;
+          ck(cudaEventElapsedTime(&ms, a, b), "timing");
+          ms /= reps;
+          char line[96];
+          snprintf(line, sizeof(line), " %s[%s]=%.4fms", pn[ph], (ph == BP_X || ph == BP_X_LES) ? fn_x[f] : fn_yz[f], ms);
+          rep += line;
+          if (ms < best) { best = ms; bf = f; }
+        }
+        form[ph] = bf;
+      }
+    }
+    cleanup();
+    probes.clear();
+    if (rc) return rc;
+    rep += " ->";
+    for (int ph : {BP_INV_Z, BP_INV_Y, BP_X, BP_X_LES, BP_FWD_Y, BP_FWD_Z}) rep += " " + std::to_string(form[ph]);
+    tune_report += rep + "; ";
+    std::lock_guard<std::mutex> g(class_tune_mu());
+    ClassTune ct;
+    for (int ph = 0; ph < BP_COUNT; ++ph) ct.form[ph] = form[ph];
+    ct.report = rep;
+    class_tune_cache()[key] = ct;
     return 0;
   }
 
@@ -653,22 +852,12 @@ class Server {
       const Slot& s = slots[k];
       if (!s.job || s.retiring) continue;
       const BatchGeom& g = s.g;
-      auto& it = items[class_of(g)];
-      for (int f = 0; f < g.nin; ++f)
-        for (int t = 0; t < g.kx_tiles; ++t) {
-          for (int jc = 0; jc < g.nyr; ++jc) it[BP_INV_Z].push_back({k, f, t, jc});
-          for (int z = 0; z < g.nz; ++z) it[BP_INV_Y].push_back({k, f, t, z});
-        }
-      auto& xt = it[g.les ? BP_X_LES : BP_X];
-      const int xg = (class_of(g) != 0 && fused_x(g)) ? g.ny * g.nz / 8 : g.yz_groups;   // fused x: 8 lines per CTA
-      for (int b = 0; b < xg; ++b) xt.push_back({k, b, 0, 0});
-      for (int f = 0; f < g.nout; ++f)
-        for (int t = 0; t < g.kx_tiles; ++t)
-          for (int z = 0; z < g.nz; ++z) it[BP_FWD_Y].push_back({k, f, t, z});
+      const int c = class_of(g);
+      auto& it = items[c];
+      const int xph = g.les ? BP_X_LES : BP_X;
+      for (int ph : {(int)BP_INV_Z, (int)BP_INV_Y, xph, (int)BP_FWD_Y, (int)BP_FWD_Z}) append_items(ph, cl[c].tile[ph], g, k, it[ph]);
       it[BP_SCALAR].push_back({k, 0, 0, 0});
       for (int b = 0; b < g.table_blocks; ++b) it[BP_TABLE].push_back({k, b, g.table_blocks, 0});
-      for (int t = 0; t < g.fwd_z_tiles; ++t)
-        for (int jc = 0; jc < g.nyr; ++jc) it[BP_FWD_Z].push_back({k, t, jc, 0});
       for (int b = 0; b < g.nparts; ++b) it[BP_STATS].push_back({k, b, g.nparts, 0});
       for (int b = 0; b < g.upd_blocks; ++b) it[BP_UPDATE].push_back({k, b, g.upd_blocks, 0});
       it[BP_FIN].push_back({k, 0, 0, 0});
@@ -1012,6 +1201,16 @@ int ffs_server_pause(ffs_server* s, int32_t paused) { FFS_SERVER_GUARD(s->s.paus
 int ffs_server_stats(ffs_server* s, ffs_server_info* o) {
   if (!o) return FFS_EINVAL;
   FFS_SERVER_GUARD(s->s.stats(o))
+}
+int64_t ffs_server_tuning(ffs_server* s, char* buf, int64_t len) {
+  if (!s) return FFS_EINVAL;
+  const std::string& r = s->s.tune_report;
+  if (buf && len > 0) {
+    const size_t m = std::min<size_t>((size_t)len - 1, r.size());
+    memcpy(buf, r.data(), m);
+    buf[m] = 0;
+  }
+  return (int64_t)r.size();
 }
 const char* ffs_server_last_error(ffs_server* s) {
   if (s) g_server_err = s->s.last_error();

@@ -37,7 +37,7 @@ mutable struct FFSParams
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
-    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64
+    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; radix_split::Int32
     FFSParams() = new()
 end
 

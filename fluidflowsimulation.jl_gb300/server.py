@@ -24,11 +24,14 @@ STATUS = {0: "done", _lib.FFS_QUEUED: "queued", _lib.FFS_RUNNING: "running"}
 class Server:
     """Python mirror of ffs_server: submit / poll / wait / results."""
 
-    def __init__(self, device: int = 0, memory_budget: int = 120 << 30, max_active: int = 256, max_n: int = 128):
+    def __init__(self, device: int = 0, memory_budget: int = 120 << 30, max_active: int = 256, max_n: int = 128,
+                 autotune: bool = False, class_forms: int = 0):
         self.L = _lib.load()
         cfg = _lib.FFSServerCfg()
         self.L.ffs_server_default(ctypes.byref(cfg))
         cfg.device, cfg.memory_budget, cfg.max_active, cfg.max_n = device, int(memory_budget), max_active, max_n
+        cfg.autotune = int(autotune)
+        cfg.class_forms = int(class_forms)
         h = ctypes.c_void_p()
         rc = self.L.ffs_server_create(ctypes.byref(cfg), ctypes.byref(h))
         if rc != 0:
@@ -100,6 +103,14 @@ class Server:
     def release(self, rid: int) -> None:
         self._check(self.L.ffs_release(self.h, rid))
         self._shape.pop(rid, None)
+
+    @property
+    def tuning(self) -> str:
+        """The size-class autotuner's report ('' without autotune)."""
+        n = self._check(self.L.ffs_server_tuning(self.h, None, 0))
+        buf = ctypes.create_string_buffer(n + 1)
+        self.L.ffs_server_tuning(self.h, buf, n + 1)
+        return buf.value.decode()
 
     def info(self) -> dict:
         i = _lib.FFSServerInfo()

@@ -110,6 +110,9 @@ typedef struct ffs_params {
                                   carries the Stats_fil.txt row (quadratic sums weighted by the Gaussian
                                   filter squared, D = 2 pi lx nf / nx) and the spectrum records the
                                   *_fil spectra; 0: off */
+  int32_t radix_split;         /* runtime FFT plans: 0 the default radix split of each axis, k = 1, 2 the
+                                  k-th alternative split (where the length has one; the autotuner times
+                                  them and keeps the fastest per axis) */
 } ffs_params;
 
 #define FFS_PF_NONE 0
@@ -284,6 +287,11 @@ typedef struct ffs_server_cfg {
   int64_t memory_budget;   /* device bytes the simulations may hold (admission limit) */
   int32_t max_active;      /* simulations advanced together at most */
   int32_t max_n;           /* largest grid side accepted (<= 128) */
+  int32_t autotune;        /* 1: at create, time every kernel form of each size class's passes on
+                              probe simulations and keep the fastest per pass (ffs_server_tuning) */
+  int32_t class_forms;     /* without autotune: 0 the default forms; 1 every size class's y/z passes one
+                              line per thread with 8 kx lines a tile and its x passes generic with 4
+                              (y,z) lines; 2 the same with 4 kx lines and 2 (y,z) lines */
 } ffs_server_cfg;
 
 typedef struct ffs_request {
@@ -337,6 +345,9 @@ int ffs_cancel(ffs_server* s, uint64_t id);
 /* Hold (1) or resume (0) admission: queued requests wait while the batch keeps running. */
 int ffs_server_pause(ffs_server* s, int32_t paused);
 int ffs_server_stats(ffs_server* s, ffs_server_info* out);
+/* The size-class autotuner's report (cfg.autotune): per class, every timed kernel form of
+ * each pass and the forms kept. Copies up to len-1 characters; returns the full length. */
+int64_t ffs_server_tuning(ffs_server* s, char* buf, int64_t len);
 const char* ffs_server_last_error(ffs_server* s);
 /* Stop the server (unfinished requests are dropped) and free its GPU memory. */
 void ffs_server_destroy(ffs_server* s);

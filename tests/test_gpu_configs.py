@@ -9,6 +9,12 @@ grid sizes (through the C ABI).
   steps plus the run's tail (FluidFlowSimulation.jl:46-49): all 26 Stats, Scales and
   Numbers rows <= 1e-10 against the committed oracle fixture
   (tests/golden/make_config_golden.py), the final state <= 1e-12.
+- DNS 1024^3 + hyperviscosity, FP32 (the large single-instance configuration): three
+  steps of the FP32 chosen form against the FP64 plain form of the same engine on the
+  same initial modes (FP32 rows within 1e-5 of FP64 on the energy, dissipation and
+  hyperviscous columns, the same dt to 1e-5), the band forcing's injected power equal
+  to forcingPower, every stats column finite. The oracle cannot run this size; the FP64
+  engine is the one pinned to it at 256^3 above.
 - Adaptive-dt ETD (the stratified LES configuration's integrator): with the engine's own
   dt sequence fed to the oracle (Delta t injection), fields <= 1e-12 and Stats rows
   <= 1e-10, at 32^3 and at the configuration's 128^3 with Smagorinsky LES and Boussinesq
@@ -96,6 +102,45 @@ def test_dns256_fp32_error_against_oracle(gpu_pkg, dns256_oracle):
     for col in (11, 14, 19):   # k, diss, tdiss
         assert np.abs(rows[:, col] - want[:, col]).max() <= 1e-5 * np.abs(want[:, col]).max()
     sim.close()
+
+
+# ---------------------------------------------------------------------------- DNS 1024^3
+def dns1024_global():
+    return {"nx": "1024", "ny": "1024", "nz": "1024", "xDomainSize": "1.0", "yDomainSize": "1.0",
+            "zDomainSize": "1.0", "kinematicViscosity": "2e-4", "dtStat": "1", "dtSpec": "1000000000",
+            "writeTime": "1000000000", "velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "true",
+            "cfl": "0.5", "dt": "0.0001", "forcing": "isotropicBand", "forcingPower": "0.1", "forcingKf": "2.5",
+            "hyperViscosity": "true", "hyperViscosityCoefficient": "1e-12", "hyperViscosityM": "2"}
+
+
+def test_dns1024_fp32_against_fp64_engine(gpu_pkg):
+    from importlib import import_module
+    f = import_module(gpu_pkg.__name__ + ".fields")
+    n, kc, steps = 1024, 48, 3
+    box = f.random_spectrum_modes(n, 8.0, 4001, kc)
+    d = dns1024_global()
+    res = {}
+    for prec in ("FP32", "FP64"):   # one at a time: ~45 GB and ~90 GB of device memory
+        sim = gpu_pkg.Simulation.from_global(d, precision=prec)
+        for c in range(3):
+            sim.set_spectral(c, f.embed_half_spectrum(box[c], n, kc))
+        sim.initialize()
+        sim.advance_in_time(steps)
+        res[prec] = (sim.records(), sim.header.split(","), sim.dt, sim.iteration)
+        sim.close()
+    r32, names, dt32, it32 = res["FP32"]
+    r64, _, dt64, it64 = res["FP64"]
+    assert it32 == it64 == steps and r32.shape == r64.shape and r32.shape[0] == steps   # rows at 0, 1, 2
+    assert np.isfinite(r32).all() and np.isfinite(r64).all()
+    assert dt32 == pytest.approx(dt64, rel=1e-5)
+    col = {k: i for i, k in enumerate(names)}
+    for k in ("u1p2", "u2p2", "u3p2", "k", "dissh", "dissv", "diss", "hdiss", "tdiss"):
+        a, b = r32[:, col[k]], r64[:, col[k]]
+        assert np.abs(a - b).max() <= 1e-5 * np.abs(b).max(), k
+    # constant-power band forcing: the injected power of each step is forcingPower (up to
+    # the O(dt) term of the increment's own energy)
+    tp = r64[:, col["tp"]]
+    assert np.allclose(tp, 0.1, rtol=1e-2), tp
 
 
 # ---------------------------------------------------------------------------- Taylor-Green 64^3

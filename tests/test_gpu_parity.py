@@ -329,3 +329,52 @@ def test_current_stats_and_spectrum(gpu_pkg, precision, tol):
     assert rel(H, sp["u.specH"]) <= tol
     assert rel(V, sp["u_h.specV"] + sp["u_v.specV"]) <= tol
     sim.close()
+
+
+# Every alternative radix split the autotuner may pick for the runtime-plan passes
+# (ffs_params.radix_split forces it on every axis that has one), FP64 against the oracle
+# at the usual bars; non-cubic grids mix axes with and without the split.
+RADIX_CASES = [(gdict(32), 1), (gdict(32), 2), (gdict(48, "ETD3rdO"), 1), (gdict(48), 2),
+               (gdict(64, lesModel="Smagorinsky"), 1), (gdict(64), 2), (gdict(96, "ETD3rdO", dt="0.005"), 1),
+               (gdict(96), 2), (gdict(128), 1), (gdict(128, "ETD3rdO", dt="0.005"), 2), (gdict(32, ny=48, nz=64), 2),
+               (gdict(16, ny=32, nz=48), 1)]
+
+
+@pytest.mark.parametrize("case", range(len(RADIX_CASES)))
+def test_radix_split_parity(gpu_pkg, case):
+    d, split = RADIX_CASES[case]
+    u, rho = make_ic(gpu_pkg, d)
+    p = gpu_pkg.parameters(d, precision="FP64")
+    p.radix_split = split
+    sim = gpu_pkg.Simulation(p)
+    sim.set_fields(*u, rho)
+    sim.initialize()
+    sim.advance_in_time(10)
+    ref = OracleSimulation(Params.from_global(d), u, rho)
+    ref.initialize()
+    ref.run(10)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= FP64_FIELD_TOL, (case, c)
+    rows, rr = sim.stats_rows(), np.array(ref.stats_rows)
+    scale = np.maximum(np.abs(rr), 1e-6 * np.abs(rr).max())
+    assert (np.abs(rows - rr) / scale).max() <= FP64_STATS_TOL
+    sim.close()
+
+
+def test_radix_split_fp32_runtime_plans(gpu_pkg):
+    """FP32 with runtime-plan kernels only (kernel_variant 1) on an alternative split."""
+    d = gdict(128)
+    u, rho = make_ic(gpu_pkg, d)
+    p = gpu_pkg.parameters(d, precision="FP32")
+    p.kernel_variant = 1
+    p.radix_split = 1
+    sim = gpu_pkg.Simulation(p)
+    sim.set_fields(*u, rho)
+    sim.initialize()
+    sim.advance_in_time(10)
+    ref = OracleSimulation(Params.from_global(d), u, rho)
+    ref.initialize()
+    ref.run(10)
+    for c in range(3):
+        assert rel(sim.spectral(c), ref.u[c]) <= FP32_FIELD_TOL
+    sim.close()

@@ -285,3 +285,47 @@ def test_cancel_queued_and_running_requests(gpu_pkg):
         assert srv.wait(c, timeout=600)["status"] == 0
         with pytest.raises(pkg.FFSError):
             srv.cancel(c)                              # already finished
+
+
+# The size classes' kernel forms (ffs_server_cfg.class_forms / autotune): every form of
+# every pass computes the same step. Forms 1 and 2 force the one-line-per-thread y/z
+# kernels (8 and 4 kx lines a tile) and the generic x passes (4 and 2 lines) on every
+# class; the autotuned server keeps the fastest form per pass. Each result is compared
+# with the default forms' (FP32 rounding: 1e-5) and with the FP64 oracle (1e-4).
+FORM_MIX = [MIX[0], MIX[1], MIX[2], MIX[3], MIX[6], MIX[7]]
+
+
+def _run_mix(pkg, mix, **kw):
+    us = [fields_of(pkg, c) for c in mix]
+    out = []
+    with pkg.Server(max_active=16, **kw) as srv:
+        report = srv.tuning
+        ids = [submit_case(srv, c, u) for c, u in zip(mix, us)]
+        for rid in ids:
+            r = srv.wait(rid, timeout=600)
+            assert r["status"] == 0, r
+            out.append((srv.fields(rid), srv.stats_rows(rid)))
+    return us, out, report
+
+
+@pytest.mark.parametrize("kw", [dict(class_forms=1), dict(class_forms=2), dict(autotune=True)])
+def test_class_forms_compute_the_same_step(gpu_pkg, kw):
+    us, base, _ = _run_mix(gpu_pkg, FORM_MIX)
+    _, got, report = _run_mix(gpu_pkg, FORM_MIX, **kw)
+    if kw.get("autotune"):
+        for n in (32, 48, 64, 96, 128):
+            assert f"n={n} " in report, report
+    for case, u, (fb, sb), (fg, sg) in zip(FORM_MIX, us, base, got):
+        for c in range(3):
+            assert np.linalg.norm(fg[c] - fb[c]) <= 1e-5 * np.linalg.norm(fb[c]), (case, c)
+        assert sg.shape == sb.shape
+        assert np.allclose(sg, sb, rtol=1e-5, atol=1e-6 * np.abs(sb).max()), case
+    # against the FP64 oracle
+    for case, u, (fg, _) in list(zip(FORM_MIX, us, got))[:3]:
+        n, les, integ, adaptive, nt, seed = case
+        ref = OracleSimulation(Params.from_global(gdict(n, les, integ, adaptive)), u)
+        ref.initialize()
+        ref.run(nt)
+        ur = ref.u_physical()
+        for c in range(3):
+            assert np.linalg.norm(fg[c] - ur[c]) <= 1e-4 * np.linalg.norm(ur[c]), (case, c)
