@@ -309,7 +309,8 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
     fields = [pkg.random_spectrum(r["n"], k0=float(r["k0"]), seed=r["seed"]) for r in reqs]
     total_steps = sum(r["nt"] for r in reqs)
     points = sum(r["nt"] * r["n"] ** 3 for r in reqs)
-    with pkg.Server(device=device, memory_budget=120 << 30, max_active=256) as srv:
+    with pkg.Server(device=device, memory_budget=120 << 30, max_active=256, autotune=True) as srv:
+        tuning = srv.tuning   # the size classes' kernel forms, timed at create
         # warm-up: one short run per grid and model (module load, first allocations)
         warm = [srv.submit(serve_global(dict(r, nt=3)), fields[r["i"]], 3)
                 for r in {(x["n"], x["les"]): x for x in reqs}.values()]
@@ -340,7 +341,7 @@ def run_serving(pkg, R: int, seq_budget: float, device: int) -> dict:
                "sim_steps_per_s": total_steps / span, "grid_point_updates_per_s": points / span,
                "wall_s": span, "batch_steps": batch_steps, "peak_active": info["peak_active"],
                "peak_bytes": info["peak_bytes"], "gpu_launches": batch_steps * SERVE_BATCH_LAUNCHES,
-               "failed": len(errors), "errors": errors[:3]}
+               "failed": len(errors), "errors": errors[:3], "tuning": tuning}
     out = {"workload": f"served ensemble: {R} requests, Poisson arrivals mean {SERVE_RATE:.0f}/s, n ~ U{{32..128}}, "
                        "k0 ~ U{2..6}, nu ~ logU[1e-3,1e-2], nt ~ U{100..1000} AB3 (CFL 0.18), 50% Smagorinsky, "
                        "FP32, 120 GB budget",

@@ -90,6 +90,18 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
 
   // pointwise: inputs from ri, outputs to s1 at the same row (same thread)
   const T d2 = T(I.les_d2);
+  // piomelliSmagorinsky (calc_cstar!, dynamic_smagorinsky.jl:9-19, dynamic_piomelli.jl:1-11):
+  // c* = c + (dt/dtm1)(c - cm1) from the last averaged c, then cm1 := c (cm1 := c first at
+  // iteration 0); dt is the step's current dt (set_dt! runs after this pass)
+  double rpi = 0.0;
+  bool first = false;
+  if (STAGE == 0 && I.piom) {
+    const double dt = I.st->dt, dtm1 = I.st->dyn_dtm1;
+    const double dtf = dt == 0.0 ? 1.0 : dt, dtm1f = dtm1 == 0.0 ? dtf : dtm1;
+    rpi = dtf / dtm1f;
+    first = I.st->iteration == 0;
+  }
+  if (STAGE == 1 && I.piom && blockIdx.x == 0 && threadIdx.x == 0) I.st->dyn_dtm1 = I.st->dt;
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const cplx<T>* row = ri + sidx(j, 0, LS);
     T f[2 * LIN];
@@ -102,7 +114,15 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
       // realspace_dynamic_les_calculation! (dynamic_smagorinsky.jl:66-72): Sa = D^2 |S| S, L = u u
       const T ux = f[0], uy = f[1], uz = f[2];
       const T xx = f[3], xy = f[4], xz = f[5], yy = f[6], yz = f[7], zz = -xx - yy;
-      const T a = d2 * sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
+      const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
+      T a = d2 * nrm;
+      if (I.piom) {   // Sa = 2 c* D^2 |S| S
+        const long long pi = g * n + j;
+        const double cv = I.dyn_c[pi], cm = first ? cv : I.dyn_cm1[pi];
+        const double cs = rpi * (cv - cm) + cv;
+        I.dyn_cm1[pi] = cv;
+        a = T(2) * T(cs) * d2 * nrm;
+      }
       o[0] = a * xx; o[1] = a * xy; o[2] = a * xz; o[3] = a * yy; o[4] = a * yz;
       o[5] = ux * ux; o[6] = ux * uy; o[7] = ux * uz; o[8] = uy * uy; o[9] = uy * uz; o[10] = uz * uz;
     } else {
@@ -113,13 +133,24 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
       T l3 = b * b - f[16], l4 = b * c - f[17], l5 = c * c - f[18];
       const T tr = (l0 + l3 + l5) / T(3);
       l0 -= tr; l3 -= tr; l5 -= tr;
-      const T s = T(I.dyn_d2h + I.les_d2) *
-                  sqrt(hxx * hxx + hyy * hyy + hzz * hzz + T(2) * (hxy * hxy + hxz * hxz + hyz * hyz));
-      const T mxx = s * hxx - f[8], mxy = s * hxy - f[9], mxz = s * hxz - f[10];
-      const T myy = s * hyy - f[11], myz = s * hyz - f[12], mzz = -mxx - myy;
-      const T lm = l0 * mxx + l3 * myy + l5 * mzz + T(2) * (l1 * mxy + l2 * mxz + l4 * myz);
-      const T mm = mxx * mxx + myy * myy + mzz * mzz + T(2) * (mxy * mxy + mxz * mxz + myz * myz);
-      T cv = T(0.5) * (lm / mm);
+      const T nh = sqrt(hxx * hxx + hyy * hyy + hzz * hzz + T(2) * (hxy * hxy + hxz * hxz + hyz * hyz));
+      T cv;
+      if (I.piom) {
+        // c = (tau^ + L) : M / (M:M), M = 2 (D^^2 + D^2) |S^| S^ (dynamic_smagorinsky.jl:174-185)
+        const T s = T(2) * T(I.dyn_d2h + I.les_d2) * nh;
+        const T mxx = s * hxx, mxy = s * hxy, mxz = s * hxz, myy = s * hyy, myz = s * hyz, mzz = -mxx - myy;
+        const T mm = mxx * mxx + myy * myy + mzz * mzz + T(2) * (mxy * mxy + mxz * mxz + myz * myz);
+        const T txx = f[8], txy = f[9], txz = f[10], tyy = f[11], tyz = f[12], tzz = -txx - tyy;
+        cv = (txx + l0) * (mxx / mm) + (tyy + l3) * (myy / mm) + (tzz + l5) * (mzz / mm) +
+             T(2) * ((txy + l1) * (mxy / mm) + (txz + l2) * (mxz / mm) + (tyz + l4) * (myz / mm));
+      } else {
+        const T s = T(I.dyn_d2h + I.les_d2) * nh;
+        const T mxx = s * hxx - f[8], mxy = s * hxy - f[9], mxz = s * hxz - f[10];
+        const T myy = s * hyy - f[11], myz = s * hyz - f[12], mzz = -mxx - myy;
+        const T lm = l0 * mxx + l3 * myy + l5 * mzz + T(2) * (l1 * mxy + l2 * mxz + l4 * myz);
+        const T mm = mxx * mxx + myy * myy + mzz * mzz + T(2) * (mxy * mxy + mxz * mxz + myz * myz);
+        cv = T(0.5) * (lm / mm);
+      }
       // max(-1, min(1, c)) with Julia's NaN propagation
       if (!isnan(cv)) cv = cv > T(1) ? T(1) : (cv < T(-1) ? T(-1) : cv);
       o[0] = cv;
@@ -148,6 +179,12 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
     D.fy[(long long)(slot0 + 2 * r) * D.fys + g * D.kxf + k] = A;
     if (2 * r + 1 < NOUT) D.fy[(long long)(slot0 + 2 * r + 1) * D.fys + g * D.kxf + k] = B;
   }
+}
+
+// fill n doubles with v (the piomelli coefficient's initial value)
+static __global__ void k_dyn_fill(double* p, long long n, double v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
 }
 
 // Test filter along z on the full layout (J: the full-spectrum instance, wz = [slot][z][y][kxf]):

@@ -208,7 +208,8 @@ class Engine : public EngineBase {
     const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
     I.les_alpha = p.smag_c * p.smag_c * fw * fw;
     I.les_model = p.les_model; I.les_c = p.smag_c; I.les_d2 = fw * fw; I.les_cp = p.les_cp; I.les_cb = p.sandp_cb;
-    I.dyn = I.les && p.les_model == FFS_LES_DYNAMIC;
+    I.dyn = I.les && (p.les_model == FFS_LES_DYNAMIC || p.les_model == FFS_LES_PIOMELLI);
+    I.piom = I.les && p.les_model == FFS_LES_PIOMELLI;
     {
       const double tw = p.les_test_width > 0 ? p.les_test_width : 2 * fw;   // les_types.jl:390
       I.dyn_d2h = I.dyn ? tw * tw : 0.0;
@@ -272,7 +273,7 @@ class Engine : public EngineBase {
     if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
     if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
     if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
-    if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_DYNAMIC)) {
+    if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_PIOMELLI)) {
       err = "unknown LES model";
       return FFS_EINVAL;
     }
@@ -343,6 +344,10 @@ class Engine : public EngineBase {
     pair_z = p.kernel_variant != 3;
     if (p.kernel_variant == 2) v_iz = v_iy = v_fy = 1;
     if (p.kernel_variant == 3) v_iz = v_iy = v_fy = 0;
+    if (p.kernel_variant == 4) {   // half tiles: TX/2 kx lines in the y/z passes, one line per thread
+      txy = TX / 2;
+      v_iz = v_iy = v_fy = 0;
+    }
     txz = TX;
     while (txz > 1 && zu_lines() * I.pz.tpl > MAXT) txz /= 2;
     if (zu_lines() * I.pz.tpl > MAXT) { err = "nz too large for this precision"; return FFS_EUNSUPPORTED; }
@@ -517,6 +522,7 @@ class Engine : public EngineBase {
       if ((rc = alloc(&dync, (size_t)p.nx * p.ny * p.nz, err))) return rc;
       FFS_CK(cudaMemsetAsync(dync, 0, sizeof(double) * (size_t)p.nx * p.ny * p.nz, s));
       I.dyn_c = dync;
+      if (I.piom && (rc = alloc(&I.dyn_cm1, (size_t)p.nx * p.ny * p.nz, err))) return rc;
     }
 
     // launch geometry / shared memory
@@ -526,6 +532,12 @@ class Engine : public EngineBase {
 
     // state and header
     if ((rc = reset_state(err))) return rc;
+    if (I.piom) {   // c = cm1 = 0.0289 at construction (les_types.jl:261-266)
+      const long long np = (long long)p.nx * p.ny * p.nz;
+      k_dyn_fill<<<(unsigned)std::min<long long>((np + 255) / 256, 65535), 256, 0, s>>>(dync, np, 0.0289);
+      k_dyn_fill<<<(unsigned)std::min<long long>((np + 255) / 256, 65535), 256, 0, s>>>(I.dyn_cm1, np, 0.0289);
+      FFS_CK(cudaGetLastError());
+    }
     header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
     if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
     else if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
@@ -614,14 +626,21 @@ class Engine : public EngineBase {
     int rc;
     if constexpr (sizeof(T) == 4) {
       constexpr size_t ps = pair_smem<NC, PAIR_LP>();
-      if (v_iz == 1 && ctz() == NC && (rc = smem_attr(k_inv_z2<NC, PAIR_LP>, ps, err))) return rc;
-      if (v_iy == 1 && cty() == NC && (rc = smem_attr(k_inv_y2<NC, PAIR_LP>, ps, err))) return rc;
-      if (v_fy == 1 && cty() == NC && (rc = smem_attr(k_fwd_y2<NC, PAIR_LP>, ps, err))) return rc;
+      const bool full = txy == TX;
+      if (full && v_iz == 1 && ctz() == NC && (rc = smem_attr(k_inv_z2<NC, PAIR_LP>, ps, err))) return rc;
+      if (full && v_iy == 1 && cty() == NC && (rc = smem_attr(k_inv_y2<NC, PAIR_LP>, ps, err))) return rc;
+      if (full && v_fy == 1 && cty() == NC && (rc = smem_attr(k_fwd_y2<NC, PAIR_LP>, ps, err))) return rc;
       if (zpair() && ctzu() == NC && (rc = smem_attr(k_fwd_z2<NC, PAIR_LP>, ps + z2_aux(), err))) return rc;
     }
-    if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
-    if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
-    if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
+    if (txy == TX) {
+      if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX, NC>, smem_z, err))) return rc;
+      if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX, NC>, smem_y, err))) return rc;
+      if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX, NC>, smem_y, err))) return rc;
+    } else if constexpr (NC >= 512) {
+      if (ctz() == NC && (rc = smem_attr(k_inv_z<T, TX / 2, NC>, smem_z, err))) return rc;
+      if (cty() == NC && (rc = smem_attr(k_inv_y<T, TX / 2, NC>, smem_y, err))) return rc;
+      if (cty() == NC && (rc = smem_attr(k_fwd_y<T, TX / 2, NC>, smem_y, err))) return rc;
+    }
     if (ctzu() == NC) {
       if (zseq) { if ((rc = smem_attr(k_fwd_z<T, TX, NC, true>, smem_zu, err))) return rc; }
       else if (NC <= 256) { if ((rc = smem_attr(k_fwd_z<T, TX, NC>, smem_zu, err))) return rc; }
@@ -681,9 +700,12 @@ class Engine : public EngineBase {
   int ct_len(int n) const {
     return (sizeof(T) == 4 && P.kernel_variant != 1 && use_ct && (n == 128 || n == 256 || n == 512 || n == 1024)) ? n : 0;
   }
-  int cty() const { return txy == TX ? ct_len(I.ny) : 0; }
+  // compile-time y/z kernels: TX lines a CTA at every compile-time length, TX/2 lines at
+  // 512 and 1024 (where one TX-line CTA takes most of an SM's shared memory)
+  int ct_tile(int n) const { return (txy == TX || (txy == TX / 2 && n >= 512)) ? n : 0; }
+  int cty() const { return ct_tile(ct_len(I.ny)); }
   static const char* vname_of(int v) { return v == 1 ? "pair" : "1"; }
-  int ctz() const { return txy == TX ? ct_len(I.nz) : 0; }
+  int ctz() const { return ct_tile(ct_len(I.nz)); }
   // compile-time forward z kernels exist for TX lines (3 components together or one at a
   // time) at 128/256, and for 2 lines (3 together) or TX lines (one at a time) at 512/1024
   int ctzu() const {
@@ -701,6 +723,12 @@ class Engine : public EngineBase {
     case 1024: { constexpr int NC = 1024; CALL; } return;            \
     default: break;                                                  \
   }
+#define FFS_CT_SWITCH_HALF(NSEL, CALL)                               \
+  switch (NSEL) {                                                    \
+    case 512: { constexpr int NC = 512; CALL; } return;              \
+    case 1024: { constexpr int NC = 1024; CALL; } return;            \
+    default: break;                                                  \
+  }
 
   // the paired one-field-at-a-time forward z pass applies (FP32, TX lines, ct plan)
   bool zpair() const { return sizeof(T) == 4 && pair_z && zseq && txz == TX; }
@@ -709,30 +737,45 @@ class Engine : public EngineBase {
 
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      if (v_iz == 1 && !I.dyn)
-        FFS_CT_SWITCH(ctz(), (k_inv_z2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.NYR), PAIR_LP * ct_tpl<NC>(),
-                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
-      FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
+      if (txy == TX) {
+        if (v_iz == 1 && !I.dyn)
+          FFS_CT_SWITCH(ctz(), (k_inv_z2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.NYR), PAIR_LP * ct_tpl<NC>(),
+                                                       pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
+        FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
+      } else {
+        FFS_CT_SWITCH_HALF(ctz(), (k_inv_z<T, TX / 2, NC><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), (TX / 2) * ct_tpl<NC>(),
+                                                          smem_z, s>>>(I, F)))
+      }
     }
     if (txy == TX) k_inv_z<T, TX><<<dim3(F.n, I.KXP / TX, I.NYR), blk(TX, I.pz), smem_z, s>>>(I, F);
     else k_inv_z<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.NYR), blk(TX / 2, I.pz), smem_z, s>>>(I, F);
   }
   void launch_inv_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      if (v_iy == 1)
-        FFS_CT_SWITCH(cty(), (k_inv_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
-                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
-      FFS_CT_SWITCH(cty(), (k_inv_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+      if (txy == TX) {
+        if (v_iy == 1)
+          FFS_CT_SWITCH(cty(), (k_inv_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
+                                                       pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
+        FFS_CT_SWITCH(cty(), (k_inv_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+      } else {
+        FFS_CT_SWITCH_HALF(cty(), (k_inv_y<T, TX / 2, NC><<<dim3(F.n, I.KXP / (TX / 2), I.nz), (TX / 2) * ct_tpl<NC>(),
+                                                          smem_y, s>>>(I, F)))
+      }
     }
     if (txy == TX) k_inv_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
     else k_inv_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
   }
   void launch_fwd_y(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
-      if (v_fy == 1)
-        FFS_CT_SWITCH(cty(), (k_fwd_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
-                                                     pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
-      FFS_CT_SWITCH(cty(), (k_fwd_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+      if (txy == TX) {
+        if (v_fy == 1)
+          FFS_CT_SWITCH(cty(), (k_fwd_y2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.nz), PAIR_LP * ct_tpl<NC>(),
+                                                       pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
+        FFS_CT_SWITCH(cty(), (k_fwd_y<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.nz), TX * ct_tpl<NC>(), smem_y, s>>>(I, F)))
+      } else {
+        FFS_CT_SWITCH_HALF(cty(), (k_fwd_y<T, TX / 2, NC><<<dim3(F.n, I.KXP / (TX / 2), I.nz), (TX / 2) * ct_tpl<NC>(),
+                                                          smem_y, s>>>(I, F)))
+      }
     }
     if (txy == TX) k_fwd_y<T, TX><<<dim3(F.n, I.KXP / TX, I.nz), blk(TX, I.py), smem_y, s>>>(I, F);
     else k_fwd_y<T, TX / 2><<<dim3(F.n, I.KXP / (TX / 2), I.nz), blk(TX / 2, I.py), smem_y, s>>>(I, F);
@@ -1408,7 +1451,8 @@ class Engine : public EngineBase {
       for (int t : {TX, TX / 2})
         for (int c : {1, 0}) {
           if (t * std::max(I.py.tpl, I.pz.tpl) > MAXT) continue;
-          if (c && (sizeof(T) != 4 || t != TX || (!ct_len_raw(P.ny) && !ct_len_raw(P.nz)))) continue;
+          const bool half_ct = t == TX / 2 && (ct_len_raw(P.ny) >= 512 || ct_len_raw(P.nz) >= 512);
+          if (c && (sizeof(T) != 4 || (t != TX && !half_ct) || (!ct_len_raw(P.ny) && !ct_len_raw(P.nz)))) continue;
           txy = t; use_ct = c;
           float ms = 0.f;
           if ((rc = timed([&] { launch_inv_z(inv_list); launch_inv_y(inv_list); launch_fwd_y(fwd_list); }, ms))) break;
@@ -1434,7 +1478,7 @@ class Engine : public EngineBase {
         v = bv;
         return 0;
       };
-      if (!rc) rc = pick(v_iz, "z_inv", I.dyn ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
+      if (!rc) rc = pick(v_iz, "z_inv", (I.dyn || txy != TX) ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
       // one launch for every field family, or one per family
       if (!rc && n_fam > 1) {
         float bms = 1e30f;
@@ -1449,8 +1493,8 @@ class Engine : public EngineBase {
         }
         split_iz = bs;
       }
-      if (!rc) rc = pick(v_iy, "y_inv", cty(), [&] { launch_inv_y(inv_list); });
-      if (!rc) rc = pick(v_fy, "y_fwd", cty(), [&] { launch_fwd_y(fwd_list); });
+      if (!rc) rc = pick(v_iy, "y_inv", txy == TX ? cty() : 0, [&] { launch_inv_y(inv_list); });
+      if (!rc) rc = pick(v_fy, "y_fwd", txy == TX ? cty() : 0, [&] { launch_fwd_y(fwd_list); });
     }
     // x pass
     if (!rc) {

@@ -63,6 +63,7 @@ struct DevState {
   double pf_hp, pf_vp;     // kz = 0 plane forcing: horizontal and vertical power of the last call
   double nl_h, nl_v, press_h, press_v;  // last non-linear / pressure stats
   double nl_hf, nl_vf, press_hf, press_vf;  // their filtered twins (Stats_fil.txt)
+  double dyn_dtm1;         // piomelliSmagorinsky: dt of its previous coefficient (dtm1)
   long long nrec;          // stats records written
   long long nspec;         // spectrum records written
   unsigned int err;        // bit 0: non-finite value in the update
@@ -131,7 +132,9 @@ template <typename T> struct Inst {
   double les_c, les_d2;    // the model's constant c and Delta^2
   double les_cp;           // Silvis P constant
   double les_cb;           // SandP: cb (0: no P term)
-  int dyn;                 // dynamic Smagorinsky (FFS_LES_DYNAMIC)
+  int dyn;                 // dynamic Smagorinsky (FFS_LES_DYNAMIC or FFS_LES_PIOMELLI)
+  int piom;                //   piomelliSmagorinsky: extrapolated coefficient in Sa
+  double* dyn_cm1;         //   its coefficient of the previous step [z][y][x]
   double dyn_d2h;          //   test filter width^2
   double les_cmin;         //   smallest coefficient kept (cmin)
   int sfil;                // filtered stats and spectra (specFil)

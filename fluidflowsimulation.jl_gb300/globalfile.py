@@ -48,13 +48,13 @@ _LES_CONST = {"Smagorinsky": ("smagorinskyConstant", 0.17), "Vreman": ("vremanCo
 
 def _set_les(p: FFSParams, d: dict[str, str]) -> None:
     """lesModel (les_types.jl:360-395): Smagorinsky, Vreman, productionViscosity, Silvis,
-    stableNonLinear, dynamicSmagorinsky (les_types.jl:388-392: filterWidth, TestFilterWidth
-    with default twice the filter width, cmin), or SandP (the P tensor term on top of
-    sLesModel = Smagorinsky, Vreman or productionViscosity). The other dynamic variants
-    (piomelliSmagorinsky, dynamicSandP, piomelliSandP) are not built."""
+    stableNonLinear, dynamicSmagorinsky or piomelliSmagorinsky (les_types.jl:388-397:
+    filterWidth, TestFilterWidth with default twice the filter width, cmin), or SandP (the
+    P tensor term on top of sLesModel = Smagorinsky, Vreman or productionViscosity). The
+    dynamic P-tensor variants (dynamicSandP, piomelliSandP) are not built."""
     m = d["lesModel"]
     base = m
-    if m == "dynamicSmagorinsky":
+    if m in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
         p.les = 1
         p.les_model = LES_MODELS[m]
         p.filter_width = parse_number(d["filterWidth"]) if "filterWidth" in d else 0.0
@@ -69,7 +69,7 @@ def _set_les(p: FFSParams, d: dict[str, str]) -> None:
         p.sandp_cb = parse_number(d.get("pConstant", "0.09"))
     if base not in _LES_CONST:
         raise ValueError(f"lesModel {m!r} is not supported (Smagorinsky, Vreman, productionViscosity, Silvis, "
-                         "stableNonLinear, dynamicSmagorinsky, SandP)")
+                         "stableNonLinear, dynamicSmagorinsky, piomelliSmagorinsky, SandP)")
     key, dflt = _LES_CONST[base]
     if m == "SandP" and base == "productionViscosity":
         dflt = 0.1                                           # les_types.jl:402

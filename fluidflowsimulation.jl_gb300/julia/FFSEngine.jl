@@ -88,8 +88,8 @@ function parameters(d)
         p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
         p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
     end
-    if haskey(d, :lesModel) && d[:lesModel] == "dynamicSmagorinsky"   # les_types.jl:388-392
-        p.les = 1; p.les_model = 5
+    if haskey(d, :lesModel) && d[:lesModel] in ("dynamicSmagorinsky", "piomelliSmagorinsky")   # les_types.jl:388-397
+        p.les = 1; p.les_model = d[:lesModel] == "dynamicSmagorinsky" ? 5 : 6
         p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) : 0.0
         p.les_test_width = haskey(d, :TestFilterWidth) ? num(d[:TestFilterWidth]) : 0.0
         p.les_cmin = haskey(d, :cmin) ? parse(Float64, d[:cmin]) : 0.0

@@ -82,12 +82,14 @@ typedef struct ffs_params {
   int32_t kernel_variant;      /* 0: specialised FP32 kernels where available (register-fused x pass,
                                   compile-time FFT lengths); 1: runtime-plan kernels only;
                                   2: as 0 with every compile-time y/z pass on line pairs (packed FP32);
-                                  3: as 0 with every compile-time y/z pass one line per thread */
+                                  3: as 0 with every compile-time y/z pass one line per thread;
+                                  4: as 3 with TX/2 kx lines a CTA in the y/z passes (compile-time
+                                  plans at 512 and 1024) */
   int32_t autotune;            /* 1: time the candidate launch shapes at create, keep the fastest */
   int32_t les_model;           /* with les != 0, the eddy-viscosity model of lesModel (les_types.jl:360-395):
                                   FFS_LES_SMAGORINSKY, FFS_LES_VREMAN, FFS_LES_PRODUCTION, FFS_LES_SILVIS,
-                                  FFS_LES_STABLE_NL, FFS_LES_DYNAMIC; smag_c holds the constant of the
-                                  pointwise models */
+                                  FFS_LES_STABLE_NL, FFS_LES_DYNAMIC, FFS_LES_PIOMELLI; smag_c holds the
+                                  constant of the pointwise models */
   double les_cp;               /* silvisPConstant (Silvis model) */
   double sandp_cb;             /* lesModel SandP: pConstant of the P tensor term (0: none) */
   int32_t passive_scalar;      /* passiveScalar (simulationtypes.jl:198-213, :320-352): a scalar phi
@@ -104,8 +106,8 @@ typedef struct ffs_params {
   double pf_kf;                /* kf */
   int32_t pf_zf_tanh;          /* Zf tanh (default: cutoff) */
   double pf_qp, pf_qc, pf_qkf; /* alveliusP, alveliusC, alveliusKf (QfForcing) */
-  double les_test_width;       /* dynamicSmagorinsky: TestFilterWidth (<= 0: twice the filter width) */
-  double les_cmin;             /* dynamicSmagorinsky: cmin, the smallest coefficient kept */
+  double les_test_width;       /* dynamic models: TestFilterWidth (<= 0: twice the filter width) */
+  double les_cmin;             /* dynamic models: cmin, the smallest coefficient kept */
   double spec_fil;             /* specFil nf (Globals.jl:173-182): with nf != 0 every stats record also
                                   carries the Stats_fil.txt row (quadratic sums weighted by the Gaussian
                                   filter squared, D = 2 pi lx nf / nx) and the spectrum records the
@@ -131,6 +133,9 @@ typedef struct ffs_params {
 #define FFS_LES_DYNAMIC 5     /* dynamic Smagorinsky: Germano coefficient from a Gaussian test filter,
                                  averaged by the same filter (dynamic_smagorinsky.jl, dynamic_piomelli.jl
                                  :13-26, les_real_calc.jl:71-73); grids with nx <= 512 in FP64 */
+#define FFS_LES_PIOMELLI 6    /* piomelliSmagorinsky: the dynamic model with the coefficient of the
+                                 previous step extrapolated in time inside the test-filtered stress
+                                 (dynamic_smagorinsky.jl:9-19, 172-185, dynamic_piomelli.jl:1-11) */
 
 /* Fill defaults: reference defaults for every key that has one. */
 int ffs_params_default(ffs_params* p);

@@ -250,7 +250,7 @@ class Params:
         to an eddy-viscosity model (sLesModel)."""
         m = d["lesModel"]
         base = m
-        if m == "dynamicSmagorinsky":                       # les_types.jl:388-392
+        if m in ("dynamicSmagorinsky", "piomelliSmagorinsky"):   # les_types.jl:388-397
             self.les = True
             self.les_model = m
             dx = (self.lx * 2 * math.pi / self.nx) / self.cutoff
@@ -929,6 +929,9 @@ class OracleSimulation:
         # records the values set_dt! produced or took.
         self.dt_sequence = None
         self.newdt_hist = []
+        # piomelliSmagorinsky's coefficient state (c, cm1, dtm1)
+        self.piom_c = self.piom_cm1 = None
+        self.piom_dtm1 = 0.0
 
     # ---------------------------------------------------------------- time helpers
     def get_dt(self):
@@ -979,7 +982,7 @@ class OracleSimulation:
             rhor = g.real(self.rho)
         if p.les:
             Sr = g.real(S)
-            if p.les_model == "dynamicSmagorinsky":
+            if p.les_model in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
                 taur = self.dynamic_smagorinsky(u, ur, S, Sr)
             else:
                 taur = les_stress(p, Sr, wr)
@@ -1064,7 +1067,26 @@ class OracleSimulation:
 
         uf = g.real(G[None] * u)                                   # u^ (physical)
         Sh = g.real(G[None] * S)                                   # S^ (physical)
-        Sa = d2 * nrm5(Sr)[None] * Sr                              # D^2 |S| S
+        piomelli = p.les_model == "piomelliSmagorinsky"
+        if piomelli:
+            # calc_cstar! (dynamic_smagorinsky.jl:9-19, dynamic_piomelli.jl:1-11): the last
+            # averaged coefficient extrapolated in time, c* = c + (dt/dtm1)(c - cm1); c and
+            # cm1 start at 0.0289 (les_types.jl:261-266), cm1 := c at iteration 0
+            if self.piom_c is None:
+                self.piom_c = np.full(ur[0].shape, 0.0289)
+                self.piom_cm1 = np.full(ur[0].shape, 0.0289)
+            dt = self.get_dt()
+            dtf = 1.0 if dt == 0.0 else dt
+            dtm1f = dtf if self.piom_dtm1 == 0.0 else self.piom_dtm1
+            if self.iteration == 0:
+                self.piom_cm1 = self.piom_c.copy()
+            r = dtf / dtm1f
+            cstar = r * (self.piom_c - self.piom_cm1) + self.piom_c
+            self.piom_cm1 = self.piom_c
+            self.piom_dtm1 = dt
+            Sa = (2 * cstar * d2 * nrm5(Sr))[None] * Sr            # 2 c* D^2 |S| S
+        else:
+            Sa = d2 * nrm5(Sr)[None] * Sr                          # D^2 |S| S
         ux, uy, uz = ur
         Lr = np.stack([ux * ux, ux * uy, ux * uz, uy * uy, uy * uz, uz * uz])
         Saf = np.stack([full_filter(x) for x in Sa])
@@ -1075,13 +1097,28 @@ class OracleSimulation:
         L6[0] -= tr
         L6[3] -= tr
         L6[5] -= tr
-        M5 = (dh2 + d2) * nrm5(Sh)[None] * Sh - Saf
-        mxx, mxy, mxz, myy, myz = M5
-        mzz = -mxx - myy
-        lm = (L6[0] * mxx + L6[3] * myy + L6[5] * mzz + 2.0 * (L6[1] * mxy + L6[2] * mxz + L6[4] * myz))
-        mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
-        cf = np.maximum(-1.0, np.minimum(1.0, 0.5 * (lm / mm)))
+        if piomelli:
+            # c = (tau^ + L) : M / (M:M), M = 2 (D^^2 + D^2) |S^| S^ (dynamic_smagorinsky.jl:174-185)
+            M5 = (2 * (dh2 + d2) * nrm5(Sh))[None] * Sh
+            mxx, mxy, mxz, myy, myz = M5
+            mzz = -mxx - myy
+            mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
+            nxx, nxy, nxz, nyy, nyz, nzz = mxx / mm, mxy / mm, mxz / mm, myy / mm, myz / mm, mzz / mm
+            txx, txy, txz, tyy, tyz = Saf
+            tzz = -txx - tyy
+            cv = ((txx + L6[0]) * nxx + (tyy + L6[3]) * nyy + (tzz + L6[5]) * nzz
+                  + 2.0 * ((txy + L6[1]) * nxy + (txz + L6[2]) * nxz + (tyz + L6[4]) * nyz))
+            cf = np.maximum(-1.0, np.minimum(1.0, cv))
+        else:
+            M5 = (dh2 + d2) * nrm5(Sh)[None] * Sh - Saf
+            mxx, mxy, mxz, myy, myz = M5
+            mzz = -mxx - myy
+            lm = (L6[0] * mxx + L6[3] * myy + L6[5] * mzz + 2.0 * (L6[1] * mxy + L6[2] * mxz + L6[4] * myz))
+            mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
+            cf = np.maximum(-1.0, np.minimum(1.0, 0.5 * (lm / mm)))
         cf = full_filter(cf)                                       # average_c!
+        if piomelli:
+            self.piom_c = cf
         nut = np.maximum(p.les_cmin, np.minimum(0.4, cf)) * d2 * nrm5(Sr)
         return 2.0 * nut[None] * Sr
 

@@ -64,3 +64,25 @@ def test_tuned_fp64_keeps_parity(gpu_pkg):
     for c in range(3):
         assert rel(sim.spectral(c), ref.u[c]) <= 1e-12, (c, sim.tuning)
     sim.close()
+
+
+@pytest.mark.parametrize("variant", [2, 3, 4])
+def test_kernel_variants_match_default_512(gpu_pkg, variant):
+    """Every forced y/z form at 512^3 (line pairs, one line per thread, and half tiles:
+    TX/2 kx lines a CTA with the compile-time plans) computes the default step (FP32
+    rounding, 3 steps)."""
+    n = 512
+    d = gdict(n)
+    u = gpu_pkg.random_spectrum(n, k0=4.0, seed=21)
+    out = []
+    for kv in (0, variant):
+        p = gpu_pkg.parameters(d, precision="FP32")
+        p.kernel_variant = kv
+        s = gpu_pkg.Simulation(p)
+        s.set_fields(*u)
+        s.initialize()
+        s.advance_in_time(3)
+        out.append([s.spectral(c) for c in range(3)])
+        s.close()
+    for c in range(3):
+        assert rel(out[1][c], out[0][c]) <= 2e-6, (variant, c)

@@ -91,6 +91,11 @@ FIXED_CASES = {
                                          densityStratification="true", Pr="1", densityGradient="1",
                                          zAcceleration="1", referenceDensity="1"),
     "etd-dynamic-noncubic": gdict(32, "ETD3rdO", ny=48, nz=64, lesModel="dynamicSmagorinsky", filterWidth="0.3"),
+    # piomelliSmagorinsky: the previous coefficient extrapolated in time (adaptive dt makes
+    # dt/dtm1 vary), c = (tau^ + L):M/M:M
+    "ab3-adaptive-piomelli": gdict(32, adaptive=True, lesModel="piomelliSmagorinsky"),
+    "etd-piomelli-48-cmin": gdict(48, "ETD3rdO", lesModel="piomelliSmagorinsky", cmin="-0.05",
+                                  TestFilterWidth="0.35"),
     # the reference's kz = 0 plane forcing family (forcing_types.jl:335-450)
     "ab3-adaptive-rf-forcing": gdict(32, adaptive=True, forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
     "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
@@ -166,7 +171,7 @@ def test_etd_adaptive_parity(gpu_pkg):
 
 
 @pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
-                                  "ab3-stable-nonlinear", "etd-dynamic-smagorinsky"])
+                                  "ab3-stable-nonlinear", "etd-dynamic-smagorinsky", "ab3-adaptive-piomelli"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)

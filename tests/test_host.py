@@ -129,7 +129,7 @@ def test_parameters_requires_dtspec(pkg):
 def test_parameters_rejects_out_of_scope_models(pkg):
     d = {"nx": "8", "ny": "8", "nz": "8", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
          "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1",
-         "lesModel": "piomelliSmagorinsky"}
+         "lesModel": "fakeSmagorinsky"}
     with pytest.raises(ValueError):
         pkg.parameters(d)
     for m in ("dynamicSandP", "piomelliSandP"):
@@ -176,6 +176,8 @@ def test_parameters_les_models(pkg):
     o = Params.from_global(dict(base, lesModel="dynamicSmagorinsky"))
     assert (o.les_model, o.les_cmin) == ("dynamicSmagorinsky", 0.0)
     assert o.filter_width == pytest.approx(dx) and o.les_test_width == pytest.approx(2 * dx)
+    p = pkg.parameters(dict(base, lesModel="piomelliSmagorinsky"))
+    assert (p.les, p.les_model, p.les_test_width) == (1, 6, 0.0)
     d = dict(base, lesModel="dynamicSmagorinsky", filterWidth="0.2", TestFilterWidth="0.5", cmin="-0.1")
     p, o = pkg.parameters(d), Params.from_global(d)
     assert (p.filter_width, p.les_test_width, p.les_cmin) == (0.2, 0.5, -0.1)
