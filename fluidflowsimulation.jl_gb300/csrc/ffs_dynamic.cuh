@@ -1,5 +1,7 @@
-// The dynamic Smagorinsky model's extra passes (dynamic_smagorinsky.jl:3-217,
-// dynamic_piomelli.jl:13-26, les_real_calc.jl:3-11).
+// The dynamic Smagorinsky models' extra passes (dynamic_smagorinsky.jl:3-217,
+// dynamic_piomelli.jl:1-26, les_real_calc.jl:3-11): dynamicSmagorinsky, piomelliSmagorinsky
+// (the previous coefficient extrapolated in time inside Sa), and either with the dynamic
+// P tensor term (dynamicSandP, piomelliSandP: a second coefficient cp for D^2 Lie(S, W)).
 //
 // The model needs, at every grid point, the Germano coefficient
 //   c = clamp(L:M / (2 M:M), -1, 1),  L = traceless(u^ u^ - (u u)^),
@@ -10,11 +12,12 @@
 // ("full" slots [slot][z][y][KXF], KXF = nx/2+1 padded to 8). The inverse z pass already
 // produced u^ = G u and S^ = G S on the retained modes (prologue families 3 and 4).
 //
-//   k_dyn_x<0>:    u, S (retained)         -> physical -> Sa = D^2 |S| S, L = u u -> r2c, all kx
-//   y/z/y passes:  full slots 0..10        -> forward y, [forward z, x G/N, inverse z], inverse y
-//   k_dyn_x<1>:    u^, S^ (retained), Sa^, L^ (full) -> physical -> c -> r2c into full slot 11
-//   y/z/y passes:  full slot 11            -> the averaged coefficient
-//   k_inv_x_phys:  full slot 11            -> physical c, read by the x pass (nu_t)
+//   k_dyn_x<0>:    u, S [, w] (retained)   -> physical -> Sa = D^2 |S| S, L = u u [, P] -> r2c, all kx
+//   y/z/y passes:  full slots 0..nsa-1     -> forward y, [forward z, x G/N, inverse z], inverse y
+//   k_dyn_x<1>:    u^, S^ [, w^] (retained), Sa~, L~ [, P~] (full) -> physical -> c [, cp]
+//                  -> r2c into full slot nsa [, nsa+1]
+//   y/z/y passes:  those slots             -> the averaged coefficients
+//   k_inv_x_phys:  those slots             -> physical c [, cp], read by the x pass
 //
 // One (y,z) line per CTA in the x kernels; the shared memory holds every input line of
 // that (y,z) line (19 fields in the coefficient pass), which bounds nx (checked at create).
@@ -27,45 +30,94 @@ template <typename T> struct DynFull {
   cplx<T>* fy;        // [slot][z][y][kxf]: x-spectral fields over the full spectrum
   long long fys;      // slot stride
   int kxf;            // row length (>= nx/2 + 1, a multiple of 8)
-  int gslot0;         // first wy slot of the test-filtered u^ (3), S^ (5)
+  int gslot0;         // first wy slot of the test-filtered u^ (3), S^ (5) [, w^ (3)]
+  int nsa;            // full slots of Sa, L [, P]; the coefficient c [and cp] follow
 };
 
-// Slots of the full layout.
-constexpr int DYN_NSA = 11;   // Sa (5: xx xy xz yy yz), then L (6: xx xy xz yy yz zz)
-constexpr int DYN_SLOT_C = 11;
+// Full slots: Sa (5: xx xy xz yy yz), L (6: xx xy xz yy yz zz), with the dynamic P tensor
+// P (5), then c and cp.
+constexpr int DYN_NSA = 11;
+constexpr int DYN_NSA_P = 16;
 constexpr int DYN_NSLOTS = 12;
+constexpr int DYN_NSLOTS_P = 18;
 
-template <int STAGE> struct DynX {
-  static constexpr int NIN = STAGE == 0 ? 8 : 19;
+template <int STAGE, bool DP> struct DynX {
+  static constexpr int NRET = DP ? 11 : 8;                        // stage 1: u^, S^ [, w^]
+  static constexpr int NIN = STAGE == 0 ? (DP ? 11 : 8) : NRET + (DP ? 16 : 11);
   static constexpr int LIN = (NIN + 1) / 2;
-  static constexpr int NOUT = STAGE == 0 ? DYN_NSA : 1;
+  static constexpr int NOUT = STAGE == 0 ? (DP ? DYN_NSA_P : DYN_NSA) : (DP ? 2 : 1);
   static constexpr int LOUT = (NOUT + 1) / 2;
   static constexpr int LS = (LIN > LOUT ? LIN : LOUT) | 1;   // odd line stride
   static size_t smem(int nx, size_t cb) { return 2 * (size_t)srows(nx) * LS * cb; }
 };
 
-template <typename T, int STAGE>
+// Lie(S, W) = S W - W S of the traceless symmetric S (xx, xy, xz, yy, yz) and
+// W = AntiSymTen(w/2), the cross-product matrix of w/2; symmetric and traceless: its
+// five stored components
+template <typename T>
+__device__ __forceinline__ void lie_sw(T xx, T xy, T xz, T yy, T yz, T wx, T wy, T wz, T* o) {
+  const T zz = -xx - yy;
+  const T S[3][3] = {{xx, xy, xz}, {xy, yy, yz}, {xz, yz, zz}};
+  const T p = T(0.5) * wx, q = T(0.5) * wy, r = T(0.5) * wz;
+  const T W[3][3] = {{T(0), -r, q}, {r, T(0), -p}, {-q, p, T(0)}};
+  T L[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      T a = T(0), b = T(0);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { a += S[i][k] * W[k][j]; b += W[i][k] * S[k][j]; }
+      L[i][j] = a - b;
+    }
+  o[0] = L[0][0]; o[1] = L[0][1]; o[2] = L[0][2]; o[3] = L[1][1]; o[4] = L[1][2];
+}
+
+// (t + L) : M / (M:M) of the traceless t, M (5 components each) and the traceless L (6)
+template <typename T>
+__device__ __forceinline__ T ddot_norm(const T* t, const T* M, const T* L6) {
+  const T mzz = -M[0] - M[3], tzz = -t[0] - t[3];
+  const T mm = M[0] * M[0] + M[3] * M[3] + mzz * mzz + T(2) * (M[1] * M[1] + M[2] * M[2] + M[4] * M[4]);
+  return (t[0] + L6[0]) * (M[0] / mm) + (t[3] + L6[3]) * (M[3] / mm) + (tzz + L6[5]) * (mzz / mm) +
+         T(2) * ((t[1] + L6[1]) * (M[1] / mm) + (t[2] + L6[2]) * (M[2] / mm) + (t[4] + L6[4]) * (M[4] / mm));
+}
+
+// max(lo, min(hi, v)) with Julia's NaN propagation
+template <typename T> __device__ __forceinline__ T clampn(T v, T lo, T hi) {
+  return isnan(v) ? v : (v > hi ? hi : (v < lo ? lo : v));
+}
+
+// calc_cstar! (dynamic_smagorinsky.jl:9-35, dynamic_piomelli.jl:1-11): the coefficient
+// ratio dt/dtm1 of this step (dt: the current one; set_dt! runs after these passes)
+__device__ __forceinline__ double cstar_ratio(double dt, double dtm1) {
+  const double dtf = dt == 0.0 ? 1.0 : dt, dtm1f = dtm1 == 0.0 ? dtf : dtm1;
+  return dtf / dtm1f;
+}
+
+template <typename T, int STAGE, bool DP>
 __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
-  using X = DynX<STAGE>;
-  constexpr int NIN = X::NIN, LIN = X::LIN, NOUT = X::NOUT, LOUT = X::LOUT, LS = X::LS;
+  using X = DynX<STAGE, DP>;
+  constexpr int NIN = X::NIN, LIN = X::LIN, NOUT = X::NOUT, LOUT = X::LOUT, LS = X::LS, NRET = X::NRET;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = I.nx, nxh = I.nxh;
   cplx<T>* s0 = reinterpret_cast<cplx<T>*>(smem_raw);
   cplx<T>* s1 = s0 + (size_t)srows(n) * LS;
   const long long g = blockIdx.x;   // (y,z) line z * ny + y
+  const long long plane = (long long)I.nx * I.ny * I.nz;
 
   // input field f of this line and the count of kx it holds
   auto src = [&](int f, int& M) -> const cplx<T>* {
-    if (STAGE == 0) {   // u (slots 0..2), S (slots 6..10)
+    if (STAGE == 0) {   // u (slots 0..2), S (slots 6..10) [, w (slots 3..5)]
       M = I.Mx;
-      return I.wy + (long long)(f < 3 ? f : f + 3) * I.wys + g * I.KXP;
+      const int slot = f < 3 ? f : (f < 8 ? f + 3 : f - 5);
+      return I.wy + (long long)slot * I.wys + g * I.KXP;
     }
-    if (f < 8) {        // u^, S^
+    if (f < NRET) {     // u^, S^ [, w^]
       M = I.Mx;
       return I.wy + (long long)(D.gslot0 + f) * I.wys + g * I.KXP;
     }
-    M = nxh;            // Sa^, L^
-    return D.fy + (long long)(f - 8) * D.fys + g * D.kxf;
+    M = nxh;            // Sa~, L~ [, P~]
+    return D.fy + (long long)(f - NRET) * D.fys + g * D.kxf;
   };
   // c2r, two real fields per complex line (brfft: unnormalised)
   auto ldi = [&](int l, int j) -> cplx<T> {
@@ -90,18 +142,19 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
 
   // pointwise: inputs from ri, outputs to s1 at the same row (same thread)
   const T d2 = T(I.les_d2);
-  // piomelliSmagorinsky (calc_cstar!, dynamic_smagorinsky.jl:9-19, dynamic_piomelli.jl:1-11):
-  // c* = c + (dt/dtm1)(c - cm1) from the last averaged c, then cm1 := c (cm1 := c first at
-  // iteration 0); dt is the step's current dt (set_dt! runs after this pass)
-  double rpi = 0.0;
+  // time-extrapolated coefficients: c* = c + (dt/dtm1)(c - cm1), then cm1 := c (cm1 := c
+  // first at iteration 0); piomelliSmagorinsky's c and piomelliSandP's cp
+  double rpi = 0.0, rpp = 0.0;
   bool first = false;
-  if (STAGE == 0 && I.piom) {
-    const double dt = I.st->dt, dtm1 = I.st->dyn_dtm1;
-    const double dtf = dt == 0.0 ? 1.0 : dt, dtm1f = dtm1 == 0.0 ? dtf : dtm1;
-    rpi = dtf / dtm1f;
+  if (STAGE == 0) {
+    rpi = cstar_ratio(I.st->dt, I.st->dyn_dtm1);
+    rpp = cstar_ratio(I.st->dt, I.st->dyn_dtpm1);
     first = I.st->iteration == 0;
   }
-  if (STAGE == 1 && I.piom && blockIdx.x == 0 && threadIdx.x == 0) I.st->dyn_dtm1 = I.st->dt;
+  if (STAGE == 1 && blockIdx.x == 0 && threadIdx.x == 0) {
+    if (I.piom) I.st->dyn_dtm1 = I.st->dt;
+    if (I.dynp == 2) I.st->dyn_dtpm1 = I.st->dt;
+  }
   for (int j = threadIdx.x; j < n; j += blockDim.x) {
     const cplx<T>* row = ri + sidx(j, 0, LS);
     T f[2 * LIN];
@@ -110,14 +163,15 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
     T o[2 * LOUT];
 #pragma unroll
     for (int r = 0; r < 2 * LOUT; ++r) o[r] = T(0);
+    const long long pi = g * n + j;   // physical index [z][y][x]
     if (STAGE == 0) {
-      // realspace_dynamic_les_calculation! (dynamic_smagorinsky.jl:66-72): Sa = D^2 |S| S, L = u u
+      // realspace_dynamic_les_calculation! (dynamic_smagorinsky.jl:42-77): Sa = D^2 |S| S
+      // (2 c* D^2 |S| S for piomelliSmagorinsky), L = u u [, P = (cp*) D^2 Lie(S, W)]
       const T ux = f[0], uy = f[1], uz = f[2];
       const T xx = f[3], xy = f[4], xz = f[5], yy = f[6], yz = f[7], zz = -xx - yy;
       const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
       T a = d2 * nrm;
-      if (I.piom) {   // Sa = 2 c* D^2 |S| S
-        const long long pi = g * n + j;
+      if (I.piom) {
         const double cv = I.dyn_c[pi], cm = first ? cv : I.dyn_cm1[pi];
         const double cs = rpi * (cv - cm) + cv;
         I.dyn_cm1[pi] = cv;
@@ -125,35 +179,78 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
       }
       o[0] = a * xx; o[1] = a * xy; o[2] = a * xz; o[3] = a * yy; o[4] = a * yz;
       o[5] = ux * ux; o[6] = ux * uy; o[7] = ux * uz; o[8] = uy * uy; o[9] = uy * uz; o[10] = uz * uz;
+      if constexpr (DP) {
+        T lie[5];
+        lie_sw<T>(xx, xy, xz, yy, yz, f[8], f[9], f[10], lie);
+        T b = d2;
+        if (I.dynp == 2) {
+          const double cv = I.dyn_c[plane + pi], cm = first ? cv : I.dyn_cpm1[pi];
+          const double cs = rpp * (cv - cm) + cv;
+          I.dyn_cpm1[pi] = cv;
+          b = T(cs) * d2;
+        }
+#pragma unroll
+        for (int q = 0; q < 5; ++q) o[11 + q] = b * lie[q];
+      }
     } else {
-      // coefficient_les_calculation! (dynamic_smagorinsky.jl:162-172)
+      // coefficient_les_calculation! (dynamic_smagorinsky.jl:118-205)
       const T a = f[0], b = f[1], c = f[2];
-      const T hxx = f[3], hxy = f[4], hxz = f[5], hyy = f[6], hyz = f[7], hzz = -hxx - hyy;
-      T l0 = a * a - f[13], l1 = a * b - f[14], l2 = a * c - f[15];
-      T l3 = b * b - f[16], l4 = b * c - f[17], l5 = c * c - f[18];
-      const T tr = (l0 + l3 + l5) / T(3);
-      l0 -= tr; l3 -= tr; l5 -= tr;
-      const T nh = sqrt(hxx * hxx + hyy * hyy + hzz * hzz + T(2) * (hxy * hxy + hxz * hxz + hyz * hyz));
+      const T* Sh = f + 3;                 // S^
+      const T* Sa = f + NRET;              // Sa~
+      const T* Lf = f + NRET + 5;          // (u u)~
+      T L6[6] = {a * a - Lf[0], a * b - Lf[1], a * c - Lf[2], b * b - Lf[3], b * c - Lf[4], c * c - Lf[5]};
+      const T tr = (L6[0] + L6[3] + L6[5]) / T(3);
+      L6[0] -= tr; L6[3] -= tr; L6[5] -= tr;
+      const T hzz = -Sh[0] - Sh[3];
+      const T nh = sqrt(Sh[0] * Sh[0] + Sh[3] * Sh[3] + hzz * hzz + T(2) * (Sh[1] * Sh[1] + Sh[2] * Sh[2] + Sh[4] * Sh[4]));
+      const T dsum = T(I.dyn_d2h + I.les_d2);
+      T tau[5];   // tau^ of the piomelli forms: Sa~ (+ P~ with piomelliSandP)
+#pragma unroll
+      for (int q = 0; q < 5; ++q) tau[q] = Sa[q];
+      if constexpr (DP) {
+        if (I.dynp == 2) {
+#pragma unroll
+          for (int q = 0; q < 5; ++q) tau[q] = Sa[q] + f[NRET + 11 + q];
+        }
+      }
       T cv;
       if (I.piom) {
-        // c = (tau^ + L) : M / (M:M), M = 2 (D^^2 + D^2) |S^| S^ (dynamic_smagorinsky.jl:174-185)
-        const T s = T(2) * T(I.dyn_d2h + I.les_d2) * nh;
-        const T mxx = s * hxx, mxy = s * hxy, mxz = s * hxz, myy = s * hyy, myz = s * hyz, mzz = -mxx - myy;
-        const T mm = mxx * mxx + myy * myy + mzz * mzz + T(2) * (mxy * mxy + mxz * mxz + myz * myz);
-        const T txx = f[8], txy = f[9], txz = f[10], tyy = f[11], tyz = f[12], tzz = -txx - tyy;
-        cv = (txx + l0) * (mxx / mm) + (tyy + l3) * (myy / mm) + (tzz + l5) * (mzz / mm) +
-             T(2) * ((txy + l1) * (mxy / mm) + (txz + l2) * (mxz / mm) + (tyz + l4) * (myz / mm));
+        // c = (tau^ + L) : M / (M:M), M = 2 (D^^2 + D^2) |S^| S^
+        const T s = T(2) * dsum * nh;
+        const T M[5] = {s * Sh[0], s * Sh[1], s * Sh[2], s * Sh[3], s * Sh[4]};
+        cv = ddot_norm<T>(tau, M, L6);
       } else {
-        const T s = T(I.dyn_d2h + I.les_d2) * nh;
-        const T mxx = s * hxx - f[8], mxy = s * hxy - f[9], mxz = s * hxz - f[10];
-        const T myy = s * hyy - f[11], myz = s * hyz - f[12], mzz = -mxx - myy;
-        const T lm = l0 * mxx + l3 * myy + l5 * mzz + T(2) * (l1 * mxy + l2 * mxz + l4 * myz);
+        // c = L:M / (2 M:M), M = (D^^2 + D^2) |S^| S^ - Sa~
+        const T s = dsum * nh;
+        const T mxx = s * Sh[0] - Sa[0], mxy = s * Sh[1] - Sa[1], mxz = s * Sh[2] - Sa[2];
+        const T myy = s * Sh[3] - Sa[3], myz = s * Sh[4] - Sa[4], mzz = -mxx - myy;
+        const T lm = L6[0] * mxx + L6[3] * myy + L6[5] * mzz + T(2) * (L6[1] * mxy + L6[2] * mxz + L6[4] * myz);
         const T mm = mxx * mxx + myy * myy + mzz * mzz + T(2) * (mxy * mxy + mxz * mxz + myz * myz);
         cv = T(0.5) * (lm / mm);
       }
-      // max(-1, min(1, c)) with Julia's NaN propagation
-      if (!isnan(cv)) cv = cv > T(1) ? T(1) : (cv < T(-1) ? T(-1) : cv);
-      o[0] = cv;
+      o[0] = clampn(cv, T(-1), T(1));
+      if constexpr (DP) {
+        // cp from P^ = Lie(S^, AntiSymTen(w^/2)) (dynamic_smagorinsky.jl:188-203)
+        T Ph[5];
+        lie_sw<T>(Sh[0], Sh[1], Sh[2], Sh[3], Sh[4], f[8], f[9], f[10], Ph);
+        const T* Pf = f + NRET + 11;       // P~
+        T cp;
+        if (I.dynp == 1) {   // Mp = (D^^2 + D^2) P^ - P~, cp = L:Mp / Mp:Mp
+          T Mp[5];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) Mp[q] = dsum * Ph[q] - Pf[q];
+          const T mzz = -Mp[0] - Mp[3];
+          const T lm = L6[0] * Mp[0] + L6[3] * Mp[3] + L6[5] * mzz + T(2) * (L6[1] * Mp[1] + L6[2] * Mp[2] + L6[4] * Mp[4]);
+          const T mm = Mp[0] * Mp[0] + Mp[3] * Mp[3] + mzz * mzz + T(2) * (Mp[1] * Mp[1] + Mp[2] * Mp[2] + Mp[4] * Mp[4]);
+          cp = lm / mm;
+        } else {             // Mp = (D^^2 + D^2) P^, cp = (tau^ + L) : Mp / Mp:Mp
+          T Mp[5], tp[5];
+#pragma unroll
+          for (int q = 0; q < 5; ++q) { Mp[q] = dsum * Ph[q]; tp[q] = I.piom ? tau[q] : Pf[q]; }
+          cp = ddot_norm<T>(tp, Mp, L6);
+        }
+        o[1] = clampn(cp, T(-1), T(1));
+      }
     }
     cplx<T>* orow = s1 + sidx(j, 0, LS);
 #pragma unroll
@@ -166,7 +263,7 @@ __global__ void __launch_bounds__(256) k_dyn_x(Inst<T> I, DynFull<T> D) {
   auto ldf = [&](int l, int j) -> cplx<T> { return s1[sidx(j, l, LS)]; };
   auto stf = [&](int l, int j, cplx<T> v) { rf[sidx(j, l, LS)] = v; };
   fft_lines<-1, LOUT, T>(I.px, s0, s1, LS, I.twx, ldf, stf);
-  const int slot0 = STAGE == 0 ? 0 : DYN_SLOT_C;
+  const int slot0 = STAGE == 0 ? 0 : D.nsa;
   for (int e = threadIdx.x; e < LOUT * D.kxf; e += blockDim.x) {
     const int k = e % D.kxf, r = e / D.kxf;
     cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));

@@ -193,8 +193,8 @@ class Engine : public EngineBase {
     smem_zu = cb * ((size_t)zu_lines() * srows(P.nz) * (I.pz.np >= 3 ? 2 : 1) +
                     (size_t)((I.les || I.density) ? 4 : 0) * I.NZR * txz);
     if (I.dyn) {
-      smem_d0 = DynX<0>::smem(P.nx, cb);
-      smem_d1 = DynX<1>::smem(P.nx, cb);
+      smem_d0 = I.dynp ? DynX<0, true>::smem(P.nx, cb) : DynX<0, false>::smem(P.nx, cb);
+      smem_d1 = I.dynp ? DynX<1, true>::smem(P.nx, cb) : DynX<1, false>::smem(P.nx, cb);
       smem_dzf = 2 * (size_t)txy * srows(P.nz) * cb;
     }
   }
@@ -210,6 +210,7 @@ class Engine : public EngineBase {
     I.les_model = p.les_model; I.les_c = p.smag_c; I.les_d2 = fw * fw; I.les_cp = p.les_cp; I.les_cb = p.sandp_cb;
     I.dyn = I.les && (p.les_model == FFS_LES_DYNAMIC || p.les_model == FFS_LES_PIOMELLI);
     I.piom = I.les && p.les_model == FFS_LES_PIOMELLI;
+    I.dynp = I.dyn ? p.les_dynp : 0;
     {
       const double tw = p.les_test_width > 0 ? p.les_test_width : 2 * fw;   // les_types.jl:390
       I.dyn_d2h = I.dyn ? tw * tw : 0.0;
@@ -283,8 +284,14 @@ class Engine : public EngineBase {
       if (p.nz < 16) { err = "kz = 0 plane forcing needs nz >= 16 (it forces kz = +-1..+-5)"; return FFS_EUNSUPPORTED; }
       if (p.plane_forcing != FFS_PF_QF && !(p.pf_tf > 0)) { err = "TF must be positive"; return FFS_EINVAL; }
     }
-    if (p.les && p.sandp_cb != 0.0 && p.les_model > FFS_LES_PRODUCTION) {
-      err = "SandP takes the Smagorinsky, Vreman or production-viscosity model";
+    if (p.les_dynp < 0 || p.les_dynp > 2 ||
+        (p.les_dynp && !(p.les && (p.les_model == FFS_LES_DYNAMIC || p.les_model == FFS_LES_PIOMELLI)))) {
+      err = "les_dynp (dynamicSandP / piomelliSandP) takes the dynamic Smagorinsky models";
+      return FFS_EINVAL;
+    }
+    if (p.les && p.sandp_cb != 0.0 &&
+        ((p.les_model > FFS_LES_PRODUCTION && p.les_model < FFS_LES_DYNAMIC) || p.les_dynp != 0)) {
+      err = "SandP takes the Smagorinsky, Vreman, production-viscosity or a dynamic Smagorinsky model";
       return FFS_EINVAL;
     }
     FFS_CK(cudaSetDevice(p.device));
@@ -363,8 +370,13 @@ class Engine : public EngineBase {
     inv_list.n = nin;
     // the dynamic model's test-filtered u^, S^: transformed with the others, read by its
     // own x kernels only (the x pass reads slots 0..nin-1)
+    static_assert(sizeof(FieldList::code) / sizeof(int) >= 12 + (F_GWZ - F_GUX + 1), "FieldList too small");
     if (I.dyn)
-      for (int c = F_GUX; c <= F_GSYZ; ++c) { inv_list.code[inv_list.n] = c; inv_list.slot[inv_list.n] = inv_list.n; ++inv_list.n; }
+      for (int c = F_GUX; c <= (I.dynp ? F_GWZ : F_GSYZ); ++c) {
+        inv_list.code[inv_list.n] = c;
+        inv_list.slot[inv_list.n] = inv_list.n;
+        ++inv_list.n;
+      }
     {
       FieldList fam[3]{};
       for (int i = 0; i < inv_list.n; ++i) {
@@ -517,12 +529,16 @@ class Engine : public EngineBase {
       dfull.kxf = ((I.nxh + 7) / 8) * 8;
       dfull.fys = (long long)p.nz * p.ny * dfull.kxf;
       dfull.gslot0 = nin;
-      if ((rc = alloc(&dfull.fy, (size_t)DYN_NSLOTS * dfull.fys, err))) return rc;
-      if ((rc = alloc(&dfz, (size_t)DYN_NSLOTS * dfull.fys, err))) return rc;
-      if ((rc = alloc(&dync, (size_t)p.nx * p.ny * p.nz, err))) return rc;
-      FFS_CK(cudaMemsetAsync(dync, 0, sizeof(double) * (size_t)p.nx * p.ny * p.nz, s));
+      dfull.nsa = I.dynp ? DYN_NSA_P : DYN_NSA;
+      const size_t nsl = I.dynp ? DYN_NSLOTS_P : DYN_NSLOTS, npl = (size_t)p.nx * p.ny * p.nz;
+      if ((rc = alloc(&dfull.fy, nsl * dfull.fys, err))) return rc;
+      if ((rc = alloc(&dfz, nsl * dfull.fys, err))) return rc;
+      // the averaged coefficients in physical space: c [, then cp]
+      if ((rc = alloc(&dync, (I.dynp ? 2 : 1) * npl, err))) return rc;
+      FFS_CK(cudaMemsetAsync(dync, 0, sizeof(double) * (I.dynp ? 2 : 1) * npl, s));
       I.dyn_c = dync;
-      if (I.piom && (rc = alloc(&I.dyn_cm1, (size_t)p.nx * p.ny * p.nz, err))) return rc;
+      if (I.piom && (rc = alloc(&I.dyn_cm1, npl, err))) return rc;
+      if (I.dynp == 2 && (rc = alloc(&I.dyn_cpm1, npl, err))) return rc;
     }
 
     // launch geometry / shared memory
@@ -532,10 +548,17 @@ class Engine : public EngineBase {
 
     // state and header
     if ((rc = reset_state(err))) return rc;
-    if (I.piom) {   // c = cm1 = 0.0289 at construction (les_types.jl:261-266)
+    {   // c = cm1 = 0.0289 (les_types.jl:261-266), cp = cpm1 = 0.09 (les_types.jl:298-305)
       const long long np = (long long)p.nx * p.ny * p.nz;
-      k_dyn_fill<<<(unsigned)std::min<long long>((np + 255) / 256, 65535), 256, 0, s>>>(dync, np, 0.0289);
-      k_dyn_fill<<<(unsigned)std::min<long long>((np + 255) / 256, 65535), 256, 0, s>>>(I.dyn_cm1, np, 0.0289);
+      const unsigned gb = (unsigned)std::min<long long>((np + 255) / 256, 65535);
+      if (I.piom) {
+        k_dyn_fill<<<gb, 256, 0, s>>>(dync, np, 0.0289);
+        k_dyn_fill<<<gb, 256, 0, s>>>(I.dyn_cm1, np, 0.0289);
+      }
+      if (I.dynp == 2) {
+        k_dyn_fill<<<gb, 256, 0, s>>>(dync + np, np, 0.09);
+        k_dyn_fill<<<gb, 256, 0, s>>>(I.dyn_cpm1, np, 0.09);
+      }
       FFS_CK(cudaGetLastError());
     }
     header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
@@ -587,7 +610,8 @@ class Engine : public EngineBase {
     if ((rc = smem_attr(k_fwd_y<T, TX / 2>, smem_y, err))) return rc;
     if ((rc = smem_attr(k_fwd_z_store<T, TX / 2>, smem_z, err))) return rc;
     if ((rc = smem_attr(xpass_ptr(), smem_x, err))) return rc;
-    if (I.dyn && ((rc = smem_attr(k_dyn_x<T, 0>, smem_d0, err)) || (rc = smem_attr(k_dyn_x<T, 1>, smem_d1, err)) ||
+    if (I.dyn && ((rc = smem_attr(I.dynp ? k_dyn_x<T, 0, true> : k_dyn_x<T, 0, false>, smem_d0, err)) ||
+                  (rc = smem_attr(I.dynp ? k_dyn_x<T, 1, true> : k_dyn_x<T, 1, false>, smem_d1, err)) ||
                   (rc = smem_attr(k_dyn_zfilter<T, TX>, smem_dzf, err)) ||
                   (rc = smem_attr(k_dyn_zfilter<T, TX / 2>, smem_dzf, err))))
       return rc;
@@ -901,16 +925,17 @@ class Engine : public EngineBase {
   void launch_dynamic() {
     const Inst<T> J = full_inst();
     const unsigned lines = (unsigned)((long long)P.ny * P.nz);
-    k_dyn_x<T, 0><<<lines, 256, smem_d0, s>>>(I, dfull);
-    launch_dyn_filter(J, 0, DYN_NSA);
-    k_dyn_x<T, 1><<<lines, 256, smem_d1, s>>>(I, dfull);
-    launch_dyn_filter(J, DYN_SLOT_C, 1);
-    Inst<T> C = J;   // physical c from the x-spectral full slot
-    C.wy = dfull.fy + (long long)DYN_SLOT_C * dfull.fys;
+    const int nc = I.dynp ? 2 : 1;   // c [, cp]
+    (I.dynp ? k_dyn_x<T, 0, true> : k_dyn_x<T, 0, false>)<<<lines, 256, smem_d0, s>>>(I, dfull);
+    launch_dyn_filter(J, 0, dfull.nsa);
+    (I.dynp ? k_dyn_x<T, 1, true> : k_dyn_x<T, 1, false>)<<<lines, 256, smem_d1, s>>>(I, dfull);
+    launch_dyn_filter(J, dfull.nsa, nc);
+    Inst<T> C = J;   // physical c [, cp] from the x-spectral full slots
+    C.wy = dfull.fy + (long long)dfull.nsa * dfull.fys;
     C.phys = dync;
-    if (lio == 4) inv_x_phys<4>(C, 1);
-    else if (lio == 2) inv_x_phys<2>(C, 1);
-    else inv_x_phys<1>(C, 1);
+    if (lio == 4) inv_x_phys<4>(C, nc);
+    else if (lio == 2) inv_x_phys<2>(C, nc);
+    else inv_x_phys<1>(C, nc);
   }
   void enqueue_step(int mode) {
     launch_inv_z_step();

@@ -17,7 +17,8 @@ enum FieldCode : int {
   // dynamic Smagorinsky: the test-filtered velocity G u and strain G S (fourierspacep1!,
   // models.jl:99-103), G = exp(-D^2 k^2 / 24) with the test filter width D
   F_GUX, F_GUY, F_GUZ,
-  F_GSXX, F_GSXY, F_GSXZ, F_GSYY, F_GSYZ
+  F_GSXX, F_GSXY, F_GSXZ, F_GSYY, F_GSYZ,
+  F_GWX, F_GWY, F_GWZ            // and with the dynamic P tensor the filtered vorticity G w
 };
 
 // Forward-field roles consumed by the forward z pass.
@@ -64,6 +65,7 @@ struct DevState {
   double nl_h, nl_v, press_h, press_v;  // last non-linear / pressure stats
   double nl_hf, nl_vf, press_hf, press_vf;  // their filtered twins (Stats_fil.txt)
   double dyn_dtm1;         // piomelliSmagorinsky: dt of its previous coefficient (dtm1)
+  double dyn_dtpm1;        // piomelliSandP: dt of its previous cp (dtpm1)
   long long nrec;          // stats records written
   long long nspec;         // spectrum records written
   unsigned int err;        // bit 0: non-finite value in the update
@@ -135,6 +137,8 @@ template <typename T> struct Inst {
   int dyn;                 // dynamic Smagorinsky (FFS_LES_DYNAMIC or FFS_LES_PIOMELLI)
   int piom;                //   piomelliSmagorinsky: extrapolated coefficient in Sa
   double* dyn_cm1;         //   its coefficient of the previous step [z][y][x]
+  int dynp;                //   dynamic P tensor: 1 dynamicSandP, 2 piomelliSandP (cp: dyn_c's second plane)
+  double* dyn_cpm1;        //   piomelliSandP's cp of the previous step
   double dyn_d2h;          //   test filter width^2
   double les_cmin;         //   smallest coefficient kept (cmin)
   int sfil;                // filtered stats and spectra (specFil)

@@ -22,8 +22,8 @@ constexpr int LYZ_IO = 4;  // (y,z) lines per CTA in the transform-only x kernel
 
 struct FieldList {
   int n;
-  int code[20];   // FieldCode (inverse z) or role (forward passes)
-  int slot[20];   // work-array slot
+  int code[24];   // FieldCode (inverse z) or role (forward passes): at most 12 + 11 filtered
+  int slot[24];   // work-array slot
 };
 
 // Block coordinates of one unit of work: the launch's own (single simulation) or an
@@ -125,6 +125,9 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
     case F_GSXZ: fam = 4; ca = 0; cb = 2; break;
     case F_GSYY: fam = 4; ca = 1; cb = 1; break;
     case F_GSYZ: fam = 4; ca = 1; cb = 2; break;
+    case F_GWX: fam = 5; ca = 1; cb = 2; break;
+    case F_GWY: fam = 5; ca = 2; cb = 0; break;
+    case F_GWZ: fam = 5; ca = 0; cb = 1; break;
     case F_UX: fam = 0; ca = 0; break;
     case F_UY: fam = 0; ca = 1; break;
     case F_UZ: fam = 0; ca = 2; break;
@@ -185,6 +188,17 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
         const int kc = zcomp(I, z);
         if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
         return scl(uh[oa + (long long)kc * rowstride + l], gk(l, kc));
+      };
+      fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+    } else if (fam == 5) {
+      auto ld = [&](int l, int z) -> cplx<T> {   // G i (k_b u_c - k_c u_b)
+        const int kc = zcomp(I, z);
+        if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+        const long long o = (long long)kc * rowstride + l;
+        const cplx<T> ub = uh[oa + o], uc = uh[ob + o];
+        const T kb = kax(ca, l, kc), kc_ = kax(cb, l, kc);
+        const T g = gk(l, kc);
+        return mk(g * (-(kb * uc.y - kc_ * ub.y)), g * (kb * uc.x - kc_ * ub.x));
       };
       fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
     } else {
@@ -502,10 +516,38 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         // c the averaged coefficient at this point (NaN kept, as Julia's min/max do)
         const T zz = -xx - yy;
         const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
-        T cc = T(I.dyn_c[(long long)(g0 + q) * n + j]);
+        const long long pi = (long long)(g0 + q) * n + j;
+        T cc = T(I.dyn_c[pi]);
         if (!isnan(cc)) cc = fmax(T(I.les_cmin), fmin(T(0.4), cc));
         const T two_nut = T(2) * (cc * T(I.les_d2) * nrm);
         o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
+        if (I.dynp || I.les_cb != 0.0) {
+          // + max(-0.8, min(0.8, cp)) D^2 Lie(S, W) (les_real_calc.jl:104-106), or SandP's
+          // cb D^2 Lie(S, W) (les_real_calc.jl:98-104)
+          T b;
+          if (I.dynp) {
+            T cp = T(I.dyn_c[(long long)I.nx * I.ny * I.nz + pi]);
+            if (!isnan(cp)) cp = fmax(T(-0.8), fmin(T(0.8), cp));
+            b = cp * T(I.les_d2);
+          } else {
+            b = T(I.les_cb) * T(I.les_d2);
+          }
+          const T zz2 = -xx - yy;
+          const T Sm[3][3] = {{xx, xy, xz}, {xy, yy, yz}, {xz, yz, zz2}};
+          const T p_ = T(0.5) * wx, q_ = T(0.5) * wy, r_ = T(0.5) * wz;
+          const T W[3][3] = {{T(0), -r_, q_}, {r_, T(0), -p_}, {-q_, p_, T(0)}};
+          T lie[5];
+          const int ii[5] = {0, 0, 0, 1, 1}, jj[5] = {0, 1, 2, 1, 2};
+#pragma unroll
+          for (int e2 = 0; e2 < 5; ++e2) {
+            T a2 = T(0), b2 = T(0);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { a2 += Sm[ii[e2]][k] * W[k][jj[e2]]; b2 += W[ii[e2]][k] * Sm[k][jj[e2]]; }
+            lie[e2] = a2 - b2;
+          }
+#pragma unroll
+          for (int e2 = 0; e2 < 5; ++e2) o[4 + e2] += b * lie[e2];
+        }
       } else {
         les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4);
       }

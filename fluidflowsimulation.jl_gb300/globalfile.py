@@ -51,9 +51,19 @@ def _set_les(p: FFSParams, d: dict[str, str]) -> None:
     stableNonLinear, dynamicSmagorinsky or piomelliSmagorinsky (les_types.jl:388-397:
     filterWidth, TestFilterWidth with default twice the filter width, cmin), or SandP (the
     P tensor term on top of sLesModel = Smagorinsky, Vreman or productionViscosity). The
-    dynamic P-tensor variants (dynamicSandP, piomelliSandP) are not built."""
+    dynamic P-tensor variants dynamicSandP and piomelliSandP take sLesModel =
+    dynamicSmagorinsky or piomelliSmagorinsky."""
     m = d["lesModel"]
     base = m
+    if m == "SandP" and d.get("sLesModel") in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
+        p.sandp_cb = parse_number(d.get("pConstant", "0.09"))   # SandP on a dynamic model (les_types.jl:401-416)
+        m = d["sLesModel"]
+    if m in ("dynamicSandP", "piomelliSandP"):          # les_types.jl:426-455
+        base = d.get("sLesModel", "")
+        if base not in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
+            raise ValueError(f"{m} with sLesModel {base!r} is not supported (dynamicSmagorinsky, piomelliSmagorinsky)")
+        p.les_dynp = 1 if m == "dynamicSandP" else 2
+        m = base
     if m in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
         p.les = 1
         p.les_model = LES_MODELS[m]

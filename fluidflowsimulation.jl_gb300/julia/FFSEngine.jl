@@ -37,7 +37,7 @@ mutable struct FFSParams
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
-    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; radix_split::Int32
+    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; les_dynp::Int32; radix_split::Int32
     FFSParams() = new()
 end
 
@@ -88,8 +88,16 @@ function parameters(d)
         p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
         p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
     end
-    if haskey(d, :lesModel) && d[:lesModel] in ("dynamicSmagorinsky", "piomelliSmagorinsky")   # les_types.jl:388-397
-        p.les = 1; p.les_model = d[:lesModel] == "dynamicSmagorinsky" ? 5 : 6
+    if haskey(d, :lesModel) && (d[:lesModel] in ("dynamicSmagorinsky", "piomelliSmagorinsky", "dynamicSandP",
+                                                  "piomelliSandP") ||
+                                (d[:lesModel] == "SandP" && get(d, :sLesModel, "") in ("dynamicSmagorinsky",
+                                                                                       "piomelliSmagorinsky")))
+        m = d[:lesModel]   # les_types.jl:388-455
+        p.les_dynp = m == "dynamicSandP" ? 1 : (m == "piomelliSandP" ? 2 : 0)
+        p.sandp_cb = m == "SandP" ? (haskey(d, :pConstant) ? num(d[:pConstant]) : 0.09) : 0.0
+        base = (p.les_dynp == 0 && m != "SandP") ? m : d[:sLesModel]
+        base in ("dynamicSmagorinsky", "piomelliSmagorinsky") || error("lesModel $m needs a dynamic sLesModel")
+        p.les = 1; p.les_model = base == "dynamicSmagorinsky" ? 5 : 6
         p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) : 0.0
         p.les_test_width = haskey(d, :TestFilterWidth) ? num(d[:TestFilterWidth]) : 0.0
         p.les_cmin = haskey(d, :cmin) ? parse(Float64, d[:cmin]) : 0.0

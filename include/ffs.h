@@ -112,6 +112,9 @@ typedef struct ffs_params {
                                   carries the Stats_fil.txt row (quadratic sums weighted by the Gaussian
                                   filter squared, D = 2 pi lx nf / nx) and the spectrum records the
                                   *_fil spectra; 0: off */
+  int32_t les_dynp;            /* with FFS_LES_DYNAMIC / FFS_LES_PIOMELLI: the dynamic P tensor term,
+                                  1 dynamicSandP, 2 piomelliSandP (les_types.jl:199-330,
+                                  les_real_calc.jl:104-106); 0 none */
   int32_t radix_split;         /* runtime FFT plans: 0 the default radix split of each axis, k = 1, 2 the
                                   k-th alternative split (where the length has one; the autotuner times
                                   them and keeps the fastest per axis) */

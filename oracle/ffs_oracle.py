@@ -151,6 +151,7 @@ class Params:
     les_cp: float = 5.0                  # silvisPConstant
     les_test_width: float = 0.0          # dynamicSmagorinsky: TestFilterWidth (default 2 filterWidth)
     les_cmin: float = 0.0                # dynamicSmagorinsky: cmin
+    les_dynp: str = ""                   # "dynamicSandP" / "piomelliSandP": the dynamic P tensor term
     sandp_cb: float = 0.0                # SandP: pConstant (0: no P term)
     filter_width: float | None = None
     scalar: bool = False                 # passiveScalar (simulationtypes.jl:198-213, :320-352)
@@ -250,6 +251,16 @@ class Params:
         to an eddy-viscosity model (sLesModel)."""
         m = d["lesModel"]
         base = m
+        if m == "SandP" and d.get("sLesModel") in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
+            # SandP on a dynamic model (les_types.jl:401-416): beta = cb D^2 (les_real_calc.jl:57-58)
+            self.sandp_cb = _num(d.get("pConstant", "0.09"))
+            m = base = d["sLesModel"]
+        if m in ("dynamicSandP", "piomelliSandP"):         # les_types.jl:426-455
+            base = d["sLesModel"]
+            if base not in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
+                raise ValueError(f"LES model {m} / {base} is not restated")
+            self.les_dynp = m
+            m = base
         if m in ("dynamicSmagorinsky", "piomelliSmagorinsky"):   # les_types.jl:388-397
             self.les = True
             self.les_model = m
@@ -932,6 +943,8 @@ class OracleSimulation:
         # piomelliSmagorinsky's coefficient state (c, cm1, dtm1)
         self.piom_c = self.piom_cm1 = None
         self.piom_dtm1 = 0.0
+        self.piom_cp = self.piom_cpm1 = None
+        self.piom_dtpm1 = 0.0
 
     # ---------------------------------------------------------------- time helpers
     def get_dt(self):
@@ -983,7 +996,7 @@ class OracleSimulation:
         if p.les:
             Sr = g.real(S)
             if p.les_model in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
-                taur = self.dynamic_smagorinsky(u, ur, S, Sr)
+                taur = self.dynamic_smagorinsky(u, ur, S, Sr, w, wr)
             else:
                 taur = les_stress(p, Sr, wr)
         # realspacecalculation! (models.jl:236-280): rhs = u x w ; flux = -rho u
@@ -1043,14 +1056,23 @@ class OracleSimulation:
             rr[g.dealias] = 0.0
             self.rhorhs = rr
 
-    def dynamic_smagorinsky(self, u, ur, S, Sr):
+    def dynamic_smagorinsky(self, u, ur, S, Sr, w=None, wr=None):
         """The dynamic Smagorinsky model (dynamic_smagorinsky.jl:3-217, les_real_calc.jl:3-11,
         71-73): test-filtered u and S (fourierspacep1!, models.jl:99-108), Sa = D^2 |S| S and
         L = u u filtered over the full spectrum (fourierspace_dynamic_les_calculation!), the
         Germano coefficient c = clamp(L:M / 2 M:M, -1, 1) with L = traceless(u^ u^ - (uu)^)
         and M = (D^^2 + D^2) |S^| S^ - (D^2 |S| S)^, c averaged by the same filter
         (average_c!, dynamic_piomelli.jl:13-26), then nu_t = max(cmin, min(0.4, c)) D^2 |S|.
-        The filter is Gaussfilter (utils.jl:220-225): exp(-D^^2 k^2 / 24)."""
+        The filter is Gaussfilter (utils.jl:220-225): exp(-D^^2 k^2 / 24).
+
+        With the dynamic P tensor (dynamicSandP / piomelliSandP, les_types.jl:199-330):
+        P = D^2 Lie(S, W), W = AntiSymTen(w/2) (times the extrapolated cp for piomelliSandP,
+        cp = cpm1 = 0.09 at construction), filtered like Sa; w^ = G w; P^ = Lie(S^, W^);
+        dynamicSandP: cp = clamp(L:Mp / Mp:Mp, -1, 1), Mp = (D^^2 + D^2) P^ - P~;
+        piomelliSandP: cp = clamp((tau^ + L):Mp / Mp:Mp, -1, 1), Mp = (D^^2 + D^2) P^, tau^ =
+        P~ (+ Sa~ with piomelliSmagorinsky, whose own tau^ then includes P~ too); cp averaged
+        like c; tau += clamp(cp, -0.8, 0.8) D^2 Lie(S, W) (dynamic_smagorinsky.jl:3-217,
+        les_real_calc.jl:104-106)."""
         p, g = self.p, self.g
         d2 = p.filter_width ** 2
         dh2 = p.les_test_width ** 2
@@ -1068,6 +1090,29 @@ class OracleSimulation:
         uf = g.real(G[None] * u)                                   # u^ (physical)
         Sh = g.real(G[None] * S)                                   # S^ (physical)
         piomelli = p.les_model == "piomelliSmagorinsky"
+        dynp = p.les_dynp
+        if dynp:
+            def lie5(S5, wv):
+                A, B = _sym33(S5), _antisym(0.5 * wv)
+                return _to5(_mm(A, B) - _mm(B, A))
+            lie_r = lie5(Sr, wr)
+            if dynp == "piomelliSandP":     # calc_cstar! on cp (dynamic_smagorinsky.jl:22-35)
+                if self.piom_cp is None:
+                    self.piom_cp = np.full(ur[0].shape, 0.09)
+                    self.piom_cpm1 = np.full(ur[0].shape, 0.09)
+                dt = self.get_dt()
+                dtf = 1.0 if dt == 0.0 else dt
+                dtm1f = dtf if self.piom_dtpm1 == 0.0 else self.piom_dtpm1
+                if self.iteration == 0:
+                    self.piom_cpm1 = self.piom_cp.copy()
+                cpstar = (dtf / dtm1f) * (self.piom_cp - self.piom_cpm1) + self.piom_cp
+                self.piom_cpm1 = self.piom_cp
+                self.piom_dtpm1 = dt
+                Pa = (cpstar * d2)[None] * lie_r                   # cp D^2 Lie(S, W)
+            else:
+                Pa = d2 * lie_r                                    # D^2 Lie(S, W)
+            Paf = np.stack([full_filter(x) for x in Pa])
+            wh = g.real(G[None] * w)                               # w^ (physical)
         if piomelli:
             # calc_cstar! (dynamic_smagorinsky.jl:9-19, dynamic_piomelli.jl:1-11): the last
             # averaged coefficient extrapolated in time, c* = c + (dt/dtm1)(c - cm1); c and
@@ -1097,6 +1142,16 @@ class OracleSimulation:
         L6[0] -= tr
         L6[3] -= tr
         L6[5] -= tr
+        def ddot_n(t5, M5):           # (t + L) : M / (M:M), t traceless (5 components)
+            mxx, mxy, mxz, myy, myz = M5
+            mzz = -mxx - myy
+            mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
+            nxx, nxy, nxz, nyy, nyz, nzz = mxx / mm, mxy / mm, mxz / mm, myy / mm, myz / mm, mzz / mm
+            txx, txy, txz, tyy, tyz = t5
+            tzz = -txx - tyy
+            return ((txx + L6[0]) * nxx + (tyy + L6[3]) * nyy + (tzz + L6[5]) * nzz
+                    + 2.0 * ((txy + L6[1]) * nxy + (txz + L6[2]) * nxz + (tyz + L6[4]) * nyz))
+
         if piomelli:
             # c = (tau^ + L) : M / (M:M), M = 2 (D^^2 + D^2) |S^| S^ (dynamic_smagorinsky.jl:174-185)
             M5 = (2 * (dh2 + d2) * nrm5(Sh))[None] * Sh
@@ -1104,7 +1159,7 @@ class OracleSimulation:
             mzz = -mxx - myy
             mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
             nxx, nxy, nxz, nyy, nyz, nzz = mxx / mm, mxy / mm, mxz / mm, myy / mm, myz / mm, mzz / mm
-            txx, txy, txz, tyy, tyz = Saf
+            txx, txy, txz, tyy, tyz = Saf + Paf if dynp == "piomelliSandP" else Saf
             tzz = -txx - tyy
             cv = ((txx + L6[0]) * nxx + (tyy + L6[3]) * nyy + (tzz + L6[5]) * nzz
                   + 2.0 * ((txy + L6[1]) * nxy + (txz + L6[2]) * nxz + (tyz + L6[4]) * nyz))
@@ -1119,8 +1174,30 @@ class OracleSimulation:
         cf = full_filter(cf)                                       # average_c!
         if piomelli:
             self.piom_c = cf
+        cpf = None
+        if dynp:
+            Ph = lie5(Sh, wh)                                      # Lie(S^, AntiSymTen(w^/2))
+            dsum = dh2 + d2
+            if dynp == "dynamicSandP":
+                Mp = dsum * Ph - Paf
+                mxx, mxy, mxz, myy, myz = Mp
+                mzz = -mxx - myy
+                lm = (L6[0] * mxx + L6[3] * myy + L6[5] * mzz + 2.0 * (L6[1] * mxy + L6[2] * mxz + L6[4] * myz))
+                mm = mxx * mxx + myy * myy + mzz * mzz + 2.0 * (mxy * mxy + mxz * mxz + myz * myz)
+                cpv = lm / mm
+            else:
+                cpv = ddot_n(Saf + Paf if piomelli else Paf, dsum * Ph)
+            cpf = full_filter(np.maximum(-1.0, np.minimum(1.0, cpv)))   # average_c! of cp
+            if dynp == "piomelliSandP":
+                self.piom_cp = cpf
         nut = np.maximum(p.les_cmin, np.minimum(0.4, cf)) * d2 * nrm5(Sr)
-        return 2.0 * nut[None] * Sr
+        tau = 2.0 * nut[None] * Sr
+        if p.sandp_cb:                # SandP: tau += cb D^2 Lie(S, W) (les_real_calc.jl:98-104)
+            A, B = _sym33(Sr), _antisym(0.5 * wr)
+            tau = tau + (p.sandp_cb * d2) * _to5(_mm(A, B) - _mm(B, A))
+        if dynp:
+            tau = tau + (np.maximum(-0.8, np.minimum(0.8, cpf)) * d2)[None] * lie_r
+        return tau
 
     def div_tau(self, tauh):
         """(i k) . tau for a symmetric traceless tau (models.jl:330)."""

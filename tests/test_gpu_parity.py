@@ -96,6 +96,14 @@ FIXED_CASES = {
     "ab3-adaptive-piomelli": gdict(32, adaptive=True, lesModel="piomelliSmagorinsky"),
     "etd-piomelli-48-cmin": gdict(48, "ETD3rdO", lesModel="piomelliSmagorinsky", cmin="-0.05",
                                   TestFilterWidth="0.35"),
+    # the dynamic P tensor term (dynamicSandP / piomelliSandP) on either dynamic model
+    "etd-dynamic-sandp": gdict(32, "ETD3rdO", lesModel="dynamicSandP", sLesModel="dynamicSmagorinsky"),
+    "ab3-adaptive-piomelli-sandp": gdict(32, adaptive=True, lesModel="piomelliSandP", sLesModel="piomelliSmagorinsky"),
+    "ab3-adaptive-piomellip-dynamic": gdict(32, adaptive=True, lesModel="piomelliSandP",
+                                            sLesModel="dynamicSmagorinsky"),
+    "etd-48-dynamicsandp-piomelli": gdict(48, "ETD3rdO", lesModel="dynamicSandP", sLesModel="piomelliSmagorinsky",
+                                          cmin="-0.02"),
+    "ab3-sandp-dynamic": gdict(32, lesModel="SandP", sLesModel="dynamicSmagorinsky", pConstant="0.12"),
     # the reference's kz = 0 plane forcing family (forcing_types.jl:335-450)
     "ab3-adaptive-rf-forcing": gdict(32, adaptive=True, forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
     "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
@@ -171,7 +179,8 @@ def test_etd_adaptive_parity(gpu_pkg):
 
 
 @pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
-                                  "ab3-stable-nonlinear", "etd-dynamic-smagorinsky", "ab3-adaptive-piomelli"])
+                                  "ab3-stable-nonlinear", "etd-dynamic-smagorinsky", "ab3-adaptive-piomelli",
+                                  "ab3-adaptive-piomelli-sandp"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)

@@ -134,11 +134,11 @@ def test_parameters_rejects_out_of_scope_models(pkg):
         pkg.parameters(d)
     for m in ("dynamicSandP", "piomelliSandP"):
         with pytest.raises(ValueError):
-            pkg.parameters(dict(d, lesModel=m, sLesModel="dynamicSmagorinsky"))
+            pkg.parameters(dict(d, lesModel=m, sLesModel="Smagorinsky"))
     with pytest.raises(ValueError):
         pkg.parameters(dict(d, lesModel="SandP", sLesModel="Silvis"))
-    with pytest.raises(ValueError):
-        pkg.parameters(dict(d, lesModel="SandP", sLesModel="dynamicSmagorinsky"))
+    p = pkg.parameters(dict(d, lesModel="SandP", sLesModel="dynamicSmagorinsky"))   # les_types.jl:401-416
+    assert (p.les_model, p.sandp_cb, p.les_dynp) == (5, 0.09, 0)
 
 
 def test_parameters_les_models(pkg):
@@ -178,6 +178,12 @@ def test_parameters_les_models(pkg):
     assert o.filter_width == pytest.approx(dx) and o.les_test_width == pytest.approx(2 * dx)
     p = pkg.parameters(dict(base, lesModel="piomelliSmagorinsky"))
     assert (p.les, p.les_model, p.les_test_width) == (1, 6, 0.0)
+    for m, dp in (("dynamicSandP", 1), ("piomelliSandP", 2)):   # les_types.jl:426-455
+        for sm, mid in (("dynamicSmagorinsky", 5), ("piomelliSmagorinsky", 6)):
+            p = pkg.parameters(dict(base, lesModel=m, sLesModel=sm))
+            assert (p.les, p.les_model, p.les_dynp) == (1, mid, dp)
+            o = Params.from_global(dict(base, lesModel=m, sLesModel=sm))
+            assert (o.les_model, o.les_dynp) == (sm, m)
     d = dict(base, lesModel="dynamicSmagorinsky", filterWidth="0.2", TestFilterWidth="0.5", cmin="-0.1")
     p, o = pkg.parameters(d), Params.from_global(d)
     assert (p.filter_width, p.les_test_width, p.les_cmin) == (0.2, 0.5, -0.1)
