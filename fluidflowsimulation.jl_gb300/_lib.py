@@ -55,7 +55,9 @@ class FFSParams(ctypes.Structure):
         ("passive_scalar", c_int32), ("scalar_pr", c_double), ("scalar_gradient", c_double), ("scalar_dir", c_int32),
         ("plane_forcing", c_int32), ("pf_tf", c_double), ("pf_alpha", c_double), ("pf_kf", c_double),
         ("pf_zf_tanh", c_int32), ("pf_qp", c_double), ("pf_qc", c_double), ("pf_qkf", c_double),
-        ("les_test_width", c_double), ("les_cmin", c_double), ("spec_fil", c_double), ("les_dynp", c_int32), ("radix_split", c_int32),
+        ("les_test_width", c_double), ("les_cmin", c_double), ("spec_fil", c_double), ("les_dynp", c_int32),
+        ("hv_kind", c_int32), ("hv_initk", c_double), ("hv_endk", c_double), ("rho_hv", c_int32), ("rho_hv_nu", c_double),
+        ("rho_hv_m", c_int32), ("rho_hv_initk", c_double), ("rho_hv_endk", c_double), ("radix_split", c_int32),
     ]
 
 

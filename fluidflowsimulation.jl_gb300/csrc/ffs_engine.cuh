@@ -204,6 +204,17 @@ class Engine : public EngineBase {
     I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
     I.ab3 = p.integrator == FFS_AB3; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
     I.hv = p.hyperviscosity != 0; I.hv_m = p.hv_m; I.hv_nu = p.hv_nu;
+    {   // the spectral barrier's defaults (simulationtypes.jl:294-297, density_stratification_types.jl
+        // :137-141): initk = cutoff 2 kx_max / 3, endk = sqrt(3 cutoff) kx_max, kx_max = (nx/2)/lx
+      const double kxm = (double)(p.nx / 2) / p.lx;
+      I.hv_kind = p.hv_kind;
+      I.hv_initk = p.hv_initk > 0 ? p.hv_initk : p.cutoff * 2 * kxm / 3;
+      I.hv_endk = p.hv_endk > 0 ? p.hv_endk : sqrt(p.cutoff * 3) * kxm;
+      I.rho_hv = p.density ? p.rho_hv : 0;
+      I.rho_hv_nu = p.rho_hv_nu; I.rho_hv_m = p.rho_hv_m;
+      I.rho_hv_initk = p.rho_hv_initk > 0 ? p.rho_hv_initk : p.cutoff * 2 * kxm / 3;
+      I.rho_hv_endk = p.rho_hv_endk > 0 ? p.rho_hv_endk : sqrt(p.cutoff * 3) * kxm;
+    }
     I.les = p.les != 0;
     const double fw = p.filter_width > 0 ? p.filter_width : (p.lx * 2 * M_PI / p.nx) / p.cutoff;
     I.les_alpha = p.smag_c * p.smag_c * fw * fw;
@@ -272,7 +283,18 @@ class Engine : public EngineBase {
     if (p.dt_stat <= 0 || p.dt_spec <= 0) { err = "dtStat and dtSpec must be positive"; return FFS_EINVAL; }
     if (p.integrator != FFS_ETD3 && p.integrator != FFS_AB3) { err = "unknown integrator"; return FFS_EINVAL; }
     if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
-    if (p.hyperviscosity && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
+    if (p.hyperviscosity && p.hv_kind == 0 && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
+    if (p.hyperviscosity && (p.hv_kind < 0 || p.hv_kind > 1)) { err = "unknown hyperviscosity kind"; return FFS_EINVAL; }
+    if (p.hyperviscosity && p.hv_kind == 1 && p.integrator == FFS_AB3) {
+      // the reference's explicit viscous term needs an exponent M the barrier does not have
+      err = "hyperViscosity spectralBarrier needs velocityTimeStep ETD3rdO";
+      return FFS_EUNSUPPORTED;
+    }
+    if (p.rho_hv < 0 || p.rho_hv > 2 || (p.rho_hv == 1 && (p.rho_hv_m < 1 || p.rho_hv_m > 8))) {
+      err = "bad densityHyperViscosity";
+      return FFS_EINVAL;
+    }
+    if (p.rho_hv && p.passive_scalar) { err = "densityHyperViscosity takes densityStratification"; return FFS_EINVAL; }
     if (p.density && (p.gravity_dir < 0 || p.gravity_dir > 2)) { err = "gravity direction must be 0..2"; return FFS_EINVAL; }
     if (p.les && (p.les_model < FFS_LES_SMAGORINSKY || p.les_model > FFS_LES_PIOMELLI)) {
       err = "unknown LES model";
@@ -485,7 +507,7 @@ class Engine : public EngineBase {
       n_sms = sms;
     }
     // record layout
-    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8) : 0) + (I.les ? 4 : 0) +
+    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8 + (I.rho_hv ? 1 : 0)) : 0) + (I.les ? 4 : 0) +
                   (I.pforce == FFS_PF_A ? 2 : ((I.forcing || I.pforce) ? 3 : 0)) + (I.hv ? 3 : 0);
     if (I.pforce && (rc = plane_forcing_tables(p, err))) return rc;
     // a record: the Stats.txt row, 13 Scales.txt inputs, then with specFil the
@@ -563,7 +585,8 @@ class Engine : public EngineBase {
     }
     header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
     if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
-    else if (I.density) header += ",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux";
+    else if (I.density) header += std::string(",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux") +
+                                  (I.rho_hv ? ",rhohdiss" : "");
     if (I.les) header += ",prh,prv,praniso,pr";
     if (I.pforce == FFS_PF_A) header += ",hp,vp";
     else if (I.forcing || I.pforce) header += ",hp,vp,tp";

@@ -41,6 +41,7 @@ enum StatQ : int {
   // only the last retained kx of each line, as the reference's filtered dx_squared_mean
   Q_FU12 = Q_IL0 + 9, Q_FU22, Q_FU32, Q_FEH, Q_FEV, Q_FNLH, Q_FNLV, Q_FLESH, Q_FLESV, Q_FHVH, Q_FHVV,
   Q_FRHO2, Q_FDR1, Q_FDR2, Q_FDR3, Q_FBF,
+  Q_RHV, Q_FRHV,   // density hyperviscous sum (rhohdiss) and its filtered twin
   Q_COUNT
 };
 constexpr int QPAD = 56;
@@ -128,6 +129,10 @@ template <typename T> struct Inst {
   int ab3, adaptive, ref_slot;
   int hv, hv_m;
   double hv_nu;
+  int hv_kind;             // 0 nuh k^2M, 1 the spectral barrier (hv_initk, hv_endk)
+  double hv_initk, hv_endk;
+  int rho_hv, rho_hv_m;    // density hyperviscosity: 0 none, 1 rho_hv_nu k^2M, 2 the spectral barrier
+  double rho_hv_nu, rho_hv_initk, rho_hv_endk;
   int les;
   double les_alpha;        // c^2 Delta^2
   int les_model;           // FFS_LES_* (Smagorinsky, Vreman, production, Silvis, stable non-linear)

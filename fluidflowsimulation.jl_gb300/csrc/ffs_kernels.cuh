@@ -601,10 +601,30 @@ __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   b_x_pass<T, LES, DEN, LYZ>(I, Blk::here());
 }
 
-// velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95);
-// muladd(modk, m_nu, modk^M * m_nuh) is a single-rounding fma in the reference.
+// The spectral barrier (hyperviscosity_types.jl:32-48): log(esp(|k|, i, p, 1/4)) with
+// esp = 1 for |k| <= i, exp(-(|k| - i)^2 / (p^(1/4) - |k|^(1/4))) for |k| < p, 0 beyond.
+__device__ __forceinline__ double barrier_f(double k, double i, double p) {
+  const double a = fabs(k);
+  const double e = a <= i ? 1.0 : (a < p ? exp(-((a - i) * (a - i)) / (pow(p, 0.25) - pow(a, 0.25))) : 0.0);
+  return log(e);
+}
+// the barrier as a stats / spectrum weight: -inf (beyond endk) counts 0 (stats.jl:1160-1161)
+__device__ __forceinline__ double barrier_w(double k2, double i, double p) {
+  const double f = barrier_f(sqrt(k2), i, p);
+  return isinf(f) ? 0.0 : f;
+}
+
+// velocity integrating-factor exponent c(k^2) = -nu k^2 - nuh (k^2)^M (ETD.jl:60-95), or
+// muladd(k^2, -nu, f(|k|)) with the spectral barrier f (ETD.jl:71-82); muladd is a
+// single-rounding fma in the reference.
 template <typename T> __device__ __forceinline__ double c_vel(const Inst<T>& I, double k2) {
   if (!I.hv) return dd::M(k2, -I.nu);
+  if (I.hv_kind == 1) {
+    // f = log(0) = -inf (beyond endk, or exp underflow): muladd gives -inf, whose ETD
+    // coefficients are 0 (ETD.jl:182-191)
+    const double f = barrier_f(sqrt(k2), I.hv_initk, I.hv_endk);
+    return isinf(f) ? -INFINITY : dd::fma_e(k2, -I.nu, f);
+  }
   double km = k2;
   for (int m = 1; m < I.hv_m; ++m) km = dd::M(km, k2);
   return dd::fma_e(k2, -I.nu, dd::M(km, -I.hv_nu));
@@ -996,12 +1016,19 @@ __device__ __forceinline__ void b_etd_table(const Inst<T>& I, int mode, const Bl
     e[0] = T(E); e[1] = T(A); e[2] = T(B); e[3] = T(C);
     if (I.density && I.etab_rho) {
       // c = -alpha k^2; the passive scalar's ETD3rdO takes the velocity's hyperviscosity
-      // (simulationtypes.jl:336): muladd(k2, -alpha, k2^M * -nuh)
+      // (simulationtypes.jl:336): muladd(k2, -alpha, k2^M * -nuh) or with the barrier
+      // muladd(k2, -alpha, f(|k|)); the density its own (densityHyperViscosity,
+      // density_stratification_types.jl:137-148, 172-176)
       double cr = dd::M(k2, -I.alpha);
-      if (I.scalar && I.hv) {
+      const int hk = I.scalar ? (I.hv ? (I.hv_kind == 1 ? 2 : 1) : 0) : I.rho_hv;
+      if (hk == 1) {
+        const int M = I.scalar ? I.hv_m : I.rho_hv_m;
         double km = k2;
-        for (int m = 1; m < I.hv_m; ++m) km = dd::M(km, k2);
-        cr = dd::fma_e(k2, -I.alpha, dd::M(km, -I.hv_nu));
+        for (int m = 1; m < M; ++m) km = dd::M(km, k2);
+        cr = dd::fma_e(k2, -I.alpha, dd::M(km, -(I.scalar ? I.hv_nu : I.rho_hv_nu)));
+      } else if (hk == 2) {
+        const double f = barrier_f(sqrt(k2), I.scalar ? I.hv_initk : I.rho_hv_initk, I.scalar ? I.hv_endk : I.rho_hv_endk);
+        cr = isinf(f) ? -INFINITY : dd::fma_e(k2, -I.alpha, f);
       }
       etd_coeffs_exact<sizeof(T) == 8>(cr, dt, dt2, dt3, stage, E, A, B, C);
       T* r = I.etab_rho + 4 * q;
@@ -1430,8 +1457,11 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       if (I.sfil) { q[Q_PH] += lh * G2; q[Q_PV] += lv * G2; }
     }
     if (I.hv) {
+      // (k^2)^M (hyperviscosity_stats, stats.jl:532-561) or the barrier weight f(|k|)
+      // (spectral_barrier_stats, hyperviscosity_types.jl:51-82)
       T km = T(1);
-      for (int i = 0; i < I.hv_m; ++i) km *= k2;
+      if (I.hv_kind == 1) km = T(barrier_w((double)k2, I.hv_initk, I.hv_endk));
+      else for (int i = 0; i < I.hv_m; ++i) km *= k2;
       q[Q_HVH] += w * km * (a2[0] + a2[1]);
       q[Q_HVV] += w * km * a2[2];
       if (I.sfil) { q[Q_FHVH] += w * km * (a2[0] + a2[1]) * G2; q[Q_FHVV] += w * km * a2[2] * G2; }
@@ -1446,7 +1476,14 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
       q[Q_RHO2] += w * r2;
       q[Q_DR1] += w * kx * kx * r2; q[Q_DR2] += w * ky * ky * r2; q[Q_DR3] += w * kz * kz * r2;
       q[Q_BF] += w * (u[I.gdir].x * rho.x + u[I.gdir].y * rho.y);
+      T rw = T(0);
+      if (I.rho_hv) {   // scalar_hvis_stats (stats.jl:1086-1110, 1145-1171)
+        if (I.rho_hv == 2) rw = T(barrier_w((double)k2, I.rho_hv_initk, I.rho_hv_endk));
+        else { rw = T(1); for (int i = 0; i < I.rho_hv_m; ++i) rw *= k2; }
+        q[Q_RHV] += w * rw * r2;
+      }
       if (I.sfil) {
+        if (I.rho_hv) q[Q_FRHV] += w * rw * r2 * G2;
         q[Q_FRHO2] += w * r2 * G2;
         if (ix == I.Mx - 1) q[Q_FDR1] += w * kx * kx * r2 * G2;   // stats.jl:370 (ee_fil = ...)
         q[Q_FDR2] += w * ky * ky * r2 * G2; q[Q_FDR3] += w * kz * kz * r2 * G2;
@@ -1573,9 +1610,11 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
       if (I.sfil) { bin(ff + 6, G2 * (pr[0] + pr[1])); bin(ff + 7, G2 * pr[2]); }
     }
     if (I.les) { bin(f, les[0] + les[1]); bin(f + 1, les[2]); f += 2; }
-    if (I.hv) {   // spectrum_hyperviscosity: nuh (k^2)^M proj(u, u)
+    if (I.hv) {   // spectrum_hyperviscosity: nuh (k^2)^M proj(u, u); spectrum_spectral_barrier: f(|k|) proj(u, u)
       double km = k2;
       for (int i = 1; i < I.hv_m; ++i) km *= k2;
+      if (I.hv_kind == 1) km = barrier_w(k2, I.hv_initk, I.hv_endk);
+      const double nuh = I.hv_kind == 1 ? 1.0 : I.hv_nu;
       bin(f, nuh * km * (a2[0] + a2[1]));
       bin(f + 1, nuh * km * a2[2]);
       if (I.sfil) { bin(ff + 8, G2 * (nuh * km * (a2[0] + a2[1]))); bin(ff + 9, G2 * (nuh * km * a2[2])); }
@@ -1665,16 +1704,24 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
         row[c++] = -(nlh + ph); row[c++] = nlv + pv;
         const double lesh = tot[f ? Q_FLESH : Q_LESH], lesv = tot[f ? Q_FLESV : Q_LESV];
         const double hvh = tot[f ? Q_FHVH : Q_HVH], hvv = tot[f ? Q_FHVV : Q_HVV];
+        // hyperviscous columns: nuh x the (k^2)^M sums, or minus the barrier sums
+        const double hvs = I.hv_kind == 1 ? -1.0 : I.hv_nu;
         double tdiss = eh + ev;
         if (I.les) tdiss += -lesh - lesv;
-        if (I.hv) tdiss += I.hv_nu * (hvh + hvv);
+        if (I.hv) tdiss += hvs * (hvh + hvv);
         row[c++] = tdiss;
         if (I.density) {   // density (BoussinesqApproximation stats) or scalar_stats (stats.jl:221-233)
           const double d1 = tot[f ? Q_FDR1 : Q_DR1], d2 = tot[f ? Q_FDR2 : Q_DR2], d3 = tot[f ? Q_FDR3 : Q_DR3];
           const double rd = I.alpha * (d1 + d2 + d3);
           row[c++] = tot[Q_RHO]; row[c++] = tot[f ? Q_FRHO2 : Q_RHO2]; row[c++] = d1; row[c++] = d2;
           row[c++] = d3; row[c++] = rd;
-          if (!I.scalar) { row[c++] = rd; row[c++] = -I.gval * tot[f ? Q_FBF : Q_BF]; }
+          if (!I.scalar) {
+            // density hyperviscosity (density_stratification_types.jl:69-84): trhodiss += rhohdiss
+            const double rh = I.rho_hv == 2 ? -tot[f ? Q_FRHV : Q_RHV] : I.rho_hv_nu * tot[f ? Q_FRHV : Q_RHV];
+            row[c++] = I.rho_hv ? rd + rh : rd;
+            row[c++] = -I.gval * tot[f ? Q_FBF : Q_BF];
+            if (I.rho_hv) row[c++] = rh;
+          }
         }
         if (I.les) {
           const double prh = -lesh, prv = -lesv;
@@ -1689,7 +1736,7 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
           row[c++] = S->pf_hp; row[c++] = S->pf_vp; row[c++] = S->pf_hp + S->pf_vp;
         }
         if (I.hv) {
-          row[c++] = I.hv_nu * hvh; row[c++] = I.hv_nu * hvv; row[c++] = I.hv_nu * (hvh + hvv);
+          row[c++] = hvs * hvh; row[c++] = hvs * hvv; row[c++] = hvs * (hvh + hvv);
         }
         return c;
       };
@@ -1707,11 +1754,12 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       double slot = tot[Q_D2DX];
       // STAT_FIL: the scalar's and the density's filtered sums go through reductionh
       // (scalar_stats, buoyancy_flux: density_stratification_types.jl:192-210)
-      if (I.sfil && I.density) slot = I.scalar ? tot[Q_FDR3] : tot[Q_FBF];
+      if (I.sfil && I.density) slot = I.scalar ? tot[Q_FDR3] : (I.rho_hv ? tot[Q_FRHV] : tot[Q_FBF]);
       if (I.les) slot = tot[Q_LESH];
       if (I.hv) slot = tot[Q_HVH];
       S->slot_u = slot;
-      if (I.density) S->slot_rho = tot[Q_BF];
+      // the density's reduction: the buoyancy flux sum, then its hyperviscous sum
+      if (I.density) S->slot_rho = I.rho_hv ? tot[Q_RHV] : tot[Q_BF];
     }
   }
   if (mode != 1 && (it % I.dt_spec) == 0) S->nspec += 1;

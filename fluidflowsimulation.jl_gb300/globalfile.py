@@ -126,12 +126,24 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
     p.variable_dt = 1 if _bool(d.get("variableTimestepFlag", "true")) else 0
     p.cfl = float(d.get("cfl", "0.18"))
     p.dt = parse_number(d["dt"]) if "dt" in d else 0.0
-    if "hyperViscosity" in d:
-        if d["hyperViscosity"] == "spectralBarrier":
-            raise ValueError("hyperViscosity spectralBarrier is not supported")
+    if d.get("hyperViscosity") == "spectralBarrier":    # simulationtypes.jl:294-297
+        p.hyperviscosity = 1
+        p.hv_kind = 1
+        p.hv_initk = float(d["initk"]) if "initk" in d else 0.0
+        p.hv_endk = float(d["endk"]) if "endk" in d else 0.0
+    elif "hyperViscosity" in d:
         p.hyperviscosity = 1
         p.hv_nu = float(d["hyperViscosityCoefficient"])
         p.hv_m = int(d.get("hyperViscosityM", "2"))
+    if "densityHyperViscosity" in d:                     # density_stratification_types.jl:137-148
+        if d["densityHyperViscosity"] == "spectralBarrier":
+            p.rho_hv = 2
+            p.rho_hv_initk = float(d["densityInitk"]) if "densityInitk" in d else 0.0
+            p.rho_hv_endk = float(d["densityEndk"]) if "densityEndk" in d else 0.0
+        else:
+            p.rho_hv = 1
+            p.rho_hv_nu = float(d["densityHyperViscosityCoefficient"])
+            p.rho_hv_m = int(d.get("densityHyperViscosityM", "2"))
     if "lesModel" in d:
         _set_les(p, d)
     if "densityStratification" in d:
@@ -140,8 +152,8 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
         p.density_gradient = parse_number(d["densityGradient"])
         p.gravity = parse_number(d["zAcceleration"]) / parse_number(d["referenceDensity"])
         p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
-        if "densityLesModel" in d or "densityHyperViscosity" in d:
-            raise ValueError("density LES / density hyperviscosity are not supported")
+        if "densityLesModel" in d:
+            raise ValueError("density LES (densityLesModel) is not supported")
     if "passiveScalar" in d:   # simulationtypes.jl:320-352
         if "lesModel" in d or "scalarLesModel" in d:
             raise ValueError("the passive scalar's LES eddy diffusion is not supported")

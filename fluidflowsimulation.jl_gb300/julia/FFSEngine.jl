@@ -37,7 +37,9 @@ mutable struct FFSParams
     passive_scalar::Int32; scalar_pr::Float64; scalar_gradient::Float64; scalar_dir::Int32
     plane_forcing::Int32; pf_tf::Float64; pf_alpha::Float64; pf_kf::Float64
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
-    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; les_dynp::Int32; radix_split::Int32
+    les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; les_dynp::Int32
+    hv_kind::Int32; hv_initk::Float64; hv_endk::Float64; rho_hv::Int32; rho_hv_nu::Float64; rho_hv_m::Int32
+    rho_hv_initk::Float64; rho_hv_endk::Float64; radix_split::Int32
     FFSParams() = new()
 end
 
@@ -84,9 +86,23 @@ function parameters(d)
     p.variable_dt = haskey(d, :variableTimestepFlag) ? Int32(parse(Bool, d[:variableTimestepFlag])) : 1
     p.cfl = haskey(d, :cfl) ? parse(Float64, d[:cfl]) : 0.18
     p.dt = haskey(d, :dt) ? num(d[:dt]) : 0.0
-    if haskey(d, :hyperViscosity)
+    if haskey(d, :hyperViscosity) && d[:hyperViscosity] == "spectralBarrier"   # simulationtypes.jl:294-297
+        p.hyperviscosity = 1; p.hv_kind = 1
+        p.hv_initk = haskey(d, :initk) ? parse(Float64, d[:initk]) : 0.0
+        p.hv_endk = haskey(d, :endk) ? parse(Float64, d[:endk]) : 0.0
+    elseif haskey(d, :hyperViscosity)
         p.hyperviscosity = 1; p.hv_nu = parse(Float64, d[:hyperViscosityCoefficient])
         p.hv_m = haskey(d, :hyperViscosityM) ? parse(Int32, d[:hyperViscosityM]) : 2
+    end
+    if haskey(d, :densityHyperViscosity)   # density_stratification_types.jl:137-148
+        if d[:densityHyperViscosity] == "spectralBarrier"
+            p.rho_hv = 2
+            p.rho_hv_initk = haskey(d, :densityInitk) ? parse(Float64, d[:densityInitk]) : 0.0
+            p.rho_hv_endk = haskey(d, :densityEndk) ? parse(Float64, d[:densityEndk]) : 0.0
+        else
+            p.rho_hv = 1; p.rho_hv_nu = parse(Float64, d[:densityHyperViscosityCoefficient])
+            p.rho_hv_m = haskey(d, :densityHyperViscosityM) ? parse(Int32, d[:densityHyperViscosityM]) : 2
+        end
     end
     if haskey(d, :lesModel) && (d[:lesModel] in ("dynamicSmagorinsky", "piomelliSmagorinsky", "dynamicSandP",
                                                   "piomelliSandP") ||

@@ -115,6 +115,16 @@ typedef struct ffs_params {
   int32_t les_dynp;            /* with FFS_LES_DYNAMIC / FFS_LES_PIOMELLI: the dynamic P tensor term,
                                   1 dynamicSandP, 2 piomelliSandP (les_types.jl:199-330,
                                   les_real_calc.jl:104-106); 0 none */
+  int32_t hv_kind;             /* with hyperviscosity: 0 nuh k^2M (HyperViscosity), 1 the spectral barrier
+                                  (hyperViscosity spectralBarrier, hyperviscosity_types.jl:32-48; ETD3rdO only) */
+  double hv_initk, hv_endk;    /* spectral barrier: initk, endk (<= 0: the reference defaults
+                                  cutoff 2 kx_max / 3 and sqrt(3 cutoff) kx_max, simulationtypes.jl:294-297) */
+  int32_t rho_hv;              /* densityHyperViscosity (density_stratification_types.jl:137-148): 0 none,
+                                  1 rho_hv_nu k^2M, 2 the spectral barrier; the density's ETD3rdO exponent and
+                                  the rhohdiss stats column (AB3 adds no term, as in the reference) */
+  double rho_hv_nu;            /* densityHyperViscosityCoefficient */
+  int32_t rho_hv_m;            /* densityHyperViscosityM, default 2 */
+  double rho_hv_initk, rho_hv_endk; /* densityInitk, densityEndk (<= 0: defaults as above) */
   int32_t radix_split;         /* runtime FFT plans: 0 the default radix split of each axis, k = 1, 2 the
                                   k-th alternative split (where the length has one; the autotuner times
                                   them and keeps the fastest per axis) */

@@ -145,6 +145,14 @@ class Params:
     hv: bool = False
     hv_nu: float = 0.0
     hv_m: int = 2
+    hv_kind: str = "power"               # "power" (HyperViscosity) or "barrier" (SpectralBarrier)
+    hv_initk: float = 0.0
+    hv_endk: float = 0.0
+    rho_hv: str = ""                     # densityHyperViscosity: "", "power", "barrier"
+    rho_hv_nu: float = 0.0
+    rho_hv_m: int = 2
+    rho_hv_initk: float = 0.0
+    rho_hv_endk: float = 0.0
     les: bool = False
     les_model: str = "Smagorinsky"       # Smagorinsky, Vreman, productionViscosity, Silvis, stableNonLinear
     smag_c: float = 0.17                 # the model's constant c
@@ -208,10 +216,25 @@ class Params:
         p.variable_dt = d.get("variableTimestepFlag", "true").strip().lower() == "true"
         p.cfl = float(d.get("cfl", 0.18))
         p.dt = _num(d["dt"]) if "dt" in d else 0.0
-        if "hyperViscosity" in d:
+        kxm = (p.nx // 2) / p.lx                          # KX[end]
+        if d.get("hyperViscosity") == "spectralBarrier":   # simulationtypes.jl:294-297
+            p.hv = True
+            p.hv_kind = "barrier"
+            p.hv_initk = float(d["initk"]) if "initk" in d else p.cutoff * 2 * kxm / 3
+            p.hv_endk = float(d["endk"]) if "endk" in d else math.sqrt(p.cutoff * 3) * kxm
+        elif "hyperViscosity" in d:
             p.hv = True
             p.hv_nu = float(d["hyperViscosityCoefficient"])
             p.hv_m = int(d.get("hyperViscosityM", 2))
+        if "densityHyperViscosity" in d and "densityStratification" in d:   # density_stratification_types.jl:137-148
+            if d["densityHyperViscosity"] == "spectralBarrier":
+                p.rho_hv = "barrier"
+                p.rho_hv_initk = float(d["densityInitk"]) if "densityInitk" in d else p.cutoff * 2 * kxm / 3
+                p.rho_hv_endk = float(d["densityEndk"]) if "densityEndk" in d else math.sqrt(p.cutoff * 3) * kxm
+            else:
+                p.rho_hv = "power"
+                p.rho_hv_nu = float(d["densityHyperViscosityCoefficient"])
+                p.rho_hv_m = int(d.get("densityHyperViscosityM", 2))
         if "lesModel" in d:
             p.set_les(d)
         if "densityStratification" in d:
@@ -720,7 +743,7 @@ def stats_header(p: Params) -> str:
     if p.scalar:
         cols.append("scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss")
     if p.density:
-        cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux")
+        cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux" + (",rhohdiss" if p.rho_hv else ""))
     if p.les:
         cols.append("prh,prv,praniso,pr")
     if p.plane_forcing == "aForcing":
@@ -730,6 +753,31 @@ def stats_header(p: Params) -> str:
     if p.hv:
         cols.append("hdissh,hdissv,hdiss")
     return ",".join(cols)
+
+
+def barrier_f(k, i, p):
+    """log(esp(|k|, i, p, 1/4)) of the spectral barrier (hyperviscosity_types.jl:40-48)."""
+    a = np.abs(k)
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        e = np.where(a <= i, 1.0, np.where(a < p, np.exp(-((a - i) * (a - i)) / (p ** 0.25 - a ** 0.25)), 0.0))
+        return np.log(e)
+
+
+def barrier_c(g, k2, mnu, i, p):
+    """muladd(k2, -nu, f(|k|)) on the retained modes, 0 elsewhere (init_c_spectral_barrier!
+    fills only XRANGE x YRANGE x ZRANGE, ETD.jl:71-82)."""
+    f = np.where(g.keep, barrier_f(np.sqrt(k2), i, p), 0.0)
+    with np.errstate(invalid="ignore"):
+        c = dd.fma(k2, np.full_like(k2, mnu), np.where(np.isinf(f), 0.0, f))
+    # f = log(0) = -inf (beyond endk, or exp underflow) makes muladd -inf: the ETD coefficients
+    # are then 0 and the mode is removed (ETD.jl:182-191)
+    return np.where(g.keep, np.where(np.isinf(f), -np.inf, c), 0.0)
+
+
+def barrier_w(k2, i, p):
+    """The barrier as a stats/spectrum weight: -inf counts 0 (stats.jl:1160-1161)."""
+    f = barrier_f(np.sqrt(k2), i, p)
+    return np.where(np.isinf(f), 0.0, f)
 
 
 def _proj(a, b):
@@ -887,7 +935,11 @@ class OracleSimulation:
         # ETD.jl:84-95), with k2 = muladd(KX,KX, muladd(KY,KY, KZ*KZ))
         k2 = dd.fma(*np.broadcast_arrays(g.KX, g.KX, dd.fma(*np.broadcast_arrays(g.KY, g.KY, g.KZ * g.KZ))))
         c = k2 * (-p.nu)
-        if p.hv:
+        if p.hv and p.hv_kind == "barrier":               # init_c_spectral_barrier! (ETD.jl:71-82)
+            if p.ab3:
+                raise ValueError("spectralBarrier has no AB3 form in the reference")
+            c = barrier_c(g, k2, -p.nu, p.hv_initk, p.hv_endk)
+        elif p.hv:
             km = k2.copy()
             for _ in range(p.hv_m - 1):
                 km = km * k2
@@ -901,10 +953,19 @@ class OracleSimulation:
             alpha = p.nu / (p.density_pr if p.density else p.scalar_pr)
             if p.ab3:
                 self.rts = AB3(p.variable_dt, p.dt)
+            elif p.scalar and p.hv and p.hv_kind == "barrier":
+                self.rts = ETD3(p.variable_dt, p.dt, barrier_c(g, k2, -alpha, p.hv_initk, p.hv_endk))
             elif p.scalar and p.hv:
                 # the scalar's ETD3rdO takes the velocity's hyperviscosity (simulationtypes.jl
                 # :336 passes the hyperviscositytype of :293-305): muladd(k2, -alpha, k2^M -nuh)
                 self.rts = ETD3(p.variable_dt, p.dt, dd.fma(k2, np.full_like(k2, -alpha), km * (-p.hv_nu)))
+            elif p.rho_hv == "barrier":                   # the density's own (density_stratification_types.jl:137-176)
+                self.rts = ETD3(p.variable_dt, p.dt, barrier_c(g, k2, -alpha, p.rho_hv_initk, p.rho_hv_endk))
+            elif p.rho_hv == "power":
+                kr = k2.copy()
+                for _ in range(p.rho_hv_m - 1):
+                    kr = kr * k2
+                self.rts = ETD3(p.variable_dt, p.dt, dd.fma(k2, np.full_like(k2, -alpha), kr * (-p.rho_hv_nu)))
             else:
                 self.rts = ETD3(p.variable_dt, p.dt, k2 * (-alpha))
             self.alpha = alpha
@@ -1408,9 +1469,14 @@ class OracleSimulation:
             rhodiss = self.alpha * (d1 + d2 + d3)
             bf_raw = self._wsum(_proj(u[p.gravity_dir], rho))
             bflux = -self.gvec[p.gravity_dir] * bf_raw
-            extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss, bflux]
+            if p.rho_hv:   # scalar_hvis_stats (stats.jl:1086-1110, 1145-1171), trhodiss += it
+                rh_raw = self._wsum(self._rho_hv_weight() * r2)
+                rh = -rh_raw if p.rho_hv == "barrier" else p.rho_hv_nu * rh_raw
+                extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss + rh, bflux, rh]
+            else:
+                extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss, bflux]
             if p.variable_dt and p.reference_cfl_slot:
-                self.slot_rho = bf_raw
+                self.slot_rho = rh_raw if p.rho_hv else bf_raw
         if p.les:
             t = self.div_tau(self.tauh)
             hraw = self._wsum(_proj(t[0], u[0]) + _proj(t[1], u[1]))
@@ -1424,10 +1490,12 @@ class OracleSimulation:
         elif p.forcing or p.plane_forcing:
             extra += [self.hp, self.vp, self.hp + self.vp]
         if p.hv:
-            hraw = self._wsum((g.K2 ** p.hv_m) * (a2[0] + a2[1]))
-            vraw = self._wsum((g.K2 ** p.hv_m) * a2[2])
-            extra += [p.hv_nu * hraw, p.hv_nu * vraw, p.hv_nu * (hraw + vraw)]
-            tdiss += p.hv_nu * (hraw + vraw)
+            hw = self._hv_weight()
+            hraw = self._wsum(hw * (a2[0] + a2[1]))
+            vraw = self._wsum(hw * a2[2])
+            sc = -1.0 if p.hv_kind == "barrier" else p.hv_nu   # spectral_barrier_stats: -sums
+            extra += [sc * hraw, sc * vraw, sc * (hraw + vraw)]
+            tdiss += sc * (hraw + vraw)
             slot = hraw
         if self.G2 is not None:
             fil, fslot = self._velocity_row_fil(a2)
@@ -1437,6 +1505,19 @@ class OracleSimulation:
         if p.variable_dt and p.reference_cfl_slot:
             self.slot_u = slot
         return row + [tdiss] + extra
+
+    def _hv_weight(self):
+        """Per-mode weight of the velocity hyperviscosity stats: (k^2)^M or the barrier."""
+        p, g = self.p, self.g
+        if p.hv_kind == "barrier":
+            return barrier_w(g.K2, p.hv_initk, p.hv_endk)
+        return g.K2 ** p.hv_m
+
+    def _rho_hv_weight(self):
+        p, g = self.p, self.g
+        if p.rho_hv == "barrier":
+            return barrier_w(g.K2, p.rho_hv_initk, p.rho_hv_endk)
+        return g.K2 ** p.rho_hv_m
 
     def _velocity_row_fil(self, a2):
         """The Stats_fil.txt row (STAT_FIL branches of velocity_stats, scalar_stats,
@@ -1477,8 +1558,14 @@ class OracleSimulation:
         if p.density:
             vals, fslot = scalar_fil(self.rho)
             bf_raw = ws(_proj(u[p.gravity_dir], self.rho))
-            extra += vals + [vals[-1], -self.gvec[p.gravity_dir] * bf_raw]
-            fslot = bf_raw
+            if p.rho_hv:
+                rh_raw = ws(self._rho_hv_weight() * np.abs(self.rho) ** 2)
+                rh = -rh_raw if p.rho_hv == "barrier" else p.rho_hv_nu * rh_raw
+                extra += vals + [vals[-1] + rh, -self.gvec[p.gravity_dir] * bf_raw, rh]
+                fslot = rh_raw
+            else:
+                extra += vals + [vals[-1], -self.gvec[p.gravity_dir] * bf_raw]
+                fslot = bf_raw
         if p.les:
             t = self.div_tau(self.tauh)
             prh = -ws(_proj(t[0], u[0]) + _proj(t[1], u[1]))
@@ -1490,10 +1577,12 @@ class OracleSimulation:
         elif p.forcing or p.plane_forcing:
             extra += [self.hp, self.vp, self.hp + self.vp]
         if p.hv:
-            hraw = ws((g.K2 ** p.hv_m) * (a2[0] + a2[1]))
-            vraw = ws((g.K2 ** p.hv_m) * a2[2])
-            extra += [p.hv_nu * hraw, p.hv_nu * vraw, p.hv_nu * (hraw + vraw)]
-            tdiss += p.hv_nu * (hraw + vraw)
+            hw = self._hv_weight()
+            hraw = ws(hw * (a2[0] + a2[1]))
+            vraw = ws(hw * a2[2])
+            sc = -1.0 if p.hv_kind == "barrier" else p.hv_nu
+            extra += [sc * hraw, sc * vraw, sc * (hraw + vraw)]
+            tdiss += sc * (hraw + vraw)
         return row + [tdiss] + extra, fslot
 
     def write_stats(self):
@@ -1603,10 +1692,10 @@ class OracleSimulation:
         if p.les:
             put("les_h", _proj(dt_[0], u[0]) + _proj(dt_[1], u[1]))       # spectrum_les
             put("les_v", _proj(dt_[2], u[2]))
-        if p.hv:
-            km = k2 ** p.hv_m
-            put("hvis_h", p.hv_nu * km * (_proj(u[0], u[0]) + _proj(u[1], u[1])), "hvis_fil_h")
-            put("hvis_v", p.hv_nu * km * _proj(u[2], u[2]), "hvis_fil_v")
+        if p.hv:   # spectrum_hyperviscosity / spectrum_spectral_barrier (spec.jl:273-314)
+            km = barrier_w(k2, p.hv_initk, p.hv_endk) if p.hv_kind == "barrier" else p.hv_nu * k2 ** p.hv_m
+            put("hvis_h", km * (_proj(u[0], u[0]) + _proj(u[1], u[1])), "hvis_fil_h")
+            put("hvis_v", km * _proj(u[2], u[2]), "hvis_fil_v")
         if p.density:
             rho = self.rho
             put("buoyancy_v", self.gvec[2] * _proj(u[2], rho), "buoyancy_fil_v")   # spectrum_buoyancy

@@ -104,6 +104,21 @@ FIXED_CASES = {
     "etd-48-dynamicsandp-piomelli": gdict(48, "ETD3rdO", lesModel="dynamicSandP", sLesModel="piomelliSmagorinsky",
                                           cmin="-0.02"),
     "ab3-sandp-dynamic": gdict(32, lesModel="SandP", sLesModel="dynamicSmagorinsky", pConstant="0.12"),
+    # the spectral barrier (hyperviscosity_types.jl:32-82, ETD.jl:71-82) and the density's
+    # own hyperviscosity (density_stratification_types.jl:137-148; AB3 adds no term)
+    "etd-spectral-barrier": gdict(32, "ETD3rdO", hyperViscosity="spectralBarrier"),
+    "etd-barrier-truncating": gdict(32, "ETD3rdO", hyperViscosity="spectralBarrier", initk="5", endk="20"),
+    "etd-density-hv": gdict(32, "ETD3rdO", densityStratification="true", Pr="1", densityGradient="1",
+                            zAcceleration="1", referenceDensity="1", densityHyperViscosity="true",
+                            densityHyperViscosityCoefficient="1e-5"),
+    "ab3-adaptive-density-hv": gdict(32, adaptive=True, densityStratification="true", Pr="2", densityGradient="1",
+                                     zAcceleration="1", referenceDensity="1", densityHyperViscosity="true",
+                                     densityHyperViscosityCoefficient="1e-4", densityHyperViscosityM="3"),
+    "etd-barriers-density-specfil": gdict(32, "ETD3rdO", hyperViscosity="spectralBarrier", densityStratification="true",
+                                          Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1",
+                                          densityHyperViscosity="spectralBarrier", densityInitk="6", specFil="2"),
+    "etd-scalar-barrier": gdict(32, "ETD3rdO", passiveScalar="true", scalarPr="0.7", scalarGradient="1",
+                                hyperViscosity="spectralBarrier", initk="6"),
     # the reference's kz = 0 plane forcing family (forcing_types.jl:335-450)
     "ab3-adaptive-rf-forcing": gdict(32, adaptive=True, forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
     "etd-crf-forcing-tanh": gdict(32, "ETD3rdO", forcing="cRfForcing", TF="0.5", alphac="1.0", kf="4.0", Zf="tanh"),
@@ -218,6 +233,7 @@ SPEC_CASES = {
     "ab3-hv-forced": dict(FIXED_CASES["ab3-64-hv-forced"], dtSpec="2"),
     "etd-scalar": dict(FIXED_CASES["etd-scalar"], dtSpec="2"),
     "etd-les-density-hv-specfil": dict(FIXED_CASES["etd-les-density-hv-specfil"], dtSpec="2"),
+    "etd-barriers-density-specfil": dict(FIXED_CASES["etd-barriers-density-specfil"], dtSpec="2"),
 }
 
 
@@ -250,6 +266,10 @@ def test_errors_and_state_checks(gpu_pkg):
     bad = dict(d, nx="40")
     with pytest.raises(gpu_pkg.FFSError) as e:
         gpu_pkg.Simulation.from_global(bad)
+    assert e.value.code == -6
+    # the reference's AB3 has no explicit term for the spectral barrier
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        gpu_pkg.Simulation.from_global(dict(d, hyperViscosity="spectralBarrier"))
     assert e.value.code == -6
     # a non-finite initial condition is reported, not propagated silently
     u, _ = make_ic(gpu_pkg, d)

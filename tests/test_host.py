@@ -190,6 +190,30 @@ def test_parameters_les_models(pkg):
     assert (o.filter_width, o.les_test_width, o.les_cmin) == (0.2, 0.5, -0.1)
 
 
+def test_parameters_hyperviscosity_kinds(pkg):
+    """hyperViscosity spectralBarrier (simulationtypes.jl:294-297) and densityHyperViscosity
+    (density_stratification_types.jl:137-148), the same in the oracle's Params."""
+    import math
+    from oracle.ffs_oracle import Params
+    base = {"nx": "48", "ny": "48", "nz": "48", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+            "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1"}
+    d = dict(base, hyperViscosity="spectralBarrier")
+    p, o = pkg.parameters(d), Params.from_global(d)
+    assert (p.hyperviscosity, p.hv_kind, p.hv_initk, p.hv_endk) == (1, 1, 0.0, 0.0)   # engine defaults
+    assert o.hv_kind == "barrier"
+    assert o.hv_initk == pytest.approx((2 / 3) * 2 * 24 / 3) and o.hv_endk == pytest.approx(math.sqrt(2) * 24)
+    d = dict(base, hyperViscosity="spectralBarrier", initk="3", endk="9.5")
+    assert (pkg.parameters(d).hv_initk, pkg.parameters(d).hv_endk) == (3.0, 9.5)
+    dens = dict(base, densityStratification="true", Pr="1", densityGradient="1", zAcceleration="1",
+                referenceDensity="1")
+    d = dict(dens, densityHyperViscosity="true", densityHyperViscosityCoefficient="1e-6", densityHyperViscosityM="3")
+    p, o = pkg.parameters(d), Params.from_global(d)
+    assert (p.rho_hv, p.rho_hv_nu, p.rho_hv_m) == (1, 1e-6, 3) and (o.rho_hv, o.rho_hv_m) == ("power", 3)
+    d = dict(dens, densityHyperViscosity="spectralBarrier", densityEndk="20")
+    p, o = pkg.parameters(d), Params.from_global(d)
+    assert (p.rho_hv, p.rho_hv_endk) == (2, 20.0) and (o.rho_hv, o.rho_hv_endk) == ("barrier", 20.0)
+
+
 def test_parse_number(pkg):
     assert pkg.parse_number("2π") == pytest.approx(2 * np.pi)
     assert pkg.parse_number("2pi/128") == pytest.approx(2 * np.pi / 128)
