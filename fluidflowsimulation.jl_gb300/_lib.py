@@ -57,7 +57,8 @@ class FFSParams(ctypes.Structure):
         ("pf_zf_tanh", c_int32), ("pf_qp", c_double), ("pf_qc", c_double), ("pf_qkf", c_double),
         ("les_test_width", c_double), ("les_cmin", c_double), ("spec_fil", c_double), ("les_dynp", c_int32),
         ("hv_kind", c_int32), ("hv_initk", c_double), ("hv_endk", c_double), ("rho_hv", c_int32), ("rho_hv_nu", c_double),
-        ("rho_hv_m", c_int32), ("rho_hv_initk", c_double), ("rho_hv_endk", c_double), ("radix_split", c_int32),
+        ("rho_hv_m", c_int32), ("rho_hv_initk", c_double), ("rho_hv_endk", c_double),
+        ("rho_les", c_int32), ("rho_les_c", c_double), ("radix_split", c_int32),
     ]
 
 

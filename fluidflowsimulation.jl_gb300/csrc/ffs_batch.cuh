@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(FFS_MAXT) kb_inv_y(const BatchInst<T>* __restr
 template <typename T, bool LES, int LYZ, int CI = 0, int N = 0>
 __global__ void __launch_bounds__(FFS_MAXT) kb_x(const BatchInst<T>* __restrict__ B, const BatchTables* __restrict__ Tb) {
   FFS_BATCH_LOOP(LES ? BP_X_LES : BP_X)
-  b_x_pass<T, LES, false, LYZ, N>(BI.I, Blk{it.x, 0, 0, 0});
+  b_x_pass<T, LES, 0, LYZ, N>(BI.I, Blk{it.x, 0, 0, 0});
   FFS_BATCH_END
 }
 template <typename T, int TX, int CI = 0, int N = 0>

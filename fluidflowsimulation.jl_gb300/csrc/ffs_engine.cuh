@@ -81,6 +81,12 @@ inline bool make_plan(int n, FftPlan& P, int variant = 0) {
 }
 
 inline int round32(int x) { return ((x + 31) / 32) * 32; }
+// real fields into the x pass: u, w [, S] [, the fourth field [, its gradient]]
+inline int x_inputs(const ffs_params& p) {
+  const bool fld = p.density || p.passive_scalar;
+  const bool dl = p.les && fld && (p.rho_les || p.passive_scalar);
+  return 6 + (p.les ? 5 : 0) + (fld ? 1 : 0) + (dl ? 3 : 0);
+}
 
 template <typename T>
 class Engine : public EngineBase {
@@ -229,6 +235,9 @@ class Engine : public EngineBase {
     }
     I.density = p.density != 0; I.gdir = p.gravity_dir;
     I.scalar = p.passive_scalar != 0;
+    // the fourth field's LES diffusion: nu_t grad rho (+ (c D^2 / 2) w x grad rho)
+    I.rho_les = (I.les && I.density) ? p.rho_les : 0;
+    I.rho_les_c = (p.rho_les_c * I.les_d2) / 2;
     I.alpha = p.density ? p.nu / p.density_pr : 0.0;
     I.dgrad = p.density_gradient; I.gval = p.gravity;
     I.forcing = p.forcing != 0; I.f_eps = p.forcing_power; I.f_kf = p.forcing_kf;
@@ -250,12 +259,20 @@ class Engine : public EngineBase {
     // a passive scalar rides the density's buffers and passes, with g = 0
     // (simulationtypes.jl:198-213): the transport, mean-gradient source and diffusion are
     // the same; buoyancy, the CFL cap, the stats columns and the spectra differ (I.scalar)
-    if (p_in.passive_scalar && (p_in.density || p_in.les)) {
-      err = p_in.density ? "a passive scalar together with density stratification is not supported"
-                         : "the passive scalar's LES eddy diffusion is not supported";
+    if (p_in.passive_scalar && p_in.density) {
+      err = "a passive scalar together with density stratification is not supported";
+      return FFS_EUNSUPPORTED;
+    }
+    if (p_in.rho_les < 0 || p_in.rho_les > 2) { err = "rho_les must be 0, 1 or 2"; return FFS_EINVAL; }
+    if (p_in.rho_les && !(p_in.les && (p_in.density || p_in.passive_scalar))) {
+      // without an LES model the reference's flux keeps a bare grad rho (nu_t = 1)
+      err = "the density / scalar LES diffusion (rho_les) needs an LES model and the density or a passive scalar";
       return FFS_EUNSUPPORTED;
     }
     ffs_params p = p_in;
+    // a passive scalar under an LES model always has its LES diffusion, eddy diffusion
+    // unless chosen otherwise (simulationtypes.jl:334-346)
+    if (p.passive_scalar && p.les && !p.rho_les) p.rho_les = 1;
     if (p.passive_scalar) {
       if (!(p.scalar_pr > 0) || p.scalar_dir < 0 || p.scalar_dir > 2) { err = "bad passive scalar parameters"; return FFS_EINVAL; }
       p.density = 1;
@@ -342,7 +359,7 @@ class Engine : public EngineBase {
     while (txy > TX / 2 && txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) txy /= 2;
     if (txy * std::max(I.py.tpl, I.pz.tpl) > MAXT) { err = "grid size too large for this precision"; return FFS_EUNSUPPORTED; }
     {
-      const int nin_x = 6 + (p.les ? 5 : 0) + (p.density ? 1 : 0);
+      const int nin_x = x_inputs(p);
       const int pin = (nin_x + 1) / 2;
       int maxs = 0;
       FFS_CK(cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, p.device));
@@ -388,11 +405,13 @@ class Engine : public EngineBase {
     nin = 0;
     for (int c = F_UX; c <= F_WZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
     if (I.les) for (int c = F_SXX; c <= F_SYZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
-    if (I.density) { inv_list.code[nin] = F_RHO; inv_list.slot[nin] = nin; ++nin; }
+    int rho_slot = -1;
+    if (I.density) { rho_slot = nin; inv_list.code[nin] = F_RHO; inv_list.slot[nin] = nin; ++nin; }
+    if (I.rho_les) for (int c = F_GRX; c <= F_GRZ; ++c) { inv_list.code[nin] = c; inv_list.slot[nin] = nin; ++nin; }
     inv_list.n = nin;
     // the dynamic model's test-filtered u^, S^: transformed with the others, read by its
     // own x kernels only (the x pass reads slots 0..nin-1)
-    static_assert(sizeof(FieldList::code) / sizeof(int) >= 12 + (F_GWZ - F_GUX + 1), "FieldList too small");
+    static_assert(sizeof(FieldList::code) / sizeof(int) >= 15 + (F_GWZ - F_GUX + 1), "FieldList too small");
     if (I.dyn)
       for (int c = F_GUX; c <= (I.dynp ? F_GWZ : F_GSYZ); ++c) {
         inv_list.code[inv_list.n] = c;
@@ -417,7 +436,7 @@ class Engine : public EngineBase {
     auto addo = [&](int role, int slot) { fwd_list.code[nout] = role; fwd_list.slot[nout] = slot; ++nout; };
     addo(R_NX, 0); addo(R_NY, 1); addo(R_NZ, 2); addo(R_KE, 3);
     if (I.les) { addo(R_TXX, 6); addo(R_TXY, 7); addo(R_TXZ, 8); addo(R_TYY, 9); addo(R_TYZ, 10); }
-    if (I.density) { addo(R_FX, 4); addo(R_FY, 5); addo(R_FZ, nin - 1); }
+    if (I.density) { addo(R_FX, 4); addo(R_FY, 5); addo(R_FZ, rho_slot); }
     fwd_list.n = nout;
     I.nin = nin; I.nout = nout;
     for (int i = 0; i < nout; ++i) { I.out_role[i] = fwd_list.code[i]; I.out_slot[i] = fwd_list.slot[i]; }
@@ -456,7 +475,7 @@ class Engine : public EngineBase {
     I.twx = tw[0]; I.twy = tw[1]; I.twz = tw[2];
     xfused = 0;
     // the register-fused LES x pass computes the Smagorinsky model only
-    const bool smag_only = !p.les || (p.les_model == FFS_LES_SMAGORINSKY && p.sandp_cb == 0.0);
+    const bool smag_only = !p.les || (p.les_model == FFS_LES_SMAGORINSKY && p.sandp_cb == 0.0 && !I.rho_les);
     if (sizeof(T) == 4 && (I.les || !I.density) && p.kernel_variant != 1 && smag_only) {
       int lyzf = 0, rf = 0;
       if (I.les) {   // LES (with or without density): n in {64, 128}
@@ -507,7 +526,7 @@ class Engine : public EngineBase {
       n_sms = sms;
     }
     // record layout
-    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8 + (I.rho_hv ? 1 : 0)) : 0) + (I.les ? 4 : 0) +
+    ncols_stats = 22 + (I.density ? (I.scalar ? 6 : 8 + (I.rho_les ? 1 : 0) + (I.rho_hv ? 1 : 0)) : 0) + (I.les ? 4 : 0) +
                   (I.pforce == FFS_PF_A ? 2 : ((I.forcing || I.pforce) ? 3 : 0)) + (I.hv ? 3 : 0);
     if (I.pforce && (rc = plane_forcing_tables(p, err))) return rc;
     // a record: the Stats.txt row, 13 Scales.txt inputs, then with specFil the
@@ -586,7 +605,7 @@ class Engine : public EngineBase {
     header = "iteration,time,u1,u2,u3,u1p2,u2p2,u3p2,kh,kv,kaniso,k,dissh,dissv,diss,nlh,nlv,pressh,pressv,tnlh,tnlv,tdiss";
     if (I.scalar) header += ",scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss";
     else if (I.density) header += std::string(",rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux") +
-                                  (I.rho_hv ? ",rhohdiss" : "");
+                                  (I.rho_les ? ",rhopr" : "") + (I.rho_hv ? ",rhohdiss" : "");
     if (I.les) header += ",prh,prv,praniso,pr";
     if (I.pforce == FFS_PF_A) header += ",hp,vp";
     else if (I.forcing || I.pforce) header += ",hp,vp,tp";
@@ -706,16 +725,18 @@ class Engine : public EngineBase {
   }
 
   using XK = void (*)(Inst<T>);
-  template <int LY> static XK xsel(bool L, bool D) {
-    if (L && D) return k_x_pass<T, true, true, LY>;
-    if (L) return k_x_pass<T, true, false, LY>;
-    if (D) return k_x_pass<T, false, true, LY>;
-    return k_x_pass<T, false, false, LY>;
+  template <int LY> static XK xsel(bool L, bool D, bool DL) {
+    if (L && DL) return k_x_pass<T, true, 2, LY>;
+    if (L && D) return k_x_pass<T, true, 1, LY>;
+    if (L) return k_x_pass<T, true, 0, LY>;
+    if (D) return k_x_pass<T, false, 1, LY>;
+    return k_x_pass<T, false, 0, LY>;
   }
   XK xpass_ptr() const {
-    if (lyz == 4) return xsel<4>(I.les, I.density);
-    if (lyz == 2) return xsel<2>(I.les, I.density);
-    return xsel<1>(I.les, I.density);
+    const bool dl = I.rho_les != 0;
+    if (lyz == 4) return xsel<4>(I.les, I.density, dl);
+    if (lyz == 2) return xsel<2>(I.les, I.density, dl);
+    return xsel<1>(I.les, I.density, dl);
   }
   using ZK = void (*)(Inst<T>, FieldList, int);
   ZK zu_ptr() const {
@@ -782,10 +803,12 @@ class Engine : public EngineBase {
   // its shared accumulators of i k.tau and i k.flux (LES / density)
   size_t z2_aux() const { return (I.les || I.density) ? fwd_z2_aux_bytes<TX>(I.NZR) : 0; }
 
+  // the paired inverse z pass knows the velocity, vorticity, strain and density codes only
+  bool pair_codes() const { return !I.dyn && !I.rho_les; }
   void launch_inv_z(const FieldList& F) {
     if constexpr (sizeof(T) == 4) {
       if (txy == TX) {
-        if (v_iz == 1 && !I.dyn)
+        if (v_iz == 1 && pair_codes())
           FFS_CT_SWITCH(ctz(), (k_inv_z2<NC, PAIR_LP><<<dim3(F.n, I.KXP / TX, I.NYR), PAIR_LP * ct_tpl<NC>(),
                                                        pair_smem<NC, PAIR_LP>(), s>>>(I, F)))
         FFS_CT_SWITCH(ctz(), (k_inv_z<T, TX, NC><<<dim3(F.n, I.KXP / TX, I.NYR), TX * ct_tpl<NC>(), smem_z, s>>>(I, F)))
@@ -1526,7 +1549,7 @@ class Engine : public EngineBase {
         v = bv;
         return 0;
       };
-      if (!rc) rc = pick(v_iz, "z_inv", (I.dyn || txy != TX) ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
+      if (!rc) rc = pick(v_iz, "z_inv", (!pair_codes() || txy != TX) ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
       // one launch for every field family, or one per family
       if (!rc && n_fam > 1) {
         float bms = 1e30f;
@@ -1660,7 +1683,7 @@ class Engine : public EngineBase {
     retained(p.nz, p.lz, p.cutoff, false, zp, zc);
     const int64_t KXP = ((xc + 7) / 8) * 8, cb = sizeof(cplx<T>);
     const int64_t cs = (int64_t)zc * yc * KXP, wzs = (int64_t)p.nz * yc * KXP, wys = (int64_t)p.nz * p.ny * KXP;
-    const int nin = 6 + (p.les ? 5 : 0) + (p.density ? 1 : 0), nslots = std::max(nin, 4);
+    const int nin = x_inputs(p), nslots = std::max(nin, 4);
     const int ncomp = p.density ? 4 : 3;
     int64_t t = cb * (2 * (int64_t)(2 * p.nx + p.ny + p.nz));   // twiddle tables, packed x table
     t += cb * (3 * ncomp * cs + (int64_t)nslots * (wzs + wys) + ((p.les || p.density) ? 8 : 4) * cs);

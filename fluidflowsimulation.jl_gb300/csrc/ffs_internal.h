@@ -18,7 +18,8 @@ enum FieldCode : int {
   // models.jl:99-103), G = exp(-D^2 k^2 / 24) with the test filter width D
   F_GUX, F_GUY, F_GUZ,
   F_GSXX, F_GSXY, F_GSXZ, F_GSYY, F_GSYZ,
-  F_GWX, F_GWY, F_GWZ            // and with the dynamic P tensor the filtered vorticity G w
+  F_GWX, F_GWY, F_GWZ,           // and with the dynamic P tensor the filtered vorticity G w
+  F_GRX, F_GRY, F_GRZ            // the fourth field's gradient i k rho (its LES diffusion)
 };
 
 // Forward-field roles consumed by the forward z pass.
@@ -42,9 +43,10 @@ enum StatQ : int {
   Q_FU12 = Q_IL0 + 9, Q_FU22, Q_FU32, Q_FEH, Q_FEV, Q_FNLH, Q_FNLV, Q_FLESH, Q_FLESV, Q_FHVH, Q_FHVV,
   Q_FRHO2, Q_FDR1, Q_FDR2, Q_FDR3, Q_FBF,
   Q_RHV, Q_FRHV,   // density hyperviscous sum (rhohdiss) and its filtered twin
+  Q_RPR, Q_FRPR,   // density LES transfer (rhopr: proj(i k . flux, rho)) and its filtered twin
   Q_COUNT
 };
-constexpr int QPAD = 56;
+constexpr int QPAD = 64;
 constexpr int FFS_PF_MAXSH = 520;   // 2D shells of the kz = 0 plane forcing: min(nx/2+1, ny/2) <= 513
 
 // Device-resident scalar state (one per simulation).
@@ -131,6 +133,8 @@ template <typename T> struct Inst {
   double hv_nu;
   int hv_kind;             // 0 nuh k^2M, 1 the spectral barrier (hv_initk, hv_endk)
   double hv_initk, hv_endk;
+  int rho_les;             // LES of the fourth field: 0 none, 1 eddy diffusion, 2 vorticity diffusion
+  double rho_les_c;        //   c Delta^2 / 2 of the vorticity term
   int rho_hv, rho_hv_m;    // density hyperviscosity: 0 none, 1 rho_hv_nu k^2M, 2 the spectral barrier
   double rho_hv_nu, rho_hv_initk, rho_hv_endk;
   int les;

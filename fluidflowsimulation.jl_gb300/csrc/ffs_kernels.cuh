@@ -22,8 +22,8 @@ constexpr int LYZ_IO = 4;  // (y,z) lines per CTA in the transform-only x kernel
 
 struct FieldList {
   int n;
-  int code[24];   // FieldCode (inverse z) or role (forward passes): at most 12 + 11 filtered
-  int slot[24];   // work-array slot
+  int code[28];   // FieldCode (inverse z) or role (forward passes): at most 15 + 11 filtered
+  int slot[28];   // work-array slot
 };
 
 // Block coordinates of one unit of work: the launch's own (single simulation) or an
@@ -125,6 +125,7 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
     case F_GSXZ: fam = 4; ca = 0; cb = 2; break;
     case F_GSYY: fam = 4; ca = 1; cb = 1; break;
     case F_GSYZ: fam = 4; ca = 1; cb = 2; break;
+    case F_GRX: case F_GRY: case F_GRZ: fam = 6; ca = code - F_GRX; break;
     case F_GWX: fam = 5; ca = 1; cb = 2; break;
     case F_GWY: fam = 5; ca = 2; cb = 0; break;
     case F_GWZ: fam = 5; ca = 0; cb = 1; break;
@@ -163,6 +164,15 @@ __device__ __forceinline__ void b_inv_z(const Inst<T>& I, const FieldList& F, co
       const cplx<T> ub = uh[oa + o], uc = uh[ob + o];
       const T kb = kax(ca, l, kc), kc_ = kax(cb, l, kc);
       return mk(-(kb * uc.y - kc_ * ub.y), kb * uc.x - kc_ * ub.x);
+    };
+    fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
+  } else if (fam == 6) {
+    auto ld = [&](int l, int z) -> cplx<T> {   // i k_a rho (fourierspacep1!, models.jl:110-112)
+      const int kc = zcomp(I, z);
+      if (kc < 0 || kx0 + l >= I.Mx) return mk(T(0), T(0));
+      const cplx<T> r = uh[3 * cs + (long long)kc * rowstride + l];
+      const T ka = kax(ca, l, kc);
+      return mk(-ka * r.y, ka * r.x);
     };
     fft_lines_n<+1, TX, T, N>(I.pz, s0, s1, TX, I.twz, ld, st);
   } else if (fam == 2) {
@@ -282,8 +292,9 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
 //   stage half spectra -> c2r (two real fields per complex line) -> physical products
 //   -> r2c (two real fields per complex line) -> Hermitian unpack -> store kx < KXP.
 // grid (ny*nz/LYZ); block >= LYZ*PIN*tpl_x
-// Real fields in:  u(3) w(3) [S(5) if LES] [rho if DEN]
+// Real fields in:  u(3) w(3) [S(5) if LES] [rho if DEN] [grad rho(3) if DEN == 2]
 // Real fields out: N(3) ke [tau(5) if LES] [flux(3) if DEN]
+// DEN: 0 no fourth field, 1 density / scalar, 2 with its LES diffusion (needs LES)
 // ====================================================================================
 // Block-wide max of |u_i| (and |rho|) in T, then one atomicMax per CTA on the state.
 // red: shared scratch of at least 32 T per quantity.
@@ -319,7 +330,7 @@ __device__ __forceinline__ void block_max_to_state(const Inst<T>& I, T umax, T r
 //   SandP (les_real_calc.jl:104-111): tau += cb D^2 Lie(S, Om)
 template <typename T>
 __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz, T yy, T yz, T wx, T wy, T wz,
-                                              T* o) {
+                                              T* o, T& nut_out) {
   const T zz = -xx - yy;
   const T S[3][3] = {{xx, xy, xz}, {xy, yy, yz}, {xz, yz, zz}};
   const T p = T(0.5) * wx, q = T(0.5) * wy, r = T(0.5) * wz;
@@ -374,6 +385,7 @@ __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz
     T B = b[0][0] * (b[1][1] + b[2][2]) + b[1][1] * b[2][2] - (b[0][1] * b[0][1] + b[0][2] * b[0][2] + b[1][2] * b[1][2]);
     B = B < T(0) ? T(0) : B;
     const T nut = c * sqrt(B / aa);
+    nut_out = nut;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -381,6 +393,7 @@ __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz
   } else if (m == FFS_LES_PRODUCTION) {
     const T qv = c * d2 * (om2s - s2s) / (T(2) * ss);
     const T nut = ss == T(0) ? T(0) : (qv > T(0) ? qv : T(0));
+    nut_out = nut;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -392,6 +405,7 @@ __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz
     const T fv = sqrt(sw[0] * sw[0] + sw[1] * sw[1] + sw[2] * sw[2]) / (sqrt(ss) * sqrt(wx * wx + wy * wy + wz * wz));
     const T nut = c * c * d2 * fv * fv * fv * sqrt(ss) / T(2);
     const T nup = T(I.les_cp) * d2 * fv * fv * fv * fv / T(4);
+    nut_out = nut;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -405,12 +419,14 @@ __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz
     const T tr = (tt[0][0] + tt[1][1] + tt[2][2]) / T(3);
     const T qv = c * d2 * (om2s - s2s) / (T(2) * ss);
     const T mnu = ss == T(0) ? T(0) : (qv < T(0) ? -qv : T(0));
+    nut_out = ss == T(0) ? T(0) : (qv > T(0) ? qv : T(0));   // stable_nl_eddy_viscosity's nu
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int j = 0; j < 3; ++j) t[i][j] = c * d2 * (tt[i][j] - (i == j ? tr : T(0))) + T(2) * mnu * S[i][j];
   } else {   // Smagorinsky (with the SandP term below)
     const T nut = c * c * d2 * sqrt(ss);
+    nut_out = nut;
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -426,14 +442,15 @@ __device__ __forceinline__ void les_model_tau(const Inst<T>& I, T xx, T xy, T xz
   o[0] = t[0][0]; o[1] = t[0][1]; o[2] = t[0][2]; o[3] = t[1][1]; o[4] = t[1][2];
 }
 
-template <bool LES, bool DEN> struct XFields {
-  static constexpr int nin = 6 + (LES ? 5 : 0) + (DEN ? 1 : 0);
+template <bool LES, int DEN> struct XFields {
+  static_assert(DEN != 2 || LES, "the fourth field's LES diffusion needs the LES model");
+  static constexpr int nin = 6 + (LES ? 5 : 0) + (DEN ? 1 : 0) + (DEN == 2 ? 3 : 0);
   static constexpr int nout = 4 + (LES ? 5 : 0) + (DEN ? 3 : 0);
   static constexpr int PIN = (nin + 1) / 2;
   static constexpr int POUT = (nout + 1) / 2;
 };
 
-template <typename T, bool LES, bool DEN, int LYZ, int N = 0>
+template <typename T, bool LES, int DEN, int LYZ, int N = 0>
 __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
   using XF = XFields<LES, DEN>;
   constexpr int PIN = XF::PIN, POUT = XF::POUT;
@@ -504,12 +521,14 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
     o[2] = ux * wy - uy * wx;
     o[3] = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);   // models.jl:224
     umaxt = fmax(umaxt, fmax(fabs(ux), fmax(fabs(uy), fabs(uz))));
+    T nut = T(0);   // the model's eddy viscosity: the fourth field's eddy diffusivity
     if (LES) {
       const T xx = f[6], xy = f[7], xz = f[8], yy = f[9], yz = f[10];
       if (I.les_model == FFS_LES_SMAGORINSKY && I.les_cb == 0.0) {
         const T zz = -xx - yy;
         const T nrm = sqrt(xx * xx + yy * yy + zz * zz + T(2) * (xy * xy + xz * xz + yz * yz));
         const T two_nut = les2 * nrm;   // tau = 2 nu_t S, nu_t = c^2 D^2 |S|
+        nut = T(0.5) * two_nut;         // exact: (2a) b = 2 (a b)
         o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
       } else if (I.dyn) {
         // dynamic Smagorinsky (les_real_calc.jl:71-73): nu_t = max(cmin, min(0.4, c)) D^2 |S|,
@@ -519,7 +538,8 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         const long long pi = (long long)(g0 + q) * n + j;
         T cc = T(I.dyn_c[pi]);
         if (!isnan(cc)) cc = fmax(T(I.les_cmin), fmin(T(0.4), cc));
-        const T two_nut = T(2) * (cc * T(I.les_d2) * nrm);
+        nut = cc * T(I.les_d2) * nrm;
+        const T two_nut = T(2) * nut;
         o[4] = two_nut * xx; o[5] = two_nut * xy; o[6] = two_nut * xz; o[7] = two_nut * yy; o[8] = two_nut * yz;
         if (I.dynp || I.les_cb != 0.0) {
           // + max(-0.8, min(0.8, cp)) D^2 Lie(S, W) (les_real_calc.jl:104-106), or SandP's
@@ -549,20 +569,33 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
           for (int e2 = 0; e2 < 5; ++e2) o[4 + e2] += b * lie[e2];
         }
       } else {
-        les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4);
+        les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4, nut);
       }
     }
     if (DEN) {
       constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
       const T rho = f[fr];
       rmaxt = fmax(rmaxt, fabs(rho));
-      o[of] = -rho * ux; o[of + 1] = -rho * uy; o[of + 2] = -rho * uz;   // models.jl:266
+      if (DEN == 2) {
+        // calc_les! (les_real_calc.jl:116-134): nu_t grad rho (+ (c D^2 / 2) w x grad rho),
+        // then realspacecalculation! adds it to -rho u (models.jl:265-268)
+        constexpr int fg = fr + 1;
+        const T gx = f[fg], gy = f[fg + 1], gz = f[fg + 2];
+        T lx = nut * gx, ly = nut * gy, lz = nut * gz;
+        if (I.rho_les == 2) {
+          const T cr = T(I.rho_les_c);
+          lx += cr * (wy * gz - wz * gy); ly += cr * (wz * gx - wx * gz); lz += cr * (wx * gy - wy * gx);
+        }
+        o[of] = -rho * ux + lx; o[of + 1] = -rho * uy + ly; o[of + 2] = -rho * uz + lz;
+      } else {
+        o[of] = -rho * ux; o[of + 1] = -rho * uy; o[of + 2] = -rho * uz;   // models.jl:266
+      }
     }
 #pragma unroll
     for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
   }
   // block max -> one atomic per CTA (the max is exact in T; FP64 only for the atomic)
-  if (I.adaptive) block_max_to_state<T, DEN>(I, umaxt, rmaxt, red);
+  if (I.adaptive) block_max_to_state<T, (DEN != 0)>(I, umaxt, rmaxt, red);
   __syncthreads();
 
   // 4. r2c of the output pairs, result back into sx
@@ -596,7 +629,7 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
     }
   }
 }
-template <typename T, bool LES, bool DEN, int LYZ>
+template <typename T, bool LES, int DEN, int LYZ>
 __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   b_x_pass<T, LES, DEN, LYZ>(I, Blk::here());
 }
@@ -1482,6 +1515,14 @@ __device__ __forceinline__ void b_stats(const Inst<T>& I, int mode, const Blk bk
         else { rw = T(1); for (int i = 0; i < I.rho_hv_m; ++i) rw *= k2; }
         q[Q_RHV] += w * rw * r2;
       }
+      if (I.rho_les && !I.scalar) {
+        // scalar_les_stats (stats.jl:1032-1083): proj(i k . flux, rho), flux the whole
+        // fourth-field flux (-rho u + the LES diffusion)
+        const cplx<T> dF = sb[7 * cs + g];
+        const T pr = w * (dF.x * rho.x + dF.y * rho.y);
+        q[Q_RPR] += pr;
+        if (I.sfil) q[Q_FRPR] += pr * G2;
+      }
       if (I.sfil) {
         if (I.rho_hv) q[Q_FRHV] += w * rw * r2 * G2;
         q[Q_FRHO2] += w * r2 * G2;
@@ -1716,10 +1757,16 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
           row[c++] = tot[Q_RHO]; row[c++] = tot[f ? Q_FRHO2 : Q_RHO2]; row[c++] = d1; row[c++] = d2;
           row[c++] = d3; row[c++] = rd;
           if (!I.scalar) {
-            // density hyperviscosity (density_stratification_types.jl:69-84): trhodiss += rhohdiss
+            // density LES and hyperviscosity (density_stratification_types.jl:46-87):
+            // trhodiss = rhodiss (+ rhopr) (+ rhohdiss), then bflux, rhopr, rhohdiss
+            const double rpr = -tot[f ? Q_FRPR : Q_RPR];
             const double rh = I.rho_hv == 2 ? -tot[f ? Q_FRHV : Q_RHV] : I.rho_hv_nu * tot[f ? Q_FRHV : Q_RHV];
-            row[c++] = I.rho_hv ? rd + rh : rd;
+            double trd = rd;
+            if (I.rho_les) trd += rpr;
+            if (I.rho_hv) trd += rh;
+            row[c++] = trd;
             row[c++] = -I.gval * tot[f ? Q_FBF : Q_BF];
+            if (I.rho_les) row[c++] = rpr;
             if (I.rho_hv) row[c++] = rh;
           }
         }
@@ -1754,12 +1801,13 @@ __device__ __forceinline__ void b_finalize(const Inst<T>& I, int mode, int npart
       double slot = tot[Q_D2DX];
       // STAT_FIL: the scalar's and the density's filtered sums go through reductionh
       // (scalar_stats, buoyancy_flux: density_stratification_types.jl:192-210)
-      if (I.sfil && I.density) slot = I.scalar ? tot[Q_FDR3] : (I.rho_hv ? tot[Q_FRHV] : tot[Q_FBF]);
+      if (I.sfil && I.density)
+        slot = I.scalar ? tot[Q_FDR3] : (I.rho_hv ? tot[Q_FRHV] : (I.rho_les ? tot[Q_FRPR] : tot[Q_FBF]));
       if (I.les) slot = tot[Q_LESH];
       if (I.hv) slot = tot[Q_HVH];
       S->slot_u = slot;
-      // the density's reduction: the buoyancy flux sum, then its hyperviscous sum
-      if (I.density) S->slot_rho = I.rho_hv ? tot[Q_RHV] : tot[Q_BF];
+      // the density's reduction: the buoyancy flux sum, then its LES and hyperviscous sums
+      if (I.density) S->slot_rho = I.rho_hv ? tot[Q_RHV] : ((I.rho_les && !I.scalar) ? tot[Q_RPR] : tot[Q_BF]);
     }
   }
   if (mode != 1 && (it % I.dt_spec) == 0) S->nspec += 1;

@@ -152,11 +152,22 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
         p.density_gradient = parse_number(d["densityGradient"])
         p.gravity = parse_number(d["zAcceleration"]) / parse_number(d["referenceDensity"])
         p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
-        if "densityLesModel" in d:
-            raise ValueError("density LES (densityLesModel) is not supported")
+        if "densityLesModel" in d:   # density_stratification_types.jl:176-185
+            if "lesModel" not in d:
+                # the reference's flux then keeps a bare grad rho (calc_les! never runs)
+                raise ValueError("densityLesModel needs lesModel")
+            if d["densityLesModel"] == "vorticityDiffusion":
+                p.rho_les = 2
+                p.rho_les_c = float(d.get("densityVorticityCoefficient", "0.1"))
+            else:
+                p.rho_les = 1
     if "passiveScalar" in d:   # simulationtypes.jl:320-352
-        if "lesModel" in d or "scalarLesModel" in d:
-            raise ValueError("the passive scalar's LES eddy diffusion is not supported")
+        if "lesModel" in d:    # the scalar's LES diffusion (simulationtypes.jl:334-346)
+            if d.get("scalarLesModel") == "vorticityDiffusion":
+                p.rho_les = 2
+                p.rho_les_c = float(d.get("scalarVorticityCoefficient", "1.0"))
+            else:
+                p.rho_les = 1
         if "densityStratification" in d:
             raise ValueError("a passive scalar together with density stratification is not supported")
         p.passive_scalar = 1

@@ -39,7 +39,7 @@ mutable struct FFSParams
     pf_zf_tanh::Int32; pf_qp::Float64; pf_qc::Float64; pf_qkf::Float64
     les_test_width::Float64; les_cmin::Float64; spec_fil::Float64; les_dynp::Int32
     hv_kind::Int32; hv_initk::Float64; hv_endk::Float64; rho_hv::Int32; rho_hv_nu::Float64; rho_hv_m::Int32
-    rho_hv_initk::Float64; rho_hv_endk::Float64; radix_split::Int32
+    rho_hv_initk::Float64; rho_hv_endk::Float64; rho_les::Int32; rho_les_c::Float64; radix_split::Int32
     FFSParams() = new()
 end
 
@@ -133,14 +133,25 @@ function parameters(d)
         p.filter_width = haskey(d, :filterWidth) ? num(d[:filterWidth]) :
                          (m == "SandP" && base == "Smagorinsky") ? 2 * (p.lx * 2π / p.nx) / p.cutoff : 0.0
     end
-    if haskey(d, :passiveScalar)   # simulationtypes.jl:320-352 (no scalar LES here)
+    if haskey(d, :passiveScalar)   # simulationtypes.jl:320-352
         p.passive_scalar = 1; p.scalar_pr = num(d[:scalarPr]); p.scalar_gradient = num(d[:scalarGradient])
         p.scalar_dir = Dict("x" => 0, "y" => 1, "z" => 2)[get(d, :scalarDirection, "z")]
+        if haskey(d, :lesModel)    # the scalar's LES diffusion (simulationtypes.jl:334-346)
+            vort = get(d, :scalarLesModel, "") == "vorticityDiffusion"
+            p.rho_les = vort ? 2 : 1
+            p.rho_les_c = vort ? (haskey(d, :scalarVorticityCoefficient) ? parse(Float64, d[:scalarVorticityCoefficient]) : 1.0) : 0.0
+        end
     end
     if haskey(d, :densityStratification)
         p.density = 1; p.density_pr = num(d[:Pr]); p.density_gradient = num(d[:densityGradient])
         p.gravity = num(d[:zAcceleration]) / num(d[:referenceDensity])
         p.gravity_dir = Dict("x" => 0, "y" => 1, "z" => 2)[get(d, :gravityDirection, "z")]
+        if haskey(d, :densityLesModel)   # density_stratification_types.jl:176-185
+            haskey(d, :lesModel) || error("densityLesModel needs lesModel")
+            vort = d[:densityLesModel] == "vorticityDiffusion"
+            p.rho_les = vort ? 2 : 1
+            p.rho_les_c = vort ? (haskey(d, :densityVorticityCoefficient) ? parse(Float64, d[:densityVorticityCoefficient]) : 0.1) : 0.0
+        end
     end
     if get(d, :forcing, "") == "isotropicBand"
         p.forcing = 1

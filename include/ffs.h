@@ -125,6 +125,12 @@ typedef struct ffs_params {
   double rho_hv_nu;            /* densityHyperViscosityCoefficient */
   int32_t rho_hv_m;            /* densityHyperViscosityM, default 2 */
   double rho_hv_initk, rho_hv_endk; /* densityInitk, densityEndk (<= 0: defaults as above) */
+  int32_t rho_les;             /* LES of the fourth field (needs les): 0 none, 1 eddy diffusion nu_t grad rho,
+                                  2 vorticity diffusion + (c Delta^2 / 2) w x grad rho (densityLesModel,
+                                  density_stratification_types.jl:176-185; a passive scalar under lesModel
+                                  takes 1, or 2 with scalarLesModel vorticityDiffusion, simulationtypes.jl
+                                  :334-346; les_real_calc.jl:116-135) */
+  double rho_les_c;            /* densityVorticityCoefficient (0.1) / scalarVorticityCoefficient (1.0) */
   int32_t radix_split;         /* runtime FFT plans: 0 the default radix split of each axis, k = 1, 2 the
                                   k-th alternative split (where the length has one; the autotuner times
                                   them and keeps the fastest per axis) */

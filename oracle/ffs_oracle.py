@@ -161,6 +161,8 @@ class Params:
     les_cmin: float = 0.0                # dynamicSmagorinsky: cmin
     les_dynp: str = ""                   # "dynamicSandP" / "piomelliSandP": the dynamic P tensor term
     sandp_cb: float = 0.0                # SandP: pConstant (0: no P term)
+    rho_les: str = ""                    # LES of the density / scalar: "", "eddy", "vorticity"
+    rho_les_c: float = 0.0               # densityVorticityCoefficient / scalarVorticityCoefficient
     filter_width: float | None = None
     scalar: bool = False                 # passiveScalar (simulationtypes.jl:198-213, :320-352)
     scalar_pr: float = 1.0
@@ -243,11 +245,19 @@ class Params:
             p.density_gradient = _num(d["densityGradient"])
             p.gravity = _num(d["zAcceleration"]) / _num(d["referenceDensity"])
             p.gravity_dir = {"x": 0, "y": 1, "z": 2}[d.get("gravityDirection", "z")]
+        if "densityLesModel" in d and "densityStratification" in d:   # density_stratification_types.jl:176-185
+            if "lesModel" not in d:
+                raise ValueError("densityLesModel without lesModel is not restated")
+            vort = d["densityLesModel"] == "vorticityDiffusion"
+            p.rho_les = "vorticity" if vort else "eddy"
+            p.rho_les_c = float(d.get("densityVorticityCoefficient", "0.1")) if vort else 0.0
         if "passiveScalar" in d:
             if "densityStratification" in d:
                 raise ValueError("a passive scalar together with density stratification is not restated")
-            if "lesModel" in d:
-                raise ValueError("the passive scalar's LES eddy diffusion is not restated")
+            if "lesModel" in d:                            # simulationtypes.jl:334-346
+                vort = d.get("scalarLesModel") == "vorticityDiffusion"
+                p.rho_les = "vorticity" if vort else "eddy"
+                p.rho_les_c = float(d.get("scalarVorticityCoefficient", "1.0")) if vort else 0.0
             p.scalar = True
             p.scalar_pr = _num(d["scalarPr"])
             p.scalar_gradient = _num(d["scalarGradient"])
@@ -743,7 +753,8 @@ def stats_header(p: Params) -> str:
     if p.scalar:
         cols.append("scalar,scalarp2,dscalardxp2,dscalardyp2,dscalardzp2,scalardiss")
     if p.density:
-        cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux" + (",rhohdiss" if p.rho_hv else ""))
+        cols.append("rho,rhop2,drhodxp2,drhodyp2,drhodzp2,rhodiss,trhodiss,bflux" + (",rhopr" if p.rho_les else "")
+                    + (",rhohdiss" if p.rho_hv else ""))
     if p.les:
         cols.append("prh,prv,praniso,pr")
     if p.plane_forcing == "aForcing":
@@ -869,7 +880,8 @@ def _to5(t):
 
 
 def les_stress(p: "Params", Sr, wr):
-    """tau of the pointwise LES models in physical space (calc_les!, les_real_calc.jl:13-139):
+    """tau of the pointwise LES models in physical space (calc_les!, les_real_calc.jl:13-139),
+    and the model's eddy viscosity nu_t (the density / scalar eddy diffusivity, :116-134):
     Smagorinsky nu_t = c^2 D^2 |S| (:77-79); Vreman (:132-139, VremanLESModel.jl); the
     production-viscosity model (ProductionViscosityLESModel.jl); Silvis (silvismodel.jl);
     the stable non-linear model (stablenonlinearmodel.jl); the SandP P term
@@ -885,17 +897,20 @@ def les_stress(p: "Params", Sr, wr):
             xx, xy, xz, yy, yz = Sr
             zz = -xx - yy
             nrm = np.sqrt(xx * xx + yy * yy + zz * zz + 2.0 * (xy * xy + xz * xz + yz * yz))
-            t = 2.0 * (c * c * d2 * nrm) * S
+            nut = c * c * d2 * nrm
+            t = 2.0 * nut * S
         elif m == "Vreman":
             a = S + _antisym(-0.5 * wr)
             b = d2 * _mm(np.swapaxes(a, 0, 1), a)
             B = b[0, 0] * (b[1, 1] + b[2, 2]) + b[1, 1] * b[2, 2] - (b[0, 1] ** 2 + b[0, 2] ** 2 + b[1, 2] ** 2)
             B = np.where(B < 0.0, 0.0, B)
-            t = 2.0 * (c * np.sqrt(B / _ddot(a, a))) * S
+            nut = c * np.sqrt(B / _ddot(a, a))
+            t = 2.0 * nut * S
         elif m == "productionViscosity":
             W = _antisym(-0.5 * wr)
             q = c * d2 * (_ddot(_mm(W, W), S) - _ddot(_mm(S, S), S)) / (2 * ss)
-            t = 2.0 * np.where(ss == 0.0, 0.0, np.maximum(0.0, q)) * S
+            nut = np.where(ss == 0.0, 0.0, np.maximum(0.0, q))
+            t = 2.0 * nut * S
         elif m == "Silvis":
             Sw = np.einsum("ij...,j...->i...", S, wr)
             fv = np.sqrt(_ddot(Sw[:, None], Sw[:, None])) / (np.sqrt(ss) * np.sqrt(np.sum(wr * wr, axis=0)))
@@ -909,13 +924,14 @@ def les_stress(p: "Params", Sr, wr):
             T = T - (np.trace(T) / 3.0) * np.eye(3).reshape(3, 3, *([1] * (T.ndim - 2)))
             q = c * d2 * (_ddot(_mm(W, W), S) - _ddot(_mm(S, S), S)) / (2 * ss)
             mnu = np.where(ss == 0.0, 0.0, -np.minimum(0.0, q))
+            nut = np.where(ss == 0.0, 0.0, np.maximum(0.0, q))      # stable_nl_eddy_viscosity's nu
             t = c * d2 * T + 2.0 * mnu * S
         else:
             raise ValueError(m)
         if p.sandp_cb:
             Om = _antisym(0.5 * wr)
             t = t + (p.sandp_cb * d2) * (_mm(S, Om) - _mm(Om, S))
-    return _to5(t)
+    return _to5(t), nut
 
 
 class OracleSimulation:
@@ -1057,14 +1073,24 @@ class OracleSimulation:
         if p.les:
             Sr = g.real(S)
             if p.les_model in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
-                taur = self.dynamic_smagorinsky(u, ur, S, Sr, w, wr)
+                taur, nut = self.dynamic_smagorinsky(u, ur, S, Sr, w, wr)
             else:
-                taur = les_stress(p, Sr, wr)
+                taur, nut = les_stress(p, Sr, wr)
         # realspacecalculation! (models.jl:236-280): rhs = u x w ; flux = -rho u
         nl = np.stack([ur[1] * wr[2] - ur[2] * wr[1], ur[2] * wr[0] - ur[0] * wr[2],
                        ur[0] * wr[1] - ur[1] * wr[0]])
         if p.fld:
             flux = -rhor[None] * ur                               # models.jl:265-275
+            if p.rho_les:
+                # calc_les! (les_real_calc.jl:116-134): nu_t grad rho (+ (c D^2 / 2) w x grad rho),
+                # grad rho = real!(i k rho) (fourierspacep1!, models.jl:110-115)
+                gr = g.real(np.stack([ikx * self.rho, iky * self.rho, ikz * self.rho]))
+                lf = nut[None] * gr
+                if p.rho_les == "vorticity":
+                    cr = p.rho_les_c * p.filter_width ** 2 / 2
+                    lf = lf + cr * np.stack([wr[1] * gr[2] - wr[2] * gr[1], wr[2] * gr[0] - wr[0] * gr[2],
+                                             wr[0] * gr[1] - wr[1] * gr[0]])
+                flux = flux + lf
         if p.variable_dt:                                         # find_max, utils.jl:247-258
             m = float(np.max(np.abs(ur)))
             self.slot_u = max(m, self.slot_u) if p.reference_cfl_slot else m
@@ -1089,6 +1115,8 @@ class OracleSimulation:
             sp.update(self.spectra_write_spec(nlh, kspec, tauh, ikflux))
             self.spectra[self.iteration] = sp
         if stats_t:                                               # models.jl:38-46
+            if p.density and p.rho_les:   # the flux scalar_les_stats reads (stats.jl:1032-1053)
+                self.ikflux_st = 1j * (KX * fluxh[0] + (KY * fluxh[1] + KZ * fluxh[2]))
             self.nlstats = self.non_linear_stats(nlh, kspec)
             self.pressstats = self.pressure_stats(nlh, kspec, tauh)
         # fourierspacep2! (models.jl:282-364)
@@ -1258,7 +1286,7 @@ class OracleSimulation:
             tau = tau + (p.sandp_cb * d2) * _to5(_mm(A, B) - _mm(B, A))
         if dynp:
             tau = tau + (np.maximum(-0.8, np.minimum(0.8, cpf)) * d2)[None] * lie_r
-        return tau
+        return tau, nut
 
     def div_tau(self, tauh):
         """(i k) . tau for a symmetric traceless tau (models.jl:330)."""
@@ -1469,14 +1497,23 @@ class OracleSimulation:
             rhodiss = self.alpha * (d1 + d2 + d3)
             bf_raw = self._wsum(_proj(u[p.gravity_dir], rho))
             bflux = -self.gvec[p.gravity_dir] * bf_raw
+            # density_stratification_types.jl:46-87: trhodiss = rhodiss (+ rhopr) (+ rhohdiss);
+            # each sum leaves its raw total in the density's reduction slot
+            trd, tail, rslot = rhodiss, [], bf_raw
+            if p.rho_les:   # scalar_les_stats (stats.jl:1032-1053): rhopr = -sum proj(i k.flux, rho)
+                pr_raw = self._wsum(_proj(self.ikflux_st, rho))
+                trd += -pr_raw
+                tail.append(-pr_raw)
+                rslot = pr_raw
             if p.rho_hv:   # scalar_hvis_stats (stats.jl:1086-1110, 1145-1171), trhodiss += it
                 rh_raw = self._wsum(self._rho_hv_weight() * r2)
                 rh = -rh_raw if p.rho_hv == "barrier" else p.rho_hv_nu * rh_raw
-                extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss + rh, bflux, rh]
-            else:
-                extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, rhodiss, bflux]
+                trd += rh
+                tail.append(rh)
+                rslot = rh_raw
+            extra += [rho[0, 0, 0].real, rho2, d1, d2, d3, rhodiss, trd, bflux] + tail
             if p.variable_dt and p.reference_cfl_slot:
-                self.slot_rho = rh_raw if p.rho_hv else bf_raw
+                self.slot_rho = rslot
         if p.les:
             t = self.div_tau(self.tauh)
             hraw = self._wsum(_proj(t[0], u[0]) + _proj(t[1], u[1]))
@@ -1558,14 +1595,19 @@ class OracleSimulation:
         if p.density:
             vals, fslot = scalar_fil(self.rho)
             bf_raw = ws(_proj(u[p.gravity_dir], self.rho))
+            trd, tail, fslot = vals[-1], [], bf_raw
+            if p.rho_les:   # the filtered sum goes through reductionh (density_stratification_types.jl:58)
+                pr_raw = ws(_proj(self.ikflux_st, self.rho))
+                trd += -pr_raw
+                tail.append(-pr_raw)
+                fslot = pr_raw
             if p.rho_hv:
                 rh_raw = ws(self._rho_hv_weight() * np.abs(self.rho) ** 2)
                 rh = -rh_raw if p.rho_hv == "barrier" else p.rho_hv_nu * rh_raw
-                extra += vals + [vals[-1] + rh, -self.gvec[p.gravity_dir] * bf_raw, rh]
+                trd += rh
+                tail.append(rh)
                 fslot = rh_raw
-            else:
-                extra += vals + [vals[-1], -self.gvec[p.gravity_dir] * bf_raw]
-                fslot = bf_raw
+            extra += vals + [trd, -self.gvec[p.gravity_dir] * bf_raw] + tail
         if p.les:
             t = self.div_tau(self.tauh)
             prh = -ws(_proj(t[0], u[0]) + _proj(t[1], u[1]))

@@ -43,8 +43,14 @@ def make_ic(pkg, d, seed=7, k0=3.0, density=False):
         uh = g.project(uh) * np.exp(-np.sqrt(g.K2) / 4)[None]
         u = tuple(g.real(uh))
     rho = None
-    if density:
-        rho = 0.1 * pkg.random_spectrum(nx, k0=k0, seed=seed + 1)[0] if nx == ny == nz else None
+    if density and nx == ny == nz:
+        rho = 0.1 * pkg.random_spectrum(nx, k0=k0, seed=seed + 1)[0]
+    elif density:
+        rng = np.random.default_rng(seed + 1)
+        g = Grid(nx, ny, nz)
+        rh = g.myfourier(rng.standard_normal((nz, ny, nx))) * np.exp(-np.sqrt(g.K2) / 4)
+        rh[0, 0, 0] = 0.0
+        rho = 0.1 * g.real(rh) / np.sqrt(np.mean(g.real(rh) ** 2))
     return u, rho
 
 
@@ -147,6 +153,36 @@ FIXED_CASES = {
                                           zAcceleration="1", referenceDensity="1", specFil="3"),
     "ab3-adaptive-scalar-specfil": gdict(32, adaptive=True, passiveScalar="true", scalarPr="0.7", scalarGradient="1",
                                          specFil="1.5", forcing="isotropicBand", forcingPower="0.1", forcingKf="2.5"),
+    # LES of the density and the scalar (les_real_calc.jl:116-134): eddy diffusion nu_t grad rho,
+    # vorticity diffusion + (c D^2 / 2) w x grad rho; nu_t of each model; rhopr and its
+    # place in trhodiss and in the CFL slots (density_stratification_types.jl:46-87)
+    "etd-les-density-eddy": gdict(32, "ETD3rdO", lesModel="Smagorinsky", densityStratification="true", Pr="1",
+                                  densityGradient="1", zAcceleration="1", referenceDensity="1",
+                                  densityLesModel="eddyDiffusion"),
+    "etd-dynamic-density-vorticity": gdict(32, "ETD3rdO", lesModel="dynamicSmagorinsky", densityStratification="true",
+                                           Pr="1", densityGradient="1", zAcceleration="1", referenceDensity="1",
+                                           densityLesModel="vorticityDiffusion", densityVorticityCoefficient="0.3"),
+    "ab3-adaptive-vreman-density-vort-specfil": gdict(32, adaptive=True, lesModel="Vreman", densityStratification="true",
+                                                      Pr="2", densityGradient="1", zAcceleration="1",
+                                                      referenceDensity="1", densityLesModel="vorticityDiffusion",
+                                                      specFil="2"),
+    "ab3-adaptive-stablenl-density-eddy-hv": gdict(32, adaptive=True, lesModel="stableNonLinear",
+                                                   densityStratification="true", Pr="1", densityGradient="1",
+                                                   zAcceleration="1", referenceDensity="1",
+                                                   densityLesModel="eddyDiffusion", densityHyperViscosity="true",
+                                                   densityHyperViscosityCoefficient="1e-4"),
+    "ab3-production-density-eddy": gdict(48, lesModel="productionViscosity", densityStratification="true", Pr="1",
+                                         densityGradient="1", zAcceleration="1", referenceDensity="1",
+                                         densityLesModel="eddyDiffusion"),
+    "etd-scalar-les": gdict(32, "ETD3rdO", lesModel="Smagorinsky", passiveScalar="true", scalarPr="0.7",
+                            scalarGradient="1"),
+    "ab3-adaptive-silvis-scalar-vort": gdict(32, adaptive=True, lesModel="Silvis", passiveScalar="true", scalarPr="1",
+                                             scalarGradient="1", scalarLesModel="vorticityDiffusion",
+                                             scalarVorticityCoefficient="0.5"),
+    # nz >= 128: the flux's z component comes from the density's slot on the one-component path
+    "etd-nz128-les-density-vort": gdict(32, "ETD3rdO", nz=128, dt="0.005", lesModel="Smagorinsky",
+                                        densityStratification="true", Pr="1", densityGradient="1", zAcceleration="1",
+                                        referenceDensity="1", densityLesModel="vorticityDiffusion"),
 }
 
 
@@ -195,7 +231,8 @@ def test_etd_adaptive_parity(gpu_pkg):
 
 @pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
                                   "ab3-stable-nonlinear", "etd-dynamic-smagorinsky", "ab3-adaptive-piomelli",
-                                  "ab3-adaptive-piomelli-sandp"])
+                                  "ab3-adaptive-piomelli-sandp", "etd-les-density-eddy",
+                                  "ab3-adaptive-silvis-scalar-vort"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)
@@ -234,6 +271,7 @@ SPEC_CASES = {
     "etd-scalar": dict(FIXED_CASES["etd-scalar"], dtSpec="2"),
     "etd-les-density-hv-specfil": dict(FIXED_CASES["etd-les-density-hv-specfil"], dtSpec="2"),
     "etd-barriers-density-specfil": dict(FIXED_CASES["etd-barriers-density-specfil"], dtSpec="2"),
+    "etd-dynamic-density-vorticity": dict(FIXED_CASES["etd-dynamic-density-vorticity"], dtSpec="2"),
 }
 
 
@@ -270,6 +308,14 @@ def test_errors_and_state_checks(gpu_pkg):
     # the reference's AB3 has no explicit term for the spectral barrier
     with pytest.raises(gpu_pkg.FFSError) as e:
         gpu_pkg.Simulation.from_global(dict(d, hyperViscosity="spectralBarrier"))
+    assert e.value.code == -6
+    # the density's LES diffusion needs an LES model (the reference's flux would keep a bare
+    # grad rho): refused through the C ABI too
+    prm = gpu_pkg.parameters(dict(d, densityStratification="true", Pr="1", densityGradient="1",
+                                  zAcceleration="1", referenceDensity="1"))
+    prm.rho_les = 1
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        gpu_pkg.Simulation(prm)
     assert e.value.code == -6
     # a non-finite initial condition is reported, not propagated silently
     u, _ = make_ic(gpu_pkg, d)

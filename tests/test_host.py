@@ -214,6 +214,40 @@ def test_parameters_hyperviscosity_kinds(pkg):
     assert (p.rho_hv, p.rho_hv_endk) == (2, 20.0) and (o.rho_hv, o.rho_hv_endk) == ("barrier", 20.0)
 
 
+def test_parameters_density_and_scalar_les(pkg):
+    """densityLesModel (density_stratification_types.jl:176-185) and the passive scalar's LES
+    diffusion under lesModel (simulationtypes.jl:334-346): eddy diffusion by default,
+    vorticity diffusion with its coefficient (0.1 for the density, 1.0 for the scalar)."""
+    from oracle.ffs_oracle import Params
+    base = {"nx": "32", "ny": "32", "nz": "32", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+            "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1"}
+    dens = dict(base, densityStratification="true", Pr="1", densityGradient="1", zAcceleration="1",
+                referenceDensity="1", lesModel="Smagorinsky")
+    scal = dict(base, passiveScalar="true", scalarPr="1", scalarGradient="1", lesModel="Vreman")
+    cases = [
+        (dict(dens), 0, 0.0, ""),
+        (dict(dens, densityLesModel="eddyDiffusion"), 1, 0.0, "eddy"),
+        (dict(dens, densityLesModel="vorticityDiffusion"), 2, 0.1, "vorticity"),
+        (dict(dens, densityLesModel="vorticityDiffusion", densityVorticityCoefficient="0.25"), 2, 0.25, "vorticity"),
+        (dict(scal), 1, 0.0, "eddy"),
+        (dict(scal, scalarLesModel="vorticityDiffusion"), 2, 1.0, "vorticity"),
+        (dict(scal, scalarLesModel="vorticityDiffusion", scalarVorticityCoefficient="0.5"), 2, 0.5, "vorticity"),
+        (dict(base, passiveScalar="true", scalarPr="1", scalarGradient="1", scalarLesModel="vorticityDiffusion"),
+         0, 0.0, ""),
+    ]
+    for d, kind, c, okind in cases:
+        p, o = pkg.parameters(d), Params.from_global(d)
+        assert (p.rho_les, p.rho_les_c) == (kind, c), d
+        assert (o.rho_les, o.rho_les_c) == (okind, c), d
+    # without lesModel the reference's density flux keeps a bare grad rho: refused
+    d = dict(dens, densityLesModel="eddyDiffusion")
+    del d["lesModel"]
+    with pytest.raises(ValueError):
+        pkg.parameters(d)
+    with pytest.raises(ValueError):
+        Params.from_global(d)
+
+
 def test_parse_number(pkg):
     assert pkg.parse_number("2π") == pytest.approx(2 * np.pi)
     assert pkg.parse_number("2pi/128") == pytest.approx(2 * np.pi / 128)
