@@ -20,7 +20,7 @@ FFS_FP64, FFS_FP32 = 0, 1
 # Every symbol include/ffs.h declares (checked by the CPU test suite).
 EXPORTS = [
     "ffs_params_default", "ffs_create", "ffs_set_fields", "ffs_initialize", "ffs_step", "ffs_finalize",
-    "ffs_forcing_shells", "ffs_forcing_array",
+    "ffs_forcing_shells", "ffs_forcing_array", "ffs_capture_output", "ffs_output_field",
     "ffs_get_fields",
     "ffs_get_spectral", "ffs_set_spectral", "ffs_stats_header", "ffs_stats_ncols", "ffs_record_ncols",
     "ffs_stats_records", "ffs_stats", "ffs_spectrum", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
@@ -114,6 +114,8 @@ def load() -> ctypes.CDLL:
         "ffs_finalize": (c_int32, [H]),
         "ffs_forcing_shells": (c_int32, [H]),
         "ffs_forcing_array": (c_int32, [H, c_int32, D, c_int32, c_int32]),
+        "ffs_capture_output": (c_int32, [H, c_int32]),
+        "ffs_output_field": (c_int32, [H, c_int32, D, POINTER(c_int64)]),
         "ffs_get_fields": (c_int32, [H, D, D, D, D, c_int32]),
         "ffs_get_spectral": (c_int32, [H, c_int32, D]),
         "ffs_set_spectral": (c_int32, [H, c_int32, D]),

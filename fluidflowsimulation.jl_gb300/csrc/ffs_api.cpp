@@ -113,6 +113,15 @@ int ffs_finalize(ffs_handle* h) {
   return guarded(h, [&] { return h->eng->finish(h->err); });
 }
 
+int ffs_capture_output(ffs_handle* h, int32_t on) {
+  return guarded(h, [&] { return h->eng->capture_output(on, h->err); });
+}
+
+int ffs_output_field(ffs_handle* h, int32_t field, double* out, int64_t* iteration) {
+  if (!out) return FFS_EINVAL;
+  return guarded(h, [&] { return h->eng->output_field(field, out, iteration, h->err); });
+}
+
 int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout) {
   return guarded(h, [&] { return h->eng->get_fields(u1, u2, u3, rho, layout, h->err); });
 }

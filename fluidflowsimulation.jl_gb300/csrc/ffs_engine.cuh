@@ -136,10 +136,21 @@ class Engine : public EngineBase {
   cplx<T>* dfz = nullptr;
   double* dync = nullptr;
   size_t smem_d0 = 0, smem_d1 = 0, smem_dzf = 0;
+  // output capture (writeoutput's LES fields, output.jl:22-42): FP64 planes written by
+  // the x pass of each output step, their iteration, the step graph that does it
+  double* obuf = nullptr;
+  int out_nf = 0;
+  int64_t out_iter = -1;
+  int64_t calls = 0;          // steps since ffs_initialize (the integrator's call counter)
+  bool diag_x = false;        // enqueue_step records the capture form of the x pass
+  cudaGraph_t graph_out = nullptr;
+  cudaGraphExec_t gexec_out = nullptr;
 
   ~Engine() override {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    if (gexec_out) cudaGraphExecDestroy(gexec_out);
+    if (graph_out) cudaGraphDestroy(graph_out);
     for (void* p : allocs) cudaFree(p);
     if (ev_fork) cudaEventDestroy(ev_fork);
     if (ev_join) cudaEventDestroy(ev_join);
@@ -876,7 +887,25 @@ class Engine : public EngineBase {
       k<<<dim3((unsigned)((long long)I.ny * I.nz / XLes<N>::LYZ)), XLes<N>::NT, XLes<N>::smem(), s>>>(I);
     }
   }
+  template <int LY> static XK xdiag_sel(bool DL) {
+    return DL ? k_x_pass_diag<T, 2, LY> : k_x_pass_diag<T, 1, LY>;
+  }
+  // the capture form of the LES x pass (every LES configuration; density or not)
+  XK xdiag_ptr() const {
+    const bool dl = I.rho_les != 0;
+    if (!I.density) return lyz == 4 ? k_x_pass_diag<T, 0, 4> : (lyz == 2 ? k_x_pass_diag<T, 0, 2> : k_x_pass_diag<T, 0, 1>);
+    if (lyz == 4) return xdiag_sel<4>(dl);
+    if (lyz == 2) return xdiag_sel<2>(dl);
+    return xdiag_sel<1>(dl);
+  }
   void launch_x() {
+    if (diag_x) {   // an output step: the generic x pass that also stores the output planes
+      Inst<T> J = I;
+      J.obuf = obuf;
+      const int PIN = (nin + 1) / 2;
+      xdiag_ptr()<<<dim3(I.ny * I.nz / lyz), blk(PIN * lyz, I.px), smem_x, s>>>(J);
+      return;
+    }
     if (xfused && I.les) {
       if (xfused == 64) launch_x_les<64>();
       else launch_x_les<128>();
@@ -1094,9 +1123,11 @@ class Engine : public EngineBase {
       modes.insert(modes.end(), byshell[n].begin(), byshell[n].end());
     }
     start[nsh] = (int)modes.size();
-    std::vector<double> d(8 * (size_t)nsh + 4 * (size_t)plane, 0.0);
+    // [9][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum, N, Nm1, Ef; then aForcing's
+    // [4][plane]: R, Em, factor, Zf per plane mode
+    std::vector<double> d(9 * (size_t)nsh + 4 * (size_t)plane, 0.0);
     for (int i = 0; i < nsh; ++i) { d[3 * nsh + i] = kh[i]; d[4 * nsh + i] = zf[i]; d[5 * nsh + i] = qr[i]; }
-    for (int m = 0; m < plane; ++m) d[8 * (size_t)nsh + 3 * (size_t)plane + m] = zf2[m];
+    for (int m = 0; m < plane; ++m) d[9 * (size_t)nsh + 3 * (size_t)plane + m] = zf2[m];
     int rc;
     double* dd_ = nullptr;
     int *ds = nullptr, *dm = nullptr, *dn = nullptr;
@@ -1117,16 +1148,41 @@ class Engine : public EngineBase {
     return 0;
   }
   std::vector<double> pf_avgk;
+  // aForcing's R as the reference's (nx/2+1) x ny matrix, kx fastest (Julia's vec order;
+  // forcing_types.jl:362-368, output.jl:49-51); modes outside the retained plane are 0
+  int forcing_modes(double* v, int n, int set, std::string& err) {
+    const int nxh = I.nxh, plane = I.NYR * I.KXP;
+    if (!v || n != nxh * P.ny) { err = "aForcing R: n must be (nx/2+1) * ny"; return FFS_EINVAL; }
+    std::vector<double> h(plane, 0.0);
+    double* dev = I.pf_d + 9 * (size_t)I.pf_nsh;
+    auto ycol = [&](int jc) { return jc < I.ypos ? jc : P.ny - I.NYR + jc; };
+    if (set) {
+      for (int jc = 0; jc < I.NYR; ++jc)
+        for (int ix = 0; ix < I.Mx; ++ix) h[(size_t)jc * I.KXP + ix] = v[(size_t)ycol(jc) * nxh + ix];
+      FFS_CK(cudaMemcpyAsync(dev, h.data(), sizeof(double) * plane, cudaMemcpyHostToDevice, s));
+      FFS_CK(cudaStreamSynchronize(s));
+      return 0;
+    }
+    FFS_CK(cudaMemcpyAsync(h.data(), dev, sizeof(double) * plane, cudaMemcpyDeviceToHost, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    std::fill(v, v + n, 0.0);
+    for (int jc = 0; jc < I.NYR; ++jc)
+      for (int ix = 0; ix < I.Mx; ++ix) v[(size_t)ycol(jc) * nxh + ix] = h[(size_t)jc * I.KXP + ix];
+    return 0;
+  }
 
   int forcing_shells() const override { return (I.pforce && I.pforce != FFS_PF_A) ? I.pf_nsh : 0; }
   int forcing_array(int which, double* v, int n, int set, std::string& err) override {
+    if (I.pforce == FFS_PF_A && which == 5) return forcing_modes(v, n, set, err);
     if (!I.pforce || I.pforce == FFS_PF_A) { err = "no per-shell plane forcing in this simulation"; return FFS_ESTATE; }
-    if (!v || n != I.pf_nsh || which < 0 || which > 3 || (which == 2 && set)) {
-      err = "forcing array: which must be 0 (R), 1 (Em), 2 (avgK, read only) or 3 (N), n the shell count";
+    if (!v || n != I.pf_nsh || which < 0 || which > 4 || (which == 2 && set) || (which == 4 && set)) {
+      err = "forcing array: which must be 0 (R), 1 (Em), 2 (avgK, read only), 3 (N) or 4 (Ef, read only), "
+            "n the shell count";
       return FFS_EINVAL;
     }
     if (which == 2) { std::copy(pf_avgk.begin(), pf_avgk.end(), v); return 0; }
-    double* dst = I.pf_d + (size_t)(which == 3 ? 6 : which) * I.pf_nsh;
+    const int row = which == 3 ? 6 : (which == 4 ? 8 : which);
+    double* dst = I.pf_d + (size_t)row * I.pf_nsh;
     if (set) FFS_CK(cudaMemcpyAsync(dst, v, sizeof(double) * n, cudaMemcpyHostToDevice, s));
     else FFS_CK(cudaMemcpyAsync(v, dst, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     FFS_CK(cudaStreamSynchronize(s));
@@ -1179,6 +1235,9 @@ class Engine : public EngineBase {
     launch_fwd_y(F);
     launch_fwd_z_store(F);
     FFS_CK(cudaGetLastError());
+    // no fourth field given: exactly zero (ScalarField's zeros, density_stratification_types
+    // .jl:166), not the rounding that the packed two-field transform leaks from u3 into it
+    if (I.density && !rho) FFS_CK(cudaMemsetAsync(I.uh + 3 * I.cstride, 0, sizeof(cplx<T>) * I.cstride, s));
     int rc;
     if ((rc = reset_state(err))) return rc;
     FFS_CK(cudaMemsetAsync(I.hist, 0, sizeof(cplx<T>) * 2 * I.ncomp * I.cstride, s));
@@ -1292,6 +1351,8 @@ class Engine : public EngineBase {
     FFS_CK(cudaStreamSynchronize(s));
     if ((rc = pull_state(err))) return rc;
     initialized = true;
+    calls = 0;
+    out_iter = -1;
     return 0;
   }
 
@@ -1299,20 +1360,70 @@ class Engine : public EngineBase {
   // included), the forcing, and writestats at the current iteration, without an update.
   int finish(std::string& err) override {
     if (!initialized) { err = "ffs_initialize must be called before ffs_finalize"; return FFS_ESTATE; }
+    diag_x = obuf != nullptr;   // the tail's calculate_rhs! feeds the final writeoutput
     enqueue_step(2);
+    diag_x = false;
+    if (obuf) out_iter = iteration;
     FFS_CK(cudaGetLastError());
     FFS_CK(cudaStreamSynchronize(s));
     return drain(iteration, iteration, err);
   }
 
-  int build_graph(std::string& err) {
-    if (gexec) return 0;
+  int capture_graph(bool diag, cudaGraph_t* g, cudaGraphExec_t* x, std::string& err) {
     FFS_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    diag_x = diag;
     enqueue_step(0);
-    cudaError_t e = cudaStreamEndCapture(s, &graph);
+    diag_x = false;
+    cudaError_t e = cudaStreamEndCapture(s, g);
     if (e != cudaSuccess) { err = std::string("graph capture: ") + cudaGetErrorString(e); return FFS_ECUDA; }
-    FFS_CK(cudaGraphInstantiate(&gexec, graph, 0));
-    n_launch = launches_per_step();
+    FFS_CK(cudaGraphInstantiate(x, *g, 0));
+    return 0;
+  }
+  int build_graph(std::string& err) {
+    int rc;
+    if (!gexec) {
+      if ((rc = capture_graph(false, &graph, &gexec, err))) return rc;
+      n_launch = launches_per_step();
+    }
+    if (obuf && !gexec_out && (rc = capture_graph(true, &graph_out, &gexec_out, err))) return rc;
+    return 0;
+  }
+  // writeoutput runs inside calculate_rhs! when a step starts at a multiple of writeTime,
+  // except the first step after initialize! (is_output_time, simulationtypes.jl:102)
+  bool output_step(int64_t it, int64_t call) const {
+    return obuf && call != 0 && it % P.write_time == 0;
+  }
+
+  int capture_output(int on, std::string& err) override {
+    if (!on) return 0;
+    if (!I.les) return 0;   // the captured fields are the LES model's
+    if (obuf) return 0;
+    out_nf = 5 + (I.dyn ? 1 : 0) + (I.dynp ? 1 : 0) + ((I.rho_les && !I.scalar) ? 3 : 0);
+    int rc;
+    if ((rc = alloc(&obuf, (size_t)out_nf * P.nx * P.ny * P.nz, err))) return rc;
+    if ((rc = smem_attr(xdiag_ptr(), smem_x, err))) return rc;
+    return 0;
+  }
+  // plane of an output field: 0..4 T11 T12 T13 T22 T23, 5 cs, 6 cp, 7..9 dflux1..3
+  int out_plane(int field) const {
+    if (field >= 0 && field < 5) return field;
+    int pl = 5;
+    if (field == FFS_OUT_CS) return I.dyn ? pl : -1;
+    if (I.dyn) ++pl;
+    if (field == FFS_OUT_CP) return I.dynp ? pl : -1;
+    if (I.dynp) ++pl;
+    if (field >= FFS_OUT_DFLUX1 && field <= FFS_OUT_DFLUX3) return (I.rho_les && !I.scalar) ? pl + field - FFS_OUT_DFLUX1 : -1;
+    return -1;
+  }
+  int output_field(int field, double* out, int64_t* it, std::string& err) override {
+    if (!obuf) { err = "output capture is off (ffs_capture_output)"; return FFS_ESTATE; }
+    const int pl = out_plane(field);
+    if (pl < 0) { err = "this simulation has no such output field"; return FFS_EINVAL; }
+    if (out_iter < 0) { err = "no output step has run since the capture was switched on"; return FFS_ESTATE; }
+    const size_t N = (size_t)P.nx * P.ny * P.nz;
+    FFS_CK(cudaMemcpyAsync(out, obuf + (size_t)pl * N, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+    FFS_CK(cudaStreamSynchronize(s));
+    if (it) *it = out_iter;
     return 0;
   }
 
@@ -1384,7 +1495,12 @@ class Engine : public EngineBase {
         ns += a; nsp += b; ++chunk;
         if (chunk >= 4096) break;
       }
-      for (int64_t i = 0; i < chunk; ++i) FFS_CK(cudaGraphLaunch(gexec, s));
+      for (int64_t i = 0; i < chunk; ++i) {
+        const bool o = output_step(it0 + i, calls);
+        FFS_CK(cudaGraphLaunch(o ? gexec_out : gexec, s));
+        if (o) out_iter = it0 + i;
+        ++calls;
+      }
       FFS_CK(cudaStreamSynchronize(s));
       if ((rc = drain(it0, it0 + chunk - 1, err))) return rc;
       done += chunk;
@@ -1401,6 +1517,7 @@ class Engine : public EngineBase {
     FFS_CK(cudaEventCreate(&b));
     FFS_CK(cudaEventRecord(a, s));
     for (int64_t i = 0; i < n; ++i) FFS_CK(cudaGraphLaunch(gexec, s));
+    calls += n;
     FFS_CK(cudaEventRecord(b, s));
     FFS_CK(cudaEventSynchronize(b));
     float f = 0.f;

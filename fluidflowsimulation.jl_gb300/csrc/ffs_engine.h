@@ -63,6 +63,9 @@ class EngineBase {
   virtual int sync_host_state(int64_t it_first, int64_t it_last, std::string& err) = 0;
   // launch shapes picked by the autotuner, with the timings of the candidates
   virtual std::string tuning() const = 0;
+  // output capture: the LES fields writeoutput writes at output steps and at the tail
+  virtual int capture_output(int on, std::string& err) = 0;
+  virtual int output_field(int field, double* out, int64_t* iteration, std::string& err) = 0;
   // host-side views
   std::string header;
   int ncols_stats = 0, ncols_rec = 0;

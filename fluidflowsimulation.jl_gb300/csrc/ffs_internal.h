@@ -112,6 +112,7 @@ template <typename T> struct Inst {
   cplx<T>* wy;             // [slot][nz][ny][KXP]
   long long wzs, wys;      // slot strides
   double* phys;            // FP64 physical staging [field][nz][ny][nx]
+  double* obuf;            // output capture (set only for the capture step's x pass)
   // scalar state and outputs
   DevState* st;
   double* partials;        // [stats CTAs][QPAD]
@@ -161,7 +162,7 @@ template <typename T> struct Inst {
   // kz = 0 plane forcing (FFS_PF_*): per-shell state and tables, plane-mode lists, force
   int pforce, pf_nsh;
   double pf_maxdk, pf_kf, pf_tf, pf_alpha, pf_cfl;
-  double* pf_d;            // [8][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum, N, Nm1;
+  double* pf_d;            // [9][nsh]: R, Em, factor, avgK, Zf, Qf power spectrum, N, Nm1, Ef;
                            // then aForcing's [4][NYR * KXP]: R, Em, factor, Zf per plane mode
   const int* pf_start;     // [nsh + 1]: retained kz = 0 modes of each spectrum shell (CSR)
   const int* pf_modes;     //   their plane index jc * KXP + ix

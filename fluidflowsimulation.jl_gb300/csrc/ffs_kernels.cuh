@@ -450,7 +450,11 @@ template <bool LES, int DEN> struct XFields {
   static constexpr int POUT = (nout + 1) / 2;
 };
 
-template <typename T, bool LES, int DEN, int LYZ, int N = 0>
+// DIAG (output iterations with output capture): also store the physical LES stress, the
+// dynamic coefficients and the fourth field's LES flux to I.obuf (writeoutput,
+// output.jl:22-42), as FP64 planes [field][z][y][x]: tau xx, xy, xz, yy, yz, then c
+// (dynamic models), cp (dynamic P tensor), then the flux's 3 components (density LES)
+template <typename T, bool LES, int DEN, int LYZ, int N = 0, bool DIAG = false>
 __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
   using XF = XFields<LES, DEN>;
   constexpr int PIN = XF::PIN, POUT = XF::POUT;
@@ -572,6 +576,7 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         les_model_tau<T>(I, xx, xy, xz, yy, yz, wx, wy, wz, o + 4, nut);
       }
     }
+    T lx = T(0), ly = T(0), lz = T(0);   // the fourth field's LES flux
     if (DEN) {
       constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
       const T rho = f[fr];
@@ -581,7 +586,7 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         // then realspacecalculation! adds it to -rho u (models.jl:265-268)
         constexpr int fg = fr + 1;
         const T gx = f[fg], gy = f[fg + 1], gz = f[fg + 2];
-        T lx = nut * gx, ly = nut * gy, lz = nut * gz;
+        lx = nut * gx; ly = nut * gy; lz = nut * gz;
         if (I.rho_les == 2) {
           const T cr = T(I.rho_les_c);
           lx += cr * (wy * gz - wz * gy); ly += cr * (wz * gx - wx * gz); lz += cr * (wx * gy - wy * gx);
@@ -589,6 +594,18 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         o[of] = -rho * ux + lx; o[of + 1] = -rho * uy + ly; o[of + 2] = -rho * uz + lz;
       } else {
         o[of] = -rho * ux; o[of + 1] = -rho * uy; o[of + 2] = -rho * uz;   // models.jl:266
+      }
+    }
+    if constexpr (DIAG && LES) {
+      const long long npl = (long long)n * I.ny * I.nz, pi = (long long)(g0 + q) * n + j;
+#pragma unroll
+      for (int c = 0; c < 5; ++c) I.obuf[c * npl + pi] = (double)o[4 + c];
+      int pl = 5;
+      if (I.dyn) I.obuf[(pl++) * npl + pi] = I.dyn_c[pi];
+      if (I.dynp) I.obuf[(pl++) * npl + pi] = I.dyn_c[npl + pi];
+      if (DEN == 2 && !I.scalar) {
+        I.obuf[pl * npl + pi] = (double)lx; I.obuf[(pl + 1) * npl + pi] = (double)ly;
+        I.obuf[(pl + 2) * npl + pi] = (double)lz;
       }
     }
 #pragma unroll
@@ -632,6 +649,10 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
 template <typename T, bool LES, int DEN, int LYZ>
 __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {
   b_x_pass<T, LES, DEN, LYZ>(I, Blk::here());
+}
+template <typename T, int DEN, int LYZ>
+__global__ void __launch_bounds__(FFS_MAXT) k_x_pass_diag(Inst<T> I) {
+  b_x_pass<T, true, DEN, LYZ, 0, true>(I, Blk::here());
 }
 
 // The spectral barrier (hyperviscosity_types.jl:32-48): log(esp(|k|, i, p, 1/4)) with
@@ -852,7 +873,8 @@ __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
   const bool nl = kind == FFS_PF_NRF || kind == FFS_PF_CNRF;
   const long long cs = I.cstride;
   const int plane = I.NYR * I.KXP;
-  double* R2 = Nm1 + nsh;          // aForcing, per plane mode
+  double* EfS = Nm1 + nsh;         // Ef of the last forcing call (the Eh.N files)
+  double* R2 = EfS + nsh;          // aForcing, per plane mode
   double* Em2 = R2 + plane;
   double* fac2 = Em2 + plane;
   const double* Zf2 = fac2 + plane;
@@ -903,6 +925,8 @@ __global__ void __launch_bounds__(256) k_plane_forcing(Inst<T> I, int mode) {
     }
     return;
   }
+  if (!af)
+    for (int n = threadIdx.x; n < nsh; n += blockDim.x) EfS[n] = Ef[n];
   const double dt = S->dt;
   const long long it = S->iteration;
   const double kf = I.pf_kf, alpha = I.pf_alpha;

@@ -328,6 +328,38 @@ function writeoutput(e::Engine)
     e.p.passive_scalar == 1 && write("scalar.$i", f[4])   # output.jl: scalar.N
 end
 
+# writeoutput's LES fields (output.jl:22-42), captured by the calculate_rhs! of iteration it
+const OUTPUT_FIELDS = ("T11", "T12", "T13", "T22", "T23", "cs", "cp", "dflux1", "dflux2", "dflux3")
+capture_output!(e::Engine) = check(e, ccall((:ffs_capture_output, LIB), Cint, (Ptr{Cvoid}, Cint), e.h, 1))
+function write_les_output(e::Engine, it::Integer)
+    p = e.p
+    a = Array{Float64}(undef, p.nx, p.ny, p.nz)
+    got = Ref{Int64}(-1)
+    for (k, name) in enumerate(OUTPUT_FIELDS)
+        rc = ccall((:ffs_output_field, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Ref{Int64}), e.h, k - 1, a, got)
+        rc == -1 && continue   # not a field of this configuration
+        check(e, rc)
+        got[] == it || error("LES output capture holds iteration $(got[]), expected $it")
+        write("$name.$it", a)
+    end
+end
+
+# the kz = 0 forcing arrays of writeoutput (output.jl:45-67), by kind
+function forcing_state(e::Engine)
+    k = e.p.plane_forcing
+    if k == 6   # aForcing: R per mode, an (nx/2+1) x ny matrix
+        nxh = e.p.nx ÷ 2 + 1
+        R = zeros(nxh * e.p.ny)
+        check(e, ccall((:ffs_forcing_array, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint), e.h, 5, R, length(R), 0))
+        return Dict("R" => reshape(R, nxh, e.p.ny))
+    end
+    k in (1, 2, 4, 5) || return Dict{String,Any}()
+    st = Dict{String,Any}("R" => forcingarray(e, 0), "Eh" => collect(zip(forcingarray(e, 2), forcingarray(e, 4))))
+    k in (4, 5) && (st["N"] = forcingarray(e, 3))
+    return st
+end
+write_forcing_output(st, it) = foreach(((name, a),) -> writedlm("$name.$it", a), st)
+
 # run_simulation() of src/FluidFlowSimulation.jl:23-65
 function run_simulation()
     d = readglobal()
@@ -361,6 +393,11 @@ function run_simulation()
         end
         isfile("R.$s") && forcingarray!(e, 0, vec(readdlm("R.$s", Float64)))
     end
+    if p.plane_forcing == 6 && isfile("R.$s")   # initialize!(f::AForcing) (forcing_types.jl:108-113)
+        R = vec(readdlm("R.$s", Float64))
+        check(e, ccall((:ffs_forcing_array, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Float64}, Cint, Cint), e.h, 5, R, length(R), 1))
+    end
+    p.les == 1 && capture_output!(e)
     total = haskey(d, :nt) ? parse(Int, d[:nt]) : typemax(Int) - s
     lengthtime = haskey(d, :timeDuration) ? parse(Float64, d[:timeDuration]) : Inf   # FluidFlowSimulation.jl:26
     final = s + total
@@ -385,22 +422,34 @@ function run_simulation()
         writespectra(e)
     end
     # the loop of FluidFlowSimulation.jl:42-44; a time-limited run checks the clock every step
+    steps = 0
+    pending = -1   # the output iteration whose LES fields the next step captures
     while iteration(e) < final && simtime(e) < finaltime
         it = iteration(e)
         nxt = isfinite(lengthtime) ? it + 1 : min(final, (it ÷ p.write_time + 1) * p.write_time)
         advance_in_time!(e, nxt - it)
+        steps += nxt - it
         flush()
+        pending >= 0 && (write_les_output(e, pending); pending = -1)
         # the reference writes u.N from calculate_rhs! when the next step starts at N
-        (iteration(e) % p.write_time == 0 && iteration(e) < final && simtime(e) < finaltime) && writeoutput(e)
+        if iteration(e) % p.write_time == 0 && iteration(e) < final && simtime(e) < finaltime
+            writeoutput(e)
+            write_forcing_output(forcing_state(e), iteration(e))
+            p.les == 1 && (pending = iteration(e))
+        end
     end
-    # the tail (FluidFlowSimulation.jl:46-58): a Stats row at the final iteration, and the
-    # final fields (written by the tail's calculate_rhs! when the iteration is a multiple
-    # of writeTime, else by the explicit writeoutput)
+    # the tail (FluidFlowSimulation.jl:46-58): a Stats row at the final iteration; the final
+    # files come from the tail's calculate_rhs! when the iteration is a multiple of
+    # writeTime (before the tail's forcing), else from the explicit writeoutput after it
+    in_rhs = iteration(e) % p.write_time == 0 && steps > 0
+    pre = in_rhs ? forcing_state(e) : nothing
     finalize!(e)
     flush()
     writeoutput(e)
+    write_forcing_output(in_rhs ? pre : forcing_state(e), iteration(e))
+    p.les == 1 && write_les_output(e, iteration(e))
     if p.plane_forcing == 1   # writedlm("R.$(iteration)", R) (FluidFlowSimulation.jl:60-62)
-        open(f -> foreach(v -> println(f, v), forcingarray(e, 0)), "R.$(iteration(e))", "w")
+        writedlm("R.$(iteration(e))", forcingarray(e, 0))
     end
     return e
 end

@@ -9,7 +9,7 @@ formats.
 from __future__ import annotations
 
 import ctypes
-from ctypes import byref, c_double, c_int32, c_void_p
+from ctypes import byref, c_double, c_int32, c_int64, c_void_p
 from pathlib import Path
 
 import numpy as np
@@ -121,13 +121,44 @@ class Simulation:
 
     def forcing_array(self, which: str, values=None) -> np.ndarray:
         """Per-shell state of the kz = 0 plane forcing: "R" (the ODE state of the R.N files),
-        "Em" (target spectrum), "avgK" (mean wavenumber, read only) or "N" (nRf/cNRf: the
-        plane's non-linear transfer, the N.N files). With values, set it."""
-        w = {"R": 0, "Em": 1, "avgK": 2, "N": 3}[which]
+        "Em" (target spectrum), "avgK" (mean wavenumber, read only), "N" (nRf/cNRf: the
+        plane's non-linear transfer, the N.N files) or "Ef" (the shell energy of the last
+        forcing call, read only, the Eh.N files). aForcing: "R" is its (nx/2+1) x ny mode
+        matrix. With values, set it."""
+        if self.params.plane_forcing == 6:   # aForcing: R per mode
+            if which != "R":
+                raise ValueError("aForcing keeps only R (per mode)")
+            nxh = self.nx // 2 + 1
+            a = (np.zeros(nxh * self.ny) if values is None
+                 else np.ascontiguousarray(np.asarray(values, dtype=np.float64).reshape(self.ny, nxh)).reshape(-1))
+            self._check(self._L.ffs_forcing_array(self._h, 5, a.ctypes.data_as(_D), a.size,
+                                                  0 if values is None else 1))
+            return a.reshape(self.ny, nxh).T.copy()   # the reference's R[i, j]: kx rows, y columns
+        w = {"R": 0, "Em": 1, "avgK": 2, "N": 3, "Ef": 4}[which]
         n = self.forcing_shells
         a = np.zeros(n) if values is None else np.ascontiguousarray(values, dtype=np.float64)
         self._check(self._L.ffs_forcing_array(self._h, w, a.ctypes.data_as(_D), n, 0 if values is None else 1))
         return a
+
+    OUTPUT_FIELDS = ("T11", "T12", "T13", "T22", "T23", "cs", "cp", "dflux1", "dflux2", "dflux3")
+
+    def capture_output(self, on: bool = True) -> None:
+        """Capture writeoutput's LES fields (T11..T23, cs, cp, dflux1..3; src/output.jl:22-42)
+        at every output step and at the run's tail."""
+        self._check(self._L.ffs_capture_output(self._h, 1 if on else 0))
+
+    def output_fields(self) -> tuple[int, dict]:
+        """The fields of the most recent capture that this configuration has, by the
+        reference's file stem, and the iteration they belong to."""
+        out, it = {}, c_int64(-1)
+        for i, name in enumerate(self.OUTPUT_FIELDS):
+            a = np.empty((self.nz, self.ny, self.nx))
+            rc = self._L.ffs_output_field(self._h, i, a.ctypes.data_as(_D), ctypes.byref(it))
+            if rc == -1:     # FFS_EINVAL: not a field of this configuration
+                continue
+            self._check(rc)
+            out[name] = a
+        return it.value, out
 
     def fields(self, layout: int = 0):
         shape = (self.nz, self.ny, self.nx if layout == 0 else 2 * (self.nx // 2 + 1))
@@ -325,6 +356,11 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         (folder / "Scales.txt").write_text(_scales.scales_header(bool(p.density)) + "\n")
         (folder / "Numbers.txt").write_text(_scales.numbers_header(bool(p.density)) + "\n")
     sim.initialize()
+    if sim.params.les:
+        sim.capture_output(True)    # T11..T23, cs, cp, dflux of each output step
+    if p.plane_forcing == 6 and (folder / f"R.{start}").exists():   # initialize!(f::AForcing), forcing_types.jl:108-113
+        rm = np.loadtxt(folder / f"R.{start}", ndmin=2)
+        sim.forcing_array("R", rm.reshape(p.nx // 2 + 1, p.ny).T)
     if sim.forcing_shells:
         # initialize!(f::RfForcing) (forcing_types.jl:66-73): the target spectrum from
         # targSpectrum.dat when present (calculate_Em!, linear interpolation at avgK), else
@@ -365,27 +401,41 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
         for rec in sim.spectra():
             write_spectrum_files(folder, rec, KH, KRZ, rhos)
 
+    steps = 0
+    les_pending = None   # the output iteration whose LES fields the next step captures
     while sim.iteration < final_step and sim.time < final_time:     # FluidFlowSimulation.jl:42-44
         it = sim.iteration
         nxt = min(final_step, (it // wt + 1) * wt)
         if lengthtime != float("inf"):
             nxt = it + 1       # time-limited runs check the clock every step
         sim.advance_in_time(nxt - it)
+        steps += nxt - it
         flush()
+        if les_pending is not None:
+            _write_les_output(folder, sim, les_pending)
+            les_pending = None
         # the reference writes u.N from calculate_rhs! when the step from N starts
-        # (is_output_time, simulationtypes.jl:102, models.jl:158)
+        # (is_output_time, simulationtypes.jl:102, models.jl:158); the LES fields of that
+        # calculate_rhs! are captured by the step and written after it
         if sim.iteration % wt == 0 and sim.iteration < final_step and sim.time < final_time:
             _write_output(folder, sim)
+            _write_forcing_output(folder, sim, sim.iteration, _forcing_state(sim))
+            if sim.params.les:
+                les_pending = sim.iteration
     # the tail (FluidFlowSimulation.jl:46-58): calculate_rhs!, forcing and a Stats row at the
-    # final iteration; the final fields are written either way (by the tail's calculate_rhs!
-    # when the iteration is a multiple of writeTime, else by the explicit writeoutput)
+    # final iteration. The final files come from the tail's calculate_rhs! when the iteration
+    # is a multiple of writeTime (before the tail's forcing), else from the explicit
+    # writeoutput after it.
+    in_rhs = sim.iteration % wt == 0 and steps > 0
+    pre = _forcing_state(sim) if in_rhs else None
     sim.finalize()
     flush()
     _write_output(folder, sim)
+    _write_forcing_output(folder, sim, sim.iteration, pre if in_rhs else _forcing_state(sim))
+    if sim.params.les:
+        _write_les_output(folder, sim, sim.iteration)
     if p.plane_forcing == 1:   # writedlm("R.$(iteration)", R) for rfForcing (FluidFlowSimulation.jl:60-62)
-        with open(folder / f"R.{sim.iteration}", "w") as f:
-            for v in sim.forcing_array("R"):
-                f.write(julia_float(float(v)) + "\n")
+        _write_dlm(folder / f"R.{sim.iteration}", sim.forcing_array("R"))
     return sim
 
 
@@ -397,3 +447,41 @@ def _write_output(folder: Path, sim: Simulation) -> None:
         _fields.write_field(folder / f"u{k + 1}.{i}", f[k])
     if sim.has_density:
         _fields.write_field(folder / f"{sim.scalar_name}.{i}", f[3])
+
+
+def _write_dlm(path: Path, rows) -> None:
+    """``writedlm`` with its default tab delimiter: one line per value of a vector, per
+    tuple of an iterator of tuples, per row of a matrix; values printed as Julia prints them."""
+    a = np.asarray(rows, dtype=np.float64)
+    with open(path, "w") as f:
+        for r in (a if a.ndim == 2 else a[:, None]):
+            f.write("\t".join(julia_float(float(v)) for v in r) + "\n")
+
+
+def _forcing_state(sim: Simulation) -> dict:
+    """The kz = 0 forcing arrays writeoutput writes (output.jl:45-67): R, and Eh = (avgK, Ef)
+    and N by kind."""
+    kind = int(sim.params.plane_forcing)
+    if kind == 6:                                       # aForcing: R (per mode)
+        return {"R": sim.forcing_array("R")}
+    if kind in (1, 2, 4, 5):                            # rf, cRf, nRf, cNRf
+        st = {"R": sim.forcing_array("R"), "Eh": np.stack([sim.forcing_array("avgK"), sim.forcing_array("Ef")], 1)}
+        if kind in (4, 5):
+            st["N"] = sim.forcing_array("N")
+        return st
+    return {}
+
+
+def _write_forcing_output(folder: Path, sim: Simulation, it: int, state: dict) -> None:
+    for name, a in state.items():
+        _write_dlm(folder / f"{name}.{it}", a)
+
+
+def _write_les_output(folder: Path, sim: Simulation, it: int) -> None:
+    """writeoutput's LES fields (output.jl:22-42): T11..T23, cs (cp) and dflux1..3, captured
+    by the calculate_rhs! of iteration it."""
+    got, fields = sim.output_fields()
+    if got != it:
+        raise RuntimeError(f"LES output capture holds iteration {got}, expected {it}")
+    for name, a in fields.items():
+        _fields.write_field(folder / f"{name}.{it}", a)

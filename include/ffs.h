@@ -191,10 +191,38 @@ int ffs_finalize(ffs_handle* h);
  * FluidFlowSimulation.jl:60-62); 1 = Em, the target spectrum (from the initial field at
  * ffs_initialize, or set from targSpectrum.dat after it, forcing_types.jl:76-83);
  * 2 = the shells' mean wavenumber avgK (read only); 3 = N, the plane's non-linear transfer
- * spectrum of nRfForcing/cNRfForcing (the N.N files, forcing_types.jl:114-116). n must
- * equal the shell count. aForcing keeps its state per mode and has no shells here. */
+ * spectrum of nRfForcing/cNRfForcing (the N.N files, forcing_types.jl:114-116); 4 = Ef, the
+ * shell energy of the last forcing call (read only; the Eh.N files, output.jl:45-67). n must
+ * equal the shell count. aForcing keeps its state per mode and has no shells: which 5 moves
+ * its R as the reference's (nx/2+1) x ny matrix in Julia's vec order (kx fastest), n =
+ * (nx/2+1)*ny (forcing_types.jl:87-118; its R.N files). */
 int ffs_forcing_shells(const ffs_handle* h);
 int ffs_forcing_array(ffs_handle* h, int32_t which, double* v, int32_t n, int32_t set);
+
+/* The LES fields of writeoutput (src/output.jl:22-42): the stress T11 T12 T13 T22 T23, the
+ * dynamic models' coefficient cs (and cp with the dynamic P tensor), and with the density's
+ * LES the flux dflux1..3 (its LES part, nu_t grad rho (+ the vorticity term)). They exist
+ * only during a step's calculate_rhs!, so they are captured there: after
+ * ffs_capture_output(h, 1) every step that starts at a multiple of write_time, except the
+ * first after ffs_initialize (is_output_time, src/simulationtypes.jl:102), and the
+ * run's tail (ffs_finalize) store them into a device buffer of nx*ny*nz doubles per field
+ * (allocated by this call; a no-op without an LES model). ffs_output_field copies one
+ * field of the most recent capture ([z][y][x], x fastest) and its iteration; FFS_EINVAL
+ * for a field this configuration does not have, FFS_ESTATE before the first capture.
+ * Capture steps run the generic x pass (not the FP32 register-fused one), so an FP32
+ * run with capture differs from one without at FP32 rounding; FP64 runs do not. */
+#define FFS_OUT_T11 0
+#define FFS_OUT_T12 1
+#define FFS_OUT_T13 2
+#define FFS_OUT_T22 3
+#define FFS_OUT_T23 4
+#define FFS_OUT_CS 5
+#define FFS_OUT_CP 6
+#define FFS_OUT_DFLUX1 7
+#define FFS_OUT_DFLUX2 8
+#define FFS_OUT_DFLUX3 9
+int ffs_capture_output(ffs_handle* h, int32_t on);
+int ffs_output_field(ffs_handle* h, int32_t field, double* out, int64_t* iteration);
 
 /* Physical fields at the current iteration (real!(s.u), src/output.jl:1-8). */
 int ffs_get_fields(ffs_handle* h, double* u1, double* u2, double* u3, double* rho, int32_t layout);

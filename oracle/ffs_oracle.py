@@ -583,6 +583,7 @@ class PlaneForcing:
             else:
                 self.Zf = (self.kh <= kf).astype(np.float64)
             self.R = np.zeros(self.nsh)
+            self.Ef = np.zeros(self.nsh)      # the shell energy of the last call (Eh.N files)
             self.Em = np.zeros(self.nsh)
             self.factor = np.zeros(self.nsh)
             self.N = np.zeros(self.nsh)
@@ -675,6 +676,7 @@ class PlaneForcing:
             else:                                              # cNRfForcing: ts = Tf, omega = 2 pi / (Tf ts)
                 omega = 2 * math.pi / (p.pf_tf * p.pf_tf)
             Ef = self.plane_spectrum(u, False)
+            self.Ef = Ef
             alpha = p.pf_alpha
             eps = np.finfo(np.float64).eps
             nl = kind in ("nRfForcing", "cNRfForcing")
@@ -1091,6 +1093,15 @@ class OracleSimulation:
                     lf = lf + cr * np.stack([wr[1] * gr[2] - wr[2] * gr[1], wr[2] * gr[0] - wr[0] * gr[2],
                                              wr[0] * gr[1] - wr[1] * gr[0]])
                 flux = flux + lf
+        if p.les:
+            # writeoutput's LES fields of this calculate_rhs! (output.jl:22-42)
+            self.les_out = {n: taur[i] for i, n in enumerate(("T11", "T12", "T13", "T22", "T23"))}
+            if p.les_model in ("dynamicSmagorinsky", "piomelliSmagorinsky"):
+                self.les_out["cs"] = self.dyn_c
+                if p.les_dynp:
+                    self.les_out["cp"] = self.dyn_cp
+            if p.density and p.rho_les:
+                self.les_out.update(dflux1=lf[0], dflux2=lf[1], dflux3=lf[2])
         if p.variable_dt:                                         # find_max, utils.jl:247-258
             m = float(np.max(np.abs(ur)))
             self.slot_u = max(m, self.slot_u) if p.reference_cfl_slot else m
@@ -1279,6 +1290,7 @@ class OracleSimulation:
             cpf = full_filter(np.maximum(-1.0, np.minimum(1.0, cpv)))   # average_c! of cp
             if dynp == "piomelliSandP":
                 self.piom_cp = cpf
+        self.dyn_c, self.dyn_cp = cf, cpf
         nut = np.maximum(p.les_cmin, np.minimum(0.4, cf)) * d2 * nrm5(Sr)
         tau = 2.0 * nut[None] * Sr
         if p.sandp_cb:                # SandP: tau += cb D^2 Lie(S, W) (les_real_calc.jl:98-104)

@@ -19,24 +19,51 @@ from oracle.ffs_oracle import OracleSimulation, Params, stats_header
 pytestmark = pytest.mark.gpu
 
 
+def forcing_files(s):
+    """writeoutput's kz = 0 forcing arrays (output.jl:45-67) of the oracle's forcing now."""
+    f, kind = s.pforce, s.p.plane_forcing
+    if kind == "aForcing":
+        return {"R": f.R2.T.copy()}                     # the reference's R[kx, y]
+    if kind in ("rfForcing", "cRfForcing", "nRfForcing", "cNRfForcing"):
+        out = {"R": f.R.copy(), "Eh": np.stack([f.kh, f.Ef], 1)}
+        if kind in ("nRfForcing", "cNRfForcing"):
+            out["N"] = f.N.copy()
+        return out
+    return {}
+
+
 def oracle_run(d, u):
-    """FluidFlowSimulation.jl:23-65 on the oracle; returns its rows, spectra and outputs."""
+    """FluidFlowSimulation.jl:23-65 on the oracle; returns its rows, spectra and outputs:
+    the u fields, the LES fields captured by the calculate_rhs! at each output iteration
+    (T11..T23, cs, cp, dflux) and the forcing files."""
     s = OracleSimulation(Params.from_global(d), u)
     total = int(d["nt"]) if "nt" in d else (1 << 62)
     lengthtime = float(d["timeDuration"]) if "timeDuration" in d else math.inf
     wt = int(d["writeTime"])
     s.initialize()
     final, finaltime = s.iteration + total, s.time + lengthtime
-    outputs = {}
+    outputs, les, forcing = {}, {}, {}
     calls = 0                                    # the integrator's call count
     while s.iteration < final and s.time < finaltime:
-        if calls != 0 and s.iteration % wt == 0:
-            outputs[s.iteration] = s.u_physical()
+        out_step = calls != 0 and s.iteration % wt == 0
+        it = s.iteration
+        if out_step:
+            outputs[it] = s.u_physical()
+            forcing[it] = forcing_files(s)
         s.advance()
+        if out_step and s.p.les:
+            les[it] = dict(s.les_out)
         calls += 1
+    in_rhs = calls != 0 and s.iteration % wt == 0
+    pre = forcing_files(s)
     s.finalize()                                 # calculate_rhs!, forcing, writestats
     outputs[s.iteration] = s.u_physical()        # tail calculate_rhs! or the explicit writeoutput
-    return s, outputs
+    forcing[s.iteration] = pre if in_rhs else forcing_files(s)
+    if s.p.plane_forcing == "rfForcing":         # FluidFlowSimulation.jl:60-62 rewrites R.N last
+        forcing[s.iteration]["R"] = s.pforce.R.copy()
+    if s.p.les:
+        les[s.iteration] = dict(s.les_out)
+    return s, outputs, les, forcing
 
 
 def read_rows(path):
@@ -68,6 +95,21 @@ CASES = {
     # specFil: Stats_fil.txt and the *_fil spectrum files (stats.jl:14-18, 48-52; spec.jl:13-142)
     "etd-specfil-hv": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "8",
                        "hyperViscosity": "true", "hyperViscosityCoefficient": "1e-5", "specFil": "2"},
+    # writeoutput's LES fields (output.jl:22-42): T11..T23, cs, cp and the density's dflux at
+    # 5 and 10 (in-loop) and at the tail's 12 (the explicit writeoutput)
+    "etd-dynamicsandp-density-les": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01",
+                                     "nt": "12", "lesModel": "dynamicSandP", "sLesModel": "dynamicSmagorinsky",
+                                     "densityStratification": "true", "Pr": "1", "densityGradient": "1",
+                                     "zAcceleration": "1", "referenceDensity": "1",
+                                     "densityLesModel": "vorticityDiffusion"},
+    # a run that ends at a multiple of writeTime: the tail's calculate_rhs! writes the final
+    # files before the tail's forcing (R, Eh and N of nRfForcing at 5, 10)
+    "ab3-nrf-forcing-smagorinsky": {"velocityTimeStep": "Adams_Bashforth3rdO", "variableTimestepFlag": "false",
+                                    "dt": "0.01", "nt": "10", "forcing": "nRfForcing", "TF": "2.0",
+                                    "alphac": "1.0", "kf": "3.0", "lesModel": "Smagorinsky"},
+    # aForcing's R.N is its (nx/2+1) x ny mode matrix
+    "etd-a-forcing": {"velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "nt": "11",
+                      "forcing": "aForcing", "TF": "2.0", "alphac": "1.0", "kf": "3.0"},
 }
 
 
@@ -82,7 +124,7 @@ def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
     for i in range(3):
         gpu_pkg.write_field(tmp_path / f"u{i + 1}.0", u[i])
     sim = gpu_pkg.run_simulation(tmp_path, precision="FP64")
-    ref, outputs = oracle_run(d, u)
+    ref, outputs, les, forcing = oracle_run(d, u)
     assert sim.iteration == ref.iteration
     sim.close()
     p = Params.from_global(d)
@@ -109,9 +151,24 @@ def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
             assert got.shape == (len(want), 2)
             scale = max(np.abs(want).max(), 1e-300)
             assert np.allclose(got[:, 1], want, rtol=1e-10, atol=1e-12 * scale), f.name
-    if d.get("forcing") == "rfForcing":
-        R = np.loadtxt(tmp_path / f"R.{ref.iteration}")
-        assert np.allclose(R, ref.pforce.R, rtol=1e-10, atol=1e-14 * np.abs(ref.pforce.R).max())
+    # the kz = 0 forcing files of every output (R, Eh = avgK Ef, N; aForcing's R matrix)
+    written_f = sorted(f.name for f in tmp_path.glob("*.*") if f.name.split(".")[0] in ("R", "Eh", "N"))
+    assert written_f == sorted(f"{k}.{it}" for it, st in forcing.items() for k in st)
+    for it, st in forcing.items():
+        for k, want in st.items():
+            got = np.loadtxt(tmp_path / f"{k}.{it}", ndmin=2 if np.ndim(want) == 2 else 1)
+            assert got.shape == np.shape(want), (k, it)
+            assert np.allclose(got, want, rtol=1e-10, atol=1e-14 * max(np.abs(want).max(), 1e-300)), (k, it)
+    # writeoutput's LES fields: raw Float64 n^3 per field and output iteration
+    names = ("T11", "T12", "T13", "T22", "T23", "cs", "cp", "dflux1", "dflux2", "dflux3")
+    written_l = sorted(f.name for f in tmp_path.glob("*.*") if f.name.split(".")[0] in names)
+    assert written_l == sorted(f"{k}.{it}" for it, st in les.items() for k in st)
+    for it, st in les.items():
+        for k, want in st.items():
+            f = tmp_path / f"{k}.{it}"
+            assert f.stat().st_size == 8 * n ** 3
+            got = gpu_pkg.read_field(f, n, n, n)
+            assert np.linalg.norm(got - want) <= 1e-10 * np.linalg.norm(want), (k, it)
     # field files: exactly the oracle's output iterations, raw Float64 n^3
     written = sorted(int(f.name.split(".")[1]) for f in tmp_path.glob("u1.*") if f.name != "u1.0")
     assert written == sorted(outputs)
