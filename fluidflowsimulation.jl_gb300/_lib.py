@@ -12,7 +12,7 @@ LIB_PATH = HERE / "libffs.so"
 FFS_OK = 0
 ERRORS = {-1: "FFS_EINVAL", -2: "FFS_ENOMEM", -3: "FFS_ECUDA", -4: "FFS_ENAN", -5: "FFS_ETIMEDOUT",
           -6: "FFS_EUNSUPPORTED", -7: "FFS_ESTATE", -8: "FFS_ECANCELED"}
-FFS_ETD3, FFS_AB3 = 0, 1
+FFS_ETD3, FFS_AB3, FFS_EULER = 0, 1, 2
 LES_MODELS = {"Smagorinsky": 0, "Vreman": 1, "productionViscosity": 2, "Silvis": 3, "stableNonLinear": 4,
               "dynamicSmagorinsky": 5, "piomelliSmagorinsky": 6}
 FFS_FP64, FFS_FP32 = 0, 1

@@ -219,7 +219,7 @@ class Engine : public EngineBase {
   // physics parameters (everything that does not change buffer sizes or the step's passes)
   void set_physics(const ffs_params& p) {
     I.nu = p.nu; I.cfl = p.cfl; I.dt0 = p.dt;
-    I.ab3 = p.integrator == FFS_AB3; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
+    I.ab3 = p.integrator != FFS_ETD3; I.euler = p.integrator == FFS_EULER; I.adaptive = p.variable_dt != 0; I.ref_slot = p.reference_cfl_slot != 0;
     I.hv = p.hyperviscosity != 0; I.hv_m = p.hv_m; I.hv_nu = p.hv_nu;
     {   // the spectral barrier's defaults (simulationtypes.jl:294-297, density_stratification_types.jl
         // :137-141): initk = cutoff 2 kx_max / 3, endk = sqrt(3 cutoff) kx_max, kx_max = (nx/2)/lx
@@ -309,11 +309,14 @@ class Engine : public EngineBase {
     if (!(p.lx > 0 && p.ly > 0 && p.lz > 0)) { err = "domain sizes must be positive"; return FFS_EINVAL; }
     if (!(p.cutoff > 0 && p.cutoff <= 1.0)) { err = "cutoff must be in (0, 1]"; return FFS_EINVAL; }
     if (p.dt_stat <= 0 || p.dt_spec <= 0) { err = "dtStat and dtSpec must be positive"; return FFS_EINVAL; }
-    if (p.integrator != FFS_ETD3 && p.integrator != FFS_AB3) { err = "unknown integrator"; return FFS_EINVAL; }
+    if (p.integrator != FFS_ETD3 && p.integrator != FFS_AB3 && p.integrator != FFS_EULER) {
+      err = "unknown integrator";
+      return FFS_EINVAL;
+    }
     if (!p.variable_dt && !(p.dt > 0)) { err = "fixed time stepping needs dt > 0"; return FFS_EINVAL; }
     if (p.hyperviscosity && p.hv_kind == 0 && (p.hv_m < 1 || p.hv_m > 8)) { err = "hyperViscosityM must be in 1..8"; return FFS_EINVAL; }
     if (p.hyperviscosity && (p.hv_kind < 0 || p.hv_kind > 1)) { err = "unknown hyperviscosity kind"; return FFS_EINVAL; }
-    if (p.hyperviscosity && p.hv_kind == 1 && p.integrator == FFS_AB3) {
+    if (p.hyperviscosity && p.hv_kind == 1 && p.integrator != FFS_ETD3) {
       // the reference's explicit viscous term needs an exponent M the barrier does not have
       err = "hyperViscosity spectralBarrier needs velocityTimeStep ETD3rdO";
       return FFS_EUNSUPPORTED;
@@ -330,6 +333,11 @@ class Engine : public EngineBase {
     }
     if (p.plane_forcing) {
       if (p.plane_forcing < FFS_PF_RF || p.plane_forcing > FFS_PF_A) { err = "unknown plane forcing"; return FFS_EINVAL; }
+      if (p.integrator == FFS_EULER && (p.plane_forcing == FFS_PF_NRF || p.plane_forcing == FFS_PF_CNRF)) {
+        // nrforcing.jl:37 reads the integrator's dt2, which Euller does not keep
+        err = "nRfForcing / cNRfForcing need an integrator with a dt history (ETD3rdO or Adams_Bashforth3rdO)";
+        return FFS_EUNSUPPORTED;
+      }
       if (p.forcing) { err = "isotropicBand and kz = 0 plane forcing together are not supported"; return FFS_EINVAL; }
       if (p.nz < 16) { err = "kz = 0 plane forcing needs nz >= 16 (it forces kz = +-1..+-5)"; return FFS_EUNSUPPORTED; }
       if (p.plane_forcing != FFS_PF_QF && !(p.pf_tf > 0)) { err = "TF must be positive"; return FFS_EINVAL; }
@@ -1807,7 +1815,7 @@ class Engine : public EngineBase {
     t += 8 * (int64_t)std::min<int64_t>((cs + 4095) / 4096, 8192) * QPAD;
     t += 8 * (int64_t)(p.stats_capacity > 0 ? p.stats_capacity : 256) * 64;   // record columns <= 53
     t += 8 * (int64_t)(p.spec_capacity > 0 ? p.spec_capacity : 16) * 4 * (std::max(p.nx, std::max(p.ny, p.nz)) / 2 + 1);
-    if (p.integrator != FFS_AB3) t += 2 * (int64_t)sizeof(T) * 4 * cs;
+    if (p.integrator == FFS_ETD3) t += 2 * (int64_t)sizeof(T) * 4 * cs;
     t += 16 * (int64_t)p.nx * p.ny * p.nz;   // FP64 staging of two physical fields
     return t + 4096;
   }

@@ -129,7 +129,8 @@ template <typename T> struct Inst {
   int qmax;
   // physics
   double nu, cfl, dt0;
-  int ab3, adaptive, ref_slot;
+  int ab3, adaptive, ref_slot;   // ab3: an explicit integrator (AB3 or Euler)
+  int euler;               // Euller: u += dt rhs, dt as set_dt! gives it
   int hv, hv_m;
   double hv_nu;
   int hv_kind;             // 0 nuh k^2M, 1 the spectral barrier (hv_initk, hv_endk)

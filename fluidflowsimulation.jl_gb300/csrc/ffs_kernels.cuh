@@ -728,7 +728,7 @@ __device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk b
         const double dt = S.dt;
         newdt = newdt < dt ? fmax(dd::D(dt, 1.25), newdt) : fmin(dd::M(1.25, dt), newdt);
       }
-      if (I.ab3) {
+      if (I.ab3 && !I.euler) {
         if (S.ts_iter == 0) { S.dt3 = S.dt2 = S.dt = dd::D(newdt, 2.0); }
         else { S.dt3 = S.dt2; S.dt2 = S.dt; S.dt = newdt; }
       } else {
@@ -747,7 +747,9 @@ __device__ __forceinline__ void b_scalar(const Inst<T>& I, int mode, const Blk b
       S.stage = i >= 3 ? 3 : (int)i;
       // with a fixed dt the stage-3 coefficients never change once computed
       S.skip_table = (!I.adaptive && prev_stage == 3 && S.stage == 3) ? 1 : 0;
-      if (I.ab3) {
+      if (I.euler) {   // muladd(dt, rhs, u) (Euller.jl:14-25)
+        S.At = S.dt; S.Bt = 0.0; S.Ct = 0.0;
+      } else if (I.ab3) {
         const double dt = S.dt, dt2 = S.dt2, dt3 = S.dt3;
         if (I.adaptive) {
           S.At = (1. + (dt * (2 * dt + 6 * dt2 + 3 * dt3)) / (6 * dt2 * (dt2 + dt3))) * dt;
@@ -1309,7 +1311,7 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
     cplx<T> un[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      if (I.ab3 && stage == 2) f2[c] = scl(rhs[c] - f1[c], fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
+      if (I.ab3 && !I.euler && stage == 2) f2[c] = scl(rhs[c] - f1[c], fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
       // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
       un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
       if (band) un[c] = un[c] + scl(u[c], fdt);   // forcing increment (add_forcing!)
@@ -1341,7 +1343,7 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
       const cplx<T> r1 = hA[3 * cs + g];
       cplx<T> r2 = hB[3 * cs + g];
       if (I.ab3) {
-        if (stage == 2) r2 = scl(rrhs - r1, fix2) + rrhs;
+        if (stage == 2 && !I.euler) r2 = scl(rrhs - r1, fix2) + rrhs;
         E = T(1); A = At; B = Bt; C = Ct;
       } else {
         const T* e = I.etab_rho + 4 * te;

@@ -12,7 +12,7 @@ import math
 import re
 from pathlib import Path
 
-from ._lib import FFS_AB3, FFS_ETD3, FFS_FP32, FFS_FP64, LES_MODELS, FFSParams, load
+from ._lib import FFS_AB3, FFS_ETD3, FFS_EULER, FFS_FP32, FFS_FP64, LES_MODELS, FFSParams, load
 
 
 def readglobal(path: str | Path = "global") -> dict[str, str]:
@@ -119,10 +119,12 @@ def parameters(d: dict[str, str], precision: str | None = None, device: int = 0)
     integ = d.get("velocityTimeStep", "ETD3rdO")
     if integ == "Adams_Bashforth3rdO":
         p.integrator = FFS_AB3
+    elif integ == "Euller":           # simulationtypes.jl:312-313, Euller.jl
+        p.integrator = FFS_EULER
     elif integ == "ETD3rdO":
         p.integrator = FFS_ETD3
     else:
-        raise ValueError(f"velocityTimeStep {integ!r} is not supported (ETD3rdO, Adams_Bashforth3rdO)")
+        raise ValueError(f"velocityTimeStep {integ!r} is not supported (ETD3rdO, Adams_Bashforth3rdO, Euller)")
     p.variable_dt = 1 if _bool(d.get("variableTimestepFlag", "true")) else 0
     p.cfl = float(d.get("cfl", "0.18"))
     p.dt = parse_number(d["dt"]) if "dt" in d else 0.0

@@ -82,7 +82,7 @@ function parameters(d)
     p.start_time = haskey(d, :startTime) ? parse(Float64, d[:startTime]) : 0.0
     p.dt_stat = parse(Int32, d[:dtStat]); p.dt_spec = parse(Int32, d[:dtSpec]); p.write_time = parse(Int32, d[:writeTime])
     p.spec_fil = haskey(d, :specFil) ? parse(Float64, d[:specFil]) : 0.0   # Globals.jl:173-178
-    p.integrator = get(d, :velocityTimeStep, "ETD3rdO") == "Adams_Bashforth3rdO" ? 1 : 0
+    p.integrator = Dict("ETD3rdO" => 0, "Adams_Bashforth3rdO" => 1, "Euller" => 2)[get(d, :velocityTimeStep, "ETD3rdO")]
     p.variable_dt = haskey(d, :variableTimestepFlag) ? Int32(parse(Bool, d[:variableTimestepFlag])) : 1
     p.cfl = haskey(d, :cfl) ? parse(Float64, d[:cfl]) : 0.18
     p.dt = haskey(d, :dt) ? num(d[:dt]) : 0.0

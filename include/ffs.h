@@ -38,6 +38,7 @@ extern "C" {
 
 #define FFS_ETD3 0 /* ETD3rdO (src/time_step_functions/ETD.jl) */
 #define FFS_AB3 1  /* Adams_Bashforth3rdO (src/time_step_functions/Adams_Bashforth.jl) */
+#define FFS_EULER 2 /* Euller (src/time_step_functions/Euller.jl): u += dt rhs, explicit viscosity */
 
 #define FFS_FP64 0
 #define FFS_FP32 1
@@ -51,7 +52,7 @@ typedef struct ffs_params {
   double lx, ly, lz;           /* xDomainSize.. in units of 2 pi: k = i / L */
   double nu;                   /* kinematicViscosity */
   double cutoff;               /* cutoff (dealias ratio), default 2/3 */
-  int32_t integrator;          /* velocityTimeStep: FFS_ETD3 | FFS_AB3 */
+  int32_t integrator;          /* velocityTimeStep: FFS_ETD3 | FFS_AB3 | FFS_EULER */
   int32_t variable_dt;         /* variableTimestepFlag (default 1) */
   double cfl;                  /* cfl, default 0.18 */
   double dt;                   /* dt (fixed dt, or the initial value) */

@@ -337,7 +337,10 @@ class Params:
 
     @property
     def ab3(self) -> bool:
-        return self.integrator == "Adams_Bashforth3rdO"
+        """An explicit integrator (Adams_Bashforth3rdO or Euller): the viscosity, the
+        hyperviscosity and the scalar's diffusion are terms of the right-hand side
+        (is_implicit, time_step_functions.jl:5-7; models.jl:296-326,356-361)."""
+        return self.integrator in ("Adams_Bashforth3rdO", "Euller")
 
 
 # ----------------------------------------------------------------------------------
@@ -393,6 +396,29 @@ class AB3:
         self.fm2 = self.fm1
         self.fm1 = rhs.copy()
         return unew
+
+
+class Euler:
+    """Euller (Euller.jl:1-25): u = dt rhs + u, dt as set_dt! gives it (no start-up
+    halving). The reference builds it as Euller{variableTimeStep,idt}, one type parameter
+    more than the struct declares (simulationtypes.jl:312-313), so this is the intended
+    integrator."""
+
+    def __init__(self, adaptive: bool, idt: float):
+        self.adaptive = adaptive
+        self.dt = self.dt2 = self.dt3 = idt
+        self.iteration = 0
+
+    def initialize(self, rhs, dt_now):
+        self.dt = dt_now
+
+    def set_dt(self, dt):
+        if self.adaptive:
+            self.dt = dt
+
+    def step(self, u, rhs, explicit=None):
+        self.iteration += 1
+        return self.dt * rhs + u
 
 
 class ETD3:
@@ -963,13 +989,17 @@ class OracleSimulation:
                 km = km * k2
             c = dd.fma(k2, np.full_like(k2, -p.nu), km * (-p.hv_nu))
         self.k2_ref = k2
-        if p.ab3:
+        if p.integrator == "Euller":
+            self.ts = Euler(p.variable_dt, p.dt)
+        elif p.ab3:
             self.ts = AB3(p.variable_dt, p.dt)
         else:
             self.ts = ETD3(p.variable_dt, p.dt, c)
         if p.fld:
             alpha = p.nu / (p.density_pr if p.density else p.scalar_pr)
-            if p.ab3:
+            if p.integrator == "Euller":
+                self.rts = Euler(p.variable_dt, p.dt)
+            elif p.ab3:
                 self.rts = AB3(p.variable_dt, p.dt)
             elif p.scalar and p.hv and p.hv_kind == "barrier":
                 self.rts = ETD3(p.variable_dt, p.dt, barrier_c(g, k2, -alpha, p.hv_initk, p.hv_endk))

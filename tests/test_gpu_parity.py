@@ -179,6 +179,13 @@ FIXED_CASES = {
     "ab3-adaptive-silvis-scalar-vort": gdict(32, adaptive=True, lesModel="Silvis", passiveScalar="true", scalarPr="1",
                                              scalarGradient="1", scalarLesModel="vorticityDiffusion",
                                              scalarVorticityCoefficient="0.5"),
+    # Euller (Euller.jl): u += dt rhs with the explicit viscosity, dt as set_dt! gives it
+    "euler-32": gdict(32, "Euller", dt="0.005"),
+    "euler-adaptive-les-density-eddy": gdict(32, "Euller", adaptive=True, lesModel="Smagorinsky",
+                                             densityStratification="true", Pr="1", densityGradient="1",
+                                             zAcceleration="1", referenceDensity="1", densityLesModel="eddyDiffusion"),
+    "euler-scalar-forced": gdict(32, "Euller", dt="0.005", passiveScalar="true", scalarPr="0.7", scalarGradient="1",
+                                 forcing="rfForcing", TF="2.0", alphac="1.0", kf="3.0"),
     # nz >= 128: the flux's z component comes from the density's slot on the one-component path
     "etd-nz128-les-density-vort": gdict(32, "ETD3rdO", nz=128, dt="0.005", lesModel="Smagorinsky",
                                         densityStratification="true", Pr="1", densityGradient="1", zAcceleration="1",
@@ -316,6 +323,11 @@ def test_errors_and_state_checks(gpu_pkg):
     prm.rho_les = 1
     with pytest.raises(gpu_pkg.FFSError) as e:
         gpu_pkg.Simulation(prm)
+    assert e.value.code == -6
+    # nRfForcing reads the integrator's dt2, which Euller does not keep (nrforcing.jl:37)
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        gpu_pkg.Simulation.from_global(dict(d, velocityTimeStep="Euller", forcing="nRfForcing", TF="2.0",
+                                            alphac="1.0", kf="3.0"))
     assert e.value.code == -6
     # a non-finite initial condition is reported, not propagated silently
     u, _ = make_ic(gpu_pkg, d)

@@ -214,6 +214,21 @@ def test_parameters_hyperviscosity_kinds(pkg):
     assert (p.rho_hv, p.rho_hv_endk) == (2, 20.0) and (o.rho_hv, o.rho_hv_endk) == ("barrier", 20.0)
 
 
+def test_parameters_integrators(pkg):
+    """velocityTimeStep (simulationtypes.jl:308-318): ETD3rdO (default), Adams_Bashforth3rdO,
+    Euller; the oracle's explicit flag covers both explicit integrators."""
+    from oracle.ffs_oracle import Params
+    base = {"nx": "16", "ny": "16", "nz": "16", "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+            "kinematicViscosity": "0.1", "dtStat": "1", "dtSpec": "1", "writeTime": "1"}
+    for name, code, explicit in (("ETD3rdO", 0, False), ("Adams_Bashforth3rdO", 1, True), ("Euller", 2, True)):
+        d = dict(base, velocityTimeStep=name)
+        assert pkg.parameters(d).integrator == code
+        assert Params.from_global(d).ab3 == explicit
+    assert pkg.parameters(base).integrator == 0
+    with pytest.raises(ValueError):
+        pkg.parameters(dict(base, velocityTimeStep="RK4"))
+
+
 def test_parameters_density_and_scalar_les(pkg):
     """densityLesModel (density_stratification_types.jl:176-185) and the passive scalar's LES
     diffusion under lesModel (simulationtypes.jl:334-346): eddy diffusion by default,
