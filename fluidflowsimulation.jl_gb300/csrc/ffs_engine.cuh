@@ -261,7 +261,7 @@ class Engine : public EngineBase {
     }
     I.Lx_t = (T)p.lx; I.Ly_t = (T)p.ly; I.Lz_t = (T)p.lz;
     I.iLx_t = (T)(1.0 / p.lx); I.iLy_t = (T)(1.0 / p.ly); I.iLz_t = (T)(1.0 / p.lz);
-    I.inv_n_t = (T)I.inv_n; I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
+    I.inv_n_t = (T)I.inv_n; I.inv_n2_t = (T)(0.5 * I.inv_n); I.nu_t = (T)p.nu; I.hvnu_t = (T)p.hv_nu; I.alpha_t = (T)I.alpha;
     I.gval_t = (T)p.gravity; I.dgrad_t = (T)p.density_gradient; I.kf2_t = (T)(p.forcing_kf * p.forcing_kf);
 
   }

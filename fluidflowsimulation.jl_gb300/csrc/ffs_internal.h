@@ -174,6 +174,7 @@ template <typename T> struct Inst {
   // the same constants in the arithmetic type (no per-element conversions)
   T Lx_t, Ly_t, Lz_t, iLx_t, iLy_t, iLz_t;
   T inv_n_t, nu_t, hvnu_t, alpha_t, gval_t, dgrad_t, kf2_t;
+  T inv_n2_t;              // 1/(2N): the step's forward z scale (the x pass leaves out its unpack 1/2)
   // field lists for the passes
   int nin;                 // inverse fields
   int in_code[12];

@@ -10,6 +10,7 @@
 //   wy   [slot][z][y][kx]         after the y pass (inverse) / before it (forward)
 // Physical space exists only in shared memory inside the x pass.
 #pragma once
+#include <type_traits>
 #include "ffs_ddmath.cuh"
 #include "ffs_internal.h"
 
@@ -296,6 +297,24 @@ __global__ void __launch_bounds__(FFS_MAXT) k_fwd_y(Inst<T> I, FieldList F) {
 // Real fields out: N(3) ke [tau(5) if LES] [flux(3) if DEN]
 // DEN: 0 no fourth field, 1 density / scalar, 2 with its LES diffusion (needs LES)
 // ====================================================================================
+// Running max of |x| (find_max, utils.jl:247-258). FP64: on the bit patterns, which order
+// non-negative doubles like their values, so the integer pipe does the work and the FP64
+// pipe (the bound of the FP64 passes) does none; FP32: fmaxf.
+template <typename T> struct AbsMax;
+template <> struct AbsMax<float> {
+  float v = 0.f;
+  __device__ __forceinline__ void add(float x) { v = fmaxf(v, fabsf(x)); }
+  __device__ __forceinline__ float get() const { return v; }
+};
+template <> struct AbsMax<double> {
+  unsigned long long b = 0ull;
+  __device__ __forceinline__ void add(double x) {
+    const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+    b = a > b ? a : b;
+  }
+  __device__ __forceinline__ double get() const { return __longlong_as_double((long long)b); }
+};
+
 // Block-wide max of |u_i| (and |rho|) in T, then one atomicMax per CTA on the state.
 // red: shared scratch of at least 32 T per quantity.
 template <typename T, bool DEN>
@@ -506,9 +525,12 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
   auto sti = [&](int l, int j, cplx<T> v) { ri[sidx(j, l, LSX)] = v; };
   fft_lines_n<+1, LIN, T, N, decltype(ldi), decltype(sti), LSX, XNT>(I.px, s0, s1, LSX, I.twx, ldi, sti);
 
-  // 3. physical space products: inputs from ri, outputs (first POUT pairs) into s1
-  T umaxt = T(0), rmaxt = T(0);
+  // 3. physical space products: inputs from ri, outputs (first POUT pairs) into s1; the
+  // loop twice, with and without the kinetic-energy field (stats / spectrum iterations only)
+  AbsMax<T> umaxt, rmaxt;
   const T les2 = T(2) * T(I.les_alpha);
+  auto products = [&](auto ke_c) {
+  constexpr bool KE = decltype(ke_c)::value;
   for (int e = threadIdx.x; e < n * LYZ; e += blockDim.x) {
     const int q = e % LYZ, j = e / LYZ;
     const cplx<T>* row = ri + sidx(j, q, LSX);
@@ -523,8 +545,8 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
     o[0] = uy * wz - uz * wy;             // (u x w), models.jl:260
     o[1] = uz * wx - ux * wz;
     o[2] = ux * wy - uy * wx;
-    o[3] = want_ke ? T(0.5) * (ux * ux + uy * uy + uz * uz) : T(0);   // models.jl:224
-    umaxt = fmax(umaxt, fmax(fabs(ux), fmax(fabs(uy), fabs(uz))));
+    if (KE) o[3] = T(0.5) * (ux * ux + uy * uy + uz * uz);   // models.jl:224
+    umaxt.add(ux); umaxt.add(uy); umaxt.add(uz);
     T nut = T(0);   // the model's eddy viscosity: the fourth field's eddy diffusivity
     if (LES) {
       const T xx = f[6], xy = f[7], xz = f[8], yy = f[9], yz = f[10];
@@ -580,7 +602,7 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
     if (DEN) {
       constexpr int fr = LES ? 11 : 6, of = LES ? 9 : 4;
       const T rho = f[fr];
-      rmaxt = fmax(rmaxt, fabs(rho));
+      rmaxt.add(rho);
       if (DEN == 2) {
         // calc_les! (les_real_calc.jl:116-134): nu_t grad rho (+ (c D^2 / 2) w x grad rho),
         // then realspacecalculation! adds it to -rho u (models.jl:265-268)
@@ -611,8 +633,11 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
 #pragma unroll
     for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
   }
+  };
+  if (want_ke) products(std::true_type{});
+  else products(std::false_type{});
   // block max -> one atomic per CTA (the max is exact in T; FP64 only for the atomic)
-  if (I.adaptive) block_max_to_state<T, (DEN != 0)>(I, umaxt, rmaxt, red);
+  if (I.adaptive) block_max_to_state<T, (DEN != 0)>(I, umaxt.get(), rmaxt.get(), red);
   __syncthreads();
 
   // 4. r2c of the output pairs, result back into sx
@@ -633,12 +658,14 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
       cplx<T>* da = I.wy + (long long)I.out_slot[wa ? oa : 0] * I.wys + (long long)(g0 + q) * KXP;
       cplx<T>* db = I.wy + (long long)I.out_slot[wb ? ob : 0] * I.wys + (long long)(g0 + q) * KXP;
       for (int k = lane; k < KXP; k += 32) {
+        // 2A = Z_k + conj Z_{n-k}, 2B = -i (Z_k - conj Z_{n-k}): the factor 1/2 is in the
+        // forward z pass's scale 1/(2N) (exact: a power of two through linear passes)
         cplx<T> A = mk(T(0), T(0)), B = mk(T(0), T(0));
         if (k < Mx) {
           const cplx<T> zk = rf[sidx(k, l, LSX)];
           const cplx<T> zm = rf[sidx(k == 0 ? 0 : n - k, l, LSX)];
-          A = mk(T(0.5) * (zk.x + zm.x), T(0.5) * (zk.y - zm.y));
-          B = mk(T(0.5) * (zk.y + zm.y), T(-0.5) * (zk.x - zm.x));
+          A = mk(zk.x + zm.x, zk.y - zm.y);
+          B = mk(zk.y + zm.y, zm.x - zk.x);
         }
         if (wa) da[k] = A;
         if (wb) db[k] = B;
@@ -1126,7 +1153,7 @@ __device__ __forceinline__ void b_fwd_z(const Inst<T>& I, const FieldList& F, in
   const long long cs = I.cstride;
   const T kyv = kval(ysig(I, jc), I.Ly_t, I.iLy_t);
   const T Lx = I.Lx_t, iLx = I.iLx_t, Lz = I.Lz_t, iLz = I.iLz_t;
-  const T sc = I.inv_n_t;
+  const T sc = I.inv_n2_t;   // 1/N and the 1/2 the x pass's Hermitian unpack leaves out
   cplx<T>* out = I.sbuf + (long long)jc * I.KXP + kx0;   // + kc * rowstride + l (+ slot * cs)
   const bool aux = I.les || I.density;
 

@@ -180,7 +180,7 @@ __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& 
   const int kx0 = bk.x * TX, jc = bk.y;
   const int rowstride = I.NYR * I.KXP;
   const long long cs = I.cstride;
-  const float2 sc = make_float2(I.inv_n_t, I.inv_n_t);
+  const float2 sc = make_float2(I.inv_n2_t, I.inv_n2_t);   // 1/N and the x pass's unpack 1/2
   cplx<T>* out = I.sbuf + (long long)jc * I.KXP + kx0;   // + c * cs + kc * rowstride + l
   const bool kzero_col = (kx0 == 0) && (ysig(I, jc) == 0);
   const bool aux = I.les || I.density;
@@ -242,9 +242,9 @@ __device__ __forceinline__ void b_fwd_z2(const Inst<float>& I, const FieldList& 
       const long long o = (long long)kc * rowstride + l;
       if (I.les) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) out[(4 + c) * cs + o] = scl(accT[c * NZR * TX + m], I.inv_n_t);
+        for (int c = 0; c < 3; ++c) out[(4 + c) * cs + o] = scl(accT[c * NZR * TX + m], I.inv_n2_t);
       }
-      if (I.density) out[7 * cs + o] = scl(accF[m], I.inv_n_t);
+      if (I.density) out[7 * cs + o] = scl(accF[m], I.inv_n2_t);
     }
   }
 }

@@ -190,10 +190,11 @@ __device__ __forceinline__ void b_x_les(const Inst<float>& I, const Blk bk) {
       if (k < Mx) {
         const cplx<float2> zk = P[c * PE + C::pix(k, q)];
         const cplx<float2> zm = P[c * PE + C::pix(k == 0 ? 0 : N - k, q)];
-        a0 = mk(T(0.5) * (zk.x.x + zm.x.x), T(0.5) * (zk.y.x - zm.y.x));
-        b0 = mk(T(0.5) * (zk.y.x + zm.y.x), T(-0.5) * (zk.x.x - zm.x.x));
-        a1 = mk(T(0.5) * (zk.x.y + zm.x.y), T(0.5) * (zk.y.y - zm.y.y));
-        b1 = mk(T(0.5) * (zk.y.y + zm.y.y), T(-0.5) * (zk.x.y - zm.x.y));
+        // twice A and B: the forward z pass scales by 1/(2N)
+        a0 = mk(zk.x.x + zm.x.x, zk.y.x - zm.y.x);
+        b0 = mk(zk.y.x + zm.y.x, zm.x.x - zk.x.x);
+        a1 = mk(zk.x.y + zm.x.y, zk.y.y - zm.y.y);
+        b1 = mk(zk.y.y + zm.y.y, zm.x.y - zk.x.y);
       }
       const int o = 4 * c;
       I.wy[(long long)I.out_slot[o] * I.wys + row + k] = a0;
