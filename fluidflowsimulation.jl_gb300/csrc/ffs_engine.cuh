@@ -573,6 +573,11 @@ class Engine : public EngineBase {
       if (I.hv) spec_names += ",hvis_fil_h,hvis_fil_v";
       if (I.density && !I.scalar) spec_names += ",buoyancy_fil_v,rho_fil,rhodiss_fil,rhonl_fil";
     }
+    if (I.pforce) {   // write_spec_forcing (spec.jl:148-170): the last field of each record
+      I.nspecf += 1;
+      spec_names += ",forcing_h";
+    }
+    static_assert(SPEC_MAX_FIELDS >= 31, "spectrum fields");
     nspecf = I.nspecf;
     if ((rc = alloc(&I.spec, (size_t)I.spec_cap * 2 * I.nspecf * std::max(lenH, lenV), err))) return rc;
     // ETD tables

@@ -1657,7 +1657,7 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
     if (I.sfil) {
       const double G = exp(-I.fil_d2 / 24.0 * k2);
       G2 = G * G;
-      ff = I.nspecf - 8 - (I.hv ? 2 : 0) - ((I.density && !I.scalar) ? 4 : 0);
+      ff = I.nspecf - (I.pforce ? 1 : 0) - 8 - (I.hv ? 2 : 0) - ((I.density && !I.scalar) ? 4 : 0);
       bin(ff, G2 * (0.5 * (a2[0] + a2[1])));                  // u_fil_h, u_fil_v
       bin(ff + 1, G2 * (0.5 * a2[2]));
       bin(ff + 2, 2.0 * nu * k2 * (G2 * (0.5 * (a2[0] + a2[1]))));   // vis_fil of u_fil
@@ -1728,6 +1728,23 @@ __device__ __forceinline__ void b_spectra(const Inst<T>& I, int mode, const Blk 
         bin(fd + 2, G2 * (alpha * k2 * (G2 * r2)));
         bin(fd + 3, G2 * ((double)dF.x * rho.x + (double)dF.y * rho.y));
       }
+    }
+    if (I.pforce && mode == 0) {
+      // write_spec_forcing (spec.jl:148-170, 262-271), after the step's forcing call
+      // (models.jl:6-9): (proj(u1, f1) + proj(u2, f2)) / dt on the forced modes, the kz = 0
+      // plane and the (0, 0, kz) modes; the run's tail writes none
+      const int plane = I.NYR * I.KXP;
+      cplx<T> f1 = mk(T(0), T(0)), f2 = f1;
+      bool forced = false;
+      if (kz_i == 0) {
+        f1 = I.pf_force[g]; f2 = I.pf_force[plane + g]; forced = true;
+      } else if (ix == 0 && ky_i == 0 && kz_i >= -5 && kz_i <= 5) {
+        const int slot = kz_i > 0 ? kz_i - 1 : 4 - kz_i;
+        f1 = I.pf_force[2 * plane + slot]; f2 = I.pf_force[2 * plane + 10 + slot]; forced = true;
+      }
+      if (forced)
+        bin(I.nspecf - 1, ((double)u[0].x * f1.x + (double)u[0].y * f1.y +
+                           ((double)u[1].x * f2.x + (double)u[1].y * f2.y)) / I.st->dt);
     }
   }
 }

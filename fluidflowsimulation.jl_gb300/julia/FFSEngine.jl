@@ -278,7 +278,9 @@ writepairs(name, k, e) = open(name, "w") do f
     end
 end
 
-function writespectra(e::Engine)
+# tail: the run's final calculate_rhs! writes no forcing spectrum (write_spec_forcing is
+# called from advance_in_time!, models.jl:6-9)
+function writespectra(e::Engine; tail::Bool = false)
     lenH = Ref{Int32}(0); lenV = Ref{Int32}(0)
     check(e, ccall((:ffs_spectrum_lengths, LIB), Cint, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}), e.h, lenH, lenV))
     nbuf = Vector{UInt8}(undef, 1024)
@@ -297,6 +299,7 @@ function writespectra(e::Engine)
         i = Int(r[1])
         spec(f) = (o = 1 + (f - 1) * (H + V); (r[o+1:o+H], r[o+H+1:o+H+V]))
         for (f, nm) in enumerate(names)
+            tail && nm == "forcing_h" && continue
             sH, sV = spec(f)
             writepairs("$nm.specH.$i", KH, sH)
             writepairs("$nm.specV.$i", KRZ, sV)
@@ -402,7 +405,7 @@ function run_simulation()
     lengthtime = haskey(d, :timeDuration) ? parse(Float64, d[:timeDuration]) : Inf   # FluidFlowSimulation.jl:26
     final = s + total
     finaltime = simtime(e) + lengthtime
-    function flush()
+    function flush(tail = false)
         recs = records(e)
         open("Stats.txt", "a+") do f
             for r in eachcol(recs)
@@ -419,7 +422,7 @@ function run_simulation()
             open(f -> join(f, (Int(r[1]), r[2], lens..., "\n"), ",", ""), "Scales.txt", "a+")
             open(f -> join(f, (Int(r[1]), r[2], anums..., "\n"), ",", ""), "Numbers.txt", "a+")
         end
-        writespectra(e)
+        writespectra(e; tail = tail)
     end
     # the loop of FluidFlowSimulation.jl:42-44; a time-limited run checks the clock every step
     steps = 0
@@ -444,7 +447,7 @@ function run_simulation()
     in_rhs = iteration(e) % p.write_time == 0 && steps > 0
     pre = in_rhs ? forcing_state(e) : nothing
     finalize!(e)
-    flush()
+    flush(true)
     writeoutput(e)
     write_forcing_output(in_rhs ? pre : forcing_state(e), iteration(e))
     p.les == 1 && write_les_output(e, iteration(e))

@@ -312,10 +312,12 @@ def stats_line(row) -> str:
     return ",".join([str(int(row[0]))] + [julia_float(v) for v in row[1:]]) + "\n"
 
 
-def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarray, rhosource: float | None = None
-                         ) -> None:
+def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarray, rhosource: float | None = None,
+                         tail: bool = False) -> None:
     """``write_spec`` (spec.jl:1-146, 173-194): tab-separated (k, E) pairs per spectrum
-    file. rhosource = -drho/dz / g_z turns the buoyancy spectra into rhosource.*."""
+    file. rhosource = -drho/dz / g_z turns the buoyancy spectra into rhosource.*. The
+    forcing spectrum forcing_h.* comes from advance_in_time! (models.jl:6-9), so the run's
+    tail (tail=True) writes none."""
     i = rec["iteration"]
 
     def put(name, k, e):
@@ -324,7 +326,7 @@ def write_spectrum_files(folder: Path, rec: dict, KH: np.ndarray, KRZ: np.ndarra
                 f.write(f"{julia_float(float(a))}\t{julia_float(float(b))}\n")
 
     for key, e in rec.items():
-        if key == "iteration":
+        if key == "iteration" or (tail and key.startswith("forcing_h.")):
             continue
         put(key, KH if key.endswith("specH") else KRZ, e)
     if rhosource is not None and "buoyancy_v.specH" in rec:
@@ -384,7 +386,7 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     # rhosource = -(buoyancy / g_z) * drho/dz (spec.jl:53-54)
     rhos = (-p.density_gradient / p.gravity) if (p.density and p.gravity_dir == 2 and p.gravity != 0) else None
 
-    def flush():
+    def flush(tail=False):
         recs = sim.records()
         with open(folder / "Stats.txt", "a") as f:
             for r in recs[:, : sim.ncols]:
@@ -399,7 +401,7 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
                 for r in rows:
                     f.write(stats_line(r))
         for rec in sim.spectra():
-            write_spectrum_files(folder, rec, KH, KRZ, rhos)
+            write_spectrum_files(folder, rec, KH, KRZ, rhos, tail=tail)
 
     steps = 0
     les_pending = None   # the output iteration whose LES fields the next step captures
@@ -429,7 +431,7 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     in_rhs = sim.iteration % wt == 0 and steps > 0
     pre = _forcing_state(sim) if in_rhs else None
     sim.finalize()
-    flush()
+    flush(tail=True)
     _write_output(folder, sim)
     _write_forcing_output(folder, sim, sim.iteration, pre if in_rhs else _forcing_state(sim))
     if sim.params.les:

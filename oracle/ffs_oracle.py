@@ -1417,6 +1417,12 @@ class OracleSimulation:
             self.compute_forcing()
         if self.pforce is not None:
             self.plane_force()
+            if self.is_spec_time():     # write_spec_forcing (spec.jl:148-170, 262-271)
+                fx, fy = self.pforce_xy
+                v = (_proj(self.u[0], fx) + _proj(self.u[1], fy)) / self.get_dt()
+                H, V = self.calculate_specHV(v)
+                self.spectra[self.iteration]["forcing_h.specH"] = H
+                self.spectra[self.iteration]["forcing_h.specV"] = V
         if self.is_stats_time():
             self.write_stats()
         # time_step! (models.jl:468-472) -> VectorTimeStep (time_step_functions.jl:72-80)

@@ -279,6 +279,9 @@ SPEC_CASES = {
     "etd-les-density-hv-specfil": dict(FIXED_CASES["etd-les-density-hv-specfil"], dtSpec="2"),
     "etd-barriers-density-specfil": dict(FIXED_CASES["etd-barriers-density-specfil"], dtSpec="2"),
     "etd-dynamic-density-vorticity": dict(FIXED_CASES["etd-dynamic-density-vorticity"], dtSpec="2"),
+    # write_spec_forcing (spec.jl:148-170): the forcing spectrum of the kz = 0 plane family
+    "ab3-adaptive-rf-forcing": dict(FIXED_CASES["ab3-adaptive-rf-forcing"], dtSpec="2"),
+    "ab3-a-forcing-tanh": dict(FIXED_CASES["ab3-a-forcing-tanh"], dtSpec="2"),
 }
 
 
