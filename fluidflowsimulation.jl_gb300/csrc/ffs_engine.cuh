@@ -139,6 +139,7 @@ class Engine : public EngineBase {
   // output capture (writeoutput's LES fields, output.jl:22-42): FP64 planes written by
   // the x pass of each output step, their iteration, the step graph that does it
   double* obuf = nullptr;
+  bool out_on = false;        // capture switched on (the buffer stays once allocated)
   int out_nf = 0;
   int64_t out_iter = -1;
   int64_t calls = 0;          // steps since ffs_initialize (the integrator's call counter)
@@ -1373,10 +1374,10 @@ class Engine : public EngineBase {
   // included), the forcing, and writestats at the current iteration, without an update.
   int finish(std::string& err) override {
     if (!initialized) { err = "ffs_initialize must be called before ffs_finalize"; return FFS_ESTATE; }
-    diag_x = obuf != nullptr;   // the tail's calculate_rhs! feeds the final writeoutput
+    diag_x = out_on;   // the tail's calculate_rhs! feeds the final writeoutput
     enqueue_step(2);
     diag_x = false;
-    if (obuf) out_iter = iteration;
+    if (out_on) out_iter = iteration;
     FFS_CK(cudaGetLastError());
     FFS_CK(cudaStreamSynchronize(s));
     return drain(iteration, iteration, err);
@@ -1404,13 +1405,12 @@ class Engine : public EngineBase {
   // writeoutput runs inside calculate_rhs! when a step starts at a multiple of writeTime,
   // except the first step after initialize! (is_output_time, simulationtypes.jl:102)
   bool output_step(int64_t it, int64_t call) const {
-    return obuf && call != 0 && it % P.write_time == 0;
+    return out_on && call != 0 && it % P.write_time == 0;
   }
 
   int capture_output(int on, std::string& err) override {
-    if (!on) return 0;
-    if (!I.les) return 0;   // the captured fields are the LES model's
-    if (obuf) return 0;
+    out_on = on && I.les;   // the captured fields are the LES model's
+    if (!out_on || obuf) return 0;
     out_nf = 5 + (I.dyn ? 1 : 0) + (I.dynp ? 1 : 0) + ((I.rho_les && !I.scalar) ? 3 : 0);
     int rc;
     if ((rc = alloc(&obuf, (size_t)out_nf * P.nx * P.ny * P.nz, err))) return rc;

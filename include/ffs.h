@@ -207,7 +207,8 @@ int ffs_forcing_array(ffs_handle* h, int32_t which, double* v, int32_t n, int32_
  * ffs_capture_output(h, 1) every step that starts at a multiple of write_time, except the
  * first after ffs_initialize (is_output_time, src/simulationtypes.jl:102), and the
  * run's tail (ffs_finalize) store them into a device buffer of nx*ny*nz doubles per field
- * (allocated by this call; a no-op without an LES model). ffs_output_field copies one
+ * (allocated by the first call that switches it on; a no-op without an LES model);
+ * ffs_capture_output(h, 0) stops the capture and keeps the buffer. ffs_output_field copies one
  * field of the most recent capture ([z][y][x], x fastest) and its iteration; FFS_EINVAL
  * for a field this configuration does not have, FFS_ESTATE before the first capture.
  * Capture steps run the generic x pass (not the FP32 register-fused one), so an FP32

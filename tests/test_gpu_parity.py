@@ -239,7 +239,7 @@ def test_etd_adaptive_parity(gpu_pkg):
 @pytest.mark.parametrize("name", ["ab3-32", "etd-les-density", "ab3-64-hv-forced", "etd-vreman", "etd-silvis",
                                   "ab3-stable-nonlinear", "etd-dynamic-smagorinsky", "ab3-adaptive-piomelli",
                                   "ab3-adaptive-piomelli-sandp", "etd-les-density-eddy",
-                                  "ab3-adaptive-silvis-scalar-vort"])
+                                  "ab3-adaptive-silvis-scalar-vort", "euler-adaptive-les-density-eddy"])
 def test_fp32_error(gpu_pkg, name):
     d = FIXED_CASES[name]
     sim, ref = run_pair(gpu_pkg, d, precision="FP32", density="densityStratification" in d)

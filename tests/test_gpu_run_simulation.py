@@ -178,3 +178,35 @@ def test_run_simulation_files_match_oracle(gpu_pkg, tmp_path, case):
             assert f.stat().st_size == 8 * n ** 3
             got = gpu_pkg.read_field(f, n, n, n)
             assert np.linalg.norm(got - ur[c]) <= 1e-12 * np.linalg.norm(ur[c]), (it, c)
+
+
+def test_output_capture_rules(gpu_pkg):
+    """ffs_capture_output: output steps are the steps that start at a multiple of writeTime,
+    except the first after ffs_initialize (is_output_time, src/simulationtypes.jl:102);
+    switched off, no step captures; without an LES model there is nothing to capture."""
+    n = 32
+    d = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1.0", "yDomainSize": "1.0",
+         "zDomainSize": "1.0", "kinematicViscosity": "0.01", "dtStat": "100", "dtSpec": "100", "writeTime": "3",
+         "velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.01", "lesModel": "Smagorinsky"}
+    u = gpu_pkg.random_spectrum(n, k0=3.0, seed=5)
+    sim = gpu_pkg.Simulation.from_global(d, precision="FP64")
+    sim.set_fields(*u)
+    sim.capture_output(True)
+    sim.initialize()
+    sim.advance_in_time(1)               # iteration 0: the first step after initialize!
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        sim.output_fields()
+    assert e.value.code == -7
+    sim.advance_in_time(3)               # steps 1, 2, 3: the step from 3 captures
+    it, f = sim.output_fields()
+    assert it == 3 and sorted(f) == ["T11", "T12", "T13", "T22", "T23"]
+    sim.capture_output(False)
+    sim.advance_in_time(4)               # through 7: the step from 6 does not capture
+    assert sim.output_fields()[0] == 3
+    sim.close()
+    plain = gpu_pkg.Simulation.from_global({k: v for k, v in d.items() if k != "lesModel"}, precision="FP64")
+    plain.capture_output(True)
+    with pytest.raises(gpu_pkg.FFSError) as e:
+        plain.output_fields()
+    assert e.value.code == -7
+    plain.close()
