@@ -677,9 +677,6 @@ def run_engine_arm(args):
     fma_tf, add_tf = ctypes.c_double(), ctypes.c_double()
     rc = L.ffs_measure_fp64_peak(local, ctypes.byref(fma_tf), ctypes.byref(add_tf))
     fp64_peak = fma_tf.value if rc == 0 else None
-    reg_tf = ctypes.c_double()
-    rc_reg = L.ffs_measure_fp64_register_rate(local, ctypes.byref(reg_tf))
-    fp64_reg = reg_tf.value if rc_reg == 0 else None
 
     if rank != 0:
         return 0
@@ -697,7 +694,6 @@ def run_engine_arm(args):
               "peak_source": "measured in this run: ffs_measure_fp64_peak (FP64 FMA chains on every SM, 2 flops "
                              "per FMA); no FP64 figure is in MEASURED_PEAKS.json",
               "fp64_add_peak": add_tf.value if rc == 0 else None,
-              "fp64_register_peak": fp64_reg,
               "flop_model": "pruned transform flops per pass: 5 L log2 L per complex line, 2.5 L log2 L per real "
                             "line, retained columns only",
               "algorithmic_flops_per_launch": fl[top64],
@@ -714,8 +710,9 @@ def run_engine_arm(args):
         # per event-timed launch against the pipe's rate at the measured peak (1 FMA = 2 flops)
         roof64["fp64_pipe_frac"] = ins64 * 32 / (top64_ms / 1e3) / (fp64_peak * 1e12 / 2)
         roof64["fp64_warp_instructions_per_launch"] = ins64
-        if fp64_reg:   # against the rate of FP64 instructions whose operands are all registers
-            roof64["fp64_pipe_frac_register_operands"] = ins64 * 32 / (top64_ms / 1e3) / (fp64_reg * 1e12 / 2)
+        if rc == 0 and add_tf.value > 0:
+            # against the add (and multiply) instruction rate, the form of most butterfly work
+            roof64["fp64_pipe_frac_add_rate"] = ins64 * 32 / (top64_ms / 1e3) / (add_tf.value * 1e12)
     ms32_step = ms32 / k32
     roof32 = kernel_roofline_hbm(prof32, nprof32, n, 8, "fp32", peak, peak_kind, ms32_step)
     cpu_rate, cpu_k, cores = (None, 0, 0)

@@ -26,8 +26,7 @@ EXPORTS = [
     "ffs_stats_records", "ffs_stats", "ffs_spectrum", "ffs_spectrum_lengths", "ffs_spectrum_fields", "ffs_spectrum_records", "ffs_iteration", "ffs_time", "ffs_dt",
     "ffs_time_steps", "ffs_profile_kernels", "ffs_launches_per_step", "ffs_device_bytes", "ffs_tuning_report",
     "ffs_stream",
-    "ffs_fourier_noalloc", "ffs_measure_fp64_peak", "ffs_measure_fp64_register_rate", "ffs_last_error",
-    "ffs_destroy",
+    "ffs_fourier_noalloc", "ffs_measure_fp64_peak", "ffs_last_error", "ffs_destroy",
     "ffs_server_default", "ffs_server_create", "ffs_submit", "ffs_poll", "ffs_wait", "ffs_fetch_stats",
     "ffs_fetch_fields", "ffs_release", "ffs_cancel", "ffs_server_pause", "ffs_server_stats", "ffs_server_tuning", "ffs_server_last_error", "ffs_server_destroy",
 ]
@@ -141,7 +140,6 @@ def load() -> ctypes.CDLL:
         "ffs_fourier_noalloc": (c_int32, [c_void_p, c_void_p, c_int32, c_int32, c_int32, c_double, c_double,
                                          c_double, c_double, c_void_p]),
         "ffs_measure_fp64_peak": (c_int32, [c_int32, D, D]),
-        "ffs_measure_fp64_register_rate": (c_int32, [c_int32, D]),
         "ffs_last_error": (c_char_p, [H]),
         "ffs_destroy": (None, [H]),
         "ffs_server_default": (c_int32, [POINTER(FFSServerCfg)]),

@@ -525,12 +525,19 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
   auto sti = [&](int l, int j, cplx<T> v) { ri[sidx(j, l, LSX)] = v; };
   fft_lines_n<+1, LIN, T, N, decltype(ldi), decltype(sti), LSX, XNT>(I.px, s0, s1, LSX, I.twx, ldi, sti);
 
-  // 3. physical space products: inputs from ri, outputs (first POUT pairs) into s1; the
-  // loop twice, with and without the kinetic-energy field (stats / spectrum iterations only)
+  // 3-5 twice, with and without the kinetic-energy field (output 3, needed only at stats
+  // and spectrum iterations). Without it the other outputs pair up in order: output
+  // index nk(t) of the t-th one; an odd one out of line q shares a complex line with
+  // that of line q ^ 1 (LYZ >= 2), so no complex line carries a zero half.
+  constexpr int NO = XF::nout, M_NK = NO - 1, P2 = M_NK / 2, ODD = M_NK % 2;
+  constexpr int LOUT_NK = P2 * LYZ + (ODD ? (LYZ >= 2 ? LYZ / 2 : 1) : 0);
+  static_assert(LOUT_NK <= LOUT && LOUT <= LIN, "output lines");
+  auto nk = [](int t) { return t < 3 ? t : t + 1; };
   AbsMax<T> umaxt, rmaxt;
   const T les2 = T(2) * T(I.les_alpha);
-  auto products = [&](auto ke_c) {
+  auto tail = [&](auto ke_c) {
   constexpr bool KE = decltype(ke_c)::value;
+  // 3. physical space products: inputs from ri, outputs into s1
   for (int e = threadIdx.x; e < n * LYZ; e += blockDim.x) {
     const int q = e % LYZ, j = e / LYZ;
     const cplx<T>* row = ri + sidx(j, q, LSX);
@@ -630,33 +637,52 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
         I.obuf[(pl + 2) * npl + pi] = (double)lz;
       }
     }
+    if (KE) {
 #pragma unroll
-    for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
+      for (int r = 0; r < POUT; ++r) orow[r * LYZ] = mk(o[2 * r], o[2 * r + 1]);
+    } else {
+#pragma unroll
+      for (int r = 0; r < P2; ++r) orow[r * LYZ] = mk(o[nk(2 * r)], o[nk(2 * r + 1)]);
+      if (ODD) {
+        const T v = o[nk(M_NK - 1)];
+        if (LYZ >= 2) reinterpret_cast<T*>(s1 + sidx(j, P2 * LYZ + q / 2, LSX))[q & 1] = v;
+        else s1[sidx(j, P2 * LYZ, LSX)] = mk(v, T(0));
+      }
+    }
   }
-  };
-  if (want_ke) products(std::true_type{});
-  else products(std::false_type{});
   // block max -> one atomic per CTA (the max is exact in T; FP64 only for the atomic)
   if (I.adaptive) block_max_to_state<T, (DEN != 0)>(I, umaxt.get(), rmaxt.get(), red);
   __syncthreads();
 
-  // 4. r2c of the output pairs, result back into sx
+  // 4. r2c of the output lines, result back into sx
+  constexpr int LO = KE ? LOUT : LOUT_NK;
   cplx<T>* rf = fft_result_buffer(I.px, s0, s1);
   auto ldf = [&](int l, int j) -> cplx<T> { return s1[sidx(j, l, LSX)]; };
   auto stf = [&](int l, int j, cplx<T> v) { rf[sidx(j, l, LSX)] = v; };
-  fft_lines_n<-1, LOUT, T, N, decltype(ldf), decltype(stf), LSX, XNT>(I.px, s0, s1, LSX, I.twx, ldf, stf);
+  fft_lines_n<-1, LO, T, N, decltype(ldf), decltype(stf), LSX, XNT>(I.px, s0, s1, LSX, I.twx, ldf, stf);
 
   // 5. unpack A = (Z_k + conj Z_{n-k})/2, B = -i (Z_k - conj Z_{n-k})/2 and store
   const int KXP = I.KXP;
   {
     const int wv = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int l = wv; l < LOUT; l += nw) {   // complex line l = r * LYZ + q carries outputs (2r, 2r+1)
-      const int r = l / LYZ, q = l % LYZ;
-      const int oa = 2 * r, ob = 2 * r + 1;
-      // output 3 is the kinetic-energy field, needed only at stats/spectrum iterations
-      const bool wa = oa < XF::nout && (oa != 3 || want_ke), wb = ob < XF::nout && (ob != 3 || want_ke);
-      cplx<T>* da = I.wy + (long long)I.out_slot[wa ? oa : 0] * I.wys + (long long)(g0 + q) * KXP;
-      cplx<T>* db = I.wy + (long long)I.out_slot[wb ? ob : 0] * I.wys + (long long)(g0 + q) * KXP;
+    for (int l = wv; l < LO; l += nw) {
+      // the outputs (oa, ob) and the (y,z) lines (qa, qb) of the two halves of line l;
+      // with KE, line r * LYZ + q carries outputs (2r, 2r+1) of line q
+      int oa, ob, qa, qb;
+      if (KE) {
+        oa = 2 * (l / LYZ); ob = oa + 1; qa = qb = l % LYZ;
+      } else if (l < P2 * LYZ) {
+        oa = nk(2 * (l / LYZ)); ob = nk(2 * (l / LYZ) + 1); qa = qb = l % LYZ;
+      } else {
+        const int t = l - P2 * LYZ;
+        oa = ob = nk(M_NK - 1);
+        qa = LYZ >= 2 ? 2 * t : 0;
+        qb = LYZ >= 2 ? 2 * t + 1 : 0;
+        if (LYZ < 2) ob = NO;   // (v, 0): no second half
+      }
+      const bool wa = oa < NO, wb = ob < NO;
+      cplx<T>* da = I.wy + (long long)I.out_slot[wa ? oa : 0] * I.wys + (long long)(g0 + qa) * KXP;
+      cplx<T>* db = I.wy + (long long)I.out_slot[wb ? ob : 0] * I.wys + (long long)(g0 + qb) * KXP;
       for (int k = lane; k < KXP; k += 32) {
         // 2A = Z_k + conj Z_{n-k}, 2B = -i (Z_k - conj Z_{n-k}): the factor 1/2 is in the
         // forward z pass's scale 1/(2N) (exact: a power of two through linear passes)
@@ -672,6 +698,9 @@ __device__ __forceinline__ void b_x_pass(const Inst<T>& I, const Blk bk) {
       }
     }
   }
+  };
+  if (want_ke) tail(std::true_type{});
+  else tail(std::false_type{});
 }
 template <typename T, bool LES, int DEN, int LYZ>
 __global__ void __launch_bounds__(FFS_MAXT) k_x_pass(Inst<T> I) {

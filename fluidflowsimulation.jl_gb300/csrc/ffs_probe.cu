@@ -7,12 +7,8 @@
 // registers; the chains never converge, so the pipe stays full. One FMA counts two
 // flops, one add one flop. Grid: every SM x 8 CTAs x 256 threads; timed with CUDA events
 // after one warm-up launch.
-//
-// ffs_measure_fp64_register_rate runs the same FMA chains with every operand in a
-// register (the multiplier and the addend are computed per thread, so the compiler can
-// take neither from the constant bank): that is the instruction form of the transforms,
-// whose operands are all data and loaded twiddles. On GB300 it runs at about 0.84 of
-// the constant-operand rate, and adds and multiplies run at the register-operand rate.
+// On GB300 FP64 adds (and multiplies) issue at about 0.84 of the FMA instruction rate,
+// so the transforms, whose butterflies are mostly adds, are bounded by the add rate.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -28,16 +24,11 @@ namespace {
 
 constexpr int NCH = 8;
 
-template <bool FMA, bool REG = false>
+template <bool FMA>
 __global__ void __launch_bounds__(256) k_fp64_chains(double* out, int iters, double a, double b) {
   double x[NCH];
 #pragma unroll
   for (int c = 0; c < NCH; ++c) x[c] = (double)(threadIdx.x + c) * 1e-3;
-  if (REG) {   // the same values, known only at run time: register operands
-    const double t = (double)(threadIdx.x & 1) * 1e-300;
-    a += t;
-    b += t;
-  }
   for (int i = 0; i < iters; ++i) {
 #pragma unroll
     for (int c = 0; c < NCH; ++c) x[c] = FMA ? fma(x[c], a, b) : x[c] + b;
@@ -48,7 +39,7 @@ __global__ void __launch_bounds__(256) k_fp64_chains(double* out, int iters, dou
   if (s == 1.2345e300) out[0] = s;   // never true for these inputs; keeps the chains live
 }
 
-int measure(int device, double* fma_tflops, double* add_tflops, bool reg = false) {
+int measure(int device, double* fma_tflops, double* add_tflops) {
   if (!fma_tflops || !add_tflops) return FFS_EINVAL;
   int old = 0;
   if (cudaGetDevice(&old) != cudaSuccess || cudaSetDevice(device) != cudaSuccess) {
@@ -65,7 +56,7 @@ int measure(int device, double* fma_tflops, double* add_tflops, bool reg = false
   const int blocks = sms * 8, threads = 256, iters = 1 << 14;
   double res[2] = {0.0, 0.0};
   for (int v = 0; v < 2 && e == cudaSuccess; ++v) {
-    auto k = v == 0 ? (reg ? k_fp64_chains<true, true> : k_fp64_chains<true>) : k_fp64_chains<false>;
+    auto k = v == 0 ? k_fp64_chains<true> : k_fp64_chains<false>;
     k<<<blocks, threads>>>(out, iters / 8, 0.999999, 1e-7);   // warm-up
     cudaEventRecord(e0);
     k<<<blocks, threads>>>(out, iters, 0.999999, 1e-7);
@@ -96,16 +87,6 @@ extern "C" int ffs_measure_fp64_peak(int32_t device, double* fma_tflops, double*
     return measure(device, fma_tflops, add_tflops);
   } catch (...) {
     ffsgpu::set_global_error("ffs_measure_fp64_peak: internal error");
-    return FFS_EINVAL;
-  }
-}
-
-extern "C" int ffs_measure_fp64_register_rate(int32_t device, double* fma_tflops) {
-  try {
-    double add = 0.0;
-    return measure(device, fma_tflops, &add, true);
-  } catch (...) {
-    ffsgpu::set_global_error("ffs_measure_fp64_register_rate: internal error");
     return FFS_EINVAL;
   }
 }

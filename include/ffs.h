@@ -310,9 +310,6 @@ int ffs_fourier_noalloc(const double* phys, double* spec, int32_t nx, int32_t ny
  * TFLOP/s. The denominator of the FP64 plain form's roofline (its transforms are FP64-
  * pipe-bound on GB300). Allocates 8 bytes of device memory for the duration. */
 int ffs_measure_fp64_peak(int32_t device, double* fma_tflops, double* add_tflops);
-/* The same FMA chains with every operand in a register (the instruction form of the
- * transforms, whose operands are data and loaded twiddles), in TFLOP/s. */
-int ffs_measure_fp64_register_rate(int32_t device, double* fma_tflops);
 
 const char* ffs_last_error(const ffs_handle* h);
 void ffs_destroy(ffs_handle* h);
