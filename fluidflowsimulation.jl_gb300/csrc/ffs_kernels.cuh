@@ -1337,9 +1337,10 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
       for (int c = 0; c < 3; ++c) rhs[c] = rhs[c] + sb[(4 + c) * cs + g];
     }
     if (I.density) rhs[I.gdir] = rhs[I.gdir] + scl(rho, I.gval_t);   // models.jl:334-336
+    // 1/k^2 of both projections (one division: the FP64 pipe is the bound of the FP64 form)
+    const T inv = k0 ? T(0) : T(1) / k2;
     {  // projection (models.jl:338-339)
       const cplx<T> kd = mk(kx * rhs[0].x + ky * rhs[1].x + kz * rhs[2].x, kx * rhs[0].y + ky * rhs[1].y + kz * rhs[2].y);
-      const T inv = k0 ? T(0) : T(1) / k2;
       const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
       rhs[0] = rhs[0] + scl(p1, kx); rhs[1] = rhs[1] + scl(p1, ky); rhs[2] = rhs[2] + scl(p1, kz);
     }
@@ -1368,8 +1369,9 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (I.ab3 && !I.euler && stage == 2) f2[c] = scl(rhs[c] - f1[c], fix2) + rhs[c];   // fix_fm2! (ETD.jl:130-140)
-      // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u)))
-      un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
+      // muladd(A, rhs, muladd(B, fm1, muladd(C, fm2, E u))); E = 1 for the explicit integrators
+      if (I.ab3) un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + u[c]));
+      else un[c] = scl(rhs[c], A) + (scl(f1[c], B) + (scl(f2[c], C) + scl(u[c], E)));
       if (band) un[c] = un[c] + scl(u[c], fdt);   // forcing increment (add_forcing!)
     }
     if (I.pforce) {   // add_Rf_forcing! (forcing_types.jl:54-64): the kz = 0 plane, then (0, 0, kz)
@@ -1385,7 +1387,6 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
     }
     {  // projection after the update (time_step_functions.jl:78)
       const cplx<T> kd = mk(kx * un[0].x + ky * un[1].x + kz * un[2].x, kx * un[0].y + ky * un[1].y + kz * un[2].y);
-      const T inv = k0 ? T(0) : T(1) / k2;
       const cplx<T> p1 = mk(-kd.x * inv, -kd.y * inv);
       un[0] = un[0] + scl(p1, kx); un[1] = un[1] + scl(p1, ky); un[2] = un[2] + scl(p1, kz);
     }
@@ -1405,7 +1406,9 @@ __device__ __forceinline__ void b_update(const Inst<T>& I, int mode, const Blk b
         const T* e = I.etab_rho + 4 * te;
         E = e[0]; A = e[1]; B = e[2]; C = e[3];
       }
-      const cplx<T> rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + scl(rho, E)));
+      cplx<T> rn;
+      if (I.ab3) rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + rho));
+      else rn = scl(rrhs, A) + (scl(r1, B) + (scl(r2, C) + scl(rho, E)));
       bad |= !(isfinite(rn.x) && isfinite(rn.y));
       uh[3 * cs + g] = rn;
       hB[3 * cs + g] = rrhs;
