@@ -101,6 +101,7 @@ class Engine : public EngineBase {
   std::vector<void*> allocs;
   int64_t bytes = 0;
   FieldList inv_list{}, fwd_list{};
+  FieldList inv_list_z{};   // the inverse z pass's fields: inv_list without a derived w_z
   // the inverse z pass's fields by prologue family (copy, curl, strain), each launched on
   // its own when split_iz: every CTA of a launch then runs one code path of the kernel
   FieldList inv_fam[3]{};
@@ -201,6 +202,7 @@ class Engine : public EngineBase {
     const size_t cb = sizeof(cplx<T>);
     smem_z = (size_t)txy * srows(P.nz) * cb * (I.pz.np >= 3 ? 2 : 1);
     smem_y = (size_t)txy * srows(P.ny) * cb * (I.py.np >= 3 ? 2 : 1);
+    if (I.wz_derived) smem_y += sizeof(T) * ((size_t)TX + I.NYR);   // the derived w_z's wavenumber table
     {
       const int PIN = (nin + 1) / 2;
       const int LIN = PIN * lyz;
@@ -438,13 +440,22 @@ class Engine : public EngineBase {
         inv_list.slot[inv_list.n] = inv_list.n;
         ++inv_list.n;
       }
+    // FP64: w_z is formed in the inverse y pass (b_inv_y), the z pass skips it
+    I.wz_derived = sizeof(T) == 8;
+    inv_list_z = FieldList{};
+    for (int i = 0; i < inv_list.n; ++i)
+      if (!(I.wz_derived && inv_list.code[i] == F_WZ)) {
+        inv_list_z.code[inv_list_z.n] = inv_list.code[i];
+        inv_list_z.slot[inv_list_z.n] = inv_list.slot[i];
+        ++inv_list_z.n;
+      }
     {
       FieldList fam[3]{};
-      for (int i = 0; i < inv_list.n; ++i) {
-        const int c = inv_list.code[i];
+      for (int i = 0; i < inv_list_z.n; ++i) {
+        const int c = inv_list_z.code[i];
         const int f = (c <= F_UZ || c == F_RHO) ? 0 : (c <= F_WZ ? 1 : 2);
         fam[f].code[fam[f].n] = c;
-        fam[f].slot[fam[f].n] = inv_list.slot[i];
+        fam[f].slot[fam[f].n] = inv_list_z.slot[i];
         ++fam[f].n;
       }
       n_fam = 0;
@@ -983,7 +994,7 @@ class Engine : public EngineBase {
     if (split_iz && n_fam > 1) {
       for (int f = 0; f < n_fam; ++f) launch_inv_z(inv_fam[f]);
     } else {
-      launch_inv_z(inv_list);
+      launch_inv_z(inv_list_z);
     }
   }
   // the full-spectrum instance of the dynamic model's filter passes: every kx, ky, kz kept
@@ -1656,7 +1667,7 @@ class Engine : public EngineBase {
           if (c && (sizeof(T) != 4 || (t != TX && !half_ct) || (!ct_len_raw(P.ny) && !ct_len_raw(P.nz)))) continue;
           txy = t; use_ct = c;
           float ms = 0.f;
-          if ((rc = timed([&] { launch_inv_z(inv_list); launch_inv_y(inv_list); launch_fwd_y(fwd_list); }, ms))) break;
+          if ((rc = timed([&] { launch_inv_z(inv_list_z); launch_inv_y(inv_list); launch_fwd_y(fwd_list); }, ms))) break;
           snprintf(line, sizeof(line), "yz[tx=%d,%s]=%.4fms ", t, c ? "ct" : "rt", ms);
           rep += line;
           if (ms < best) { best = ms; bt = t; bc = c; }
@@ -1679,7 +1690,7 @@ class Engine : public EngineBase {
         v = bv;
         return 0;
       };
-      if (!rc) rc = pick(v_iz, "z_inv", (!pair_codes() || txy != TX) ? 0 : ctz(), [&] { launch_inv_z(inv_list); });
+      if (!rc) rc = pick(v_iz, "z_inv", (!pair_codes() || txy != TX) ? 0 : ctz(), [&] { launch_inv_z(inv_list_z); });
       // one launch for every field family, or one per family
       if (!rc && n_fam > 1) {
         float bms = 1e30f;

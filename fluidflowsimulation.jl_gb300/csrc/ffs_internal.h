@@ -176,6 +176,8 @@ template <typename T> struct Inst {
   T inv_n_t, nu_t, hvnu_t, alpha_t, gval_t, dgrad_t, kf2_t;
   T inv_n2_t;              // 1/(2N): the step's forward z scale (the x pass leaves out its unpack 1/2)
   // field lists for the passes
+  int wz_derived;          // FP64: the y pass forms w_z = i (kx Uy - ky Ux) from the z-transformed
+                           // u (no kz in it), so the z pass skips one transform
   int nin;                 // inverse fields
   int in_code[12];
   int nout;                // forward fields (incl. kinetic-energy field)

@@ -246,12 +246,35 @@ __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, co
   const int fi = bk.x, kx0 = bk.y * TX, z = bk.z;
   const cplx<T>* in = I.wz + (long long)F.slot[fi] * I.wzs + (long long)z * I.NYR * I.KXP + kx0;
   cplx<T>* out = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
+  auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
+  if constexpr (sizeof(T) == 8) {
+    if (I.wz_derived && F.code[fi] == F_WZ) {
+      // w_z = i (kx u_y - ky u_x) has no kz: formed here from the z-transformed u_x, u_y
+      // (slots 0 and 1), the same expression as the spectral prologue's curl. The
+      // wavenumbers come from a table after the FFT buffers (no FP64 conversions per element).
+      T* ktab = reinterpret_cast<T*>(s0 + (size_t)srows(I.ny) * TX * (I.py.np >= 3 ? 2 : 1));   // [TX] kx, [NYR] ky
+      for (int t = threadIdx.x; t < TX + I.NYR; t += blockDim.x)
+        ktab[t] = t < TX ? kval(kx0 + t, I.Lx_t, I.iLx_t) : kval(ysig(I, t - TX), I.Ly_t, I.iLy_t);
+      __syncthreads();
+      const long long o = (long long)z * I.NYR * I.KXP + kx0;
+      const cplx<T>* ux = I.wz + o;
+      const cplx<T>* uy = I.wz + I.wzs + o;
+      auto ldw = [&](int l, int y) -> cplx<T> {
+        const int jc = ycomp(I, y);
+        if (jc < 0) return mk(T(0), T(0));
+        const cplx<T> a = ux[(long long)jc * I.KXP + l], b = uy[(long long)jc * I.KXP + l];
+        const T kx = ktab[l], ky = ktab[TX + jc];
+        return mk(-(kx * b.y - ky * a.y), kx * b.x - ky * a.x);
+      };
+      fft_lines_n<+1, TX, T, N>(I.py, s0, s1, TX, I.twy, ldw, st);
+      return;
+    }
+  }
   auto ld = [&](int l, int y) -> cplx<T> {
     const int jc = ycomp(I, y);
     if (jc < 0) return mk(T(0), T(0));
     return in[(long long)jc * I.KXP + l];
   };
-  auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
   fft_lines_n<+1, TX, T, N>(I.py, s0, s1, TX, I.twy, ld, st);
 }
 template <typename T, int TX, int N = 0>
