@@ -76,6 +76,48 @@ def test_shear_flow_decays_exactly_under_etd():
     assert np.abs(ur[1]).max() < 1e-13 and np.abs(ur[2]).max() < 1e-13
 
 
+def test_shear_flow_decays_exactly_under_euler():
+    """The same shear flow under Euller (Euller.jl:14-25): u_{n+1} = (1 - nu k^2 dt) u_n with
+    the explicit viscous term, so after 10 steps the amplitude is (1 - nu k^2 dt)^10."""
+    n = 32
+    z = 2 * np.pi * np.arange(n) / n
+    u1 = np.broadcast_to(np.sin(2 * z)[:, None, None], (n, n, n)).copy()
+    p = Params(nx=n, ny=n, nz=n, nu=0.05, integrator="Euller", variable_dt=False, dt=0.1, dt_stat=1000,
+               dt_spec=1000)
+    s = OracleSimulation(p, (u1, np.zeros_like(u1), np.zeros_like(u1)))
+    s.initialize()
+    s.run(10)
+    ur = s.u_physical()
+    expect = u1 * (1 - p.nu * 4 * 0.1) ** 10
+    assert np.abs(ur[0] - expect).max() < 1e-13
+    assert np.abs(ur[1]).max() < 1e-13 and np.abs(ur[2]).max() < 1e-13
+
+
+def test_density_eddy_diffusion_is_a_dissipation():
+    """densityLesModel eddyDiffusion (les_real_calc.jl:116-123): the LES flux nu_t grad rho
+    with nu_t >= 0 only removes density variance, and rhopr = -sum proj(i k . flux, rho)
+    counts it (stats.jl:1032-1053) in trhodiss."""
+    n = 32
+    rng = np.random.default_rng(3)
+    base = {"nx": str(n), "ny": str(n), "nz": str(n), "xDomainSize": "1", "yDomainSize": "1", "zDomainSize": "1",
+            "kinematicViscosity": "0.01", "dtStat": "1", "dtSpec": "1000", "writeTime": "1000",
+            "velocityTimeStep": "ETD3rdO", "variableTimestepFlag": "false", "dt": "0.005",
+            "densityStratification": "true", "Pr": "1", "densityGradient": "0", "zAcceleration": "0",
+            "referenceDensity": "1", "lesModel": "Smagorinsky", "densityLesModel": "eddyDiffusion"}
+    g = Grid(n, n, n)
+    rho = g.real(g.myfourier(rng.standard_normal((n, n, n))) * np.exp(-np.sqrt(g.K2) / 3))
+    u = [g.real(g.myfourier(rng.standard_normal((n, n, n))) * np.exp(-np.sqrt(g.K2) / 3)) for _ in range(3)]
+    h = stats_header(Params.from_global(base)).split(",")
+    s = OracleSimulation(Params.from_global(base), u, rho)
+    s.initialize()
+    s.run(2)
+    rows = np.array(s.stats_rows)
+    assert (rows[:, h.index("rhopr")] > 0).all()
+    # trhodiss = rhodiss + rhopr (density_stratification_types.jl:52-56)
+    assert np.allclose(rows[:, h.index("trhodiss")], rows[:, h.index("rhodiss")] + rows[:, h.index("rhopr")],
+                       rtol=1e-14, atol=0)
+
+
 def test_ab3_coefficients_reduce_to_constant_dt():
     t = AB3(True, 0.1)
     t.dt = t.dt2 = t.dt3 = 0.1
