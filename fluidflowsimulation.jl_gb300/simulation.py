@@ -437,7 +437,7 @@ def run_simulation(folder: str | Path = ".", precision: str | None = None, devic
     if sim.params.les:
         _write_les_output(folder, sim, sim.iteration)
     if p.plane_forcing == 1:   # writedlm("R.$(iteration)", R) for rfForcing (FluidFlowSimulation.jl:60-62)
-        _write_dlm(folder / f"R.{sim.iteration}", sim.forcing_array("R"))
+        write_dlm(folder / f"R.{sim.iteration}", sim.forcing_array("R"))
     return sim
 
 
@@ -451,7 +451,7 @@ def _write_output(folder: Path, sim: Simulation) -> None:
         _fields.write_field(folder / f"{sim.scalar_name}.{i}", f[3])
 
 
-def _write_dlm(path: Path, rows) -> None:
+def write_dlm(path: Path, rows) -> None:
     """``writedlm`` with its default tab delimiter: one line per value of a vector, per
     tuple of an iterator of tuples, per row of a matrix; values printed as Julia prints them."""
     a = np.asarray(rows, dtype=np.float64)
@@ -476,7 +476,7 @@ def _forcing_state(sim: Simulation) -> dict:
 
 def _write_forcing_output(folder: Path, sim: Simulation, it: int, state: dict) -> None:
     for name, a in state.items():
-        _write_dlm(folder / f"{name}.{it}", a)
+        write_dlm(folder / f"{name}.{it}", a)
 
 
 def _write_les_output(folder: Path, sim: Simulation, it: int) -> None:

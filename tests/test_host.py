@@ -263,6 +263,18 @@ def test_parameters_density_and_scalar_les(pkg):
         Params.from_global(d)
 
 
+def test_write_dlm_matches_julia_writedlm(pkg, tmp_path):
+    """writedlm's default layout (the R.N, Eh.N and N.N files): one value per line for a
+    vector, tab-separated for an iterator of pairs or a matrix's rows, values as Julia
+    prints them."""
+    pkg.write_dlm(tmp_path / "v", [0.5, 2.0, 1e-5])
+    assert (tmp_path / "v").read_text() == "0.5\n2.0\n1.0e-5\n"
+    pkg.write_dlm(tmp_path / "p", np.stack([[1.0, 2.0], [0.25, 3.0]], 1))
+    assert (tmp_path / "p").read_text() == "1.0\t0.25\n2.0\t3.0\n"
+    pkg.write_dlm(tmp_path / "m", np.array([[1.0, 0.0, 2.5], [0.0, 4.0, 0.0]]))
+    assert (tmp_path / "m").read_text() == "1.0\t0.0\t2.5\n0.0\t4.0\t0.0\n"
+
+
 def test_parse_number(pkg):
     assert pkg.parse_number("2π") == pytest.approx(2 * np.pi)
     assert pkg.parse_number("2pi/128") == pytest.approx(2 * np.pi / 128)
