@@ -440,11 +440,13 @@ class Engine : public EngineBase {
         inv_list.slot[inv_list.n] = inv_list.n;
         ++inv_list.n;
       }
-    // FP64: w_z is formed in the inverse y pass (b_inv_y), the z pass skips it
+    // FP64: w_z and the strain's xx, xy, yy (no kz in them) are formed in the inverse y
+    // pass (b_inv_y); the z pass skips them
     I.wz_derived = sizeof(T) == 8;
     inv_list_z = FieldList{};
     for (int i = 0; i < inv_list.n; ++i)
-      if (!(I.wz_derived && inv_list.code[i] == F_WZ)) {
+      if (!(I.wz_derived && (inv_list.code[i] == F_WZ || inv_list.code[i] == F_SXX || inv_list.code[i] == F_SXY ||
+                             inv_list.code[i] == F_SYY))) {
         inv_list_z.code[inv_list_z.n] = inv_list.code[i];
         inv_list_z.slot[inv_list_z.n] = inv_list.slot[i];
         ++inv_list_z.n;

@@ -248,10 +248,12 @@ __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, co
   cplx<T>* out = I.wy + (long long)F.slot[fi] * I.wys + (long long)z * I.ny * I.KXP + kx0;
   auto st = [&](int l, int y, cplx<T> v) { out[(long long)y * I.KXP + l] = v; };
   if constexpr (sizeof(T) == 8) {
-    if (I.wz_derived && F.code[fi] == F_WZ) {
-      // w_z = i (kx u_y - ky u_x) has no kz: formed here from the z-transformed u_x, u_y
-      // (slots 0 and 1), the same expression as the spectral prologue's curl. The
-      // wavenumbers come from a table after the FFT buffers (no FP64 conversions per element).
+    const int code = F.code[fi];
+    if (I.wz_derived && (code == F_WZ || code == F_SXX || code == F_SXY || code == F_SYY)) {
+      // w_z = i (kx u_y - ky u_x) and the strain components xx, xy, yy have no kz: formed
+      // here from the z-transformed u_x, u_y (slots 0 and 1), with the spectral prologue's
+      // expressions. The wavenumbers come from a table after the FFT buffers (no FP64
+      // conversions per element).
       T* ktab = reinterpret_cast<T*>(s0 + (size_t)srows(I.ny) * TX * (I.py.np >= 3 ? 2 : 1));   // [TX] kx, [NYR] ky
       for (int t = threadIdx.x; t < TX + I.NYR; t += blockDim.x)
         ktab[t] = t < TX ? kval(kx0 + t, I.Lx_t, I.iLx_t) : kval(ysig(I, t - TX), I.Ly_t, I.iLy_t);
@@ -264,7 +266,12 @@ __device__ __forceinline__ void b_inv_y(const Inst<T>& I, const FieldList& F, co
         if (jc < 0) return mk(T(0), T(0));
         const cplx<T> a = ux[(long long)jc * I.KXP + l], b = uy[(long long)jc * I.KXP + l];
         const T kx = ktab[l], ky = ktab[TX + jc];
-        return mk(-(kx * b.y - ky * a.y), kx * b.x - ky * a.x);
+        if (code == F_WZ) return mk(-(kx * b.y - ky * a.y), kx * b.x - ky * a.x);
+        // (i/2)(k_a u_b + k_b u_a) with (a, b) = (x, x), (x, y), (y, y)
+        const T k1 = code == F_SYY ? ky : kx, k2 = code == F_SXX ? kx : ky;
+        const cplx<T> v1 = code == F_SXX ? a : b, v2 = code == F_SYY ? b : a;
+        const cplx<T> q = mk(k1 * v1.x + k2 * v2.x, k1 * v1.y + k2 * v2.y);
+        return mk(-T(0.5) * q.y, T(0.5) * q.x);
       };
       fft_lines_n<+1, TX, T, N>(I.py, s0, s1, TX, I.twy, ldw, st);
       return;
