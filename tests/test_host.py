@@ -349,3 +349,22 @@ def test_bench_byte_models():
     assert f["x_pass"] == 9 * n * n * 2.5 * n * 8
     assert f["inv_z"] == 6 * 86 * 171 * 5 * n * 8
     assert sum(v for k, v in f.items() if k != "step") == f["step"]
+
+
+def test_gpu_parity_cases_parse_on_both_sides(pkg):
+    """Every global of the GPU parity cases parses in the host mirror and in the oracle,
+    with the same integrator, LES model, fourth field and forcing (a parse regression
+    shows here without a GPU)."""
+    import sys
+    from pathlib import Path
+    from oracle.ffs_oracle import Params
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from test_gpu_parity import FIXED_CASES, SPEC_CASES
+    integ = {"ETD3rdO": 0, "Adams_Bashforth3rdO": 1, "Euller": 2}
+    for name, d in list(FIXED_CASES.items()) + list(SPEC_CASES.items()):
+        p, o = pkg.parameters(d), Params.from_global(d)
+        assert p.integrator == integ[o.integrator], name
+        assert bool(p.les) == o.les and bool(p.density) == o.density and bool(p.passive_scalar) == o.scalar, name
+        assert p.rho_les == {"": 0, "eddy": 1, "vorticity": 2}[o.rho_les], name
+        assert bool(p.plane_forcing) == bool(o.plane_forcing) and bool(p.forcing) == o.forcing, name
+        assert (p.spec_fil != 0) == (o.spec_fil != 0) and bool(p.hyperviscosity) == o.hv, name
